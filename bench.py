@@ -1,0 +1,285 @@
+"""Benchmark: Beyn contour step on the star domain (CFIE Kress), one GB300.
+
+Workload (the BASELINE metric's configuration): CFIE_kress on the star
+r(theta) = 1 + 0.2 cos(5 theta), N = 2048 nodes, one disk k0 = 200, R = 0.5,
+nq = 48 trapezoid contour nodes, L = 64 seeded complex Gaussian probes (std 1),
+svd_tol = 1e-12, the reference's single r -> 2r regrowth when the rank
+saturates. A step = one full Beyn disk: assembly of the 48 T(z_j), batched
+LU, T^-1 V solves (+ regrowth solves), moments, host SVD/eig.
+
+metric: eigenvalues/s of the mixed form (FP32 assembly/LU + compensated
+refinement) counting eigenvalues inside the disk that agree with the plain
+FP64 GPU path to <= 1e-10 relative; the plain FP64 path is timed beside it.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "quantumbilliards.jl_gb300"))
+
+N_NODES, K0, RADIUS, NQ, L_PROBES, SVD_TOL = 2048, 200.0, 0.5, 48, 64, 1e-12
+TOL_EIG = 1e-10
+IMAG_TOL = 1e-6
+SEED = 2
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def star_workspace(qb, kind="cfie"):
+    b = qb.make_star(0.2, 5)
+    sol = qb.CFIE_kress(1.0, b) if kind == "cfie" else qb.DLP_kress(1.0, b)
+    pts, sol = qb.points_with_n(sol, b, N_NODES, K0)
+    return b, sol, pts
+
+
+def select(lam, k0=K0, R=RADIUS):
+    lam = np.asarray(lam)
+    return np.sort_complex(lam[(np.abs(lam - k0) <= R) & (np.abs(lam.imag) < IMAG_TOL)])
+
+
+def match(lam, ref):
+    """Per-eigenvalue relative error against the nearest reference eigenvalue."""
+    if len(ref) == 0:
+        return np.full(len(lam), np.inf)
+    return np.array([np.min(np.abs(ref - l)) / abs(l) for l in lam])
+
+
+def run_step(qb, sol, pts, ws, mixed, rng_seed=SEED, with_geometry=False):
+    t0 = time.perf_counter()
+    if with_geometry:
+        ws = qb.Workspace(sol, pts)
+    lam, Uk, Y, info = qb.solve_vect(sol, pts, K0 + 0j, RADIUS, nq=NQ, r=L_PROBES, svd_tol=SVD_TOL,
+                                     rng=np.random.default_rng(rng_seed), mixed=mixed, ws=ws)
+    dt = time.perf_counter() - t0
+    if with_geometry:
+        ws.close()
+    return lam, info, dt
+
+
+def cpu_baseline(qb, sol, pts, nsample=1):
+    """Oracle (NumPy/SciPy FP64 restatement) on a bounded sample: assembly +
+    LU + solves for `nsample` contour nodes, extrapolated to the 48-node disk."""
+    from oracle import assembly as OA
+    import scipy.linalg as sla
+    zj = K0 + RADIUS * np.exp(2j * math.pi * np.arange(NQ) / NQ)
+    V = qb.probe_matrix(pts[0].n, L_PROBES, np.random.default_rng(SEED))
+    t0 = time.perf_counter()
+    for z in zj[:nsample]:
+        T = OA.cfie_matrix(pts, z)
+        f = sla.lu_factor(T, check_finite=False)
+        sla.lu_solve(f, V, check_finite=False)
+    dt = (time.perf_counter() - t0) / nsample * NQ
+    return dt
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-steps", type=int, default=1)
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        return reference_arm(args)
+
+    from qbgpu import build as B
+    B.build()
+    import qbgpu as qb
+    from qbgpu import _lib
+
+    b, sol, pts = star_workspace(qb)
+    ws = qb.Workspace(sol, pts)
+
+    # FP64 reference eigenvalues for the accuracy filter (plain GPU path, validated against the oracle in tests)
+    lam64, info64, t_plain_first = run_step(qb, sol, pts, ws, mixed=False)
+    ref = select(lam64)
+    plain_times = []
+    for _ in range(max(0, args.plain_steps)):
+        _, _, dt = run_step(qb, sol, pts, ws, mixed=False)
+        plain_times.append(dt)
+    t_plain = float(np.median(plain_times)) if plain_times else t_plain_first
+
+    for _ in range(args.warmup):
+        run_step(qb, sol, pts, ws, mixed=True)
+    _lib.load().qbg_device_sync()
+    clk = ClockSampler()
+    clk.start()
+    times, counts, errs, stats = [], [], [], []
+    for s in range(args.steps):
+        lam, info, dt = run_step(qb, sol, pts, ws, mixed=True)
+        sel = select(lam)
+        e = match(sel, ref)
+        counts.append(int(np.count_nonzero(e <= TOL_EIG)))
+        errs.append(float(e.max()) if len(e) else float("nan"))
+        times.append(dt)
+        stats.append(info["stats"])
+    _lib.load().qbg_device_sync()
+    clocks = clk.stop()
+    # end to end through the public API including the geometry upload
+    e2e_times = []
+    for _ in range(max(1, min(args.steps, 3))):
+        _, _, dt = run_step(qb, sol, pts, None, mixed=True, with_geometry=True)
+        e2e_times.append(dt)
+
+    t_step = float(np.mean(times))
+    n_eig = float(np.mean(counts))
+    value = n_eig / t_step
+    plain_eigs = len(ref)
+    st0 = stats[-1][0]
+    r_final = info["r"]
+    N = ws.dim
+    h2d = 8 * 8 * N + 16 * N * (L_PROBES + (r_final if r_final != L_PROBES else 0))
+    d2h = 2 * 16 * N * (L_PROBES + (r_final if r_final != L_PROBES else 0))
+    hbm, bf16, peak_kind = _peaks()
+    # dominant-kernel roofline: batched LU+solves are the bulk; report the LU phase as one "launch set"
+    lu_flops = NQ * (8.0 / 3.0) * N ** 3
+    ms_factor = float(np.mean([s[0]["ms_factor"] for s in stats]))
+    achieved = lu_flops / (ms_factor * 1e-3) / 1e12
+    line = {
+        "metric": "eigenvalues/s at <=1e-10 rel err (mixed FP32+refinement vs plain FP64), Beyn CFIE Kress star",
+        "value": value,
+        "unit": "eigenvalues/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t_step * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "c64+c128",
+        "data": "synthetic",
+        "config": {"workload": "beyn_cfie_kress_star_N2048_k0_200_R0.5_nq48_L64", "N": N, "k0": K0, "R": RADIUS,
+                   "nq": NQ, "L": L_PROBES, "r_final": r_final, "l2": "inputs larger than L2 (3.2 GB of T(z_j))"},
+        "plain_fp64": {"value": plain_eigs / t_plain, "ms_per_step": t_plain * 1e3, "eigenvalues": plain_eigs},
+        "speedup_vs_plain": (value / (plain_eigs / t_plain)) if plain_eigs else None,
+        "eigenvalues_per_step": n_eig,
+        "max_rel_err_vs_fp64": float(np.max(errs)),
+        "phases_ms": {"assemble": st0["ms_assemble"], "factor": st0["ms_factor"],
+                      "solve_refine": sum(s["ms_solve"] for s in stats[-1])},
+        "refine_sweeps": [s["refine_sweeps"] for s in stats[-1]],
+        "e2e": {"value": n_eig / float(np.mean(e2e_times)), "unit": "eigenvalues/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+                     "frac": achieved / bf16, "traffic": None, "kernel": "batched LU (FP32 CUDA cores)",
+                     "peak_kind": peak_kind},
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline and rank == 0 and world == 1:
+        t_cpu = cpu_baseline(qb, sol, pts, 1)
+        line["cpu_baseline"] = {"value": plain_eigs / t_cpu, "unit": "eigenvalues/s", "cores": os.cpu_count(),
+                                "kind": "port",
+                                "sample": "oracle assembly+LU+solve of 1 of 48 contour nodes, extrapolated x48"}
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def reference_arm(args):
+    """--impl reference: the oracle's FP64 CPU restatement on the host cores."""
+    import qbgpu.geometry as G  # host-only modules (no GPU work)
+    from qbgpu import solvers as S
+    b = G.make_star(0.2, 5)
+    pts, sol = S.points_with_n(S.CFIE_kress(1.0, b), b, N_NODES, K0)
+    from oracle import assembly as OA
+    import scipy.linalg as sla
+    zj = K0 + RADIUS * np.exp(2j * math.pi * np.arange(NQ) / NQ)
+    rng = np.random.default_rng(SEED)
+    V = (rng.standard_normal((pts[0].n, L_PROBES)) + 1j * rng.standard_normal((pts[0].n, L_PROBES))) * math.sqrt(.5)
+    times = []
+    for s in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        z = zj[s % NQ]
+        T = OA.cfie_matrix(pts, z)
+        f = sla.lu_factor(T, check_finite=False)
+        sla.lu_solve(f, V, check_finite=False)
+        if s >= args.warmup:
+            times.append((time.perf_counter() - t0) * NQ)
+    t = float(np.mean(times))
+    eig_per_disk = 100.0  # Weyl estimate for the disk (area*k/2pi*2R - L/4pi*2R)
+    val = eig_per_disk / t
+    print(json.dumps({"impl": "reference", "metric": "eigenvalues/s (Beyn disk, FP64 CPU restatement)", "value": val,
+                      "unit": "eigenvalues/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": t * 1e3, "higher_is_better": True, "dtype": "c128", "data": "synthetic",
+                      "config": {"workload": "beyn_cfie_kress_star_N2048_k0_200_R0.5_nq48_L64"},
+                      "cpu_baseline": {"value": val, "unit": "eigenvalues/s", "cores": os.cpu_count(), "kind": "port",
+                                       "sample": "one contour node per step, extrapolated x48"},
+                      "e2e": {"value": val, "unit": "eigenvalues/s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,140 @@
+/*
+ * qbgpu.h — C ABI of libqbgpu, the GB300 (sm_103a) boundary-integral hot path
+ * of QuantumBilliards.jl.
+ *
+ * Conventions
+ *   - Every function returns qbg_status (0 = QBG_OK). No exception or longjmp
+ *     crosses the ABI. qbg_last_error() returns the calling thread's message.
+ *   - Complex numbers are interleaved (re, im) doubles, bit-identical to Julia
+ *     ComplexF64 / C double _Complex. Matrices are column-major with leading
+ *     dimension equal to their row count (Julia Matrix{ComplexF64}).
+ *   - Pointers are host pointers unless a call's flags contain
+ *     QBG_PTR_DEVICE, in which case they are device pointers on the current
+ *     CUDA device.
+ *   - Handles own their device memory and one CUDA stream each. Calls on
+ *     different handles may run concurrently from different threads; calls on
+ *     the same handle are serialised by the handle.
+ *
+ * Each entry point names the reference function it replaces
+ * (paths inside QuantumBilliards.jl).
+ */
+#ifndef QBGPU_H
+#define QBGPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t qbg_status;
+
+enum {
+  QBG_OK = 0,
+  QBG_EINVAL = 1,     /* bad argument */
+  QBG_ENOMEM = 2,     /* device allocation failed */
+  QBG_EBUDGET = 3,    /* request exceeds the handle's HBM budget */
+  QBG_ESINGULAR = 4,  /* exactly singular pivot met (factorisation continues, as lu!(; check=false)) */
+  QBG_ETIMEOUT = 5,   /* a bounded device wait gave up */
+  QBG_ECUDA = 6,      /* CUDA runtime / library error */
+  QBG_ENOTSUP = 7     /* combination not implemented */
+};
+
+enum { QBG_FORM_DLP = 0, QBG_FORM_CFIE = 1 };
+enum { QBG_PREC_FP64 = 0, QBG_PREC_MIXED = 1 };
+enum { QBG_PTR_DEVICE = 1 };
+
+/* Boundary discretisation (BoundaryPointsCFIE, boundarypoints.jl:487-503),
+ * components concatenated; holes already orientation-reversed as
+ * evaluate_points returns them (cfie.jl:822-834). */
+typedef struct qbg_geom_desc {
+  int32_t form;                 /* QBG_FORM_DLP (one component) or QBG_FORM_CFIE */
+  int32_t ncomp;                /* number of closed components */
+  const int64_t* comp_offsets;  /* ncomp+1 offsets, [0] = 0, [ncomp] = n */
+  const double* x;              /* n node coordinates */
+  const double* y;
+  const double* dx;             /* n first derivatives d gamma / d sigma */
+  const double* dy;
+  const double* ddx;            /* n second derivatives */
+  const double* ddy;
+  const double* ts;             /* n computational parameters sigma (Kress log term) */
+  const double* ws;             /* n quadrature weights */
+  /* optional symmetry reduction for DLP (DLPKressReducedWorkspace, dlp_kress.jl:65-78):
+   * m fundamental nodes, each with norb images (its own index included) */
+  int64_t m;                    /* 0 = no reduction */
+  int32_t norb;
+  const int64_t* fund;          /* m full indices I_a */
+  const int64_t* orbit;         /* m*norb full indices of the images of I_b */
+  const double* orbit_scale;    /* m*norb complex scale factors (character values) */
+} qbg_geom_desc;
+
+typedef struct qbg_geom qbg_geom;
+typedef struct qbg_beyn qbg_beyn;
+
+/* Library / error helpers */
+qbg_status qbg_version(int32_t* major, int32_t* minor);
+size_t qbg_last_error(char* buf, size_t len);
+qbg_status qbg_device_sync(void);
+
+/* Upload a discretisation; computes the Kress circulant column per component
+ * (kress_R!, boundarypoints.jl:310-358) and the speed/curvature terms
+ * (cfie_geom_cache, boundarypoints.jl:854-880) on the device.
+ * Replaces: build_dlp_kress_workspace (dlp_kress.jl:679-708),
+ *           build_cfie_kress_workspace (cfie_kress.jl:230-270). */
+qbg_status qbg_geom_create(const qbg_geom_desc* desc, qbg_geom** out);
+qbg_status qbg_geom_destroy(qbg_geom* g);
+qbg_status qbg_geom_dim(const qbg_geom* g, int64_t* dim);
+
+/* Assemble the boundary matrix (and, with deriv = 1, its first and second
+ * k-derivatives) at nk wavenumbers ks (complex, interleaved).
+ *   outs: nk*(1+2*deriv) pointers to dim x dim complex matrices, ordered
+ *         [A(k_1..k_nk), A'(k_1..k_nk), A''(k_1..k_nk)].
+ *   prec = QBG_PREC_FP64: complex128 outputs; QBG_PREC_MIXED: complex64.
+ * Replaces: construct_matrices! (dlp_kress.jl:1627-1679, cfie_kress.jl:893-929),
+ *           construct_boundary_matrices! (chebyshev_euclidian_helmholtz_dlp_kress.jl:1110,
+ *           ..._cfie_kress.jl:1431) and construct_boundary_matrices_with_derivatives!
+ *           (..._dlp_kress.jl:1126). */
+qbg_status qbg_assemble(qbg_geom* g, const double* ks, int64_t nk, int32_t deriv, int32_t prec, int32_t flags,
+                        void* const* outs);
+
+/* Beyn contour step (construct_B_matrix, beyn.jl:257-322), device side:
+ * create = contour nodes z_j = k0 + R e^{i theta_j}, assembly of all T(z_j),
+ * batched LU; moments = T(z_j)^{-1} V for every node and the sums
+ * A0 = sum w_j X_j, A1 = sum w_j z_j X_j. The host does the rank-revealing
+ * SVD of A0 and the small eigenproblem. moments may be called again with a
+ * wider V (the reference's r -> 2r regrowth, beyn.jl:291-309) without
+ * refactoring. */
+typedef struct qbg_beyn_opts {
+  int32_t flags;        /* QBG_PTR_DEVICE: V, A0, A1 are device pointers */
+  int32_t max_refine;   /* mixed form: maximum refinement sweeps (default 4) */
+  double refine_tol;    /* mixed form: stop when max|R| <= tol * max|V| (default 1e-14) */
+  int32_t nb;           /* LU block size (0 = default) */
+} qbg_beyn_opts;
+
+typedef struct qbg_beyn_stats {
+  int32_t refine_sweeps;   /* refinement sweeps performed in the last moments call */
+  double refine_residual;  /* final max|R| / max|V| (mixed form) */
+  int32_t singular;        /* number of contour nodes with an exactly zero pivot */
+  double ms_assemble, ms_factor, ms_solve;  /* device time of the phases */
+} qbg_beyn_stats;
+
+qbg_status qbg_beyn_create(qbg_geom* g, double k0_re, double k0_im, double R, int32_t nq, int32_t prec,
+                           const qbg_beyn_opts* opts, qbg_beyn** out);
+qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0, double* A1,
+                            qbg_beyn_stats* stats);
+qbg_status qbg_beyn_destroy(qbg_beyn* b);
+
+/* Smallest singular value of A(k) for nk real wavenumbers (the :svd branch of
+ * @svd_or_det_solve, macros.jl:159-161, called by k_sweep,
+ * sweepmethods.jl:132-152). */
+qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig);
+
+/* Device special functions, for validation: out[4*i..] = J0, J1, Y0, Y1 at z[i]
+ * (complex interleaved). f32 = 1 selects the FP32 asymptotic evaluator. */
+qbg_status qbg_bessel01(const double* z, int64_t n, int32_t f32, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,606 @@
+// C ABI of libqbgpu (declarations and reference citations in include/qbgpu.h).
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include <cusolverDn.h>
+
+#include "qbg_assemble.cuh"
+#include "qbg_linalg.cuh"
+
+namespace qbg {
+static thread_local std::string g_err;
+void set_error(const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+}
+int cuda_status(cudaError_t e, const char* what) {
+  set_error("%s: %s", what, cudaGetErrorString(e));
+  return (e == cudaErrorMemoryAllocation) ? QBG_ENOMEM : QBG_ECUDA;
+}
+
+template <class P>
+static int dmalloc(P** p, size_t bytes) {
+  cudaError_t e = cudaMalloc((void**)p, bytes ? bytes : 1);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return cuda_status(e, "cudaMalloc");
+  }
+  return QBG_OK;
+}
+}  // namespace qbg
+
+using namespace qbg;
+
+struct qbg_geom {
+  GeomDev d;
+  int64_t dim = 0;
+  std::vector<void*> allocs;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+  ~qbg_geom() {
+    for (void* p : allocs) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+  template <class P>
+  int upload(const P* host, size_t count, const P** dev) {
+    P* p = nullptr;
+    int s = dmalloc(&p, count * sizeof(P));
+    if (s) return s;
+    allocs.push_back(p);
+    QBG_CUDA(cudaMemcpyAsync(p, host, count * sizeof(P), cudaMemcpyHostToDevice, stream));
+    *dev = p;
+    return QBG_OK;
+  }
+};
+
+#define QBG_TRY(x)          \
+  do {                      \
+    int _s = (x);           \
+    if (_s) return _s;      \
+  } while (0)
+
+extern "C" {
+
+qbg_status qbg_version(int32_t* major, int32_t* minor) {
+  if (major) *major = 0;
+  if (minor) *minor = 1;
+  return QBG_OK;
+}
+
+size_t qbg_last_error(char* buf, size_t len) {
+  const std::string& e = qbg::g_err;
+  if (buf && len) {
+    size_t n = std::min(len - 1, e.size());
+    memcpy(buf, e.data(), n);
+    buf[n] = 0;
+  }
+  return e.size();
+}
+
+qbg_status qbg_device_sync(void) {
+  QBG_CUDA(cudaDeviceSynchronize());
+  return QBG_OK;
+}
+
+qbg_status qbg_geom_create(const qbg_geom_desc* desc, qbg_geom** out) {
+  if (!desc || !out) { set_error("qbg_geom_create: null argument"); return QBG_EINVAL; }
+  *out = nullptr;
+  if (desc->ncomp < 1 || !desc->comp_offsets || !desc->x || !desc->y || !desc->dx || !desc->dy || !desc->ddx ||
+      !desc->ddy || !desc->ts || !desc->ws) {
+    set_error("qbg_geom_create: missing geometry arrays");
+    return QBG_EINVAL;
+  }
+  if (desc->form != QBG_FORM_DLP && desc->form != QBG_FORM_CFIE) {
+    set_error("qbg_geom_create: unknown form %d", desc->form);
+    return QBG_EINVAL;
+  }
+  if (desc->form == QBG_FORM_DLP && desc->ncomp != 1) {
+    set_error("DLP_kress supports exactly one closed boundary component; use a CFIE form");
+    return QBG_EINVAL;
+  }
+  const int64_t n = desc->comp_offsets[desc->ncomp];
+  if (desc->comp_offsets[0] != 0 || n < 2 || n > (1ll << 30)) {
+    set_error("qbg_geom_create: bad component offsets (n = %lld)", (long long)n);
+    return QBG_EINVAL;
+  }
+  for (int c = 0; c < desc->ncomp; ++c)
+    if (desc->comp_offsets[c + 1] - desc->comp_offsets[c] < 2) {
+      set_error("qbg_geom_create: component %d has fewer than 2 nodes", c);
+      return QBG_EINVAL;
+    }
+  qbg_geom* g = new (std::nothrow) qbg_geom();
+  if (!g) { set_error("host allocation failed"); return QBG_ENOMEM; }
+  auto fail = [&](int s) { delete g; return s; };
+  cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return fail(cuda_status(e, "cudaStreamCreate"));
+  std::vector<double> speed(n), kappa(n), nx(n), ny(n);
+  std::vector<int> comp(n), lidx(n), coff(desc->ncomp + 1);
+  for (int c = 0; c <= desc->ncomp; ++c) coff[c] = (int)desc->comp_offsets[c];
+  for (int c = 0; c < desc->ncomp; ++c)
+    for (int64_t i = coff[c]; i < coff[c + 1]; ++i) { comp[i] = c; lidx[i] = (int)(i - coff[c]); }
+  for (int64_t i = 0; i < n; ++i) {
+    const double dx = desc->dx[i], dy = desc->dy[i], ddx = desc->ddx[i], ddy = desc->ddy[i];
+    const double s2 = dx * dx + dy * dy;
+    if (!(s2 > 0.0) || !std::isfinite(desc->x[i]) || !std::isfinite(desc->y[i])) {
+      delete g;
+      set_error("qbg_geom_create: degenerate or non-finite node %lld", (long long)i);
+      return QBG_EINVAL;
+    }
+    speed[i] = std::sqrt(s2);
+    kappa[i] = (1.0 / (2.0 * M_PI)) * (-(dx * ddy - dy * ddx)) / s2;  // boundarypoints.jl:876-878
+    nx[i] = dy / speed[i];                                               // dlp_kress.jl:686-699
+    ny[i] = -dx / speed[i];
+  }
+  GeomDev& d = g->d;
+  d.n = (int)n;
+  d.ncomp = desc->ncomp;
+  d.form = desc->form;
+  int s = QBG_OK;
+  if ((s = g->upload(desc->x, n, &d.x)) || (s = g->upload(desc->y, n, &d.y)) || (s = g->upload(desc->dx, n, &d.dx)) ||
+      (s = g->upload(desc->dy, n, &d.dy)) || (s = g->upload(desc->ts, n, &d.ts)) ||
+      (s = g->upload(desc->ws, n, &d.ws)) || (s = g->upload(speed.data(), n, &d.speed)) ||
+      (s = g->upload(kappa.data(), n, &d.kappa)) || (s = g->upload(comp.data(), n, &d.comp)) ||
+      (s = g->upload(lidx.data(), n, &d.lidx)) || (s = g->upload(coff.data(), coff.size(), &d.coff)) ||
+      (s = g->upload(nx.data(), n, &d.nx)) || (s = g->upload(ny.data(), n, &d.ny)))
+    return fail(s);
+  double* kcol = nullptr;
+  if ((s = dmalloc(&kcol, sizeof(double) * n))) return fail(s);
+  g->allocs.push_back(kcol);
+  for (int c = 0; c < desc->ncomp; ++c)
+    if ((s = launch_kress_column(kcol + coff[c], coff[c + 1] - coff[c], g->stream))) return fail(s);
+  d.kcol = kcol;
+  d.m = (int)n;
+  if (desc->m > 0) {
+    if (desc->form != QBG_FORM_DLP || desc->norb < 1 || !desc->fund || !desc->orbit || !desc->orbit_scale ||
+        desc->m > n) {
+      delete g;
+      set_error("qbg_geom_create: invalid symmetry reduction arguments");
+      return QBG_EINVAL;
+    }
+    std::vector<int> fund(desc->m), orb((size_t)desc->m * desc->norb);
+    for (int64_t a = 0; a < desc->m; ++a) {
+      if (desc->fund[a] < 0 || desc->fund[a] >= n) { delete g; set_error("fund index out of range"); return QBG_EINVAL; }
+      fund[a] = (int)desc->fund[a];
+    }
+    for (size_t q = 0; q < orb.size(); ++q) {
+      if (desc->orbit[q] < 0 || desc->orbit[q] >= n) { delete g; set_error("orbit index out of range"); return QBG_EINVAL; }
+      orb[q] = (int)desc->orbit[q];
+    }
+    d.m = (int)desc->m;
+    d.norb = desc->norb;
+    if ((s = g->upload(fund.data(), fund.size(), &d.fund)) || (s = g->upload(orb.data(), orb.size(), &d.orb)) ||
+        (s = g->upload(desc->orbit_scale, orb.size() * 2, &d.orb_scale)))
+      return fail(s);
+  }
+  g->dim = d.m;
+  e = cudaStreamSynchronize(g->stream);
+  if (e != cudaSuccess) return fail(cuda_status(e, "qbg_geom_create sync"));
+  *out = g;
+  return QBG_OK;
+}
+
+qbg_status qbg_geom_destroy(qbg_geom* g) {
+  delete g;
+  return QBG_OK;
+}
+
+qbg_status qbg_geom_dim(const qbg_geom* g, int64_t* dim) {
+  if (!g || !dim) { set_error("qbg_geom_dim: null argument"); return QBG_EINVAL; }
+  *dim = g->dim;
+  return QBG_OK;
+}
+
+static int check_ks(const double* ks, int64_t nk) {
+  for (int64_t q = 0; q < 2 * nk; ++q)
+    if (!std::isfinite(ks[q])) { set_error("non-finite wavenumber at index %lld", (long long)(q / 2)); return QBG_EINVAL; }
+  for (int64_t q = 0; q < nk; ++q)
+    if (ks[2 * q] == 0.0 && ks[2 * q + 1] == 0.0) { set_error("wavenumber k = 0 is not allowed"); return QBG_EINVAL; }
+  return QBG_OK;
+}
+
+qbg_status qbg_assemble(qbg_geom* g, const double* ks, int64_t nk, int32_t deriv, int32_t prec, int32_t flags,
+                        void* const* outs) {
+  if (!g || !ks || !outs || nk < 1 || (deriv != 0 && deriv != 1) || (prec != 0 && prec != 1)) {
+    set_error("qbg_assemble: invalid arguments");
+    return QBG_EINVAL;
+  }
+  QBG_TRY(check_ks(ks, nk));
+  std::lock_guard<std::mutex> lk(g->mu);
+  const int64_t dim = g->dim;
+  const size_t esz = prec ? sizeof(cxf) : sizeof(cxd);
+  const size_t mat_bytes = (size_t)dim * dim * esz;
+  const int nout = 1 + 2 * deriv;
+  const bool dev = (flags & QBG_PTR_DEVICE) != 0;
+  // chunk the k list so that device staging stays below 8 GiB for host outputs
+  int64_t chunk = nk;
+  if (!dev) chunk = std::max<int64_t>(1, std::min<int64_t>(nk, (int64_t)((8ull << 30) / (mat_bytes * nout))));
+  cxd* dks = nullptr;
+  void** dptrs = nullptr;
+  char* stage = nullptr;
+  int s = QBG_OK;
+  if ((s = dmalloc(&dks, sizeof(cxd) * nk))) return s;
+  if ((s = dmalloc(&dptrs, sizeof(void*) * chunk * nout))) { cudaFree(dks); return s; }
+  if (!dev && (s = dmalloc(&stage, mat_bytes * chunk * nout))) { cudaFree(dks); cudaFree(dptrs); return s; }
+  cudaStream_t st = g->stream;
+  std::vector<void*> hp(chunk * nout);
+  auto cleanup = [&]() { cudaFree(dks); cudaFree(dptrs); if (stage) cudaFree(stage); };
+  cudaError_t e = cudaMemcpyAsync(dks, ks, sizeof(cxd) * nk, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) { cleanup(); return cuda_status(e, "qbg_assemble H2D"); }
+  for (int64_t k0 = 0; k0 < nk; k0 += chunk) {
+    const int64_t c = std::min(chunk, nk - k0);
+    for (int o = 0; o < nout; ++o)
+      for (int64_t q = 0; q < c; ++q)
+        hp[o * c + q] = dev ? outs[o * nk + k0 + q] : (void*)(stage + (size_t)(o * c + q) * mat_bytes);
+    e = cudaMemcpyAsync(dptrs, hp.data(), sizeof(void*) * c * nout, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) { cleanup(); return cuda_status(e, "qbg_assemble ptrs"); }
+    s = launch_assemble(g->d, dks + k0, (int)c, deriv, prec, dptrs, dim, st);
+    if (s) { cleanup(); return s; }
+    if (!dev) {
+      for (int o = 0; o < nout; ++o)
+        for (int64_t q = 0; q < c; ++q) {
+          e = cudaMemcpyAsync(outs[o * nk + k0 + q], stage + (size_t)(o * c + q) * mat_bytes, mat_bytes,
+                              cudaMemcpyDeviceToHost, st);
+          if (e != cudaSuccess) { cleanup(); return cuda_status(e, "qbg_assemble D2H"); }
+        }
+    }
+    e = cudaStreamSynchronize(st);  // also keeps hp/dptrs valid for the next chunk
+    if (e != cudaSuccess) { cleanup(); return cuda_status(e, "qbg_assemble"); }
+  }
+  cleanup();
+  return QBG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Beyn contour step
+// ---------------------------------------------------------------------------
+struct qbg_beyn {
+  qbg_geom* g = nullptr;
+  int n = 0, nq = 0, prec = 0;
+  qbg_beyn_opts opts{};
+  cxd* zj = nullptr;  // device contour nodes
+  cxd* wj = nullptr;  // device contour weights
+  LUBatch<double> fd;
+  LUBatch<float> ff;
+  cxf* Tcopy = nullptr;  // mixed: unfactored complex64 T(z_j) for the refinement residual
+  std::vector<void*> allocs;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  float ms_assemble = 0, ms_factor = 0;
+  int singular = 0;
+  std::mutex mu;
+  ~qbg_beyn() {
+    for (void* p : allocs) cudaFree(p);
+    for (auto& e : ev) if (e) cudaEventDestroy(e);
+  }
+  template <class P>
+  int alloc(P** p, size_t bytes) {
+    int s = dmalloc(p, bytes);
+    if (!s) allocs.push_back(*p);
+    return s;
+  }
+};
+
+template <class T>
+static int beyn_setup_lu(qbg_beyn* b, LUBatch<T>& f, int nb) {
+  f.n = b->n;
+  f.batch = b->nq;
+  f.nb = nb;
+  f.nblk = (b->n + nb - 1) / nb;
+  f.stride = (long long)b->n * b->n;
+  QBG_TRY(b->alloc(&f.A, sizeof(cx<T>) * (size_t)f.stride * f.batch));
+  QBG_TRY(b->alloc(&f.ipiv, sizeof(int) * (size_t)b->n * f.batch));
+  QBG_TRY(b->alloc(&f.perm, sizeof(int) * (size_t)b->n * f.batch));
+  QBG_TRY(b->alloc(&f.info, sizeof(int) * f.batch));
+  QBG_TRY(b->alloc(&f.Linv, sizeof(cx<T>) * (size_t)f.nblk * nb * nb * f.batch));
+  QBG_TRY(b->alloc(&f.Uinv, sizeof(cx<T>) * (size_t)f.nblk * nb * nb * f.batch));
+  return QBG_OK;
+}
+
+static int beyn_create_impl(qbg_beyn* b, double k0_re, double k0_im, double R) {
+  const int n = b->n, nq = b->nq;
+  cudaStream_t st = b->st;
+  // contour (beyn.jl:258-261): theta_j = 2 pi j / nq, z_j = k0 + R e^{i theta}, w_j = (R/nq) e^{i theta}
+  std::vector<cxd> z(nq), w(nq);
+  for (int j = 0; j < nq; ++j) {
+    const double th = 2.0 * M_PI * (double)j / (double)nq;
+    const double c = std::cos(th), s = std::sin(th);
+    z[j] = cxd(k0_re + R * c, k0_im + R * s);
+    w[j] = cxd((R / nq) * c, (R / nq) * s);
+  }
+  QBG_TRY(b->alloc(&b->zj, sizeof(cxd) * nq));
+  QBG_TRY(b->alloc(&b->wj, sizeof(cxd) * nq));
+  QBG_CUDA(cudaMemcpyAsync(b->zj, z.data(), sizeof(cxd) * nq, cudaMemcpyHostToDevice, st));
+  QBG_CUDA(cudaMemcpyAsync(b->wj, w.data(), sizeof(cxd) * nq, cudaMemcpyHostToDevice, st));
+  for (auto& e : b->ev) QBG_CUDA(cudaEventCreate(&e));
+  const int nb = b->opts.nb > 0 ? b->opts.nb : (b->prec ? 64 : 32);
+  if (nb != 32 && nb != 64) { set_error("LU block size must be 32 or 64"); return QBG_EINVAL; }
+  std::vector<void*> ptrs(nq);
+  void** dptrs = nullptr;
+  QBG_TRY(b->alloc(&dptrs, sizeof(void*) * nq));
+  if (b->prec == 0) {
+    QBG_TRY(beyn_setup_lu(b, b->fd, nb));
+    for (int j = 0; j < nq; ++j) ptrs[j] = b->fd.A + (size_t)j * b->fd.stride;
+  } else {
+    QBG_TRY(beyn_setup_lu(b, b->ff, nb));
+    for (int j = 0; j < nq; ++j) ptrs[j] = b->ff.A + (size_t)j * b->ff.stride;
+  }
+  QBG_CUDA(cudaMemcpyAsync(dptrs, ptrs.data(), sizeof(void*) * nq, cudaMemcpyHostToDevice, st));
+  QBG_CUDA(cudaEventRecord(b->ev[0], st));
+  QBG_TRY(launch_assemble(b->g->d, b->zj, nq, 0, b->prec, dptrs, n, st));
+  QBG_CUDA(cudaEventRecord(b->ev[1], st));
+  if (b->prec == 0) {
+    QBG_TRY(lu_factor<double>(b->fd, st));
+  } else {
+    const size_t bytes = sizeof(cxf) * (size_t)b->ff.stride * nq;
+    QBG_TRY(b->alloc(&b->Tcopy, bytes));
+    QBG_CUDA(cudaMemcpyAsync(b->Tcopy, b->ff.A, bytes, cudaMemcpyDeviceToDevice, st));
+    QBG_TRY(lu_factor<float>(b->ff, st));
+  }
+  QBG_CUDA(cudaEventRecord(b->ev[2], st));
+  std::vector<int> info(nq);
+  QBG_CUDA(cudaMemcpyAsync(info.data(), b->prec ? b->ff.info : b->fd.info, sizeof(int) * nq,
+                           cudaMemcpyDeviceToHost, st));
+  QBG_CUDA(cudaStreamSynchronize(st));
+  b->singular = 0;
+  for (int v : info) b->singular += (v != 0);
+  QBG_CUDA(cudaEventElapsedTime(&b->ms_assemble, b->ev[0], b->ev[1]));
+  QBG_CUDA(cudaEventElapsedTime(&b->ms_factor, b->ev[1], b->ev[2]));
+  return QBG_OK;
+}
+
+extern "C" {
+
+qbg_status qbg_beyn_create(qbg_geom* g, double k0_re, double k0_im, double R, int32_t nq, int32_t prec,
+                           const qbg_beyn_opts* opts, qbg_beyn** out) {
+  if (!g || !out || nq < 2 || !(R > 0.0) || (prec != 0 && prec != 1) || !std::isfinite(k0_re) ||
+      !std::isfinite(k0_im) || !std::isfinite(R)) {
+    set_error("qbg_beyn_create: invalid arguments");
+    return QBG_EINVAL;
+  }
+  *out = nullptr;
+  if (g->d.m != g->d.n && prec != 0) {
+    set_error("symmetry-reduced Beyn runs in the FP64 form only");
+    return QBG_ENOTSUP;
+  }
+  qbg_beyn* b = new (std::nothrow) qbg_beyn();
+  if (!b) { set_error("host allocation failed"); return QBG_ENOMEM; }
+  b->g = g;
+  b->n = (int)g->dim;
+  b->nq = nq;
+  b->prec = prec;
+  b->opts.flags = 0;
+  b->opts.max_refine = 4;
+  b->opts.refine_tol = 1e-14;
+  b->opts.nb = 0;
+  if (opts) {
+    b->opts = *opts;
+    if (b->opts.max_refine <= 0) b->opts.max_refine = 4;
+    if (!(b->opts.refine_tol > 0.0)) b->opts.refine_tol = 1e-14;
+  }
+  std::lock_guard<std::mutex> lk(g->mu);
+  b->st = g->stream;
+  int s = beyn_create_impl(b, k0_re, k0_im, R);
+  if (s) {
+    cudaStreamSynchronize(b->st);
+    delete b;
+    return s;
+  }
+  *out = b;
+  return QBG_OK;
+}
+
+qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0, double* A1,
+                            qbg_beyn_stats* stats) {
+  if (!b || !V || !A0 || !A1 || L < 1) {
+    set_error("qbg_beyn_moments: invalid arguments");
+    return QBG_EINVAL;
+  }
+  std::lock_guard<std::mutex> lk(b->g->mu);
+  const int n = b->n, nq = b->nq;
+  const bool dev = (b->opts.flags & QBG_PTR_DEVICE) != 0;
+  cudaStream_t st = b->st;
+  const size_t nl = (size_t)n * L;
+  std::vector<void*> tmp;
+  auto cleanup = [&]() { for (void* p : tmp) cudaFree(p); };
+  auto talloc = [&](void** p, size_t bytes) {
+    int s = dmalloc(p, bytes);
+    if (!s) tmp.push_back(*p);
+    return s;
+  };
+  int s = QBG_OK;
+  cxd *dV = nullptr, *dA0 = nullptr, *dA1 = nullptr;
+  if (dev) {
+    dV = (cxd*)V; dA0 = (cxd*)A0; dA1 = (cxd*)A1;
+  } else {
+    if ((s = talloc((void**)&dV, sizeof(cxd) * nl)) || (s = talloc((void**)&dA0, sizeof(cxd) * nl)) ||
+        (s = talloc((void**)&dA1, sizeof(cxd) * nl))) { cleanup(); return s; }
+    cudaError_t e = cudaMemcpyAsync(dV, V, sizeof(cxd) * nl, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) { cleanup(); return cuda_status(e, "V H2D"); }
+  }
+  cudaEventRecord(b->ev[0], st);
+  int sweeps = 0;
+  double rel = 0.0;
+  if (b->prec == 0) {
+    cxd* X = nullptr;
+    if ((s = talloc((void**)&X, sizeof(cxd) * nl * nq))) { cleanup(); return s; }
+    if ((s = lu_solve_shared<double>(b->fd, dV, (int)L, X, 0, st)) ||
+        (s = moments<double>(X, (long long)nl, nq, n, (int)L, b->wj, b->zj, dA0, dA1, 0, st))) {
+      cleanup(); return s;
+    }
+  } else {
+    // mixed: X32 = LU32 \ V32, X64 = X32, then R = V - T X64 (compensated), X64 += LU32 \ R32
+    cxf *V32 = nullptr, *X32 = nullptr, *R32 = nullptr;
+    cxd *X64 = nullptr, *R64 = nullptr;
+    double* dmax = nullptr;
+    if ((s = talloc((void**)&V32, sizeof(cxf) * nl)) || (s = talloc((void**)&X32, sizeof(cxf) * nl * nq)) ||
+        (s = talloc((void**)&R32, sizeof(cxf) * nl * nq)) || (s = talloc((void**)&X64, sizeof(cxd) * nl * nq)) ||
+        (s = talloc((void**)&R64, sizeof(cxd) * nl * nq)) || (s = talloc((void**)&dmax, sizeof(double)))) {
+      cleanup(); return s;
+    }
+    // max |V| (|re|+|im|) on the host side of the copy is not available for device V: compute by residual with X=0
+    cudaError_t e = cudaMemsetAsync(X64, 0, sizeof(cxd) * nl * nq, st);
+    if (e != cudaSuccess) { cleanup(); return cuda_status(e, "memset"); }
+    if ((s = convert_d2f(dV, V32, (long long)nl, st)) ||
+        (s = lu_solve_shared<float>(b->ff, V32, (int)L, X32, 0, st)) ||
+        (s = axpy_f2d(X32, X64, (long long)(nl * nq), st))) { cleanup(); return s; }
+    double vmax = 0.0;
+    {
+      // |V|max via the residual kernel on one matrix with X = 0 is wasteful; do it on the host copy instead
+      std::vector<cxd> hv;
+      if (!dev) {
+        const cxd* hvp = reinterpret_cast<const cxd*>(V);
+        for (size_t q = 0; q < nl; ++q) vmax = std::max(vmax, std::fabs(hvp[q].re) + std::fabs(hvp[q].im));
+      } else {
+        hv.resize(nl);
+        e = cudaMemcpyAsync(hv.data(), dV, sizeof(cxd) * nl, cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) { cleanup(); return cuda_status(e, "V D2H"); }
+        cudaStreamSynchronize(st);
+        for (size_t q = 0; q < nl; ++q) vmax = std::max(vmax, std::fabs(hv[q].re) + std::fabs(hv[q].im));
+      }
+    }
+    if (!(vmax > 0.0)) vmax = 1.0;
+    for (int it = 0; it < b->opts.max_refine; ++it) {
+      e = cudaMemsetAsync(dmax, 0, sizeof(double), st);
+      if (e != cudaSuccess) { cleanup(); return cuda_status(e, "memset"); }
+      if ((s = residual_df32(b->Tcopy, b->ff.stride, X64, (long long)nl, dV, R64, (long long)nl, n, (int)L, nq,
+                             dmax, st))) { cleanup(); return s; }
+      double rmax = 0.0;
+      e = cudaMemcpyAsync(&rmax, dmax, sizeof(double), cudaMemcpyDeviceToHost, st);
+      if (e != cudaSuccess) { cleanup(); return cuda_status(e, "rmax D2H"); }
+      e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) { cleanup(); return cuda_status(e, "refine sync"); }
+      rel = rmax / vmax;
+      if (rel <= b->opts.refine_tol) break;
+      ++sweeps;
+      // correction solves, one right-hand block per contour node
+      if ((s = convert_d2f(R64, R32, (long long)(nl * nq), st)) ||
+          (s = lu_solve_shared<float>(b->ff, R32, (int)L, X32, (long long)nl, st)) ||
+          (s = axpy_f2d(X32, X64, (long long)(nl * nq), st))) { cleanup(); return s; }
+    }
+    if ((s = moments<double>(X64, (long long)nl, nq, n, (int)L, b->wj, b->zj, dA0, dA1, 0, st))) {
+      cleanup(); return s;
+    }
+  }
+  cudaEventRecord(b->ev[3], st);
+  if (!dev) {
+    cudaError_t e = cudaMemcpyAsync(A0, dA0, sizeof(cxd) * nl, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(A1, dA1, sizeof(cxd) * nl, cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) { cleanup(); return cuda_status(e, "A0/A1 D2H"); }
+  }
+  cudaError_t e = cudaStreamSynchronize(st);
+  cleanup();
+  if (e != cudaSuccess) return cuda_status(e, "qbg_beyn_moments");
+  if (stats) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, b->ev[0], b->ev[3]);
+    stats->refine_sweeps = sweeps;
+    stats->refine_residual = rel;
+    stats->singular = b->singular;
+    stats->ms_assemble = b->ms_assemble;
+    stats->ms_factor = b->ms_factor;
+    stats->ms_solve = ms;
+  }
+  return QBG_OK;
+}
+
+qbg_status qbg_beyn_destroy(qbg_beyn* b) {
+  if (b) {
+    cudaStreamSynchronize(b->st);
+    delete b;
+  }
+  return QBG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// sigma_min via cuSOLVER gesvd (values only)
+// ---------------------------------------------------------------------------
+qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig) {
+  if (!g || !ks || !sig || nk < 1) { set_error("qbg_sigma_min: invalid arguments"); return QBG_EINVAL; }
+  std::vector<double> kc(2 * nk);
+  for (int64_t q = 0; q < nk; ++q) { kc[2 * q] = ks[q]; kc[2 * q + 1] = 0.0; }
+  QBG_TRY(check_ks(kc.data(), nk));
+  std::lock_guard<std::mutex> lk(g->mu);
+  const int n = (int)g->dim;
+  cudaStream_t st = g->stream;
+  const int chunk = (int)std::min<int64_t>(nk, 16);
+  cxd *A = nullptr, *dks = nullptr, *work = nullptr;
+  double *S = nullptr, *rwork = nullptr;
+  int* dinfo = nullptr;
+  void** dptrs = nullptr;
+  cusolverDnHandle_t h = nullptr;
+  std::vector<void*> tmp;
+  auto cleanup = [&]() {
+    for (void* p : tmp) cudaFree(p);
+    if (h) cusolverDnDestroy(h);
+  };
+  auto talloc = [&](void** p, size_t bytes) {
+    int s = dmalloc(p, bytes);
+    if (!s) tmp.push_back(*p);
+    return s;
+  };
+  int s = QBG_OK;
+  if ((s = talloc((void**)&A, sizeof(cxd) * (size_t)n * n * chunk)) || (s = talloc((void**)&dks, sizeof(cxd) * nk)) ||
+      (s = talloc((void**)&S, sizeof(double) * n)) || (s = talloc((void**)&rwork, sizeof(double) * n)) ||
+      (s = talloc((void**)&dinfo, sizeof(int))) || (s = talloc((void**)&dptrs, sizeof(void*) * chunk))) {
+    cleanup(); return s;
+  }
+  if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) { cleanup(); set_error("cusolverDnCreate failed"); return QBG_ECUDA; }
+  cusolverDnSetStream(h, st);
+  int lwork = 0;
+  if (cusolverDnZgesvd_bufferSize(h, n, n, &lwork) != CUSOLVER_STATUS_SUCCESS) {
+    cleanup(); set_error("gesvd buffer size failed"); return QBG_ECUDA;
+  }
+  if ((s = talloc((void**)&work, sizeof(cxd) * (size_t)lwork))) { cleanup(); return s; }
+  cudaError_t e = cudaMemcpyAsync(dks, kc.data(), sizeof(cxd) * nk, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) { cleanup(); return cuda_status(e, "ks H2D"); }
+  std::vector<void*> hp(chunk);
+  for (int64_t k0 = 0; k0 < nk; k0 += chunk) {
+    const int c = (int)std::min<int64_t>(chunk, nk - k0);
+    for (int q = 0; q < c; ++q) hp[q] = A + (size_t)q * n * n;
+    e = cudaMemcpyAsync(dptrs, hp.data(), sizeof(void*) * c, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) { cleanup(); return cuda_status(e, "ptrs"); }
+    if ((s = launch_assemble(g->d, dks + k0, c, 0, 0, dptrs, n, st))) { cleanup(); return s; }
+    for (int q = 0; q < c; ++q) {
+      cusolverStatus_t cs = cusolverDnZgesvd(h, 'N', 'N', n, n, (cuDoubleComplex*)(A + (size_t)q * n * n), n, S,
+                                             nullptr, n, nullptr, n, (cuDoubleComplex*)work, lwork, rwork, dinfo);
+      if (cs != CUSOLVER_STATUS_SUCCESS) { cleanup(); set_error("cusolverDnZgesvd failed (%d)", (int)cs); return QBG_ECUDA; }
+      e = cudaMemcpyAsync(sig + k0 + q, S + (n - 1), sizeof(double), cudaMemcpyDeviceToHost, st);
+      if (e != cudaSuccess) { cleanup(); return cuda_status(e, "S D2H"); }
+    }
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { cleanup(); return cuda_status(e, "sigma_min"); }
+  }
+  cleanup();
+  return QBG_OK;
+}
+
+qbg_status qbg_bessel01(const double* z, int64_t n, int32_t f32, double* out) {
+  if (!z || !out || n < 1) { set_error("qbg_bessel01: invalid arguments"); return QBG_EINVAL; }
+  cxd *dz = nullptr, *dout = nullptr;
+  int s = dmalloc(&dz, sizeof(cxd) * n);
+  if (s) return s;
+  if ((s = dmalloc(&dout, sizeof(cxd) * 4 * n))) { cudaFree(dz); return s; }
+  cudaError_t e = cudaMemcpy(dz, z, sizeof(cxd) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    s = launch_bessel_eval(dz, (int)n, dout, f32, 0);
+    if (!s) e = cudaMemcpy(out, dout, sizeof(cxd) * 4 * n, cudaMemcpyDeviceToHost);
+  }
+  cudaFree(dz);
+  cudaFree(dout);
+  if (s) return s;
+  if (e != cudaSuccess) return cuda_status(e, "qbg_bessel01");
+  return QBG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,12 @@
+#pragma once
+#include "qbg_common.cuh"
+#include "qbg_geom.cuh"
+
+namespace qbg {
+// prec: 0 = FP64 (complex128 outputs), 1 = mixed (complex64 outputs)
+// outs_dev: device array of nk*(1+2*deriv) device pointers, each an ld x dim column-major matrix
+int launch_assemble(const GeomDev& g, const cxd* ks, int nk, int deriv, int prec, void* const* outs_dev,
+                    long long ld, cudaStream_t st);
+int launch_kress_column(double* out, int N, cudaStream_t st);
+int launch_bessel_eval(const cxd* z, int n, cxd* out, int f32, cudaStream_t st);
+}  // namespace qbg

@@ -1,0 +1,572 @@
+// Batched complex LU with partial pivoting, blocked triangular solves with a
+// probe block shared by the batch, contour moments and the mixed-form
+// refinement residual.
+//
+// Algorithm (right-looking blocked LU, the same factorisation LAPACK zgetrf
+// computes; the reference calls lu!(T; check=false), beyn.jl:270-277):
+//   for each block column [j0, j0+nb):
+//     1. k_getf2_panel   one CTA per matrix factors the n-j0 x nb panel
+//                        column by column (pivot = first max of |re|+|im|,
+//                        as izamax); zero pivots are recorded in info and
+//                        skipped, matching check=false.
+//     2. k_laswp         applies the panel's row interchanges to the columns
+//                        left and right of the panel.
+//     3. k_trtri         inverts the unit-lower diagonal block L11.
+//     4. gemm            U12 = inv(L11) A12   (in place, one M tile)
+//     5. gemm            A22 -= L21 U12       (trailing update)
+//   After the last panel the upper diagonal blocks are inverted so that the
+//   triangular solves are sequences of GEMMs.
+#include "qbg_linalg.cuh"
+
+namespace qbg {
+
+// ---------------------------------------------------------------------------
+// batched complex GEMM  C = alpha A B + beta C   (column-major)
+// 64 x 64 tile, K step 16, 256 threads, 4 x 4 outputs per thread.
+// Thread (tx, ty): rows tx + 16 a, columns ty + 16 b, so that the 16 lanes
+// with consecutive tx store 16 consecutive rows of a column.
+// Safe for C == B when one M tile covers all of K (used for inv(L11) A12).
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, cx<T> alpha, const cx<T>* __restrict__ A,
+                                              long long lda, long long sA, const cx<T>* B, long long ldb,
+                                              long long sB, cx<T> beta, cx<T>* C, long long ldc, long long sC) {
+  constexpr int BM = 64, BN = 64, BK = 16;
+  __shared__ cx<T> As[BK][BM];
+  __shared__ cx<T> Bs[BK][BN + 1];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  const long long bz = blockIdx.z;
+  const cx<T>* Ab = A + bz * sA;
+  const cx<T>* Bb = B + bz * sB;
+  cx<T>* Cb = C + bz * sC;
+  cx<T> acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = cx<T>(0, 0);
+  for (int k0 = 0; k0 < K; k0 += BK) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int idx = tid + q * 256;
+      const int i = idx & (BM - 1), kk = idx >> 6;
+      const int gi = m0 + i, gk = k0 + kk;
+      As[kk][i] = (gi < M && gk < K) ? Ab[(long long)gi + (long long)gk * lda] : cx<T>(0, 0);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int idx = tid + q * 256;
+      const int kk = idx & (BK - 1), jj = idx >> 4;
+      const int gk = k0 + kk, gj = n0 + jj;
+      Bs[kk][jj] = (gk < K && gj < N) ? Bb[(long long)gk + (long long)gj * ldb] : cx<T>(0, 0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      cx<T> ar[4], br[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) ar[a] = As[kk][tx + 16 * a];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) br[b] = Bs[kk][ty + 16 * b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) cfma(acc[a][b], ar[a], br[b]);
+    }
+    __syncthreads();
+  }
+  const bool use_beta = !(beta.re == T(0) && beta.im == T(0));
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    const int gj = n0 + ty + 16 * b;
+    if (gj >= N) continue;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int gi = m0 + tx + 16 * a;
+      if (gi >= M) continue;
+      cx<T>* c = Cb + (long long)gi + (long long)gj * ldc;
+      cx<T> v = alpha * acc[a][b];
+      if (use_beta) v += beta * (*c);
+      *c = v;
+    }
+  }
+}
+
+template <class T>
+int gemm_batched(int M, int N, int K, cx<T> alpha, const cx<T>* A, long long lda, long long sA, const cx<T>* B,
+                 long long ldb, long long sB, cx<T> beta, cx<T>* C, long long ldc, long long sC, int batch,
+                 cudaStream_t st) {
+  if (M <= 0 || N <= 0 || batch <= 0) return QBG_OK;
+  dim3 grd((M + 63) / 64, (N + 63) / 64, batch);
+  k_gemm<T><<<grd, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
+  QBG_LAUNCH_CHECK("k_gemm");
+  return QBG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// panel factorisation (one CTA per matrix)
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ void argmax_merge(T& v, int& i, T ov, int oi) {
+  if (ov > v || (ov == v && oi < i)) {
+    v = ov;
+    i = oi;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(512) k_getf2_panel(cx<T>* A, int n, long long stride, int j0, int nb,
+                                                     int* ipiv, int* info) {
+  cx<T>* a = A + (long long)blockIdx.x * stride;
+  int* piv = ipiv + (long long)blockIdx.x * n;
+  __shared__ cx<T> urow[64];
+  __shared__ T wv[16];
+  __shared__ int wi[16];
+  __shared__ int s_p;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int jend = min(j0 + nb, n);
+  for (int c = j0; c < jend; ++c) {
+    cx<T>* col = a + (long long)c * n;
+    T best = T(-1);
+    int bi = 0x7fffffff;
+    for (int r = c + tid; r < n; r += nt) {
+      T v = cabs1(col[r]);
+      if (v > best) { best = v; bi = r; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      T ov = __shfl_down_sync(0xffffffffu, best, o);
+      int oi = __shfl_down_sync(0xffffffffu, bi, o);
+      argmax_merge(best, bi, ov, oi);
+    }
+    if ((tid & 31) == 0) { wv[tid >> 5] = best; wi[tid >> 5] = bi; }
+    __syncthreads();
+    if (tid < 32) {
+      const int nw = nt >> 5;
+      best = (tid < nw) ? wv[tid] : T(-1);
+      bi = (tid < nw) ? wi[tid] : 0x7fffffff;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        T ov = __shfl_down_sync(0xffffffffu, best, o);
+        int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        argmax_merge(best, bi, ov, oi);
+      }
+      if (tid == 0) {
+        if (bi >= n) bi = c;
+        s_p = bi;
+        piv[c] = bi;
+        if (!(best > T(0)) && info[blockIdx.x] == 0) info[blockIdx.x] = c + 1;
+      }
+    }
+    __syncthreads();
+    const int p = s_p;
+    if (p != c) {
+      for (int cc = j0 + tid; cc < jend; cc += nt) {
+        cx<T> t0 = a[c + (long long)cc * n];
+        a[c + (long long)cc * n] = a[p + (long long)cc * n];
+        a[p + (long long)cc * n] = t0;
+      }
+    }
+    __syncthreads();
+    const cx<T> pv = col[c];
+    const int nrem = jend - c - 1;
+    if (tid < nrem) urow[tid] = a[c + (long long)(c + 1 + tid) * n];
+    __syncthreads();
+    const bool nz = (pv.re != T(0) || pv.im != T(0));
+    const cx<T> inv = nz ? cinv(pv) : cx<T>(0, 0);
+    for (int r = c + 1 + tid; r < n; r += nt) {
+      cx<T> l = col[r];
+      if (nz) {
+        l = l * inv;
+        col[r] = l;
+      }
+      for (int q = 0; q < nrem; ++q) cfms(a[r + (long long)(c + 1 + q) * n], l, urow[q]);
+    }
+    __syncthreads();
+  }
+}
+
+// row interchanges of one panel on the columns outside the panel
+template <class T>
+__global__ void k_laswp(cx<T>* A, int n, long long stride, int j0, int nb, const int* ipiv) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  const int jend = min(j0 + nb, n);
+  if (col >= n || (col >= j0 && col < jend)) return;
+  cx<T>* a = A + (long long)blockIdx.y * stride + (long long)col * n;
+  const int* piv = ipiv + (long long)blockIdx.y * n;
+  for (int c = j0; c < jend; ++c) {
+    const int p = piv[c];
+    if (p != c) {
+      cx<T> t0 = a[c];
+      a[c] = a[p];
+      a[p] = t0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// inverse of one nb x nb diagonal block by recursive doubling:
+// lower unit:  inv([A 0; C B]) = [Ai 0; -Bi C Ai  Bi]
+// upper:       inv([A C; 0 B]) = [Ai -Ai C Bi; 0  Bi]
+// A partial last block is padded with the identity.
+// grid (nblocks_to_do, batch); block 256; dynamic smem = 1.25 nb^2 cx<T>
+// ---------------------------------------------------------------------------
+template <class T, bool UPPER>
+__global__ void __launch_bounds__(256) k_trtri(const cx<T>* A, int n, long long stride, int nb, int blk0,
+                                               cx<T>* inv, int nblk) {
+  extern __shared__ unsigned char smraw[];
+  cx<T>* S = reinterpret_cast<cx<T>*>(smraw);  // nb x nb, column-major
+  cx<T>* Tm = S + nb * nb;                       // scratch, nb*nb/4
+  const int blk = blk0 + blockIdx.x;
+  const int b = blockIdx.y;
+  const int r0 = blk * nb;
+  const int nr = min(nb, n - r0);
+  const cx<T>* a = A + (long long)b * stride;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < nb * nb; e += blockDim.x) {
+    const int i = e % nb, j = e / nb;
+    cx<T> v(0, 0);
+    if (i < nr && j < nr) {
+      if (UPPER) {
+        if (i < j) v = a[(r0 + i) + (long long)(r0 + j) * n];
+        else if (i == j) v = cinv(a[(r0 + i) + (long long)(r0 + j) * n]);
+      } else {
+        if (i > j) v = a[(r0 + i) + (long long)(r0 + j) * n];
+        else if (i == j) v = cx<T>(1, 0);
+      }
+    } else if (i == j) {
+      v = cx<T>(1, 0);
+    }
+    S[i + j * nb] = v;
+  }
+  __syncthreads();
+  for (int s = 1; s < nb; s <<= 1) {
+    const int npair = nb / (2 * s);
+    // T = C * Xi  (lower: C = S[o+s.., o..], Xi = Ai = S[o.., o..])
+    //             (upper: C = S[o.., o+s..], Xi = Bi = S[o+s.., o+s..])
+    for (int e = tid; e < npair * s * s; e += blockDim.x) {
+      const int pr = e / (s * s), rem = e % (s * s);
+      const int i = rem % s, j = rem / s;
+      const int o = pr * 2 * s;
+      cx<T> acc(0, 0);
+      if (!UPPER) {
+        for (int q = 0; q < s; ++q) cfma(acc, S[(o + s + i) + (o + q) * nb], S[(o + q) + (o + j) * nb]);
+      } else {
+        for (int q = 0; q < s; ++q) cfma(acc, S[(o + i) + (o + s + q) * nb], S[(o + s + q) + (o + s + j) * nb]);
+      }
+      Tm[pr * s * s + i + j * s] = acc;
+    }
+    __syncthreads();
+    for (int e = tid; e < npair * s * s; e += blockDim.x) {
+      const int pr = e / (s * s), rem = e % (s * s);
+      const int i = rem % s, j = rem / s;
+      const int o = pr * 2 * s;
+      cx<T> acc(0, 0);
+      if (!UPPER) {
+        // -Bi T, Bi = S[o+s.., o+s..]
+        for (int q = 0; q < s; ++q) cfma(acc, S[(o + s + i) + (o + s + q) * nb], Tm[pr * s * s + q + j * s]);
+        S[(o + s + i) + (o + j) * nb] = -acc;
+      } else {
+        // -Ai T, Ai = S[o.., o..]
+        for (int q = 0; q < s; ++q) cfma(acc, S[(o + i) + (o + q) * nb], Tm[pr * s * s + q + j * s]);
+        S[(o + i) + (o + s + j) * nb] = -acc;
+      }
+    }
+    __syncthreads();
+  }
+  cx<T>* out = inv + ((long long)b * nblk + blk) * nb * nb;
+  for (int e = tid; e < nb * nb; e += blockDim.x) out[e] = S[e];
+}
+
+// row permutation from the interchange list (sequential per matrix)
+__global__ void k_perm_from_ipiv(const int* ipiv, int* perm, int n) {
+  extern __shared__ int pm[];
+  const int b = blockIdx.x;
+  const int* piv = ipiv + (long long)b * n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) pm[i] = i;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int c = 0; c < n; ++c) {
+      const int p = piv[c];
+      const int t0 = pm[c];
+      pm[c] = pm[p];
+      pm[p] = t0;
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) perm[(long long)b * n + i] = pm[i];
+}
+
+template <class T>
+__global__ void k_gather_rows(const cx<T>* V, long long strideV, const int* perm, int n, int L, cx<T>* X) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (e >= (long long)n * L) return;
+  const int i = (int)(e % n), l = (int)(e / n);
+  X[(long long)b * n * L + e] = V[(long long)b * strideV + perm[(long long)b * n + i] + (long long)l * n];
+}
+
+template <class T>
+int lu_factor(LUBatch<T>& f, cudaStream_t st) {
+  const int n = f.n, nb = f.nb, batch = f.batch;
+  const size_t sm = (size_t)nb * nb * sizeof(cx<T>) * 5 / 4;
+  static bool attr_set[2] = {false, false};
+  if (!attr_set[sizeof(T) == 8]) {
+    QBG_CUDA(cudaFuncSetAttribute(k_trtri<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+    QBG_CUDA(cudaFuncSetAttribute(k_trtri<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+    attr_set[sizeof(T) == 8] = true;
+  }
+  QBG_CUDA(cudaMemsetAsync(f.info, 0, sizeof(int) * batch, st));
+  for (int j0 = 0; j0 < n; j0 += nb) {
+    const int w = min(nb, n - j0);
+    k_getf2_panel<T><<<batch, 512, 0, st>>>(f.A, n, f.stride, j0, nb, f.ipiv, f.info);
+    QBG_LAUNCH_CHECK("k_getf2_panel");
+    dim3 g2((n + 255) / 256, batch);
+    k_laswp<T><<<g2, 256, 0, st>>>(f.A, n, f.stride, j0, nb, f.ipiv);
+    QBG_LAUNCH_CHECK("k_laswp");
+    k_trtri<T, false><<<dim3(1, batch), 256, sm, st>>>(f.A, n, f.stride, nb, j0 / nb, f.Linv, f.nblk);
+    QBG_LAUNCH_CHECK("k_trtri lower");
+    const int rest = n - j0 - w;
+    if (rest > 0) {
+      // U12 = inv(L11) A12
+      int s = gemm_batched<T>(w, rest, w, cx<T>(1, 0), f.Linv + (long long)(j0 / nb) * nb * nb, nb,
+                              (long long)f.nblk * nb * nb, f.A + j0 + (long long)(j0 + w) * n, n, f.stride,
+                              cx<T>(0, 0), f.A + j0 + (long long)(j0 + w) * n, n, f.stride, batch, st);
+      if (s) return s;
+      // A22 -= L21 U12
+      s = gemm_batched<T>(rest, rest, w, cx<T>(-1, 0), f.A + (j0 + w) + (long long)j0 * n, n, f.stride,
+                          f.A + j0 + (long long)(j0 + w) * n, n, f.stride, cx<T>(1, 0),
+                          f.A + (j0 + w) + (long long)(j0 + w) * n, n, f.stride, batch, st);
+      if (s) return s;
+    }
+  }
+  k_trtri<T, true><<<dim3(f.nblk, batch), 256, sm, st>>>(f.A, n, f.stride, nb, 0, f.Uinv, f.nblk);
+  QBG_LAUNCH_CHECK("k_trtri upper");
+  if (sizeof(int) * (size_t)n > 48 * 1024)
+    QBG_CUDA(cudaFuncSetAttribute(k_perm_from_ipiv, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(sizeof(int) * (size_t)n)));
+  k_perm_from_ipiv<<<batch, 256, sizeof(int) * n, st>>>(f.ipiv, f.perm, n);
+  QBG_LAUNCH_CHECK("k_perm_from_ipiv");
+  return QBG_OK;
+}
+
+template <class T>
+int lu_solve_shared(const LUBatch<T>& f, const cx<T>* V, int L, cx<T>* X, long long strideV, cudaStream_t st) {
+  const int n = f.n, nb = f.nb, batch = f.batch;
+  const long long sX = (long long)n * L;
+  dim3 g((unsigned)(((long long)n * L + 255) / 256), batch);
+  k_gather_rows<T><<<g, 256, 0, st>>>(V, strideV, f.perm, n, L, X);
+  QBG_LAUNCH_CHECK("k_gather_rows");
+  const long long sInv = (long long)f.nblk * nb * nb;
+  for (int blk = 0; blk < f.nblk; ++blk) {
+    const int r0 = blk * nb, w = min(nb, n - r0);
+    int s = gemm_batched<T>(w, L, w, cx<T>(1, 0), f.Linv + (long long)blk * nb * nb, nb, sInv, X + r0, n, sX,
+                            cx<T>(0, 0), X + r0, n, sX, batch, st);
+    if (s) return s;
+    const int rest = n - r0 - w;
+    if (rest > 0) {
+      s = gemm_batched<T>(rest, L, w, cx<T>(-1, 0), f.A + (r0 + w) + (long long)r0 * n, n, f.stride, X + r0, n,
+                          sX, cx<T>(1, 0), X + r0 + w, n, sX, batch, st);
+      if (s) return s;
+    }
+  }
+  for (int blk = f.nblk - 1; blk >= 0; --blk) {
+    const int r0 = blk * nb, w = min(nb, n - r0);
+    int s = gemm_batched<T>(w, L, w, cx<T>(1, 0), f.Uinv + (long long)blk * nb * nb, nb, sInv, X + r0, n, sX,
+                            cx<T>(0, 0), X + r0, n, sX, batch, st);
+    if (s) return s;
+    if (r0 > 0) {
+      s = gemm_batched<T>(r0, L, w, cx<T>(-1, 0), f.A + (long long)r0 * n, n, f.stride, X + r0, n, sX,
+                          cx<T>(1, 0), X, n, sX, batch, st);
+      if (s) return s;
+    }
+  }
+  return QBG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// contour moments, one thread per (i, l), loop over contour nodes
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_moments(const cx<T>* X, long long sX, int batch, long long count, const cxd* w, const cxd* z,
+                          cxd* A0, cxd* A1, int accumulate) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= count) return;
+  cxd a0(0, 0), a1(0, 0);
+  if (accumulate) { a0 = A0[e]; a1 = A1[e]; }
+  for (int b = 0; b < batch; ++b) {
+    const cxd x(X[(long long)b * sX + e]);
+    const cxd wx = w[b] * x;
+    a0 += wx;
+    a1 += z[b] * wx;
+  }
+  A0[e] = a0;
+  A1[e] = a1;
+}
+
+template <class T>
+int moments(const cx<T>* X, long long sX, int batch, int n, int L, const cxd* w, const cxd* z, cxd* A0, cxd* A1,
+            int accumulate, cudaStream_t st) {
+  const long long count = (long long)n * L;
+  k_moments<T><<<(unsigned)((count + 255) / 256), 256, 0, st>>>(X, sX, batch, count, w, z, A0, A1, accumulate);
+  QBG_LAUNCH_CHECK("k_moments");
+  return QBG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// refinement residual R = V - T X with compensated FP32 arithmetic.
+// Each real product a*(xh + xl) is split exactly (p + e via FMA); the hi
+// parts are accumulated with Knuth's TwoSum, the error terms in a second FP32
+// word, and the (hi, lo) pair is flushed into an FP64 accumulator after every
+// 32-term K tile so the low word never grows.
+// tile: 64 rows x 32 columns, K step 32; 256 threads, 4 x 2 outputs each.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void df_acc(float& sh, float& sl, float a, float bh, float bl) {
+  const float p = a * bh;
+  float e = fmaf(a, bh, -p);
+  e = fmaf(a, bl, e);
+  const float s = sh + p;
+  const float v = s - sh;
+  const float err = (sh - (s - v)) + (p - v);
+  sh = s;
+  sl += err + e;
+}
+
+__global__ void __launch_bounds__(256) k_residual_df32(const cxf* __restrict__ Tm, long long sT,
+                                                       const cxd* __restrict__ X, long long sX,
+                                                       const cxd* __restrict__ V, cxd* R, long long sR, int n,
+                                                       int L, unsigned long long* rmax) {
+  constexpr int BM = 64, BN = 32, BK = 32;
+  __shared__ cxf Ts[BK][BM];
+  __shared__ float4 Xs[BK][BN + 1];  // (re_hi, re_lo, im_hi, im_lo)
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;  // rows tx + 16a (a<4), cols ty + 16b (b<2)
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  const long long bz = blockIdx.z;
+  const cxf* Tb = Tm + bz * sT;
+  const cxd* Xb = X + bz * sX;
+  double accr[4][2], acci[4][2];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 2; ++b) { accr[a][b] = 0.0; acci[a][b] = 0.0; }
+  for (int k0 = 0; k0 < n; k0 += BK) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int idx = tid + q * 256;
+      const int i = idx & (BM - 1), kk = idx >> 6;
+      const int gi = m0 + i, gk = k0 + kk;
+      Ts[kk][i] = (gi < n && gk < n) ? Tb[(long long)gi + (long long)gk * n] : cxf(0.f, 0.f);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int idx = tid + q * 256;
+      const int kk = idx & (BK - 1), jj = idx >> 5;
+      const int gk = k0 + kk, gj = n0 + jj;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gk < n && gj < L) {
+        const cxd x = Xb[(long long)gk + (long long)gj * n];
+        const float rh = (float)x.re, ih = (float)x.im;
+        v = make_float4(rh, (float)(x.re - (double)rh), ih, (float)(x.im - (double)ih));
+      }
+      Xs[kk][jj] = v;
+    }
+    __syncthreads();
+    float hr[4][2], lr[4][2], hi_[4][2], li[4][2];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 2; ++b) { hr[a][b] = 0.f; lr[a][b] = 0.f; hi_[a][b] = 0.f; li[a][b] = 0.f; }
+#pragma unroll 4
+    for (int kk = 0; kk < BK; ++kk) {
+      cxf t[4];
+      float4 x[2];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) t[a] = Ts[kk][tx + 16 * a];
+#pragma unroll
+      for (int b = 0; b < 2; ++b) x[b] = Xs[kk][ty + 16 * b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+          // re += t.re*x.re - t.im*x.im ; im += t.re*x.im + t.im*x.re
+          df_acc(hr[a][b], lr[a][b], t[a].re, x[b].x, x[b].y);
+          df_acc(hr[a][b], lr[a][b], -t[a].im, x[b].z, x[b].w);
+          df_acc(hi_[a][b], li[a][b], t[a].re, x[b].z, x[b].w);
+          df_acc(hi_[a][b], li[a][b], t[a].im, x[b].x, x[b].y);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 2; ++b) {
+        accr[a][b] += (double)hr[a][b] + (double)lr[a][b];
+        acci[a][b] += (double)hi_[a][b] + (double)li[a][b];
+      }
+    __syncthreads();
+  }
+  double lmax = 0.0;
+#pragma unroll
+  for (int b = 0; b < 2; ++b) {
+    const int gj = n0 + ty + 16 * b;
+    if (gj >= L) continue;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int gi = m0 + tx + 16 * a;
+      if (gi >= n) continue;
+      const cxd v = V[(long long)gi + (long long)gj * n];
+      const cxd r(v.re - accr[a][b], v.im - acci[a][b]);
+      R[bz * sR + (long long)gi + (long long)gj * n] = r;
+      lmax = fmax(lmax, fabs(r.re) + fabs(r.im));
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_down_sync(0xffffffffu, lmax, o));
+  if ((tid & 31) == 0 && rmax) atomicMax(rmax, (unsigned long long)__double_as_longlong(lmax));
+}
+
+int residual_df32(const cxf* Tm, long long sT, const cxd* X, long long sX, const cxd* V, cxd* R, long long sR,
+                  int n, int L, int batch, double* rmax, cudaStream_t st) {
+  dim3 grd((n + 63) / 64, (L + 31) / 32, batch);
+  k_residual_df32<<<grd, 256, 0, st>>>(Tm, sT, X, sX, V, R, sR, n, L, reinterpret_cast<unsigned long long*>(rmax));
+  QBG_LAUNCH_CHECK("k_residual_df32");
+  return QBG_OK;
+}
+
+__global__ void k_d2f(const cxd* in, cxf* out, long long count) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < count) out[e] = cxf(in[e]);
+}
+__global__ void k_axpy_f2d(const cxf* d, cxd* x, long long count) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < count) {
+    x[e].re += (double)d[e].re;
+    x[e].im += (double)d[e].im;
+  }
+}
+int convert_d2f(const cxd* in, cxf* out, long long count, cudaStream_t st) {
+  k_d2f<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(in, out, count);
+  QBG_LAUNCH_CHECK("k_d2f");
+  return QBG_OK;
+}
+int axpy_f2d(const cxf* d, cxd* x, long long count, cudaStream_t st) {
+  k_axpy_f2d<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(d, x, count);
+  QBG_LAUNCH_CHECK("k_axpy_f2d");
+  return QBG_OK;
+}
+
+template int lu_factor<double>(LUBatch<double>&, cudaStream_t);
+template int lu_factor<float>(LUBatch<float>&, cudaStream_t);
+template int lu_solve_shared<double>(const LUBatch<double>&, const cxd*, int, cxd*, long long, cudaStream_t);
+template int lu_solve_shared<float>(const LUBatch<float>&, const cxf*, int, cxf*, long long, cudaStream_t);
+template int gemm_batched<double>(int, int, int, cxd, const cxd*, long long, long long, const cxd*, long long,
+                                  long long, cxd, cxd*, long long, long long, int, cudaStream_t);
+template int gemm_batched<float>(int, int, int, cxf, const cxf*, long long, long long, const cxf*, long long,
+                                 long long, cxf, cxf*, long long, long long, int, cudaStream_t);
+template int moments<double>(const cxd*, long long, int, int, int, const cxd*, const cxd*, cxd*, cxd*, int,
+                             cudaStream_t);
+template int moments<float>(const cxf*, long long, int, int, int, const cxd*, const cxd*, cxd*, cxd*, int,
+                            cudaStream_t);
+
+}  // namespace qbg

@@ -1,0 +1,19 @@
+"""qbgpu — GB300-native boundary-integral hot path of QuantumBilliards.jl.
+
+Host-side mirror of the reference's operator API for the path (geometry,
+workspaces, assembly, Beyn contour step, sigma_min sweep) over the C ABI of
+libqbgpu.so. Import fails if the library has not been built.
+"""
+from . import _lib
+from .geometry import (BoundaryPointsCFIE, make_circle, make_star, make_full_stadium, make_circle_with_hole,
+                       s_mid)
+from .solvers import (DLP_kress, DLP_kress_global_corners, CFIE_kress, CFIE_kress_global_corners,
+                      evaluate_points, points_with_n)
+from .operators import (Workspace, build_workspace, assemble, construct_matrices, construct_boundary_matrices,
+                        construct_boundary_matrices_with_derivatives, bessel01, sigma_min)
+from .beyn import BeynHandle, construct_B_matrix, solve_vect, solve, probe_matrix, contour
+from .sweep import k_sweep, get_eigenvalues
+
+_lib.load()
+
+__all__ = [n for n in dir() if not n.startswith("_")]

@@ -1,0 +1,112 @@
+"""ctypes binding of libqbgpu (the C ABI declared in include/qbgpu.h).
+
+This is the Python counterpart of the Julia ``ccall`` shim: plain pointers and
+sizes, no torch types. The product has no CPU fallback: if the shared library
+is missing or cannot be loaded, importing this module raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = Path(os.environ.get("QBGPU_LIB", _HERE / "libqbgpu.so"))
+
+QBG_OK, QBG_EINVAL, QBG_ENOMEM, QBG_EBUDGET, QBG_ESINGULAR, QBG_ETIMEOUT, QBG_ECUDA, QBG_ENOTSUP = range(8)
+QBG_FORM_DLP, QBG_FORM_CFIE = 0, 1
+QBG_PREC_FP64, QBG_PREC_MIXED = 0, 1
+QBG_PTR_DEVICE = 1
+
+STATUS_NAMES = {0: "QBG_OK", 1: "QBG_EINVAL", 2: "QBG_ENOMEM", 3: "QBG_EBUDGET", 4: "QBG_ESINGULAR",
+                5: "QBG_ETIMEOUT", 6: "QBG_ECUDA", 7: "QBG_ENOTSUP"}
+
+
+class QBGError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"qbgpu: {STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class GeomDesc(C.Structure):
+    _fields_ = [("form", C.c_int32), ("ncomp", C.c_int32), ("comp_offsets", C.POINTER(C.c_int64)),
+                ("x", C.POINTER(C.c_double)), ("y", C.POINTER(C.c_double)),
+                ("dx", C.POINTER(C.c_double)), ("dy", C.POINTER(C.c_double)),
+                ("ddx", C.POINTER(C.c_double)), ("ddy", C.POINTER(C.c_double)),
+                ("ts", C.POINTER(C.c_double)), ("ws", C.POINTER(C.c_double)),
+                ("m", C.c_int64), ("norb", C.c_int32), ("fund", C.POINTER(C.c_int64)),
+                ("orbit", C.POINTER(C.c_int64)), ("orbit_scale", C.POINTER(C.c_double))]
+
+
+class BeynOpts(C.Structure):
+    _fields_ = [("flags", C.c_int32), ("max_refine", C.c_int32), ("refine_tol", C.c_double), ("nb", C.c_int32)]
+
+
+class BeynStats(C.Structure):
+    _fields_ = [("refine_sweeps", C.c_int32), ("refine_residual", C.c_double), ("singular", C.c_int32),
+                ("ms_assemble", C.c_double), ("ms_factor", C.c_double), ("ms_solve", C.c_double)]
+
+
+# symbol -> (restype, argtypes); the list is the ABI surface the tests check
+_SIGS = {
+    "qbg_version": (C.c_int32, [C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "qbg_last_error": (C.c_size_t, [C.c_char_p, C.c_size_t]),
+    "qbg_device_sync": (C.c_int32, []),
+    "qbg_geom_create": (C.c_int32, [C.POINTER(GeomDesc), C.POINTER(C.c_void_p)]),
+    "qbg_geom_destroy": (C.c_int32, [C.c_void_p]),
+    "qbg_geom_dim": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "qbg_assemble": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.c_int32, C.c_int32, C.c_int32,
+                                 C.POINTER(C.c_void_p)]),
+    "qbg_beyn_create": (C.c_int32, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
+                                    C.POINTER(BeynOpts), C.POINTER(C.c_void_p)]),
+    "qbg_beyn_moments": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                     C.POINTER(BeynStats)]),
+    "qbg_beyn_destroy": (C.c_int32, [C.c_void_p]),
+    "qbg_sigma_min": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]),
+    "qbg_bessel01": (C.c_int32, [C.POINTER(C.c_double), C.c_int64, C.c_int32, C.POINTER(C.c_double)]),
+}
+
+_lib = None
+
+
+def load(path: Path | None = None):
+    """Load (once) and return the shared library; raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise ImportError(f"libqbgpu.so not found at {p}; build it with __graft_entry__.build()")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in _SIGS.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return list(_SIGS)
+
+
+def last_error() -> str:
+    lib = load()
+    buf = C.create_string_buffer(2048)
+    lib.qbg_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(status: int):
+    if status != QBG_OK:
+        raise QBGError(status, last_error())
+
+
+def dptr(a: np.ndarray, ctype=C.c_double):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def vptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data)

@@ -1,0 +1,138 @@
+"""Beyn contour method, host side (mirrors beyn.jl).
+
+The N^2 and N^3 work of ``construct_B_matrix`` (beyn.jl:257-322) — assembly of
+T(z_j) at every contour node, LU of every node, T(z_j)^-1 V and the moment
+sums — runs on the GPU behind ``qbg_beyn_create`` / ``qbg_beyn_moments``.
+The host keeps what the reference keeps in FP64 on small matrices: the thin
+SVD of A0 (N x r), the absolute rank test ``count(S >= svd_tol)``, the single
+r -> 2r regrowth (beyn.jl:291-309, leaving the loop after one pass exactly as
+the reference's ``;break`` does at :307), B = U_k^H A1 W_k Sigma_k^-1 and
+``eigen(B)`` (beyn.jl:371).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+from .operators import Workspace
+
+
+def probe_matrix(N: int, r: int, rng: np.random.Generator) -> np.ndarray:
+    """Complex Gaussian probes, Re and Im ~ N(0, 1/2) (E|v|^2 = 1) like Julia's
+    randn(ComplexF64) (beyn.jl:193); the stream is NumPy's PCG64."""
+    s = math.sqrt(0.5)
+    V = rng.standard_normal((N, r)) * s + 1j * (rng.standard_normal((N, r)) * s)
+    return np.asfortranarray(V.astype(np.complex128))
+
+
+def contour(k0: complex, R: float, nq: int):
+    th = 2 * math.pi * np.arange(nq) / nq
+    e = np.cos(th) + 1j * np.sin(th)
+    return k0 + R * e, (R / nq) * e
+
+
+class BeynHandle:
+    """Contour nodes assembled and factored on the device (owns a qbg_beyn)."""
+
+    def __init__(self, ws: Workspace, k0: complex, R: float, nq: int, mixed: bool = False, max_refine: int = 4,
+                 refine_tol: float = 1e-14, nb: int = 0):
+        lib = L.load()
+        self.ws, self.k0, self.R, self.nq, self.mixed = ws, complex(k0), float(R), int(nq), bool(mixed)
+        o = L.BeynOpts(0, int(max_refine), float(refine_tol), int(nb))
+        h = C.c_void_p()
+        L.check(lib.qbg_beyn_create(ws.handle, self.k0.real, self.k0.imag, self.R, self.nq,
+                                    L.QBG_PREC_MIXED if mixed else L.QBG_PREC_FP64, C.byref(o), C.byref(h)))
+        self._h = h
+        self.N = ws.dim
+        self.last_stats = None
+
+    def moments(self, V: np.ndarray):
+        lib = L.load()
+        V = np.asfortranarray(V, dtype=np.complex128)
+        N, r = V.shape
+        if N != self.N:
+            raise ValueError(f"V has {N} rows, the operator has {self.N}")
+        A0 = np.empty((N, r), dtype=np.complex128, order="F")
+        A1 = np.empty((N, r), dtype=np.complex128, order="F")
+        st = L.BeynStats()
+        L.check(lib.qbg_beyn_moments(self._h, L.vptr(V), r, L.vptr(A0), L.vptr(A1), C.byref(st)))
+        self.last_stats = dict(refine_sweeps=st.refine_sweeps, refine_residual=st.refine_residual,
+                               singular=st.singular, ms_assemble=st.ms_assemble, ms_factor=st.ms_factor,
+                               ms_solve=st.ms_solve)
+        return A0, A1
+
+    def close(self):
+        if getattr(self, "_h", None):
+            L.load().qbg_beyn_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=None, mixed=False, ws=None,
+                       max_refine=4, refine_tol=1e-14, return_info=False):
+    """construct_B_matrix (beyn.jl:257-322). Returns (B, Uk) [, info]."""
+    rng = rng if rng is not None else np.random.default_rng(0)
+    ws = ws if ws is not None else Workspace(solver, pts)
+    if ws.dim != N:
+        raise ValueError(f"N={N} does not match the operator dimension {ws.dim}")
+    bh = BeynHandle(ws, k0, R, nq, mixed, max_refine, refine_tol)
+    info = dict(stats=[])
+    try:
+        V = probe_matrix(N, r, rng)
+        A0, A1 = bh.moments(V)
+        info["stats"].append(bh.last_stats)
+        U, S, Wh = np.linalg.svd(A0, full_matrices=False)
+        rk = int(np.count_nonzero(S >= svd_tol))
+        rused = r
+        if rk == 0:
+            out = (np.zeros((0, 0), complex), np.zeros((N, 0), complex))
+            info.update(rk=0, r=r, S=S)
+            return (*out, info) if return_info else out
+        if rk == r:
+            r_tmp = 2 * r
+            if r_tmp < N:
+                V = probe_matrix(N, r_tmp, rng)
+                A0, A1 = bh.moments(V)
+                info["stats"].append(bh.last_stats)
+                U, S, Wh = np.linalg.svd(A0, full_matrices=False)
+                rk = int(np.count_nonzero(S >= svd_tol))
+                rused = r_tmp
+    finally:
+        bh.close()
+    Uk = U[:, :rk]
+    Wk = Wh.conj().T[:, :rk]
+    tmp = (A1 @ Wk) / S[:rk][None, :]
+    B = Uk.conj().T @ tmp
+    info.update(rk=rk, r=rused, S=S)
+    return (B, Uk, info) if return_info else (B, Uk)
+
+
+def solve_vect(solver, pts, k0, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed=False, ws=None, **kw):
+    """solve_vect (beyn.jl:364-375): eigenvalues lambda, U_k and eigenvectors Y of B."""
+    N = ws.dim if ws is not None else None
+    if N is None:
+        ws = Workspace(solver, pts)
+        N = ws.dim
+    B, Uk, info = construct_B_matrix(solver, pts, N, k0, R, nq, r, svd_tol, rng, mixed, ws, return_info=True, **kw)
+    if B.size == 0:
+        return np.zeros(0, complex), Uk, np.zeros((0, 0), complex), info
+    lam, Y = np.linalg.eig(B)
+    return lam, Uk, Y, info
+
+
+def solve(solver, pts, k0, R, **kw):
+    """Eigenvalues only (beyn.jl:388-397)."""
+    return solve_vect(solver, pts, k0, R, **kw)[0]
+
+
+def inside(lam, k0, R):
+    return np.abs(lam - k0) <= R

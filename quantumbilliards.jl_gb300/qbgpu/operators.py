@@ -1,0 +1,147 @@
+"""Device workspaces and operator assembly (host mirror of the reference API).
+
+Reference seams replaced here:
+* ``build_dlp_kress_workspace`` / ``build_cfie_kress_workspace``
+  (dlp_kress.jl:679-712, cfie_kress.jl:230-270)  -> ``Workspace``
+* ``construct_matrices!`` (dlp_kress.jl:1627-1679, cfie_kress.jl:893-929)
+* ``construct_boundary_matrices!`` and ``..._with_derivatives!``
+  (chebyshev_euclidian_helmholtz_dlp_kress.jl:1110-1144,
+  chebyshev_euclidian_helmholtz_cfie_kress.jl:1431-1573)
+
+All arithmetic runs in libqbgpu on the GPU; this module only packs the
+O(N) geometry and moves matrices.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import List, Sequence
+
+import numpy as np
+
+from . import _lib as L
+from .solvers import as_list
+
+
+def _concat(pts):
+    pts = as_list(pts)
+    offs = np.zeros(len(pts) + 1, dtype=np.int64)
+    for a, p in enumerate(pts):
+        offs[a + 1] = offs[a] + p.n
+    cat = lambda f: np.ascontiguousarray(np.concatenate([f(p) for p in pts]), dtype=np.float64)
+    arrs = dict(x=cat(lambda p: p.xy[:, 0]), y=cat(lambda p: p.xy[:, 1]),
+                dx=cat(lambda p: p.tangent[:, 0]), dy=cat(lambda p: p.tangent[:, 1]),
+                ddx=cat(lambda p: p.tangent_2[:, 0]), ddy=cat(lambda p: p.tangent_2[:, 1]),
+                ts=cat(lambda p: p.ts), ws=cat(lambda p: p.ws))
+    return offs, arrs
+
+
+class Workspace:
+    """Device-resident geometry for one discretisation (owns a qbg_geom)."""
+
+    def __init__(self, solver, pts, reduction=None):
+        lib = L.load()
+        self.solver = solver
+        self.kind = solver.kind
+        pts_l = as_list(pts)
+        if self.kind == "dlp" and len(pts_l) != 1:
+            raise ValueError("DLP_kress expects one BoundaryPointsCFIE component")
+        self._offs, self._arrs = _concat(pts_l)
+        d = L.GeomDesc()
+        d.form = L.QBG_FORM_DLP if self.kind == "dlp" else L.QBG_FORM_CFIE
+        d.ncomp = len(pts_l)
+        d.comp_offsets = L.dptr(self._offs, C.c_int64)
+        for f in ("x", "y", "dx", "dy", "ddx", "ddy", "ts", "ws"):
+            setattr(d, f, L.dptr(self._arrs[f]))
+        d.m = 0
+        self._red = None
+        if reduction is not None:
+            fund, orbit, scale = reduction
+            self._red = (np.ascontiguousarray(fund, dtype=np.int64), np.ascontiguousarray(orbit, dtype=np.int64),
+                         np.ascontiguousarray(np.asarray(scale, dtype=np.complex128).view(np.float64)))
+            d.m = len(fund)
+            d.norb = orbit.shape[1]
+            d.fund = L.dptr(self._red[0], C.c_int64)
+            d.orbit = L.dptr(self._red[1], C.c_int64)
+            d.orbit_scale = L.dptr(self._red[2])
+        h = C.c_void_p()
+        L.check(lib.qbg_geom_create(C.byref(d), C.byref(h)))
+        self._h = h
+        dim = C.c_int64()
+        L.check(lib.qbg_geom_dim(h, C.byref(dim)))
+        self.dim = int(dim.value)
+        self.n_full = int(self._offs[-1])
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            L.load().qbg_geom_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def build_workspace(solver, pts, reduction=None) -> Workspace:
+    return Workspace(solver, pts, reduction)
+
+
+def _ks_array(ks) -> np.ndarray:
+    k = np.ascontiguousarray(np.atleast_1d(np.asarray(ks, dtype=np.complex128)))
+    return k
+
+
+def assemble(ws: Workspace, ks, deriv: bool = False, mixed: bool = False) -> List[np.ndarray]:
+    """Return [A(k)...] (+ [A'(k)...], [A''(k)...]) as Fortran-ordered arrays."""
+    lib = L.load()
+    k = _ks_array(ks)
+    nk = len(k)
+    nout = 3 if deriv else 1
+    dt = np.complex64 if mixed else np.complex128
+    outs = [np.empty((ws.dim, ws.dim), dtype=dt, order="F") for _ in range(nk * nout)]
+    ptrs = (C.c_void_p * len(outs))(*[o.ctypes.data for o in outs])
+    kd = k.view(np.float64)
+    L.check(lib.qbg_assemble(ws.handle, L.dptr(kd), nk, 1 if deriv else 0,
+                             L.QBG_PREC_MIXED if mixed else L.QBG_PREC_FP64, 0, ptrs))
+    return outs
+
+
+def construct_matrices(solver, pts, ws: Workspace, k, derivs: bool = False):
+    """construct_matrices!(solver, A[, A1, A2], pts, ws, k) -> A or (A, A1, A2)."""
+    out = assemble(ws, [k], deriv=derivs)
+    return tuple(out) if derivs else out[0]
+
+
+def construct_boundary_matrices(solver, pts, zj: Sequence[complex], ws: Workspace = None, mixed=False):
+    """construct_boundary_matrices!(Tbufs, solver, pts, zj) -> list of T(z_j)."""
+    ws = ws if ws is not None else Workspace(solver, pts)
+    return assemble(ws, zj, mixed=mixed)
+
+
+def construct_boundary_matrices_with_derivatives(solver, pts, zj, ws: Workspace = None):
+    ws = ws if ws is not None else Workspace(solver, pts)
+    out = assemble(ws, zj, deriv=True)
+    nk = len(np.atleast_1d(zj))
+    return out[:nk], out[nk:2 * nk], out[2 * nk:]
+
+
+def bessel01(z, f32: bool = False) -> np.ndarray:
+    """Device J0, J1, Y0, Y1 at complex z (validation helper): shape (n, 4)."""
+    lib = L.load()
+    zz = np.ascontiguousarray(np.atleast_1d(np.asarray(z, dtype=np.complex128)))
+    out = np.empty(4 * len(zz), dtype=np.complex128)
+    L.check(lib.qbg_bessel01(L.dptr(zz.view(np.float64)), len(zz), 1 if f32 else 0, L.dptr(out.view(np.float64))))
+    return out.reshape(-1, 4)
+
+
+def sigma_min(ws: Workspace, ks) -> np.ndarray:
+    lib = L.load()
+    k = np.ascontiguousarray(np.atleast_1d(np.asarray(ks, dtype=np.float64)))
+    sig = np.empty(len(k))
+    L.check(lib.qbg_sigma_min(ws.handle, L.dptr(k), len(k), L.dptr(sig)))
+    return sig

@@ -1,0 +1,39 @@
+import os
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+PKG_DIR = ROOT / "quantumbilliards.jl_gb300"
+for p in (str(ROOT), str(PKG_DIR)):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a) and libqbgpu.so")
+
+
+def have_gpu() -> bool:
+    try:
+        import ctypes
+        rt = ctypes.CDLL("libcudart.so")
+        n = ctypes.c_int(0)
+        return rt.cudaGetDeviceCount(ctypes.byref(n)) == 0 and n.value > 0
+    except OSError:
+        pass
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.fixture(scope="session")
+def qb():
+    """The product package, with its CUDA library built (fails loudly otherwise)."""
+    from qbgpu import build as B
+    B.build()
+    import qbgpu
+    return qbgpu
