@@ -157,7 +157,7 @@ def main():
             return
         return reference_arm(args)
 
-    from qbgpu import build as B
+    import build_qbgpu as B
     B.build()
     import qbgpu as qb
     from qbgpu import _lib
@@ -195,6 +195,13 @@ def main():
     for _ in range(max(1, min(args.steps, 3))):
         _, _, dt = run_step(qb, sol, pts, None, mixed=True, with_geometry=True)
         e2e_times.append(dt)
+    # FP32 form (FP32 kernel values): reported beside, with its own accuracy
+    lam32, info32, t32 = run_step(qb, sol, pts, ws, mixed="fp32")
+    lam32, info32, t32 = run_step(qb, sol, pts, ws, mixed="fp32")
+    e32 = match(select(lam32), ref)
+    fp32_form = {"ms_per_step": t32 * 1e3, "eigenvalues_inside": int(len(e32)),
+                 "eigenvalues_le_1e-10": int(np.count_nonzero(e32 <= TOL_EIG)),
+                 "max_rel_err_vs_fp64": float(e32.max()) if len(e32) else None}
 
     t_step = float(np.mean(times))
     n_eig = float(np.mean(counts))
@@ -232,6 +239,7 @@ def main():
         "phases_ms": {"assemble": st0["ms_assemble"], "factor": st0["ms_factor"],
                       "solve_refine": sum(s["ms_solve"] for s in stats[-1])},
         "refine_sweeps": [s["refine_sweeps"] for s in stats[-1]],
+        "fp32_form": fp32_form,
         "e2e": {"value": n_eig / float(np.mean(e2e_times)), "unit": "eigenvalues/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",

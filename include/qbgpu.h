@@ -42,7 +42,17 @@ enum {
 };
 
 enum { QBG_FORM_DLP = 0, QBG_FORM_CFIE = 1 };
-enum { QBG_PREC_FP64 = 0, QBG_PREC_MIXED = 1 };
+/* Precision forms:
+ *   QBG_PREC_FP64  complex128 kernel values, FP64 LU and solves (the drop-in form).
+ *   QBG_PREC_MIXED FP64 kernel values stored as a complex64 pair (hi, lo);
+ *                  FP32 LU of hi, FP32 solves, and refinement of T X = V with
+ *                  residuals of hi + lo in compensated (double-float) FP32
+ *                  arithmetic, so the refined solution is that of the FP64 operator.
+ *   QBG_PREC_FP32  FP32 kernel values (FP64 geometry, FP64 phase reduction,
+ *                  FP64 near-diagonal band |k r| < 12), FP32 LU, refinement
+ *                  against the FP32 operator: fastest, accuracy bounded by the
+ *                  FP32 rounding of the operator. */
+enum { QBG_PREC_FP64 = 0, QBG_PREC_MIXED = 1, QBG_PREC_FP32 = 2 };
 enum { QBG_PTR_DEVICE = 1 };
 
 /* Boundary discretisation (BoundaryPointsCFIE, boundarypoints.jl:487-503),
@@ -90,7 +100,8 @@ qbg_status qbg_geom_dim(const qbg_geom* g, int64_t* dim);
  * k-derivatives) at nk wavenumbers ks (complex, interleaved).
  *   outs: nk*(1+2*deriv) pointers to dim x dim complex matrices, ordered
  *         [A(k_1..k_nk), A'(k_1..k_nk), A''(k_1..k_nk)].
- *   prec = QBG_PREC_FP64: complex128 outputs; QBG_PREC_MIXED: complex64.
+ *   prec = QBG_PREC_FP64: complex128 outputs; QBG_PREC_MIXED (FP64 values
+ *   rounded once) and QBG_PREC_FP32: complex64 outputs.
  * Replaces: construct_matrices! (dlp_kress.jl:1627-1679, cfie_kress.jl:893-929),
  *           construct_boundary_matrices! (chebyshev_euclidian_helmholtz_dlp_kress.jl:1110,
  *           ..._cfie_kress.jl:1431) and construct_boundary_matrices_with_derivatives!

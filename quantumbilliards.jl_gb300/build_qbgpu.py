@@ -13,8 +13,8 @@ import subprocess
 import sys
 from pathlib import Path
 
-PKG = Path(__file__).resolve().parent
-ROOT = PKG.parent                       # quantumbilliards.jl_gb300/
+ROOT = Path(__file__).resolve().parent   # quantumbilliards.jl_gb300/
+PKG = ROOT / "qbgpu"
 CSRC = ROOT / "csrc"
 INCLUDE = ROOT.parent / "include"
 BUILD = ROOT / "_build"

@@ -209,7 +209,7 @@ static int check_ks(const double* ks, int64_t nk) {
 
 qbg_status qbg_assemble(qbg_geom* g, const double* ks, int64_t nk, int32_t deriv, int32_t prec, int32_t flags,
                         void* const* outs) {
-  if (!g || !ks || !outs || nk < 1 || (deriv != 0 && deriv != 1) || (prec != 0 && prec != 1)) {
+  if (!g || !ks || !outs || nk < 1 || (deriv != 0 && deriv != 1) || prec < 0 || prec > 2) {
     set_error("qbg_assemble: invalid arguments");
     return QBG_EINVAL;
   }
@@ -272,7 +272,8 @@ struct qbg_beyn {
   cxd* wj = nullptr;  // device contour weights
   LUBatch<double> fd;
   LUBatch<float> ff;
-  cxf* Tcopy = nullptr;  // mixed: unfactored complex64 T(z_j) for the refinement residual
+  cxf* Tcopy = nullptr;  // complex64 forms: unfactored T(z_j) (hi word) for the refinement residual
+  cxf* Tlo = nullptr;    // mixed form: lo word, T = hi + lo to ~2^-48
   std::vector<void*> allocs;
   cudaStream_t st = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -336,8 +337,17 @@ static int beyn_create_impl(qbg_beyn* b, double k0_re, double k0_im, double R) {
     for (int j = 0; j < nq; ++j) ptrs[j] = b->ff.A + (size_t)j * b->ff.stride;
   }
   QBG_CUDA(cudaMemcpyAsync(dptrs, ptrs.data(), sizeof(void*) * nq, cudaMemcpyHostToDevice, st));
+  void** dlo = nullptr;
+  if (b->prec == QBG_PREC_MIXED) {
+    QBG_TRY(b->alloc(&b->Tlo, sizeof(cxf) * (size_t)b->ff.stride * nq));
+    QBG_TRY(b->alloc(&dlo, sizeof(void*) * nq));
+    std::vector<void*> lp(nq);
+    for (int j = 0; j < nq; ++j) lp[j] = b->Tlo + (size_t)j * b->ff.stride;
+    QBG_CUDA(cudaMemcpyAsync(dlo, lp.data(), sizeof(void*) * nq, cudaMemcpyHostToDevice, st));
+    QBG_CUDA(cudaStreamSynchronize(st));  // keep lp alive until the copy has run
+  }
   QBG_CUDA(cudaEventRecord(b->ev[0], st));
-  QBG_TRY(launch_assemble(b->g->d, b->zj, nq, 0, b->prec, dptrs, n, st));
+  QBG_TRY(launch_assemble(b->g->d, b->zj, nq, 0, b->prec, dptrs, n, st, dlo));
   QBG_CUDA(cudaEventRecord(b->ev[1], st));
   if (b->prec == 0) {
     QBG_TRY(lu_factor<double>(b->fd, st));
@@ -363,7 +373,7 @@ extern "C" {
 
 qbg_status qbg_beyn_create(qbg_geom* g, double k0_re, double k0_im, double R, int32_t nq, int32_t prec,
                            const qbg_beyn_opts* opts, qbg_beyn** out) {
-  if (!g || !out || nq < 2 || !(R > 0.0) || (prec != 0 && prec != 1) || !std::isfinite(k0_re) ||
+  if (!g || !out || nq < 2 || !(R > 0.0) || prec < 0 || prec > 2 || !std::isfinite(k0_re) ||
       !std::isfinite(k0_im) || !std::isfinite(R)) {
     set_error("qbg_beyn_create: invalid arguments");
     return QBG_EINVAL;
@@ -473,7 +483,7 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
     for (int it = 0; it < b->opts.max_refine; ++it) {
       e = cudaMemsetAsync(dmax, 0, sizeof(double), st);
       if (e != cudaSuccess) { cleanup(); return cuda_status(e, "memset"); }
-      if ((s = residual_df32(b->Tcopy, b->ff.stride, X64, (long long)nl, dV, R64, (long long)nl, n, (int)L, nq,
+      if ((s = residual_df32(b->Tcopy, b->Tlo, b->ff.stride, X64, (long long)nl, dV, R64, (long long)nl, n, (int)L, nq,
                              dmax, st))) { cleanup(); return s; }
       double rmax = 0.0;
       e = cudaMemcpyAsync(&rmax, dmax, sizeof(double), cudaMemcpyDeviceToHost, st);

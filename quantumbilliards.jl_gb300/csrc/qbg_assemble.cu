@@ -111,7 +111,7 @@ template <int FORM>
 static __device__ __forceinline__ cxd diag_fp64(const GeomDev& g, int i, cxd k) {
   const double wi = g.ws[i], ki = g.kappa[i];
   if (FORM == 0) return cxd(1.0 - wi * ki, 0.0);
-  const double inv2pi = 0.15915494309189533577, euler_over_pi = 0.18373178987508208782;
+  const double inv2pi = 0.15915494309189533577, euler_over_pi = 0.18373345259830797886;  // gamma/pi
   const double si = g.speed[i];
   const int o = g.coff[g.comp[i]];
   const double rii = g.kcol[o];
@@ -160,13 +160,44 @@ __global__ void __launch_bounds__(256) k_assemble_fp64(GeomDev g, const cxd* __r
 }
 
 // ---------------------------------------------------------------------------
-// Mixed form: FP32 kernel values with FP64 pair geometry and FP64 phase
-// reduction; entries whose argument |k r| < 12 (the near-diagonal band, where
-// the Kress log split is most delicate) are evaluated entirely in FP64 and
-// rounded once.
+// Mixed form: kernel values in FP64, written as an FP32 pair (hi, lo) with
+// hi = fl32(F) and lo = fl32(F - hi). The LU factors hi in FP32; the
+// refinement residual uses hi + lo, so the refined solves see the FP64
+// operator (to ~2^-48) although every bulk O(N^3) step runs in FP32.
 // ---------------------------------------------------------------------------
 template <int FORM>
-__global__ void __launch_bounds__(256) k_assemble_mixed(GeomDev g, const cxd* __restrict__ ks, int nk,
+__global__ void __launch_bounds__(256) k_assemble_split(GeomDev g, const cxd* __restrict__ ks, int nk,
+                                                        cxf* const* __restrict__ his, cxf* const* __restrict__ los,
+                                                        long long ld) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.n || j >= g.n) return;
+  const size_t off = (size_t)i + (size_t)j * (size_t)ld;
+  PairGeom p;
+  const bool diag = (i == j);
+  bool zero = false;
+  if (!diag) {
+    p = pair_geom(g, i, j);
+    zero = (FORM == 1 && !p.same && p.r * p.r <= 4.93038065763132e-32);
+  }
+  for (int q = 0; q < nk; ++q) {
+    cxd F(0.0, 0.0), F1, F2;
+    if (diag) F = diag_fp64<FORM>(g, i, ks[q]);
+    else if (!zero) entry_fp64<FORM, 0>(p, ks[q], ks[q].im == 0.0, &F, &F1, &F2);
+    const cxf hi(F);
+    his[q][off] = hi;
+    if (los) los[q][off] = cxf((float)(F.re - (double)hi.re), (float)(F.im - (double)hi.im));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP32 form: FP32 kernel values with FP64 pair geometry and FP64 phase
+// reduction; entries whose argument |k r| < 12 (the near-diagonal band, where
+// the Kress log split is most delicate) are evaluated entirely in FP64 and
+// rounded once. Accuracy is bounded by FP32 rounding of the operator itself.
+// ---------------------------------------------------------------------------
+template <int FORM>
+__global__ void __launch_bounds__(256) k_assemble_fp32(GeomDev g, const cxd* __restrict__ ks, int nk,
                                                         cxf* const* __restrict__ outs, long long ld) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -307,7 +338,7 @@ int launch_kress_column(double* out, int N, cudaStream_t st) {
 }
 
 int launch_assemble(const GeomDev& g, const cxd* ks, int nk, int deriv, int prec, void* const* outs_dev,
-                    long long ld, cudaStream_t st) {
+                    long long ld, cudaStream_t st, void* const* lo_outs_dev) {
   const bool reduced = (g.m != g.n);
   const int dim = reduced ? g.m : g.n;
   dim3 blk(32, 8);
@@ -324,7 +355,7 @@ int launch_assemble(const GeomDev& g, const cxd* ks, int nk, int deriv, int prec
     QBG_LAUNCH_CHECK("k_assemble_dlp_reduced_fp64");
     return QBG_OK;
   }
-  if (prec == 0) {
+  if (prec == QBG_PREC_FP64) {
     if (g.form == 0) {
       if (deriv)
         k_assemble_fp64<0, 1><<<grd, blk, 0, st>>>(g, ks, nk, (cxd* const*)outs_dev, ld);
@@ -341,14 +372,22 @@ int launch_assemble(const GeomDev& g, const cxd* ks, int nk, int deriv, int prec
     return QBG_OK;
   }
   if (deriv) {
-    set_error("mixed-precision assembly has no derivative form");
+    set_error("the complex64 forms have no derivative assembly");
     return QBG_ENOTSUP;
   }
+  if (prec == QBG_PREC_MIXED) {
+    if (g.form == 0)
+      k_assemble_split<0><<<grd, blk, 0, st>>>(g, ks, nk, (cxf* const*)outs_dev, (cxf* const*)lo_outs_dev, ld);
+    else
+      k_assemble_split<1><<<grd, blk, 0, st>>>(g, ks, nk, (cxf* const*)outs_dev, (cxf* const*)lo_outs_dev, ld);
+    QBG_LAUNCH_CHECK("k_assemble_split");
+    return QBG_OK;
+  }
   if (g.form == 0)
-    k_assemble_mixed<0><<<grd, blk, 0, st>>>(g, ks, nk, (cxf* const*)outs_dev, ld);
+    k_assemble_fp32<0><<<grd, blk, 0, st>>>(g, ks, nk, (cxf* const*)outs_dev, ld);
   else
-    k_assemble_mixed<1><<<grd, blk, 0, st>>>(g, ks, nk, (cxf* const*)outs_dev, ld);
-  QBG_LAUNCH_CHECK("k_assemble_mixed");
+    k_assemble_fp32<1><<<grd, blk, 0, st>>>(g, ks, nk, (cxf* const*)outs_dev, ld);
+  QBG_LAUNCH_CHECK("k_assemble_fp32");
   return QBG_OK;
 }
 

@@ -3,10 +3,11 @@
 #include "qbg_geom.cuh"
 
 namespace qbg {
-// prec: 0 = FP64 (complex128 outputs), 1 = mixed (complex64 outputs)
+// prec: QBG_PREC_FP64 (complex128 outputs), QBG_PREC_MIXED (FP64 values split into complex64 hi in
+// outs_dev and complex64 lo in lo_outs_dev when non-null), QBG_PREC_FP32 (FP32 values, complex64)
 // outs_dev: device array of nk*(1+2*deriv) device pointers, each an ld x dim column-major matrix
 int launch_assemble(const GeomDev& g, const cxd* ks, int nk, int deriv, int prec, void* const* outs_dev,
-                    long long ld, cudaStream_t st);
+                    long long ld, cudaStream_t st, void* const* lo_outs_dev = nullptr);
 int launch_kress_column(double* out, int N, cudaStream_t st);
 int launch_bessel_eval(const cxd* z, int n, cxd* out, int f32, cudaStream_t st);
 }  // namespace qbg

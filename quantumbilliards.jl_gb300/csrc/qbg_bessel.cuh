@@ -5,7 +5,7 @@
 // src/utils/special_functions_calls.jl:3-7. AMOS is not restated here; these
 // routines are written from the published mathematics:
 //
-//  * |z| < 16: Miller's backward recurrence for J_n(z) (Abramowitz & Stegun
+//  * |z| < 14.5: Miller's backward recurrence for J_n(z) (Abramowitz & Stegun
 //    9.1.27 recurrence run downward from n0 ~ |z| + 26), normalised with the
 //    generating-function identity exp(-/+ i z) = J0 + 2 sum_{n>=1} (-/+ i)^n J_n
 //    (sign chosen so that no cancellation occurs for Im z != 0), and the
@@ -13,7 +13,7 @@
 //        Y0 = (2/pi) [ (log(z/2)+gamma) J0 - 2 sum_{k>=1} (-1)^k J_{2k}/k ]
 //        Y1 = (2/pi) [ (log(z/2)+gamma) J1 - J0/z - J1
 //                      + sum_{m>=1} (-1)^{m+1} (2m+1)/(m(m+1)) J_{2m+1} ]
-//  * |z| >= 16: Hankel's asymptotic expansion (A&S 9.2.5-9.2.10,
+//  * |z| >= 14.5: Hankel's asymptotic expansion (A&S 9.2.5-9.2.10,
 //    DLMF 10.17.1-10.17.4), summed until the terms stop decreasing:
 //        J_nu = sqrt(2/(pi z)) (P cos w - Q sin w),
 //        Y_nu = sqrt(2/(pi z)) (P sin w + Q cos w),   w = z - nu pi/2 - pi/4,
@@ -142,7 +142,7 @@ __device__ __noinline__ Bessel01d bessel01_asym(cxd z) {
 }
 
 __device__ __forceinline__ Bessel01d bessel01(cxd z) {
-  return (hypot(z.re, z.im) < 16.0) ? bessel01_miller(z) : bessel01_asym(z);
+  return (hypot(z.re, z.im) < 14.5) ? bessel01_miller(z) : bessel01_asym(z);
 }
 
 // ---------------------------------------------------------------------------

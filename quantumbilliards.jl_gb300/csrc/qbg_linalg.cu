@@ -433,18 +433,21 @@ __device__ __forceinline__ void df_acc(float& sh, float& sl, float a, float bh, 
   sl += err + e;
 }
 
-__global__ void __launch_bounds__(256) k_residual_df32(const cxf* __restrict__ Tm, long long sT,
-                                                       const cxd* __restrict__ X, long long sX,
+template <bool LO>
+__global__ void __launch_bounds__(256) k_residual_df32(const cxf* __restrict__ Tm, const cxf* __restrict__ Tl,
+                                                       long long sT, const cxd* __restrict__ X, long long sX,
                                                        const cxd* __restrict__ V, cxd* R, long long sR, int n,
                                                        int L, unsigned long long* rmax) {
   constexpr int BM = 64, BN = 32, BK = 32;
   __shared__ cxf Ts[BK][BM];
+  __shared__ cxf Tls[LO ? BK : 1][LO ? BM : 1];
   __shared__ float4 Xs[BK][BN + 1];  // (re_hi, re_lo, im_hi, im_lo)
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;  // rows tx + 16a (a<4), cols ty + 16b (b<2)
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
   const long long bz = blockIdx.z;
   const cxf* Tb = Tm + bz * sT;
+  const cxf* Tlb = LO ? Tl + bz * sT : nullptr;
   const cxd* Xb = X + bz * sX;
   double accr[4][2], acci[4][2];
 #pragma unroll
@@ -458,6 +461,7 @@ __global__ void __launch_bounds__(256) k_residual_df32(const cxf* __restrict__ T
       const int i = idx & (BM - 1), kk = idx >> 6;
       const int gi = m0 + i, gk = k0 + kk;
       Ts[kk][i] = (gi < n && gk < n) ? Tb[(long long)gi + (long long)gk * n] : cxf(0.f, 0.f);
+      if (LO) Tls[kk][i] = (gi < n && gk < n) ? Tlb[(long long)gi + (long long)gk * n] : cxf(0.f, 0.f);
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -496,6 +500,20 @@ __global__ void __launch_bounds__(256) k_residual_df32(const cxf* __restrict__ T
           df_acc(hi_[a][b], li[a][b], t[a].re, x[b].z, x[b].w);
           df_acc(hi_[a][b], li[a][b], t[a].im, x[b].x, x[b].y);
         }
+      if (LO) {
+        // lo part of the operator (|lo| <= 2^-24 |hi|): plain FP32 products into the low words
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          const cxf tl = Tls[kk][tx + 16 * a];
+#pragma unroll
+          for (int b = 0; b < 2; ++b) {
+            lr[a][b] = fmaf(tl.re, x[b].x, lr[a][b]);
+            lr[a][b] = fmaf(-tl.im, x[b].z, lr[a][b]);
+            li[a][b] = fmaf(tl.re, x[b].z, li[a][b]);
+            li[a][b] = fmaf(tl.im, x[b].x, li[a][b]);
+          }
+        }
+      }
     }
 #pragma unroll
     for (int a = 0; a < 4; ++a)
@@ -526,10 +544,14 @@ __global__ void __launch_bounds__(256) k_residual_df32(const cxf* __restrict__ T
   if ((tid & 31) == 0 && rmax) atomicMax(rmax, (unsigned long long)__double_as_longlong(lmax));
 }
 
-int residual_df32(const cxf* Tm, long long sT, const cxd* X, long long sX, const cxd* V, cxd* R, long long sR,
-                  int n, int L, int batch, double* rmax, cudaStream_t st) {
+int residual_df32(const cxf* Tm, const cxf* Tlo, long long sT, const cxd* X, long long sX, const cxd* V, cxd* R,
+                  long long sR, int n, int L, int batch, double* rmax, cudaStream_t st) {
   dim3 grd((n + 63) / 64, (L + 31) / 32, batch);
-  k_residual_df32<<<grd, 256, 0, st>>>(Tm, sT, X, sX, V, R, sR, n, L, reinterpret_cast<unsigned long long*>(rmax));
+  auto* rm = reinterpret_cast<unsigned long long*>(rmax);
+  if (Tlo)
+    k_residual_df32<true><<<grd, 256, 0, st>>>(Tm, Tlo, sT, X, sX, V, R, sR, n, L, rm);
+  else
+    k_residual_df32<false><<<grd, 256, 0, st>>>(Tm, nullptr, sT, X, sX, V, R, sR, n, L, rm);
   QBG_LAUNCH_CHECK("k_residual_df32");
   return QBG_OK;
 }

@@ -17,8 +17,21 @@ LIB_PATH = Path(os.environ.get("QBGPU_LIB", _HERE / "libqbgpu.so"))
 
 QBG_OK, QBG_EINVAL, QBG_ENOMEM, QBG_EBUDGET, QBG_ESINGULAR, QBG_ETIMEOUT, QBG_ECUDA, QBG_ENOTSUP = range(8)
 QBG_FORM_DLP, QBG_FORM_CFIE = 0, 1
-QBG_PREC_FP64, QBG_PREC_MIXED = 0, 1
+QBG_PREC_FP64, QBG_PREC_MIXED, QBG_PREC_FP32 = 0, 1, 2
 QBG_PTR_DEVICE = 1
+
+
+def prec_code(p) -> int:
+    """'fp64' | 'mixed' | 'fp32' (or False/True for fp64/mixed) -> QBG_PREC_*."""
+    if p is None or p is False or p == "fp64":
+        return QBG_PREC_FP64
+    if p is True or p == "mixed":
+        return QBG_PREC_MIXED
+    if p == "fp32":
+        return QBG_PREC_FP32
+    if p in (0, 1, 2):
+        return int(p)
+    raise ValueError(f"unknown precision form {p!r}")
 
 STATUS_NAMES = {0: "QBG_OK", 1: "QBG_EINVAL", 2: "QBG_ENOMEM", 3: "QBG_EBUDGET", 4: "QBG_ESINGULAR",
                 5: "QBG_ETIMEOUT", 6: "QBG_ECUDA", 7: "QBG_ENOTSUP"}
@@ -69,6 +82,24 @@ _SIGS = {
 }
 
 _lib = None
+_shutting_down = False
+
+
+def _mark_shutdown():
+    global _shutting_down
+    _shutting_down = True
+
+
+import atexit as _atexit  # noqa: E402
+
+# handles are released explicitly or by the garbage collector while the
+# process is alive; after interpreter shutdown starts, the CUDA runtime may
+# already be torn down, so destructors must not call into the library.
+_atexit.register(_mark_shutdown)
+
+
+def alive() -> bool:
+    return _lib is not None and not _shutting_down
 
 
 def load(path: Path | None = None):

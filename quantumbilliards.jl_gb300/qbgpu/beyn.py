@@ -41,11 +41,12 @@ class BeynHandle:
     def __init__(self, ws: Workspace, k0: complex, R: float, nq: int, mixed: bool = False, max_refine: int = 4,
                  refine_tol: float = 1e-14, nb: int = 0):
         lib = L.load()
-        self.ws, self.k0, self.R, self.nq, self.mixed = ws, complex(k0), float(R), int(nq), bool(mixed)
+        self.ws, self.k0, self.R, self.nq = ws, complex(k0), float(R), int(nq)
+        self.prec = L.prec_code(mixed)
         o = L.BeynOpts(0, int(max_refine), float(refine_tol), int(nb))
         h = C.c_void_p()
-        L.check(lib.qbg_beyn_create(ws.handle, self.k0.real, self.k0.imag, self.R, self.nq,
-                                    L.QBG_PREC_MIXED if mixed else L.QBG_PREC_FP64, C.byref(o), C.byref(h)))
+        L.check(lib.qbg_beyn_create(ws.handle, self.k0.real, self.k0.imag, self.R, self.nq, self.prec, C.byref(o),
+                                    C.byref(h)))
         self._h = h
         self.N = ws.dim
         self.last_stats = None
@@ -66,7 +67,7 @@ class BeynHandle:
         return A0, A1
 
     def close(self):
-        if getattr(self, "_h", None):
+        if getattr(self, "_h", None) and L.alive():
             L.load().qbg_beyn_destroy(self._h)
             self._h = None
 

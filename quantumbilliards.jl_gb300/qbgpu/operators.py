@@ -76,7 +76,7 @@ class Workspace:
         return self._h
 
     def close(self):
-        if getattr(self, "_h", None):
+        if getattr(self, "_h", None) and L.alive():
             L.load().qbg_geom_destroy(self._h)
             self._h = None
 
@@ -102,12 +102,12 @@ def assemble(ws: Workspace, ks, deriv: bool = False, mixed: bool = False) -> Lis
     k = _ks_array(ks)
     nk = len(k)
     nout = 3 if deriv else 1
-    dt = np.complex64 if mixed else np.complex128
+    pc = L.prec_code(mixed)
+    dt = np.complex128 if pc == L.QBG_PREC_FP64 else np.complex64
     outs = [np.empty((ws.dim, ws.dim), dtype=dt, order="F") for _ in range(nk * nout)]
     ptrs = (C.c_void_p * len(outs))(*[o.ctypes.data for o in outs])
     kd = k.view(np.float64)
-    L.check(lib.qbg_assemble(ws.handle, L.dptr(kd), nk, 1 if deriv else 0,
-                             L.QBG_PREC_MIXED if mixed else L.QBG_PREC_FP64, 0, ptrs))
+    L.check(lib.qbg_assemble(ws.handle, L.dptr(kd), nk, 1 if deriv else 0, pc, 0, ptrs))
     return outs
 
 

@@ -33,7 +33,7 @@ def have_gpu() -> bool:
 @pytest.fixture(scope="session")
 def qb():
     """The product package, with its CUDA library built (fails loudly otherwise)."""
-    from qbgpu import build as B
+    import build_qbgpu as B
     B.build()
     import qbgpu
     return qbgpu

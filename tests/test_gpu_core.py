@@ -79,10 +79,13 @@ def test_mixed_assembly_vs_oracle(qb):
     pts = qb.evaluate_points(sol, b, 60.0)
     ws = qb.Workspace(sol, pts)
     ks = [60.0 + 0.5j, 60.3 - 0.2j]
-    got = qb.assemble(ws, ks, mixed=True)
-    for g_, k in zip(got, ks):
-        assert g_.dtype == np.complex64
-        assert _relerr(g_.astype(np.complex128), OA.cfie_matrix(pts, k)) < 2e-6
+    got = qb.assemble(ws, ks, mixed="mixed")   # FP64 values rounded once to complex64
+    got32 = qb.assemble(ws, ks, mixed="fp32")  # FP32 kernel values
+    for g_, g32, k in zip(got, got32, ks):
+        ref = OA.cfie_matrix(pts, k)
+        assert g_.dtype == np.complex64 and g32.dtype == np.complex64
+        assert _relerr(g_.astype(np.complex128), ref) < 1.2e-7
+        assert _relerr(g32.astype(np.complex128), ref) < 2e-6
 
 
 def test_sigma_min_vs_oracle_and_bessel_zero(qb):
@@ -143,3 +146,9 @@ def test_beyn_eigenvalues_plain_vs_oracle_and_mixed(qb):
     assert len(m) == len(a)
     assert np.max(np.abs(m - a) / np.abs(a)) < 1e-10
     assert infom["stats"][0]["refine_sweeps"] >= 1
+    # FP32 form: operator rounded to FP32, so the error is bounded by that rounding, not by 1e-10
+    lf, _, _, _ = qb.solve_vect(sol, pts, k0, R, nq=nq, r=r, svd_tol=1e-12, rng=np.random.default_rng(7),
+                                ws=ws, mixed="fp32")
+    f = sel(lf)
+    assert len(f) == len(a)
+    assert np.max(np.abs(f - a) / np.abs(a)) < 1e-7
