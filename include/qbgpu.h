@@ -109,6 +109,21 @@ qbg_status qbg_geom_dim(const qbg_geom* g, int64_t* dim);
 qbg_status qbg_assemble(qbg_geom* g, const double* ks, int64_t nk, int32_t deriv, int32_t prec, int32_t flags,
                         void* const* outs);
 
+/* Same assembly as qbg_assemble, for callers that cannot allocate device
+ * memory during the call (they own every device buffer, e.g. a pre-reserved
+ * arena or a loop where cudaMalloc's device synchronisation is not allowed).
+ * No counterpart in the reference: it exists only for this library's users.
+ * Outputs are device pointers (outs_dev, as in qbg_assemble with
+ * QBG_PTR_DEVICE). The wavenumbers and the output-pointer table are staged in
+ * a fixed device array of QBG_NOALLOC_MAX_K entries (20 KiB, resident on each
+ * device until exit); nk > QBG_NOALLOC_MAX_K is rejected with QBG_EINVAL.
+ * Calls share that array and are serialised inside the process; each returns
+ * after its kernel finished. The first call on a device resolves the array's
+ * address on that device: make it before any stream capture. */
+#define QBG_NOALLOC_MAX_K 512
+qbg_status qbg_assemble_noalloc(qbg_geom* g, const double* ks, int64_t nk, int32_t deriv, int32_t prec,
+                                void* const* outs_dev);
+
 /* Beyn contour step (construct_B_matrix, beyn.jl:257-322), device side:
  * create = contour nodes z_j = k0 + R e^{i theta_j}, assembly of all T(z_j),
  * batched LU; moments = T(z_j)^{-1} V for every node and the sums

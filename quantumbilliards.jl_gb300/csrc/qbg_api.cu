@@ -10,6 +10,7 @@
 #include <cusolverDn.h>
 
 #include "qbg_assemble.cuh"
+#include "qbg_handles.cuh"
 #include "qbg_linalg.cuh"
 
 namespace qbg {
@@ -27,40 +28,9 @@ int cuda_status(cudaError_t e, const char* what) {
   return (e == cudaErrorMemoryAllocation) ? QBG_ENOMEM : QBG_ECUDA;
 }
 
-template <class P>
-static int dmalloc(P** p, size_t bytes) {
-  cudaError_t e = cudaMalloc((void**)p, bytes ? bytes : 1);
-  if (e != cudaSuccess) {
-    *p = nullptr;
-    return cuda_status(e, "cudaMalloc");
-  }
-  return QBG_OK;
-}
 }  // namespace qbg
 
 using namespace qbg;
-
-struct qbg_geom {
-  GeomDev d;
-  int64_t dim = 0;
-  std::vector<void*> allocs;
-  cudaStream_t stream = nullptr;
-  std::mutex mu;
-  ~qbg_geom() {
-    for (void* p : allocs) cudaFree(p);
-    if (stream) cudaStreamDestroy(stream);
-  }
-  template <class P>
-  int upload(const P* host, size_t count, const P** dev) {
-    P* p = nullptr;
-    int s = dmalloc(&p, count * sizeof(P));
-    if (s) return s;
-    allocs.push_back(p);
-    QBG_CUDA(cudaMemcpyAsync(p, host, count * sizeof(P), cudaMemcpyHostToDevice, stream));
-    *dev = p;
-    return QBG_OK;
-  }
-};
 
 #define QBG_TRY(x)          \
   do {                      \

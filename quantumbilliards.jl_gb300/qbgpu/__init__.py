@@ -9,7 +9,9 @@ from .geometry import (BoundaryPointsCFIE, make_circle, make_star, make_full_sta
                        s_mid)
 from .solvers import (DLP_kress, DLP_kress_global_corners, CFIE_kress, CFIE_kress_global_corners,
                       evaluate_points, points_with_n)
-from .operators import (Workspace, build_workspace, assemble, construct_matrices, construct_boundary_matrices,
+from . import operators
+from .operators import (Workspace, build_workspace, assemble, assemble_noalloc, construct_matrices,
+                        construct_boundary_matrices,
                         construct_boundary_matrices_with_derivatives, bessel01, sigma_min)
 from .beyn import BeynHandle, construct_B_matrix, solve_vect, solve, probe_matrix, contour
 from .sweep import k_sweep, get_eigenvalues

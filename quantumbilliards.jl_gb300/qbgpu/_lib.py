@@ -72,6 +72,8 @@ _SIGS = {
     "qbg_geom_dim": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64)]),
     "qbg_assemble": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                  C.POINTER(C.c_void_p)]),
+    "qbg_assemble_noalloc": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.c_int32, C.c_int32,
+                                         C.POINTER(C.c_void_p)]),
     "qbg_beyn_create": (C.c_int32, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
                                     C.POINTER(BeynOpts), C.POINTER(C.c_void_p)]),
     "qbg_beyn_moments": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,

@@ -111,6 +111,20 @@ def assemble(ws: Workspace, ks, deriv: bool = False, mixed: bool = False) -> Lis
     return outs
 
 
+NOALLOC_MAX_K = 512  # QBG_NOALLOC_MAX_K in include/qbgpu.h
+
+
+def assemble_noalloc(ws: Workspace, ks, dev_ptrs, deriv: bool = False, prec="fp64"):
+    """Assembly into caller-owned device buffers without any device allocation
+    inside the call (qbg_assemble_noalloc). ``dev_ptrs`` are integer device
+    addresses, ordered as for ``assemble``; at most NOALLOC_MAX_K wavenumbers."""
+    lib = L.load()
+    k = _ks_array(ks)
+    ptrs = (C.c_void_p * len(dev_ptrs))(*[int(p) for p in dev_ptrs])
+    L.check(lib.qbg_assemble_noalloc(ws.handle, L.dptr(k.view(np.float64)), len(k), 1 if deriv else 0,
+                                     L.prec_code(prec), ptrs))
+
+
 def construct_matrices(solver, pts, ws: Workspace, k, derivs: bool = False):
     """construct_matrices!(solver, A[, A1, A2], pts, ws, k) -> A or (A, A1, A2)."""
     out = assemble(ws, [k], deriv=derivs)
