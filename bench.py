@@ -239,6 +239,9 @@ def main():
         "phases_ms": {"assemble": st0["ms_assemble"], "factor": st0["ms_factor"],
                       "solve_refine": sum(s["ms_solve"] for s in stats[-1])},
         "refine_sweeps": [s["refine_sweeps"] for s in stats[-1]],
+        "refine_history": [[float("%.3g" % v) for v in s["refine_history"]] for s in stats[-1]],
+        "plain_phases_ms": {"assemble": info64["stats"][0]["ms_assemble"], "factor": info64["stats"][0]["ms_factor"],
+                            "solve": sum(s["ms_solve"] for s in info64["stats"])},
         "fp32_form": fp32_form,
         "e2e": {"value": n_eig / float(np.mean(e2e_times)), "unit": "eigenvalues/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},

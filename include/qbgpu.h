@@ -109,6 +109,25 @@ qbg_status qbg_geom_dim(const qbg_geom* g, int64_t* dim);
 qbg_status qbg_assemble(qbg_geom* g, const double* ks, int64_t nk, int32_t deriv, int32_t prec, int32_t flags,
                         void* const* outs);
 
+/* Chebyshev-panel parameters (the reference's n_panels_h, M_h, n_panels_j,
+ * M_j keywords; zero fields take the reference defaults 15000, 5, 3000, 5). */
+typedef struct qbg_cheb_params {
+  int32_t n_panels_h;  /* uniform panels of [0.95 r_min, 1.05 r_max] for H0, H1 */
+  int32_t M_h;         /* Chebyshev degree per Hankel panel (2..16) */
+  int32_t n_panels_j;  /* uniform panels of [0, 1.05 r_max] for J0, J1 */
+  int32_t M_j;
+} qbg_cheb_params;
+
+/* Assembly with kernel values interpolated from per-k Chebyshev panels built
+ * on the device (the reference's complex-k route:
+ * construct_boundary_matrices!(...; use_chebyshev=true),
+ * chebyshev_euclidian_helmholtz_cfie_kress.jl:1431-1470,
+ * ..._dlp_kress.jl:1110-1124; tables as plan_h / plan_j,
+ * chebyshev_bessels.jl:461-528). Same outputs as qbg_assemble; prec FP64 or
+ * MIXED; deriv = 1 for DLP in FP64. */
+qbg_status qbg_assemble_cheb(qbg_geom* g, const double* ks, int64_t nk, int32_t deriv, int32_t prec, int32_t flags,
+                             const qbg_cheb_params* cheb, void* const* outs);
+
 /* Same assembly as qbg_assemble, for callers that cannot allocate device
  * memory during the call (they own every device buffer, e.g. a pre-reserved
  * arena or a loop where cudaMalloc's device synchronisation is not allowed).
@@ -136,6 +155,9 @@ typedef struct qbg_beyn_opts {
   int32_t max_refine;   /* mixed form: maximum refinement sweeps (default 4) */
   double refine_tol;    /* mixed form: stop when max|R| <= tol * max|V| (default 1e-14) */
   int32_t nb;           /* LU block size (0 = default) */
+  int32_t eval_mode;    /* 0: Chebyshev panels (the reference's default, use_chebyshev=true);
+                           1: direct evaluation of H0, H1, J0, J1 */
+  qbg_cheb_params cheb; /* panel parameters for eval_mode 0 (zeros = reference defaults) */
 } qbg_beyn_opts;
 
 typedef struct qbg_beyn_stats {
@@ -143,6 +165,8 @@ typedef struct qbg_beyn_stats {
   double refine_residual;  /* final max|R| / max|V| (mixed form) */
   int32_t singular;        /* number of contour nodes with an exactly zero pivot */
   double ms_assemble, ms_factor, ms_solve;  /* device time of the phases */
+  int32_t nhist;                           /* residuals recorded in refine_history */
+  double refine_history[8];                /* max|R|/max|V| before each correction sweep */
 } qbg_beyn_stats;
 
 qbg_status qbg_beyn_create(qbg_geom* g, double k0_re, double k0_im, double R, int32_t nq, int32_t prec,

@@ -177,8 +177,66 @@ static int check_ks(const double* ks, int64_t nk) {
   return QBG_OK;
 }
 
-qbg_status qbg_assemble(qbg_geom* g, const double* ks, int64_t nk, int32_t deriv, int32_t prec, int32_t flags,
-                        void* const* outs) {
+}  // extern "C"
+
+// Chebyshev tables for nk device wavenumbers; rmin/rmax padded by 0.95/1.05
+// exactly as build_cfie_kress_block_caches (chebyshev_euclidian_helmholtz_cfie_kress.jl:396-456).
+static int cheb_params_check(const qbg_cheb_params* prm) {
+  if (prm->n_panels_h < 1 || prm->n_panels_j < 1 || prm->M_h < 2 || prm->M_j < 2 ||
+      prm->M_h > QBG_CHEB_MAX_DEGREE || prm->M_j > QBG_CHEB_MAX_DEGREE || prm->n_panels_h > (1 << 24) ||
+      prm->n_panels_j > (1 << 24)) {
+    set_error("Chebyshev parameters out of range (panels >= 1, 2 <= degree <= %d)", QBG_CHEB_MAX_DEGREE);
+    return QBG_EINVAL;
+  }
+  return QBG_OK;
+}
+
+static qbg_cheb_params cheb_defaults(const qbg_cheb_params* prm) {
+  // the reference's defaults: n_panels_h = 15000, M_h = 5, n_panels_j = 3000, M_j = 5
+  qbg_cheb_params p{15000, 5, 3000, 5};
+  if (prm) {
+    if (prm->n_panels_h > 0) p.n_panels_h = prm->n_panels_h;
+    if (prm->M_h > 0) p.M_h = prm->M_h;
+    if (prm->n_panels_j > 0) p.n_panels_j = prm->n_panels_j;
+    if (prm->M_j > 0) p.M_j = prm->M_j;
+  }
+  return p;
+}
+
+static int make_cheb(qbg_geom* g, const cxd* dks, int nk, const qbg_cheb_params& prm, ChebTables& t,
+                     std::vector<void*>& tmp, cudaStream_t st) {
+  unsigned long long* red = nullptr;
+  QBG_TRY(dmalloc(&red, 2 * sizeof(unsigned long long)));
+  tmp.push_back(red);
+  double lo = 0, hi = 0;
+  QBG_TRY(cheb_r_range(g->d, red, &lo, &hi, st));
+  if (!(hi > 0.0) || !(lo < 1e299)) {
+    set_error("Chebyshev range: no pair distance above eps");
+    return QBG_EINVAL;
+  }
+  t.nk = nk;
+  t.nh = prm.n_panels_h; t.Mh = prm.M_h;
+  t.nj = prm.n_panels_j; t.Mj = prm.M_j;
+  t.rmin = 0.95 * lo;
+  t.rmax = 1.05 * hi;
+  t.dr_h = (t.rmax - t.rmin) / t.nh;
+  t.invdr_h = 1.0 / t.dr_h;
+  t.dr_j = t.rmax / t.nj;
+  t.invdr_j = 1.0 / t.dr_j;
+  // CFIE route: direct Hankel values below |k r| = 0.2 (chebyshev_bessels.jl:1190-1207);
+  // DLP route: panels everywhere above rmin (chebyshev_bessels.jl:1051-1073)
+  t.small_cut = (g->d.form == QBG_FORM_CFIE) ? 0.2 : 0.0;
+  QBG_TRY(dmalloc(&t.H, sizeof(cxd) * (size_t)nk * t.nh * (t.Mh + 1) * 2));
+  tmp.push_back(t.H);
+  QBG_TRY(dmalloc(&t.J, sizeof(cxd) * (size_t)nk * t.nj * (t.Mj + 1) * 2));
+  tmp.push_back(t.J);
+  return cheb_build(t, dks, st);
+}
+
+extern "C" {
+
+static int assemble_impl(qbg_geom* g, const double* ks, int64_t nk, int32_t deriv, int32_t prec, int32_t flags,
+                         const qbg_cheb_params* cheb, void* const* outs) {
   if (!g || !ks || !outs || nk < 1 || (deriv != 0 && deriv != 1) || prec < 0 || prec > 2) {
     set_error("qbg_assemble: invalid arguments");
     return QBG_EINVAL;
@@ -212,7 +270,17 @@ qbg_status qbg_assemble(qbg_geom* g, const double* ks, int64_t nk, int32_t deriv
         hp[o * c + q] = dev ? outs[o * nk + k0 + q] : (void*)(stage + (size_t)(o * c + q) * mat_bytes);
     e = cudaMemcpyAsync(dptrs, hp.data(), sizeof(void*) * c * nout, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) { cleanup(); return cuda_status(e, "qbg_assemble ptrs"); }
-    s = launch_assemble(g->d, dks + k0, (int)c, deriv, prec, dptrs, dim, st);
+    if (cheb) {
+      std::vector<void*> ctmp;
+      ChebTables t;
+      s = make_cheb(g, dks + k0, (int)c, *cheb, t, ctmp, st);
+      if (!s) s = launch_assemble_cheb(g->d, t, dks + k0, (int)c, deriv, prec, dptrs, nullptr, dim, st);
+      cudaError_t e2 = cudaStreamSynchronize(st);
+      for (void* p : ctmp) cudaFree(p);
+      if (!s && e2 != cudaSuccess) s = cuda_status(e2, "qbg_assemble_cheb");
+    } else {
+      s = launch_assemble(g->d, dks + k0, (int)c, deriv, prec, dptrs, dim, st);
+    }
     if (s) { cleanup(); return s; }
     if (!dev) {
       for (int o = 0; o < nout; ++o)
@@ -227,6 +295,18 @@ qbg_status qbg_assemble(qbg_geom* g, const double* ks, int64_t nk, int32_t deriv
   }
   cleanup();
   return QBG_OK;
+}
+
+qbg_status qbg_assemble(qbg_geom* g, const double* ks, int64_t nk, int32_t deriv, int32_t prec, int32_t flags,
+                        void* const* outs) {
+  return assemble_impl(g, ks, nk, deriv, prec, flags, nullptr, outs);
+}
+
+qbg_status qbg_assemble_cheb(qbg_geom* g, const double* ks, int64_t nk, int32_t deriv, int32_t prec, int32_t flags,
+                             const qbg_cheb_params* cheb, void* const* outs) {
+  const qbg_cheb_params p = cheb_defaults(cheb);
+  QBG_TRY(cheb_params_check(&p));
+  return assemble_impl(g, ks, nk, deriv, prec, flags, &p, outs);
 }
 
 }  // extern "C"
@@ -317,8 +397,25 @@ static int beyn_create_impl(qbg_beyn* b, double k0_re, double k0_im, double R) {
     QBG_CUDA(cudaStreamSynchronize(st));  // keep lp alive until the copy has run
   }
   QBG_CUDA(cudaEventRecord(b->ev[0], st));
-  QBG_TRY(launch_assemble(b->g->d, b->zj, nq, 0, b->prec, dptrs, n, st, dlo));
-  QBG_CUDA(cudaEventRecord(b->ev[1], st));
+  const bool use_cheb = b->opts.eval_mode == 0 && b->prec != QBG_PREC_FP32 && b->g->d.m == b->g->d.n;
+  if (use_cheb) {
+    const qbg_cheb_params cp = cheb_defaults(&b->opts.cheb);
+    QBG_TRY(cheb_params_check(&cp));
+    std::vector<void*> ctmp;
+    ChebTables t;
+    int s = make_cheb(b->g, b->zj, nq, cp, t, ctmp, st);
+    if (!s) s = launch_assemble_cheb(b->g->d, t, b->zj, nq, 0, b->prec, dptrs, dlo, n, st);
+    if (!s) {
+      QBG_CUDA(cudaEventRecord(b->ev[1], st));
+      cudaError_t e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) s = cuda_status(e, "Chebyshev assembly");
+    }
+    for (void* p : ctmp) cudaFree(p);
+    if (s) return s;
+  } else {
+    QBG_TRY(launch_assemble(b->g->d, b->zj, nq, 0, b->prec, dptrs, n, st, dlo));
+    QBG_CUDA(cudaEventRecord(b->ev[1], st));
+  }
   if (b->prec == 0) {
     QBG_TRY(lu_factor<double>(b->fd, st));
   } else {
@@ -363,6 +460,8 @@ qbg_status qbg_beyn_create(qbg_geom* g, double k0_re, double k0_im, double R, in
   b->opts.max_refine = 4;
   b->opts.refine_tol = 1e-14;
   b->opts.nb = 0;
+  b->opts.eval_mode = 0;
+  b->opts.cheb = qbg_cheb_params{0, 0, 0, 0};
   if (opts) {
     b->opts = *opts;
     if (b->opts.max_refine <= 0) b->opts.max_refine = 4;
@@ -411,6 +510,8 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
   cudaEventRecord(b->ev[0], st);
   int sweeps = 0;
   double rel = 0.0;
+  double hist[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int nhist = 0;
   if (b->prec == 0) {
     cxd* X = nullptr;
     if ((s = talloc((void**)&X, sizeof(cxd) * nl * nq))) { cleanup(); return s; }
@@ -461,6 +562,7 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
       e = cudaStreamSynchronize(st);
       if (e != cudaSuccess) { cleanup(); return cuda_status(e, "refine sync"); }
       rel = rmax / vmax;
+      if (nhist < 8) hist[nhist++] = rel;
       if (rel <= b->opts.refine_tol) break;
       ++sweeps;
       // correction solves, one right-hand block per contour node
@@ -490,6 +592,8 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
     stats->ms_assemble = b->ms_assemble;
     stats->ms_factor = b->ms_factor;
     stats->ms_solve = ms;
+    stats->nhist = nhist;
+    for (int q = 0; q < 8; ++q) stats->refine_history[q] = hist[q];
   }
   return QBG_OK;
 }

@@ -20,6 +20,8 @@
 //   CFIE cross-component (smooth kernel)              cfie_kress.jl:480-503
 //   complex k: J0/J1 evaluated separately from H0/H1 and the coefficients
 //   hoisted exactly as chebyshev_euclidian_helmholtz_cfie_kress.jl:596-611.
+#include <cstring>
+
 #include "qbg_assemble.cuh"
 #include "qbg_bessel.cuh"
 
@@ -62,16 +64,9 @@ static __device__ __forceinline__ PairGeom pair_geom(const GeomDev& g, int i, in
 // FP64 entry for one wavenumber
 // ---------------------------------------------------------------------------
 template <int FORM, int DERIV>
-static __device__ __forceinline__ void entry_fp64(const PairGeom& p, cxd k, bool realk, cxd* F, cxd* F1,
-                                                  cxd* F2) {
+static __device__ __forceinline__ void entry_vals(const PairGeom& p, cxd k, cxd h0, cxd h1, cxd j0, cxd j1, cxd* F,
+                                                  cxd* F1, cxd* F2) {
   const double inv2pi = 0.15915494309189533577;
-  cxd z = p.r * k;
-  Bessel01d b = bessel01(z);
-  if (realk) {  // reference: J = Re H for real k (dlp_kress.jl:821-822)
-    b.j0.im = 0.0;
-    b.j1.im = 0.0;
-  }
-  const cxd h0 = b.h0(), h1 = b.h1(), j0 = b.j0, j1 = b.j1;
   const cxd ik = cmul_i(k);
   const cxd aL1 = (-inv2pi) * k;
   const cxd aL2 = 0.5 * ik;
@@ -105,6 +100,18 @@ static __device__ __forceinline__ void entry_fp64(const PairGeom& p, cxd k, bool
     cxd sval = cS1 * M1 + cS2 * M2 - cS3 * M1;
     *F = -(dval + ik * sval);
   }
+}
+
+// direct evaluation: H0, H1, J0, J1 from the device Bessel routines
+template <int FORM, int DERIV>
+static __device__ __forceinline__ void entry_fp64(const PairGeom& p, cxd k, bool realk, cxd* F, cxd* F1,
+                                                  cxd* F2) {
+  Bessel01d b = bessel01(p.r * k);
+  if (realk) {  // reference: J = Re H for real k (dlp_kress.jl:821-822)
+    b.j0.im = 0.0;
+    b.j1.im = 0.0;
+  }
+  entry_vals<FORM, DERIV>(p, k, b.h0(), b.h1(), b.j0, b.j1, F, F1, F2);
 }
 
 template <int FORM>
@@ -326,6 +333,230 @@ __global__ void k_kress_column(double* out, int N) {
   double c = -(4.0 * 3.14159265358979323846 / (double)N) * s;
   if (even) c -= (4.0 * 3.14159265358979323846 / ((double)N * (double)N)) * ((m & 1) ? -1.0 : 1.0);
   out[m] = c;
+}
+
+// ---------------------------------------------------------------------------
+// Chebyshev-panel evaluation (the reference's complex-k route,
+// chebyshev_bessels.jl:316-528, 950-1241, chebyshev_core.jl:67-345):
+// for every wavenumber, H0/H1 are tabulated on np_h uniform panels of
+// [rmin, rmax] and J0/J1 on np_j uniform panels of [0, rmax]; on each panel a
+// degree-M Chebyshev-Lobatto interpolant (DCT-I of the values at
+// t_j = cos(pi j / M), c_0 halved) is evaluated by Clenshaw's recurrence at
+// t = (2 r - (a + b)) / (b - a). The tables are built on the device from the
+// direct evaluator. Hankel values at |k r| below `small_cut` (0.2 on the CFIE
+// route, chebyshev_bessels.jl:1190-1207) and at r < rmin use the direct
+// evaluator; J always uses its panels, which start at r = 0.
+// ---------------------------------------------------------------------------
+__global__ void k_pair_rminmax(GeomDev g, unsigned long long* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  double lo = 1e300, hi = 0.0;
+  if (i < g.n && j < g.n && i != j) {
+    const double r = hypot(g.x[i] - g.x[j], g.y[i] - g.y[j]);
+    if (r > 2.220446049250313e-16) { lo = r; hi = r; }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_down_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_down_sync(0xffffffffu, hi, o));
+  }
+  if (((threadIdx.y * blockDim.x + threadIdx.x) & 31) == 0) {
+    atomicMin(&out[0], (unsigned long long)__double_as_longlong(lo));  // positive doubles order as integers
+    atomicMax(&out[1], (unsigned long long)__double_as_longlong(hi));
+  }
+}
+
+__global__ void k_cheb_build(ChebTables t, const cxd* __restrict__ ks) {
+  constexpr int MMAX = QBG_CHEB_MAX_DEGREE;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int q = blockIdx.y;
+  const int tab = blockIdx.z;  // 0: (H0, H1) on [rmin, rmax]; 1: (J0, J1) on [0, rmax]
+  const int np = tab ? t.nj : t.nh;
+  const int M = tab ? t.Mj : t.Mh;
+  if (p >= np) return;
+  const double lo = tab ? 0.0 : t.rmin;
+  const double h = tab ? t.dr_j : t.dr_h;
+  const double a = fma((double)p, h, lo);
+  const double b = (p + 1 == np) ? t.rmax : fma((double)(p + 1), h, lo);
+  const cxd k = ks[q];
+  const bool realk = (k.im == 0.0);
+  cxd f0[MMAX + 1], f1[MMAX + 1];
+  for (int jn = 0; jn <= M; ++jn) {
+    const double tn = cospi((double)jn / (double)M);
+    const double r = 0.5 * ((b + a) + (b - a) * tn);
+    if (r == 0.0) {  // J0(0) = 1, J1(0) = 0 (only the J table reaches r = 0)
+      f0[jn] = cxd(1.0, 0.0);
+      f1[jn] = cxd(0.0, 0.0);
+      continue;
+    }
+    Bessel01d bz = bessel01(r * k);
+    if (tab == 0) {
+      f0[jn] = bz.h0();
+      f1[jn] = bz.h1();
+    } else {
+      if (realk) { bz.j0.im = 0.0; bz.j1.im = 0.0; }
+      f0[jn] = bz.j0;
+      f1[jn] = bz.j1;
+    }
+  }
+  cxd* out = (tab ? t.J : t.H) + (((size_t)q * np + p) * (M + 1)) * 2;
+  for (int m = 0; m <= M; ++m) {
+    const double sg = (m & 1) ? -1.0 : 1.0;
+    cxd s0 = 0.5 * f0[0] + (0.5 * sg) * f0[M];
+    cxd s1 = 0.5 * f1[0] + (0.5 * sg) * f1[M];
+    for (int jn = 1; jn < M; ++jn) {
+      const double c = cospi((double)(jn * m) / (double)M);
+      s0 += c * f0[jn];
+      s1 += c * f1[jn];
+    }
+    double sc = 2.0 / (double)M;
+    if (m == 0) sc *= 0.5;
+    out[2 * m] = sc * s0;
+    out[2 * m + 1] = sc * s1;
+  }
+}
+
+// Clenshaw for two interleaved series: c[2m], c[2m+1], m = 0..M
+static __device__ __forceinline__ void clenshaw2(const cxd* __restrict__ c, int M, double t, cxd& v0, cxd& v1) {
+  const double u = 2.0 * t;
+  cxd b1a(0.0, 0.0), b2a(0.0, 0.0), b1b(0.0, 0.0), b2b(0.0, 0.0);
+  for (int m = M; m >= 1; --m) {
+    const cxd ca = c[2 * m], cb = c[2 * m + 1];
+    cxd b0a(fma(u, b1a.re, -b2a.re) + ca.re, fma(u, b1a.im, -b2a.im) + ca.im);
+    cxd b0b(fma(u, b1b.re, -b2b.re) + cb.re, fma(u, b1b.im, -b2b.im) + cb.im);
+    b2a = b1a; b1a = b0a;
+    b2b = b1b; b1b = b0b;
+  }
+  v0 = cxd(fma(t, b1a.re, -b2a.re) + c[0].re, fma(t, b1a.im, -b2a.im) + c[0].im);
+  v1 = cxd(fma(t, b1b.re, -b2b.re) + c[1].re, fma(t, b1b.im, -b2b.im) + c[1].im);
+}
+
+static __device__ __forceinline__ void panel_of(double r, double lo, double hi, double h, double invh, int np,
+                                                int& p, double& t) {
+  int q = (int)floor((r - lo) * invh);
+  q = q < 0 ? 0 : (q >= np ? np - 1 : q);
+  const double a = fma((double)q, h, lo);
+  const double b = (q + 1 == np) ? hi : fma((double)(q + 1), h, lo);
+  p = q;
+  t = (2.0 * r - (b + a)) / (b - a);
+}
+
+// OUT: 0 = complex128, 1 = complex64 hi (+ lo when los != nullptr)
+template <int FORM, int DERIV, int OUT>
+__global__ void __launch_bounds__(256) k_assemble_cheb(GeomDev g, ChebTables t, const cxd* __restrict__ ks,
+                                                       int nk, int kchunk, void* const* __restrict__ outs,
+                                                       void* const* __restrict__ los, long long ld) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.n || j >= g.n) return;
+  const int q0 = blockIdx.z * kchunk, q1 = min(nk, q0 + kchunk);
+  const size_t off = (size_t)i + (size_t)j * (size_t)ld;
+  auto store = [&](int slot, cxd v) {
+    if (OUT == 0) {
+      reinterpret_cast<cxd*>(outs[slot])[off] = v;
+    } else {
+      const cxf hi(v);
+      reinterpret_cast<cxf*>(outs[slot])[off] = hi;
+      if (los) reinterpret_cast<cxf*>(los[slot])[off] = cxf((float)(v.re - (double)hi.re), (float)(v.im - (double)hi.im));
+    }
+  };
+  if (i == j) {
+    for (int q = q0; q < q1; ++q) {
+      store(q, diag_fp64<FORM>(g, i, ks[q]));
+      if (DERIV) { store(nk + q, cxd(0.0, 0.0)); store(2 * nk + q, cxd(0.0, 0.0)); }
+    }
+    return;
+  }
+  const PairGeom p = pair_geom(g, i, j);
+  if (FORM == 1 && !p.same && p.r * p.r <= 4.93038065763132e-32) {
+    for (int q = q0; q < q1; ++q) store(q, cxd(0.0, 0.0));
+    return;
+  }
+  int ph, pj;
+  double th, tj;
+  panel_of(p.r, t.rmin, t.rmax, t.dr_h, t.invdr_h, t.nh, ph, th);
+  panel_of(p.r, 0.0, t.rmax, t.dr_j, t.invdr_j, t.nj, pj, tj);
+  const bool below = p.r < t.rmin;
+  const bool needj = !(FORM == 1 && !p.same);
+  for (int q = q0; q < q1; ++q) {
+    const cxd k = ks[q];
+    const double az = p.r * hypot(k.re, k.im);
+    cxd h0, h1, j0(0.0, 0.0), j1(0.0, 0.0);
+    if (below || az < t.small_cut) {
+      const Bessel01d b = bessel01(p.r * k);
+      h0 = b.h0();
+      h1 = b.h1();
+    } else {
+      clenshaw2(t.H + (((size_t)q * t.nh + ph) * (t.Mh + 1)) * 2, t.Mh, th, h0, h1);
+    }
+    if (needj) clenshaw2(t.J + (((size_t)q * t.nj + pj) * (t.Mj + 1)) * 2, t.Mj, tj, j0, j1);
+    cxd F, F1, F2;
+    entry_vals<FORM, DERIV>(p, k, h0, h1, j0, j1, &F, &F1, &F2);
+    store(q, F);
+    if (DERIV) { store(nk + q, F1); store(2 * nk + q, F2); }
+  }
+}
+
+int cheb_r_range(const GeomDev& g, unsigned long long* dscratch2, double* rmin, double* rmax, cudaStream_t st) {
+  unsigned long long init[2] = {0ull, 0ull};
+  const double big = 1e300;
+  memcpy(&init[0], &big, sizeof(double));
+  QBG_CUDA(cudaMemcpyAsync(dscratch2, init, sizeof(init), cudaMemcpyHostToDevice, st));
+  dim3 blk(32, 8), grd((g.n + 31) / 32, (g.n + 7) / 8);
+  k_pair_rminmax<<<grd, blk, 0, st>>>(g, dscratch2);
+  QBG_LAUNCH_CHECK("k_pair_rminmax");
+  unsigned long long res[2];
+  QBG_CUDA(cudaMemcpyAsync(res, dscratch2, sizeof(res), cudaMemcpyDeviceToHost, st));
+  QBG_CUDA(cudaStreamSynchronize(st));
+  double lo, hi;
+  memcpy(&lo, &res[0], sizeof(double));
+  memcpy(&hi, &res[1], sizeof(double));
+  *rmin = lo;
+  *rmax = hi;
+  return QBG_OK;
+}
+
+int cheb_build(ChebTables& t, const cxd* ks, cudaStream_t st) {
+  const int npmax = t.nh > t.nj ? t.nh : t.nj;
+  dim3 grd((npmax + 127) / 128, t.nk, 2);
+  k_cheb_build<<<grd, 128, 0, st>>>(t, ks);
+  QBG_LAUNCH_CHECK("k_cheb_build");
+  return QBG_OK;
+}
+
+int launch_assemble_cheb(const GeomDev& g, const ChebTables& t, const cxd* ks, int nk, int deriv, int prec,
+                         void* const* outs_dev, void* const* lo_outs_dev, long long ld, cudaStream_t st) {
+  if (g.m != g.n) {
+    set_error("Chebyshev-panel assembly of the symmetry-reduced operator is not available; use direct evaluation");
+    return QBG_ENOTSUP;
+  }
+  if (prec == QBG_PREC_FP32) {
+    set_error("the FP32 form evaluates its kernel values directly (no Chebyshev panels)");
+    return QBG_ENOTSUP;
+  }
+  if (deriv && (g.form != 0 || prec != QBG_PREC_FP64)) {
+    set_error("Chebyshev derivative assembly is available for DLP in FP64");
+    return QBG_ENOTSUP;
+  }
+  const int kchunk = 8;
+  dim3 blk(32, 8), grd((g.n + 31) / 32, (g.n + 7) / 8, (nk + kchunk - 1) / kchunk);
+  if (prec == QBG_PREC_FP64) {
+    if (g.form == 0) {
+      if (deriv)
+        k_assemble_cheb<0, 1, 0><<<grd, blk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
+      else
+        k_assemble_cheb<0, 0, 0><<<grd, blk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
+    } else {
+      k_assemble_cheb<1, 0, 0><<<grd, blk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
+    }
+  } else {
+    if (g.form == 0)
+      k_assemble_cheb<0, 0, 1><<<grd, blk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, lo_outs_dev, ld);
+    else
+      k_assemble_cheb<1, 0, 1><<<grd, blk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, lo_outs_dev, ld);
+  }
+  QBG_LAUNCH_CHECK("k_assemble_cheb");
+  return QBG_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -9,5 +9,21 @@ namespace qbg {
 int launch_assemble(const GeomDev& g, const cxd* ks, int nk, int deriv, int prec, void* const* outs_dev,
                     long long ld, cudaStream_t st, void* const* lo_outs_dev = nullptr);
 int launch_kress_column(double* out, int N, cudaStream_t st);
+
+// Chebyshev panel tables for nk wavenumbers (layout [k][panel][m][2], the pair
+// (H0, H1) on [rmin, rmax] in H and (J0, J1) on [0, rmax] in J).
+#define QBG_CHEB_MAX_DEGREE 16
+struct ChebTables {
+  int nk = 0, nh = 0, Mh = 0, nj = 0, Mj = 0;
+  double rmin = 0, rmax = 0, dr_h = 0, invdr_h = 0, dr_j = 0, invdr_j = 0;
+  double small_cut = 0.2;  // |k r| below which Hankel values are evaluated directly
+  cxd* H = nullptr;
+  cxd* J = nullptr;
+};
+// min / max pair distance over all off-diagonal pairs (host values; dscratch2 = 2 device words)
+int cheb_r_range(const GeomDev& g, unsigned long long* dscratch2, double* rmin, double* rmax, cudaStream_t st);
+int cheb_build(ChebTables& t, const cxd* ks, cudaStream_t st);
+int launch_assemble_cheb(const GeomDev& g, const ChebTables& t, const cxd* ks, int nk, int deriv, int prec,
+                         void* const* outs_dev, void* const* lo_outs_dev, long long ld, cudaStream_t st);
 int launch_bessel_eval(const cxd* z, int n, cxd* out, int f32, cudaStream_t st);
 }  // namespace qbg

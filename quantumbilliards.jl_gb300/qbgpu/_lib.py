@@ -53,13 +53,19 @@ class GeomDesc(C.Structure):
                 ("orbit", C.POINTER(C.c_int64)), ("orbit_scale", C.POINTER(C.c_double))]
 
 
+class ChebParams(C.Structure):
+    _fields_ = [("n_panels_h", C.c_int32), ("M_h", C.c_int32), ("n_panels_j", C.c_int32), ("M_j", C.c_int32)]
+
+
 class BeynOpts(C.Structure):
-    _fields_ = [("flags", C.c_int32), ("max_refine", C.c_int32), ("refine_tol", C.c_double), ("nb", C.c_int32)]
+    _fields_ = [("flags", C.c_int32), ("max_refine", C.c_int32), ("refine_tol", C.c_double), ("nb", C.c_int32),
+                ("eval_mode", C.c_int32), ("cheb", ChebParams)]
 
 
 class BeynStats(C.Structure):
     _fields_ = [("refine_sweeps", C.c_int32), ("refine_residual", C.c_double), ("singular", C.c_int32),
-                ("ms_assemble", C.c_double), ("ms_factor", C.c_double), ("ms_solve", C.c_double)]
+                ("ms_assemble", C.c_double), ("ms_factor", C.c_double), ("ms_solve", C.c_double),
+                ("nhist", C.c_int32), ("refine_history", C.c_double * 8)]
 
 
 # symbol -> (restype, argtypes); the list is the ABI surface the tests check
@@ -72,6 +78,8 @@ _SIGS = {
     "qbg_geom_dim": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64)]),
     "qbg_assemble": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                  C.POINTER(C.c_void_p)]),
+    "qbg_assemble_cheb": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.c_int32, C.c_int32,
+                                      C.c_int32, C.POINTER(ChebParams), C.POINTER(C.c_void_p)]),
     "qbg_assemble_noalloc": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.c_int32, C.c_int32,
                                          C.POINTER(C.c_void_p)]),
     "qbg_beyn_create": (C.c_int32, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,

@@ -39,11 +39,12 @@ class BeynHandle:
     """Contour nodes assembled and factored on the device (owns a qbg_beyn)."""
 
     def __init__(self, ws: Workspace, k0: complex, R: float, nq: int, mixed: bool = False, max_refine: int = 4,
-                 refine_tol: float = 1e-14, nb: int = 0):
+                 refine_tol: float = 1e-14, nb: int = 0, use_chebyshev: bool = True, cheb=None):
         lib = L.load()
         self.ws, self.k0, self.R, self.nq = ws, complex(k0), float(R), int(nq)
         self.prec = L.prec_code(mixed)
-        o = L.BeynOpts(0, int(max_refine), float(refine_tol), int(nb))
+        cp = L.ChebParams(*(cheb if cheb else (0, 0, 0, 0)))
+        o = L.BeynOpts(0, int(max_refine), float(refine_tol), int(nb), 0 if use_chebyshev else 1, cp)
         h = C.c_void_p()
         L.check(lib.qbg_beyn_create(ws.handle, self.k0.real, self.k0.imag, self.R, self.nq, self.prec, C.byref(o),
                                     C.byref(h)))
@@ -63,7 +64,7 @@ class BeynHandle:
         L.check(lib.qbg_beyn_moments(self._h, L.vptr(V), r, L.vptr(A0), L.vptr(A1), C.byref(st)))
         self.last_stats = dict(refine_sweeps=st.refine_sweeps, refine_residual=st.refine_residual,
                                singular=st.singular, ms_assemble=st.ms_assemble, ms_factor=st.ms_factor,
-                               ms_solve=st.ms_solve)
+                               ms_solve=st.ms_solve, refine_history=list(st.refine_history[:st.nhist]))
         return A0, A1
 
     def close(self):
@@ -79,13 +80,20 @@ class BeynHandle:
 
 
 def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=None, mixed=False, ws=None,
-                       max_refine=4, refine_tol=1e-14, return_info=False):
-    """construct_B_matrix (beyn.jl:257-322). Returns (B, Uk) [, info]."""
+                       max_refine=4, refine_tol=1e-14, return_info=False, regrow="extend", use_chebyshev=True,
+                       cheb=None):
+    """construct_B_matrix (beyn.jl:257-322). Returns (B, Uk) [, info].
+
+    regrow: when the rank saturates (rk == r) the reference draws a fresh
+    N x 2r probe block and solves all 2r columns again (beyn.jl:291-309).
+    "fresh" does the same; "extend" (default) keeps the r columns already
+    solved and draws only r new ones, so the moments of the 2r block cost r
+    new solves. The eigenvalues of B do not depend on the probe block."""
     rng = rng if rng is not None else np.random.default_rng(0)
     ws = ws if ws is not None else Workspace(solver, pts)
     if ws.dim != N:
         raise ValueError(f"N={N} does not match the operator dimension {ws.dim}")
-    bh = BeynHandle(ws, k0, R, nq, mixed, max_refine, refine_tol)
+    bh = BeynHandle(ws, k0, R, nq, mixed, max_refine, refine_tol, use_chebyshev=use_chebyshev, cheb=cheb)
     info = dict(stats=[])
     try:
         V = probe_matrix(N, r, rng)
@@ -101,8 +109,14 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
         if rk == r:
             r_tmp = 2 * r
             if r_tmp < N:
-                V = probe_matrix(N, r_tmp, rng)
-                A0, A1 = bh.moments(V)
+                if regrow == "extend":
+                    Vn = probe_matrix(N, r_tmp - r, rng)
+                    A0n, A1n = bh.moments(Vn)
+                    A0 = np.asfortranarray(np.hstack([A0, A0n]))
+                    A1 = np.asfortranarray(np.hstack([A1, A1n]))
+                else:
+                    V = probe_matrix(N, r_tmp, rng)
+                    A0, A1 = bh.moments(V)
                 info["stats"].append(bh.last_stats)
                 U, S, Wh = np.linalg.svd(A0, full_matrices=False)
                 rk = int(np.count_nonzero(S >= svd_tol))

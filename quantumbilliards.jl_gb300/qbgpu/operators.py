@@ -96,8 +96,14 @@ def _ks_array(ks) -> np.ndarray:
     return k
 
 
-def assemble(ws: Workspace, ks, deriv: bool = False, mixed: bool = False) -> List[np.ndarray]:
-    """Return [A(k)...] (+ [A'(k)...], [A''(k)...]) as Fortran-ordered arrays."""
+DEFAULT_CHEB = (15000, 5, 3000, 5)  # the reference's n_panels_h, M_h, n_panels_j, M_j
+
+
+def assemble(ws: Workspace, ks, deriv: bool = False, mixed: bool = False, cheb=None) -> List[np.ndarray]:
+    """Return [A(k)...] (+ [A'(k)...], [A''(k)...]) as Fortran-ordered arrays.
+
+    cheb: None for direct evaluation of H0, H1, J0, J1; True or a tuple
+    (n_panels_h, M_h, n_panels_j, M_j) for the Chebyshev-panel route."""
     lib = L.load()
     k = _ks_array(ks)
     nk = len(k)
@@ -107,7 +113,11 @@ def assemble(ws: Workspace, ks, deriv: bool = False, mixed: bool = False) -> Lis
     outs = [np.empty((ws.dim, ws.dim), dtype=dt, order="F") for _ in range(nk * nout)]
     ptrs = (C.c_void_p * len(outs))(*[o.ctypes.data for o in outs])
     kd = k.view(np.float64)
-    L.check(lib.qbg_assemble(ws.handle, L.dptr(kd), nk, 1 if deriv else 0, pc, 0, ptrs))
+    if cheb is None or cheb is False:
+        L.check(lib.qbg_assemble(ws.handle, L.dptr(kd), nk, 1 if deriv else 0, pc, 0, ptrs))
+    else:
+        prm = L.ChebParams(*(DEFAULT_CHEB if cheb is True else cheb))
+        L.check(lib.qbg_assemble_cheb(ws.handle, L.dptr(kd), nk, 1 if deriv else 0, pc, 0, C.byref(prm), ptrs))
     return outs
 
 

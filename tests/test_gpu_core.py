@@ -114,7 +114,7 @@ def test_beyn_moments_fp64_vs_oracle(qb):
     N = ws.dim
     k0, R, nq, r = 30.0 + 0j, 0.3, 16, 12
     V = qb.probe_matrix(N, r, np.random.default_rng(5))
-    bh = qb.BeynHandle(ws, k0, R, nq)
+    bh = qb.BeynHandle(ws, k0, R, nq, use_chebyshev=False)
     A0, A1 = bh.moments(V)
     zj, wj = OB.contour(k0, R, nq)
     Ts = [OA.cfie_matrix(pts, z) for z in zj]
@@ -133,7 +133,7 @@ def test_beyn_eigenvalues_plain_vs_oracle_and_mixed(qb):
     N = ws.dim
     k0, R, nq, r = 30.0 + 0j, 0.3, 24, 16
     lam, Uk, Y, info = qb.solve_vect(sol, pts, k0, R, nq=nq, r=r, svd_tol=1e-12, rng=np.random.default_rng(7),
-                                     ws=ws)
+                                     ws=ws, use_chebyshev=False)
     lo, _, _, _ = OB.solve_beyn(lambda zj: [OA.cfie_matrix(pts, z) for z in zj], N, k0, R, nq=nq, r=r,
                                 svd_tol=1e-12, rng=np.random.default_rng(7))
     sel = lambda l: np.sort_complex(l[(np.abs(l - k0) < R) & (np.abs(l.imag) < 1e-6)])
@@ -141,7 +141,7 @@ def test_beyn_eigenvalues_plain_vs_oracle_and_mixed(qb):
     assert len(a) == len(o) and len(a) > 0
     assert np.max(np.abs(a - o) / np.abs(o)) < 1e-12
     lm, _, _, infom = qb.solve_vect(sol, pts, k0, R, nq=nq, r=r, svd_tol=1e-12, rng=np.random.default_rng(7),
-                                    ws=ws, mixed=True)
+                                    ws=ws, mixed=True, use_chebyshev=False)
     m = sel(lm)
     assert len(m) == len(a)
     assert np.max(np.abs(m - a) / np.abs(a)) < 1e-10

@@ -120,3 +120,18 @@ def test_oracle_beyn_circle():
     exd = sorted(ex + [x for m in range(1, 30) for x in sp.jn_zeros(m, 10) if abs(x - k0) < R - 0.02])
     assert len(got) == len(exd)
     assert np.max(np.abs(np.array(got) - np.array(exd))) < 1e-9
+
+
+def test_oracle_chebyshev_route_matches_direct():
+    """The panel route (reference defaults) reproduces the direct operator to ~1e-12."""
+    from oracle import chebyshev as OC
+    b = G.make_star()
+    pts = S.evaluate_points(S.CFIE_kress(8.0, b), b, 40.0)
+    k = 40.0 + 0.3j
+    A_d = OA.cfie_matrix(pts, k)
+    A_c = OC.cfie_matrix(pts, k)
+    assert np.max(np.abs(A_c - A_d)) < 1e-11
+    p = S.evaluate_points(S.DLP_kress(8.0, b), b, 40.0)
+    F_d = OA.dlp_fredholm(p, k)
+    F_c = OC.dlp_fredholm(p, k)
+    assert np.max(np.abs(F_c - F_d)) < 1e-11
