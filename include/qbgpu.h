@@ -153,7 +153,9 @@ qbg_status qbg_assemble_noalloc(qbg_geom* g, const double* ks, int64_t nk, int32
 typedef struct qbg_beyn_opts {
   int32_t flags;        /* QBG_PTR_DEVICE: V, A0, A1 are device pointers */
   int32_t max_refine;   /* mixed form: maximum refinement sweeps (default 4) */
-  double refine_tol;    /* mixed form: stop when max|R| <= tol * max|V| (default 1e-14) */
+  double refine_tol;    /* complex64 forms: the first correction uses an FP32 residual; later residuals
+                           are compensated; once max|R| <= tol * max|V| the correction from that
+                           residual is applied and refinement stops (default 1e-7) */
   int32_t nb;           /* LU block size (0 = default) */
   int32_t eval_mode;    /* 0: Chebyshev panels (the reference's default, use_chebyshev=true);
                            1: direct evaluation of H0, H1, J0, J1 */

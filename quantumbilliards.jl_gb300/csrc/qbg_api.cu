@@ -458,14 +458,14 @@ qbg_status qbg_beyn_create(qbg_geom* g, double k0_re, double k0_im, double R, in
   b->prec = prec;
   b->opts.flags = 0;
   b->opts.max_refine = 4;
-  b->opts.refine_tol = 1e-14;
+  b->opts.refine_tol = 1e-7;
   b->opts.nb = 0;
   b->opts.eval_mode = 0;
   b->opts.cheb = qbg_cheb_params{0, 0, 0, 0};
   if (opts) {
     b->opts = *opts;
     if (b->opts.max_refine <= 0) b->opts.max_refine = 4;
-    if (!(b->opts.refine_tol > 0.0)) b->opts.refine_tol = 1e-14;
+    if (!(b->opts.refine_tol > 0.0)) b->opts.refine_tol = 1e-7;
   }
   std::lock_guard<std::mutex> lk(g->mu);
   b->st = g->stream;
@@ -551,6 +551,16 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
       }
     }
     if (!(vmax > 0.0)) vmax = 1.0;
+    // First correction from a plain FP32 residual V - hi X0: the residual of the
+    // FP32 solve is O(1e-2) of |V|, far above the FP32 rounding of the GEMM, so
+    // compensated arithmetic buys nothing yet. Later residuals (and the
+    // convergence test) use the compensated kernel with hi + lo.
+    if ((s = broadcast_f(V32, (long long)nl, nq, R32, st)) ||
+        (s = gemm_batched<float>(n, (int)L, n, cxf(-1.f, 0.f), b->Tcopy, n, b->ff.stride, X32, n, (long long)nl,
+                                 cxf(1.f, 0.f), R32, n, (long long)nl, nq, st)) ||
+        (s = lu_solve_shared<float>(b->ff, R32, (int)L, X32, (long long)nl, st)) ||
+        (s = axpy_f2d(X32, X64, (long long)(nl * nq), st))) { cleanup(); return s; }
+    ++sweeps;
     for (int it = 0; it < b->opts.max_refine; ++it) {
       e = cudaMemsetAsync(dmax, 0, sizeof(double), st);
       if (e != cudaSuccess) { cleanup(); return cuda_status(e, "memset"); }
@@ -563,12 +573,14 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
       if (e != cudaSuccess) { cleanup(); return cuda_status(e, "refine sync"); }
       rel = rmax / vmax;
       if (nhist < 8) hist[nhist++] = rel;
-      if (rel <= b->opts.refine_tol) break;
       ++sweeps;
-      // correction solves, one right-hand block per contour node
+      // correction solves, one right-hand block per contour node; when the
+      // residual already meets the tolerance this is the final correction
+      // (the residual is in hand, the solve costs one FP32 pass)
       if ((s = convert_d2f(R64, R32, (long long)(nl * nq), st)) ||
           (s = lu_solve_shared<float>(b->ff, R32, (int)L, X32, (long long)nl, st)) ||
           (s = axpy_f2d(X32, X64, (long long)(nl * nq), st))) { cleanup(); return s; }
+      if (rel <= b->opts.refine_tol) break;
     }
     if ((s = moments<double>(X64, (long long)nl, nq, n, (int)L, b->wj, b->zj, dA0, dA1, 0, st))) {
       cleanup(); return s;

@@ -187,6 +187,140 @@ __global__ void __launch_bounds__(512) k_getf2_panel(cx<T>* A, int n, long long 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Panel factorisation with shared-memory sub-panels (one CTA per matrix).
+// The panel [j0, jend) is factored in sub-panels of `sub` columns. A
+// sub-panel (rows s0..n-1) is loaded into shared memory, factored column by
+// column there (pivot search, swap, scale, rank-1 update all in smem; the
+// swaps are mirrored in global memory on the other panel columns), written
+// back, and the rest of the panel is updated by one rank-`sub` step
+// (U12 = inv(L11) A12 by forward substitution, A22 -= L21 U12). The L2 traffic
+// of the panel drops from ~n nb^2/2 element updates to ~n nb^2/(2 sub).
+// Dynamic smem: (n - j0) * sub * sizeof(cx<T>) (host picks sub so this fits).
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(1024) k_getrf_panel_smem(cx<T>* A, int n, long long stride, int j0, int nb,
+                                                          int sub, int* ipiv, int* info) {
+  extern __shared__ unsigned char smraw[];
+  cx<T>* S = reinterpret_cast<cx<T>*>(smraw);
+  __shared__ T wv[32];
+  __shared__ int wi[32];
+  __shared__ int s_p;
+  __shared__ cx<T> Us[8 * 64];  // U rows of the current sub-panel on the remaining panel columns
+  cx<T>* a = A + (long long)blockIdx.x * stride;
+  int* piv = ipiv + (long long)blockIdx.x * n;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int jend = min(j0 + nb, n);
+  for (int s0 = j0; s0 < jend; s0 += sub) {
+    const int w = min(sub, jend - s0);
+    const int m = n - s0;  // rows held in smem
+    for (int e = tid; e < m * w; e += nt) {
+      const int r = e % m, c = e / m;
+      S[c * m + r] = a[(s0 + r) + (long long)(s0 + c) * n];
+    }
+    __syncthreads();
+    for (int c = 0; c < w; ++c) {
+      const int cc = s0 + c;
+      T best = T(-1);
+      int bi = 0x7fffffff;
+      for (int r = c + tid; r < m; r += nt) {
+        const T v = cabs1(S[c * m + r]);
+        if (v > best) { best = v; bi = r; }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        T ov = __shfl_down_sync(0xffffffffu, best, o);
+        int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        argmax_merge(best, bi, ov, oi);
+      }
+      if ((tid & 31) == 0) { wv[tid >> 5] = best; wi[tid >> 5] = bi; }
+      __syncthreads();
+      if (tid < 32) {
+        const int nw = nt >> 5;
+        best = (tid < nw) ? wv[tid] : T(-1);
+        bi = (tid < nw) ? wi[tid] : 0x7fffffff;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          T ov = __shfl_down_sync(0xffffffffu, best, o);
+          int oi = __shfl_down_sync(0xffffffffu, bi, o);
+          argmax_merge(best, bi, ov, oi);
+        }
+        if (tid == 0) {
+          if (bi >= m) bi = c;
+          s_p = bi;
+          piv[cc] = s0 + bi;
+          if (!(best > T(0)) && info[blockIdx.x] == 0) info[blockIdx.x] = cc + 1;
+        }
+      }
+      __syncthreads();
+      const int p = s_p;  // local row
+      if (p != c) {
+        // smem sub-panel columns
+        for (int q = tid; q < w; q += nt) {
+          cx<T> t0 = S[q * m + c];
+          S[q * m + c] = S[q * m + p];
+          S[q * m + p] = t0;
+        }
+        // the other panel columns in global memory: [j0, s0) and [s0 + w, jend)
+        const int nother = (s0 - j0) + (jend - s0 - w);
+        for (int q = tid; q < nother; q += nt) {
+          const int col = (q < s0 - j0) ? (j0 + q) : (s0 + w + (q - (s0 - j0)));
+          cx<T>* pc = a + (long long)col * n;
+          cx<T> t0 = pc[cc];
+          pc[cc] = pc[s0 + p];
+          pc[s0 + p] = t0;
+        }
+      }
+      __syncthreads();
+      const cx<T> pv = S[c * m + c];
+      const bool nz = (pv.re != T(0) || pv.im != T(0));
+      const cx<T> inv = nz ? cinv(pv) : cx<T>(0, 0);
+      for (int r = c + 1 + tid; r < m; r += nt) {
+        cx<T> l = S[c * m + r];
+        if (nz) {
+          l = l * inv;
+          S[c * m + r] = l;
+        }
+        for (int q = c + 1; q < w; ++q) cfms(S[q * m + r], l, S[q * m + c]);
+      }
+      __syncthreads();
+    }
+    for (int e = tid; e < m * w; e += nt) {
+      const int r = e % m, c = e / m;
+      a[(s0 + r) + (long long)(s0 + c) * n] = S[c * m + r];
+    }
+    // rank-w update of the rest of the panel: columns [s0 + w, jend)
+    const int nr = jend - s0 - w;
+    if (nr > 0) {
+      // U12 = inv(L11) A12 : forward substitution, one thread per column
+      for (int q = tid; q < nr; q += nt) {
+        cx<T>* pc = a + (long long)(s0 + w + q) * n + s0;
+        cx<T> x[8];
+        for (int k = 0; k < w; ++k) {
+          cx<T> v = pc[k];
+          for (int l = 0; l < k; ++l) cfms(v, S[l * m + k], x[l]);
+          x[k] = v;
+          pc[k] = v;
+          Us[k * 64 + q] = v;
+        }
+      }
+      __syncthreads();
+      // A22 -= L21 U12, one thread per row
+      for (int r = w + tid; r < m; r += nt) {
+        cx<T> lr[8];
+        for (int l = 0; l < w; ++l) lr[l] = S[l * m + r];
+        cx<T>* pr = a + (s0 + r);
+        for (int q = 0; q < nr; ++q) {
+          cx<T> v = pr[(long long)(s0 + w + q) * n];
+          for (int l = 0; l < w; ++l) cfms(v, lr[l], Us[l * 64 + q]);
+          pr[(long long)(s0 + w + q) * n] = v;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // row interchanges of one panel on the columns outside the panel
 template <class T>
 __global__ void k_laswp(cx<T>* A, int n, long long stride, int j0, int nb, const int* ipiv) {
@@ -317,11 +451,28 @@ int lu_factor(LUBatch<T>& f, cudaStream_t st) {
     QBG_CUDA(cudaFuncSetAttribute(k_trtri<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
     attr_set[sizeof(T) == 8] = true;
   }
+  // shared-memory sub-panel width: the widest of 8, 4, 2, 1 columns whose n-row sub-panel fits 160 KiB
+  constexpr size_t kPanelSmem = 160 * 1024;
+  int sub = 8;
+  while (sub > 1 && (size_t)n * sub * sizeof(cx<T>) > kPanelSmem) sub >>= 1;
+  const bool smem_panel = (size_t)n * sub * sizeof(cx<T>) <= kPanelSmem;
+  static bool panel_attr[2] = {false, false};
+  if (smem_panel && !panel_attr[sizeof(T) == 8]) {
+    QBG_CUDA(cudaFuncSetAttribute(k_getrf_panel_smem<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kPanelSmem));
+    panel_attr[sizeof(T) == 8] = true;
+  }
   QBG_CUDA(cudaMemsetAsync(f.info, 0, sizeof(int) * batch, st));
   for (int j0 = 0; j0 < n; j0 += nb) {
     const int w = min(nb, n - j0);
-    k_getf2_panel<T><<<batch, 512, 0, st>>>(f.A, n, f.stride, j0, nb, f.ipiv, f.info);
-    QBG_LAUNCH_CHECK("k_getf2_panel");
+    if (smem_panel) {
+      const size_t smem = (size_t)(n - j0) * sub * sizeof(cx<T>);
+      k_getrf_panel_smem<T><<<batch, 1024, smem, st>>>(f.A, n, f.stride, j0, nb, sub, f.ipiv, f.info);
+      QBG_LAUNCH_CHECK("k_getrf_panel_smem");
+    } else {
+      k_getf2_panel<T><<<batch, 512, 0, st>>>(f.A, n, f.stride, j0, nb, f.ipiv, f.info);
+      QBG_LAUNCH_CHECK("k_getf2_panel");
+    }
     dim3 g2((n + 255) / 256, batch);
     k_laswp<T><<<g2, 256, 0, st>>>(f.A, n, f.stride, j0, nb, f.ipiv);
     QBG_LAUNCH_CHECK("k_laswp");
@@ -566,6 +717,17 @@ __global__ void k_axpy_f2d(const cxf* d, cxd* x, long long count) {
     x[e].re += (double)d[e].re;
     x[e].im += (double)d[e].im;
   }
+}
+__global__ void k_bcast_f(const cxf* in, long long count, int batch, cxf* out) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= count) return;
+  const cxf v = in[e];
+  for (int b = 0; b < batch; ++b) out[(long long)b * count + e] = v;
+}
+int broadcast_f(const cxf* in, long long count, int batch, cxf* out, cudaStream_t st) {
+  k_bcast_f<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(in, count, batch, out);
+  QBG_LAUNCH_CHECK("k_bcast_f");
+  return QBG_OK;
 }
 int convert_d2f(const cxd* in, cxf* out, long long count, cudaStream_t st) {
   k_d2f<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(in, out, count);

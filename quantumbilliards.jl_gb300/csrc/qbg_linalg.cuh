@@ -45,6 +45,7 @@ int moments(const cx<T>* X, long long sX, int batch, int n, int L, const cxd* w,
 int residual_df32(const cxf* Tm, const cxf* Tlo, long long sT, const cxd* X, long long sX, const cxd* V, cxd* R,
                   long long sR, int n, int L, int batch, double* rmax, cudaStream_t st);
 int convert_d2f(const cxd* in, cxf* out, long long count, cudaStream_t st);
+int broadcast_f(const cxf* in, long long count, int batch, cxf* out, cudaStream_t st);  // out[b] = in
 int axpy_f2d(const cxf* d, cxd* x, long long count, cudaStream_t st);  // x += d
 
 }  // namespace qbg

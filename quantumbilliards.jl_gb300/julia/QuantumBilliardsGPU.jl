@@ -33,11 +33,20 @@ struct QbgGeomDesc
     fund::Ptr{Int64}; orbit::Ptr{Int64}; orbit_scale::Ptr{Float64}
 end
 
+struct QbgChebParams
+    n_panels_h::Int32
+    M_h::Int32
+    n_panels_j::Int32
+    M_j::Int32
+end
+
 struct QbgBeynOpts
     flags::Int32
     max_refine::Int32
     refine_tol::Float64
     nb::Int32
+    eval_mode::Int32        # 0 = Chebyshev panels (use_chebyshev=true), 1 = direct
+    cheb::QbgChebParams     # zeros = the reference defaults 15000, 5, 3000, 5
 end
 
 function qbg_check(st::Int32)
@@ -122,7 +131,7 @@ function QB.construct_B_matrix(solver::GPUSolver, pts, N::Int, k0::Complex{Float
     ws = gpu_workspace(solver, pts)
     @assert ws.dim == N
     h = Ref{Ptr{Cvoid}}(C_NULL)
-    opts = QbgBeynOpts(0, 4, 1e-14, 0)
+    opts = QbgBeynOpts(0, 4, 1e-7, 0, 0, QbgChebParams(0, 0, 0, 0))
     qbg_check(ccall((:qbg_beyn_create, libqbgpu), Int32,
         (Ptr{Cvoid}, Float64, Float64, Float64, Int32, Int32, Ref{QbgBeynOpts}, Ref{Ptr{Cvoid}}),
         ws.h, real(k0), imag(k0), R, nq, solver.prec, opts, h))

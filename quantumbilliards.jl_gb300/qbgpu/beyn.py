@@ -39,7 +39,7 @@ class BeynHandle:
     """Contour nodes assembled and factored on the device (owns a qbg_beyn)."""
 
     def __init__(self, ws: Workspace, k0: complex, R: float, nq: int, mixed: bool = False, max_refine: int = 4,
-                 refine_tol: float = 1e-14, nb: int = 0, use_chebyshev: bool = True, cheb=None):
+                 refine_tol: float = 1e-7, nb: int = 0, use_chebyshev: bool = True, cheb=None):
         lib = L.load()
         self.ws, self.k0, self.R, self.nq = ws, complex(k0), float(R), int(nq)
         self.prec = L.prec_code(mixed)
@@ -80,7 +80,7 @@ class BeynHandle:
 
 
 def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=None, mixed=False, ws=None,
-                       max_refine=4, refine_tol=1e-14, return_info=False, regrow="extend", use_chebyshev=True,
+                       max_refine=4, refine_tol=1e-7, return_info=False, regrow="extend", use_chebyshev=True,
                        cheb=None):
     """construct_B_matrix (beyn.jl:257-322). Returns (B, Uk) [, info].
 
