@@ -497,6 +497,149 @@ __global__ void __launch_bounds__(256) k_assemble_cheb(GeomDev g, ChebTables t, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Symmetric-pair Chebyshev assembly (value only, no derivatives).
+// The kernel values of (i, j) and (j, i) depend on the pair only through r, so
+// one panel evaluation serves both entries. With the pair coefficients folded,
+//   F_ij = -(alpha J1 + beta H1 + gamma J0 + delta H0),
+//   alpha = (cD1 - cD3) (-k/2pi), beta = cD2 (ik/2),
+//   gamma = (cS1 - cS3) (-ik/2pi), delta = cS2 (-k/2),
+// which is dval + ik sval of entry_vals regrouped (cross-component CFIE
+// pairs keep only beta = w inner/r and delta = w s). CTA = one 32 x 32 tile
+// pair (bi <= bj); the mirrored tile is written through shared memory so both
+// stores are coalesced.
+// ---------------------------------------------------------------------------
+struct Fold {
+  double A, B, C, D;  // real pair coefficients of J1, H1, J0, H0
+};
+
+template <int FORM>
+static __device__ __forceinline__ Fold fold_of(const PairGeom& p) {
+  Fold f;
+  if (FORM == 1 && !p.same) {
+    f.A = 0.0; f.B = p.wj * p.inn * p.invr; f.C = 0.0; f.D = p.wj * p.sj;
+    return f;
+  }
+  const double cD1 = p.Rk * p.inn * p.invr, cD2 = p.wj * p.inn * p.invr, cD3 = p.wj * p.lt * p.inn * p.invr;
+  f.A = cD1 - cD3;
+  f.B = cD2;
+  if (FORM == 1) {
+    const double cS1 = p.Rk * p.sj, cS2 = p.wj * p.sj, cS3 = p.wj * p.sj * p.lt;
+    f.C = cS1 - cS3;
+    f.D = cS2;
+  } else {
+    f.C = 0.0;
+    f.D = 0.0;
+  }
+  return f;
+}
+
+static __device__ __forceinline__ cxd folded_entry(const Fold& f, cxd kaL1, cxd kaL2, cxd kg, cxd kd, cxd h0,
+                                                   cxd h1, cxd j0, cxd j1) {
+  cxd s = (f.A * kaL1) * j1;
+  cfma(s, f.B * kaL2, h1);
+  cfma(s, f.C * kg, j0);
+  cfma(s, f.D * kd, h0);
+  return -s;
+}
+
+static __device__ __forceinline__ int2 tile_pair(int t) {
+  int bj = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+  while ((bj + 1) * (bj + 2) / 2 <= t) ++bj;
+  while (bj * (bj + 1) / 2 > t) --bj;
+  return make_int2(t - bj * (bj + 1) / 2, bj);
+}
+
+template <int FORM, int OUT>
+__global__ void __launch_bounds__(512) k_assemble_cheb_sym(GeomDev g, ChebTables t, const cxd* __restrict__ ks,
+                                                           int nk, int kchunk, void* const* __restrict__ outs,
+                                                           void* const* __restrict__ los, long long ld) {
+  __shared__ cxd sm[32][33];
+  const int2 bp = tile_pair(blockIdx.x);
+  const int bi = bp.x, bj = bp.y;
+  const bool dtile = (bi == bj);
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 16
+  const int i = bi * 32 + tx;
+  const int q0 = blockIdx.z * kchunk, q1 = min(nk, q0 + kchunk);
+  auto store = [&](int slot, size_t off, cxd v) {
+    if (OUT == 0) {
+      reinterpret_cast<cxd*>(outs[slot])[off] = v;
+    } else {
+      const cxf hi(v);
+      reinterpret_cast<cxf*>(outs[slot])[off] = hi;
+      if (los) reinterpret_cast<cxf*>(los[slot])[off] = cxf((float)(v.re - (double)hi.re), (float)(v.im - (double)hi.im));
+    }
+  };
+  // pair data for the two column slots s = 0, 1 (j = bj*32 + ty + 16 s)
+  bool act[2], isdiag[2], zero[2], direct[2];
+  Fold fij[2], fji[2];
+  int ph[2], pj[2];
+  double th[2], tj[2], rr[2];
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    const int j = bj * 32 + ty + 16 * s;
+    const bool inb = (i < g.n) && (j < g.n);
+    isdiag[s] = inb && (i == j);
+    act[s] = inb && !isdiag[s] && (!dtile || i < j);
+    zero[s] = false;
+    direct[s] = false;
+    rr[s] = 0.0;
+    ph[s] = pj[s] = 0;
+    th[s] = tj[s] = 0.0;
+    if (act[s]) {
+      const PairGeom pa = pair_geom(g, i, j);
+      const PairGeom pb = pair_geom(g, j, i);
+      fij[s] = fold_of<FORM>(pa);
+      fji[s] = fold_of<FORM>(pb);
+      rr[s] = pa.r;
+      zero[s] = (FORM == 1 && !pa.same && pa.r * pa.r <= 4.93038065763132e-32);
+      panel_of(pa.r, t.rmin, t.rmax, t.dr_h, t.invdr_h, t.nh, ph[s], th[s]);
+      panel_of(pa.r, 0.0, t.rmax, t.dr_j, t.invdr_j, t.nj, pj[s], tj[s]);
+      direct[s] = pa.r < t.rmin;
+    }
+  }
+  const double inv2pi = 0.15915494309189533577;
+  for (int q = q0; q < q1; ++q) {
+    const cxd k = ks[q];
+    const double ak = hypot(k.re, k.im);
+    const cxd kaL1 = (-inv2pi) * k, kaL2 = 0.5 * cmul_i(k), kg = (-inv2pi) * cmul_i(k), kd = -0.5 * k;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const int j = bj * 32 + ty + 16 * s;
+      cxd vij(0.0, 0.0), vji(0.0, 0.0);
+      if (isdiag[s]) {
+        store(q, (size_t)i + (size_t)j * ld, diag_fp64<FORM>(g, i, k));
+      } else if (act[s]) {
+        if (!zero[s]) {
+          cxd h0, h1, j0(0.0, 0.0), j1(0.0, 0.0);
+          if (direct[s] || rr[s] * ak < t.small_cut) {
+            const Bessel01d b = bessel01(rr[s] * k);
+            h0 = b.h0();
+            h1 = b.h1();
+          } else {
+            clenshaw2(t.H + (((size_t)q * t.nh + ph[s]) * (t.Mh + 1)) * 2, t.Mh, th[s], h0, h1);
+          }
+          if (fij[s].A != 0.0 || fij[s].C != 0.0 || fji[s].A != 0.0 || fji[s].C != 0.0)
+            clenshaw2(t.J + (((size_t)q * t.nj + pj[s]) * (t.Mj + 1)) * 2, t.Mj, tj[s], j0, j1);
+          vij = folded_entry(fij[s], kaL1, kaL2, kg, kd, h0, h1, j0, j1);
+          vji = folded_entry(fji[s], kaL1, kaL2, kg, kd, h0, h1, j0, j1);
+        }
+        store(q, (size_t)i + (size_t)j * ld, vij);
+      }
+      sm[ty + 16 * s][tx] = vji;  // row = j - bj*32, column = i - bi*32
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const int jl = tx, il = ty + 16 * s;  // output (row j, column i)
+      const int j = bj * 32 + jl, ii = bi * 32 + il;
+      const bool ok = (j < g.n) && (ii < g.n) && (dtile ? (jl > il) : true);
+      if (ok) store(q, (size_t)j + (size_t)ii * ld, sm[jl][il]);
+    }
+    __syncthreads();
+  }
+}
+
 int cheb_r_range(const GeomDev& g, unsigned long long* dscratch2, double* rmin, double* rmax, cudaStream_t st) {
   unsigned long long init[2] = {0ull, 0ull};
   const double big = 1e300;
@@ -539,6 +682,23 @@ int launch_assemble_cheb(const GeomDev& g, const ChebTables& t, const cxd* ks, i
     return QBG_ENOTSUP;
   }
   const int kchunk = 8;
+  if (!deriv) {
+    const int nt = (g.n + 31) / 32;
+    dim3 sblk(32, 16), sgrd((unsigned)(nt * (nt + 1) / 2), 1, (nk + kchunk - 1) / kchunk);
+    if (prec == QBG_PREC_FP64) {
+      if (g.form == 0)
+        k_assemble_cheb_sym<0, 0><<<sgrd, sblk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
+      else
+        k_assemble_cheb_sym<1, 0><<<sgrd, sblk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
+    } else {
+      if (g.form == 0)
+        k_assemble_cheb_sym<0, 1><<<sgrd, sblk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, lo_outs_dev, ld);
+      else
+        k_assemble_cheb_sym<1, 1><<<sgrd, sblk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, lo_outs_dev, ld);
+    }
+    QBG_LAUNCH_CHECK("k_assemble_cheb_sym");
+    return QBG_OK;
+  }
   dim3 blk(32, 8), grd((g.n + 31) / 32, (g.n + 7) / 8, (nk + kchunk - 1) / kchunk);
   if (prec == QBG_PREC_FP64) {
     if (g.form == 0) {
