@@ -116,8 +116,8 @@ def run_step(qb, sol, pts, ws, mixed, rng_seed=SEED, with_geometry=False):
     t0 = time.perf_counter()
     if with_geometry:
         ws = qb.Workspace(sol, pts)
-    lam, Uk, Y, info = qb.solve_vect(sol, pts, K0 + 0j, RADIUS, nq=NQ, r=L_PROBES, svd_tol=SVD_TOL,
-                                     rng=np.random.default_rng(rng_seed), mixed=mixed, ws=ws)
+    lam, info = qb.solve(sol, pts, K0 + 0j, RADIUS, nq=NQ, r=L_PROBES, svd_tol=SVD_TOL,
+                         rng=np.random.default_rng(rng_seed), mixed=mixed, ws=ws, return_info=True)
     dt = time.perf_counter() - t0
     if with_geometry:
         ws.close()

@@ -99,8 +99,12 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
         V = probe_matrix(N, r, rng)
         A0, A1 = bh.moments(V)
         info["stats"].append(bh.last_stats)
-        U, S, Wh = np.linalg.svd(A0, full_matrices=False)
+        # the saturation test needs only the singular values; the factors are
+        # computed once, for the block that is finally used
+        S = np.linalg.svd(A0, compute_uv=False)
         rk = int(np.count_nonzero(S >= svd_tol))
+        if not (rk == r and 2 * r < N) and rk > 0:
+            U, S, Wh = np.linalg.svd(A0, full_matrices=False)
         rused = r
         if rk == 0:
             out = (np.zeros((0, 0), complex), np.zeros((N, 0), complex))
@@ -144,9 +148,15 @@ def solve_vect(solver, pts, k0, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed=F
     return lam, Uk, Y, info
 
 
-def solve(solver, pts, k0, R, **kw):
-    """Eigenvalues only (beyn.jl:388-397)."""
-    return solve_vect(solver, pts, k0, R, **kw)[0]
+def solve(solver, pts, k0, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed=False, ws=None, return_info=False,
+          **kw):
+    """Eigenvalues only (beyn.jl:388-397): eigvals(B), no eigenvectors."""
+    if ws is None:
+        ws = Workspace(solver, pts)
+    B, Uk, info = construct_B_matrix(solver, pts, ws.dim, k0, R, nq, r, svd_tol, rng, mixed, ws, return_info=True,
+                                     **kw)
+    lam = np.zeros(0, complex) if B.size == 0 else np.linalg.eigvals(B)
+    return (lam, info) if return_info else lam
 
 
 def inside(lam, k0, R):
