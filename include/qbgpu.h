@@ -169,6 +169,8 @@ typedef struct qbg_beyn_stats {
   double ms_assemble, ms_factor, ms_solve;  /* device time of the phases */
   int32_t nhist;                           /* residuals recorded in refine_history */
   double refine_history[8];                /* max|R|/max|V| before each correction sweep */
+  double ms_residual;                      /* device time of the compensated residual launches */
+  int32_t n_residual;                      /* number of compensated residual launches */
 } qbg_beyn_stats;
 
 qbg_status qbg_beyn_create(qbg_geom* g, double k0_re, double k0_im, double R, int32_t nq, int32_t prec,

@@ -326,7 +326,7 @@ struct qbg_beyn {
   cxf* Tlo = nullptr;    // mixed form: lo word, T = hi + lo to ~2^-48
   std::vector<void*> allocs;
   cudaStream_t st = nullptr;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   float ms_assemble = 0, ms_factor = 0;
   int singular = 0;
   std::mutex mu;
@@ -512,6 +512,8 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
   double rel = 0.0;
   double hist[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int nhist = 0;
+  double ms_resid = 0.0;
+  int n_resid = 0;
   if (b->prec == 0) {
     cxd* X = nullptr;
     if ((s = talloc((void**)&X, sizeof(cxd) * nl * nq))) { cleanup(); return s; }
@@ -564,13 +566,17 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
     for (int it = 0; it < b->opts.max_refine; ++it) {
       e = cudaMemsetAsync(dmax, 0, sizeof(double), st);
       if (e != cudaSuccess) { cleanup(); return cuda_status(e, "memset"); }
+      cudaEventRecord(b->ev[4], st);
       if ((s = residual_df32(b->Tcopy, b->Tlo, b->ff.stride, X64, (long long)nl, dV, R64, (long long)nl, n, (int)L, nq,
                              dmax, st))) { cleanup(); return s; }
+      cudaEventRecord(b->ev[5], st);
       double rmax = 0.0;
       e = cudaMemcpyAsync(&rmax, dmax, sizeof(double), cudaMemcpyDeviceToHost, st);
       if (e != cudaSuccess) { cleanup(); return cuda_status(e, "rmax D2H"); }
       e = cudaStreamSynchronize(st);
       if (e != cudaSuccess) { cleanup(); return cuda_status(e, "refine sync"); }
+      float ms_r = 0.f;
+      if (cudaEventElapsedTime(&ms_r, b->ev[4], b->ev[5]) == cudaSuccess) { ms_resid += ms_r; ++n_resid; }
       rel = rmax / vmax;
       if (nhist < 8) hist[nhist++] = rel;
       ++sweeps;
@@ -605,6 +611,8 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
     stats->ms_factor = b->ms_factor;
     stats->ms_solve = ms;
     stats->nhist = nhist;
+    stats->ms_residual = ms_resid;
+    stats->n_residual = n_resid;
     for (int q = 0; q < 8; ++q) stats->refine_history[q] = hist[q];
   }
   return QBG_OK;

@@ -65,7 +65,8 @@ class BeynOpts(C.Structure):
 class BeynStats(C.Structure):
     _fields_ = [("refine_sweeps", C.c_int32), ("refine_residual", C.c_double), ("singular", C.c_int32),
                 ("ms_assemble", C.c_double), ("ms_factor", C.c_double), ("ms_solve", C.c_double),
-                ("nhist", C.c_int32), ("refine_history", C.c_double * 8)]
+                ("nhist", C.c_int32), ("refine_history", C.c_double * 8), ("ms_residual", C.c_double),
+                ("n_residual", C.c_int32)]
 
 
 # symbol -> (restype, argtypes); the list is the ABI surface the tests check

@@ -64,7 +64,8 @@ class BeynHandle:
         L.check(lib.qbg_beyn_moments(self._h, L.vptr(V), r, L.vptr(A0), L.vptr(A1), C.byref(st)))
         self.last_stats = dict(refine_sweeps=st.refine_sweeps, refine_residual=st.refine_residual,
                                singular=st.singular, ms_assemble=st.ms_assemble, ms_factor=st.ms_factor,
-                               ms_solve=st.ms_solve, refine_history=list(st.refine_history[:st.nhist]))
+                               ms_solve=st.ms_solve, refine_history=list(st.refine_history[:st.nhist]),
+                               ms_residual=st.ms_residual, n_residual=st.n_residual)
         return A0, A1
 
     def close(self):
