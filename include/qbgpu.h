@@ -155,11 +155,17 @@ typedef struct qbg_beyn_opts {
   int32_t max_refine;   /* mixed form: maximum refinement sweeps (default 4) */
   double refine_tol;    /* complex64 forms: the first correction uses an FP32 residual; later residuals
                            are compensated; once max|R| <= tol * max|V| the correction from that
-                           residual is applied and refinement stops (default 1e-7) */
+                           residual is applied and refinement stops (default 1e-6). Each correction
+                           contracts the residual by rho ~ cond(T) * 2^-24 (refine_history shows it),
+                           so the returned solution's residual is about tol * rho. */
   int32_t nb;           /* LU block size (0 = default) */
   int32_t eval_mode;    /* 0: Chebyshev panels (the reference's default, use_chebyshev=true);
                            1: direct evaluation of H0, H1, J0, J1 */
   qbg_cheb_params cheb; /* panel parameters for eval_mode 0 (zeros = reference defaults) */
+  int32_t fp32_sweeps;  /* complex64 forms: corrections from plain FP32 residuals V - hi X before the
+                           compensated ones (0 = default 1, at most 4) */
+  int32_t solve_block;  /* complex64 forms: rows per block of the triangular solves, nb, 2 nb or 4 nb
+                           (0 = default 4 nb for N >= 8 nb) */
 } qbg_beyn_opts;
 
 typedef struct qbg_beyn_stats {
@@ -171,6 +177,10 @@ typedef struct qbg_beyn_stats {
   double refine_history[8];                /* max|R|/max|V| before each correction sweep */
   double ms_residual;                      /* device time of the compensated residual launches */
   int32_t n_residual;                      /* number of compensated residual launches */
+  int32_t nfp32;                           /* plain FP32 residuals recorded in fp32_history */
+  double fp32_history[4];                  /* max|V - hi X| / max|V| of each FP32 residual */
+  double ms_solves;                        /* device time of the triangular solves */
+  int32_t n_solves;                        /* number of solve passes (each over every contour node) */
 } qbg_beyn_stats;
 
 qbg_status qbg_beyn_create(qbg_geom* g, double k0_re, double k0_im, double R, int32_t nq, int32_t prec,
@@ -187,6 +197,24 @@ qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig)
 /* Device special functions, for validation: out[4*i..] = J0, J1, Y0, Y1 at z[i]
  * (complex interleaved). f32 = 1 selects the FP32 asymptotic evaluator. */
 qbg_status qbg_bessel01(const double* z, int64_t n, int32_t f32, double* out);
+
+/* Device complex64 GEMM, for validation: C_b = alpha A_b B_b + beta C_b for
+ * b < batch, column-major host buffers (complex interleaved floats; A_b at
+ * A + 2*b*lda*K, B_b at B + 2*b*ldb*N, C_b at C + 2*b*ldc*N). engine selects
+ * the GEMM inside the FP32 LU and solves: 0 = CUDA-core FMA tiles,
+ * 1 = tcgen05 tensor cores (3xTF32). No reference counterpart: the reference's
+ * GEMMs run inside LAPACK's getrf/getrs (beyn.jl:270-280). */
+qbg_status qbg_cgemm_c64(int32_t engine, int32_t M, int32_t N, int32_t K, const float* alpha, const float* A,
+                         int64_t lda, const float* B, int64_t ldb, const float* beta, float* C, int64_t ldc,
+                         int32_t batch);
+
+/* Selects the complex64 GEMM engine (0 or 1 as above) for later calls,
+ * process-wide; the default is 1. No reference counterpart. */
+qbg_status qbg_set_gemm_engine(int32_t engine);
+
+/* Number of CUDA kernels this library has launched in the process so far
+ * (diagnostic; no reference counterpart). */
+qbg_status qbg_launch_count(uint64_t* count);
 
 #ifdef __cplusplus
 }

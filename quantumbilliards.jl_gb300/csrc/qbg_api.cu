@@ -8,6 +8,7 @@
 #include <vector>
 #include <algorithm>
 #include <cusolverDn.h>
+#include <atomic>
 
 #include "qbg_assemble.cuh"
 #include "qbg_handles.cuh"
@@ -15,6 +16,9 @@
 
 namespace qbg {
 static thread_local std::string g_err;
+static std::atomic<unsigned long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
 void set_error(const char* fmt, ...) {
   char buf[1024];
   va_list ap;
@@ -343,7 +347,7 @@ struct qbg_beyn {
 };
 
 template <class T>
-static int beyn_setup_lu(qbg_beyn* b, LUBatch<T>& f, int nb) {
+static int beyn_setup_lu(qbg_beyn* b, LUBatch<T>& f, int nb, int solve_levels) {
   f.n = b->n;
   f.batch = b->nq;
   f.nb = nb;
@@ -355,6 +359,11 @@ static int beyn_setup_lu(qbg_beyn* b, LUBatch<T>& f, int nb) {
   QBG_TRY(b->alloc(&f.info, sizeof(int) * f.batch));
   QBG_TRY(b->alloc(&f.Linv, sizeof(cx<T>) * (size_t)f.nblk * nb * nb * f.batch));
   QBG_TRY(b->alloc(&f.Uinv, sizeof(cx<T>) * (size_t)f.nblk * nb * nb * f.batch));
+  if (solve_levels > 0) {
+    void* mem = nullptr;
+    QBG_TRY(b->alloc(&mem, lu_solve_blocks_bytes<T>(f, solve_levels, 128)));
+    lu_solve_blocks_bind<T>(f, mem);
+  }
   return QBG_OK;
 }
 
@@ -380,10 +389,19 @@ static int beyn_create_impl(qbg_beyn* b, double k0_re, double k0_im, double R) {
   void** dptrs = nullptr;
   QBG_TRY(b->alloc(&dptrs, sizeof(void*) * nq));
   if (b->prec == 0) {
-    QBG_TRY(beyn_setup_lu(b, b->fd, nb));
+    QBG_TRY(beyn_setup_lu(b, b->fd, nb, 0));
     for (int j = 0; j < nq; ++j) ptrs[j] = b->fd.A + (size_t)j * b->fd.stride;
   } else {
-    QBG_TRY(beyn_setup_lu(b, b->ff, nb));
+    int levels = n >= 8 * nb ? 2 : (n >= 4 * nb ? 1 : 0);
+    if (b->opts.solve_block != 0) {
+      const int sb = b->opts.solve_block;
+      if (sb != nb && sb != 2 * nb && sb != 4 * nb) {
+        set_error("solve_block must be nb, 2 nb or 4 nb (nb = %d)", nb);
+        return QBG_EINVAL;
+      }
+      levels = sb == nb ? 0 : (sb == 2 * nb ? 1 : 2);
+    }
+    QBG_TRY(beyn_setup_lu(b, b->ff, nb, levels));
     for (int j = 0; j < nq; ++j) ptrs[j] = b->ff.A + (size_t)j * b->ff.stride;
   }
   QBG_CUDA(cudaMemcpyAsync(dptrs, ptrs.data(), sizeof(void*) * nq, cudaMemcpyHostToDevice, st));
@@ -429,6 +447,7 @@ static int beyn_create_impl(qbg_beyn* b, double k0_re, double k0_im, double R) {
   QBG_CUDA(cudaMemcpyAsync(info.data(), b->prec ? b->ff.info : b->fd.info, sizeof(int) * nq,
                            cudaMemcpyDeviceToHost, st));
   QBG_CUDA(cudaStreamSynchronize(st));
+  if (b->prec != 0) QBG_TRY(tc_check(st));
   b->singular = 0;
   for (int v : info) b->singular += (v != 0);
   QBG_CUDA(cudaEventElapsedTime(&b->ms_assemble, b->ev[0], b->ev[1]));
@@ -458,14 +477,14 @@ qbg_status qbg_beyn_create(qbg_geom* g, double k0_re, double k0_im, double R, in
   b->prec = prec;
   b->opts.flags = 0;
   b->opts.max_refine = 4;
-  b->opts.refine_tol = 1e-7;
+  b->opts.refine_tol = 1e-6;
   b->opts.nb = 0;
   b->opts.eval_mode = 0;
   b->opts.cheb = qbg_cheb_params{0, 0, 0, 0};
   if (opts) {
     b->opts = *opts;
     if (b->opts.max_refine <= 0) b->opts.max_refine = 4;
-    if (!(b->opts.refine_tol > 0.0)) b->opts.refine_tol = 1e-7;
+    if (!(b->opts.refine_tol > 0.0)) b->opts.refine_tol = 1e-6;
   }
   std::lock_guard<std::mutex> lk(g->mu);
   b->st = g->stream;
@@ -491,7 +510,12 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
   cudaStream_t st = b->st;
   const size_t nl = (size_t)n * L;
   std::vector<void*> tmp;
-  auto cleanup = [&]() { for (void* p : tmp) cudaFree(p); };
+  std::vector<cudaEvent_t> sev;  // solve start/stop pairs
+  auto cleanup = [&]() {
+    for (void* p : tmp) cudaFree(p);
+    for (cudaEvent_t e : sev) cudaEventDestroy(e);
+    sev.clear();
+  };
   auto talloc = [&](void** p, size_t bytes) {
     int s = dmalloc(p, bytes);
     if (!s) tmp.push_back(*p);
@@ -514,6 +538,8 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
   int nhist = 0;
   double ms_resid = 0.0;
   int n_resid = 0;
+  double f32hist[4] = {0, 0, 0, 0};
+  int nf32 = 0;
   if (b->prec == 0) {
     cxd* X = nullptr;
     if ((s = talloc((void**)&X, sizeof(cxd) * nl * nq))) { cleanup(); return s; }
@@ -531,11 +557,26 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
         (s = talloc((void**)&R64, sizeof(cxd) * nl * nq)) || (s = talloc((void**)&dmax, sizeof(double)))) {
       cleanup(); return s;
     }
+    // every solve pass is bracketed by a pair of events, summed after the last sync
+    auto timed_solve = [&](const cxf* rhs, long long srhs) -> int {
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      if (sev.size() < 32 && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
+        sev.push_back(e0);
+        sev.push_back(e1);
+        cudaEventRecord(e0, st);
+      } else {
+        if (e0) cudaEventDestroy(e0);
+        e0 = e1 = nullptr;
+      }
+      int r = lu_solve_shared<float>(b->ff, rhs, (int)L, X32, srhs, st);
+      if (e1) cudaEventRecord(e1, st);
+      return r;
+    };
     // max |V| (|re|+|im|) on the host side of the copy is not available for device V: compute by residual with X=0
     cudaError_t e = cudaMemsetAsync(X64, 0, sizeof(cxd) * nl * nq, st);
     if (e != cudaSuccess) { cleanup(); return cuda_status(e, "memset"); }
     if ((s = convert_d2f(dV, V32, (long long)nl, st)) ||
-        (s = lu_solve_shared<float>(b->ff, V32, (int)L, X32, 0, st)) ||
+        (s = timed_solve(V32, 0)) ||
         (s = axpy_f2d(X32, X64, (long long)(nl * nq), st))) { cleanup(); return s; }
     double vmax = 0.0;
     {
@@ -553,16 +594,29 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
       }
     }
     if (!(vmax > 0.0)) vmax = 1.0;
-    // First correction from a plain FP32 residual V - hi X0: the residual of the
-    // FP32 solve is O(1e-2) of |V|, far above the FP32 rounding of the GEMM, so
-    // compensated arithmetic buys nothing yet. Later residuals (and the
-    // convergence test) use the compensated kernel with hi + lo.
-    if ((s = broadcast_f(V32, (long long)nl, nq, R32, st)) ||
-        (s = gemm_batched<float>(n, (int)L, n, cxf(-1.f, 0.f), b->Tcopy, n, b->ff.stride, X32, n, (long long)nl,
-                                 cxf(1.f, 0.f), R32, n, (long long)nl, nq, st)) ||
-        (s = lu_solve_shared<float>(b->ff, R32, (int)L, X32, (long long)nl, st)) ||
-        (s = axpy_f2d(X32, X64, (long long)(nl * nq), st))) { cleanup(); return s; }
-    ++sweeps;
+    // Corrections from plain FP32 residuals V32 - hi X: while the residual is far
+    // above the FP32 rounding of the product, compensated arithmetic buys
+    // nothing. Later residuals (and the convergence test) use the compensated
+    // kernel with hi + lo.
+    const int nf = std::min(b->opts.fp32_sweeps > 0 ? b->opts.fp32_sweeps : 1, 4);
+    for (int q = 0; q < nf; ++q) {
+      // X32 holds the first solve's result for q == 0, a correction afterwards
+      if (q > 0 && (s = convert_d2f(X64, X32, (long long)(nl * nq), st))) { cleanup(); return s; }
+      e = cudaMemsetAsync(dmax, 0, sizeof(double), st);
+      if (e != cudaSuccess) { cleanup(); return cuda_status(e, "memset"); }
+      if ((s = broadcast_f(V32, (long long)nl, nq, R32, st)) ||
+          (s = gemm_batched<float>(n, (int)L, n, cxf(-1.f, 0.f), b->Tcopy, n, b->ff.stride, X32, n, (long long)nl,
+                                   cxf(1.f, 0.f), R32, n, (long long)nl, nq, st)) ||
+          (s = maxabs_c64(R32, (long long)(nl * nq), dmax, st)) ||
+          (s = timed_solve(R32, (long long)nl)) ||
+          (s = axpy_f2d(X32, X64, (long long)(nl * nq), st))) { cleanup(); return s; }
+      double fmax = 0.0;
+      e = cudaMemcpyAsync(&fmax, dmax, sizeof(double), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) { cleanup(); return cuda_status(e, "FP32 residual"); }
+      if (nf32 < 4) f32hist[nf32++] = fmax / vmax;
+      ++sweeps;
+    }
     for (int it = 0; it < b->opts.max_refine; ++it) {
       e = cudaMemsetAsync(dmax, 0, sizeof(double), st);
       if (e != cudaSuccess) { cleanup(); return cuda_status(e, "memset"); }
@@ -584,7 +638,7 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
       // residual already meets the tolerance this is the final correction
       // (the residual is in hand, the solve costs one FP32 pass)
       if ((s = convert_d2f(R64, R32, (long long)(nl * nq), st)) ||
-          (s = lu_solve_shared<float>(b->ff, R32, (int)L, X32, (long long)nl, st)) ||
+          (s = timed_solve(R32, (long long)nl)) ||
           (s = axpy_f2d(X32, X64, (long long)(nl * nq), st))) { cleanup(); return s; }
       if (rel <= b->opts.refine_tol) break;
     }
@@ -599,8 +653,15 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
     if (e != cudaSuccess) { cleanup(); return cuda_status(e, "A0/A1 D2H"); }
   }
   cudaError_t e = cudaStreamSynchronize(st);
+  double ms_solves = 0.0;
+  const int n_solves = (int)sev.size() / 2;
+  for (size_t q = 0; e == cudaSuccess && q + 1 < sev.size(); q += 2) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, sev[q], sev[q + 1]) == cudaSuccess) ms_solves += ms;
+  }
   cleanup();
   if (e != cudaSuccess) return cuda_status(e, "qbg_beyn_moments");
+  if (b->prec != 0) QBG_TRY(tc_check(st));
   if (stats) {
     float ms = 0;
     cudaEventElapsedTime(&ms, b->ev[0], b->ev[3]);
@@ -613,6 +674,10 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
     stats->nhist = nhist;
     stats->ms_residual = ms_resid;
     stats->n_residual = n_resid;
+    stats->nfp32 = nf32;
+    for (int q = 0; q < 4; ++q) stats->fp32_history[q] = f32hist[q];
+    stats->ms_solves = ms_solves;
+    stats->n_solves = n_solves;
     for (int q = 0; q < 8; ++q) stats->refine_history[q] = hist[q];
   }
   return QBG_OK;
@@ -704,6 +769,57 @@ qbg_status qbg_bessel01(const double* z, int64_t n, int32_t f32, double* out) {
   cudaFree(dout);
   if (s) return s;
   if (e != cudaSuccess) return cuda_status(e, "qbg_bessel01");
+  return QBG_OK;
+}
+
+qbg_status qbg_cgemm_c64(int32_t engine, int32_t M, int32_t N, int32_t K, const float* alpha, const float* A,
+                         int64_t lda, const float* B, int64_t ldb, const float* beta, float* C, int64_t ldc,
+                         int32_t batch) {
+  if (!alpha || !beta || !A || !B || !C || M < 1 || N < 1 || K < 1 || batch < 1 || batch > 65535 || lda < M ||
+      ldb < K || ldc < M || (engine != GEMM_ENGINE_SIMT && engine != GEMM_ENGINE_TCGEN05)) {
+    set_error("qbg_cgemm_c64: invalid arguments");
+    return QBG_EINVAL;
+  }
+  const long long sA = lda * (long long)K, sB = ldb * (long long)N, sC = ldc * (long long)N;
+  cxf *dA = nullptr, *dB = nullptr, *dC = nullptr;
+  int s = dmalloc(&dA, sizeof(cxf) * sA * batch);
+  if (!s) s = dmalloc(&dB, sizeof(cxf) * sB * batch);
+  if (!s) s = dmalloc(&dC, sizeof(cxf) * sC * batch);
+  cudaError_t e = cudaSuccess;
+  if (!s) {
+    e = cudaMemcpy(dA, A, sizeof(cxf) * sA * batch, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dB, B, sizeof(cxf) * sB * batch, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dC, C, sizeof(cxf) * sC * batch, cudaMemcpyHostToDevice);
+  }
+  if (!s && e == cudaSuccess) {
+    const cxf al(alpha[0], alpha[1]), be(beta[0], beta[1]);
+    if (engine == GEMM_ENGINE_TCGEN05)
+      s = tc_gemm_c64(M, N, K, al, dA, lda, sA, dB, ldb, sB, be, dC, ldc, sC, batch, 0);
+    else
+      s = gemm_batched_simt<float>(M, N, K, al, dA, lda, sA, dB, ldb, sB, be, dC, ldc, sC, batch, 0);
+    if (!s && engine == GEMM_ENGINE_TCGEN05) s = tc_check(0);
+    if (!s) e = cudaMemcpy(C, dC, sizeof(cxf) * sC * batch, cudaMemcpyDeviceToHost);
+  }
+  cudaFree(dA);
+  cudaFree(dB);
+  cudaFree(dC);
+  if (s) return s;
+  if (e != cudaSuccess) return cuda_status(e, "qbg_cgemm_c64");
+  return QBG_OK;
+}
+
+qbg_status qbg_launch_count(uint64_t* count) {
+  if (!count) { set_error("qbg_launch_count: null pointer"); return QBG_EINVAL; }
+  *count = g_launches.load(std::memory_order_relaxed);
+  return QBG_OK;
+}
+
+qbg_status qbg_set_gemm_engine(int32_t engine) {
+  if (engine != GEMM_ENGINE_SIMT && engine != GEMM_ENGINE_TCGEN05) {
+    set_error("qbg_set_gemm_engine: engine must be 0 or 1");
+    return QBG_EINVAL;
+  }
+  set_gemm_engine(engine);
   return QBG_OK;
 }
 

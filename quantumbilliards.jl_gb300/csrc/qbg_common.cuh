@@ -66,6 +66,7 @@ typedef cx<float> cxf;
 
 namespace qbg {
 void set_error(const char* fmt, ...);
+void note_launch();
 int cuda_status(cudaError_t e, const char* what);
 }  // namespace qbg
 
@@ -75,8 +76,11 @@ int cuda_status(cudaError_t e, const char* what);
     if (_e != cudaSuccess) return qbg::cuda_status(_e, #call);  \
   } while (0)
 
+// Every kernel launch of the library is followed by exactly one
+// QBG_LAUNCH_CHECK, which also counts it (qbg_launch_count).
 #define QBG_LAUNCH_CHECK(what)                                              \
   do {                                                                      \
+    qbg::note_launch();                                                     \
     cudaError_t _e = cudaGetLastError();                                    \
     if (_e != cudaSuccess) return qbg::cuda_status(_e, what);               \
   } while (0)

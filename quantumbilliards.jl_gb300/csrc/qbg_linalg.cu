@@ -16,6 +16,8 @@
 //     5. gemm            A22 -= L21 U12       (trailing update)
 //   After the last panel the upper diagonal blocks are inverted so that the
 //   triangular solves are sequences of GEMMs.
+#include <algorithm>
+#include <type_traits>
 #include "qbg_linalg.cuh"
 
 namespace qbg {
@@ -94,14 +96,26 @@ __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, cx<T> alpha, 
 }
 
 template <class T>
-int gemm_batched(int M, int N, int K, cx<T> alpha, const cx<T>* A, long long lda, long long sA, const cx<T>* B,
-                 long long ldb, long long sB, cx<T> beta, cx<T>* C, long long ldc, long long sC, int batch,
-                 cudaStream_t st) {
+int gemm_batched_simt(int M, int N, int K, cx<T> alpha, const cx<T>* A, long long lda, long long sA, const cx<T>* B,
+                      long long ldb, long long sB, cx<T> beta, cx<T>* C, long long ldc, long long sC, int batch,
+                      cudaStream_t st) {
   if (M <= 0 || N <= 0 || batch <= 0) return QBG_OK;
   dim3 grd((M + 63) / 64, (N + 63) / 64, batch);
   k_gemm<T><<<grd, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
   QBG_LAUNCH_CHECK("k_gemm");
   return QBG_OK;
+}
+
+template <class T>
+int gemm_batched(int M, int N, int K, cx<T> alpha, const cx<T>* A, long long lda, long long sA, const cx<T>* B,
+                 long long ldb, long long sB, cx<T> beta, cx<T>* C, long long ldc, long long sC, int batch,
+                 cudaStream_t st) {
+  if (M <= 0 || N <= 0 || batch <= 0) return QBG_OK;
+  if constexpr (std::is_same<T, float>::value) {
+    if (K > 0 && gemm_engine() == GEMM_ENGINE_TCGEN05)
+      return tc_gemm_c64(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch, st);
+  }
+  return gemm_batched_simt<T>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -441,6 +455,145 @@ __global__ void k_gather_rows(const cx<T>* V, long long strideV, const int* perm
   X[(long long)b * n * L + e] = V[(long long)b * strideV + perm[(long long)b * n + i] + (long long)l * n];
 }
 
+// ---------------------------------------------------------------------------
+// solve blocks of nbs = nb * 2^levels rows: doubling of the diagonal-block
+// inverses (the same identities as k_trtri, one level per pass):
+//   lower unit: inv([A 0; C B]) = [Ai 0; -Bi (C Ai)  Bi]
+//   upper:      inv([A C; 0 B]) = [Ai -Ai (C Bi); 0  Bi]
+// ---------------------------------------------------------------------------
+template <class T>
+static int gemm_batched2(int M, int N, int K, cx<T> alpha, const cx<T>* A, long long lda, long long sA,
+                         long long sA2, const cx<T>* B, long long ldb, long long sB, long long sB2, cx<T> beta,
+                         cx<T>* C, long long ldc, long long sC, long long sC2, int batch, int batch2,
+                         cudaStream_t st) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (gemm_engine() == GEMM_ENGINE_TCGEN05)
+      return tc_gemm_c64(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch, st, batch2, sA2, sB2,
+                         sC2);
+  }
+  for (int q = 0; q < batch2; ++q) {
+    int s = gemm_batched<T>(M, N, K, alpha, A + q * sA2, lda, sA, B + q * sB2, ldb, sB, beta, C + q * sC2, ldc, sC,
+                            batch, st);
+    if (s) return s;
+  }
+  return QBG_OK;
+}
+
+// out block p (2b x 2b, ld 2b): diagonal b x b blocks from in[2p], in[2p+1]
+// (identity where the second block lies beyond the matrix), zeros elsewhere.
+template <class T>
+__global__ void k_place_diag(const cx<T>* Lin, const cx<T>* Uin, int b, int nin, cx<T>* Lout, cx<T>* Uout,
+                             int nout) {
+  const long long per = (long long)nout * 4 * b * b;
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= per) return;
+  const long long node = blockIdx.y;
+  const int b2 = 2 * b;
+  const int p = (int)(e / ((long long)b2 * b2));
+  const int rem = (int)(e % ((long long)b2 * b2));
+  const int i = rem % b2, j = rem / b2;
+  const int hi = i >= b, hj = j >= b;
+  cx<T> lv(0, 0), uv(0, 0);
+  if (hi == hj) {
+    const int q = 2 * p + hi, ii = i - hi * b, jj = j - hj * b;
+    if (q < nin) {
+      const long long o = node * nin * (long long)b * b + (long long)q * b * b + ii + (long long)jj * b;
+      lv = Lin[o];
+      uv = Uin[o];
+    } else if (ii == jj) {
+      lv = cx<T>(1, 0);
+      uv = cx<T>(1, 0);
+    }
+  }
+  Lout[node * per + e] = lv;
+  Uout[node * per + e] = uv;
+}
+
+// one doubling pass: b x b block inverses (nin per matrix) -> 2b x 2b (ceil(nin/2))
+template <class T>
+static int double_level(const LUBatch<T>& f, const cx<T>* Lin, const cx<T>* Uin, int b, int nin, cx<T>* Lout,
+                        cx<T>* Uout, cudaStream_t st) {
+  const int n = f.n, batch = f.batch, b2 = 2 * b, nout = (nin + 1) / 2;
+  const long long per = (long long)nout * b2 * b2;
+  dim3 g((unsigned)((per + 255) / 256), batch);
+  k_place_diag<T><<<g, 256, 0, st>>>(Lin, Uin, b, nin, Lout, Uout, nout);
+  QBG_LAUNCH_CHECK("k_place_diag");
+  const int npairs = nin / 2;
+  if (npairs == 0) return QBG_OK;
+  const long long sIn = (long long)nin * b * b, sOut = per;
+  const long long sW = (long long)((f.nblk + 1) / 2) * (f.nbs / 2) * (f.nbs / 2);
+  // the second block of the last pair may be partial
+  const int wlast = min(b, n - (2 * npairs - 1) * b);
+  const int nfull = wlast < b ? npairs - 1 : npairs;
+  const cx<T> one(1, 0), mone(-1, 0), zero(0, 0);
+  auto run = [&](int p0, int np, int w2) -> int {
+    const long long sA2 = 2LL * b * (n + 1), sB2 = 2LL * b * b, sC2 = (long long)b2 * b2, sW2 = (long long)b * b;
+    // lower: W = L21 Ai (w2 x b), then bottom-left = -Bi W
+    const cx<T>* L21 = f.A + (long long)(2 * p0 + 1) * b + (long long)(2 * p0) * b * n;
+    int s = gemm_batched2<T>(w2, b, b, one, L21, n, f.stride, sA2, Lin + 2LL * p0 * b * b, b, sIn, sB2, zero,
+                             f.W, b, sW, sW2, batch, np, st);
+    if (!s)
+      s = gemm_batched2<T>(w2, b, w2, mone, Lin + (2LL * p0 + 1) * b * b, b, sIn, sB2, f.W, b, sW, sW2, zero,
+                           Lout + (long long)p0 * b2 * b2 + b, b2, sOut, sC2, batch, np, st);
+    // upper: W = U12 Bi (b x w2), then top-right = -Ai W
+    const cx<T>* U12 = f.A + (long long)(2 * p0) * b + (long long)(2 * p0 + 1) * b * n;
+    if (!s)
+      s = gemm_batched2<T>(b, w2, w2, one, U12, n, f.stride, sA2, Uin + (2LL * p0 + 1) * b * b, b, sIn, sB2, zero,
+                           f.W, b, sW, sW2, batch, np, st);
+    if (!s)
+      s = gemm_batched2<T>(b, w2, b, mone, Uin + 2LL * p0 * b * b, b, sIn, sB2, f.W, b, sW, sW2, zero,
+                           Uout + (long long)p0 * b2 * b2 + (long long)b * b2, b2, sOut, sC2, batch, np, st);
+    return s;
+  };
+  if (nfull > 0)
+    if (int s = run(0, nfull, b)) return s;
+  if (nfull < npairs)
+    if (int s = run(nfull, 1, wlast)) return s;
+  return QBG_OK;
+}
+
+template <class T>
+size_t lu_solve_blocks_bytes(LUBatch<T>& f, int levels, int ymax_L) {
+  f.levels = levels;
+  f.nbs = f.nb << levels;
+  f.nblks = (f.n + f.nbs - 1) / f.nbs;
+  f.ymax_L = levels > 0 ? ymax_L : 0;
+  if (levels == 0) return 0;
+  const size_t e = sizeof(cx<T>);
+  const size_t mid = levels == 2 ? (size_t)((f.nblk + 1) / 2) * (2 * f.nb) * (2 * f.nb) : 0;
+  const size_t fin = (size_t)f.nblks * f.nbs * f.nbs;
+  const size_t w = (size_t)((f.nblk + 1) / 2) * (f.nbs / 2) * (f.nbs / 2);
+  const size_t y = (size_t)f.n * f.ymax_L;
+  auto r256 = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  return r256(e * mid * f.batch) * 2 + r256(e * fin * f.batch) * 2 + r256(e * w * f.batch) + r256(e * y * f.batch);
+}
+
+template <class T>
+void lu_solve_blocks_bind(LUBatch<T>& f, void* mem) {
+  if (f.levels == 0) return;
+  auto r256 = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t e = sizeof(cx<T>);
+  const size_t mid = f.levels == 2 ? (size_t)((f.nblk + 1) / 2) * (2 * f.nb) * (2 * f.nb) : 0;
+  const size_t fin = (size_t)f.nblks * f.nbs * f.nbs;
+  const size_t w = (size_t)((f.nblk + 1) / 2) * (f.nbs / 2) * (f.nbs / 2);
+  unsigned char* p = static_cast<unsigned char*>(mem);
+  f.Linv_mid = reinterpret_cast<cx<T>*>(p); p += r256(e * mid * f.batch);
+  f.Uinv_mid = reinterpret_cast<cx<T>*>(p); p += r256(e * mid * f.batch);
+  f.Linv2 = reinterpret_cast<cx<T>*>(p); p += r256(e * fin * f.batch);
+  f.Uinv2 = reinterpret_cast<cx<T>*>(p); p += r256(e * fin * f.batch);
+  f.W = reinterpret_cast<cx<T>*>(p); p += r256(e * w * f.batch);
+  f.Y = reinterpret_cast<cx<T>*>(p);
+}
+
+template <class T>
+static int build_solve_blocks(const LUBatch<T>& f, cudaStream_t st) {
+  if (f.levels == 1) return double_level<T>(f, f.Linv, f.Uinv, f.nb, f.nblk, f.Linv2, f.Uinv2, st);
+  const int nmid = (f.nblk + 1) / 2;
+  int s = double_level<T>(f, f.Linv, f.Uinv, f.nb, f.nblk, f.Linv_mid, f.Uinv_mid, st);
+  if (!s) s = double_level<T>(f, f.Linv_mid, f.Uinv_mid, 2 * f.nb, nmid, f.Linv2, f.Uinv2, st);
+  return s;
+}
+
 template <class T>
 int lu_factor(LUBatch<T>& f, cudaStream_t st) {
   const int n = f.n, nb = f.nb, batch = f.batch;
@@ -499,6 +652,7 @@ int lu_factor(LUBatch<T>& f, cudaStream_t st) {
                                   (int)(sizeof(int) * (size_t)n)));
   k_perm_from_ipiv<<<batch, 256, sizeof(int) * n, st>>>(f.ipiv, f.perm, n);
   QBG_LAUNCH_CHECK("k_perm_from_ipiv");
+  if (f.levels > 0) return build_solve_blocks<T>(f, st);
   return QBG_OK;
 }
 
@@ -509,6 +663,38 @@ int lu_solve_shared(const LUBatch<T>& f, const cx<T>* V, int L, cx<T>* X, long l
   dim3 g((unsigned)(((long long)n * L + 255) / 256), batch);
   k_gather_rows<T><<<g, 256, 0, st>>>(V, strideV, f.perm, n, L, X);
   QBG_LAUNCH_CHECK("k_gather_rows");
+  if (f.levels > 0) {
+    // blocks of nbs rows; forward: Y_b = Linv_b X_b, X_rest -= L_rest,b Y_b;
+    // backward: X_b = Uinv_b Y_b, Y_above -= U_above,b X_b (no in-place products)
+    const int bs = f.nbs;
+    const long long sI2 = (long long)f.nblks * bs * bs;
+    const cx<T> one(1, 0), mone(-1, 0), zero(0, 0);
+    for (int c0 = 0; c0 < L; c0 += f.ymax_L) {
+      const int Lc = min(f.ymax_L, L - c0);
+      cx<T>* Xc = X + (long long)c0 * n;
+      cx<T>* Yc = f.Y;
+      const long long sY = (long long)n * Lc;
+      for (int blk = 0; blk < f.nblks; ++blk) {
+        const int r0 = blk * bs, w = min(bs, n - r0), rest = n - r0 - w;
+        int s = gemm_batched<T>(w, Lc, w, one, f.Linv2 + (long long)blk * bs * bs, bs, sI2, Xc + r0, n, sX, zero,
+                                Yc + r0, n, sY, batch, st);
+        if (!s && rest > 0)
+          s = gemm_batched<T>(rest, Lc, w, mone, f.A + (r0 + w) + (long long)r0 * n, n, f.stride, Yc + r0, n, sY,
+                              one, Xc + r0 + w, n, sX, batch, st);
+        if (s) return s;
+      }
+      for (int blk = f.nblks - 1; blk >= 0; --blk) {
+        const int r0 = blk * bs, w = min(bs, n - r0);
+        int s = gemm_batched<T>(w, Lc, w, one, f.Uinv2 + (long long)blk * bs * bs, bs, sI2, Yc + r0, n, sY, zero,
+                                Xc + r0, n, sX, batch, st);
+        if (!s && r0 > 0)
+          s = gemm_batched<T>(r0, Lc, w, mone, f.A + (long long)r0 * n, n, f.stride, Xc + r0, n, sX, one, Yc, n,
+                              sY, batch, st);
+        if (s) return s;
+      }
+    }
+    return QBG_OK;
+  }
   const long long sInv = (long long)f.nblk * nb * nb;
   for (int blk = 0; blk < f.nblk; ++blk) {
     const int r0 = blk * nb, w = min(nb, n - r0);
@@ -735,6 +921,22 @@ int broadcast_f(const cxf* in, long long count, int batch, cxf* out, cudaStream_
   QBG_LAUNCH_CHECK("k_bcast_f");
   return QBG_OK;
 }
+__global__ void k_maxabs_c64(const cxf* __restrict__ x, long long count, unsigned long long* out) {
+  float m = 0.f;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (long long)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(x[e].re) + fabsf(x[e].im));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  // non-negative doubles order like their bit patterns
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong((double)m));
+}
+int maxabs_c64(const cxf* x, long long count, double* out, cudaStream_t st) {
+  if (count <= 0) return QBG_OK;
+  const long long blocks = std::min<long long>((count + 255) / 256, 152 * 8);
+  k_maxabs_c64<<<(unsigned)blocks, 256, 0, st>>>(x, count, reinterpret_cast<unsigned long long*>(out));
+  QBG_LAUNCH_CHECK("k_maxabs_c64");
+  return QBG_OK;
+}
 int convert_d2f(const cxd* in, cxf* out, long long count, cudaStream_t st) {
   k_d2f<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(in, out, count);
   QBG_LAUNCH_CHECK("k_d2f");
@@ -747,11 +949,17 @@ int axpy_f2d(const cxf* d, cxd* x, long long count, cudaStream_t st) {
 }
 
 template int lu_factor<double>(LUBatch<double>&, cudaStream_t);
+template size_t lu_solve_blocks_bytes<double>(LUBatch<double>&, int, int);
+template size_t lu_solve_blocks_bytes<float>(LUBatch<float>&, int, int);
+template void lu_solve_blocks_bind<double>(LUBatch<double>&, void*);
+template void lu_solve_blocks_bind<float>(LUBatch<float>&, void*);
 template int lu_factor<float>(LUBatch<float>&, cudaStream_t);
 template int lu_solve_shared<double>(const LUBatch<double>&, const cxd*, int, cxd*, long long, cudaStream_t);
 template int lu_solve_shared<float>(const LUBatch<float>&, const cxf*, int, cxf*, long long, cudaStream_t);
 template int gemm_batched<double>(int, int, int, cxd, const cxd*, long long, long long, const cxd*, long long,
                                   long long, cxd, cxd*, long long, long long, int, cudaStream_t);
+template int gemm_batched_simt<float>(int, int, int, cxf, const cxf*, long long, long long, const cxf*, long long,
+                                      long long, cxf, cxf*, long long, long long, int, cudaStream_t);
 template int gemm_batched<float>(int, int, int, cxf, const cxf*, long long, long long, const cxf*, long long,
                                  long long, cxf, cxf*, long long, long long, int, cudaStream_t);
 template int moments<double>(const cxd*, long long, int, int, int, const cxd*, const cxd*, cxd*, cxd*, int,

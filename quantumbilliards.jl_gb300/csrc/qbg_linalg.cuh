@@ -17,7 +17,25 @@ struct LUBatch {
   int* info = nullptr;      // batch
   cx<T>* Linv = nullptr;    // batch * nblk * nb * nb
   cx<T>* Uinv = nullptr;    // batch * nblk * nb * nb
+  // Triangular solves in blocks of nbs = nb * 2^levels rows (levels 0..2):
+  // inverses of the nbs x nbs diagonal blocks, built from the nb x nb ones by
+  // doubling after the factorisation; the solve ping-pongs between X and Y.
+  int levels = 0, nbs = 0, nblks = 0;
+  cx<T>* Linv_mid = nullptr;  // batch * ceil(n / 2nb) * (2nb)^2 (levels == 2)
+  cx<T>* Uinv_mid = nullptr;
+  cx<T>* Linv2 = nullptr;     // batch * nblks * nbs^2
+  cx<T>* Uinv2 = nullptr;
+  cx<T>* W = nullptr;         // doubling scratch: batch * ceil(nblk / 2) * (nbs / 2)^2
+  cx<T>* Y = nullptr;         // solve scratch: batch * n * ymax_L
+  int ymax_L = 0;
 };
+
+// Sets levels/nbs/nblks and returns the device bytes the solve blocks need.
+template <class T>
+size_t lu_solve_blocks_bytes(LUBatch<T>& f, int levels, int ymax_L);
+// Points the solve-block buffers into one device allocation of that size.
+template <class T>
+void lu_solve_blocks_bind(LUBatch<T>& f, void* mem);
 
 template <class T>
 int lu_factor(LUBatch<T>& f, cudaStream_t st);
@@ -33,6 +51,12 @@ int gemm_batched(int M, int N, int K, cx<T> alpha, const cx<T>* A, long long lda
                  long long ldb, long long sB, cx<T> beta, cx<T>* C, long long ldc, long long sC, int batch,
                  cudaStream_t st);
 
+// The CUDA-core (FMA) tile GEMM, whatever the engine setting.
+template <class T>
+int gemm_batched_simt(int M, int N, int K, cx<T> alpha, const cx<T>* A, long long lda, long long sA, const cx<T>* B,
+                      long long ldb, long long sB, cx<T> beta, cx<T>* C, long long ldc, long long sC, int batch,
+                      cudaStream_t st);
+
 // A0 = sum_b w_b X_b, A1 = sum_b w_b z_b X_b  (outputs complex128, n x L)
 template <class T>
 int moments(const cx<T>* X, long long sX, int batch, int n, int L, const cxd* w, const cxd* z, cxd* A0, cxd* A1,
@@ -45,7 +69,29 @@ int moments(const cx<T>* X, long long sX, int batch, int n, int L, const cxd* w,
 int residual_df32(const cxf* Tm, const cxf* Tlo, long long sT, const cxd* X, long long sX, const cxd* V, cxd* R,
                   long long sR, int n, int L, int batch, double* rmax, cudaStream_t st);
 int convert_d2f(const cxd* in, cxf* out, long long count, cudaStream_t st);
+// out = max(out, max_e |re x_e| + |im x_e|); out must be zeroed (or hold a
+// previous maximum) before the first call
+int maxabs_c64(const cxf* x, long long count, double* out, cudaStream_t st);
 int broadcast_f(const cxf* in, long long count, int batch, cxf* out, cudaStream_t st);  // out[b] = in
 int axpy_f2d(const cxf* d, cxd* x, long long count, cudaStream_t st);  // x += d
+
+// Complex64 GEMM on the tcgen05 tensor cores (3xTF32 split, FP32-class
+// accuracy); same argument meaning as gemm_batched. K must be positive.
+// batch2 > 1 adds an inner batch index (strides sA2, sB2, sC2): matrix
+// (outer o, inner q) starts at A + o sA + q sA2, and so on.
+int tc_gemm_c64(int M, int N, int K, cxf alpha, const cxf* A, long long lda, long long sA, const cxf* B,
+                long long ldb, long long sB, cxf beta, cxf* C, long long ldc, long long sC, int batch,
+                cudaStream_t st, int batch2 = 1, long long sA2 = 0, long long sB2 = 0, long long sC2 = 0);
+// Reads and clears the tensor-core GEMM's device error flag (set when an
+// mbarrier wait gave up); synchronizes the stream. Returns QBG_OK or QBG_ECUDA.
+int tc_check(cudaStream_t st);
+
+// Engine of the complex64 GEMMs inside gemm_batched<float> (LU trailing
+// updates, triangular-solve updates, refinement products): 0 = CUDA-core FMA
+// tiles, 1 = tcgen05 tensor cores. Process-wide.
+constexpr int GEMM_ENGINE_SIMT = 0;
+constexpr int GEMM_ENGINE_TCGEN05 = 1;
+void set_gemm_engine(int e);
+int gemm_engine();
 
 }  // namespace qbg

@@ -12,7 +12,8 @@ from .solvers import (DLP_kress, DLP_kress_global_corners, CFIE_kress, CFIE_kres
 from . import operators
 from .operators import (Workspace, build_workspace, assemble, assemble_noalloc, construct_matrices,
                         construct_boundary_matrices,
-                        construct_boundary_matrices_with_derivatives, bessel01, sigma_min)
+                        construct_boundary_matrices_with_derivatives, bessel01, sigma_min, cgemm,
+                        set_gemm_engine, launch_count)
 from .beyn import BeynHandle, construct_B_matrix, solve_vect, solve, probe_matrix, contour
 from .sweep import k_sweep, get_eigenvalues
 

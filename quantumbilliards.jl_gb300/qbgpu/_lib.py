@@ -59,14 +59,16 @@ class ChebParams(C.Structure):
 
 class BeynOpts(C.Structure):
     _fields_ = [("flags", C.c_int32), ("max_refine", C.c_int32), ("refine_tol", C.c_double), ("nb", C.c_int32),
-                ("eval_mode", C.c_int32), ("cheb", ChebParams)]
+                ("eval_mode", C.c_int32), ("cheb", ChebParams), ("fp32_sweeps", C.c_int32),
+                ("solve_block", C.c_int32)]
 
 
 class BeynStats(C.Structure):
     _fields_ = [("refine_sweeps", C.c_int32), ("refine_residual", C.c_double), ("singular", C.c_int32),
                 ("ms_assemble", C.c_double), ("ms_factor", C.c_double), ("ms_solve", C.c_double),
                 ("nhist", C.c_int32), ("refine_history", C.c_double * 8), ("ms_residual", C.c_double),
-                ("n_residual", C.c_int32)]
+                ("n_residual", C.c_int32), ("nfp32", C.c_int32), ("fp32_history", C.c_double * 4),
+                ("ms_solves", C.c_double), ("n_solves", C.c_int32)]
 
 
 # symbol -> (restype, argtypes); the list is the ABI surface the tests check
@@ -90,6 +92,11 @@ _SIGS = {
     "qbg_beyn_destroy": (C.c_int32, [C.c_void_p]),
     "qbg_sigma_min": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]),
     "qbg_bessel01": (C.c_int32, [C.POINTER(C.c_double), C.c_int64, C.c_int32, C.POINTER(C.c_double)]),
+    "qbg_cgemm_c64": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_float), C.c_void_p,
+                                  C.c_int64, C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.c_void_p, C.c_int64,
+                                  C.c_int32]),
+    "qbg_set_gemm_engine": (C.c_int32, [C.c_int32]),
+    "qbg_launch_count": (C.c_int32, [C.POINTER(C.c_uint64)]),
 }
 
 _lib = None

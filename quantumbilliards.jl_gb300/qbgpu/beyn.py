@@ -39,12 +39,14 @@ class BeynHandle:
     """Contour nodes assembled and factored on the device (owns a qbg_beyn)."""
 
     def __init__(self, ws: Workspace, k0: complex, R: float, nq: int, mixed: bool = False, max_refine: int = 4,
-                 refine_tol: float = 1e-7, nb: int = 0, use_chebyshev: bool = True, cheb=None):
+                 refine_tol: float = 1e-6, nb: int = 0, use_chebyshev: bool = True, cheb=None, fp32_sweeps: int = 0,
+                 solve_block: int = 0):
         lib = L.load()
         self.ws, self.k0, self.R, self.nq = ws, complex(k0), float(R), int(nq)
         self.prec = L.prec_code(mixed)
         cp = L.ChebParams(*(cheb if cheb else (0, 0, 0, 0)))
-        o = L.BeynOpts(0, int(max_refine), float(refine_tol), int(nb), 0 if use_chebyshev else 1, cp)
+        o = L.BeynOpts(0, int(max_refine), float(refine_tol), int(nb), 0 if use_chebyshev else 1, cp,
+                       int(fp32_sweeps), int(solve_block))
         h = C.c_void_p()
         L.check(lib.qbg_beyn_create(ws.handle, self.k0.real, self.k0.imag, self.R, self.nq, self.prec, C.byref(o),
                                     C.byref(h)))
@@ -65,7 +67,9 @@ class BeynHandle:
         self.last_stats = dict(refine_sweeps=st.refine_sweeps, refine_residual=st.refine_residual,
                                singular=st.singular, ms_assemble=st.ms_assemble, ms_factor=st.ms_factor,
                                ms_solve=st.ms_solve, refine_history=list(st.refine_history[:st.nhist]),
-                               ms_residual=st.ms_residual, n_residual=st.n_residual)
+                               ms_residual=st.ms_residual, n_residual=st.n_residual,
+                               fp32_history=list(st.fp32_history[:st.nfp32]), ms_solves=st.ms_solves,
+                               n_solves=st.n_solves)
         return A0, A1
 
     def close(self):
@@ -81,8 +85,8 @@ class BeynHandle:
 
 
 def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=None, mixed=False, ws=None,
-                       max_refine=4, refine_tol=1e-7, return_info=False, regrow="extend", use_chebyshev=True,
-                       cheb=None):
+                       max_refine=4, refine_tol=1e-6, return_info=False, regrow="extend", use_chebyshev=True,
+                       cheb=None, fp32_sweeps=0, solve_block=0):
     """construct_B_matrix (beyn.jl:257-322). Returns (B, Uk) [, info].
 
     regrow: when the rank saturates (rk == r) the reference draws a fresh
@@ -94,7 +98,8 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
     ws = ws if ws is not None else Workspace(solver, pts)
     if ws.dim != N:
         raise ValueError(f"N={N} does not match the operator dimension {ws.dim}")
-    bh = BeynHandle(ws, k0, R, nq, mixed, max_refine, refine_tol, use_chebyshev=use_chebyshev, cheb=cheb)
+    bh = BeynHandle(ws, k0, R, nq, mixed, max_refine, refine_tol, use_chebyshev=use_chebyshev, cheb=cheb,
+                    fp32_sweeps=fp32_sweeps, solve_block=solve_block)
     info = dict(stats=[])
     try:
         V = probe_matrix(N, r, rng)

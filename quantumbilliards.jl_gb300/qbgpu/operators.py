@@ -163,6 +163,45 @@ def bessel01(z, f32: bool = False) -> np.ndarray:
     return out.reshape(-1, 4)
 
 
+def cgemm(A, B, C=None, alpha=1.0, beta=0.0, engine: int = 1) -> np.ndarray:
+    """Device complex64 GEMM alpha A B + beta C (validation helper).
+
+    A: (M, K) or (batch, M, K); B: (K, N) or (batch, K, N). engine 0 = CUDA-core
+    FMA tiles, 1 = tcgen05 tensor cores (the engine of the FP32 LU)."""
+    lib = L.load()
+    A = np.asarray(A, dtype=np.complex64)
+    B = np.asarray(B, dtype=np.complex64)
+    single = A.ndim == 2
+    if single:
+        A, B = A[None], B[None]
+    nb, M, K = A.shape
+    N = B.shape[2]
+    if B.shape[:2] != (nb, K):
+        raise ValueError("A and B shapes do not chain")
+    Cin = np.zeros((nb, M, N), np.complex64) if C is None else np.asarray(C, np.complex64).reshape(nb, M, N)
+    a = np.ascontiguousarray(A.transpose(0, 2, 1))  # column-major per matrix
+    b = np.ascontiguousarray(B.transpose(0, 2, 1))
+    c = np.array(Cin.transpose(0, 2, 1), order="C", copy=True)  # never write into the caller's C
+    al = np.array([complex(alpha).real, complex(alpha).imag], np.float32)
+    be = np.array([complex(beta).real, complex(beta).imag], np.float32)
+    L.check(lib.qbg_cgemm_c64(int(engine), M, N, K, al.ctypes.data_as(L.C.POINTER(L.C.c_float)), L.vptr(a), M,
+                              L.vptr(b), K, be.ctypes.data_as(L.C.POINTER(L.C.c_float)), L.vptr(c), M, nb))
+    out = c.transpose(0, 2, 1)
+    return out[0] if single else out
+
+
+def launch_count() -> int:
+    """Kernels launched by the library in this process (its own kernels, not cuSOLVER's)."""
+    c = L.C.c_uint64(0)
+    L.check(L.load().qbg_launch_count(L.C.byref(c)))
+    return int(c.value)
+
+
+def set_gemm_engine(engine: int) -> None:
+    """Engine of the complex64 GEMMs in the FP32 LU and solves (0 FMA tiles, 1 tcgen05)."""
+    L.check(L.load().qbg_set_gemm_engine(int(engine)))
+
+
 def sigma_min(ws: Workspace, ks) -> np.ndarray:
     lib = L.load()
     k = np.ascontiguousarray(np.atleast_1d(np.asarray(ks, dtype=np.float64)))
