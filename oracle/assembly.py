@@ -5,7 +5,9 @@ Follows:
 * cfie_geom_cache                        boundarypoints.jl:854-880
 * construct_fredholm_matrix!             dlp_kress.jl:906-932
 * construct_dlp_matrix_derivatives!      dlp_kress.jl:975-1019 (real k)
-* CFIE construct_matrices!               cfie_kress.jl:416-510
+* CFIE construct_matrices!               cfie_kress.jl:416-510, derivatives :619-757
+* symmetry orbits                        symmetry.jl:214-319
+* reduced DLP (images)                   dlp_kress.jl:1081-1100, 1151-1189, 1293-1345
 * complex-k multi-k CFIE (Chebyshev)     chebyshev_euclidian_helmholtz_cfie_kress.jl:543-666
 * complex-k DLP (Chebyshev)              chebyshev_euclidian_helmholtz_dlp_kress.jl:702-769
 
@@ -182,11 +184,165 @@ def cfie_matrix(pts, k, funcs_same=None, funcs_off=None):
     return A
 
 
+def cfie_matrix_derivs(pts, k, funcs_same=None, funcs_off=None):
+    """(A, dA/dk, d2A/dk2) over all components (cfie_kress.jl:619-757; the
+    Chebyshev route chebyshev_euclidian_helmholtz_cfie_kress.jl:881-1060 uses
+    the same expressions). The off-component double-layer derivatives carry
+    the sign written there (cfie_kress.jl:729-731)."""
+    offs = component_offsets(pts)
+    Nt = offs[-1]
+    A = np.zeros((Nt, Nt), dtype=np.complex128)
+    A1 = np.zeros_like(A)
+    A2 = np.zeros_like(A)
+    ik = 1j * k
+    aL1 = -k * INV_TWO_PI
+    aL2 = 0.5j * k
+    aM1 = -INV_TWO_PI
+    aM2 = 0.5j
+    pi = math.pi
+    for a, p in enumerate(pts):
+        g = geom_cache(p)
+        Rm = kress_R(p.n)
+        r, invr, lt, inn = g["R"], g["invR"], g["logterm"], g["inner"]
+        s = g["speed"][None, :]
+        h0, h1, j0, j1 = funcs_same[a] if funcs_same is not None else _bessels(k, r)
+        w = p.ws[None, :]
+        kr = k * r
+        l1 = aL1 * inn * j1 * invr
+        l2 = aL2 * inn * h1 * invr - l1 * lt
+        dval = Rm * l1 + w * l2
+        dval1 = Rm * (-(inn * k * j0) * INV_TWO_PI) + w * ((inn * k * (lt * j0 + 1j * pi * h0)) * INV_TWO_PI)
+        dval2 = Rm * ((inn * (kr * j1 - j0)) * INV_TWO_PI) + \
+            w * ((inn * (lt * (j0 - kr * j1) + 1j * pi * (h0 - kr * h1))) * INV_TWO_PI)
+        m1 = aM1 * j0 * s
+        m2 = aM2 * h0 * s - m1 * lt
+        sval = Rm * m1 + w * m2
+        m1_1 = (r * s * j1) * INV_TWO_PI
+        m1_2 = (r * s * (kr * j0 - j1)) * INV_TWO_PI / k
+        m2_1 = -(r * s * (lt * j1 + 1j * pi * h1)) * INV_TWO_PI
+        m2_2 = (r * s * (lt * (j1 - kr * j0) - 1j * pi * kr * h0 + 1j * pi * h1)) * INV_TWO_PI / k
+        sval1 = Rm * m1_1 + w * m2_1
+        sval2 = Rm * m1_2 + w * m2_2
+        blk = -(dval + ik * sval)
+        blk1 = -(dval1 + 1j * sval + ik * sval1)
+        blk2 = -(dval2 + 2j * sval1 + ik * sval2)
+        # diagonal (cfie_kress.jl:636-646)
+        si, ki, wi = g["speed"], g["kappa"], p.ws
+        m2d = ((0.5j - EULER_OVER_PI) - INV_TWO_PI * np.log((k ** 2 / 4) * si ** 2 + 0j)) * si
+        sd = np.diag(Rm) * (aM1 * si) + wi * m2d
+        sd1 = wi * (-(si / (pi * k)))
+        sd2 = wi * (si / (pi * k ** 2))
+        np.fill_diagonal(blk, 1.0 - (wi * ki + ik * sd))
+        np.fill_diagonal(blk1, -(1j * sd + ik * sd1))
+        np.fill_diagonal(blk2, -(2j * sd1 + ik * sd2))
+        sl = slice(offs[a], offs[a + 1])
+        A[sl, sl], A1[sl, sl], A2[sl, sl] = blk, blk1, blk2
+    for a, pa in enumerate(pts):
+        for b, pb in enumerate(pts):
+            if a == b:
+                continue
+            dx = pa.xy[:, 0][:, None] - pb.xy[:, 0][None, :]
+            dy = pa.xy[:, 1][:, None] - pb.xy[:, 1][None, :]
+            r = np.hypot(dx, dy)
+            invr = 1.0 / r
+            inn = pb.tangent[:, 1][None, :] * dx - pb.tangent[:, 0][None, :] * dy
+            sb = np.hypot(pb.tangent[:, 0], pb.tangent[:, 1])[None, :]
+            h0, h1 = funcs_off[(a, b)] if funcs_off is not None else (sp.hankel1(0, k * r), sp.hankel1(1, k * r))
+            wj = pb.ws[None, :]
+            dval = wj * (aL2 * inn * h1 * invr)
+            dval1 = wj * (-0.5j * inn * k * h0)
+            dval2 = wj * (-0.5j * inn * (h0 - k * r * h1))
+            sval = wj * (aM2 * h0 * sb)
+            sval1 = wj * (-0.5j * r * h1 * sb)
+            sval2 = wj * (0.5j * r * (h1 - k * r * h0) * sb / k)
+            sa, sb_ = slice(offs[a], offs[a + 1]), slice(offs[b], offs[b + 1])
+            A[sa, sb_] = -(dval + ik * sval)
+            A1[sa, sb_] = -(dval1 + 1j * sval + ik * sval1)
+            A2[sa, sb_] = -(dval2 + 2j * sval1 + ik * sval2)
+    return A, A1, A2
+
+
+# --------------------------------------------------------------------------
+# symmetry-reduced DLP
+# --------------------------------------------------------------------------
+def periodic_symmetry_index_orbits(N: int, sym):
+    """Orbits of a cyclic node index under a reflection or rotation
+    (symmetry.jl:214-319), 0-based. ``sym`` is ("x", p) (x -> -x),
+    ("y", p) (y -> -y), ("xy", px, py) or ("rot", n, m).
+    Returns (fund, fund_to_full [m, norb], fund_to_scale [m, norb])."""
+    kind = sym[0]
+    if kind in ("x", "y"):
+        if N % 2:
+            raise ValueError("reflection symmetry needs even N")
+        m = N // 2
+        orb = lambda q: ([q, (N - q - 1) % N], [1.0, float(sym[1])])
+    elif kind == "xy":
+        if N % 4:
+            raise ValueError("XY reflection needs N divisible by 4")
+        m = N // 4
+        px, py = float(sym[1]), float(sym[2])
+        orb = lambda q: ([q, (N // 2 - q - 1) % N, (N - q - 1) % N, (q + N // 2) % N], [1.0, px, py, px * py])
+    elif kind == "rot":
+        n, mm = int(sym[1]), int(sym[2])
+        if N % n:
+            raise ValueError("rotation order must divide N")
+        m = N // n
+        chi = [complex(math.cos(2 * math.pi * mm * l / n), math.sin(2 * math.pi * mm * l / n)) for l in range(n)]
+        orb = lambda q: ([(q + l * (N // n)) % N for l in range(n)], chi)
+    else:
+        raise ValueError(kind)
+    fund = np.arange(m)
+    qs, ss = zip(*(orb(q) for q in fund))
+    full = np.array(qs, dtype=np.int64)
+    scale = np.array(ss, dtype=np.complex128)
+    seen = np.zeros(N, dtype=np.int64)
+    np.add.at(seen, full.ravel(), 1)
+    if not np.all(seen == 1):
+        raise ValueError("orbits do not partition the nodes")
+    return fund, full, scale
+
+
+def dlp_fredholm_reduced(p, k, orbits, derivs: bool = False, funcs=None, image_h=None):
+    """Reduced F = I - D_red on the fundamental indices (dlp_kress.jl:1151-1189;
+    derivatives :1293-1345): the Kress-split entry of D at (I_a, I_b) plus the
+    regular image kernels of the other orbit members of I_b."""
+    fund, full, scale = orbits
+    m = len(fund)
+    res = dlp_fredholm(p, k, derivs, funcs)
+    Ffull = res if not derivs else res[0]
+    idx = np.ix_(fund, fund)
+    F = Ffull[idx].copy()
+    if derivs:
+        F1, F2 = res[1][idx].copy(), res[2][idx].copy()
+    X, Y = p.xy[:, 0], p.xy[:, 1]
+    dX, dY = p.tangent[:, 0], p.tangent[:, 1]
+    sp_ = np.hypot(dX, dY)
+    nx, ny = dY / sp_, -dX / sp_
+    xi, yi = X[fund][:, None], Y[fund][:, None]
+    for l in range(full.shape[1]):
+        q = full[:, l]
+        sc = scale[:, l][None, :]
+        skip = (q == fund)[None, :]
+        dx = xi - X[q][None, :]
+        dy = yi - Y[q][None, :]
+        r = np.hypot(dx, dy)
+        rs = np.where(r < np.finfo(float).eps, 1.0, r)
+        c = (nx[q][None, :] * dx + ny[q][None, :] * dy) / rs
+        wq = (sp_[q] * p.ws[q])[None, :]
+        h0, h1 = image_h(rs) if image_h is not None else (sp.hankel1(0, k * rs), sp.hankel1(1, k * rs))
+        mask = (~skip) & (r >= np.finfo(float).eps)
+        F -= np.where(mask, sc * (0.5j * k) * c * h1 * wq, 0.0)
+        if derivs:
+            kr = k * rs
+            F1 -= np.where(mask, sc * 0.5j * c * (kr * h0) * wq, 0.0)
+            F2 -= np.where(mask, sc * 0.5j * c * (rs * h0 - k * rs ** 2 * h1) * wq, 0.0)
+    return (F, F1, F2) if derivs else F
+
+
 def assemble(kind, pts, k, derivs=False):
     """Single entry used by the tests: 'dlp' -> one component, 'cfie' -> list."""
     if kind == "dlp":
         p = pts[0] if isinstance(pts, list) else pts
         return dlp_fredholm(p, k, derivs)
-    if derivs:
-        raise NotImplementedError
-    return cfie_matrix(pts if isinstance(pts, list) else [pts], k)
+    pl = pts if isinstance(pts, list) else [pts]
+    return cfie_matrix_derivs(pl, k) if derivs else cfie_matrix(pl, k)

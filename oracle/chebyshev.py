@@ -123,3 +123,43 @@ def dlp_fredholm(p, k, params=(15000, 5, 3000, 5), derivs=False):
     rmin, rmax = r_range([p])
     R = OA.geom_cache(p)["R"]
     return OA.dlp_fredholm(p, k, derivs=derivs, funcs=funcs(k, R, rmin, rmax, params, 0.0))
+
+
+def cfie_matrix_derivs(pts, k, params=(15000, 5, 3000, 5)):
+    """(A, A', A'') with interpolated H0, H1, J0, J1
+    (chebyshev_euclidian_helmholtz_cfie_kress.jl:881-1060)."""
+    pts = pts if isinstance(pts, list) else [pts]
+    rmin, rmax = r_range(pts)
+    same, off = {}, {}
+    for a, p in enumerate(pts):
+        same[a] = funcs(k, OA.geom_cache(p)["R"], rmin, rmax, params, 0.2)
+    for a, pa in enumerate(pts):
+        for b, pb in enumerate(pts):
+            if a != b:
+                R = np.hypot(pa.xy[:, 0][:, None] - pb.xy[:, 0][None, :], pa.xy[:, 1][:, None] - pb.xy[:, 1][None, :])
+                h0, h1, _, _ = funcs(k, R, rmin, rmax, params, 0.2)
+                off[(a, b)] = (h0, h1)
+    return OA.cfie_matrix_derivs(pts, k, funcs_same=same, funcs_off=off)
+
+
+def dlp_fredholm_reduced(p, k, orbits, params=(15000, 5, 3000, 5), derivs=False):
+    """Symmetry-reduced DLP with the H/J panels for the Kress-split entries and
+    the H panels for the image kernels
+    (chebyshev_euclidian_helmholtz_dlp_kress.jl:771-847, 953-1054)."""
+    rmin, rmax = r_range([p])
+    nh, Mh, _, _ = params
+    h0p = Plan(k, rmin, rmax, nh, Mh, lambda z: sp.hankel1(0, z))
+    h1p = Plan(k, rmin, rmax, nh, Mh, lambda z: sp.hankel1(1, z))
+
+    def image_h(r):
+        rr = r.ravel()
+        h0, h1 = h0p(rr), h1p(rr)
+        d = rr < rmin
+        if np.any(d):
+            h0[d] = sp.hankel1(0, k * rr[d])
+            h1[d] = sp.hankel1(1, k * rr[d])
+        return h0.reshape(r.shape), h1.reshape(r.shape)
+
+    R = OA.geom_cache(p)["R"]
+    return OA.dlp_fredholm_reduced(p, k, orbits, derivs=derivs, funcs=funcs(k, R, rmin, rmax, params, 0.0),
+                                   image_h=image_h)

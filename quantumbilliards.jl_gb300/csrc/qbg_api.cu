@@ -415,7 +415,7 @@ static int beyn_create_impl(qbg_beyn* b, double k0_re, double k0_im, double R) {
     QBG_CUDA(cudaStreamSynchronize(st));  // keep lp alive until the copy has run
   }
   QBG_CUDA(cudaEventRecord(b->ev[0], st));
-  const bool use_cheb = b->opts.eval_mode == 0 && b->prec != QBG_PREC_FP32 && b->g->d.m == b->g->d.n;
+  const bool use_cheb = b->opts.eval_mode == 0 && b->prec != QBG_PREC_FP32;
   if (use_cheb) {
     const qbg_cheb_params cp = cheb_defaults(&b->opts.cheb);
     QBG_TRY(cheb_params_check(&cp));
@@ -465,10 +465,6 @@ qbg_status qbg_beyn_create(qbg_geom* g, double k0_re, double k0_im, double R, in
     return QBG_EINVAL;
   }
   *out = nullptr;
-  if (g->d.m != g->d.n && prec != 0) {
-    set_error("symmetry-reduced Beyn runs in the FP64 form only");
-    return QBG_ENOTSUP;
-  }
   qbg_beyn* b = new (std::nothrow) qbg_beyn();
   if (!b) { set_error("host allocation failed"); return QBG_ENOMEM; }
   b->g = g;

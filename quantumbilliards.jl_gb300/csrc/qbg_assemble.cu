@@ -75,6 +75,19 @@ static __device__ __forceinline__ void entry_vals(const PairGeom& p, cxd k, cxd 
     cxd dval = (p.wj * p.inn * p.invr) * (aL2 * h1);
     cxd sval = (p.wj * p.sj) * cmul_i(0.5 * h0);
     *F = -(dval + ik * sval);
+    if (DERIV) {
+      // cfie_kress.jl:729-734 (and the Chebyshev route,
+      // chebyshev_euclidian_helmholtz_cfie_kress.jl:1041-1045): the k-derivatives
+      // of the double-layer part carry the sign written there
+      const cxd kr = p.r * k;
+      const double cD = p.wj * p.inn, cS = p.wj * p.sj;
+      cxd dval1 = cmul_i(-0.5 * cD * (k * h0));
+      cxd dval2 = cmul_i(-0.5 * cD * (h0 - kr * h1));
+      cxd sval1 = cmul_i(-0.5 * cS * p.r * h1);
+      cxd sval2 = cmul_i(0.5 * cS * p.r * (h1 - kr * h0)) / k;
+      *F1 = -(dval1 + cmul_i(sval) + ik * sval1);
+      *F2 = -(dval2 + cmul_i(2.0 * sval1) + ik * sval2);
+    }
     return;
   }
   const double cD1 = p.Rk * p.inn * p.invr, cD2 = p.wj * p.inn * p.invr, cD3 = p.wj * p.lt * p.inn * p.invr;
@@ -99,6 +112,26 @@ static __device__ __forceinline__ void entry_vals(const PairGeom& p, cxd k, cxd 
     const cxd M1 = (-inv2pi) * j0, M2 = cmul_i(0.5 * h0);
     cxd sval = cS1 * M1 + cS2 * M2 - cS3 * M1;
     *F = -(dval + ik * sval);
+    if (DERIV) {
+      // cfie_kress.jl:658-681
+      const double pi = 3.14159265358979323846;
+      const cxd kr = p.r * k;
+      cxd l1_1 = (-p.inn * inv2pi) * (k * j0);
+      cxd l2_1 = (p.inn * inv2pi) * (k * (p.lt * j0 + cmul_i(pi * h0)));
+      cxd l1_2 = (p.inn * inv2pi) * (kr * j1 - j0);
+      cxd l2_2 = (p.inn * inv2pi) * (p.lt * (j0 - kr * j1) + cmul_i(pi * (h0 - kr * h1)));
+      const cxd dval1 = p.Rk * l1_1 + p.wj * l2_1;
+      const cxd dval2 = p.Rk * l1_2 + p.wj * l2_2;
+      const double rs = p.r * p.sj * inv2pi;
+      cxd m1_1 = rs * j1;
+      cxd m1_2 = (rs * (kr * j0 - j1)) / k;
+      cxd m2_1 = (-rs) * (p.lt * j1 + cmul_i(pi * h1));
+      cxd m2_2 = (rs * (p.lt * (j1 - kr * j0) + cmul_i(pi * (h1 - kr * h0)))) / k;
+      const cxd sval1 = p.Rk * m1_1 + p.wj * m2_1;
+      const cxd sval2 = p.Rk * m1_2 + p.wj * m2_2;
+      *F1 = -(dval1 + cmul_i(sval) + ik * sval1);
+      *F2 = -(dval2 + cmul_i(2.0 * sval1) + ik * sval2);
+    }
   }
 }
 
@@ -112,6 +145,28 @@ static __device__ __forceinline__ void entry_fp64(const PairGeom& p, cxd k, bool
     b.j1.im = 0.0;
   }
   entry_vals<FORM, DERIV>(p, k, b.h0(), b.h1(), b.j0, b.j1, F, F1, F2);
+}
+
+// diagonal and its k-derivatives (DLP: zero; CFIE: cfie_kress.jl:636-646)
+template <int FORM>
+static __device__ __forceinline__ void diag_derivs(const GeomDev& g, int i, cxd k, cxd* F1, cxd* F2) {
+  if (FORM == 0) {
+    *F1 = cxd(0.0, 0.0);
+    *F2 = cxd(0.0, 0.0);
+    return;
+  }
+  const double inv2pi = 0.15915494309189533577, euler_over_pi = 0.18373345259830797886;
+  const double pi = 3.14159265358979323846;
+  const double wi = g.ws[i], si = g.speed[i];
+  const double rii = g.kcol[g.coff[g.comp[i]]];
+  const cxd ik = cmul_i(k);
+  cxd lg = clog_d((0.25 * si * si) * (k * k));
+  cxd m2 = (cxd(-euler_over_pi, 0.5) - inv2pi * lg) * si;
+  const cxd sval = cxd(rii * (-inv2pi * si), 0.0) + wi * m2;
+  const cxd sval1 = cxd(-wi * si / pi, 0.0) / k;
+  const cxd sval2 = cxd(wi * si / pi, 0.0) / (k * k);
+  *F1 = -(cmul_i(sval) + ik * sval1);
+  *F2 = -(cmul_i(2.0 * sval1) + ik * sval2);
 }
 
 template <int FORM>
@@ -142,16 +197,16 @@ __global__ void __launch_bounds__(256) k_assemble_fp64(GeomDev g, const cxd* __r
   if (i == j) {
     for (int q = 0; q < nk; ++q) {
       outs[q][off] = diag_fp64<FORM>(g, i, ks[q]);
-      if (DERIV) {
-        outs[nk + q][off] = cxd(0.0, 0.0);
-        outs[2 * nk + q][off] = cxd(0.0, 0.0);
-      }
+      if (DERIV) diag_derivs<FORM>(g, i, ks[q], &outs[nk + q][off], &outs[2 * nk + q][off]);
     }
     return;
   }
   PairGeom p = pair_geom(g, i, j);
   if (FORM == 1 && !p.same && p.r * p.r <= 4.93038065763132e-32) {  // eps(T)^2 guard, cfie_kress.jl:494
-    for (int q = 0; q < nk; ++q) outs[q][off] = cxd(0.0, 0.0);
+    for (int q = 0; q < nk; ++q) {
+      outs[q][off] = cxd(0.0, 0.0);
+      if (DERIV) { outs[nk + q][off] = cxd(0.0, 0.0); outs[2 * nk + q][off] = cxd(0.0, 0.0); }
+    }
     return;
   }
   for (int q = 0; q < nk; ++q) {
@@ -263,10 +318,38 @@ __global__ void __launch_bounds__(256) k_assemble_fp32(GeomDev g, const cxd* __r
 // D_red[a,b] = D_full[I_a, I_b] (Kress split) + sum over images q != I_b of
 // scale_q (ik/2) c H1(kr) |t_q| w_q, c = n_q.(x_i - x_q)/r.
 // ---------------------------------------------------------------------------
+// value store for the entry at `off`: OUT 0 = complex128, 1 = complex64 hi
+// (+ lo = fl32(v - hi) when los != nullptr)
+template <int OUT>
+static __device__ __forceinline__ void store_entry(void* const* outs, void* const* los, int slot, size_t off,
+                                                   cxd v) {
+  if (OUT == 0) {
+    reinterpret_cast<cxd*>(outs[slot])[off] = v;
+  } else {
+    const cxf hi(v);
+    reinterpret_cast<cxf*>(outs[slot])[off] = hi;
+    if (los) reinterpret_cast<cxf*>(los[slot])[off] = cxf((float)(v.re - (double)hi.re), (float)(v.im - (double)hi.im));
+  }
+}
+
+// regular image kernel of orbit member qn seen from node (xi, yi), subtracted
+// from F = I - D (dlp_kress.jl:1081-1100): D += sc (ik/2) c H1(kr) speed_q w_q,
+// dD/dk = sc (i/2) c kr H0 speed_q w_q, d2D/dk2 = sc (i/2) c (r H0 - k r^2 H1) speed_q w_q
 template <int DERIV>
-__global__ void __launch_bounds__(256) k_assemble_dlp_reduced_fp64(GeomDev g, const cxd* __restrict__ ks,
-                                                                   int nk, cxd* const* __restrict__ outs,
-                                                                   long long ld) {
+static __device__ __forceinline__ void image_terms(double c, double wq, cxd sc, double r, cxd k, cxd h0, cxd h1,
+                                                   cxd& F, cxd& F1, cxd& F2) {
+  F -= (c * wq) * (sc * (cmul_i(0.5 * k) * h1));
+  if (DERIV) {
+    const cxd kr = r * k;
+    F1 -= (c * wq) * (sc * cmul_i(0.5 * (kr * h0)));
+    F2 -= (c * wq) * (sc * cmul_i(0.5 * (r * h0 - (r * r) * (k * h1))));
+  }
+}
+
+template <int DERIV, int OUT>
+__global__ void __launch_bounds__(256) k_assemble_dlp_reduced(GeomDev g, const cxd* __restrict__ ks, int nk,
+                                                              void* const* __restrict__ outs,
+                                                              void* const* __restrict__ los, long long ld) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   const int bcol = blockIdx.y * blockDim.y + threadIdx.y;
   if (a >= g.m || bcol >= g.m) return;
@@ -284,7 +367,6 @@ __global__ void __launch_bounds__(256) k_assemble_dlp_reduced_fp64(GeomDev g, co
     } else {
       entry_fp64<0, DERIV>(p, k, realk, &F, &F1, &F2);
     }
-    // image contributions (regular kernel), subtracted because F = I - D
     for (int l = 0; l < g.norb; ++l) {
       const int qn = g.orb[bcol * g.norb + l];
       if (qn == j) continue;
@@ -293,21 +375,13 @@ __global__ void __launch_bounds__(256) k_assemble_dlp_reduced_fp64(GeomDev g, co
       if (r < 2.220446049250313e-16) continue;
       const double c = (g.nx[qn] * dxq + g.ny[qn] * dyq) / r;
       const cxd sc(g.orb_scale[2 * (bcol * g.norb + l)], g.orb_scale[2 * (bcol * g.norb + l) + 1]);
-      const double wq = g.speed[qn] * g.ws[qn];
-      Bessel01d bb = bessel01(r * k);
-      if (realk) { bb.j0.im = 0.0; bb.j1.im = 0.0; }
-      const cxd h0 = bb.h0(), h1 = bb.h1();
-      F -= (c * wq) * (sc * (cmul_i(0.5 * k) * h1));
-      if (DERIV) {
-        const cxd kr = r * k;
-        F1 -= (c * wq) * (sc * cmul_i(0.5 * (kr * h0)));
-        F2 -= (c * wq) * (sc * cmul_i(0.5 * (r * h0 - (r * r) * (k * h1))));
-      }
+      const Bessel01d bb = bessel01(r * k);
+      image_terms<DERIV>(c, g.speed[qn] * g.ws[qn], sc, r, k, bb.h0(), bb.h1(), F, F1, F2);
     }
-    outs[q][off] = F;
+    store_entry<OUT>(outs, los, q, off, F);
     if (DERIV) {
-      outs[nk + q][off] = F1;
-      outs[2 * nk + q][off] = F2;
+      store_entry<OUT>(outs, los, nk + q, off, F1);
+      store_entry<OUT>(outs, los, 2 * nk + q, off, F2);
     }
   }
 }
@@ -463,13 +537,21 @@ __global__ void __launch_bounds__(256) k_assemble_cheb(GeomDev g, ChebTables t, 
   if (i == j) {
     for (int q = q0; q < q1; ++q) {
       store(q, diag_fp64<FORM>(g, i, ks[q]));
-      if (DERIV) { store(nk + q, cxd(0.0, 0.0)); store(2 * nk + q, cxd(0.0, 0.0)); }
+      if (DERIV) {
+        cxd d1, d2;
+        diag_derivs<FORM>(g, i, ks[q], &d1, &d2);
+        store(nk + q, d1);
+        store(2 * nk + q, d2);
+      }
     }
     return;
   }
   const PairGeom p = pair_geom(g, i, j);
   if (FORM == 1 && !p.same && p.r * p.r <= 4.93038065763132e-32) {
-    for (int q = q0; q < q1; ++q) store(q, cxd(0.0, 0.0));
+    for (int q = q0; q < q1; ++q) {
+      store(q, cxd(0.0, 0.0));
+      if (DERIV) { store(nk + q, cxd(0.0, 0.0)); store(2 * nk + q, cxd(0.0, 0.0)); }
+    }
     return;
   }
   int ph, pj;
@@ -494,6 +576,77 @@ __global__ void __launch_bounds__(256) k_assemble_cheb(GeomDev g, ChebTables t, 
     entry_vals<FORM, DERIV>(p, k, h0, h1, j0, j1, &F, &F1, &F2);
     store(q, F);
     if (DERIV) { store(nk + q, F1); store(2 * nk + q, F2); }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Symmetry-reduced DLP through the Chebyshev panels (the reduced multi-k route,
+// chebyshev_euclidian_helmholtz_dlp_kress.jl:771-847, derivatives :953-1054):
+// entry (a, b) = Kress-split entry of the full operator at (fund[a], fund[b])
+// minus the regular image kernels of the other members of orbit b. Image
+// distances are node-pair distances of the full boundary, so they lie inside
+// the panel range [rmin, rmax] built over all pairs.
+// ---------------------------------------------------------------------------
+static __device__ __forceinline__ void cheb_h01(const ChebTables& t, int q, double r, cxd k, cxd& h0, cxd& h1) {
+  const double az = r * hypot(k.re, k.im);
+  if (r < t.rmin || az < t.small_cut) {
+    const Bessel01d b = bessel01(r * k);
+    h0 = b.h0();
+    h1 = b.h1();
+    return;
+  }
+  int ph;
+  double th;
+  panel_of(r, t.rmin, t.rmax, t.dr_h, t.invdr_h, t.nh, ph, th);
+  clenshaw2(t.H + (((size_t)q * t.nh + ph) * (t.Mh + 1)) * 2, t.Mh, th, h0, h1);
+}
+
+template <int DERIV, int OUT>
+__global__ void __launch_bounds__(256) k_assemble_cheb_reduced(GeomDev g, ChebTables t, const cxd* __restrict__ ks,
+                                                               int nk, int kchunk, void* const* __restrict__ outs,
+                                                               void* const* __restrict__ los, long long ld) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const int bcol = blockIdx.y * blockDim.y + threadIdx.y;
+  if (a >= g.m || bcol >= g.m) return;
+  const int q0 = blockIdx.z * kchunk, q1 = min(nk, q0 + kchunk);
+  const int i = g.fund[a], j = g.fund[bcol];
+  const size_t off = (size_t)a + (size_t)bcol * (size_t)ld;
+  const double xi = g.x[i], yi = g.y[i];
+  PairGeom p;
+  int pj = 0;
+  double tj = 0.0;
+  if (i != j) {
+    p = pair_geom(g, i, j);
+    panel_of(p.r, 0.0, t.rmax, t.dr_j, t.invdr_j, t.nj, pj, tj);
+  }
+  for (int q = q0; q < q1; ++q) {
+    const cxd k = ks[q];
+    cxd F, F1(0.0, 0.0), F2(0.0, 0.0);
+    if (i == j) {
+      F = cxd(1.0 - g.ws[i] * g.kappa[i], 0.0);
+    } else {
+      cxd h0, h1, j0, j1;
+      cheb_h01(t, q, p.r, k, h0, h1);
+      clenshaw2(t.J + (((size_t)q * t.nj + pj) * (t.Mj + 1)) * 2, t.Mj, tj, j0, j1);
+      entry_vals<0, DERIV>(p, k, h0, h1, j0, j1, &F, &F1, &F2);
+    }
+    for (int l = 0; l < g.norb; ++l) {
+      const int qn = g.orb[bcol * g.norb + l];
+      if (qn == j) continue;
+      const double dxq = xi - g.x[qn], dyq = yi - g.y[qn];
+      const double r = hypot(dxq, dyq);
+      if (r < 2.220446049250313e-16) continue;
+      const double c = (g.nx[qn] * dxq + g.ny[qn] * dyq) / r;
+      const cxd sc(g.orb_scale[2 * (bcol * g.norb + l)], g.orb_scale[2 * (bcol * g.norb + l) + 1]);
+      cxd h0, h1;
+      cheb_h01(t, q, r, k, h0, h1);
+      image_terms<DERIV>(c, g.speed[qn] * g.ws[qn], sc, r, k, h0, h1, F, F1, F2);
+    }
+    store_entry<OUT>(outs, los, q, off, F);
+    if (DERIV) {
+      store_entry<OUT>(outs, los, nk + q, off, F1);
+      store_entry<OUT>(outs, los, 2 * nk + q, off, F2);
+    }
   }
 }
 
@@ -669,19 +822,32 @@ int cheb_build(ChebTables& t, const cxd* ks, cudaStream_t st) {
 
 int launch_assemble_cheb(const GeomDev& g, const ChebTables& t, const cxd* ks, int nk, int deriv, int prec,
                          void* const* outs_dev, void* const* lo_outs_dev, long long ld, cudaStream_t st) {
-  if (g.m != g.n) {
-    set_error("Chebyshev-panel assembly of the symmetry-reduced operator is not available; use direct evaluation");
-    return QBG_ENOTSUP;
-  }
   if (prec == QBG_PREC_FP32) {
     set_error("the FP32 form evaluates its kernel values directly (no Chebyshev panels)");
     return QBG_ENOTSUP;
   }
-  if (deriv && (g.form != 0 || prec != QBG_PREC_FP64)) {
-    set_error("Chebyshev derivative assembly is available for DLP in FP64");
+  if (deriv && prec != QBG_PREC_FP64) {
+    set_error("Chebyshev derivative assembly is available in FP64");
     return QBG_ENOTSUP;
   }
   const int kchunk = 8;
+  if (g.m != g.n) {
+    if (g.form != 0) {
+      set_error("symmetry reduction is built for the DLP formulation");
+      return QBG_ENOTSUP;
+    }
+    dim3 blk(32, 8), grd((g.m + 31) / 32, (g.m + 7) / 8, (nk + kchunk - 1) / kchunk);
+    if (prec == QBG_PREC_FP64) {
+      if (deriv)
+        k_assemble_cheb_reduced<1, 0><<<grd, blk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
+      else
+        k_assemble_cheb_reduced<0, 0><<<grd, blk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
+    } else {
+      k_assemble_cheb_reduced<0, 1><<<grd, blk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, lo_outs_dev, ld);
+    }
+    QBG_LAUNCH_CHECK("k_assemble_cheb_reduced");
+    return QBG_OK;
+  }
   if (!deriv) {
     const int nt = (g.n + 31) / 32;
     dim3 sblk(32, 16), sgrd((unsigned)(nt * (nt + 1) / 2), 1, (nk + kchunk - 1) / kchunk);
@@ -707,7 +873,10 @@ int launch_assemble_cheb(const GeomDev& g, const ChebTables& t, const cxd* ks, i
       else
         k_assemble_cheb<0, 0, 0><<<grd, blk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
     } else {
-      k_assemble_cheb<1, 0, 0><<<grd, blk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
+      if (deriv)
+        k_assemble_cheb<1, 1, 0><<<grd, blk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
+      else
+        k_assemble_cheb<1, 0, 0><<<grd, blk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
     }
   } else {
     if (g.form == 0)
@@ -735,15 +904,24 @@ int launch_assemble(const GeomDev& g, const cxd* ks, int nk, int deriv, int prec
   dim3 blk(32, 8);
   dim3 grd((dim + 31) / 32, (dim + 7) / 8);
   if (reduced) {
-    if (g.form != 0 || prec != 0) {
-      set_error("symmetry-reduced assembly is implemented for DLP in FP64");
+    if (g.form != 0) {
+      set_error("symmetry reduction is built for the DLP formulation");
       return QBG_ENOTSUP;
     }
-    if (deriv)
-      k_assemble_dlp_reduced_fp64<1><<<grd, blk, 0, st>>>(g, ks, nk, (cxd* const*)outs_dev, ld);
-    else
-      k_assemble_dlp_reduced_fp64<0><<<grd, blk, 0, st>>>(g, ks, nk, (cxd* const*)outs_dev, ld);
-    QBG_LAUNCH_CHECK("k_assemble_dlp_reduced_fp64");
+    if (deriv && prec != QBG_PREC_FP64) {
+      set_error("derivative assembly is available in FP64");
+      return QBG_ENOTSUP;
+    }
+    if (prec == QBG_PREC_FP64) {
+      if (deriv)
+        k_assemble_dlp_reduced<1, 0><<<grd, blk, 0, st>>>(g, ks, nk, outs_dev, nullptr, ld);
+      else
+        k_assemble_dlp_reduced<0, 0><<<grd, blk, 0, st>>>(g, ks, nk, outs_dev, nullptr, ld);
+    } else {
+      k_assemble_dlp_reduced<0, 1><<<grd, blk, 0, st>>>(g, ks, nk, outs_dev,
+                                                         prec == QBG_PREC_MIXED ? lo_outs_dev : nullptr, ld);
+    }
+    QBG_LAUNCH_CHECK("k_assemble_dlp_reduced");
     return QBG_OK;
   }
   if (prec == QBG_PREC_FP64) {
@@ -753,11 +931,10 @@ int launch_assemble(const GeomDev& g, const cxd* ks, int nk, int deriv, int prec
       else
         k_assemble_fp64<0, 0><<<grd, blk, 0, st>>>(g, ks, nk, (cxd* const*)outs_dev, ld);
     } else {
-      if (deriv) {
-        set_error("CFIE derivative assembly is not available");
-        return QBG_ENOTSUP;
-      }
-      k_assemble_fp64<1, 0><<<grd, blk, 0, st>>>(g, ks, nk, (cxd* const*)outs_dev, ld);
+      if (deriv)
+        k_assemble_fp64<1, 1><<<grd, blk, 0, st>>>(g, ks, nk, (cxd* const*)outs_dev, ld);
+      else
+        k_assemble_fp64<1, 0><<<grd, blk, 0, st>>>(g, ks, nk, (cxd* const*)outs_dev, ld);
     }
     QBG_LAUNCH_CHECK("k_assemble_fp64");
     return QBG_OK;

@@ -26,6 +26,15 @@ template <class T> QBG_HD cx<T> operator*(cx<T> a, cx<T> b) {
 }
 template <class T> QBG_HD cx<T> operator*(T s, cx<T> a) { return {s * a.re, s * a.im}; }
 template <class T> QBG_HD cx<T> operator*(cx<T> a, T s) { return {s * a.re, s * a.im}; }
+// complex quotient by Smith's scaling (avoids overflow of |b|^2)
+template <class T> QBG_HD cx<T> operator/(cx<T> a, cx<T> b) {
+  if ((b.re < 0 ? -b.re : b.re) >= (b.im < 0 ? -b.im : b.im)) {
+    const T r = b.im / b.re, d = b.re + b.im * r;
+    return {(a.re + a.im * r) / d, (a.im - a.re * r) / d};
+  }
+  const T r = b.re / b.im, d = b.re * r + b.im;
+  return {(a.re * r + a.im) / d, (a.im * r - a.re) / d};
+}
 template <class T> QBG_HD cx<T>& operator+=(cx<T>& a, cx<T> b) { a.re += b.re; a.im += b.im; return a; }
 template <class T> QBG_HD cx<T>& operator-=(cx<T>& a, cx<T> b) { a.re -= b.re; a.im -= b.im; return a; }
 template <class T> QBG_HD cx<T> cmul_i(cx<T> a) { return {-a.im, a.re}; }          // i*a

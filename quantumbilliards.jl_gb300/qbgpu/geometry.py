@@ -245,11 +245,8 @@ def node_count(k: float, L: float, b: float, min_pts: int = 20, needed: int = 2)
 
 
 def _needed(symmetry, base=2):
-    if symmetry is None:
-        return base
-    if symmetry[0] == "rotation":
-        return math.lcm(base, int(symmetry[1]))
-    return math.lcm(base, 4)
+    from .symmetry import needed_multiple
+    return needed_multiple(symmetry, base)
 
 
 def points_single_curve(crv, N: int, compid: int = 1) -> BoundaryPointsCFIE:

@@ -39,7 +39,12 @@ class Workspace:
     """Device-resident geometry for one discretisation (owns a qbg_geom)."""
 
     def __init__(self, solver, pts, reduction=None):
+        """reduction: orbit maps (fund, fund_to_full, fund_to_scale); by default
+        they follow the solver's symmetry (none: the full operator)."""
         lib = L.load()
+        if reduction is None:
+            from .symmetry import reduction as _red
+            reduction = _red(solver, pts)
         self.solver = solver
         self.kind = solver.kind
         pts_l = as_list(pts)

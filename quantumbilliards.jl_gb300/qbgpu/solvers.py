@@ -27,7 +27,7 @@ class _Solver:
     pts_scaling_factor: float
     billiard: G.Billiard
     min_pts: int = 20
-    symmetry: Optional[Tuple] = None   # None | ("reflection", "x"|"y"|"xy") | ("rotation", n)
+    symmetry: Optional[object] = None  # None | symmetry.Reflection | symmetry.Rotation
     kressq: int = 4
 
     kind = "dlp"      # formulation: "dlp" (F = I - D) or "cfie" (A = I - (D + ikS))
