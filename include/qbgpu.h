@@ -166,6 +166,9 @@ typedef struct qbg_beyn_opts {
                            compensated ones (0 = default 1, at most 4) */
   int32_t solve_block;  /* complex64 forms: rows per block of the triangular solves, nb, 2 nb or 4 nb
                            (0 = default 4 nb for N >= 8 nb) */
+  int32_t node_chunk;   /* 0: every contour node's operator stays factored from create on;
+                           c > 0: at most c operators are resident and each moments call streams
+                           the nodes through them (assemble, factor, solve, accumulate) */
 } qbg_beyn_opts;
 
 typedef struct qbg_beyn_stats {
@@ -185,6 +188,14 @@ typedef struct qbg_beyn_stats {
 
 qbg_status qbg_beyn_create(qbg_geom* g, double k0_re, double k0_im, double R, int32_t nq, int32_t prec,
                            const qbg_beyn_opts* opts, qbg_beyn** out);
+/* Several disks in one handle: the contour nodes of all disks (disk-major)
+ * are assembled in one launch and factored as one batch. This is the loop of
+ * compute_spectrum_beyn over its disks (beyn.jl:778-921) with all of them
+ * resident at once. k0s: ndisk complex centres (interleaved re, im); Rs:
+ * ndisk radii; ndisk * nq <= 65535. */
+qbg_status qbg_beyn_create_disks(qbg_geom* g, const double* k0s, const double* Rs, int32_t ndisk, int32_t nq,
+                                 int32_t prec, const qbg_beyn_opts* opts, qbg_beyn** out);
+/* A0 and A1 hold one N x L block per disk (disk d at offset d * N * L). */
 qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0, double* A1,
                             qbg_beyn_stats* stats);
 qbg_status qbg_beyn_destroy(qbg_beyn* b);

@@ -36,11 +36,6 @@ int cuda_status(cudaError_t e, const char* what) {
 
 using namespace qbg;
 
-#define QBG_TRY(x)          \
-  do {                      \
-    int _s = (x);           \
-    if (_s) return _s;      \
-  } while (0)
 
 extern "C" {
 
@@ -173,19 +168,21 @@ qbg_status qbg_geom_dim(const qbg_geom* g, int64_t* dim) {
   return QBG_OK;
 }
 
-static int check_ks(const double* ks, int64_t nk) {
+}  // extern "C"
+namespace qbg {
+int check_ks(const double* ks, int64_t nk) {
   for (int64_t q = 0; q < 2 * nk; ++q)
     if (!std::isfinite(ks[q])) { set_error("non-finite wavenumber at index %lld", (long long)(q / 2)); return QBG_EINVAL; }
   for (int64_t q = 0; q < nk; ++q)
     if (ks[2 * q] == 0.0 && ks[2 * q + 1] == 0.0) { set_error("wavenumber k = 0 is not allowed"); return QBG_EINVAL; }
   return QBG_OK;
 }
-
-}  // extern "C"
+}  // namespace qbg
 
 // Chebyshev tables for nk device wavenumbers; rmin/rmax padded by 0.95/1.05
 // exactly as build_cfie_kress_block_caches (chebyshev_euclidian_helmholtz_cfie_kress.jl:396-456).
-static int cheb_params_check(const qbg_cheb_params* prm) {
+namespace qbg {
+int cheb_params_check(const qbg_cheb_params* prm) {
   if (prm->n_panels_h < 1 || prm->n_panels_j < 1 || prm->M_h < 2 || prm->M_j < 2 ||
       prm->M_h > QBG_CHEB_MAX_DEGREE || prm->M_j > QBG_CHEB_MAX_DEGREE || prm->n_panels_h > (1 << 24) ||
       prm->n_panels_j > (1 << 24)) {
@@ -195,7 +192,7 @@ static int cheb_params_check(const qbg_cheb_params* prm) {
   return QBG_OK;
 }
 
-static qbg_cheb_params cheb_defaults(const qbg_cheb_params* prm) {
+qbg_cheb_params cheb_defaults(const qbg_cheb_params* prm) {
   // the reference's defaults: n_panels_h = 15000, M_h = 5, n_panels_j = 3000, M_j = 5
   qbg_cheb_params p{15000, 5, 3000, 5};
   if (prm) {
@@ -207,8 +204,8 @@ static qbg_cheb_params cheb_defaults(const qbg_cheb_params* prm) {
   return p;
 }
 
-static int make_cheb(qbg_geom* g, const cxd* dks, int nk, const qbg_cheb_params& prm, ChebTables& t,
-                     std::vector<void*>& tmp, cudaStream_t st) {
+int make_cheb(qbg_geom* g, const cxd* dks, int nk, const qbg_cheb_params& prm, ChebTables& t,
+              std::vector<void*>& tmp, cudaStream_t st) {
   unsigned long long* red = nullptr;
   QBG_TRY(dmalloc(&red, 2 * sizeof(unsigned long long)));
   tmp.push_back(red);
@@ -236,6 +233,7 @@ static int make_cheb(qbg_geom* g, const cxd* dks, int nk, const qbg_cheb_params&
   tmp.push_back(t.J);
   return cheb_build(t, dks, st);
 }
+}  // namespace qbg
 
 extern "C" {
 
@@ -315,377 +313,7 @@ qbg_status qbg_assemble_cheb(qbg_geom* g, const double* ks, int64_t nk, int32_t 
 
 }  // extern "C"
 
-// ---------------------------------------------------------------------------
-// Beyn contour step
-// ---------------------------------------------------------------------------
-struct qbg_beyn {
-  qbg_geom* g = nullptr;
-  int n = 0, nq = 0, prec = 0;
-  qbg_beyn_opts opts{};
-  cxd* zj = nullptr;  // device contour nodes
-  cxd* wj = nullptr;  // device contour weights
-  LUBatch<double> fd;
-  LUBatch<float> ff;
-  cxf* Tcopy = nullptr;  // complex64 forms: unfactored T(z_j) (hi word) for the refinement residual
-  cxf* Tlo = nullptr;    // mixed form: lo word, T = hi + lo to ~2^-48
-  std::vector<void*> allocs;
-  cudaStream_t st = nullptr;
-  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-  float ms_assemble = 0, ms_factor = 0;
-  int singular = 0;
-  std::mutex mu;
-  ~qbg_beyn() {
-    for (void* p : allocs) cudaFree(p);
-    for (auto& e : ev) if (e) cudaEventDestroy(e);
-  }
-  template <class P>
-  int alloc(P** p, size_t bytes) {
-    int s = dmalloc(p, bytes);
-    if (!s) allocs.push_back(*p);
-    return s;
-  }
-};
-
-template <class T>
-static int beyn_setup_lu(qbg_beyn* b, LUBatch<T>& f, int nb, int solve_levels) {
-  f.n = b->n;
-  f.batch = b->nq;
-  f.nb = nb;
-  f.nblk = (b->n + nb - 1) / nb;
-  f.stride = (long long)b->n * b->n;
-  QBG_TRY(b->alloc(&f.A, sizeof(cx<T>) * (size_t)f.stride * f.batch));
-  QBG_TRY(b->alloc(&f.ipiv, sizeof(int) * (size_t)b->n * f.batch));
-  QBG_TRY(b->alloc(&f.perm, sizeof(int) * (size_t)b->n * f.batch));
-  QBG_TRY(b->alloc(&f.info, sizeof(int) * f.batch));
-  QBG_TRY(b->alloc(&f.Linv, sizeof(cx<T>) * (size_t)f.nblk * nb * nb * f.batch));
-  QBG_TRY(b->alloc(&f.Uinv, sizeof(cx<T>) * (size_t)f.nblk * nb * nb * f.batch));
-  if (solve_levels > 0) {
-    void* mem = nullptr;
-    QBG_TRY(b->alloc(&mem, lu_solve_blocks_bytes<T>(f, solve_levels, 128)));
-    lu_solve_blocks_bind<T>(f, mem);
-  }
-  return QBG_OK;
-}
-
-static int beyn_create_impl(qbg_beyn* b, double k0_re, double k0_im, double R) {
-  const int n = b->n, nq = b->nq;
-  cudaStream_t st = b->st;
-  // contour (beyn.jl:258-261): theta_j = 2 pi j / nq, z_j = k0 + R e^{i theta}, w_j = (R/nq) e^{i theta}
-  std::vector<cxd> z(nq), w(nq);
-  for (int j = 0; j < nq; ++j) {
-    const double th = 2.0 * M_PI * (double)j / (double)nq;
-    const double c = std::cos(th), s = std::sin(th);
-    z[j] = cxd(k0_re + R * c, k0_im + R * s);
-    w[j] = cxd((R / nq) * c, (R / nq) * s);
-  }
-  QBG_TRY(b->alloc(&b->zj, sizeof(cxd) * nq));
-  QBG_TRY(b->alloc(&b->wj, sizeof(cxd) * nq));
-  QBG_CUDA(cudaMemcpyAsync(b->zj, z.data(), sizeof(cxd) * nq, cudaMemcpyHostToDevice, st));
-  QBG_CUDA(cudaMemcpyAsync(b->wj, w.data(), sizeof(cxd) * nq, cudaMemcpyHostToDevice, st));
-  for (auto& e : b->ev) QBG_CUDA(cudaEventCreate(&e));
-  const int nb = b->opts.nb > 0 ? b->opts.nb : (b->prec ? 64 : 32);
-  if (nb != 32 && nb != 64) { set_error("LU block size must be 32 or 64"); return QBG_EINVAL; }
-  std::vector<void*> ptrs(nq);
-  void** dptrs = nullptr;
-  QBG_TRY(b->alloc(&dptrs, sizeof(void*) * nq));
-  if (b->prec == 0) {
-    QBG_TRY(beyn_setup_lu(b, b->fd, nb, 0));
-    for (int j = 0; j < nq; ++j) ptrs[j] = b->fd.A + (size_t)j * b->fd.stride;
-  } else {
-    int levels = n >= 8 * nb ? 2 : (n >= 4 * nb ? 1 : 0);
-    if (b->opts.solve_block != 0) {
-      const int sb = b->opts.solve_block;
-      if (sb != nb && sb != 2 * nb && sb != 4 * nb) {
-        set_error("solve_block must be nb, 2 nb or 4 nb (nb = %d)", nb);
-        return QBG_EINVAL;
-      }
-      levels = sb == nb ? 0 : (sb == 2 * nb ? 1 : 2);
-    }
-    QBG_TRY(beyn_setup_lu(b, b->ff, nb, levels));
-    for (int j = 0; j < nq; ++j) ptrs[j] = b->ff.A + (size_t)j * b->ff.stride;
-  }
-  QBG_CUDA(cudaMemcpyAsync(dptrs, ptrs.data(), sizeof(void*) * nq, cudaMemcpyHostToDevice, st));
-  void** dlo = nullptr;
-  if (b->prec == QBG_PREC_MIXED) {
-    QBG_TRY(b->alloc(&b->Tlo, sizeof(cxf) * (size_t)b->ff.stride * nq));
-    QBG_TRY(b->alloc(&dlo, sizeof(void*) * nq));
-    std::vector<void*> lp(nq);
-    for (int j = 0; j < nq; ++j) lp[j] = b->Tlo + (size_t)j * b->ff.stride;
-    QBG_CUDA(cudaMemcpyAsync(dlo, lp.data(), sizeof(void*) * nq, cudaMemcpyHostToDevice, st));
-    QBG_CUDA(cudaStreamSynchronize(st));  // keep lp alive until the copy has run
-  }
-  QBG_CUDA(cudaEventRecord(b->ev[0], st));
-  const bool use_cheb = b->opts.eval_mode == 0 && b->prec != QBG_PREC_FP32;
-  if (use_cheb) {
-    const qbg_cheb_params cp = cheb_defaults(&b->opts.cheb);
-    QBG_TRY(cheb_params_check(&cp));
-    std::vector<void*> ctmp;
-    ChebTables t;
-    int s = make_cheb(b->g, b->zj, nq, cp, t, ctmp, st);
-    if (!s) s = launch_assemble_cheb(b->g->d, t, b->zj, nq, 0, b->prec, dptrs, dlo, n, st);
-    if (!s) {
-      QBG_CUDA(cudaEventRecord(b->ev[1], st));
-      cudaError_t e = cudaStreamSynchronize(st);
-      if (e != cudaSuccess) s = cuda_status(e, "Chebyshev assembly");
-    }
-    for (void* p : ctmp) cudaFree(p);
-    if (s) return s;
-  } else {
-    QBG_TRY(launch_assemble(b->g->d, b->zj, nq, 0, b->prec, dptrs, n, st, dlo));
-    QBG_CUDA(cudaEventRecord(b->ev[1], st));
-  }
-  if (b->prec == 0) {
-    QBG_TRY(lu_factor<double>(b->fd, st));
-  } else {
-    const size_t bytes = sizeof(cxf) * (size_t)b->ff.stride * nq;
-    QBG_TRY(b->alloc(&b->Tcopy, bytes));
-    QBG_CUDA(cudaMemcpyAsync(b->Tcopy, b->ff.A, bytes, cudaMemcpyDeviceToDevice, st));
-    QBG_TRY(lu_factor<float>(b->ff, st));
-  }
-  QBG_CUDA(cudaEventRecord(b->ev[2], st));
-  std::vector<int> info(nq);
-  QBG_CUDA(cudaMemcpyAsync(info.data(), b->prec ? b->ff.info : b->fd.info, sizeof(int) * nq,
-                           cudaMemcpyDeviceToHost, st));
-  QBG_CUDA(cudaStreamSynchronize(st));
-  if (b->prec != 0) QBG_TRY(tc_check(st));
-  b->singular = 0;
-  for (int v : info) b->singular += (v != 0);
-  QBG_CUDA(cudaEventElapsedTime(&b->ms_assemble, b->ev[0], b->ev[1]));
-  QBG_CUDA(cudaEventElapsedTime(&b->ms_factor, b->ev[1], b->ev[2]));
-  return QBG_OK;
-}
-
 extern "C" {
-
-qbg_status qbg_beyn_create(qbg_geom* g, double k0_re, double k0_im, double R, int32_t nq, int32_t prec,
-                           const qbg_beyn_opts* opts, qbg_beyn** out) {
-  if (!g || !out || nq < 2 || !(R > 0.0) || prec < 0 || prec > 2 || !std::isfinite(k0_re) ||
-      !std::isfinite(k0_im) || !std::isfinite(R)) {
-    set_error("qbg_beyn_create: invalid arguments");
-    return QBG_EINVAL;
-  }
-  *out = nullptr;
-  qbg_beyn* b = new (std::nothrow) qbg_beyn();
-  if (!b) { set_error("host allocation failed"); return QBG_ENOMEM; }
-  b->g = g;
-  b->n = (int)g->dim;
-  b->nq = nq;
-  b->prec = prec;
-  b->opts.flags = 0;
-  b->opts.max_refine = 4;
-  b->opts.refine_tol = 1e-6;
-  b->opts.nb = 0;
-  b->opts.eval_mode = 0;
-  b->opts.cheb = qbg_cheb_params{0, 0, 0, 0};
-  if (opts) {
-    b->opts = *opts;
-    if (b->opts.max_refine <= 0) b->opts.max_refine = 4;
-    if (!(b->opts.refine_tol > 0.0)) b->opts.refine_tol = 1e-6;
-  }
-  std::lock_guard<std::mutex> lk(g->mu);
-  b->st = g->stream;
-  int s = beyn_create_impl(b, k0_re, k0_im, R);
-  if (s) {
-    cudaStreamSynchronize(b->st);
-    delete b;
-    return s;
-  }
-  *out = b;
-  return QBG_OK;
-}
-
-qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0, double* A1,
-                            qbg_beyn_stats* stats) {
-  if (!b || !V || !A0 || !A1 || L < 1) {
-    set_error("qbg_beyn_moments: invalid arguments");
-    return QBG_EINVAL;
-  }
-  std::lock_guard<std::mutex> lk(b->g->mu);
-  const int n = b->n, nq = b->nq;
-  const bool dev = (b->opts.flags & QBG_PTR_DEVICE) != 0;
-  cudaStream_t st = b->st;
-  const size_t nl = (size_t)n * L;
-  std::vector<void*> tmp;
-  std::vector<cudaEvent_t> sev;  // solve start/stop pairs
-  auto cleanup = [&]() {
-    for (void* p : tmp) cudaFree(p);
-    for (cudaEvent_t e : sev) cudaEventDestroy(e);
-    sev.clear();
-  };
-  auto talloc = [&](void** p, size_t bytes) {
-    int s = dmalloc(p, bytes);
-    if (!s) tmp.push_back(*p);
-    return s;
-  };
-  int s = QBG_OK;
-  cxd *dV = nullptr, *dA0 = nullptr, *dA1 = nullptr;
-  if (dev) {
-    dV = (cxd*)V; dA0 = (cxd*)A0; dA1 = (cxd*)A1;
-  } else {
-    if ((s = talloc((void**)&dV, sizeof(cxd) * nl)) || (s = talloc((void**)&dA0, sizeof(cxd) * nl)) ||
-        (s = talloc((void**)&dA1, sizeof(cxd) * nl))) { cleanup(); return s; }
-    cudaError_t e = cudaMemcpyAsync(dV, V, sizeof(cxd) * nl, cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) { cleanup(); return cuda_status(e, "V H2D"); }
-  }
-  cudaEventRecord(b->ev[0], st);
-  int sweeps = 0;
-  double rel = 0.0;
-  double hist[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  int nhist = 0;
-  double ms_resid = 0.0;
-  int n_resid = 0;
-  double f32hist[4] = {0, 0, 0, 0};
-  int nf32 = 0;
-  if (b->prec == 0) {
-    cxd* X = nullptr;
-    if ((s = talloc((void**)&X, sizeof(cxd) * nl * nq))) { cleanup(); return s; }
-    if ((s = lu_solve_shared<double>(b->fd, dV, (int)L, X, 0, st)) ||
-        (s = moments<double>(X, (long long)nl, nq, n, (int)L, b->wj, b->zj, dA0, dA1, 0, st))) {
-      cleanup(); return s;
-    }
-  } else {
-    // mixed: X32 = LU32 \ V32, X64 = X32, then R = V - T X64 (compensated), X64 += LU32 \ R32
-    cxf *V32 = nullptr, *X32 = nullptr, *R32 = nullptr;
-    cxd *X64 = nullptr, *R64 = nullptr;
-    double* dmax = nullptr;
-    if ((s = talloc((void**)&V32, sizeof(cxf) * nl)) || (s = talloc((void**)&X32, sizeof(cxf) * nl * nq)) ||
-        (s = talloc((void**)&R32, sizeof(cxf) * nl * nq)) || (s = talloc((void**)&X64, sizeof(cxd) * nl * nq)) ||
-        (s = talloc((void**)&R64, sizeof(cxd) * nl * nq)) || (s = talloc((void**)&dmax, sizeof(double)))) {
-      cleanup(); return s;
-    }
-    // every solve pass is bracketed by a pair of events, summed after the last sync
-    auto timed_solve = [&](const cxf* rhs, long long srhs) -> int {
-      cudaEvent_t e0 = nullptr, e1 = nullptr;
-      if (sev.size() < 32 && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
-        sev.push_back(e0);
-        sev.push_back(e1);
-        cudaEventRecord(e0, st);
-      } else {
-        if (e0) cudaEventDestroy(e0);
-        e0 = e1 = nullptr;
-      }
-      int r = lu_solve_shared<float>(b->ff, rhs, (int)L, X32, srhs, st);
-      if (e1) cudaEventRecord(e1, st);
-      return r;
-    };
-    // max |V| (|re|+|im|) on the host side of the copy is not available for device V: compute by residual with X=0
-    cudaError_t e = cudaMemsetAsync(X64, 0, sizeof(cxd) * nl * nq, st);
-    if (e != cudaSuccess) { cleanup(); return cuda_status(e, "memset"); }
-    if ((s = convert_d2f(dV, V32, (long long)nl, st)) ||
-        (s = timed_solve(V32, 0)) ||
-        (s = axpy_f2d(X32, X64, (long long)(nl * nq), st))) { cleanup(); return s; }
-    double vmax = 0.0;
-    {
-      // |V|max via the residual kernel on one matrix with X = 0 is wasteful; do it on the host copy instead
-      std::vector<cxd> hv;
-      if (!dev) {
-        const cxd* hvp = reinterpret_cast<const cxd*>(V);
-        for (size_t q = 0; q < nl; ++q) vmax = std::max(vmax, std::fabs(hvp[q].re) + std::fabs(hvp[q].im));
-      } else {
-        hv.resize(nl);
-        e = cudaMemcpyAsync(hv.data(), dV, sizeof(cxd) * nl, cudaMemcpyDeviceToHost, st);
-        if (e != cudaSuccess) { cleanup(); return cuda_status(e, "V D2H"); }
-        cudaStreamSynchronize(st);
-        for (size_t q = 0; q < nl; ++q) vmax = std::max(vmax, std::fabs(hv[q].re) + std::fabs(hv[q].im));
-      }
-    }
-    if (!(vmax > 0.0)) vmax = 1.0;
-    // Corrections from plain FP32 residuals V32 - hi X: while the residual is far
-    // above the FP32 rounding of the product, compensated arithmetic buys
-    // nothing. Later residuals (and the convergence test) use the compensated
-    // kernel with hi + lo.
-    const int nf = std::min(b->opts.fp32_sweeps > 0 ? b->opts.fp32_sweeps : 1, 4);
-    for (int q = 0; q < nf; ++q) {
-      // X32 holds the first solve's result for q == 0, a correction afterwards
-      if (q > 0 && (s = convert_d2f(X64, X32, (long long)(nl * nq), st))) { cleanup(); return s; }
-      e = cudaMemsetAsync(dmax, 0, sizeof(double), st);
-      if (e != cudaSuccess) { cleanup(); return cuda_status(e, "memset"); }
-      if ((s = broadcast_f(V32, (long long)nl, nq, R32, st)) ||
-          (s = gemm_batched<float>(n, (int)L, n, cxf(-1.f, 0.f), b->Tcopy, n, b->ff.stride, X32, n, (long long)nl,
-                                   cxf(1.f, 0.f), R32, n, (long long)nl, nq, st)) ||
-          (s = maxabs_c64(R32, (long long)(nl * nq), dmax, st)) ||
-          (s = timed_solve(R32, (long long)nl)) ||
-          (s = axpy_f2d(X32, X64, (long long)(nl * nq), st))) { cleanup(); return s; }
-      double fmax = 0.0;
-      e = cudaMemcpyAsync(&fmax, dmax, sizeof(double), cudaMemcpyDeviceToHost, st);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-      if (e != cudaSuccess) { cleanup(); return cuda_status(e, "FP32 residual"); }
-      if (nf32 < 4) f32hist[nf32++] = fmax / vmax;
-      ++sweeps;
-    }
-    for (int it = 0; it < b->opts.max_refine; ++it) {
-      e = cudaMemsetAsync(dmax, 0, sizeof(double), st);
-      if (e != cudaSuccess) { cleanup(); return cuda_status(e, "memset"); }
-      cudaEventRecord(b->ev[4], st);
-      if ((s = residual_df32(b->Tcopy, b->Tlo, b->ff.stride, X64, (long long)nl, dV, R64, (long long)nl, n, (int)L, nq,
-                             dmax, st))) { cleanup(); return s; }
-      cudaEventRecord(b->ev[5], st);
-      double rmax = 0.0;
-      e = cudaMemcpyAsync(&rmax, dmax, sizeof(double), cudaMemcpyDeviceToHost, st);
-      if (e != cudaSuccess) { cleanup(); return cuda_status(e, "rmax D2H"); }
-      e = cudaStreamSynchronize(st);
-      if (e != cudaSuccess) { cleanup(); return cuda_status(e, "refine sync"); }
-      float ms_r = 0.f;
-      if (cudaEventElapsedTime(&ms_r, b->ev[4], b->ev[5]) == cudaSuccess) { ms_resid += ms_r; ++n_resid; }
-      rel = rmax / vmax;
-      if (nhist < 8) hist[nhist++] = rel;
-      ++sweeps;
-      // correction solves, one right-hand block per contour node; when the
-      // residual already meets the tolerance this is the final correction
-      // (the residual is in hand, the solve costs one FP32 pass)
-      if ((s = convert_d2f(R64, R32, (long long)(nl * nq), st)) ||
-          (s = timed_solve(R32, (long long)nl)) ||
-          (s = axpy_f2d(X32, X64, (long long)(nl * nq), st))) { cleanup(); return s; }
-      if (rel <= b->opts.refine_tol) break;
-    }
-    if ((s = moments<double>(X64, (long long)nl, nq, n, (int)L, b->wj, b->zj, dA0, dA1, 0, st))) {
-      cleanup(); return s;
-    }
-  }
-  cudaEventRecord(b->ev[3], st);
-  if (!dev) {
-    cudaError_t e = cudaMemcpyAsync(A0, dA0, sizeof(cxd) * nl, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(A1, dA1, sizeof(cxd) * nl, cudaMemcpyDeviceToHost, st);
-    if (e != cudaSuccess) { cleanup(); return cuda_status(e, "A0/A1 D2H"); }
-  }
-  cudaError_t e = cudaStreamSynchronize(st);
-  double ms_solves = 0.0;
-  const int n_solves = (int)sev.size() / 2;
-  for (size_t q = 0; e == cudaSuccess && q + 1 < sev.size(); q += 2) {
-    float ms = 0.f;
-    if (cudaEventElapsedTime(&ms, sev[q], sev[q + 1]) == cudaSuccess) ms_solves += ms;
-  }
-  cleanup();
-  if (e != cudaSuccess) return cuda_status(e, "qbg_beyn_moments");
-  if (b->prec != 0) QBG_TRY(tc_check(st));
-  if (stats) {
-    float ms = 0;
-    cudaEventElapsedTime(&ms, b->ev[0], b->ev[3]);
-    stats->refine_sweeps = sweeps;
-    stats->refine_residual = rel;
-    stats->singular = b->singular;
-    stats->ms_assemble = b->ms_assemble;
-    stats->ms_factor = b->ms_factor;
-    stats->ms_solve = ms;
-    stats->nhist = nhist;
-    stats->ms_residual = ms_resid;
-    stats->n_residual = n_resid;
-    stats->nfp32 = nf32;
-    for (int q = 0; q < 4; ++q) stats->fp32_history[q] = f32hist[q];
-    stats->ms_solves = ms_solves;
-    stats->n_solves = n_solves;
-    for (int q = 0; q < 8; ++q) stats->refine_history[q] = hist[q];
-  }
-  return QBG_OK;
-}
-
-qbg_status qbg_beyn_destroy(qbg_beyn* b) {
-  if (b) {
-    cudaStreamSynchronize(b->st);
-    delete b;
-  }
-  return QBG_OK;
-}
 
 // ---------------------------------------------------------------------------
 // sigma_min via cuSOLVER gesvd (values only)

@@ -1,0 +1,503 @@
+// Beyn contour step on the device (construct_B_matrix, beyn.jl:257-322): the
+// contour nodes of one or more disks, T(z_j) at every node, the LU of every
+// node, X_j = T(z_j)^{-1} V and the moment sums A0 = sum w_j X_j,
+// A1 = sum w_j z_j X_j per disk.
+//
+// Residency. By default every node's operator stays factored in HBM between
+// qbg_beyn_create and the moments calls (the reference keeps its nq LU
+// factors the same way, beyn.jl:270-277). With opts.node_chunk > 0 the handle
+// keeps only node_chunk operators resident: each moments call streams the
+// nodes through them in groups (assemble, factor, solve, accumulate), which
+// bounds the memory at large N at the price of re-assembling per call.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "qbg_assemble.cuh"
+#include "qbg_handles.cuh"
+#include "qbg_linalg.cuh"
+
+using namespace qbg;
+
+struct qbg_beyn {
+  qbg_geom* g = nullptr;
+  int n = 0;        // operator dimension
+  int nq = 0;       // contour nodes per disk
+  int ndisk = 1;
+  int nn = 0;       // nq * ndisk contour nodes, disk-major
+  int cap = 0;      // operators resident at once
+  int prec = 0;
+  qbg_beyn_opts opts{};
+  cxd* zj = nullptr;  // device contour nodes (nn)
+  cxd* wj = nullptr;  // device contour weights (nn)
+  LUBatch<double> fd;  // FP64 form: cap operators
+  LUBatch<float> ff;   // complex64 forms: cap operators
+  cxf* Tcopy = nullptr;  // complex64 forms: unfactored hi words for the refinement residual
+  cxf* Tlo = nullptr;    // mixed form: lo words, T = hi + lo to ~2^-48
+  void** dptrs = nullptr;  // device array of the cap operator slots
+  void** dlo = nullptr;    // device array of the cap lo slots (mixed form)
+  int res0 = -1, resn = 0;  // nodes [res0, res0 + resn) are factored in the slots
+  std::vector<void*> allocs;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  double ms_assemble = 0, ms_factor = 0;  // device time of the last load(s)
+  int singular = 0;
+  std::mutex mu;
+  ~qbg_beyn() {
+    if (st) cudaStreamSynchronize(st);
+    for (void* p : allocs) cudaFree(p);
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    if (st) cudaStreamDestroy(st);
+  }
+  template <class P>
+  int alloc(P** p, size_t bytes) {
+    int s = dmalloc(p, bytes);
+    if (!s) allocs.push_back(*p);
+    return s;
+  }
+};
+
+namespace {
+
+template <class T>
+int setup_lu(qbg_beyn* b, LUBatch<T>& f, int nb, int solve_levels) {
+  f.n = b->n;
+  f.batch = b->cap;
+  f.nb = nb;
+  f.nblk = (b->n + nb - 1) / nb;
+  f.stride = (long long)b->n * b->n;
+  QBG_TRY(b->alloc(&f.A, sizeof(cx<T>) * (size_t)f.stride * f.batch));
+  QBG_TRY(b->alloc(&f.ipiv, sizeof(int) * (size_t)b->n * f.batch));
+  QBG_TRY(b->alloc(&f.perm, sizeof(int) * (size_t)b->n * f.batch));
+  QBG_TRY(b->alloc(&f.info, sizeof(int) * f.batch));
+  QBG_TRY(b->alloc(&f.Linv, sizeof(cx<T>) * (size_t)f.nblk * nb * nb * f.batch));
+  QBG_TRY(b->alloc(&f.Uinv, sizeof(cx<T>) * (size_t)f.nblk * nb * nb * f.batch));
+  if (solve_levels > 0) {
+    void* mem = nullptr;
+    QBG_TRY(b->alloc(&mem, lu_solve_blocks_bytes<T>(f, solve_levels, 128)));
+    lu_solve_blocks_bind<T>(f, mem);
+  }
+  return QBG_OK;
+}
+
+// contour (beyn.jl:258-261): theta_j = 2 pi j / nq, z_j = k0 + R e^{i theta_j}, w_j = (R / nq) e^{i theta_j}
+int setup(qbg_beyn* b, const double* k0s, const double* Rs) {
+  const int n = b->n, nq = b->nq, nn = b->nn;
+  cudaStream_t st = b->st;
+  std::vector<cxd> z(nn), w(nn);
+  for (int d = 0; d < b->ndisk; ++d) {
+    const double k0r = k0s[2 * d], k0i = k0s[2 * d + 1], R = Rs[d];
+    for (int j = 0; j < nq; ++j) {
+      const double th = 2.0 * M_PI * (double)j / (double)nq;
+      const double c = std::cos(th), s = std::sin(th);
+      z[d * nq + j] = cxd(k0r + R * c, k0i + R * s);
+      w[d * nq + j] = cxd((R / nq) * c, (R / nq) * s);
+    }
+  }
+  QBG_TRY(b->alloc(&b->zj, sizeof(cxd) * nn));
+  QBG_TRY(b->alloc(&b->wj, sizeof(cxd) * nn));
+  QBG_CUDA(cudaMemcpyAsync(b->zj, z.data(), sizeof(cxd) * nn, cudaMemcpyHostToDevice, st));
+  QBG_CUDA(cudaMemcpyAsync(b->wj, w.data(), sizeof(cxd) * nn, cudaMemcpyHostToDevice, st));
+  for (auto& e : b->ev) QBG_CUDA(cudaEventCreate(&e));
+  const int nb = b->opts.nb > 0 ? b->opts.nb : (b->prec ? 64 : 32);
+  if (nb != 32 && nb != 64) {
+    set_error("LU block size must be 32 or 64");
+    return QBG_EINVAL;
+  }
+  const int cap = b->cap;
+  std::vector<void*> ptrs(cap), lp(cap);
+  QBG_TRY(b->alloc(&b->dptrs, sizeof(void*) * cap));
+  if (b->prec == QBG_PREC_FP64) {
+    QBG_TRY(setup_lu(b, b->fd, nb, 0));
+    for (int j = 0; j < cap; ++j) ptrs[j] = b->fd.A + (size_t)j * b->fd.stride;
+  } else {
+    int levels = n >= 8 * nb ? 2 : (n >= 4 * nb ? 1 : 0);
+    if (b->opts.solve_block != 0) {
+      const int sb = b->opts.solve_block;
+      if (sb != nb && sb != 2 * nb && sb != 4 * nb) {
+        set_error("solve_block must be nb, 2 nb or 4 nb (nb = %d)", nb);
+        return QBG_EINVAL;
+      }
+      levels = sb == nb ? 0 : (sb == 2 * nb ? 1 : 2);
+    }
+    QBG_TRY(setup_lu(b, b->ff, nb, levels));
+    for (int j = 0; j < cap; ++j) ptrs[j] = b->ff.A + (size_t)j * b->ff.stride;
+    QBG_TRY(b->alloc(&b->Tcopy, sizeof(cxf) * (size_t)b->ff.stride * cap));
+  }
+  QBG_CUDA(cudaMemcpyAsync(b->dptrs, ptrs.data(), sizeof(void*) * cap, cudaMemcpyHostToDevice, st));
+  if (b->prec == QBG_PREC_MIXED) {
+    QBG_TRY(b->alloc(&b->Tlo, sizeof(cxf) * (size_t)b->ff.stride * cap));
+    QBG_TRY(b->alloc(&b->dlo, sizeof(void*) * cap));
+    for (int j = 0; j < cap; ++j) lp[j] = b->Tlo + (size_t)j * b->ff.stride;
+    QBG_CUDA(cudaMemcpyAsync(b->dlo, lp.data(), sizeof(void*) * cap, cudaMemcpyHostToDevice, st));
+  }
+  QBG_CUDA(cudaStreamSynchronize(st));  // the host pointer tables must outlive their copies
+  return QBG_OK;
+}
+
+// assemble and factor nodes [n0, n0 + c) into slots 0 .. c-1
+int load(qbg_beyn* b, int n0, int c) {
+  const int n = b->n;
+  cudaStream_t st = b->st;
+  b->res0 = -1;
+  b->resn = 0;
+  QBG_CUDA(cudaEventRecord(b->ev[0], st));
+  const bool use_cheb = b->opts.eval_mode == 0 && b->prec != QBG_PREC_FP32;
+  if (use_cheb) {
+    const qbg_cheb_params cp = cheb_defaults(&b->opts.cheb);
+    QBG_TRY(cheb_params_check(&cp));
+    std::vector<void*> ctmp;
+    ChebTables t;
+    int s = make_cheb(b->g, b->zj + n0, c, cp, t, ctmp, st);
+    if (!s) s = launch_assemble_cheb(b->g->d, t, b->zj + n0, c, 0, b->prec, b->dptrs, b->dlo, n, st);
+    if (!s) {
+      cudaEventRecord(b->ev[1], st);
+      cudaError_t e = cudaStreamSynchronize(st);  // the tables are freed below
+      if (e != cudaSuccess) s = cuda_status(e, "Chebyshev assembly");
+    }
+    for (void* p : ctmp) cudaFree(p);
+    if (s) return s;
+  } else {
+    QBG_TRY(launch_assemble(b->g->d, b->zj + n0, c, 0, b->prec, b->dptrs, n, st, b->dlo));
+    QBG_CUDA(cudaEventRecord(b->ev[1], st));
+  }
+  int* info = nullptr;
+  if (b->prec == QBG_PREC_FP64) {
+    b->fd.batch = c;
+    QBG_TRY(lu_factor<double>(b->fd, st));
+    info = b->fd.info;
+  } else {
+    QBG_CUDA(cudaMemcpyAsync(b->Tcopy, b->ff.A, sizeof(cxf) * (size_t)b->ff.stride * c, cudaMemcpyDeviceToDevice,
+                             st));
+    b->ff.batch = c;
+    QBG_TRY(lu_factor<float>(b->ff, st));
+    info = b->ff.info;
+  }
+  QBG_CUDA(cudaEventRecord(b->ev[2], st));
+  std::vector<int> hinfo(c);
+  QBG_CUDA(cudaMemcpyAsync(hinfo.data(), info, sizeof(int) * c, cudaMemcpyDeviceToHost, st));
+  QBG_CUDA(cudaStreamSynchronize(st));
+  if (b->prec != QBG_PREC_FP64) QBG_TRY(tc_check(st));
+  for (int v : hinfo) b->singular += (v != 0);
+  float ma = 0.f, mf = 0.f;
+  QBG_CUDA(cudaEventElapsedTime(&ma, b->ev[0], b->ev[1]));
+  QBG_CUDA(cudaEventElapsedTime(&mf, b->ev[1], b->ev[2]));
+  b->ms_assemble += ma;
+  b->ms_factor += mf;
+  b->res0 = n0;
+  b->resn = c;
+  return QBG_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// state of one moments call
+struct Call {
+  qbg_beyn* b = nullptr;
+  int L = 0;
+  size_t nl = 0;
+  cxd *dV = nullptr, *dA0 = nullptr, *dA1 = nullptr;
+  double vmax = 1.0;
+  cxd *X64 = nullptr, *R64 = nullptr;
+  cxf *V32 = nullptr, *X32 = nullptr, *R32 = nullptr;
+  double* dmax = nullptr;
+  std::vector<void*> tmp;
+  std::vector<cudaEvent_t> sev;  // start/stop pairs around the solve passes
+  // statistics (the history is the last node group's)
+  int sweeps = 0, nhist = 0, n_resid = 0, nf32 = 0;
+  double rel = 0.0, ms_resid = 0.0;
+  double hist[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  double f32hist[4] = {0, 0, 0, 0};
+  ~Call() {
+    for (void* p : tmp) cudaFree(p);
+    for (cudaEvent_t e : sev) cudaEventDestroy(e);
+  }
+  template <class P>
+  int talloc(P** p, size_t bytes) {
+    int s = dmalloc(p, bytes);
+    if (!s) tmp.push_back(*p);
+    return s;
+  }
+  int timed_solve(const cxf* rhs, long long srhs) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (sev.size() < 64 && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
+      sev.push_back(e0);
+      sev.push_back(e1);
+      cudaEventRecord(e0, b->st);
+    } else {
+      if (e0) cudaEventDestroy(e0);
+      e0 = e1 = nullptr;
+    }
+    int r = lu_solve_shared<float>(b->ff, rhs, L, X32, srhs, b->st);
+    if (e1) cudaEventRecord(e1, b->st);
+    return r;
+  }
+};
+
+// complex64 forms: X32 = LU32 \ V32; corrections from plain FP32 residuals;
+// then compensated residuals R = V - (hi + lo) X64 and corrections until
+// max|R| <= refine_tol max|V| (the correction from that residual is applied)
+int refine_resident(Call& c) {
+  qbg_beyn* b = c.b;
+  cudaStream_t st = b->st;
+  const int n = b->n, nr = b->resn, L = c.L;
+  const size_t nl = c.nl;
+  const long long tot = (long long)(nl * nr);
+  int s = QBG_OK;
+  QBG_CUDA(cudaMemsetAsync(c.X64, 0, sizeof(cxd) * tot, st));
+  if ((s = c.timed_solve(c.V32, 0)) || (s = axpy_f2d(c.X32, c.X64, tot, st))) return s;
+  int sweeps = 0;
+  c.nhist = 0;
+  c.nf32 = 0;
+  const int nf = std::min(b->opts.fp32_sweeps > 0 ? b->opts.fp32_sweeps : 1, 4);
+  for (int q = 0; q < nf; ++q) {
+    // X32 holds the first solve's result for q == 0, a correction afterwards
+    if (q > 0 && (s = convert_d2f(c.X64, c.X32, tot, st))) return s;
+    QBG_CUDA(cudaMemsetAsync(c.dmax, 0, sizeof(double), st));
+    if ((s = broadcast_f(c.V32, (long long)nl, nr, c.R32, st)) ||
+        (s = gemm_batched<float>(n, L, n, cxf(-1.f, 0.f), b->Tcopy, n, b->ff.stride, c.X32, n, (long long)nl,
+                                 cxf(1.f, 0.f), c.R32, n, (long long)nl, nr, st)) ||
+        (s = maxabs_c64(c.R32, tot, c.dmax, st)) || (s = c.timed_solve(c.R32, (long long)nl)) ||
+        (s = axpy_f2d(c.X32, c.X64, tot, st)))
+      return s;
+    double fmax = 0.0;
+    QBG_CUDA(cudaMemcpyAsync(&fmax, c.dmax, sizeof(double), cudaMemcpyDeviceToHost, st));
+    QBG_CUDA(cudaStreamSynchronize(st));
+    if (c.nf32 < 4) c.f32hist[c.nf32++] = fmax / c.vmax;
+    ++sweeps;
+  }
+  double rel = 0.0;
+  for (int it = 0; it < b->opts.max_refine; ++it) {
+    QBG_CUDA(cudaMemsetAsync(c.dmax, 0, sizeof(double), st));
+    cudaEventRecord(b->ev[4], st);
+    if ((s = residual_df32(b->Tcopy, b->Tlo, b->ff.stride, c.X64, (long long)nl, c.dV, c.R64, (long long)nl, n, L,
+                           nr, c.dmax, st)))
+      return s;
+    cudaEventRecord(b->ev[5], st);
+    double rmax = 0.0;
+    QBG_CUDA(cudaMemcpyAsync(&rmax, c.dmax, sizeof(double), cudaMemcpyDeviceToHost, st));
+    QBG_CUDA(cudaStreamSynchronize(st));
+    float ms_r = 0.f;
+    if (cudaEventElapsedTime(&ms_r, b->ev[4], b->ev[5]) == cudaSuccess) {
+      c.ms_resid += ms_r;
+      ++c.n_resid;
+    }
+    rel = rmax / c.vmax;
+    if (c.nhist < 8) c.hist[c.nhist++] = rel;
+    ++sweeps;
+    // correction from this residual; when it already meets the tolerance this
+    // is the final correction (the residual is in hand, the solve costs one FP32 pass)
+    if ((s = convert_d2f(c.R64, c.R32, tot, st)) || (s = c.timed_solve(c.R32, (long long)nl)) ||
+        (s = axpy_f2d(c.X32, c.X64, tot, st)))
+      return s;
+    if (rel <= b->opts.refine_tol) break;
+  }
+  c.sweeps = std::max(c.sweeps, sweeps);
+  c.rel = std::max(c.rel, rel);
+  return QBG_OK;
+}
+
+// solves for the resident nodes and adds their moments to the disks' A0, A1
+int solve_and_accumulate(Call& c) {
+  qbg_beyn* b = c.b;
+  cudaStream_t st = b->st;
+  const int n = b->n, nr = b->resn, r0 = b->res0;
+  if (b->prec == QBG_PREC_FP64) {
+    QBG_TRY(lu_solve_shared<double>(b->fd, c.dV, c.L, c.X64, 0, st));
+  } else {
+    QBG_TRY(refine_resident(c));
+  }
+  for (int node = r0; node < r0 + nr;) {
+    const int d = node / b->nq;
+    const int end = std::min((d + 1) * b->nq, r0 + nr);
+    QBG_TRY(moments<double>(c.X64 + (size_t)(node - r0) * c.nl, (long long)c.nl, end - node, n, c.L, b->wj + node,
+                            b->zj + node, c.dA0 + (size_t)d * c.nl, c.dA1 + (size_t)d * c.nl, 1, st));
+    node = end;
+  }
+  return QBG_OK;
+}
+
+qbg_status create_impl(qbg_geom* g, const double* k0s, const double* Rs, int ndisk, int nq, int prec,
+                       const qbg_beyn_opts* opts, qbg_beyn** out) {
+  if (!g || !out || !k0s || !Rs || ndisk < 1 || nq < 2 || prec < 0 || prec > 2 ||
+      (long long)ndisk * nq > 65535) {
+    set_error("qbg_beyn_create: invalid arguments");
+    return QBG_EINVAL;
+  }
+  for (int d = 0; d < ndisk; ++d)
+    if (!(Rs[d] > 0.0) || !std::isfinite(Rs[d]) || !std::isfinite(k0s[2 * d]) || !std::isfinite(k0s[2 * d + 1])) {
+      set_error("qbg_beyn_create: disk %d has a non-finite centre or a radius <= 0", d);
+      return QBG_EINVAL;
+    }
+  *out = nullptr;
+  qbg_beyn* b = new (std::nothrow) qbg_beyn();
+  if (!b) {
+    set_error("host allocation failed");
+    return QBG_ENOMEM;
+  }
+  b->g = g;
+  b->n = (int)g->dim;
+  b->nq = nq;
+  b->ndisk = ndisk;
+  b->nn = nq * ndisk;
+  b->prec = prec;
+  b->opts = qbg_beyn_opts{};
+  b->opts.max_refine = 4;
+  b->opts.refine_tol = 1e-6;
+  if (opts) {
+    b->opts = *opts;
+    if (b->opts.max_refine <= 0) b->opts.max_refine = 4;
+    if (!(b->opts.refine_tol > 0.0)) b->opts.refine_tol = 1e-6;
+  }
+  b->cap = (b->opts.node_chunk > 0 && b->opts.node_chunk < b->nn) ? b->opts.node_chunk : b->nn;
+  int s = QBG_OK;
+  {
+    // the geometry was uploaded on its own stream
+    std::lock_guard<std::mutex> lk(g->mu);
+    cudaError_t e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) s = cuda_status(e, "geometry stream");
+  }
+  if (!s) {
+    cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) s = cuda_status(e, "cudaStreamCreate");
+  }
+  if (!s) s = setup(b, k0s, Rs);
+  if (!s && b->cap == b->nn) s = load(b, 0, b->nn);
+  if (s) {
+    delete b;
+    return s;
+  }
+  *out = b;
+  return QBG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+qbg_status qbg_beyn_create(qbg_geom* g, double k0_re, double k0_im, double R, int32_t nq, int32_t prec,
+                           const qbg_beyn_opts* opts, qbg_beyn** out) {
+  const double k0[2] = {k0_re, k0_im};
+  return create_impl(g, k0, &R, 1, nq, prec, opts, out);
+}
+
+qbg_status qbg_beyn_create_disks(qbg_geom* g, const double* k0s, const double* Rs, int32_t ndisk, int32_t nq,
+                                 int32_t prec, const qbg_beyn_opts* opts, qbg_beyn** out) {
+  return create_impl(g, k0s, Rs, ndisk, nq, prec, opts, out);
+}
+
+qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0, double* A1,
+                            qbg_beyn_stats* stats) {
+  if (!b || !V || !A0 || !A1 || L < 1 || L > (1 << 20)) {
+    set_error("qbg_beyn_moments: invalid arguments");
+    return QBG_EINVAL;
+  }
+  std::lock_guard<std::mutex> lk(b->mu);
+  const int n = b->n;
+  const bool dev = (b->opts.flags & QBG_PTR_DEVICE) != 0;
+  cudaStream_t st = b->st;
+  Call c;
+  c.b = b;
+  c.L = (int)L;
+  c.nl = (size_t)n * L;
+  const size_t nl = c.nl, nA = nl * b->ndisk;
+  if (dev) {
+    c.dV = (cxd*)V;
+    c.dA0 = (cxd*)A0;
+    c.dA1 = (cxd*)A1;
+  } else {
+    QBG_TRY(c.talloc(&c.dV, sizeof(cxd) * nl));
+    QBG_TRY(c.talloc(&c.dA0, sizeof(cxd) * nA));
+    QBG_TRY(c.talloc(&c.dA1, sizeof(cxd) * nA));
+    QBG_CUDA(cudaMemcpyAsync(c.dV, V, sizeof(cxd) * nl, cudaMemcpyHostToDevice, st));
+  }
+  QBG_CUDA(cudaMemsetAsync(c.dA0, 0, sizeof(cxd) * nA, st));
+  QBG_CUDA(cudaMemsetAsync(c.dA1, 0, sizeof(cxd) * nA, st));
+  const size_t cap = (size_t)b->cap;
+  QBG_TRY(c.talloc(&c.X64, sizeof(cxd) * nl * cap));
+  if (b->prec != QBG_PREC_FP64) {
+    QBG_TRY(c.talloc(&c.V32, sizeof(cxf) * nl));
+    QBG_TRY(c.talloc(&c.X32, sizeof(cxf) * nl * cap));
+    QBG_TRY(c.talloc(&c.R32, sizeof(cxf) * nl * cap));
+    QBG_TRY(c.talloc(&c.R64, sizeof(cxd) * nl * cap));
+    QBG_TRY(c.talloc(&c.dmax, sizeof(double)));
+    QBG_TRY(convert_d2f(c.dV, c.V32, (long long)nl, st));
+    // max |V| (|re| + |im|) scales the convergence test
+    std::vector<cxd> hv;
+    const cxd* hvp = reinterpret_cast<const cxd*>(V);
+    if (dev) {
+      hv.resize(nl);
+      QBG_CUDA(cudaMemcpyAsync(hv.data(), c.dV, sizeof(cxd) * nl, cudaMemcpyDeviceToHost, st));
+      QBG_CUDA(cudaStreamSynchronize(st));
+      hvp = hv.data();
+    }
+    double vmax = 0.0;
+    for (size_t q = 0; q < nl; ++q) vmax = std::max(vmax, std::fabs(hvp[q].re) + std::fabs(hvp[q].im));
+    c.vmax = vmax > 0.0 ? vmax : 1.0;
+  }
+  const bool streamed = b->cap < b->nn;
+  if (streamed) {
+    b->ms_assemble = 0.0;
+    b->ms_factor = 0.0;
+    b->singular = 0;
+  }
+  QBG_CUDA(cudaEventRecord(b->ev[3], st));
+  float ms_total = 0.f;
+  if (!streamed) {
+    QBG_TRY(solve_and_accumulate(c));
+  } else {
+    for (int n0 = 0; n0 < b->nn; n0 += b->cap) {
+      QBG_TRY(load(b, n0, std::min(b->cap, b->nn - n0)));
+      QBG_TRY(solve_and_accumulate(c));
+    }
+  }
+  if (!dev) {
+    QBG_CUDA(cudaMemcpyAsync(A0, c.dA0, sizeof(cxd) * nA, cudaMemcpyDeviceToHost, st));
+    QBG_CUDA(cudaMemcpyAsync(A1, c.dA1, sizeof(cxd) * nA, cudaMemcpyDeviceToHost, st));
+  }
+  cudaEvent_t e_end = nullptr;
+  QBG_CUDA(cudaEventCreate(&e_end));
+  cudaEventRecord(e_end, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  cudaEventElapsedTime(&ms_total, b->ev[3], e_end);
+  cudaEventDestroy(e_end);
+  if (e != cudaSuccess) return cuda_status(e, "qbg_beyn_moments");
+  if (b->prec != QBG_PREC_FP64) QBG_TRY(tc_check(st));
+  double ms_solves = 0.0;
+  for (size_t q = 0; q + 1 < c.sev.size(); q += 2) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c.sev[q], c.sev[q + 1]) == cudaSuccess) ms_solves += ms;
+  }
+  if (stats) {
+    stats->refine_sweeps = c.sweeps;
+    stats->refine_residual = c.rel;
+    stats->singular = b->singular;
+    stats->ms_assemble = b->ms_assemble;
+    stats->ms_factor = b->ms_factor;
+    // device time of this call; a streamed handle's assembly and factorisation are inside it
+    stats->ms_solve = streamed ? ms_total - b->ms_assemble - b->ms_factor : ms_total;
+    stats->nhist = c.nhist;
+    for (int q = 0; q < 8; ++q) stats->refine_history[q] = c.hist[q];
+    stats->ms_residual = c.ms_resid;
+    stats->n_residual = c.n_resid;
+    stats->nfp32 = c.nf32;
+    for (int q = 0; q < 4; ++q) stats->fp32_history[q] = c.f32hist[q];
+    stats->ms_solves = ms_solves;
+    stats->n_solves = (int)c.sev.size() / 2;
+  }
+  return QBG_OK;
+}
+
+qbg_status qbg_beyn_destroy(qbg_beyn* b) {
+  delete b;
+  return QBG_OK;
+}
+
+}  // extern "C"

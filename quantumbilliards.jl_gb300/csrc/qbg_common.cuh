@@ -85,6 +85,12 @@ int cuda_status(cudaError_t e, const char* what);
     if (_e != cudaSuccess) return qbg::cuda_status(_e, #call);  \
   } while (0)
 
+#define QBG_TRY(x)          \
+  do {                      \
+    int _s = (x);           \
+    if (_s) return _s;      \
+  } while (0)
+
 // Every kernel launch of the library is followed by exactly one
 // QBG_LAUNCH_CHECK, which also counts it (qbg_launch_count).
 #define QBG_LAUNCH_CHECK(what)                                              \

@@ -5,6 +5,7 @@
 #include <vector>
 #include "qbg_common.cuh"
 #include "qbg_geom.cuh"
+#include "qbg_assemble.cuh"
 
 namespace qbg {
 template <class P>
@@ -39,3 +40,13 @@ struct qbg_geom {
     return QBG_OK;
   }
 };
+
+namespace qbg {
+// host-side helpers shared by the entry-point translation units
+int check_ks(const double* ks, int64_t nk);  // finite, non-zero complex wavenumbers
+int cheb_params_check(const qbg_cheb_params* prm);
+qbg_cheb_params cheb_defaults(const qbg_cheb_params* prm);  // zeros -> 15000, 5, 3000, 5
+// Chebyshev tables for nk device wavenumbers (device buffers appended to tmp)
+int make_cheb(qbg_geom* g, const cxd* dks, int nk, const qbg_cheb_params& prm, ChebTables& t,
+              std::vector<void*>& tmp, cudaStream_t st);
+}  // namespace qbg

@@ -82,7 +82,7 @@ int axpy_f2d(const cxf* d, cxd* x, long long count, cudaStream_t st);  // x += d
 int tc_gemm_c64(int M, int N, int K, cxf alpha, const cxf* A, long long lda, long long sA, const cxf* B,
                 long long ldb, long long sB, cxf beta, cxf* C, long long ldc, long long sC, int batch,
                 cudaStream_t st, int batch2 = 1, long long sA2 = 0, long long sB2 = 0, long long sC2 = 0);
-// Reads and clears the tensor-core GEMM's device error flag (set when an
+// Reads the tensor-core GEMM's device error flag (set, and kept set, once an
 // mbarrier wait gave up); synchronizes the stream. Returns QBG_OK or QBG_ECUDA.
 int tc_check(cudaStream_t st);
 

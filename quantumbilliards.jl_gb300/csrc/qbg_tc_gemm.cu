@@ -370,8 +370,7 @@ int tc_check(cudaStream_t st) {
   int h = 0;
   QBG_CUDA(cudaMemcpy(&h, derr, sizeof(int), cudaMemcpyDeviceToHost));
   if (h != 0) {
-    const int z = 0;
-    QBG_CUDA(cudaMemcpy(derr, &z, sizeof(int), cudaMemcpyHostToDevice));
+    // sticky for the process, like a CUDA context error: every handle sees it
     set_error("tensor-core GEMM: an mbarrier wait gave up; results discarded");
     return QBG_ECUDA;
   }

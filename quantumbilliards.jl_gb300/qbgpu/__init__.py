@@ -14,7 +14,7 @@ from .operators import (Workspace, build_workspace, assemble, assemble_noalloc, 
                         construct_boundary_matrices,
                         construct_boundary_matrices_with_derivatives, bessel01, sigma_min, cgemm,
                         set_gemm_engine, launch_count)
-from .beyn import BeynHandle, construct_B_matrix, solve_vect, solve, probe_matrix, contour
+from .beyn import BeynHandle, construct_B_matrix, solve_vect, solve, solve_disks, probe_matrix, contour
 from .sweep import k_sweep, get_eigenvalues
 from .symmetry import (Reflection, Rotation, XReflection, YReflection, XYReflection,
                        periodic_symmetry_index_orbits)

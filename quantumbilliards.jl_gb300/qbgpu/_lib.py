@@ -60,7 +60,7 @@ class ChebParams(C.Structure):
 class BeynOpts(C.Structure):
     _fields_ = [("flags", C.c_int32), ("max_refine", C.c_int32), ("refine_tol", C.c_double), ("nb", C.c_int32),
                 ("eval_mode", C.c_int32), ("cheb", ChebParams), ("fp32_sweeps", C.c_int32),
-                ("solve_block", C.c_int32)]
+                ("solve_block", C.c_int32), ("node_chunk", C.c_int32)]
 
 
 class BeynStats(C.Structure):
@@ -97,6 +97,8 @@ _SIGS = {
                                   C.c_int32]),
     "qbg_set_gemm_engine": (C.c_int32, [C.c_int32]),
     "qbg_launch_count": (C.c_int32, [C.POINTER(C.c_uint64)]),
+    "qbg_beyn_create_disks": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32,
+                                          C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
 }
 
 _lib = None

@@ -36,20 +36,36 @@ def contour(k0: complex, R: float, nq: int):
 
 
 class BeynHandle:
-    """Contour nodes assembled and factored on the device (owns a qbg_beyn)."""
+    """Contour nodes assembled and factored on the device (owns a qbg_beyn).
 
-    def __init__(self, ws: Workspace, k0: complex, R: float, nq: int, mixed: bool = False, max_refine: int = 4,
+    k0 may be a sequence of disk centres (R a scalar or one radius per disk):
+    all disks' nodes are then assembled in one launch and factored as one
+    batch, and moments() returns arrays of shape (ndisk, N, L).
+    node_chunk > 0 keeps at most that many node operators resident and
+    streams the nodes through them in every moments() call."""
+
+    def __init__(self, ws: Workspace, k0, R, nq: int, mixed: bool = False, max_refine: int = 4,
                  refine_tol: float = 1e-6, nb: int = 0, use_chebyshev: bool = True, cheb=None, fp32_sweeps: int = 0,
-                 solve_block: int = 0):
+                 solve_block: int = 0, node_chunk: int = 0):
         lib = L.load()
-        self.ws, self.k0, self.R, self.nq = ws, complex(k0), float(R), int(nq)
+        self.multi = np.ndim(k0) > 0
+        k0s = np.atleast_1d(np.asarray(k0, dtype=np.complex128))
+        Rs = np.broadcast_to(np.asarray(R, dtype=np.float64), k0s.shape).copy()
+        self.ws, self.nq, self.ndisk = ws, int(nq), len(k0s)
+        self.k0s, self.Rs = k0s, Rs
+        self.k0, self.R = complex(k0s[0]), float(Rs[0])
         self.prec = L.prec_code(mixed)
         cp = L.ChebParams(*(cheb if cheb else (0, 0, 0, 0)))
         o = L.BeynOpts(0, int(max_refine), float(refine_tol), int(nb), 0 if use_chebyshev else 1, cp,
-                       int(fp32_sweeps), int(solve_block))
+                       int(fp32_sweeps), int(solve_block), int(node_chunk))
         h = C.c_void_p()
-        L.check(lib.qbg_beyn_create(ws.handle, self.k0.real, self.k0.imag, self.R, self.nq, self.prec, C.byref(o),
-                                    C.byref(h)))
+        if self.multi:
+            kk = np.ascontiguousarray(k0s).view(np.float64)
+            L.check(lib.qbg_beyn_create_disks(ws.handle, L.dptr(kk), L.dptr(Rs), self.ndisk, self.nq, self.prec,
+                                              C.byref(o), C.byref(h)))
+        else:
+            L.check(lib.qbg_beyn_create(ws.handle, self.k0.real, self.k0.imag, self.R, self.nq, self.prec,
+                                        C.byref(o), C.byref(h)))
         self._h = h
         self.N = ws.dim
         self.last_stats = None
@@ -60,8 +76,9 @@ class BeynHandle:
         N, r = V.shape
         if N != self.N:
             raise ValueError(f"V has {N} rows, the operator has {self.N}")
-        A0 = np.empty((N, r), dtype=np.complex128, order="F")
-        A1 = np.empty((N, r), dtype=np.complex128, order="F")
+        # per disk an N x r column-major block
+        A0 = np.empty((self.ndisk, r, N), dtype=np.complex128)
+        A1 = np.empty((self.ndisk, r, N), dtype=np.complex128)
         st = L.BeynStats()
         L.check(lib.qbg_beyn_moments(self._h, L.vptr(V), r, L.vptr(A0), L.vptr(A1), C.byref(st)))
         self.last_stats = dict(refine_sweeps=st.refine_sweeps, refine_residual=st.refine_residual,
@@ -70,7 +87,11 @@ class BeynHandle:
                                ms_residual=st.ms_residual, n_residual=st.n_residual,
                                fp32_history=list(st.fp32_history[:st.nfp32]), ms_solves=st.ms_solves,
                                n_solves=st.n_solves)
-        return A0, A1
+        A0 = A0.transpose(0, 2, 1)
+        A1 = A1.transpose(0, 2, 1)
+        if self.multi:
+            return A0, A1
+        return np.asfortranarray(A0[0]), np.asfortranarray(A1[0])
 
     def close(self):
         if getattr(self, "_h", None) and L.alive():
@@ -84,9 +105,62 @@ class BeynHandle:
             pass
 
 
+def _B_from_moments(A0, A1, svd_tol):
+    """Thin SVD of A0, absolute rank, B = U_k^H A1 W_k Sigma_k^-1 (beyn.jl:286-320)."""
+    U, S, Wh = np.linalg.svd(A0, full_matrices=False)
+    rk = int(np.count_nonzero(S >= svd_tol))
+    Uk = U[:, :rk]
+    Wk = Wh.conj().T[:, :rk]
+    B = Uk.conj().T @ ((A1 @ Wk) / S[:rk][None, :])
+    return B, Uk, rk, S
+
+
+def solve_disks(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed=False, ws=None,
+                return_info=False, **kw):
+    """Eigenvalues of several disks from one device batch: construct_B_matrix
+    for every disk (beyn.jl:257-322, one r -> 2r regrowth per disk, extending
+    the probe block) with the contour nodes of all disks resident together.
+    Returns a list of eigenvalue arrays, one per disk."""
+    rng = rng if rng is not None else np.random.default_rng(0)
+    ws = ws if ws is not None else Workspace(solver, pts)
+    N = ws.dim
+    k0s = np.atleast_1d(np.asarray(k0s, dtype=np.complex128))
+    bh = BeynHandle(ws, k0s, R, nq, mixed, **kw)
+    info = dict(stats=[], rk=[], r=[])
+    try:
+        V = probe_matrix(N, r, rng)
+        A0s, A1s = bh.moments(V)
+        info["stats"].append(bh.last_stats)
+        S = [np.linalg.svd(a, compute_uv=False) for a in A0s]
+        rks = [int(np.count_nonzero(s >= svd_tol)) for s in S]
+        grow = [rk == r and 2 * r < N for rk in rks]
+        if any(grow):
+            Vn = probe_matrix(N, r, rng)
+            A0n, A1n = bh.moments(Vn)
+            info["stats"].append(bh.last_stats)
+    finally:
+        bh.close()
+    out = []
+    for d in range(len(k0s)):
+        A0, A1 = A0s[d], A1s[d]
+        if grow[d]:
+            A0 = np.hstack([A0, A0n[d]])
+            A1 = np.hstack([A1, A1n[d]])
+        if rks[d] == 0:
+            out.append(np.zeros(0, complex))
+            info["rk"].append(0)
+            info["r"].append(r)
+            continue
+        B, Uk, rk, _ = _B_from_moments(A0, A1, svd_tol)
+        info["rk"].append(rk)
+        info["r"].append(A0.shape[1])
+        out.append(np.linalg.eigvals(B) if rk else np.zeros(0, complex))
+    return (out, info) if return_info else out
+
+
 def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=None, mixed=False, ws=None,
                        max_refine=4, refine_tol=1e-6, return_info=False, regrow="extend", use_chebyshev=True,
-                       cheb=None, fp32_sweeps=0, solve_block=0):
+                       cheb=None, fp32_sweeps=0, solve_block=0, node_chunk=0):
     """construct_B_matrix (beyn.jl:257-322). Returns (B, Uk) [, info].
 
     regrow: when the rank saturates (rk == r) the reference draws a fresh
@@ -99,7 +173,7 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
     if ws.dim != N:
         raise ValueError(f"N={N} does not match the operator dimension {ws.dim}")
     bh = BeynHandle(ws, k0, R, nq, mixed, max_refine, refine_tol, use_chebyshev=use_chebyshev, cheb=cheb,
-                    fp32_sweeps=fp32_sweeps, solve_block=solve_block)
+                    fp32_sweeps=fp32_sweeps, solve_block=solve_block, node_chunk=node_chunk)
     info = dict(stats=[])
     try:
         V = probe_matrix(N, r, rng)
