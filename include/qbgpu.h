@@ -53,7 +53,7 @@ enum { QBG_FORM_DLP = 0, QBG_FORM_CFIE = 1 };
  *                  against the FP32 operator: fastest, accuracy bounded by the
  *                  FP32 rounding of the operator. */
 enum { QBG_PREC_FP64 = 0, QBG_PREC_MIXED = 1, QBG_PREC_FP32 = 2 };
-enum { QBG_PTR_DEVICE = 1 };
+enum { QBG_PTR_DEVICE = 1, QBG_V_PER_DISK = 2 };
 
 /* Boundary discretisation (BoundaryPointsCFIE, boundarypoints.jl:487-503),
  * components concatenated; holes already orientation-reversed as
@@ -151,7 +151,8 @@ qbg_status qbg_assemble_noalloc(qbg_geom* g, const double* ks, int64_t nk, int32
  * wider V (the reference's r -> 2r regrowth, beyn.jl:291-309) without
  * refactoring. */
 typedef struct qbg_beyn_opts {
-  int32_t flags;        /* QBG_PTR_DEVICE: V, A0, A1 are device pointers */
+  int32_t flags;        /* QBG_PTR_DEVICE: V, A0, A1 are device pointers;
+                           QBG_V_PER_DISK: V holds one N x L probe block per disk */
   int32_t max_refine;   /* mixed form: maximum refinement sweeps (default 4) */
   double refine_tol;    /* complex64 forms: the first correction uses an FP32 residual; later residuals
                            are compensated; once max|R| <= tol * max|V| the correction from that
@@ -208,6 +209,67 @@ qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig)
 /* Device special functions, for validation: out[4*i..] = J0, J1, Y0, Y1 at z[i]
  * (complex interleaved). f32 = 1 selects the FP32 asymptotic evaluator. */
 qbg_status qbg_bessel01(const double* z, int64_t n, int32_t f32, double* out);
+
+/* ------------------------------------------------------------------------
+ * Request server (no reference counterpart: the reference runs one call at a
+ * time). Requests are admitted against an HBM budget (each request's device
+ * footprint is estimated before it starts), run on worker threads with their
+ * own CUDA streams, and queued Beyn requests on the same geometry with the
+ * same contour size, precision and probe count are merged into one multi-disk
+ * device batch (continuous batching: a request joins as soon as memory frees,
+ * it does not wait for a batch to fill). All buffers in a request are host
+ * memory owned by the caller and must stay valid until the request is done.
+ * ------------------------------------------------------------------------ */
+typedef struct qbg_server qbg_server;
+
+typedef struct qbg_serve_opts {
+  int64_t hbm_budget;   /* device bytes the running requests may hold (0 = 80% of free memory) */
+  int32_t workers;      /* requests in flight at once (0 = 4) */
+  int32_t max_batch;    /* most Beyn requests merged into one device batch (0 = 8; 1 = no merging) */
+} qbg_serve_opts;
+
+enum { QBG_REQ_BEYN = 0, QBG_REQ_EBIM = 1, QBG_REQ_SWEEP = 2 };
+
+typedef struct qbg_request_desc {
+  int32_t kind;     /* QBG_REQ_* */
+  qbg_geom* geom;
+  int32_t prec;     /* Beyn: QBG_PREC_*; EBIM and sweep run in FP64 */
+  /* Beyn (construct_B_matrix's device part): contour k0, R, nq; probe block V
+   * (N x L, host); outputs A0, A1 (N x L, host) */
+  double k0_re, k0_im, R;
+  int32_t nq;
+  int64_t L;
+  const double* V;
+  double* A0;
+  double* A1;
+  /* EBIM (A, A', A'' at one real k, ebim.jl:931-939): outputs N x N each */
+  double k;
+  double* out_A;
+  double* out_dA;
+  double* out_ddA;
+  /* sweep (sigma_min at nk real wavenumbers, k_sweep): sig[nk] */
+  const double* ks;
+  int64_t nk;
+  double* sig;
+} qbg_request_desc;
+
+typedef struct qbg_request_result {
+  int32_t status;      /* the request's own status (QBG_OK, ...) */
+  int32_t batched;     /* Beyn requests in the device batch this one ran in */
+  double queue_ms;     /* submit -> start */
+  double run_ms;       /* start -> done */
+} qbg_request_result;
+
+qbg_status qbg_serve_create(const qbg_serve_opts* opts, qbg_server** out);
+/* QBG_EBUDGET when the request alone does not fit the budget */
+qbg_status qbg_serve_submit(qbg_server* s, const qbg_request_desc* req, int64_t* id);
+/* done = 1 once the request has finished (successfully or not) */
+qbg_status qbg_serve_poll(qbg_server* s, int64_t id, int32_t* done);
+/* waits up to timeout_s seconds (< 0: no limit); QBG_ETIMEOUT if still running.
+ * On return with QBG_OK the request is finished and forgotten by the server. */
+qbg_status qbg_serve_wait(qbg_server* s, int64_t id, double timeout_s, qbg_request_result* res);
+/* finishes the queued and running requests, then stops the workers */
+qbg_status qbg_serve_destroy(qbg_server* s);
 
 /* Device complex64 GEMM, for validation: C_b = alpha A_b B_b + beta C_b for
  * b < batch, column-major host buffers (complex interleaved floats; A_b at

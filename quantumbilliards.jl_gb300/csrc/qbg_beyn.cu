@@ -204,6 +204,9 @@ struct Call {
   int L = 0;
   size_t nl = 0;
   cxd *dV = nullptr, *dA0 = nullptr, *dA1 = nullptr;
+  bool per_disk = false;  // V holds one N x L block per disk
+  cxd* Vn = nullptr;      // per-disk V: the resident nodes' blocks, node-major
+  cxf* Vn32 = nullptr;
   double vmax = 1.0;
   cxd *X64 = nullptr, *R64 = nullptr;
   cxf *V32 = nullptr, *X32 = nullptr, *R32 = nullptr;
@@ -252,7 +255,10 @@ int refine_resident(Call& c) {
   const long long tot = (long long)(nl * nr);
   int s = QBG_OK;
   QBG_CUDA(cudaMemsetAsync(c.X64, 0, sizeof(cxd) * tot, st));
-  if ((s = c.timed_solve(c.V32, 0)) || (s = axpy_f2d(c.X32, c.X64, tot, st))) return s;
+  const cxd* V64 = c.per_disk ? c.Vn : c.dV;
+  const cxf* V32 = c.per_disk ? c.Vn32 : c.V32;
+  const long long sV = c.per_disk ? (long long)nl : 0;
+  if ((s = c.timed_solve(V32, sV)) || (s = axpy_f2d(c.X32, c.X64, tot, st))) return s;
   int sweeps = 0;
   c.nhist = 0;
   c.nf32 = 0;
@@ -261,7 +267,11 @@ int refine_resident(Call& c) {
     // X32 holds the first solve's result for q == 0, a correction afterwards
     if (q > 0 && (s = convert_d2f(c.X64, c.X32, tot, st))) return s;
     QBG_CUDA(cudaMemsetAsync(c.dmax, 0, sizeof(double), st));
-    if ((s = broadcast_f(c.V32, (long long)nl, nr, c.R32, st)) ||
+    if (c.per_disk)
+      QBG_CUDA(cudaMemcpyAsync(c.R32, c.Vn32, sizeof(cxf) * tot, cudaMemcpyDeviceToDevice, st));
+    else if ((s = broadcast_f(c.V32, (long long)nl, nr, c.R32, st)))
+      return s;
+    if (
         (s = gemm_batched<float>(n, L, n, cxf(-1.f, 0.f), b->Tcopy, n, b->ff.stride, c.X32, n, (long long)nl,
                                  cxf(1.f, 0.f), c.R32, n, (long long)nl, nr, st)) ||
         (s = maxabs_c64(c.R32, tot, c.dmax, st)) || (s = c.timed_solve(c.R32, (long long)nl)) ||
@@ -277,8 +287,8 @@ int refine_resident(Call& c) {
   for (int it = 0; it < b->opts.max_refine; ++it) {
     QBG_CUDA(cudaMemsetAsync(c.dmax, 0, sizeof(double), st));
     cudaEventRecord(b->ev[4], st);
-    if ((s = residual_df32(b->Tcopy, b->Tlo, b->ff.stride, c.X64, (long long)nl, c.dV, c.R64, (long long)nl, n, L,
-                           nr, c.dmax, st)))
+    if ((s = residual_df32(b->Tcopy, b->Tlo, b->ff.stride, c.X64, (long long)nl, V64, sV, c.R64, (long long)nl, n,
+                           L, nr, c.dmax, st)))
       return s;
     cudaEventRecord(b->ev[5], st);
     double rmax = 0.0;
@@ -309,8 +319,18 @@ int solve_and_accumulate(Call& c) {
   qbg_beyn* b = c.b;
   cudaStream_t st = b->st;
   const int n = b->n, nr = b->resn, r0 = b->res0;
+  if (c.per_disk) {
+    // node j's right-hand side is its disk's probe block
+    for (int j = 0; j < nr; ++j) {
+      const int d = (r0 + j) / b->nq;
+      QBG_CUDA(cudaMemcpyAsync(c.Vn + (size_t)j * c.nl, c.dV + (size_t)d * c.nl, sizeof(cxd) * c.nl,
+                               cudaMemcpyDeviceToDevice, st));
+    }
+    if (b->prec != QBG_PREC_FP64) QBG_TRY(convert_d2f(c.Vn, c.Vn32, (long long)(c.nl * nr), st));
+  }
   if (b->prec == QBG_PREC_FP64) {
-    QBG_TRY(lu_solve_shared<double>(b->fd, c.dV, c.L, c.X64, 0, st));
+    QBG_TRY(lu_solve_shared<double>(b->fd, c.per_disk ? c.Vn : c.dV, c.L, c.X64, c.per_disk ? (long long)c.nl : 0,
+                                    st));
   } else {
     QBG_TRY(refine_resident(c));
   }
@@ -408,20 +428,26 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
   c.L = (int)L;
   c.nl = (size_t)n * L;
   const size_t nl = c.nl, nA = nl * b->ndisk;
+  c.per_disk = (b->opts.flags & QBG_V_PER_DISK) != 0 && b->ndisk > 1;
+  const size_t nV = c.per_disk ? nA : nl;
   if (dev) {
     c.dV = (cxd*)V;
     c.dA0 = (cxd*)A0;
     c.dA1 = (cxd*)A1;
   } else {
-    QBG_TRY(c.talloc(&c.dV, sizeof(cxd) * nl));
+    QBG_TRY(c.talloc(&c.dV, sizeof(cxd) * nV));
     QBG_TRY(c.talloc(&c.dA0, sizeof(cxd) * nA));
     QBG_TRY(c.talloc(&c.dA1, sizeof(cxd) * nA));
-    QBG_CUDA(cudaMemcpyAsync(c.dV, V, sizeof(cxd) * nl, cudaMemcpyHostToDevice, st));
+    QBG_CUDA(cudaMemcpyAsync(c.dV, V, sizeof(cxd) * nV, cudaMemcpyHostToDevice, st));
   }
   QBG_CUDA(cudaMemsetAsync(c.dA0, 0, sizeof(cxd) * nA, st));
   QBG_CUDA(cudaMemsetAsync(c.dA1, 0, sizeof(cxd) * nA, st));
   const size_t cap = (size_t)b->cap;
   QBG_TRY(c.talloc(&c.X64, sizeof(cxd) * nl * cap));
+  if (c.per_disk) {
+    QBG_TRY(c.talloc(&c.Vn, sizeof(cxd) * nl * cap));
+    if (b->prec != QBG_PREC_FP64) QBG_TRY(c.talloc(&c.Vn32, sizeof(cxf) * nl * cap));
+  }
   if (b->prec != QBG_PREC_FP64) {
     QBG_TRY(c.talloc(&c.V32, sizeof(cxf) * nl));
     QBG_TRY(c.talloc(&c.X32, sizeof(cxf) * nl * cap));
@@ -433,13 +459,13 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
     std::vector<cxd> hv;
     const cxd* hvp = reinterpret_cast<const cxd*>(V);
     if (dev) {
-      hv.resize(nl);
-      QBG_CUDA(cudaMemcpyAsync(hv.data(), c.dV, sizeof(cxd) * nl, cudaMemcpyDeviceToHost, st));
+      hv.resize(nV);
+      QBG_CUDA(cudaMemcpyAsync(hv.data(), c.dV, sizeof(cxd) * nV, cudaMemcpyDeviceToHost, st));
       QBG_CUDA(cudaStreamSynchronize(st));
       hvp = hv.data();
     }
     double vmax = 0.0;
-    for (size_t q = 0; q < nl; ++q) vmax = std::max(vmax, std::fabs(hvp[q].re) + std::fabs(hvp[q].im));
+    for (size_t q = 0; q < nV; ++q) vmax = std::max(vmax, std::fabs(hvp[q].re) + std::fabs(hvp[q].im));
     c.vmax = vmax > 0.0 ? vmax : 1.0;
   }
   const bool streamed = b->cap < b->nn;

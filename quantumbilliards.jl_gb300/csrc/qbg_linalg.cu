@@ -773,8 +773,8 @@ __device__ __forceinline__ void df_acc(float& sh, float& sl, float a, float bh, 
 template <bool LO>
 __global__ void __launch_bounds__(256) k_residual_df32(const cxf* __restrict__ Tm, const cxf* __restrict__ Tl,
                                                        long long sT, const cxd* __restrict__ X, long long sX,
-                                                       const cxd* __restrict__ V, cxd* R, long long sR, int n,
-                                                       int L, unsigned long long* rmax) {
+                                                       const cxd* __restrict__ V, long long sV, cxd* R,
+                                                       long long sR, int n, int L, unsigned long long* rmax) {
   constexpr int BM = 64, BN = 32, BK = 32;
   __shared__ cxf Ts[BK][BM];
   __shared__ cxf Tls[LO ? BK : 1][LO ? BM : 1];
@@ -786,6 +786,7 @@ __global__ void __launch_bounds__(256) k_residual_df32(const cxf* __restrict__ T
   const cxf* Tb = Tm + bz * sT;
   const cxf* Tlb = LO ? Tl + bz * sT : nullptr;
   const cxd* Xb = X + bz * sX;
+  const cxd* Vb = V + bz * sV;
   float hr[4][2], lr[4][2], hi_[4][2], li[4][2];
 #pragma unroll
   for (int a = 0; a < 4; ++a)
@@ -876,7 +877,7 @@ __global__ void __launch_bounds__(256) k_residual_df32(const cxf* __restrict__ T
     for (int a = 0; a < 4; ++a) {
       const int gi = m0 + tx + 16 * a;
       if (gi >= n) continue;
-      const cxd v = V[(long long)gi + (long long)gj * n];
+      const cxd v = Vb[(long long)gi + (long long)gj * n];
       const cxd r(v.re - accr[a][b], v.im - acci[a][b]);
       R[bz * sR + (long long)gi + (long long)gj * n] = r;
       lmax = fmax(lmax, fabs(r.re) + fabs(r.im));
@@ -887,14 +888,14 @@ __global__ void __launch_bounds__(256) k_residual_df32(const cxf* __restrict__ T
   if ((tid & 31) == 0 && rmax) atomicMax(rmax, (unsigned long long)__double_as_longlong(lmax));
 }
 
-int residual_df32(const cxf* Tm, const cxf* Tlo, long long sT, const cxd* X, long long sX, const cxd* V, cxd* R,
-                  long long sR, int n, int L, int batch, double* rmax, cudaStream_t st) {
+int residual_df32(const cxf* Tm, const cxf* Tlo, long long sT, const cxd* X, long long sX, const cxd* V,
+                  long long sV, cxd* R, long long sR, int n, int L, int batch, double* rmax, cudaStream_t st) {
   dim3 grd((n + 63) / 64, (L + 31) / 32, batch);
   auto* rm = reinterpret_cast<unsigned long long*>(rmax);
   if (Tlo)
-    k_residual_df32<true><<<grd, 256, 0, st>>>(Tm, Tlo, sT, X, sX, V, R, sR, n, L, rm);
+    k_residual_df32<true><<<grd, 256, 0, st>>>(Tm, Tlo, sT, X, sX, V, sV, R, sR, n, L, rm);
   else
-    k_residual_df32<false><<<grd, 256, 0, st>>>(Tm, nullptr, sT, X, sX, V, R, sR, n, L, rm);
+    k_residual_df32<false><<<grd, 256, 0, st>>>(Tm, nullptr, sT, X, sX, V, sV, R, sR, n, L, rm);
   QBG_LAUNCH_CHECK("k_residual_df32");
   return QBG_OK;
 }

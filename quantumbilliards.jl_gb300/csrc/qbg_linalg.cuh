@@ -63,11 +63,12 @@ int moments(const cx<T>* X, long long sX, int batch, int n, int L, const cxd* w,
             int accumulate, cudaStream_t st);
 
 // Mixed-form refinement pieces.
-// R_b = V - (T_b + Tlo_b) X_b computed with compensated FP32 products
-// (double-float) flushed to FP64 every 32 terms; T_b, Tlo_b complex64 (Tlo may
-// be null), X_b complex128. rmax receives max |R| (|re|+|im|), must be zeroed.
-int residual_df32(const cxf* Tm, const cxf* Tlo, long long sT, const cxd* X, long long sX, const cxd* V, cxd* R,
-                  long long sR, int n, int L, int batch, double* rmax, cudaStream_t st);
+// R_b = V_b - (T_b + Tlo_b) X_b computed with compensated FP32 products
+// (double-float) flushed to FP64 every 256 terms; T_b, Tlo_b complex64 (Tlo
+// may be null), X_b, V_b = V + b sV complex128 (sV = 0: one V for all). rmax
+// receives max |R| (|re|+|im|), must be zeroed.
+int residual_df32(const cxf* Tm, const cxf* Tlo, long long sT, const cxd* X, long long sX, const cxd* V,
+                  long long sV, cxd* R, long long sR, int n, int L, int batch, double* rmax, cudaStream_t st);
 int convert_d2f(const cxd* in, cxf* out, long long count, cudaStream_t st);
 // out = max(out, max_e |re x_e| + |im x_e|); out must be zeroed (or hold a
 // previous maximum) before the first call

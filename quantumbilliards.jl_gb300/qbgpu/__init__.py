@@ -16,6 +16,7 @@ from .operators import (Workspace, build_workspace, assemble, assemble_noalloc, 
                         set_gemm_engine, launch_count)
 from .beyn import BeynHandle, construct_B_matrix, solve_vect, solve, solve_disks, probe_matrix, contour
 from .sweep import k_sweep, get_eigenvalues
+from .serve import Server
 from .symmetry import (Reflection, Rotation, XReflection, YReflection, XYReflection,
                        periodic_symmetry_index_orbits)
 

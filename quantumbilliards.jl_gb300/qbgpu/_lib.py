@@ -19,6 +19,7 @@ QBG_OK, QBG_EINVAL, QBG_ENOMEM, QBG_EBUDGET, QBG_ESINGULAR, QBG_ETIMEOUT, QBG_EC
 QBG_FORM_DLP, QBG_FORM_CFIE = 0, 1
 QBG_PREC_FP64, QBG_PREC_MIXED, QBG_PREC_FP32 = 0, 1, 2
 QBG_PTR_DEVICE = 1
+QBG_V_PER_DISK = 2
 
 
 def prec_code(p) -> int:
@@ -72,6 +73,22 @@ class BeynStats(C.Structure):
 
 
 # symbol -> (restype, argtypes); the list is the ABI surface the tests check
+class ServeOpts(C.Structure):
+    _fields_ = [("hbm_budget", C.c_int64), ("workers", C.c_int32), ("max_batch", C.c_int32)]
+
+
+class RequestDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("geom", C.c_void_p), ("prec", C.c_int32),
+                ("k0_re", C.c_double), ("k0_im", C.c_double), ("R", C.c_double), ("nq", C.c_int32),
+                ("L", C.c_int64), ("V", C.c_void_p), ("A0", C.c_void_p), ("A1", C.c_void_p),
+                ("k", C.c_double), ("out_A", C.c_void_p), ("out_dA", C.c_void_p), ("out_ddA", C.c_void_p),
+                ("ks", C.c_void_p), ("nk", C.c_int64), ("sig", C.c_void_p)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("status", C.c_int32), ("batched", C.c_int32), ("queue_ms", C.c_double), ("run_ms", C.c_double)]
+
+
 _SIGS = {
     "qbg_version": (C.c_int32, [C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "qbg_last_error": (C.c_size_t, [C.c_char_p, C.c_size_t]),
@@ -96,6 +113,11 @@ _SIGS = {
                                   C.c_int64, C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.c_void_p, C.c_int64,
                                   C.c_int32]),
     "qbg_set_gemm_engine": (C.c_int32, [C.c_int32]),
+    "qbg_serve_create": (C.c_int32, [C.POINTER(ServeOpts), C.POINTER(C.c_void_p)]),
+    "qbg_serve_submit": (C.c_int32, [C.c_void_p, C.POINTER(RequestDesc), C.POINTER(C.c_int64)]),
+    "qbg_serve_poll": (C.c_int32, [C.c_void_p, C.c_int64, C.POINTER(C.c_int32)]),
+    "qbg_serve_wait": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double, C.POINTER(RequestResult)]),
+    "qbg_serve_destroy": (C.c_int32, [C.c_void_p]),
     "qbg_launch_count": (C.c_int32, [C.POINTER(C.c_uint64)]),
     "qbg_beyn_create_disks": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32,
                                           C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
