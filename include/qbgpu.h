@@ -206,6 +206,16 @@ qbg_status qbg_beyn_destroy(qbg_beyn* b);
  * sweepmethods.jl:132-152). */
 qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig);
 
+/* Panel autotuner (chebyshev_params, chebyshev_optimal_panelization.jl:221-307):
+ * starting from *io (zeros = 15000, 5, 3000, 5), grows the panel counts by
+ * 1.5x per iteration (every 5th iteration the degrees by 2 instead) until the
+ * max absolute error of the interpolated H0, H1 (on [rmin, rmax]) and J0, J1
+ * (on [0, rmax]) at nsample radii is below tol for every wavenumber. Writes
+ * the parameters to *io and the worst errors to err4 (may be null). Returns
+ * QBG_ETIMEOUT with the best effort when max_iter is reached. */
+qbg_status qbg_cheb_autotune(qbg_geom* g, const double* ks, int64_t nk, double tol, int32_t nsample,
+                             int32_t max_iter, qbg_cheb_params* io, double* err4);
+
 /* Device special functions, for validation: out[4*i..] = J0, J1, Y0, Y1 at z[i]
  * (complex interleaved). f32 = 1 selects the FP32 asymptotic evaluator. */
 qbg_status qbg_bessel01(const double* z, int64_t n, int32_t f32, double* out);

@@ -378,6 +378,73 @@ qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig)
   return QBG_OK;
 }
 
+// chebyshev_params (chebyshev_optimal_panelization.jl:221-307): grow the panel
+// counts by 1.5 (every 5th iteration the degrees by 2 instead) until the max
+// absolute error of every interpolated H0, H1, J0, J1 over all wavenumbers is
+// below tol at nsample radii.
+qbg_status qbg_cheb_autotune(qbg_geom* g, const double* ks, int64_t nk, double tol, int32_t nsample,
+                             int32_t max_iter, qbg_cheb_params* io, double* err4) {
+  if (!g || !ks || !io || nk < 1 || nk > 65535 || !(tol > 0.0) || nsample < 2 || max_iter < 1) {
+    set_error("qbg_cheb_autotune: invalid arguments");
+    return QBG_EINVAL;
+  }
+  QBG_TRY(check_ks(ks, nk));
+  qbg_cheb_params p = cheb_defaults(io);
+  QBG_TRY(cheb_params_check(&p));
+  std::lock_guard<std::mutex> lk(g->mu);
+  cudaStream_t st = g->stream;
+  cxd* dks = nullptr;
+  unsigned long long* derr = nullptr;
+  QBG_TRY(dmalloc(&dks, sizeof(cxd) * nk));
+  int s = dmalloc(&derr, sizeof(unsigned long long) * 4 * nk);
+  if (s) { cudaFree(dks); return s; }
+  std::vector<unsigned long long> herr(4 * nk);
+  double worst[4] = {0, 0, 0, 0};
+  cudaError_t e = cudaMemcpyAsync(dks, ks, sizeof(cxd) * nk, cudaMemcpyHostToDevice, st);
+  bool ok = false;
+  for (int it = 1; e == cudaSuccess && !s && it <= max_iter; ++it) {
+    std::vector<void*> ctmp;
+    ChebTables t;
+    s = make_cheb(g, dks, (int)nk, p, t, ctmp, st);
+    if (!s) e = cudaMemsetAsync(derr, 0, sizeof(unsigned long long) * 4 * nk, st);
+    if (!s && e == cudaSuccess) s = cheb_errors(t, dks, nsample, derr, st);
+    if (!s && e == cudaSuccess)
+      e = cudaMemcpyAsync(herr.data(), derr, sizeof(unsigned long long) * 4 * nk, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    for (void* q : ctmp) cudaFree(q);
+    if (s || e != cudaSuccess) break;
+    for (int f = 0; f < 4; ++f) worst[f] = 0.0;
+    for (int64_t q = 0; q < nk; ++q)
+      for (int f = 0; f < 4; ++f) {
+        double v;
+        memcpy(&v, &herr[4 * q + f], sizeof(double));
+        worst[f] = std::max(worst[f], v);
+      }
+    const bool okH = worst[0] < tol && worst[1] < tol, okJ = worst[2] < tol && worst[3] < tol;
+    if (okH && okJ) { ok = true; break; }
+    if (it == max_iter) break;
+    auto grow = [&](int& npan, int& M) {
+      if (it % 5 == 0 && M + 2 <= QBG_CHEB_MAX_DEGREE) M += 2;
+      else npan = (int)std::ceil(1.5 * (double)npan);
+    };
+    if (!okH) grow(p.n_panels_h, p.M_h);
+    if (!okJ) grow(p.n_panels_j, p.M_j);
+    if (p.n_panels_h > (1 << 24) || p.n_panels_j > (1 << 24)) break;
+  }
+  cudaFree(dks);
+  cudaFree(derr);
+  if (s) return s;
+  if (e != cudaSuccess) return cuda_status(e, "qbg_cheb_autotune");
+  *io = p;
+  if (err4)
+    for (int f = 0; f < 4; ++f) err4[f] = worst[f];
+  if (!ok) {
+    set_error("Chebyshev tuning did not reach tol = %g after %d iterations (best effort returned)", tol, max_iter);
+    return QBG_ETIMEOUT;
+  }
+  return QBG_OK;
+}
+
 qbg_status qbg_bessel01(const double* z, int64_t n, int32_t f32, double* out) {
   if (!z || !out || n < 1) { set_error("qbg_bessel01: invalid arguments"); return QBG_EINVAL; }
   cxd *dz = nullptr, *dout = nullptr;

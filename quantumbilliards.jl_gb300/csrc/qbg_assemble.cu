@@ -812,6 +812,55 @@ int cheb_r_range(const GeomDev& g, unsigned long long* dscratch2, double* rmin, 
   return QBG_OK;
 }
 
+// Panel error check of the autotuner (chebyshev_optimal_panelization.jl:221-307):
+// max |interpolated - direct| of H0, H1 at ns radii uniform on [t.rmin, t.rmax]
+// and of J0, J1 at ns radii uniform on [0, t.rmax], per wavenumber;
+// err[4 q + f] (f = H0, H1, J0, J1) holds the bits of non-negative doubles.
+__global__ void k_cheb_errors(ChebTables t, const cxd* __restrict__ ks, int ns, unsigned long long* err) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int q = blockIdx.y;
+  const cxd k = ks[q];
+  const bool realk = (k.im == 0.0);
+  double e[4] = {0.0, 0.0, 0.0, 0.0};
+  if (s < ns) {
+    const double u = ns > 1 ? (double)s / (double)(ns - 1) : 0.0;
+    const double rh = t.rmin + (t.rmax - t.rmin) * u;
+    int p;
+    double tt;
+    cxd v0, v1;
+    panel_of(rh, t.rmin, t.rmax, t.dr_h, t.invdr_h, t.nh, p, tt);
+    clenshaw2(t.H + (((size_t)q * t.nh + p) * (t.Mh + 1)) * 2, t.Mh, tt, v0, v1);
+    const Bessel01d bh = bessel01(rh * k);
+    e[0] = cabs_d(v0 - bh.h0());
+    e[1] = cabs_d(v1 - bh.h1());
+    const double rj = t.rmax * u;
+    panel_of(rj, 0.0, t.rmax, t.dr_j, t.invdr_j, t.nj, p, tt);
+    clenshaw2(t.J + (((size_t)q * t.nj + p) * (t.Mj + 1)) * 2, t.Mj, tt, v0, v1);
+    cxd j0(1.0, 0.0), j1(0.0, 0.0);
+    if (rj > 0.0) {
+      Bessel01d bj = bessel01(rj * k);
+      if (realk) { bj.j0.im = 0.0; bj.j1.im = 0.0; }
+      j0 = bj.j0;
+      j1 = bj.j1;
+    }
+    e[2] = cabs_d(v0 - j0);
+    e[3] = cabs_d(v1 - j1);
+  }
+#pragma unroll
+  for (int f = 0; f < 4; ++f) {
+    double m = e[f];
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(&err[4 * q + f], (unsigned long long)__double_as_longlong(m));
+  }
+}
+
+int cheb_errors(const ChebTables& t, const cxd* ks, int ns, unsigned long long* err, cudaStream_t st) {
+  dim3 grd((ns + 255) / 256, t.nk);
+  k_cheb_errors<<<grd, 256, 0, st>>>(t, ks, ns, err);
+  QBG_LAUNCH_CHECK("k_cheb_errors");
+  return QBG_OK;
+}
+
 int cheb_build(ChebTables& t, const cxd* ks, cudaStream_t st) {
   const int npmax = t.nh > t.nj ? t.nh : t.nj;
   dim3 grd((npmax + 127) / 128, t.nk, 2);

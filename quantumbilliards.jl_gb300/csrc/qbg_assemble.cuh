@@ -23,6 +23,8 @@ struct ChebTables {
 // min / max pair distance over all off-diagonal pairs (host values; dscratch2 = 2 device words)
 int cheb_r_range(const GeomDev& g, unsigned long long* dscratch2, double* rmin, double* rmax, cudaStream_t st);
 int cheb_build(ChebTables& t, const cxd* ks, cudaStream_t st);
+// max interpolation errors of H0, H1, J0, J1 per wavenumber at ns sampled radii (err: 4 nk zeroed words)
+int cheb_errors(const ChebTables& t, const cxd* ks, int ns, unsigned long long* err, cudaStream_t st);
 int launch_assemble_cheb(const GeomDev& g, const ChebTables& t, const cxd* ks, int nk, int deriv, int prec,
                          void* const* outs_dev, void* const* lo_outs_dev, long long ld, cudaStream_t st);
 int launch_bessel_eval(const cxd* z, int n, cxd* out, int f32, cudaStream_t st);

@@ -40,6 +40,7 @@ template <class T> QBG_HD cx<T>& operator-=(cx<T>& a, cx<T> b) { a.re -= b.re; a
 template <class T> QBG_HD cx<T> cmul_i(cx<T> a) { return {-a.im, a.re}; }          // i*a
 template <class T> QBG_HD T cabs2(cx<T> a) { return a.re * a.re + a.im * a.im; }
 template <class T> QBG_HD T cabs1(cx<T> a) { return fabs(a.re) + fabs(a.im); }  // LAPACK izamax measure
+QBG_HD double cabs_d(cx<double> a) { return hypot(a.re, a.im); }
 template <class T> QBG_HD cx<T> conj(cx<T> a) { return {a.re, -a.im}; }
 template <class T> QBG_HD cx<T> cinv(cx<T> a) {
   // 1/a with Smith's scaling to avoid overflow in |a|^2

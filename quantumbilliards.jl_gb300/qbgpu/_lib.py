@@ -72,7 +72,6 @@ class BeynStats(C.Structure):
                 ("ms_solves", C.c_double), ("n_solves", C.c_int32)]
 
 
-# symbol -> (restype, argtypes); the list is the ABI surface the tests check
 class ServeOpts(C.Structure):
     _fields_ = [("hbm_budget", C.c_int64), ("workers", C.c_int32), ("max_batch", C.c_int32)]
 
@@ -89,6 +88,7 @@ class RequestResult(C.Structure):
     _fields_ = [("status", C.c_int32), ("batched", C.c_int32), ("queue_ms", C.c_double), ("run_ms", C.c_double)]
 
 
+# symbol -> (restype, argtypes); the list is the ABI surface the tests check
 _SIGS = {
     "qbg_version": (C.c_int32, [C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "qbg_last_error": (C.c_size_t, [C.c_char_p, C.c_size_t]),
@@ -119,6 +119,8 @@ _SIGS = {
     "qbg_serve_wait": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double, C.POINTER(RequestResult)]),
     "qbg_serve_destroy": (C.c_int32, [C.c_void_p]),
     "qbg_launch_count": (C.c_int32, [C.POINTER(C.c_uint64)]),
+    "qbg_cheb_autotune": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.c_double, C.c_int32,
+                                      C.c_int32, C.POINTER(ChebParams), C.POINTER(C.c_double)]),
     "qbg_beyn_create_disks": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32,
                                           C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
 }

@@ -159,6 +159,23 @@ def construct_boundary_matrices_with_derivatives(solver, pts, zj, ws: Workspace 
     return out[:nk], out[nk:2 * nk], out[2 * nk:]
 
 
+def chebyshev_params(solver, pts, zj, ws: Workspace = None, npanels_h_init=15000, M_h_init=5, npanels_j_init=3000,
+                     M_j_init=5, tol=1e-10, sampling_points=50000, max_iter=20, strict=False):
+    """chebyshev_params (chebyshev_optimal_panelization.jl:221-307) on the device.
+
+    Returns (n_panels_h, M_h, n_panels_j, M_j, errors[H0, H1, J0, J1]). When
+    max_iter is reached the best effort is returned (strict=True raises)."""
+    ws = ws if ws is not None else Workspace(solver, pts)
+    k = _ks_array(zj)
+    prm = L.ChebParams(int(npanels_h_init), int(M_h_init), int(npanels_j_init), int(M_j_init))
+    err = np.zeros(4)
+    st = L.load().qbg_cheb_autotune(ws.handle, L.dptr(k.view(np.float64)), len(k), float(tol), int(sampling_points),
+                                    int(max_iter), C.byref(prm), L.dptr(err))
+    if st != L.QBG_OK and (strict or st != L.QBG_ETIMEOUT):
+        L.check(st)
+    return prm.n_panels_h, prm.M_h, prm.n_panels_j, prm.M_j, err
+
+
 def bessel01(z, f32: bool = False) -> np.ndarray:
     """Device J0, J1, Y0, Y1 at complex z (validation helper): shape (n, 4)."""
     lib = L.load()
