@@ -216,6 +216,15 @@ qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig)
 qbg_status qbg_cheb_autotune(qbg_geom* g, const double* ks, int64_t nk, double tol, int32_t nsample,
                              int32_t max_iter, qbg_cheb_params* io, double* err4);
 
+/* Residuals of Beyn candidates, the device part of residual_and_norm_select
+ * and imag_k_check_EXPERIMENTAL (beyn.jl:557-593, 623-721): for each candidate
+ * j (lambdas: n complex) assembles T(lambda_j) in FP64 (through the Chebyshev
+ * panels when cheb != NULL, zeros = defaults) and writes
+ * out[5 j + 0..4] = ||T phi_j||_2, ||T phi_j||_1, opnorm(T, 1), ||phi_j||_1,
+ * ||phi_j||_2 with Phi the N x n column-major block (host) of phi_j = U_k Y_j. */
+qbg_status qbg_candidate_residuals(qbg_geom* g, const double* lambdas, int64_t n, const double* Phi,
+                                   const qbg_cheb_params* cheb, double* out);
+
 /* Device special functions, for validation: out[4*i..] = J0, J1, Y0, Y1 at z[i]
  * (complex interleaved). f32 = 1 selects the FP32 asymptotic evaluator. */
 qbg_status qbg_bessel01(const double* z, int64_t n, int32_t f32, double* out);

@@ -445,6 +445,85 @@ qbg_status qbg_cheb_autotune(qbg_geom* g, const double* ks, int64_t nk, double t
   return QBG_OK;
 }
 
+// residual_and_norm_select's device part (beyn.jl:557-593): T(lambda_j) at
+// each candidate, y = T phi_j, and the norms the selection uses
+qbg_status qbg_candidate_residuals(qbg_geom* g, const double* lambdas, int64_t n, const double* Phi,
+                                   const qbg_cheb_params* cheb, double* out) {
+  if (!g || !lambdas || !Phi || !out || n < 1) {
+    set_error("qbg_candidate_residuals: invalid arguments");
+    return QBG_EINVAL;
+  }
+  QBG_TRY(check_ks(lambdas, n));
+  qbg_cheb_params cp{};
+  if (cheb) {
+    cp = cheb_defaults(cheb);
+    QBG_TRY(cheb_params_check(&cp));
+  }
+  std::lock_guard<std::mutex> lk(g->mu);
+  const int N = (int)g->dim;
+  cudaStream_t st = g->stream;
+  const int chunk = (int)std::min<int64_t>(n, 8);
+  const size_t NN = (size_t)N * N;
+  cxd *T = nullptr, *dl = nullptr, *phi = nullptr, *y = nullptr;
+  double *nrm = nullptr, *an = nullptr;
+  void** dptrs = nullptr;
+  std::vector<void*> tmp;
+  auto cleanup = [&]() { for (void* p : tmp) cudaFree(p); };
+  auto talloc = [&](auto** p, size_t bytes) {
+    int s = dmalloc(p, bytes);
+    if (!s) tmp.push_back(*p);
+    return s;
+  };
+  int s = QBG_OK;
+  if ((s = talloc(&T, sizeof(cxd) * NN * chunk)) || (s = talloc(&dl, sizeof(cxd) * n)) ||
+      (s = talloc(&phi, sizeof(cxd) * (size_t)N * chunk)) || (s = talloc(&y, sizeof(cxd) * (size_t)N * chunk)) ||
+      (s = talloc(&nrm, sizeof(double) * 4 * chunk)) || (s = talloc(&an, sizeof(double) * chunk)) ||
+      (s = talloc(&dptrs, sizeof(void*) * chunk))) {
+    cleanup();
+    return s;
+  }
+  std::vector<void*> hp(chunk);
+  for (int q = 0; q < chunk; ++q) hp[q] = T + (size_t)q * NN;
+  cudaError_t e = cudaMemcpyAsync(dl, lambdas, sizeof(cxd) * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dptrs, hp.data(), sizeof(void*) * chunk, cudaMemcpyHostToDevice, st);
+  std::vector<double> hn(4 * chunk), ha(chunk);
+  for (int64_t q0 = 0; e == cudaSuccess && !s && q0 < n; q0 += chunk) {
+    const int c = (int)std::min<int64_t>(chunk, n - q0);
+    e = cudaMemcpyAsync(phi, Phi + 2 * (size_t)N * q0, sizeof(cxd) * (size_t)N * c, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) break;
+    std::vector<void*> ctmp;
+    if (cheb) {
+      ChebTables t;
+      s = make_cheb(g, dl + q0, c, cp, t, ctmp, st);
+      if (!s) s = launch_assemble_cheb(g->d, t, dl + q0, c, 0, QBG_PREC_FP64, dptrs, nullptr, N, st);
+    } else {
+      s = launch_assemble(g->d, dl + q0, c, 0, QBG_PREC_FP64, dptrs, N, st);
+    }
+    if (!s) s = gemm_batched<double>(N, 1, N, cxd(1.0, 0.0), T, N, (long long)NN, phi, N, N, cxd(0.0, 0.0), y, N, N,
+                                     c, st);
+    if (!s) e = cudaMemsetAsync(an, 0, sizeof(double) * c, st);
+    if (!s && e == cudaSuccess) s = opnorm1_batched(T, N, (long long)NN, c, an, st);
+    if (!s && e == cudaSuccess) s = vec_norms(y, phi, N, c, nrm, st);
+    if (!s && e == cudaSuccess) e = cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * 4 * c, cudaMemcpyDeviceToHost, st);
+    if (!s && e == cudaSuccess) e = cudaMemcpyAsync(ha.data(), an, sizeof(double) * c, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    for (void* p : ctmp) cudaFree(p);
+    if (s || e != cudaSuccess) break;
+    for (int q = 0; q < c; ++q) {
+      double* o = out + 5 * (q0 + q);
+      o[0] = std::sqrt(hn[4 * q + 0]);  // ||T phi||_2
+      o[1] = hn[4 * q + 1];             // ||T phi||_1
+      o[2] = ha[q];                     // opnorm(T, 1)
+      o[3] = hn[4 * q + 2];             // ||phi||_1
+      o[4] = std::sqrt(hn[4 * q + 3]);  // ||phi||_2
+    }
+  }
+  cleanup();
+  if (s) return s;
+  if (e != cudaSuccess) return cuda_status(e, "qbg_candidate_residuals");
+  return QBG_OK;
+}
+
 qbg_status qbg_bessel01(const double* z, int64_t n, int32_t f32, double* out) {
   if (!z || !out || n < 1) { set_error("qbg_bessel01: invalid arguments"); return QBG_EINVAL; }
   cxd *dz = nullptr, *dout = nullptr;

@@ -938,6 +938,65 @@ int maxabs_c64(const cxf* x, long long count, double* out, cudaStream_t st) {
   QBG_LAUNCH_CHECK("k_maxabs_c64");
   return QBG_OK;
 }
+// column |.|-sums of a batch of n x n complex128 matrices: out[b] = max_j sum_i |A_b(i, j)|
+// (opnorm(A, 1)); one CTA per (column, matrix); out holds non-negative double bits, zeroed
+__global__ void k_opnorm1(const cxd* __restrict__ A, int n, long long sA, unsigned long long* out) {
+  const int j = blockIdx.x, b = blockIdx.y;
+  const cxd* col = A + (long long)b * sA + (long long)j * n;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += hypot(col[i].re, col[i].im);
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (int)(blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) atomicMax(&out[b], (unsigned long long)__double_as_longlong(s));
+  }
+}
+
+// per column b of the n x batch blocks y, phi: out[4 b + 0..3] = ||y||_2^2, ||y||_1, ||phi||_1, ||phi||_2^2
+__global__ void k_vec_norms(const cxd* __restrict__ y, const cxd* __restrict__ phi, int n, double* out) {
+  const int b = blockIdx.x;
+  double a[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const cxd u = y[(long long)b * n + i], v = phi[(long long)b * n + i];
+    a[0] += u.re * u.re + u.im * u.im;
+    a[1] += hypot(u.re, u.im);
+    a[2] += hypot(v.re, v.im);
+    a[3] += v.re * v.re + v.im * v.im;
+  }
+  __shared__ double red[4][32];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    double s = a[q];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      double s = threadIdx.x < (int)(blockDim.x >> 5) ? red[q][threadIdx.x] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (threadIdx.x == 0) out[4 * b + q] = s;
+    }
+  }
+}
+
+int opnorm1_batched(const cxd* A, int n, long long sA, int batch, double* out, cudaStream_t st) {
+  k_opnorm1<<<dim3(n, batch), 256, 0, st>>>(A, n, sA, reinterpret_cast<unsigned long long*>(out));
+  QBG_LAUNCH_CHECK("k_opnorm1");
+  return QBG_OK;
+}
+
+int vec_norms(const cxd* y, const cxd* phi, int n, int batch, double* out, cudaStream_t st) {
+  k_vec_norms<<<batch, 256, 0, st>>>(y, phi, n, out);
+  QBG_LAUNCH_CHECK("k_vec_norms");
+  return QBG_OK;
+}
+
 int convert_d2f(const cxd* in, cxf* out, long long count, cudaStream_t st) {
   k_d2f<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(in, out, count);
   QBG_LAUNCH_CHECK("k_d2f");

@@ -70,6 +70,10 @@ int moments(const cx<T>* X, long long sX, int batch, int n, int L, const cxd* w,
 int residual_df32(const cxf* Tm, const cxf* Tlo, long long sT, const cxd* X, long long sX, const cxd* V,
                   long long sV, cxd* R, long long sR, int n, int L, int batch, double* rmax, cudaStream_t st);
 int convert_d2f(const cxd* in, cxf* out, long long count, cudaStream_t st);
+// out[b] = opnorm(A_b, 1) (out zeroed before the call)
+int opnorm1_batched(const cxd* A, int n, long long sA, int batch, double* out, cudaStream_t st);
+// out[4 b + q] = ||y_b||_2^2, ||y_b||_1, ||phi_b||_1, ||phi_b||_2^2 for n x batch column blocks
+int vec_norms(const cxd* y, const cxd* phi, int n, int batch, double* out, cudaStream_t st);
 // out = max(out, max_e |re x_e| + |im x_e|); out must be zeroed (or hold a
 // previous maximum) before the first call
 int maxabs_c64(const cxf* x, long long count, double* out, cudaStream_t st);

@@ -17,6 +17,8 @@ from .operators import (Workspace, build_workspace, assemble, assemble_noalloc, 
 from .beyn import BeynHandle, construct_B_matrix, solve_vect, solve, solve_disks, probe_matrix, contour
 from .sweep import k_sweep, get_eigenvalues
 from .serve import Server
+from .spectrum import (plan_weyl_windows, beyn_disks_from_windows, candidate_residuals,
+                       residual_and_norm_select, imag_k_check, compute_spectrum_beyn)
 from .symmetry import (Reflection, Rotation, XReflection, YReflection, XYReflection,
                        periodic_symmetry_index_orbits)
 

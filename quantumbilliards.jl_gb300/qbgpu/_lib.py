@@ -119,6 +119,8 @@ _SIGS = {
     "qbg_serve_wait": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double, C.POINTER(RequestResult)]),
     "qbg_serve_destroy": (C.c_int32, [C.c_void_p]),
     "qbg_launch_count": (C.c_int32, [C.POINTER(C.c_uint64)]),
+    "qbg_candidate_residuals": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.c_void_p,
+                                            C.POINTER(ChebParams), C.POINTER(C.c_double)]),
     "qbg_cheb_autotune": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.c_double, C.c_int32,
                                       C.c_int32, C.POINTER(ChebParams), C.POINTER(C.c_double)]),
     "qbg_beyn_create_disks": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32,
