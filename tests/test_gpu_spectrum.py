@@ -55,4 +55,4 @@ def test_compute_spectrum_beyn_unit_disk(qb, batched, imag_check):
     ref = _bessel_zeros(k1, k2)
     assert len(ks) == len(ref)
     assert np.max(np.abs(ks - ref) / ref) < 1e-9
-    assert len(us) == len(ks) and all(u.shape[0] == pts[0].n for u in us)
+    assert len(us) == len(ks) and all(u.shape[0] == p.n for u, p in zip(us, pts))
