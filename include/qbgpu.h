@@ -77,6 +77,20 @@ typedef struct qbg_geom_desc {
   const int64_t* fund;          /* m full indices I_a */
   const int64_t* orbit;         /* m*norb full indices of the images of I_b */
   const double* orbit_scale;    /* m*norb complex scale factors (character values) */
+  /* CFIE_alpert quadrature (cfie_alpert.jl:947-1013, 1261-1350); quad = 0 is
+   * Kress. Every component is a closed curve on a periodic midpoint grid; its
+   * self block drops the trapezoid band |i - j| < alpert_a and adds, per
+   * target, alpert_j correction nodes on each side whose kernel values are
+   * spread over alpert_ninterp grid nodes. */
+  int32_t quad;                 /* 0 = Kress log split, 1 = Alpert */
+  int32_t alpert_a;
+  int32_t alpert_j;
+  int32_t alpert_ninterp;
+  const double* alpert_w;       /* j rule weights */
+  const int64_t* alpert_off;    /* [2][j][ninterp] stencil offsets, + side then - side */
+  const double* alpert_wt;      /* [2][j][ninterp] interpolation weights */
+  const double* alpert_nodes;   /* [6][j][n]: r+, r-, inner+, inner-, speed+, speed- of the correction
+                                   nodes of every target (r = +inf: skipped) */
 } qbg_geom_desc;
 
 typedef struct qbg_geom qbg_geom;

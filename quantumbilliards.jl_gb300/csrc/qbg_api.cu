@@ -150,6 +150,32 @@ qbg_status qbg_geom_create(const qbg_geom_desc* desc, qbg_geom** out) {
         (s = g->upload(desc->orbit_scale, orb.size() * 2, &d.orb_scale)))
       return fail(s);
   }
+  if (desc->quad == 1) {
+    const int aj = desc->alpert_j, ani = desc->alpert_ninterp;
+    if (desc->form != QBG_FORM_CFIE || desc->m > 0 || desc->alpert_a < 1 || aj < 1 || ani < 2 || ani > 64 ||
+        !desc->alpert_w || !desc->alpert_off || !desc->alpert_wt || !desc->alpert_nodes) {
+      delete g;
+      set_error("qbg_geom_create: invalid Alpert arguments (CFIE only, no symmetry reduction)");
+      return QBG_EINVAL;
+    }
+    std::vector<int> off((size_t)2 * aj * ani);
+    for (size_t q = 0; q < off.size(); ++q) {
+      if (std::llabs(desc->alpert_off[q]) > n) { delete g; set_error("Alpert offset out of range"); return QBG_EINVAL; }
+      off[q] = (int)desc->alpert_off[q];
+    }
+    d.quad = 1;
+    d.aa = desc->alpert_a;
+    d.aj = aj;
+    d.ani = ani;
+    if ((s = g->upload(desc->alpert_w, (size_t)aj, &d.aw)) || (s = g->upload(off.data(), off.size(), &d.aoff)) ||
+        (s = g->upload(desc->alpert_wt, off.size(), &d.awt)) ||
+        (s = g->upload(desc->alpert_nodes, (size_t)6 * aj * n, &d.anodes)))
+      return fail(s);
+  } else if (desc->quad != 0) {
+    delete g;
+    set_error("qbg_geom_create: unknown quadrature %d", desc->quad);
+    return QBG_EINVAL;
+  }
   g->dim = d.m;
   e = cudaStreamSynchronize(g->stream);
   if (e != cudaSuccess) return fail(cuda_status(e, "qbg_geom_create sync"));

@@ -35,6 +35,13 @@ struct GeomDev {
   const double* orb_scale = nullptr;  // m*norb complex (re, im) scale factors
   const double* nx = nullptr;     // unit normals (ty, -tx)/|t| for image terms
   const double* ny = nullptr;
+  // Alpert quadrature (quad == 1)
+  int quad = 0;
+  int aa = 0, aj = 0, ani = 0;    // near band, correction nodes per side, stencil
+  const double* aw = nullptr;     // aj rule weights
+  const int* aoff = nullptr;      // [2][aj][ani]
+  const double* awt = nullptr;    // [2][aj][ani]
+  const double* anodes = nullptr; // [6][aj][n]
 };
 
 }  // namespace qbg

@@ -31,6 +31,9 @@ struct QbgGeomDesc
     ts::Ptr{Float64}; ws::Ptr{Float64}
     m::Int64; norb::Int32
     fund::Ptr{Int64}; orbit::Ptr{Int64}; orbit_scale::Ptr{Float64}
+    quad::Int32                      # 0 = Kress, 1 = Alpert (cache built by the caller)
+    alpert_a::Int32; alpert_j::Int32; alpert_ninterp::Int32
+    alpert_w::Ptr{Float64}; alpert_off::Ptr{Int64}; alpert_wt::Ptr{Float64}; alpert_nodes::Ptr{Float64}
 end
 
 struct QbgChebParams
@@ -97,7 +100,8 @@ function gpu_workspace(solver::GPUSolver, pts)
     GC.@preserve keep begin
         d = QbgGeomDesc(_form(solver.inner), Int32(length(comps)), pointer(offs), pointer(x), pointer(y),
                         pointer(dx), pointer(dy), pointer(ddx), pointer(ddy), pointer(ts), pointer(wsv),
-                        0, 0, C_NULL, C_NULL, C_NULL)
+                        0, 0, C_NULL, C_NULL, C_NULL,
+                        0, 0, 0, 0, C_NULL, C_NULL, C_NULL, C_NULL)  # Kress; an Alpert solver fills the cache fields
         qbg_check(ccall((:qbg_geom_create, libqbgpu), Int32, (Ref{QbgGeomDesc}, Ref{Ptr{Cvoid}}), d, h))
     end
     dim = Ref{Int64}(0)

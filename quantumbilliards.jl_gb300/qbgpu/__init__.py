@@ -7,7 +7,7 @@ libqbgpu.so. Import fails if the library has not been built.
 from . import _lib
 from .geometry import (BoundaryPointsCFIE, make_circle, make_star, make_full_stadium, make_circle_with_hole,
                        s_mid)
-from .solvers import (DLP_kress, DLP_kress_global_corners, CFIE_kress, CFIE_kress_global_corners,
+from .solvers import (DLP_kress, DLP_kress_global_corners, CFIE_kress, CFIE_kress_global_corners, CFIE_alpert,
                       evaluate_points, points_with_n)
 from . import operators
 from .operators import (Workspace, build_workspace, assemble, assemble_noalloc, construct_matrices,

@@ -51,7 +51,11 @@ class GeomDesc(C.Structure):
                 ("ddx", C.POINTER(C.c_double)), ("ddy", C.POINTER(C.c_double)),
                 ("ts", C.POINTER(C.c_double)), ("ws", C.POINTER(C.c_double)),
                 ("m", C.c_int64), ("norb", C.c_int32), ("fund", C.POINTER(C.c_int64)),
-                ("orbit", C.POINTER(C.c_int64)), ("orbit_scale", C.POINTER(C.c_double))]
+                ("orbit", C.POINTER(C.c_int64)), ("orbit_scale", C.POINTER(C.c_double)),
+                ("quad", C.c_int32), ("alpert_a", C.c_int32), ("alpert_j", C.c_int32),
+                ("alpert_ninterp", C.c_int32), ("alpert_w", C.POINTER(C.c_double)),
+                ("alpert_off", C.POINTER(C.c_int64)), ("alpert_wt", C.POINTER(C.c_double)),
+                ("alpert_nodes", C.POINTER(C.c_double))]
 
 
 class ChebParams(C.Structure):

@@ -35,6 +35,26 @@ def _concat(pts):
     return offs, arrs
 
 
+def _alpert_arrays(solver, pts_l):
+    """Periodic Alpert caches of every component (cfie_alpert.jl:1351-1363),
+    flattened for qbg_geom_create: nodes [6][j][n] with the components in
+    their global order."""
+    from .alpert import alpert_log_rule, periodic_cache
+    rule = alpert_log_rule(solver.alpert_order)
+    comps = solver.billiard.components
+    caches = []
+    for comp, p in zip(comps, pts_l):
+        if len(comp) != 1:
+            raise NotImplementedError("CFIE_alpert components must be single closed curves")
+        caches.append(periodic_cache(comp[0], p, rule, solver.alpert_order))
+    c0 = caches[0]
+    nodes = np.concatenate([np.stack([c.rp, c.rm, c.innp, c.innm, c.sp, c.sm]) for c in caches], axis=2)
+    return dict(a=rule.a, j=rule.j, ninterp=c0.ninterp, w=np.ascontiguousarray(rule.w),
+                off=np.ascontiguousarray(np.stack([c0.offp, c0.offm]).astype(np.int64)),
+                wt=np.ascontiguousarray(np.stack([c0.wtp, c0.wtm])),
+                nodes=np.ascontiguousarray(nodes))
+
+
 class Workspace:
     """Device-resident geometry for one discretisation (owns a qbg_geom)."""
 
@@ -68,6 +88,17 @@ class Workspace:
             d.fund = L.dptr(self._red[0], C.c_int64)
             d.orbit = L.dptr(self._red[1], C.c_int64)
             d.orbit_scale = L.dptr(self._red[2])
+        d.quad = 0
+        self._alp = None
+        if getattr(solver, "alpert_order", None) is not None:
+            self._alp = _alpert_arrays(solver, pts_l)
+            a = self._alp
+            d.quad = 1
+            d.alpert_a, d.alpert_j, d.alpert_ninterp = a["a"], a["j"], a["ninterp"]
+            d.alpert_w = L.dptr(a["w"])
+            d.alpert_off = L.dptr(a["off"], C.c_int64)
+            d.alpert_wt = L.dptr(a["wt"])
+            d.alpert_nodes = L.dptr(a["nodes"])
         h = C.c_void_p()
         L.check(lib.qbg_geom_create(C.byref(d), C.byref(h)))
         self._h = h

@@ -49,6 +49,19 @@ class CFIE_kress_global_corners(_Solver):
     kind = "cfie"
 
 
+class CFIE_alpert(_Solver):
+    """CFIE with Alpert hybrid Gauss-trapezoidal self correction (cfie.jl:381-419,
+    cfie_alpert.jl); alpert_order in 2, 3, 4, 5, 6, 8, 10, 12, 14, 16."""
+    kind = "cfie"
+
+    def __init__(self, pts_scaling_factor, billiard, min_pts=20, symmetry=None, kressq=4, alpert_order=12):
+        super().__init__(pts_scaling_factor, billiard, min_pts, symmetry, kressq)
+        from .alpert import ALPERT_LOG_RULES
+        if alpert_order not in ALPERT_LOG_RULES:
+            raise ValueError("Alpert order not currently supported")
+        self.alpert_order = int(alpert_order)
+
+
 def _points_component(solver: _Solver, comp, k: float, idx: int) -> G.BoundaryPointsCFIE:
     L = sum(c.length for c in comp)
     needed = G._needed(solver.symmetry, 2)
@@ -61,10 +74,30 @@ def _points_component(solver: _Solver, comp, k: float, idx: int) -> G.BoundaryPo
     return G.points_smooth_composite(comp, N, idx)
 
 
+def _points_alpert(solver, comp, k: float, idx: int) -> G.BoundaryPointsCFIE:
+    """_evaluate_points_periodic (cfie.jl:946-972): periodic midpoint grid,
+    N = max(min_pts, round(k L b / 2pi)) rounded up to the symmetry multiple
+    (no evenness requirement)."""
+    if len(comp) != 1:
+        raise NotImplementedError("CFIE_alpert here takes components that are single closed curves "
+                                  "(the periodic Alpert cache); composite panels are not built")
+    crv = comp[0]
+    from .symmetry import needed_multiple
+    needed = 1 if solver.symmetry is None else needed_multiple(solver.symmetry, 1)
+    N = G.node_count(k, crv.length, solver.pts_scaling_factor, solver.min_pts, needed)
+    return G.points_single_curve(crv, N, idx)
+
+
 def evaluate_points(solver: _Solver, billiard: G.Billiard, k: float):
     """DLP solvers return one ``BoundaryPointsCFIE``; CFIE solvers a list with
     holes orientation-reversed (cfie.jl:822-834)."""
     comps = billiard.components
+    if isinstance(solver, CFIE_alpert):
+        out = []
+        for idx, comp in enumerate(comps, start=1):
+            p = _points_alpert(solver, comp, k, idx)
+            out.append(p if idx == 1 else G.reverse_orientation(p))
+        return out
     if solver.kind == "dlp":
         if len(comps) != 1:
             raise ValueError("DLP_kress supports exactly one outer boundary component; use a CFIE solver")
@@ -86,6 +119,8 @@ def points_with_n(solver: _Solver, billiard: G.Billiard, n_outer: int, k_ref: fl
     import math
     b = 2 * math.pi * n_outer / (k_ref * billiard.outer_length)
     s = type(solver)(b, billiard, solver.min_pts, solver.symmetry, solver.kressq)
+    if isinstance(solver, CFIE_alpert):
+        s.alpert_order = solver.alpert_order
     return evaluate_points(s, billiard, k_ref), s
 
 
