@@ -6,6 +6,7 @@ libqbgpu.so. Import fails if the library has not been built.
 """
 from . import _lib
 from .geometry import (BoundaryPointsCFIE, make_circle, make_star, make_full_stadium, make_circle_with_hole,
+                       make_rectangle, make_full_ellipse_mushroom, multi_kress_graded_nodes_data,
                        s_mid)
 from .solvers import (DLP_kress, DLP_kress_global_corners, CFIE_kress, CFIE_kress_global_corners, CFIE_alpert,
                       evaluate_points, points_with_n)

@@ -149,6 +149,45 @@ class PolarSegment:
         return out
 
 
+class EllipseArc:
+    """gamma(u) = c + (a cos th, b sin th), th = th0 + (th1 - th0) u: the
+    elliptic cap of the mushroom billiards (ellipse_mushroom.jl; the reference
+    writes it as a PolarSegment of a parametric closure)."""
+
+    def __init__(self, a, b, th0, th1, cx=0.0, cy=0.0, nquad=2048):
+        self.a, self.b, self.th0, self.th1, self.c = float(a), float(b), float(th0), float(th1), (cx, cy)
+        self.length = float(self.arc_length(1.0)[0])
+
+    def _th(self, u):
+        u = np.asarray(u, dtype=np.float64)
+        return self.th0 + (self.th1 - self.th0) * u, self.th1 - self.th0
+
+    def curve(self, u):
+        th, _ = self._th(u)
+        return np.stack([self.c[0] + self.a * np.cos(th), self.c[1] + self.b * np.sin(th)], axis=-1)
+
+    def tangent(self, u):
+        th, d = self._th(u)
+        return d * np.stack([-self.a * np.sin(th), self.b * np.cos(th)], axis=-1)
+
+    def tangent_2(self, u):
+        th, d = self._th(u)
+        return d * d * np.stack([-self.a * np.cos(th), -self.b * np.sin(th)], axis=-1)
+
+    def arc_length(self, u):
+        u = np.atleast_1d(np.asarray(u, dtype=np.float64))
+        x, w = np.polynomial.legendre.leggauss(64)
+        out = np.empty_like(u)
+        for n, uu in enumerate(u):
+            edges = np.linspace(0.0, uu, 17)
+            acc = 0.0
+            for lo, hi in zip(edges[:-1], edges[1:]):
+                t = 0.5 * (hi - lo) * x + 0.5 * (hi + lo)
+                acc += 0.5 * (hi - lo) * np.sum(w * np.hypot(*self.tangent(t).T))
+            out[n] = acc
+        return out
+
+
 # --------------------------------------------------------------------------
 # billiards
 # --------------------------------------------------------------------------
@@ -196,6 +235,31 @@ def make_full_stadium(half_width: float = 1.0, radius: float = 1.0) -> Billiard:
     arc3 = CircleSegment(r, math.pi / 2, 3 * math.pi / 2, hw, 0.0)
     area = 4.0 * hw * r + math.pi * r * r
     return Billiard("stadium", [[arc1, line1, arc2, line2, arc3]], area, ("x", "y"))
+
+
+def make_rectangle(width: float = 1.0, height: float = 1.0) -> Billiard:
+    """Counter-clockwise rectangle [0, w] x [0, h] of four line segments (four
+    corners); Dirichlet eigenvalues k^2 = pi^2 (m^2/w^2 + n^2/h^2)."""
+    w, h = float(width), float(height)
+    pts = [(0.0, 0.0), (w, 0.0), (w, h), (0.0, h)]
+    segs = [LineSegment(pts[j], pts[(j + 1) % 4]) for j in range(4)]
+    return Billiard("rectangle", [segs], w * h, ())
+
+
+def make_full_ellipse_mushroom(stem_width=0.6, stem_height=1.0, cap_height=0.8, cap_width=1.2) -> Billiard:
+    """make_full_ellipse_mushroom (ellipse_mushroom.jl): rectangular stem of
+    width stem_width and height stem_height under a half-ellipse cap of
+    semi-axes cap_width, cap_height; segments stem bottom, stem right, right
+    connector, cap, left connector, stem left, all shifted by (stem_width/2, 0)
+    as there. Six true corners."""
+    w2, hs, a, b = 0.5 * stem_width, stem_height, cap_width, cap_height
+    ox = w2
+    P = lambda x, y: (x + ox, y)
+    segs = [LineSegment(P(-w2, -hs), P(w2, -hs)), LineSegment(P(w2, -hs), P(w2, 0.0)),
+            LineSegment(P(w2, 0.0), P(a, 0.0)), EllipseArc(a, b, 0.0, math.pi, ox, 0.0),
+            LineSegment(P(-a, 0.0), P(-w2, 0.0)), LineSegment(P(-w2, 0.0), P(-w2, -hs))]
+    area = stem_width * stem_height + 0.5 * math.pi * a * b
+    return Billiard("ellipse_mushroom", [segs], area, ())
 
 
 def make_circle_with_hole(R: float = 1.0, hole=(0.3, 0.1, 0.2)) -> Billiard:
@@ -292,6 +356,82 @@ def points_smooth_composite(comp, N: int, compid: int = 1) -> BoundaryPointsCFIE
         xy[i], t1[i], t2[i] = q, gt, gtt
     ds = np.hypot(t1[:, 0], t1[:, 1]) * h
     return BoundaryPointsCFIE(xy, t1, t2, ts, ts.copy(), np.full(N, h), np.ones(N), ds, compid, True)
+
+
+def _smoothstep(u, q):
+    u = np.clip(u, 0.0, 1.0)
+    a, b = u ** q, (1.0 - u) ** q
+    return a / (a + b)
+
+
+def _smoothstep_1(u, q):
+    u = np.clip(u, np.finfo(float).eps, 1.0 - np.finfo(float).eps)
+    a, b = u ** q, (1.0 - u) ** q
+    return q * u ** (q - 1) * (1.0 - u) ** (q - 1) / (a + b) ** 2
+
+
+def _smoothstep_2(u, q):
+    u = np.clip(u, np.finfo(float).eps, 1.0 - np.finfo(float).eps)
+    d = u ** q + (1.0 - u) ** q
+    dp = q * (u ** (q - 1) - (1.0 - u) ** (q - 1))
+    return _smoothstep_1(u, q) * ((q - 1) / u - (q - 1) / (1.0 - u) - 2.0 * dp / d)
+
+
+def multi_kress_graded_nodes_data(N: int, corners, q: float = 3.0, minsep_tol: float = 1e-12):
+    """kress_grading_global_multi_corner.jl:53-146: uniform sigma_j = h (j - 1/2)
+    mapped by t = left + L v((sigma - left)/L) between consecutive corners with
+    the Kress smoothstep v(u) = u^q / (u^q + (1-u)^q). Returns (sigma, t, dt/dsigma,
+    d2t/dsigma2, weights h dt/dsigma); q shrinks by 0.9 while mapped nodes are
+    closer than minsep_tol."""
+    h = TWO_PI / N
+    sig = np.sort(np.mod(0.5 * h + h * np.arange(N), TWO_PI))
+    cs = sorted({float(np.mod(c, TWO_PI)) for c in corners})
+    cu = []
+    for c in cs:
+        if not cu or abs(c - cu[-1]) > math.sqrt(np.finfo(float).eps):
+            cu.append(c)
+    if not cu:
+        return sig, sig.copy(), np.ones(N), np.zeros(N), np.full(N, h)
+    cu = np.array(cu)
+    qq = float(q)
+    if qq <= 1.0:
+        raise ValueError("Require q > 1.")
+    while qq > 1.0:
+        if len(cu) == 1:
+            left = np.full(N, cu[0]) - np.where(sig < cu[0], TWO_PI, 0.0)
+            right = left + TWO_PI
+        else:
+            j = np.searchsorted(cu, sig, side="right") - 1
+            left = np.where(j < 0, cu[-1] - TWO_PI, cu[np.clip(j, 0, len(cu) - 1)])
+            right = np.where(j < 0, cu[0], np.where(j >= len(cu) - 1, cu[0] + TWO_PI, cu[np.clip(j + 1, 0, len(cu) - 1)]))
+        Lw = right - left
+        u = (sig - left) / Lw
+        tmap = np.mod(left + Lw * _smoothstep(u, qq), TWO_PI)
+        jac = _smoothstep_1(u, qq)
+        jac2 = _smoothstep_2(u, qq) / Lw
+        ts = np.sort(tmap)
+        gaps = np.diff(np.concatenate([ts, [ts[0] + TWO_PI]]))
+        if gaps.min() >= minsep_tol:
+            return sig, tmap, jac, jac2, h * jac
+        qq = max(1.0, 0.9 * qq)
+    raise ValueError("Kress grading is impossible: q reached 1 with nodes closer than minsep_tol")
+
+
+def points_graded_composite(comp, N: int, corners, q: float, compid: int = 1,
+                            minsep_tol: float = 1e-12) -> BoundaryPointsCFIE:
+    """_evaluate_points(::DLP_kress_global_corners, comp) with corners
+    (dlp_kress.jl:505-540): nodes at t(sigma_j), gamma' = gamma_t jac,
+    gamma'' = gamma_tt jac^2 + gamma_t jac2, weights h, sigma for the Kress log term."""
+    sig, tmap, jac, jac2, _ = multi_kress_graded_nodes_data(N, corners, q, minsep_tol)
+    h = TWO_PI / N
+    xy = np.empty((N, 2)); t1 = np.empty((N, 2)); t2 = np.empty((N, 2))
+    for i in range(N):
+        qpt, gt, gtt = _composite_eval(comp, tmap[i])
+        xy[i] = qpt
+        t1[i] = np.asarray(gt) * jac[i]
+        t2[i] = np.asarray(gtt) * jac[i] ** 2 + np.asarray(gt) * jac2[i]
+    ds = np.hypot(t1[:, 0], t1[:, 1]) * h
+    return BoundaryPointsCFIE(xy, t1, t2, sig, tmap, np.full(N, h), jac, ds, compid, True)
 
 
 def reverse_orientation(p: BoundaryPointsCFIE) -> BoundaryPointsCFIE:

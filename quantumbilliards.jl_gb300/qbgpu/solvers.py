@@ -64,13 +64,19 @@ class CFIE_alpert(_Solver):
 
 def _points_component(solver: _Solver, comp, k: float, idx: int) -> G.BoundaryPointsCFIE:
     L = sum(c.length for c in comp)
+    if len(comp) > 1:
+        corners = G._component_corners(comp)
+        if corners:
+            # graded Kress nodes (dlp_kress.jl:505-540): no evenness rule, the symmetry multiple only
+            if isinstance(solver, (DLP_kress, CFIE_kress)):
+                raise ValueError("the boundary has corners; use a *_global_corners solver")
+            needed = 1 if solver.symmetry is None else G._needed(solver.symmetry, 1)
+            N = G.node_count(k, L, solver.pts_scaling_factor, solver.min_pts, needed)
+            return G.points_graded_composite(comp, N, corners, float(solver.kressq), idx)
     needed = G._needed(solver.symmetry, 2)
     N = G.node_count(k, L, solver.pts_scaling_factor, solver.min_pts, needed)
     if len(comp) == 1:
         return G.points_single_curve(comp[0], N, idx)
-    if G._component_corners(comp):
-        raise NotImplementedError("corner-graded Kress nodes are outside this path (no geometry here has a "
-                                  "true corner)")
     return G.points_smooth_composite(comp, N, idx)
 
 

@@ -6,7 +6,8 @@ p50/p99 latency (arrival -> result on the host) and throughput.
 
 Seeded synthetic stream: geometry uniform over {unit circle with an
 off-centre hole of radius 0.2 (CFIE), full stadium (DLP, smooth composite),
-star r = 1 + 0.2 cos 5 theta (CFIE)}; N log-uniform in [nmin, nmax] (rounded
+half-ellipse-cap mushroom (DLP, corner-graded, kressq = 4), star
+r = 1 + 0.2 cos 5 theta (CFIE)}; N log-uniform in [nmin, nmax] (rounded
 to the node-count rule); k uniform in [kmin, kmax]; 60% Beyn disks (radius
 0.5, 32..64 contour nodes, L probes, mixed form), 30% EBIM (A, A', A'' at
 one k), 10% sigma_min sweeps (nk wavenumbers). Discretisations are built and
@@ -34,6 +35,7 @@ def make_stream(qb, args):
     rng = np.random.default_rng(args.seed)
     geoms = [("hole", qb.make_circle_with_hole(1.0, (0.3, 0.1, 0.2)), qb.CFIE_kress),
              ("stadium", qb.make_full_stadium(1.0, 1.0), qb.DLP_kress_global_corners),
+             ("mushroom", qb.make_full_ellipse_mushroom(), qb.DLP_kress_global_corners),
              ("star", qb.make_star(0.2, 5), qb.CFIE_kress)]
     reqs = []
     t = 0.0
