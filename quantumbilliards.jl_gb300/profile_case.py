@@ -2,6 +2,8 @@
 
     python quantumbilliards.jl_gb300/profile_case.py beyn --nq 8 --form mixed
     python quantumbilliards.jl_gb300/profile_case.py assemble --nq 8
+    python quantumbilliards.jl_gb300/profile_case.py disks --n 4096 --ndisk 32 --nq 48 --L 96
+    python quantumbilliards.jl_gb300/profile_case.py large --n 16384 --nq 48 --L 128 --chunk 8
 
 Cases use the bench workload (CFIE Kress, star r = 1 + 0.2 cos 5 theta,
 N = 2048, k0 = 200, R = 0.5, L = 64) with an adjustable number of contour nodes
@@ -10,6 +12,7 @@ so that a capture stays small (a few GB on the device at most).
 from __future__ import annotations
 
 import argparse
+import json
 import math
 import sys
 import time
@@ -28,9 +31,62 @@ def star_case(qb, n_nodes=2048, k0=200.0, kind="cfie"):
     return b, sol, pts
 
 
+def disks_case(qb, a):
+    """Batched Beyn on the desymmetrised stadium: DLP_kress_global_corners with
+    XYReflection(-1, -1), N full nodes (m = N/4), ndisk disks of radius 0.5
+    centred at 300.5 + d, nq nodes each, L probes, panels tuned to 1e-12."""
+    b = qb.make_full_stadium(1.0, 1.0)
+    sol = qb.DLP_kress_global_corners(1.0, b, symmetry=qb.XYReflection(-1, -1))
+    k0s = 300.5 + np.arange(a.ndisk)
+    pts, sol = qb.points_with_n(sol, b, a.n, float(k0s[-1] + 0.5))
+    ws = qb.Workspace(sol, pts)
+    t0 = time.perf_counter()
+    zref = k0s[-1] + 0.5 * np.exp(2j * math.pi * np.arange(a.nq) / a.nq)
+    cheb = qb.chebyshev_params(sol, pts, zref, ws=ws, tol=1e-12, sampling_points=50000)[:4]
+    t1 = time.perf_counter()
+    lams, info = qb.solve_disks(sol, pts, k0s, 0.5, nq=a.nq, r=a.L, svd_tol=1e-10, rng=np.random.default_rng(3),
+                                mixed=a.form, ws=ws, return_info=True, cheb=cheb)
+    t2 = time.perf_counter()
+    n_in = sum(int(np.count_nonzero((np.abs(l - k) < 0.5) & (np.abs(l.imag) < 1e-3))) for l, k in zip(lams, k0s))
+    st = info["stats"]
+    print(json.dumps(dict(case="disks", N=pts.n, m=ws.dim, ndisk=a.ndisk, nq=a.nq, operators=a.ndisk * a.nq, L=a.L,
+                          form=a.form, cheb=list(map(int, cheb)), autotune_s=t1 - t0, solve_s=t2 - t1,
+                          eigenvalues=n_in, eigenvalues_per_s=n_in / (t2 - t1), rk=info["rk"],
+                          ms_assemble=st[0]["ms_assemble"], ms_factor=st[0]["ms_factor"],
+                          ms_solve=[s["ms_solve"] for s in st], refine=[s["refine_history"] for s in st])))
+
+
+def large_case(qb, a):
+    """CFIE_kress_global_corners on the full stadium at N = a.n, k0 = 1500:
+    A, A', A'' in complex128 at k0 (EBIM), then one Beyn moments call with
+    nq nodes streamed a.chunk at a time and L probes."""
+    b = qb.make_full_stadium(1.0, 1.0)
+    sol = qb.CFIE_kress_global_corners(1.0, b)
+    pts, sol = qb.points_with_n(sol, b, a.n, 1500.0)
+    ws = qb.Workspace(sol, pts)
+    t0 = time.perf_counter()
+    mats = qb.assemble(ws, [1500.0 + 0j], deriv=True, cheb=True)
+    t1 = time.perf_counter()
+    del mats
+    bh = qb.BeynHandle(ws, 1500.0, 0.5, a.nq, mixed=a.form, node_chunk=a.chunk)
+    V = qb.probe_matrix(ws.dim, a.L, np.random.default_rng(5))
+    t2 = time.perf_counter()
+    A0, A1 = bh.moments(V)
+    t3 = time.perf_counter()
+    st = bh.last_stats
+    bh.close()
+    S = np.linalg.svd(A0, compute_uv=False)
+    print(json.dumps(dict(case="large", N=ws.dim, ebim_assembly_s=t1 - t0, moments_s=t3 - t2, nq=a.nq, L=a.L,
+                          chunk=a.chunk, form=a.form, rank_1e10=int(np.count_nonzero(S >= 1e-10)),
+                          ms_assemble=st["ms_assemble"], ms_factor=st["ms_factor"], ms_solve=st["ms_solve"],
+                          refine=st["refine_history"], ms_residual=st["ms_residual"])))
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["beyn", "assemble"])
+    ap.add_argument("case", choices=["beyn", "assemble", "disks", "large"])
+    ap.add_argument("--ndisk", type=int, default=32)
+    ap.add_argument("--chunk", type=int, default=8)
     ap.add_argument("--nq", type=int, default=8)
     ap.add_argument("--n", type=int, default=2048)
     ap.add_argument("--L", type=int, default=64)
@@ -40,6 +96,10 @@ def main(argv=None):
     import build_qbgpu
     build_qbgpu.build()
     import qbgpu as qb
+    if a.case == "disks":
+        return disks_case(qb, a)
+    if a.case == "large":
+        return large_case(qb, a)
     b, sol, pts = star_case(qb, a.n)
     ws = qb.Workspace(sol, pts)
     t0 = time.perf_counter()
