@@ -167,7 +167,8 @@ qbg_status qbg_assemble_noalloc(qbg_geom* g, const double* ks, int64_t nk, int32
 typedef struct qbg_beyn_opts {
   int32_t flags;        /* QBG_PTR_DEVICE: V, A0, A1 are device pointers;
                            QBG_V_PER_DISK: V holds one N x L probe block per disk */
-  int32_t max_refine;   /* mixed form: maximum refinement sweeps (default 4) */
+  int32_t max_refine;   /* complex64 forms: maximum compensated refinement sweeps (default 10); refinement
+                           also stops when a sweep contracts the residual by less than 2 */
   double refine_tol;    /* complex64 forms: the first correction uses an FP32 residual; later residuals
                            are compensated; once max|R| <= tol * max|V| the correction from that
                            residual is applied and refinement stops (default 1e-6). Each correction

@@ -309,6 +309,9 @@ int refine_resident(Call& c) {
         (s = axpy_f2d(c.X32, c.X64, tot, st)))
       return s;
     if (rel <= b->opts.refine_tol) break;
+    // no progress (the FP32 factors contract the residual by less than 2 per
+    // sweep): further sweeps cannot converge; the caller sees refine_residual
+    if (c.nhist >= 2 && rel > 0.5 * c.hist[c.nhist - 2]) break;
   }
   c.sweeps = std::max(c.sweeps, sweeps);
   c.rel = std::max(c.rel, rel);
@@ -370,11 +373,11 @@ qbg_status create_impl(qbg_geom* g, const double* k0s, const double* Rs, int ndi
   b->nn = nq * ndisk;
   b->prec = prec;
   b->opts = qbg_beyn_opts{};
-  b->opts.max_refine = 4;
+  b->opts.max_refine = 10;
   b->opts.refine_tol = 1e-6;
   if (opts) {
     b->opts = *opts;
-    if (b->opts.max_refine <= 0) b->opts.max_refine = 4;
+    if (b->opts.max_refine <= 0) b->opts.max_refine = 10;
     if (!(b->opts.refine_tol > 0.0)) b->opts.refine_tol = 1e-6;
   }
   b->cap = (b->opts.node_chunk > 0 && b->opts.node_chunk < b->nn) ? b->opts.node_chunk : b->nn;

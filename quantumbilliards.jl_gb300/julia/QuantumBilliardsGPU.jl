@@ -138,7 +138,7 @@ function QB.construct_B_matrix(solver::GPUSolver, pts, N::Int, k0::Complex{Float
     ws = gpu_workspace(solver, pts)
     @assert ws.dim == N
     h = Ref{Ptr{Cvoid}}(C_NULL)
-    opts = QbgBeynOpts(0, 4, 1e-6, 0, 0, QbgChebParams(0, 0, 0, 0), 0, 0, 0)
+    opts = QbgBeynOpts(0, 10, 1e-6, 0, 0, QbgChebParams(0, 0, 0, 0), 0, 0, 0)
     qbg_check(ccall((:qbg_beyn_create, libqbgpu), Int32,
         (Ptr{Cvoid}, Float64, Float64, Float64, Int32, Int32, Ref{QbgBeynOpts}, Ref{Ptr{Cvoid}}),
         ws.h, real(k0), imag(k0), R, nq, solver.prec, opts, h))

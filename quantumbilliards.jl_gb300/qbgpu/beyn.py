@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import warnings
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -44,7 +45,7 @@ class BeynHandle:
     node_chunk > 0 keeps at most that many node operators resident and
     streams the nodes through them in every moments() call."""
 
-    def __init__(self, ws: Workspace, k0, R, nq: int, mixed: bool = False, max_refine: int = 4,
+    def __init__(self, ws: Workspace, k0, R, nq: int, mixed: bool = False, max_refine: int = 10,
                  refine_tol: float = 1e-6, nb: int = 0, use_chebyshev: bool = True, cheb=None, fp32_sweeps: int = 0,
                  solve_block: int = 0, node_chunk: int = 0):
         lib = L.load()
@@ -55,6 +56,7 @@ class BeynHandle:
         self.k0s, self.Rs = k0s, Rs
         self.k0, self.R = complex(k0s[0]), float(Rs[0])
         self.prec = L.prec_code(mixed)
+        self.refine_tol = float(refine_tol)
         cp = L.ChebParams(*(cheb if cheb else (0, 0, 0, 0)))
         o = L.BeynOpts(0, int(max_refine), float(refine_tol), int(nb), 0 if use_chebyshev else 1, cp,
                        int(fp32_sweeps), int(solve_block), int(node_chunk))
@@ -81,6 +83,10 @@ class BeynHandle:
         A1 = np.empty((self.ndisk, r, N), dtype=np.complex128)
         st = L.BeynStats()
         L.check(lib.qbg_beyn_moments(self._h, L.vptr(V), r, L.vptr(A0), L.vptr(A1), C.byref(st)))
+        if self.prec != L.QBG_PREC_FP64 and st.nhist and st.refine_residual > self.refine_tol:
+            warnings.warn(f"qbgpu: mixed refinement stopped at relative residual {st.refine_residual:.2e} > "
+                          f"refine_tol {self.refine_tol:.1e} (history {list(st.refine_history[:st.nhist])}); "
+                          "the moments are less accurate than requested", RuntimeWarning, stacklevel=2)
         self.last_stats = dict(refine_sweeps=st.refine_sweeps, refine_residual=st.refine_residual,
                                singular=st.singular, ms_assemble=st.ms_assemble, ms_factor=st.ms_factor,
                                ms_solve=st.ms_solve, refine_history=list(st.refine_history[:st.nhist]),
@@ -159,7 +165,7 @@ def solve_disks(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed
 
 
 def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=None, mixed=False, ws=None,
-                       max_refine=4, refine_tol=1e-6, return_info=False, regrow="extend", use_chebyshev=True,
+                       max_refine=10, refine_tol=1e-6, return_info=False, regrow="extend", use_chebyshev=True,
                        cheb=None, fp32_sweeps=0, solve_block=0, node_chunk=0):
     """construct_B_matrix (beyn.jl:257-322). Returns (B, Uk) [, info].
 
