@@ -223,13 +223,14 @@ qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig)
 
 /* Panel autotuner (chebyshev_params, chebyshev_optimal_panelization.jl:221-307):
  * starting from *io (zeros = 15000, 5, 3000, 5), grows the panel counts by
- * 1.5x per iteration (every 5th iteration the degrees by 2 instead) until the
+ * 1.5x per iteration (every 5th iteration the degrees by grow_M instead; the
+ * reference uses 2, 0 keeps the degrees fixed) until the
  * max absolute error of the interpolated H0, H1 (on [rmin, rmax]) and J0, J1
  * (on [0, rmax]) at nsample radii is below tol for every wavenumber. Writes
  * the parameters to *io and the worst errors to err4 (may be null). Returns
  * QBG_ETIMEOUT with the best effort when max_iter is reached. */
 qbg_status qbg_cheb_autotune(qbg_geom* g, const double* ks, int64_t nk, double tol, int32_t nsample,
-                             int32_t max_iter, qbg_cheb_params* io, double* err4);
+                             int32_t max_iter, int32_t grow_M, qbg_cheb_params* io, double* err4);
 
 /* Residuals of Beyn candidates, the device part of residual_and_norm_select
  * and imag_k_check_EXPERIMENTAL (beyn.jl:557-593, 623-721): for each candidate

@@ -409,8 +409,8 @@ qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig)
 // absolute error of every interpolated H0, H1, J0, J1 over all wavenumbers is
 // below tol at nsample radii.
 qbg_status qbg_cheb_autotune(qbg_geom* g, const double* ks, int64_t nk, double tol, int32_t nsample,
-                             int32_t max_iter, qbg_cheb_params* io, double* err4) {
-  if (!g || !ks || !io || nk < 1 || nk > 65535 || !(tol > 0.0) || nsample < 2 || max_iter < 1) {
+                             int32_t max_iter, int32_t grow_M, qbg_cheb_params* io, double* err4) {
+  if (!g || !ks || !io || nk < 1 || nk > 65535 || !(tol > 0.0) || nsample < 2 || max_iter < 1 || grow_M < 0) {
     set_error("qbg_cheb_autotune: invalid arguments");
     return QBG_EINVAL;
   }
@@ -450,7 +450,7 @@ qbg_status qbg_cheb_autotune(qbg_geom* g, const double* ks, int64_t nk, double t
     if (okH && okJ) { ok = true; break; }
     if (it == max_iter) break;
     auto grow = [&](int& npan, int& M) {
-      if (it % 5 == 0 && M + 2 <= QBG_CHEB_MAX_DEGREE) M += 2;
+      if (grow_M > 0 && it % 5 == 0 && M + grow_M <= QBG_CHEB_MAX_DEGREE) M += grow_M;
       else npan = (int)std::ceil(1.5 * (double)npan);
     };
     if (!okH) grow(p.n_panels_h, p.M_h);

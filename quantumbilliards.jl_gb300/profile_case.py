@@ -42,7 +42,12 @@ def disks_case(qb, a):
     ws = qb.Workspace(sol, pts)
     t0 = time.perf_counter()
     zref = k0s[-1] + 0.5 * np.exp(2j * math.pi * np.arange(a.nq) / a.nq)
-    cheb = qb.chebyshev_params(sol, pts, zref, ws=ws, tol=1e-12, sampling_points=50000)[:4]
+    if a.tune == "reference":
+        cheb = qb.chebyshev_params(sol, pts, zref, ws=ws, tol=1e-12, sampling_points=50000)[:4]
+    else:
+        # the main entry plus norb - 1 image terms per reduced entry, tables for every node of every disk
+        cheb = qb.chebyshev_params_min_cost(sol, pts, zref, ws=ws, tol=1e-12, entries=float(ws.dim) ** 2 * a.ndisk
+                                            * a.nq, terms_per_entry=4.0, tables_per_call=a.ndisk * a.nq)[:4]
     t1 = time.perf_counter()
     lams, info = qb.solve_disks(sol, pts, k0s, 0.5, nq=a.nq, r=a.L, svd_tol=1e-10, rng=np.random.default_rng(3),
                                 mixed=a.form, ws=ws, return_info=True, cheb=cheb)
@@ -87,6 +92,7 @@ def main(argv=None):
     ap.add_argument("case", choices=["beyn", "assemble", "disks", "large"])
     ap.add_argument("--ndisk", type=int, default=32)
     ap.add_argument("--chunk", type=int, default=8)
+    ap.add_argument("--tune", default="min_cost", choices=["min_cost", "reference"])
     ap.add_argument("--nq", type=int, default=8)
     ap.add_argument("--n", type=int, default=2048)
     ap.add_argument("--L", type=int, default=64)

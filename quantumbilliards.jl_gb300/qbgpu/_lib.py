@@ -126,7 +126,7 @@ _SIGS = {
     "qbg_candidate_residuals": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.c_void_p,
                                             C.POINTER(ChebParams), C.POINTER(C.c_double)]),
     "qbg_cheb_autotune": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.c_double, C.c_int32,
-                                      C.c_int32, C.POINTER(ChebParams), C.POINTER(C.c_double)]),
+                                      C.c_int32, C.c_int32, C.POINTER(ChebParams), C.POINTER(C.c_double)]),
     "qbg_beyn_create_disks": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32,
                                           C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
 }

@@ -191,7 +191,7 @@ def construct_boundary_matrices_with_derivatives(solver, pts, zj, ws: Workspace 
 
 
 def chebyshev_params(solver, pts, zj, ws: Workspace = None, npanels_h_init=15000, M_h_init=5, npanels_j_init=3000,
-                     M_j_init=5, tol=1e-10, sampling_points=50000, max_iter=20, strict=False):
+                     M_j_init=5, tol=1e-10, sampling_points=50000, max_iter=20, grow_M=2, strict=False):
     """chebyshev_params (chebyshev_optimal_panelization.jl:221-307) on the device.
 
     Returns (n_panels_h, M_h, n_panels_j, M_j, errors[H0, H1, J0, J1]). When
@@ -201,10 +201,41 @@ def chebyshev_params(solver, pts, zj, ws: Workspace = None, npanels_h_init=15000
     prm = L.ChebParams(int(npanels_h_init), int(M_h_init), int(npanels_j_init), int(M_j_init))
     err = np.zeros(4)
     st = L.load().qbg_cheb_autotune(ws.handle, L.dptr(k.view(np.float64)), len(k), float(tol), int(sampling_points),
-                                    int(max_iter), C.byref(prm), L.dptr(err))
+                                    int(max_iter), int(grow_M), C.byref(prm), L.dptr(err))
     if st != L.QBG_OK and (strict or st != L.QBG_ETIMEOUT):
         L.check(st)
     return prm.n_panels_h, prm.M_h, prm.n_panels_j, prm.M_j, err
+
+
+def chebyshev_params_min_cost(solver, pts, zj, ws: Workspace = None, tol=1e-10, entries=None, terms_per_entry=1.0,
+                              degrees=(5, 7, 9, 11, 13, 15), sampling_points=50000, bessel_cost=60.0,
+                              tables_per_call=None):
+    """Panels of the lowest estimated assembly cost that still meet tol.
+
+    For every degree M in ``degrees`` (kept fixed) the device tuner grows the
+    panel counts until every interpolated H0, H1, J0, J1 is within tol. The
+    cost of a candidate is the table build (one device Bessel evaluation,
+    about ``bessel_cost`` Clenshaw steps, per Lobatto node per panel per
+    wavenumber) plus the Clenshaw steps of the assembly (``entries`` matrix
+    entries, ``terms_per_entry`` H evaluations each plus one J evaluation).
+    Returns (n_panels_h, M_h, n_panels_j, M_j, errors, cost)."""
+    ws = ws if ws is not None else Workspace(solver, pts)
+    nk = len(np.atleast_1d(zj)) if tables_per_call is None else int(tables_per_call)
+    entries = float(ws.dim) ** 2 * nk if entries is None else float(entries)
+    best = None
+    for M in degrees:
+        # start from few panels; the tuner only grows them
+        nh, Mh, nj, Mj, err = chebyshev_params(solver, pts, zj, ws=ws, npanels_h_init=200, M_h_init=M,
+                                               npanels_j_init=50, M_j_init=M, tol=tol,
+                                               sampling_points=sampling_points, max_iter=40, grow_M=0)
+        if not np.all(err < tol):
+            continue
+        cost = nk * (nh * (Mh + 1) + nj * (Mj + 1)) * bessel_cost + entries * (terms_per_entry * Mh + Mj)
+        if best is None or cost < best[-1]:
+            best = (nh, Mh, nj, Mj, err, cost)
+    if best is None:
+        raise RuntimeError(f"no degree in {degrees} reached tol = {tol}")
+    return best
 
 
 def bessel01(z, f32: bool = False) -> np.ndarray:

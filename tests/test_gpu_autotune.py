@@ -44,3 +44,17 @@ def test_autotune_best_effort(qb):
     with pytest.raises(qb._lib.QBGError):
         qb.chebyshev_params(sol, pts, zj, ws=ws, npanels_h_init=50, M_h_init=3, npanels_j_init=50, M_j_init=3,
                             tol=1e-15, max_iter=2, strict=True)
+
+
+def test_min_cost_choice_meets_tol(qb):
+    b = qb.make_star(0.2, 5)
+    sol = qb.CFIE_kress(1.0, b)
+    pts, sol = qb.points_with_n(sol, b, 400, 25.0)
+    ws = qb.Workspace(sol, pts)
+    zj, _ = qb.contour(25.0 + 0j, 0.4, 8)
+    nh, Mh, nj, Mj, err, cost = qb.chebyshev_params_min_cost(sol, pts, zj, ws=ws, tol=1e-10, degrees=(5, 9, 13),
+                                                             sampling_points=20000)
+    assert Mh in (5, 9, 13) and np.all(err < 1e-10) and cost > 0
+    cheb = qb.assemble(ws, zj[:1], cheb=(nh, Mh, nj, Mj))[0]
+    direct = qb.assemble(ws, zj[:1])[0]
+    assert np.max(np.abs(cheb - direct)) / np.max(np.abs(direct)) < 1e-9
