@@ -185,6 +185,9 @@ typedef struct qbg_beyn_opts {
   int32_t node_chunk;   /* 0: every contour node's operator stays factored from create on;
                            c > 0: at most c operators are resident and each moments call streams
                            the nodes through them (assemble, factor, solve, accumulate) */
+  int32_t resid_engine; /* complex64 forms, the compensated residual R = V - (hi + lo) X:
+                           0 = tensor cores (exact 7-bit digit products, 28 B of digits per operator
+                           entry held beside the factors), 1 = compensated FP32 on CUDA cores */
 } qbg_beyn_opts;
 
 typedef struct qbg_beyn_stats {
@@ -315,6 +318,14 @@ qbg_status qbg_serve_destroy(qbg_server* s);
 qbg_status qbg_cgemm_c64(int32_t engine, int32_t M, int32_t N, int32_t K, const float* alpha, const float* A,
                          int64_t lda, const float* B, int64_t ldb, const float* beta, float* C, int64_t ldc,
                          int32_t batch);
+
+/* Refinement residual, for validation: R_b = V_b - (Th_b + Tl_b) X_b for b < batch
+ * (host buffers, column-major; Th, Tl: n x n complex64 per b, Tl may be NULL;
+ * X, V, R: n x L complex128 per b), rmax = max |re R| + |im R|. engine 0 =
+ * tensor cores (exact digit products), 1 = compensated FP32 on CUDA cores.
+ * No reference counterpart (the reference has no refinement). */
+qbg_status qbg_residual_c64(int32_t engine, int32_t n, int32_t L, int32_t batch, const float* Th, const float* Tl,
+                            const double* X, const double* V, double* R, double* rmax);
 
 /* Selects the complex64 GEMM engine (0 or 1 as above) for later calls,
  * process-wide; the default is 1. No reference counterpart. */

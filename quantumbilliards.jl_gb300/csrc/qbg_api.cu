@@ -610,6 +610,61 @@ qbg_status qbg_launch_count(uint64_t* count) {
   return QBG_OK;
 }
 
+qbg_status qbg_residual_c64(int32_t engine, int32_t n, int32_t L, int32_t batch, const float* Th, const float* Tl,
+                            const double* X, const double* V, double* R, double* rmax) {
+  if (!Th || !X || !V || !R || !rmax || n < 1 || L < 1 || batch < 1 || batch > 65535 ||
+      (engine != 0 && engine != 1)) {
+    set_error("qbg_residual_c64: invalid arguments");
+    return QBG_EINVAL;
+  }
+  const size_t nn = (size_t)n * n, nl = (size_t)n * L;
+  std::vector<void*> tmp;
+  auto cleanup = [&]() { for (void* p : tmp) cudaFree(p); };
+  auto talloc = [&](auto** p, size_t bytes) {
+    int s = dmalloc(p, bytes);
+    if (!s) tmp.push_back(*p);
+    return s;
+  };
+  cxf *dTh = nullptr, *dTl = nullptr;
+  cxd *dX = nullptr, *dV = nullptr, *dR = nullptr;
+  double* dmax = nullptr;
+  void *tmem = nullptr, *xmem = nullptr;
+  int s = QBG_OK;
+  if ((s = talloc(&dTh, sizeof(cxf) * nn * batch)) || (Tl && (s = talloc(&dTl, sizeof(cxf) * nn * batch))) ||
+      (s = talloc(&dX, sizeof(cxd) * nl * batch)) || (s = talloc(&dV, sizeof(cxd) * nl * batch)) ||
+      (s = talloc(&dR, sizeof(cxd) * nl * batch)) || (s = talloc(&dmax, sizeof(double)))) {
+    cleanup();
+    return s;
+  }
+  cudaError_t e = cudaMemcpy(dTh, Th, sizeof(cxf) * nn * batch, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && Tl) e = cudaMemcpy(dTl, Tl, sizeof(cxf) * nn * batch, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dX, X, sizeof(cxd) * nl * batch, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dV, V, sizeof(cxd) * nl * batch, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(dmax, 0, sizeof(double));
+  if (e != cudaSuccess) { cleanup(); return cuda_status(e, "qbg_residual_c64 staging"); }
+  if (engine == 1) {
+    s = residual_df32(dTh, dTl, (long long)nn, dX, (long long)nl, dV, (long long)nl, dR, (long long)nl, n, L, batch,
+                      dmax, 0);
+  } else {
+    TcResidT t;
+    if (!(s = talloc(&tmem, tc_resid_T_bytes(n, batch))) && !(s = talloc(&xmem, tc_resid_X_bytes(n, L, batch)))) {
+      e = cudaMemset(xmem, 0, tc_resid_X_bytes(n, L, batch));
+      if (e != cudaSuccess) s = cuda_status(e, "memset");
+    }
+    if (!s) s = tc_resid_bind_T(t, n, batch, tmem, 0);
+    if (!s) s = tc_resid_prepare_T(t, dTh, dTl, (long long)nn, batch, 0);
+    if (!s) s = tc_residual(t, dX, (long long)nl, dV, (long long)nl, dR, (long long)nl, L, batch, dmax, xmem, 0);
+    if (!s) s = tc_check(0);
+  }
+  if (!s) {
+    e = cudaMemcpy(R, dR, sizeof(cxd) * nl * batch, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(rmax, dmax, sizeof(double), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) s = cuda_status(e, "qbg_residual_c64 D2H");
+  }
+  cleanup();
+  return s;
+}
+
 qbg_status qbg_set_gemm_engine(int32_t engine) {
   if (engine != GEMM_ENGINE_SIMT && engine != GEMM_ENGINE_TCGEN05) {
     set_error("qbg_set_gemm_engine: engine must be 0 or 1");

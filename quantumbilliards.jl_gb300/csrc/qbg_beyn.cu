@@ -38,6 +38,8 @@ struct qbg_beyn {
   LUBatch<float> ff;   // complex64 forms: cap operators
   cxf* Tcopy = nullptr;  // complex64 forms: unfactored hi words for the refinement residual
   cxf* Tlo = nullptr;    // mixed form: lo words, T = hi + lo to ~2^-48
+  bool tc_resid = false;  // complex64 forms: residual on the tensor cores from digit planes of T
+  TcResidT tr;
   void** dptrs = nullptr;  // device array of the cap operator slots
   void** dlo = nullptr;    // device array of the cap lo slots (mixed form)
   int res0 = -1, resn = 0;  // nodes [res0, res0 + resn) are factored in the slots
@@ -136,6 +138,15 @@ int setup(qbg_beyn* b, const double* k0s, const double* Rs) {
     for (int j = 0; j < cap; ++j) lp[j] = b->Tlo + (size_t)j * b->ff.stride;
     QBG_CUDA(cudaMemcpyAsync(b->dlo, lp.data(), sizeof(void*) * cap, cudaMemcpyHostToDevice, st));
   }
+  if (b->prec != QBG_PREC_FP64 && b->opts.resid_engine == 0) {
+    void* mem = nullptr;
+    QBG_TRY(b->alloc(&mem, tc_resid_T_bytes(n, cap)));
+    QBG_TRY(tc_resid_bind_T(b->tr, n, cap, mem, st));
+    b->tc_resid = true;
+  } else if (b->opts.resid_engine != 0 && b->opts.resid_engine != 1) {
+    set_error("resid_engine must be 0 (tensor cores) or 1 (compensated FP32)");
+    return QBG_EINVAL;
+  }
   QBG_CUDA(cudaStreamSynchronize(st));  // the host pointer tables must outlive their copies
   return QBG_OK;
 }
@@ -175,6 +186,7 @@ int load(qbg_beyn* b, int n0, int c) {
   } else {
     QBG_CUDA(cudaMemcpyAsync(b->Tcopy, b->ff.A, sizeof(cxf) * (size_t)b->ff.stride * c, cudaMemcpyDeviceToDevice,
                              st));
+    if (b->tc_resid) QBG_TRY(tc_resid_prepare_T(b->tr, b->Tcopy, b->Tlo, b->ff.stride, c, st));
     b->ff.batch = c;
     QBG_TRY(lu_factor<float>(b->ff, st));
     info = b->ff.info;
@@ -212,6 +224,7 @@ struct Call {
   cxd *X64 = nullptr, *R64 = nullptr;
   cxf *V32 = nullptr, *X32 = nullptr, *R32 = nullptr;
   double* dmax = nullptr;
+  void* xmem = nullptr;  // digit planes of X for the tensor-core residual
   std::vector<void*> tmp;
   std::vector<cudaEvent_t> sev;  // start/stop pairs around the solve passes
   // statistics (the history is the last node group's)
@@ -288,9 +301,12 @@ int refine_resident(Call& c) {
   for (int it = 0; it < b->opts.max_refine; ++it) {
     QBG_CUDA(cudaMemsetAsync(c.dmax, 0, sizeof(double), st));
     cudaEventRecord(b->ev[4], st);
-    if ((s = residual_df32(b->Tcopy, b->Tlo, b->ff.stride, c.X64, (long long)nl, V64, sV, c.R64, (long long)nl, n,
-                           L, nr, c.dmax, st)))
-      return s;
+    if (b->tc_resid)
+      s = tc_residual(b->tr, c.X64, (long long)nl, V64, sV, c.R64, (long long)nl, L, nr, c.dmax, c.xmem, st);
+    else
+      s = residual_df32(b->Tcopy, b->Tlo, b->ff.stride, c.X64, (long long)nl, V64, sV, c.R64, (long long)nl, n, L,
+                        nr, c.dmax, st);
+    if (s) return s;
     cudaEventRecord(b->ev[5], st);
     double rmax = 0.0;
     QBG_CUDA(cudaMemcpyAsync(&rmax, c.dmax, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -458,6 +474,11 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
     QBG_TRY(c.talloc(&c.R32, sizeof(cxf) * nl * cap));
     QBG_TRY(c.talloc(&c.R64, sizeof(cxd) * nl * cap));
     QBG_TRY(c.talloc(&c.dmax, sizeof(double)));
+    if (b->tc_resid) {
+      const size_t xb = tc_resid_X_bytes(n, (int)L, b->cap);
+      QBG_TRY(c.talloc(&c.xmem, xb));
+      QBG_CUDA(cudaMemsetAsync(c.xmem, 0, xb, st));
+    }
     QBG_TRY(convert_d2f(c.dV, c.V32, (long long)nl, st));
     // max |V| (|re| + |im|) scales the convergence test
     std::vector<cxd> hv;

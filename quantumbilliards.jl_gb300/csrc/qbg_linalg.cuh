@@ -91,6 +91,23 @@ int tc_gemm_c64(int M, int N, int K, cxf alpha, const cxf* A, long long lda, lon
 // mbarrier wait gave up); synchronizes the stream. Returns QBG_OK or QBG_ECUDA.
 int tc_check(cudaStream_t st);
 
+// Refinement residual on the tensor cores (exact 7-bit digit products, see
+// qbg_tc_resid.cu). The digit planes of the operators T = hi + lo are built
+// once per factorisation; each residual splits X and forms R = V - T X.
+struct TcResidT {
+  int n = 0, batch = 0, Kp = 0;
+  void* TD = nullptr;   // bf16 digit planes
+  int* erow = nullptr;  // row exponents
+};
+size_t tc_resid_T_bytes(int n, int batch);
+int tc_resid_bind_T(TcResidT& t, int n, int batch, void* mem, cudaStream_t st);  // zeroes mem
+int tc_resid_prepare_T(TcResidT& t, const cxf* Th, const cxf* Tl, long long sT, int c, cudaStream_t st);
+size_t tc_resid_X_bytes(int n, int L, int batch);  // scratch per residual call (zeroed once by the caller)
+int tc_residual(const TcResidT& t, const cxd* X, long long sX, const cxd* V, long long sV, cxd* R, long long sR,
+                int L, int c, double* rmax, void* xmem, cudaStream_t st);
+// device address of the tensor-core error flag (shared by the GEMM and the residual)
+int tc_error_ptr(int** p);
+
 // Engine of the complex64 GEMMs inside gemm_batched<float> (LU trailing
 // updates, triangular-solve updates, refinement products): 0 = CUDA-core FMA
 // tiles, 1 = tcgen05 tensor cores. Process-wide.

@@ -343,6 +343,8 @@ int tc_device_setup(int** err_out) {
 }
 }  // namespace
 
+int tc_error_ptr(int** p) { return tc_device_setup(p); }
+
 void set_gemm_engine(int e) { g_engine.store(e == GEMM_ENGINE_SIMT ? GEMM_ENGINE_SIMT : GEMM_ENGINE_TCGEN05); }
 int gemm_engine() { return g_engine.load(); }
 

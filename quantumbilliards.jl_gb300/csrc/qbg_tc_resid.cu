@@ -1,0 +1,498 @@
+// Refinement residual R = V - T X on the tensor cores with exact digit
+// products (tcgen05, kind::f16 with bf16 operands, FP32 accumulation in TMEM).
+//
+// T (the FP64 value hi + lo of each operator entry) is scaled per row and X
+// (complex128) per column so that every scaled value t satisfies |t| < 1/2,
+// and both are split into 7 signed digits of 7 bits,
+//   t = sum_{a=1..7} d_a 2^{-7a},  |d_a| <= 64,
+// each digit an integer that bf16 holds exactly. The product of two digits
+// is at most 2^12 and is exact in FP32; the digit pairs (a, b) with
+// a + b = g <= 8 (28 pairs, 7 levels g = 2..8) are summed per level in its
+// own TMEM accumulator. A level collects at most 7 pairs, so over 512 real
+// terms its partial sum stays below 7 * 2^21 < 2^24 and is exact; every 512
+// terms the levels are read back and added, scaled by 2^{-7g}, into
+// double-float (hi + lo FP32) sums, which carry ~48 bits. The pairs left out
+// (a + b >= 9) and the truncation of both digit expansions are below 2^-47 of
+// max|T_i.| max|X_.l| per term, the accuracy of the compensated FP32 kernel
+// this replaces. The complex product uses the real mapping of the complex
+// GEMM kernel: A' rows interleave (Re, Im) along k, B' rows are (Re, -Im) for
+// the real part of an output column and (Im, Re) for its imaginary part.
+//
+// Layouts (bf16, row-major, K padded to Kp, a multiple of 32, with zeros):
+//   T digits  [node][a][i][Kp]          (i < n)
+//   X digits  [node][b][j][Kp]          (j < Lp: real-part rows, Lp + j: imaginary-part rows)
+// One CTA (128 threads) owns 128 rows x 32 complex columns of R: 7 levels x
+// 64 FP32 TMEM columns. Operands stream through two shared-memory stages of
+// 32 real k (84 KB each) by cp.async; thread 0 issues the 28 x 2 MMAs of a
+// stage and commits them to the stage's mbarrier. Every mbarrier wait is
+// bounded (1e9 SM cycles): on timeout the CTA records an error, waits
+// (bounded) for its own MMAs, frees its TMEM and returns without writing R.
+#include <cstdint>
+#include <cuda_bf16.h>
+#include "qbg_common.cuh"
+#include "qbg_linalg.cuh"
+
+namespace qbg {
+namespace {
+
+constexpr int RD = 7;                 // digits per operand
+constexpr int RLEV = 7;               // levels g = 2..8
+constexpr int RBM = 128;              // rows of R per CTA
+constexpr int RBN = 32;               // complex columns of R per CTA (B' rows: 64)
+constexpr int RKS = 32;               // real k per stage (2 MMA k-steps of 16)
+constexpr int RCHUNK = 16;            // stages between exact flushes (512 real k)
+constexpr int RA_STEP = RBM * 16 * 2;           // bytes of one A plane per k-step (4096)
+constexpr int RB_STEP = 2 * RBN * 16 * 2;       // bytes of one B plane per k-step (2048)
+constexpr int RA_STAGE = RD * 2 * RA_STEP;      // 57344
+constexpr int RB_STAGE = RD * 2 * RB_STEP;      // 28672
+constexpr int RSTAGE = RA_STAGE + RB_STAGE;     // 86016
+constexpr uint32_t RTMEM_COLS = 512;
+constexpr long long RSPIN = 1ll << 26;
+// D f32, A/B bf16, K-major, N = 64, M = 128
+constexpr uint32_t R_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ uint32_t r_smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint64_t r_desc(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((128u >> 4) & 0x3FFFu) << 16;  // LBO: the two core matrices along k
+  d |= (uint64_t)((256u >> 4) & 0x3FFFu) << 32;  // SBO: consecutive 8-row groups
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+__device__ __forceinline__ void r_mma(uint32_t dtmem, uint64_t da, uint64_t db, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(da), "l"(db), "r"(R_IDESC), "r"(acc));
+}
+
+__device__ __forceinline__ void r_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ bool r_wait(uint32_t mbar, uint32_t parity) {
+  const long long t0 = clock64();
+  for (long long it = 0; it < RSPIN; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (clock64() - t0 > 1000000000ll) break;
+  }
+  return false;
+}
+
+// 16-byte global -> shared copy; src_bytes = 0 fills zeros without reading
+__device__ __forceinline__ void r_cp16(uint32_t dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+
+// exact df32 accumulation of one FP32 value
+__device__ __forceinline__ void df_add(float& hi, float& lo, float x) {
+  const float s = hi + x;
+  const float bb = s - hi;
+  const float e = (hi - (s - bb)) + (x - bb);
+  lo += e;
+  const float h2 = s + lo;
+  lo -= h2 - s;
+  hi = h2;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// digit preparation
+// ---------------------------------------------------------------------------
+// row exponent e_i with max_k |T_ik| < 2^(e_i - 1) (re and im parts; T = hi + lo)
+__global__ void k_t_rowexp(const cxf* __restrict__ Th, const cxf* __restrict__ Tl, long long sT, int n,
+                           int* __restrict__ erow) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const long long b = blockIdx.y;
+  if (i >= n) return;
+  const cxf* h = Th + b * sT;
+  const cxf* l = Tl ? Tl + b * sT : nullptr;
+  double m = 0.0;
+  for (int j = 0; j < n; ++j) {
+    const long long e = (long long)i + (long long)j * n;
+    double re = h[e].re, im = h[e].im;
+    if (l) { re += (double)l[e].re; im += (double)l[e].im; }
+    m = fmax(m, fmax(fabs(re), fabs(im)));
+  }
+  int E = 0;
+  frexp(m, &E);
+  erow[b * n + i] = m > 0.0 ? E + 1 : 0;
+}
+
+__device__ __forceinline__ void digits7(double t, float* d) {
+#pragma unroll
+  for (int a = 0; a < RD; ++a) {
+    const double y = t * 128.0;
+    const double q = rint(y);
+    t = y - q;
+    d[a] = (float)q;
+  }
+}
+
+// T digit planes through a 32 x 32 shared-memory transpose (column-major in,
+// row-major out); grid (n/32, n/32, batch), block (32, 8)
+__global__ void k_t_digits(const cxf* __restrict__ Th, const cxf* __restrict__ Tl, long long sT, int n, int Kp,
+                           const int* __restrict__ erow, __nv_bfloat16* __restrict__ TD) {
+  __shared__ cxd tile[32][33];  // [column][row]
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  const long long b = blockIdx.z;
+  const cxf* h = Th + b * sT;
+  const cxf* l = Tl ? Tl + b * sT : nullptr;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int c = ty + 8 * r, i = i0 + tx, k = k0 + c;
+    cxd v(0.0, 0.0);
+    if (i < n && k < n) {
+      const long long e = (long long)i + (long long)k * n;
+      v = cxd(h[e]);
+      if (l) { v.re += (double)l[e].re; v.im += (double)l[e].im; }
+    }
+    tile[c][tx] = v;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int row = ty + 8 * r, i = i0 + row, k = k0 + tx;
+    if (i >= n || k >= n) continue;
+    const cxd v = tile[tx][row];
+    const int e = erow[b * n + i];
+    float dr[RD], di[RD];
+    digits7(ldexp(v.re, -e), dr);
+    digits7(ldexp(v.im, -e), di);
+#pragma unroll
+    for (int a = 0; a < RD; ++a) {
+      __nv_bfloat162 p;
+      p.x = __float2bfloat16_rn(dr[a]);
+      p.y = __float2bfloat16_rn(di[a]);
+      *reinterpret_cast<__nv_bfloat162*>(TD + (((b * RD + a) * n + i) * (long long)Kp + 2 * (long long)k)) = p;
+    }
+  }
+}
+
+// column exponent f_l with max_k |X_kl| < 2^(f_l - 1); grid (L, batch)
+__global__ void k_x_colexp(const cxd* __restrict__ X, long long sX, int n, int L, int* __restrict__ fcol) {
+  const int l = blockIdx.x;
+  const long long b = blockIdx.y;
+  const cxd* x = X + b * sX + (long long)l * n;
+  double m = 0.0;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) m = fmax(m, fmax(fabs(x[k].re), fabs(x[k].im)));
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = threadIdx.x < (int)(blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) {
+      int E = 0;
+      frexp(m, &E);
+      fcol[b * L + l] = m > 0.0 ? E + 1 : 0;
+    }
+  }
+}
+
+// X digit planes in the B' layout: row l = (Re, -Im), row Lp + l = (Im, Re)
+// of column l along k; columns l in [L, Lp) are zero. grid (n/256, Lp, batch)
+__global__ void k_x_digits(const cxd* __restrict__ X, long long sX, int n, int L, int Lp, int Kp,
+                           const int* __restrict__ fcol, __nv_bfloat16* __restrict__ XD) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int l = blockIdx.y;
+  const long long b = blockIdx.z;
+  if (k >= n) return;
+  cxd v(0.0, 0.0);
+  int f = 0;
+  if (l < L) {
+    v = X[b * sX + (long long)l * n + k];
+    f = fcol[b * L + l];
+  }
+  float dr[RD], di[RD];
+  digits7(ldexp(v.re, -f), dr);
+  digits7(ldexp(v.im, -f), di);
+#pragma unroll
+  for (int a = 0; a < RD; ++a) {
+    __nv_bfloat162 pr, pi;
+    pr.x = __float2bfloat16_rn(dr[a]);
+    pr.y = __float2bfloat16_rn(-di[a]);
+    pi.x = __float2bfloat16_rn(di[a]);
+    pi.y = __float2bfloat16_rn(dr[a]);
+    const long long base = (b * RD + a) * 2LL * Lp;
+    *reinterpret_cast<__nv_bfloat162*>(XD + ((base + l) * Kp + 2LL * k)) = pr;
+    *reinterpret_cast<__nv_bfloat162*>(XD + ((base + Lp + l) * Kp + 2LL * k)) = pi;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// R = V - T X from the digit planes; grid (Lp / 32, ceil(n / 128), batch)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128, 1) k_resid_tc(const __nv_bfloat16* __restrict__ TD,
+                                                     const int* __restrict__ erow,
+                                                     const __nv_bfloat16* __restrict__ XD,
+                                                     const int* __restrict__ fcol, int n, int L, int Lp, int Kp,
+                                                     const cxd* __restrict__ V, long long sV, cxd* R, long long sR,
+                                                     unsigned long long* rmax, int* err) {
+  extern __shared__ __align__(1024) unsigned char r_smem[];
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(r_smem + 2 * RSTAGE);  // [2]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 2);
+  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int n0 = blockIdx.x * RBN, m0 = blockIdx.y * RBM;
+  const long long b = blockIdx.z;
+  const __nv_bfloat16* Tb = TD + b * (long long)RD * n * Kp;
+  const __nv_bfloat16* Xb = XD + b * (long long)RD * 2 * Lp * Kp;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(r_smem_u32(tmem_slot)),
+                 "r"(RTMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(r_smem_u32(mbar)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(r_smem_u32(mbar + 1)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    *abort_flag = (*reinterpret_cast<volatile int*>(err) != 0) ? 1 : 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t mb0 = r_smem_u32(mbar), mb1 = r_smem_u32(mbar + 1);
+  const uint32_t sbase = r_smem_u32(r_smem);
+
+  // cp.async of one stage: T digits (7 planes x 128 rows x 4 chunks of 8 k) and
+  // X digits (7 planes x 64 B' rows x 4 chunks) into the canonical K-major layout
+  auto load_stage = [&](int kt, int st) {
+    const uint32_t so = sbase + (uint32_t)st * RSTAGE;
+    const long long k0 = (long long)kt * RKS;
+#pragma unroll 4
+    for (int it = 0; it < (RD * RBM * 4) / 128; ++it) {
+      const int q = tid + 128 * it;
+      const int kc = q & 3, row = (q >> 2) & (RBM - 1), a = q >> 9;
+      const int gi = m0 + row;
+      const bool ok = gi < n;
+      const __nv_bfloat16* src = Tb + ((long long)a * n + (ok ? gi : 0)) * Kp + k0 + 8 * kc;
+      const uint32_t dst = so + (uint32_t)((a * 2 + (kc >> 1)) * RA_STEP + (row >> 3) * 256 + (kc & 1) * 128 +
+                                           (row & 7) * 16);
+      r_cp16(dst, src, ok ? 16u : 0u);
+    }
+#pragma unroll 2
+    for (int it = 0; it < (RD * 2 * RBN * 4) / 128; ++it) {
+      const int q = tid + 128 * it;
+      const int kc = q & 3, row = (q >> 2) & (2 * RBN - 1), a = q >> 8;
+      const int gj = row < RBN ? n0 + row : Lp + n0 + row - RBN;
+      const __nv_bfloat16* src = Xb + ((long long)a * 2 * Lp + gj) * Kp + k0 + 8 * kc;
+      const uint32_t dst = so + RA_STAGE +
+                           (uint32_t)((a * 2 + (kc >> 1)) * RB_STEP + (row >> 3) * 256 + (kc & 1) * 128 + (row & 7) * 16);
+      r_cp16(dst, src, 16u);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+
+  float acc_hi[2 * RBN], acc_lo[2 * RBN];
+#pragma unroll
+  for (int c = 0; c < 2 * RBN; ++c) { acc_hi[c] = 0.f; acc_lo[c] = 0.f; }
+
+  uint32_t wph0 = 0u, wph1 = 0u;
+  bool pend0 = false, pend1 = false;
+  bool ok = (*abort_flag == 0);
+  const int ktiles = Kp / RKS;
+  uint32_t started = 0u;  // thread 0: levels whose accumulator holds this chunk's sum (bit g - 2)
+
+  if (ok) load_stage(0, 0);
+  for (int kt = 0; kt < ktiles && ok; ++kt) {
+    const int st = kt & 1;
+    if (kt + 1 < ktiles) {
+      // the other stage was read by the MMAs of tile kt - 1
+      if (st ? pend0 : pend1) {
+        if (r_wait(st ? mb0 : mb1, st ? wph0 : wph1)) {
+          if (st) { wph0 ^= 1u; pend0 = false; } else { wph1 ^= 1u; pend1 = false; }
+        } else {
+          atomicExch(abort_flag, 1);
+        }
+      }
+      load_stage(kt + 1, st ^ 1);
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (*abort_flag) { ok = false; break; }
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t so = sbase + (uint32_t)st * RSTAGE;
+#pragma unroll
+      for (int ks = 0; ks < 2; ++ks) {
+#pragma unroll
+        for (int a = 1; a <= RD; ++a) {
+          const uint64_t da = r_desc(so + (uint32_t)(((a - 1) * 2 + ks) * RA_STEP));
+#pragma unroll
+          for (int bq = 1; bq + a <= RLEV + 1; ++bq) {
+            const int g = a + bq;  // 2 .. 8
+            const uint64_t db = r_desc(so + RA_STAGE + (uint32_t)(((bq - 1) * 2 + ks) * RB_STEP));
+            const uint32_t bit = 1u << (g - 2);
+            r_mma(tmem + (uint32_t)((g - 2) * 2 * RBN), da, db, (started & bit) ? 1u : 0u);
+            started |= bit;
+          }
+        }
+      }
+      r_commit(st ? mb1 : mb0);
+    }
+    if (st) pend1 = true; else pend0 = true;
+    if ((kt + 1) % RCHUNK == 0 || kt + 1 == ktiles) {
+      // every MMA so far completes before the exact level sums are read back
+      bool good = true;
+      if (pend0) { if (r_wait(mb0, wph0)) { wph0 ^= 1u; pend0 = false; } else good = false; }
+      if (pend1) { if (r_wait(mb1, wph1)) { wph1 ^= 1u; pend1 = false; } else good = false; }
+      if (!good) atomicExch(abort_flag, 1);
+      // the warp-synchronous TMEM loads run only on a CTA-wide decision
+      __syncthreads();
+      const bool flush = (*abort_flag == 0);
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (flush) {
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+        for (int lev = 0; lev < RLEV; ++lev) {
+          const float sc = ldexpf(1.f, -7 * (lev + 2));
+#pragma unroll
+          for (int qt = 0; qt < 4; ++qt) {
+            uint32_t v[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15])
+                : "r"(taddr + (uint32_t)(lev * 2 * RBN + qt * 16)));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int c = 0; c < 16; ++c) df_add(acc_hi[qt * 16 + c], acc_lo[qt * 16 + c], __uint_as_float(v[c]) * sc);
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      if (tid == 0) started = 0u;  // the next chunk restarts every level
+      if (*abort_flag) { ok = false; break; }
+    }
+  }
+  if (!ok) {
+    if (tid == 0) atomicExch(err, 1);
+    if (pend0) r_wait(mb0, wph0);
+    if (pend1) r_wait(mb1, wph1);
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+  } else {
+    const int i = m0 + tid;
+    if (i < n) {
+      const int ei = erow[b * n + i];
+      const cxd* Vb = V + b * sV;
+      cxd* Rb = R + b * sR;
+      double lmax = 0.0;
+#pragma unroll
+      for (int c = 0; c < RBN; ++c) {
+        const int col = n0 + c;
+        if (col >= L) continue;  // full unroll keeps the sums in registers
+        const int f = fcol[b * L + col];
+        const double re = ldexp((double)acc_hi[c] + (double)acc_lo[c], ei + f);
+        const double im = ldexp((double)acc_hi[RBN + c] + (double)acc_lo[RBN + c], ei + f);
+        const long long e = (long long)i + (long long)col * n;
+        const cxd v = Vb[e];
+        const cxd r(v.re - re, v.im - im);
+        Rb[e] = r;
+        lmax = fmax(lmax, fabs(r.re) + fabs(r.im));
+      }
+      if (rmax) atomicMax(rmax, (unsigned long long)__double_as_longlong(lmax));
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(RTMEM_COLS) : "memory");
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static int kp_of(int n) { return ((2 * n + RKS - 1) / RKS) * RKS; }
+static int lp_of(int L) { return ((L + RBN - 1) / RBN) * RBN; }
+
+size_t tc_resid_T_bytes(int n, int batch) {
+  const size_t dig = (size_t)batch * RD * n * kp_of(n) * sizeof(__nv_bfloat16);
+  return ((dig + 255) & ~(size_t)255) + (size_t)batch * n * sizeof(int);
+}
+
+int tc_resid_bind_T(TcResidT& t, int n, int batch, void* mem, cudaStream_t st) {
+  t.n = n;
+  t.batch = batch;
+  t.Kp = kp_of(n);
+  const size_t dig = (size_t)batch * RD * n * t.Kp * sizeof(__nv_bfloat16);
+  t.TD = mem;
+  t.erow = reinterpret_cast<int*>(static_cast<unsigned char*>(mem) + ((dig + 255) & ~(size_t)255));
+  // the k padding of every digit row stays zero
+  QBG_CUDA(cudaMemsetAsync(mem, 0, tc_resid_T_bytes(n, batch), st));
+  return QBG_OK;
+}
+
+int tc_resid_prepare_T(TcResidT& t, const cxf* Th, const cxf* Tl, long long sT, int c, cudaStream_t st) {
+  if (c > t.batch) {
+    set_error("tc_resid_prepare_T: %d operators, room for %d", c, t.batch);
+    return QBG_EINVAL;
+  }
+  const int n = t.n;
+  k_t_rowexp<<<dim3((n + 255) / 256, c), 256, 0, st>>>(Th, Tl, sT, n, t.erow);
+  QBG_LAUNCH_CHECK("k_t_rowexp");
+  k_t_digits<<<dim3((n + 31) / 32, (n + 31) / 32, c), dim3(32, 8), 0, st>>>(Th, Tl, sT, n, t.Kp, t.erow, static_cast<__nv_bfloat16*>(t.TD));
+  QBG_LAUNCH_CHECK("k_t_digits");
+  return QBG_OK;
+}
+
+size_t tc_resid_X_bytes(int n, int L, int batch) {
+  const size_t dig = (size_t)batch * RD * 2 * lp_of(L) * kp_of(n) * sizeof(__nv_bfloat16);
+  return ((dig + 255) & ~(size_t)255) + (size_t)batch * L * sizeof(int);
+}
+
+int tc_residual(const TcResidT& t, const cxd* X, long long sX, const cxd* V, long long sV, cxd* R, long long sR,
+                int L, int c, double* rmax, void* xmem, cudaStream_t st) {
+  const int n = t.n, Kp = t.Kp, Lp = lp_of(L);
+  if (c > t.batch || c < 1 || c > 65535 || L < 1) {
+    set_error("tc_residual: bad sizes");
+    return QBG_EINVAL;
+  }
+  const size_t dig = (size_t)c * RD * 2 * Lp * Kp * sizeof(__nv_bfloat16);
+  __nv_bfloat16* XD = static_cast<__nv_bfloat16*>(xmem);
+  int* fcol = reinterpret_cast<int*>(static_cast<unsigned char*>(xmem) + ((dig + 255) & ~(size_t)255));
+  int* derr = nullptr;
+  QBG_TRY(tc_error_ptr(&derr));
+  static bool attr[64] = {};
+  int dev = 0;
+  QBG_CUDA(cudaGetDevice(&dev));
+  const size_t smem = 2 * (size_t)RSTAGE + 64;
+  if (dev >= 0 && dev < 64 && !attr[dev]) {
+    QBG_CUDA(cudaFuncSetAttribute(k_resid_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr[dev] = true;
+  }
+  k_x_colexp<<<dim3(L, c), 256, 0, st>>>(X, sX, n, L, fcol);
+  QBG_LAUNCH_CHECK("k_x_colexp");
+  k_x_digits<<<dim3((n + 255) / 256, Lp, c), 256, 0, st>>>(X, sX, n, L, Lp, Kp, fcol, XD);
+  QBG_LAUNCH_CHECK("k_x_digits");
+  k_resid_tc<<<dim3(Lp / RBN, (n + RBM - 1) / RBM, c), 128, smem, st>>>(
+      static_cast<const __nv_bfloat16*>(t.TD), t.erow, XD, fcol, n, L, Lp, Kp, V, sV, R, sR, reinterpret_cast<unsigned long long*>(rmax), derr);
+  QBG_LAUNCH_CHECK("k_resid_tc");
+  return QBG_OK;
+}
+
+}  // namespace qbg

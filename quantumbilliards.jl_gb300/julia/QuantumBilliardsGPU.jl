@@ -53,6 +53,7 @@ struct QbgBeynOpts
     fp32_sweeps::Int32      # complex64 forms: plain FP32 residual corrections (0 = default)
     solve_block::Int32      # complex64 forms: triangular-solve block rows (0 = default)
     node_chunk::Int32       # 0: all node operators resident; c > 0: stream the nodes c at a time
+    resid_engine::Int32     # 0: tensor-core residual (digit products), 1: compensated FP32
 end
 
 function qbg_check(st::Int32)
@@ -138,7 +139,7 @@ function QB.construct_B_matrix(solver::GPUSolver, pts, N::Int, k0::Complex{Float
     ws = gpu_workspace(solver, pts)
     @assert ws.dim == N
     h = Ref{Ptr{Cvoid}}(C_NULL)
-    opts = QbgBeynOpts(0, 10, 1e-6, 0, 0, QbgChebParams(0, 0, 0, 0), 0, 0, 0)
+    opts = QbgBeynOpts(0, 10, 1e-6, 0, 0, QbgChebParams(0, 0, 0, 0), 0, 0, 0, 0)
     qbg_check(ccall((:qbg_beyn_create, libqbgpu), Int32,
         (Ptr{Cvoid}, Float64, Float64, Float64, Int32, Int32, Ref{QbgBeynOpts}, Ref{Ptr{Cvoid}}),
         ws.h, real(k0), imag(k0), R, nq, solver.prec, opts, h))

@@ -65,7 +65,7 @@ class ChebParams(C.Structure):
 class BeynOpts(C.Structure):
     _fields_ = [("flags", C.c_int32), ("max_refine", C.c_int32), ("refine_tol", C.c_double), ("nb", C.c_int32),
                 ("eval_mode", C.c_int32), ("cheb", ChebParams), ("fp32_sweeps", C.c_int32),
-                ("solve_block", C.c_int32), ("node_chunk", C.c_int32)]
+                ("solve_block", C.c_int32), ("node_chunk", C.c_int32), ("resid_engine", C.c_int32)]
 
 
 class BeynStats(C.Structure):
@@ -117,6 +117,8 @@ _SIGS = {
                                   C.c_int64, C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.c_void_p, C.c_int64,
                                   C.c_int32]),
     "qbg_set_gemm_engine": (C.c_int32, [C.c_int32]),
+    "qbg_residual_c64": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
     "qbg_serve_create": (C.c_int32, [C.POINTER(ServeOpts), C.POINTER(C.c_void_p)]),
     "qbg_serve_submit": (C.c_int32, [C.c_void_p, C.POINTER(RequestDesc), C.POINTER(C.c_int64)]),
     "qbg_serve_poll": (C.c_int32, [C.c_void_p, C.c_int64, C.POINTER(C.c_int32)]),

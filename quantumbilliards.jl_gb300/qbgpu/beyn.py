@@ -47,7 +47,7 @@ class BeynHandle:
 
     def __init__(self, ws: Workspace, k0, R, nq: int, mixed: bool = False, max_refine: int = 10,
                  refine_tol: float = 1e-6, nb: int = 0, use_chebyshev: bool = True, cheb=None, fp32_sweeps: int = 0,
-                 solve_block: int = 0, node_chunk: int = 0):
+                 solve_block: int = 0, node_chunk: int = 0, resid_engine: int = 0):
         lib = L.load()
         self.multi = np.ndim(k0) > 0
         k0s = np.atleast_1d(np.asarray(k0, dtype=np.complex128))
@@ -59,7 +59,7 @@ class BeynHandle:
         self.refine_tol = float(refine_tol)
         cp = L.ChebParams(*(cheb if cheb else (0, 0, 0, 0)))
         o = L.BeynOpts(0, int(max_refine), float(refine_tol), int(nb), 0 if use_chebyshev else 1, cp,
-                       int(fp32_sweeps), int(solve_block), int(node_chunk))
+                       int(fp32_sweeps), int(solve_block), int(node_chunk), int(resid_engine))
         h = C.c_void_p()
         if self.multi:
             kk = np.ascontiguousarray(k0s).view(np.float64)
@@ -166,7 +166,7 @@ def solve_disks(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed
 
 def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=None, mixed=False, ws=None,
                        max_refine=10, refine_tol=1e-6, return_info=False, regrow="extend", use_chebyshev=True,
-                       cheb=None, fp32_sweeps=0, solve_block=0, node_chunk=0):
+                       cheb=None, fp32_sweeps=0, solve_block=0, node_chunk=0, resid_engine=0):
     """construct_B_matrix (beyn.jl:257-322). Returns (B, Uk) [, info].
 
     regrow: when the rank saturates (rk == r) the reference draws a fresh
@@ -179,7 +179,8 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
     if ws.dim != N:
         raise ValueError(f"N={N} does not match the operator dimension {ws.dim}")
     bh = BeynHandle(ws, k0, R, nq, mixed, max_refine, refine_tol, use_chebyshev=use_chebyshev, cheb=cheb,
-                    fp32_sweeps=fp32_sweeps, solve_block=solve_block, node_chunk=node_chunk)
+                    fp32_sweeps=fp32_sweeps, solve_block=solve_block, node_chunk=node_chunk,
+                    resid_engine=resid_engine)
     info = dict(stats=[])
     try:
         V = probe_matrix(N, r, rng)

@@ -274,6 +274,29 @@ def cgemm(A, B, C=None, alpha=1.0, beta=0.0, engine: int = 1) -> np.ndarray:
     return out[0] if single else out
 
 
+def residual_c64(Th, Tl, X, V, engine: int = 0):
+    """Device refinement residual R = V - (Th + Tl) X (validation helper).
+    Th, Tl: (batch, n, n) complex64 (Tl may be None); X, V: (batch, n, L)
+    complex128. engine 0 = tensor cores, 1 = compensated FP32. Returns (R, rmax)."""
+    Th = np.asarray(Th, np.complex64)
+    single = Th.ndim == 2
+    Th = Th[None] if single else Th
+    bsz, n, _ = Th.shape
+    X = np.asarray(X, np.complex128).reshape(bsz, n, -1)
+    V = np.asarray(V, np.complex128).reshape(bsz, n, -1)
+    L_ = X.shape[2]
+    f = lambda a: np.ascontiguousarray(a.transpose(0, 2, 1))
+    th = f(Th)
+    tl = f(np.asarray(Tl, np.complex64).reshape(bsz, n, n)) if Tl is not None else None
+    x, v = f(X), f(V)
+    r = np.empty_like(x)
+    rmax = C.c_double(0.0)
+    L.check(L.load().qbg_residual_c64(int(engine), n, L_, bsz, L.vptr(th), L.vptr(tl) if tl is not None else None,
+                                      L.vptr(x), L.vptr(v), L.vptr(r), C.byref(rmax)))
+    R = r.transpose(0, 2, 1)
+    return (R[0] if single else R), float(rmax.value)
+
+
 def launch_count() -> int:
     """Kernels launched by the library in this process (its own kernels, not cuSOLVER's)."""
     c = L.C.c_uint64(0)
