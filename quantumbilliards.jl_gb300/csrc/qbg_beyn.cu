@@ -10,6 +10,7 @@
 // nodes through them in groups (assemble, factor, solve, accumulate), which
 // bounds the memory at large N at the price of re-assembling per call.
 #include <algorithm>
+#include <limits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -319,6 +320,7 @@ int refine_resident(Call& c) {
     rel = rmax / c.vmax;
     if (c.nhist < 8) c.hist[c.nhist++] = rel;
     ++sweeps;
+    if (!(rel == rel)) break;  // Inf or NaN in T or X: no correction can help; NaN is reported
     // correction from this residual; when it already meets the tolerance this
     // is the final correction (the residual is in hand, the solve costs one FP32 pass)
     if ((s = convert_d2f(c.R64, c.R32, tot, st)) || (s = c.timed_solve(c.R32, (long long)nl)) ||
@@ -330,7 +332,7 @@ int refine_resident(Call& c) {
     if (c.nhist >= 2 && rel > 0.5 * c.hist[c.nhist - 2]) break;
   }
   c.sweeps = std::max(c.sweeps, sweeps);
-  c.rel = std::max(c.rel, rel);
+  c.rel = (c.rel != c.rel || rel != rel) ? std::numeric_limits<double>::quiet_NaN() : std::max(c.rel, rel);
   return QBG_OK;
 }
 

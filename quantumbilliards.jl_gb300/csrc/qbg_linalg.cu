@@ -869,6 +869,7 @@ __global__ void __launch_bounds__(256) k_residual_df32(const cxf* __restrict__ T
     __syncthreads();
   }
   double lmax = 0.0;
+  bool bad = false;
 #pragma unroll
   for (int b = 0; b < 2; ++b) {
     const int gj = n0 + ty + 16 * b;
@@ -880,12 +881,17 @@ __global__ void __launch_bounds__(256) k_residual_df32(const cxf* __restrict__ T
       const cxd v = Vb[(long long)gi + (long long)gj * n];
       const cxd r(v.re - accr[a][b], v.im - acci[a][b]);
       R[bz * sR + (long long)gi + (long long)gj * n] = r;
-      lmax = fmax(lmax, fabs(r.re) + fabs(r.im));
+      const double m = fabs(r.re) + fabs(r.im);
+      bad |= !(m == m);
+      lmax = fmax(lmax, m);
     }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_down_sync(0xffffffffu, lmax, o));
-  if ((tid & 31) == 0 && rmax) atomicMax(rmax, (unsigned long long)__double_as_longlong(lmax));
+  bad = __any_sync(0xffffffffu, bad);
+  // a NaN (bit pattern above +Inf) wins the unsigned maximum
+  if ((tid & 31) == 0 && rmax)
+    atomicMax(rmax, bad ? 0x7FF8000000000000ull : (unsigned long long)__double_as_longlong(lmax));
 }
 
 int residual_df32(const cxf* Tm, const cxf* Tlo, long long sT, const cxd* X, long long sX, const cxd* V,

@@ -3,9 +3,14 @@
 //
 // T (the FP64 value hi + lo of each operator entry) is scaled per row and X
 // (complex128) per column so that every scaled value t satisfies |t| < 1/2,
-// and both are split into 7 signed digits of 7 bits,
-//   t = sum_{a=1..7} d_a 2^{-7a},  |d_a| <= 64,
-// each digit an integer that bf16 holds exactly. The product of two digits
+// rounded to the fixed-point integer V = round(t 2^49) (|V| <= 2^48) and
+// split into 7 balanced base-128 digits,
+//   V = sum_{a=1..7} d_a 128^{7-a},  |d_a| <= 64,
+// each digit an integer that bf16 holds exactly. The rounding and the
+// splitting are integer operations on the IEEE bit fields (FP64 arithmetic
+// is slow on this part); the fixed point drops at most 2^-50 of the row or
+// column scale per value. Rows of T or columns of X holding a non-finite
+// value give NaN in R and in rmax. The product of two digits
 // is at most 2^12 and is exact in FP32; the digit pairs (a, b) with
 // a + b = g <= 8 (28 pairs, 7 levels g = 2..8) are summed per level in its
 // own TMEM accumulator. A level collects at most 7 pairs, so over 512 real
@@ -110,33 +115,88 @@ __device__ __forceinline__ void df_add(float& hi, float& lo, float x) {
 // ---------------------------------------------------------------------------
 // digit preparation
 // ---------------------------------------------------------------------------
-// row exponent e_i with max_k |T_ik| < 2^(e_i - 1) (re and im parts; T = hi + lo)
-__global__ void k_t_rowexp(const cxf* __restrict__ Th, const cxf* __restrict__ Tl, long long sT, int n,
-                           int* __restrict__ erow) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const long long b = blockIdx.y;
-  if (i >= n) return;
-  const cxf* h = Th + b * sT;
-  const cxf* l = Tl ? Tl + b * sT : nullptr;
-  double m = 0.0;
-  for (int j = 0; j < n; ++j) {
-    const long long e = (long long)i + (long long)j * n;
-    double re = h[e].re, im = h[e].im;
-    if (l) { re += (double)l[e].re; im += (double)l[e].im; }
-    m = fmax(m, fmax(fabs(re), fabs(im)));
-  }
-  int E = 0;
-  frexp(m, &E);
-  erow[b * n + i] = m > 0.0 ? E + 1 : 0;
+constexpr int R_NONFINITE = 0x40000000;  // row / column exponent of a row / column with Inf or NaN
+
+// round(v 2^Q) of an FP32 value as an integer, from its bit fields; the caller
+// guarantees |v| 2^Q < 2^49 (so a shift left stays below 2^49)
+__device__ __forceinline__ long long fx_f32(float v, int Q) {
+  const uint32_t u = __float_as_uint(v);
+  const int ex = (int)((u >> 23) & 255u);
+  long long m = (long long)(ex ? ((u & 0x7FFFFFu) | 0x800000u) : (u & 0x7FFFFFu));
+  const int sh = (ex ? ex : 1) - 150 + Q;
+  if (sh >= 0) m <<= sh;
+  else if (sh > -26) m = (m + (1ll << (-sh - 1))) >> (-sh);
+  else m = 0;
+  return (u >> 31) ? -m : m;
 }
 
-__device__ __forceinline__ void digits7(double t, float* d) {
+// round(v 2^Q) of an FP64 value as an integer (|v| 2^Q < 2^49)
+__device__ __forceinline__ long long fx_f64(double v, int Q) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  const int ex = (int)((u >> 52) & 2047u);
+  long long m = (long long)(u & 0xFFFFFFFFFFFFFull);
+  if (ex) m |= 1ll << 52;
+  const int sh = (ex ? ex : 1) - 1075 + Q;
+  if (sh >= 0) m <<= sh;
+  else if (sh > -55) m = (m + (1ll << (-sh - 1))) >> (-sh);
+  else m = 0;
+  return (u >> 63) ? -m : m;
+}
+
+// balanced base-128 digits of V (|V| <= 2^48 + 1): d[0] most significant, |d| <= 64
+__device__ __forceinline__ void digits7(long long V, float* d) {
 #pragma unroll
-  for (int a = 0; a < RD; ++a) {
-    const double y = t * 128.0;
-    const double q = rint(y);
-    t = y - q;
+  for (int a = RD - 1; a > 0; --a) {
+    const int q = (int)(((uint32_t)V + 64u) & 127u) - 64;
     d[a] = (float)q;
+    V = (V - q) >> 7;
+  }
+  d[0] = (float)V;
+}
+
+// row exponent e_i with max_k |T_ik| < 2^(e_i - 1) (re and im parts; T = hi + lo).
+// From FP32 maxima: |hi + lo| <= max|hi| + max|lo|, and that sum rounded to
+// FP32 is below a power of two whenever the exact sum is. Block (32, 8): 32
+// rows, 8 column strides; grid (n/32, batch).
+__global__ void k_t_rowexp(const cxf* __restrict__ Th, const cxf* __restrict__ Tl, long long sT, int n,
+                           int* __restrict__ erow) {
+  __shared__ float red[3][8][33];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i = blockIdx.x * 32 + tx;
+  const long long b = blockIdx.y;
+  const cxf* h = Th + b * sT;
+  const cxf* l = Tl ? Tl + b * sT : nullptr;
+  float mh = 0.f, ml = 0.f, chk = 0.f;  // chk turns NaN on any Inf or NaN (x * 0)
+  if (i < n) {
+    for (int j = ty; j < n; j += 8) {
+      const long long e = (long long)i + (long long)j * n;
+      const cxf v = h[e];
+      mh = fmaxf(mh, fmaxf(fabsf(v.re), fabsf(v.im)));
+      chk = fmaf(v.re, 0.f, fmaf(v.im, 0.f, chk));
+      if (l) {
+        const cxf w = l[e];
+        ml = fmaxf(ml, fmaxf(fabsf(w.re), fabsf(w.im)));
+        chk = fmaf(w.re, 0.f, fmaf(w.im, 0.f, chk));
+      }
+    }
+  }
+  red[0][ty][tx] = mh;
+  red[1][ty][tx] = ml;
+  red[2][ty][tx] = chk;
+  __syncthreads();
+  if (ty == 0 && i < n) {
+    bool bad = false;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      mh = fmaxf(mh, red[0][r][tx]);
+      ml = fmaxf(ml, red[1][r][tx]);
+      bad |= (red[2][r][tx] != 0.f);
+    }
+    const float m = mh + ml;
+    bad |= !(m <= 3.40282346638528859812e38f);  // the bound itself overflowed
+    int E = 0;
+    frexpf(m, &E);
+    erow[b * n + i] = bad ? R_NONFINITE : (m > 0.f ? E + 1 : 0);
   }
 }
 
@@ -144,7 +204,7 @@ __device__ __forceinline__ void digits7(double t, float* d) {
 // row-major out); grid (n/32, n/32, batch), block (32, 8)
 __global__ void k_t_digits(const cxf* __restrict__ Th, const cxf* __restrict__ Tl, long long sT, int n, int Kp,
                            const int* __restrict__ erow, __nv_bfloat16* __restrict__ TD) {
-  __shared__ cxd tile[32][33];  // [column][row]
+  __shared__ cxf th[32][33], tl[32][33];  // [column][row]
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
   const long long b = blockIdx.z;
@@ -153,24 +213,31 @@ __global__ void k_t_digits(const cxf* __restrict__ Th, const cxf* __restrict__ T
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     const int c = ty + 8 * r, i = i0 + tx, k = k0 + c;
-    cxd v(0.0, 0.0);
+    cxf vh(0.f, 0.f), vl(0.f, 0.f);
     if (i < n && k < n) {
       const long long e = (long long)i + (long long)k * n;
-      v = cxd(h[e]);
-      if (l) { v.re += (double)l[e].re; v.im += (double)l[e].im; }
+      vh = h[e];
+      if (l) vl = l[e];
     }
-    tile[c][tx] = v;
+    th[c][tx] = vh;
+    tl[c][tx] = vl;
   }
   __syncthreads();
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     const int row = ty + 8 * r, i = i0 + row, k = k0 + tx;
     if (i >= n || k >= n) continue;
-    const cxd v = tile[tx][row];
+    const cxf vh = th[tx][row], vl = tl[tx][row];
     const int e = erow[b * n + i];
     float dr[RD], di[RD];
-    digits7(ldexp(v.re, -e), dr);
-    digits7(ldexp(v.im, -e), di);
+    if (e == R_NONFINITE) {
+#pragma unroll
+      for (int a = 0; a < RD; ++a) { dr[a] = 0.f; di[a] = 0.f; }
+    } else {
+      const int Q = 49 - e;
+      digits7(fx_f32(vh.re, Q) + fx_f32(vl.re, Q), dr);
+      digits7(fx_f32(vh.im, Q) + fx_f32(vl.im, Q), di);
+    }
 #pragma unroll
     for (int a = 0; a < RD; ++a) {
       __nv_bfloat162 p;
@@ -187,18 +254,32 @@ __global__ void k_x_colexp(const cxd* __restrict__ X, long long sX, int n, int L
   const long long b = blockIdx.y;
   const cxd* x = X + b * sX + (long long)l * n;
   double m = 0.0;
-  for (int k = threadIdx.x; k < n; k += blockDim.x) m = fmax(m, fmax(fabs(x[k].re), fabs(x[k].im)));
+  int bad = 0;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const double a = fmax(fabs(x[k].re), fabs(x[k].im));
+    bad |= !(a <= 1.79769313486231570815e308);  // Inf or NaN
+    m = fmax(m, a);
+  }
   __shared__ double red[32];
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __shared__ int redb[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  if ((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5] = m; redb[threadIdx.x >> 5] = bad; }
   __syncthreads();
   if (threadIdx.x < 32) {
-    m = threadIdx.x < (int)(blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    const bool in = threadIdx.x < (int)(blockDim.x >> 5);
+    m = in ? red[threadIdx.x] : 0.0;
+    bad = in ? redb[threadIdx.x] : 0;
+    for (int o = 16; o > 0; o >>= 1) {
+      m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+      bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
     if (threadIdx.x == 0) {
       int E = 0;
       frexp(m, &E);
-      fcol[b * L + l] = m > 0.0 ? E + 1 : 0;
+      fcol[b * L + l] = bad ? R_NONFINITE : (m > 0.0 ? E + 1 : 0);
     }
   }
 }
@@ -211,15 +292,16 @@ __global__ void k_x_digits(const cxd* __restrict__ X, long long sX, int n, int L
   const int l = blockIdx.y;
   const long long b = blockIdx.z;
   if (k >= n) return;
-  cxd v(0.0, 0.0);
-  int f = 0;
-  if (l < L) {
-    v = X[b * sX + (long long)l * n + k];
-    f = fcol[b * L + l];
-  }
   float dr[RD], di[RD];
-  digits7(ldexp(v.re, -f), dr);
-  digits7(ldexp(v.im, -f), di);
+  const int f = l < L ? fcol[b * L + l] : R_NONFINITE;
+  if (f == R_NONFINITE) {  // padding column, or a column holding Inf / NaN
+#pragma unroll
+    for (int a = 0; a < RD; ++a) { dr[a] = 0.f; di[a] = 0.f; }
+  } else {
+    const cxd v = X[b * sX + (long long)l * n + k];
+    digits7(fx_f64(v.re, 49 - f), dr);
+    digits7(fx_f64(v.im, 49 - f), di);
+  }
 #pragma unroll
   for (int a = 0; a < RD; ++a) {
     __nv_bfloat162 pr, pi;
@@ -400,20 +482,30 @@ __global__ void __launch_bounds__(128, 1) k_resid_tc(const __nv_bfloat16* __rest
       const cxd* Vb = V + b * sV;
       cxd* Rb = R + b * sR;
       double lmax = 0.0;
+      bool bad = false;
 #pragma unroll
       for (int c = 0; c < RBN; ++c) {
         const int col = n0 + c;
         if (col >= L) continue;  // full unroll keeps the sums in registers
         const int f = fcol[b * L + col];
-        const double re = ldexp((double)acc_hi[c] + (double)acc_lo[c], ei + f);
-        const double im = ldexp((double)acc_hi[RBN + c] + (double)acc_lo[RBN + c], ei + f);
         const long long e = (long long)i + (long long)col * n;
         const cxd v = Vb[e];
-        const cxd r(v.re - re, v.im - im);
+        cxd r;
+        if (ei == R_NONFINITE || f == R_NONFINITE) {
+          r = cxd(__longlong_as_double(0x7FF8000000000000ll), __longlong_as_double(0x7FF8000000000000ll));
+        } else {
+          const double re = ldexp((double)acc_hi[c] + (double)acc_lo[c], ei + f);
+          const double im = ldexp((double)acc_hi[RBN + c] + (double)acc_lo[RBN + c], ei + f);
+          r = cxd(v.re - re, v.im - im);
+        }
         Rb[e] = r;
-        lmax = fmax(lmax, fabs(r.re) + fabs(r.im));
+        const double a = fabs(r.re) + fabs(r.im);
+        bad |= !(a == a);
+        lmax = fmax(lmax, a);
       }
-      if (rmax) atomicMax(rmax, (unsigned long long)__double_as_longlong(lmax));
+      // a NaN (bit pattern above +Inf) wins the unsigned maximum
+      if (rmax)
+        atomicMax(rmax, bad ? 0x7FF8000000000000ull : (unsigned long long)__double_as_longlong(lmax));
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -453,7 +545,7 @@ int tc_resid_prepare_T(TcResidT& t, const cxf* Th, const cxf* Tl, long long sT, 
     return QBG_EINVAL;
   }
   const int n = t.n;
-  k_t_rowexp<<<dim3((n + 255) / 256, c), 256, 0, st>>>(Th, Tl, sT, n, t.erow);
+  k_t_rowexp<<<dim3((n + 31) / 32, c), dim3(32, 8), 0, st>>>(Th, Tl, sT, n, t.erow);
   QBG_LAUNCH_CHECK("k_t_rowexp");
   k_t_digits<<<dim3((n + 31) / 32, (n + 31) / 32, c), dim3(32, 8), 0, st>>>(Th, Tl, sT, n, t.Kp, t.erow, static_cast<__nv_bfloat16*>(t.TD));
   QBG_LAUNCH_CHECK("k_t_digits");

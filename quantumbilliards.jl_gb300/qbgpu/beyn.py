@@ -83,7 +83,7 @@ class BeynHandle:
         A1 = np.empty((self.ndisk, r, N), dtype=np.complex128)
         st = L.BeynStats()
         L.check(lib.qbg_beyn_moments(self._h, L.vptr(V), r, L.vptr(A0), L.vptr(A1), C.byref(st)))
-        if self.prec != L.QBG_PREC_FP64 and st.nhist and st.refine_residual > self.refine_tol:
+        if self.prec != L.QBG_PREC_FP64 and st.nhist and not st.refine_residual <= self.refine_tol:
             warnings.warn(f"qbgpu: mixed refinement stopped at relative residual {st.refine_residual:.2e} > "
                           f"refine_tol {self.refine_tol:.1e} (history {list(st.refine_history[:st.nhist])}); "
                           "the moments are less accurate than requested", RuntimeWarning, stacklevel=2)

@@ -69,3 +69,29 @@ def test_beyn_moments_both_residual_engines(qb, mixed):
         bh.close()
     for a, r in zip(out[0], out[1]):
         assert np.max(np.abs(a - r)) / np.max(np.abs(r)) < 1e-10
+
+
+@pytest.mark.parametrize("engine", [0, 1])
+def test_residual_nonfinite_rows_and_columns(qb, engine):
+    """Inf or NaN in a row of T or a column of X gives a non-finite residual
+    there and a non-finite rmax; every other entry keeps its accuracy."""
+    rng = np.random.default_rng(17)
+    n, L = 160, 24
+    Th, Tl, X, V = _case(rng, 1, n, L)
+    Th[0, 7, 30] = np.nan
+    X[0, 11, 5] = np.inf
+    R, rmax = qb.residual_c64(Th, Tl, X, V, engine=engine)
+    assert not np.isfinite(rmax)
+    assert not np.all(np.isfinite(R[0, 7, :]))
+    assert not np.all(np.isfinite(R[0, :, 5]))
+    keep_r = np.ones(n, bool); keep_r[7] = False
+    keep_c = np.ones(L, bool); keep_c[5] = False
+    Th2, Tl2, X2 = Th.copy(), Tl.copy(), X.copy()
+    Th2[0, 7, 30] = 0
+    X2[0, 11, 5] = 0
+    ref, bound = _exact(Th2, Tl2, X2, V)
+    sub = np.ix_(keep_r, keep_c)
+    err = np.abs(R[0][sub].astype(np.clongdouble) - ref[0][sub]).astype(np.float64)
+    allowed = 1e-12 * bound[0][sub] + 2.0 ** -52 * np.abs(ref[0][sub]).astype(np.float64)
+    assert np.all(np.isfinite(R[0][sub]))
+    assert np.max(err / allowed) <= 1.0
