@@ -252,9 +252,10 @@ def main():
     h2d = 8 * 8 * N + 16 * N * (L_PROBES + (r_final if r_final != L_PROBES else 0))
     d2h = 2 * 16 * N * (L_PROBES + (r_final if r_final != L_PROBES else 0))
     hbm, bf16, peak_kind = _peaks()
-    # dominant kernel of the mixed step: the compensated refinement residual
-    # R = V - (hi + lo) X over all nodes; algorithmic work per launch = one complex
-    # GEMM, 8 N^2 L nq real flops (the compensation arithmetic is not counted).
+    # roofline kernel: the tensor-core refinement residual R = V - (hi + lo) X over
+    # all nodes (k_resid_tc). Algorithmic work per launch = one complex GEMM,
+    # 8 N^2 L nq real flops; the kernel issues 28 digit-pair bf16 products of
+    # that real-mapped GEMM (224 N^2 Lp nq flops, Lp = L rounded up to 32).
     res_ms, res_n = 0.0, 0
     for srun in stats:
         for s in srun:
@@ -262,12 +263,15 @@ def main():
             res_n += s["n_residual"]
     res_launch_ms = res_ms / max(res_n, 1)
     res_flops = 8.0 * N * N * L_PROBES * NQ
+    lp = ((L_PROBES + 31) // 32) * 32
+    res_issued = 224.0 * N * N * lp * NQ
     achieved = res_flops / (res_launch_ms * 1e-3) / 1e12
-    sm_mhz = clocks.get("sm_mhz") or 2070.0
-    fp32_core_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12  # FP32 CUDA-core FMA peak at the sampled clock
-    # DRAM traffic per launch: ncu capture of the same kernel on nq = 8 (644.5 MB read + 14.4 MB written,
-    # profiles/k_residual_df32_beyn_star_N2048.md), scaled by the units processed (48 / 8 contour nodes)
-    res_traffic = (644.5e6 + 14.4e6) * (NQ / 8.0)
+    issued_tflops = res_issued / (res_launch_ms * 1e-3) / 1e12
+    # DRAM traffic per launch: ncu capture of the same kernel at nq = 8, L = 64
+    # (1009.99 MB read + 16.34 MB written), scaled by the contour nodes (48 / 8);
+    # the algorithmic bytes (digit planes of T and X, V, R) are 1.03 GB at nq = 8
+    res_traffic = (1009.99e6 + 16.34e6) * (NQ / 8.0)
+    res_alg_bytes = (7 * N * 2 * N * 2 + 7 * 2 * lp * 2 * N * 2 + 2 * 16 * N * L_PROBES) * NQ
     lu_flops = NQ * (8.0 / 3.0) * N ** 3
     ms_factor = float(np.mean([s[0]["ms_factor"] for s in stats]))
     lu_achieved = lu_flops / (ms_factor * 1e-3) / 1e12
@@ -294,6 +298,7 @@ def main():
         "max_rel_err_vs_fp64": float(np.max(errs)),
         "phases_ms": {"assemble": st0["ms_assemble"], "factor": st0["ms_factor"],
                       "solve_refine": sum(s["ms_solve"] for s in stats[-1])},
+        "host_ms": {k: float("%.3g" % v) for k, v in info["host_ms"].items()},
         "refine_sweeps": [s["refine_sweeps"] for s in stats[-1]],
         "refine_history": [[float("%.3g" % v) for v in s["refine_history"]] for s in stats[-1]],
         "plain_phases_ms": {"assemble": info64["stats"][0]["ms_assemble"], "factor": info64["stats"][0]["ms_factor"],
@@ -302,12 +307,14 @@ def main():
         "e2e": {"value": n_eig / float(np.mean(e2e_times)), "unit": "eigenvalues/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
-                     "frac": achieved / bf16, "traffic": res_traffic,
-                     "kernel": "k_residual_df32 (compensated FP32 on CUDA cores)", "peak_kind": peak_kind,
-                     "launch_ms": res_launch_ms, "launches_per_step": res_n / max(len(stats), 1),
-                     "fp32_core_peak_tflops": fp32_core_peak, "frac_of_fp32_core_peak": achieved / fp32_core_peak,
-                     "note": "peak is the measured bf16 tensor figure the contract requires; the kernel runs on "
-                             "FP32 CUDA cores, so frac_of_fp32_core_peak is the meaningful ratio"},
+                     "frac": achieved / bf16, "traffic": res_traffic, "algorithmic_bytes": res_alg_bytes,
+                     "kernel": "k_resid_tc (exact 7-bit digit products on tcgen05, bf16 -> FP32 TMEM)",
+                     "peak_kind": peak_kind, "launch_ms": res_launch_ms,
+                     "launches_per_step": res_n / max(len(stats), 1),
+                     "issued_tflops": issued_tflops, "frac_issued": issued_tflops / bf16,
+                     "note": "achieved counts the complex GEMM's 8 N^2 L flops; the tensor pipe executes 28 "
+                             "digit-pair products of it, whose rate is issued_tflops (frac_issued of the "
+                             "measured bf16 peak)"},
         "lu_phase": {"achieved_tflops": lu_achieved, "ms": ms_factor, "flops": lu_flops,
                      "engine": "FP32 panels on CUDA cores; trailing updates and solves on tcgen05 (3xTF32)"},
         "clocks": clocks,

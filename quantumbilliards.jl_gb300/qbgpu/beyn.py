@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import time
 import warnings
 from dataclasses import dataclass, field
 
@@ -178,20 +179,28 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
     ws = ws if ws is not None else Workspace(solver, pts)
     if ws.dim != N:
         raise ValueError(f"N={N} does not match the operator dimension {ws.dim}")
+    clk = time.perf_counter
+    host = dict(create=0.0, moments=0.0, svd=0.0, B=0.0)  # wall-clock ms of the host-visible phases
+    t = clk()
     bh = BeynHandle(ws, k0, R, nq, mixed, max_refine, refine_tol, use_chebyshev=use_chebyshev, cheb=cheb,
                     fp32_sweeps=fp32_sweeps, solve_block=solve_block, node_chunk=node_chunk,
                     resid_engine=resid_engine)
-    info = dict(stats=[])
+    host["create"] += (clk() - t) * 1e3
+    info = dict(stats=[], host_ms=host)
     try:
         V = probe_matrix(N, r, rng)
+        t = clk()
         A0, A1 = bh.moments(V)
+        host["moments"] += (clk() - t) * 1e3
         info["stats"].append(bh.last_stats)
         # the saturation test needs only the singular values; the factors are
         # computed once, for the block that is finally used
+        t = clk()
         S = np.linalg.svd(A0, compute_uv=False)
         rk = int(np.count_nonzero(S >= svd_tol))
         if not (rk == r and 2 * r < N) and rk > 0:
             U, S, Wh = np.linalg.svd(A0, full_matrices=False)
+        host["svd"] += (clk() - t) * 1e3
         rused = r
         if rk == 0:
             out = (np.zeros((0, 0), complex), np.zeros((N, 0), complex))
@@ -200,6 +209,7 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
         if rk == r:
             r_tmp = 2 * r
             if r_tmp < N:
+                t = clk()
                 if regrow == "extend":
                     Vn = probe_matrix(N, r_tmp - r, rng)
                     A0n, A1n = bh.moments(Vn)
@@ -208,16 +218,23 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
                 else:
                     V = probe_matrix(N, r_tmp, rng)
                     A0, A1 = bh.moments(V)
+                host["moments"] += (clk() - t) * 1e3
                 info["stats"].append(bh.last_stats)
+                t = clk()
                 U, S, Wh = np.linalg.svd(A0, full_matrices=False)
                 rk = int(np.count_nonzero(S >= svd_tol))
+                host["svd"] += (clk() - t) * 1e3
                 rused = r_tmp
     finally:
+        t = clk()
         bh.close()
+        host["create"] += (clk() - t) * 1e3
+    t = clk()
     Uk = U[:, :rk]
     Wk = Wh.conj().T[:, :rk]
     tmp = (A1 @ Wk) / S[:rk][None, :]
     B = Uk.conj().T @ tmp
+    host["B"] += (clk() - t) * 1e3
     info.update(rk=rk, r=rused, S=S)
     return (B, Uk, info) if return_info else (B, Uk)
 
@@ -242,7 +259,9 @@ def solve(solver, pts, k0, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed=False,
         ws = Workspace(solver, pts)
     B, Uk, info = construct_B_matrix(solver, pts, ws.dim, k0, R, nq, r, svd_tol, rng, mixed, ws, return_info=True,
                                      **kw)
+    t = time.perf_counter()
     lam = np.zeros(0, complex) if B.size == 0 else np.linalg.eigvals(B)
+    info["host_ms"]["eigvals"] = (time.perf_counter() - t) * 1e3
     return (lam, info) if return_info else lam
 
 
