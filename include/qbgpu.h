@@ -217,6 +217,17 @@ qbg_status qbg_beyn_create_disks(qbg_geom* g, const double* k0s, const double* R
 /* A0 and A1 hold one N x L block per disk (disk d at offset d * N * L). */
 qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0, double* A1,
                             qbg_beyn_stats* stats);
+/* The moments of V reduced on the device for B = U_k^H A1 W_k Sigma_k^-1
+ * (construct_B_matrix, beyn.jl:286-320): the handle keeps every disk's A0 and
+ * A1 columns (append = 0 replaces them with this call's L columns, append = 1
+ * puts them behind the columns kept so far, the reference's r -> 2r regrowth,
+ * beyn.jl:291-309), takes the thin QR A0 = Q R of the m kept columns and
+ * returns R (m x m upper triangular) and C = Q^H A1 (m x m), column-major,
+ * disk d at offset d * m * m. With R = U_R S W^H the SVD of A0 is
+ * (Q U_R) S W^H, so B = U_R,k^H C W_k S_k^-1 on the host from m x m data.
+ * m must equal the column count after this call. */
+qbg_status qbg_beyn_moments_qr(qbg_beyn* b, const double* V, int64_t L, int32_t append, int64_t m, double* R,
+                               double* C, qbg_beyn_stats* stats);
 qbg_status qbg_beyn_destroy(qbg_beyn* b);
 
 /* Smallest singular value of A(k) for nk real wavenumbers (the :svd branch of
@@ -334,6 +345,18 @@ qbg_status qbg_set_gemm_engine(int32_t engine);
 /* Number of CUDA kernels this library has launched in the process so far
  * (diagnostic; no reference counterpart). */
 qbg_status qbg_launch_count(uint64_t* count);
+
+/* Device memory cache. Every library buffer comes from a caching allocator:
+ * freed blocks are kept for later requests of the same size class (reuse
+ * waits for the stream work that last used a block), up to QBG_POOL_BYTES
+ * bytes (environment; default a quarter of device memory; 0 disables it).
+ * qbg_pool_release returns every cached block to the driver (for callers that
+ * share the device with another allocator); qbg_pool_stats reports the cached
+ * and live bytes and the reuse hits / driver allocations so far (any pointer
+ * may be NULL). No reference counterpart (Julia's GC owns the reference's
+ * host arrays). */
+qbg_status qbg_pool_release(void);
+qbg_status qbg_pool_stats(uint64_t* cached_bytes, uint64_t* live_bytes, uint64_t* hits, uint64_t* misses);
 
 #ifdef __cplusplus
 }

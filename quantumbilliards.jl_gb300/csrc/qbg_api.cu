@@ -284,11 +284,11 @@ static int assemble_impl(qbg_geom* g, const double* ks, int64_t nk, int32_t deri
   char* stage = nullptr;
   int s = QBG_OK;
   if ((s = dmalloc(&dks, sizeof(cxd) * nk))) return s;
-  if ((s = dmalloc(&dptrs, sizeof(void*) * chunk * nout))) { cudaFree(dks); return s; }
-  if (!dev && (s = dmalloc(&stage, mat_bytes * chunk * nout))) { cudaFree(dks); cudaFree(dptrs); return s; }
+  if ((s = dmalloc(&dptrs, sizeof(void*) * chunk * nout))) { dfree(dks); return s; }
+  if (!dev && (s = dmalloc(&stage, mat_bytes * chunk * nout))) { dfree(dks); dfree(dptrs); return s; }
   cudaStream_t st = g->stream;
   std::vector<void*> hp(chunk * nout);
-  auto cleanup = [&]() { cudaFree(dks); cudaFree(dptrs); if (stage) cudaFree(stage); };
+  auto cleanup = [&]() { dfree(dks); dfree(dptrs); if (stage) dfree(stage); };
   cudaError_t e = cudaMemcpyAsync(dks, ks, sizeof(cxd) * nk, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) { cleanup(); return cuda_status(e, "qbg_assemble H2D"); }
   for (int64_t k0 = 0; k0 < nk; k0 += chunk) {
@@ -304,7 +304,7 @@ static int assemble_impl(qbg_geom* g, const double* ks, int64_t nk, int32_t deri
       s = make_cheb(g, dks + k0, (int)c, *cheb, t, ctmp, st);
       if (!s) s = launch_assemble_cheb(g->d, t, dks + k0, (int)c, deriv, prec, dptrs, nullptr, dim, st);
       cudaError_t e2 = cudaStreamSynchronize(st);
-      for (void* p : ctmp) cudaFree(p);
+      for (void* p : ctmp) dfree(p);
       if (!s && e2 != cudaSuccess) s = cuda_status(e2, "qbg_assemble_cheb");
     } else {
       s = launch_assemble(g->d, dks + k0, (int)c, deriv, prec, dptrs, dim, st);
@@ -360,7 +360,7 @@ qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig)
   cusolverDnHandle_t h = nullptr;
   std::vector<void*> tmp;
   auto cleanup = [&]() {
-    for (void* p : tmp) cudaFree(p);
+    for (void* p : tmp) dfree(p);
     if (h) cusolverDnDestroy(h);
   };
   auto talloc = [&](void** p, size_t bytes) {
@@ -423,7 +423,7 @@ qbg_status qbg_cheb_autotune(qbg_geom* g, const double* ks, int64_t nk, double t
   unsigned long long* derr = nullptr;
   QBG_TRY(dmalloc(&dks, sizeof(cxd) * nk));
   int s = dmalloc(&derr, sizeof(unsigned long long) * 4 * nk);
-  if (s) { cudaFree(dks); return s; }
+  if (s) { dfree(dks); return s; }
   std::vector<unsigned long long> herr(4 * nk);
   double worst[4] = {0, 0, 0, 0};
   cudaError_t e = cudaMemcpyAsync(dks, ks, sizeof(cxd) * nk, cudaMemcpyHostToDevice, st);
@@ -437,7 +437,7 @@ qbg_status qbg_cheb_autotune(qbg_geom* g, const double* ks, int64_t nk, double t
     if (!s && e == cudaSuccess)
       e = cudaMemcpyAsync(herr.data(), derr, sizeof(unsigned long long) * 4 * nk, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    for (void* q : ctmp) cudaFree(q);
+    for (void* q : ctmp) dfree(q);
     if (s || e != cudaSuccess) break;
     for (int f = 0; f < 4; ++f) worst[f] = 0.0;
     for (int64_t q = 0; q < nk; ++q)
@@ -457,8 +457,8 @@ qbg_status qbg_cheb_autotune(qbg_geom* g, const double* ks, int64_t nk, double t
     if (!okJ) grow(p.n_panels_j, p.M_j);
     if (p.n_panels_h > (1 << 24) || p.n_panels_j > (1 << 24)) break;
   }
-  cudaFree(dks);
-  cudaFree(derr);
+  dfree(dks);
+  dfree(derr);
   if (s) return s;
   if (e != cudaSuccess) return cuda_status(e, "qbg_cheb_autotune");
   *io = p;
@@ -494,7 +494,7 @@ qbg_status qbg_candidate_residuals(qbg_geom* g, const double* lambdas, int64_t n
   double *nrm = nullptr, *an = nullptr;
   void** dptrs = nullptr;
   std::vector<void*> tmp;
-  auto cleanup = [&]() { for (void* p : tmp) cudaFree(p); };
+  auto cleanup = [&]() { for (void* p : tmp) dfree(p); };
   auto talloc = [&](auto** p, size_t bytes) {
     int s = dmalloc(p, bytes);
     if (!s) tmp.push_back(*p);
@@ -533,7 +533,7 @@ qbg_status qbg_candidate_residuals(qbg_geom* g, const double* lambdas, int64_t n
     if (!s && e == cudaSuccess) e = cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * 4 * c, cudaMemcpyDeviceToHost, st);
     if (!s && e == cudaSuccess) e = cudaMemcpyAsync(ha.data(), an, sizeof(double) * c, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    for (void* p : ctmp) cudaFree(p);
+    for (void* p : ctmp) dfree(p);
     if (s || e != cudaSuccess) break;
     for (int q = 0; q < c; ++q) {
       double* o = out + 5 * (q0 + q);
@@ -555,14 +555,14 @@ qbg_status qbg_bessel01(const double* z, int64_t n, int32_t f32, double* out) {
   cxd *dz = nullptr, *dout = nullptr;
   int s = dmalloc(&dz, sizeof(cxd) * n);
   if (s) return s;
-  if ((s = dmalloc(&dout, sizeof(cxd) * 4 * n))) { cudaFree(dz); return s; }
+  if ((s = dmalloc(&dout, sizeof(cxd) * 4 * n))) { dfree(dz); return s; }
   cudaError_t e = cudaMemcpy(dz, z, sizeof(cxd) * n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) {
     s = launch_bessel_eval(dz, (int)n, dout, f32, 0);
     if (!s) e = cudaMemcpy(out, dout, sizeof(cxd) * 4 * n, cudaMemcpyDeviceToHost);
   }
-  cudaFree(dz);
-  cudaFree(dout);
+  dfree(dz);
+  dfree(dout);
   if (s) return s;
   if (e != cudaSuccess) return cuda_status(e, "qbg_bessel01");
   return QBG_OK;
@@ -596,9 +596,9 @@ qbg_status qbg_cgemm_c64(int32_t engine, int32_t M, int32_t N, int32_t K, const 
     if (!s && engine == GEMM_ENGINE_TCGEN05) s = tc_check(0);
     if (!s) e = cudaMemcpy(C, dC, sizeof(cxf) * sC * batch, cudaMemcpyDeviceToHost);
   }
-  cudaFree(dA);
-  cudaFree(dB);
-  cudaFree(dC);
+  dfree(dA);
+  dfree(dB);
+  dfree(dC);
   if (s) return s;
   if (e != cudaSuccess) return cuda_status(e, "qbg_cgemm_c64");
   return QBG_OK;
@@ -619,7 +619,7 @@ qbg_status qbg_residual_c64(int32_t engine, int32_t n, int32_t L, int32_t batch,
   }
   const size_t nn = (size_t)n * n, nl = (size_t)n * L;
   std::vector<void*> tmp;
-  auto cleanup = [&]() { for (void* p : tmp) cudaFree(p); };
+  auto cleanup = [&]() { for (void* p : tmp) dfree(p); };
   auto talloc = [&](auto** p, size_t bytes) {
     int s = dmalloc(p, bytes);
     if (!s) tmp.push_back(*p);

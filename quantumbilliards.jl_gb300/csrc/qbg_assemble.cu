@@ -24,6 +24,7 @@
 
 #include <vector>
 #include "qbg_assemble.cuh"
+#include "qbg_handles.cuh"
 #include "qbg_bessel.cuh"
 
 namespace qbg {
@@ -542,12 +543,11 @@ static int launch_alpert(const GeomDev& g, const cxd* ks, int nk, int deriv, int
   const long long count = (long long)g.n * ld;
   cxd* stage = nullptr;
   cxd** dp = nullptr;
-  QBG_CUDA(cudaMalloc(&stage, sizeof(cxd) * (size_t)count * grp));
-  cudaError_t e = cudaMalloc(&dp, sizeof(cxd*) * grp);
-  if (e != cudaSuccess) { cudaFree(stage); return cuda_status(e, "cudaMalloc"); }
+  QBG_TRY(dmalloc(&stage, sizeof(cxd) * (size_t)count * grp));
+  if (int sa = dmalloc(&dp, sizeof(cxd*) * grp)) { dfree(stage, st); return sa; }
   std::vector<cxd*> hp(grp);
   for (int q = 0; q < grp; ++q) hp[q] = stage + (size_t)q * count;
-  e = cudaMemcpyAsync(dp, hp.data(), sizeof(cxd*) * grp, cudaMemcpyHostToDevice, st);
+  cudaError_t e = cudaMemcpyAsync(dp, hp.data(), sizeof(cxd*) * grp, cudaMemcpyHostToDevice, st);
   int s = e == cudaSuccess ? QBG_OK : cuda_status(e, "Alpert staging pointers");
   for (int q0 = 0; !s && q0 < nk; q0 += grp) {
     const int c = nk - q0 < grp ? nk - q0 : grp;
@@ -560,8 +560,8 @@ static int launch_alpert(const GeomDev& g, const cxd* ks, int nk, int deriv, int
     }
   }
   e = cudaStreamSynchronize(st);  // the staging buffers are freed below
-  cudaFree(stage);
-  cudaFree(dp);
+  dfree(stage, st);
+  dfree(dp, st);
   if (s) return s;
   if (e != cudaSuccess) return cuda_status(e, "Alpert assembly");
   return QBG_OK;

@@ -10,6 +10,7 @@
 // nodes through them in groups (assemble, factor, solve, accumulate), which
 // bounds the memory at large N at the price of re-assembling per call.
 #include <algorithm>
+#include <cusolverDn.h>
 #include <limits>
 #include <cmath>
 #include <cstdio>
@@ -49,10 +50,17 @@ struct qbg_beyn {
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   double ms_assemble = 0, ms_factor = 0;  // device time of the last load(s)
   int singular = 0;
+  // moment blocks kept on the device for qbg_beyn_moments_qr: per disk N x mcap,
+  // column-major, the first mcols columns filled
+  cxd* macc0 = nullptr;
+  cxd* macc1 = nullptr;
+  int mcap = 0, mcols = 0;
   std::mutex mu;
   ~qbg_beyn() {
     if (st) cudaStreamSynchronize(st);
-    for (void* p : allocs) cudaFree(p);
+    for (void* p : allocs) dfree(p, st);
+    dfree(macc0, st);
+    dfree(macc1, st);
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     if (st) cudaStreamDestroy(st);
@@ -173,7 +181,7 @@ int load(qbg_beyn* b, int n0, int c) {
       cudaError_t e = cudaStreamSynchronize(st);  // the tables are freed below
       if (e != cudaSuccess) s = cuda_status(e, "Chebyshev assembly");
     }
-    for (void* p : ctmp) cudaFree(p);
+    for (void* p : ctmp) dfree(p, st);
     if (s) return s;
   } else {
     QBG_TRY(launch_assemble(b->g->d, b->zj + n0, c, 0, b->prec, b->dptrs, n, st, b->dlo));
@@ -234,7 +242,7 @@ struct Call {
   double hist[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   double f32hist[4] = {0, 0, 0, 0};
   ~Call() {
-    for (void* p : tmp) cudaFree(p);
+    for (void* p : tmp) dfree(p, b ? b->st : nullptr);
     for (cudaEvent_t e : sev) cudaEventDestroy(e);
   }
   template <class P>
@@ -435,13 +443,39 @@ qbg_status qbg_beyn_create_disks(qbg_geom* g, const double* k0s, const double* R
   return create_impl(g, k0s, Rs, ndisk, nq, prec, opts, out);
 }
 
-qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0, double* A1,
-                            qbg_beyn_stats* stats) {
-  if (!b || !V || !A0 || !A1 || L < 1 || L > (1 << 20)) {
-    set_error("qbg_beyn_moments: invalid arguments");
-    return QBG_EINVAL;
+}  // extern "C"
+
+namespace {
+
+// grows the kept moment blocks to at least m columns per disk (existing columns copied)
+int ensure_moment_blocks(qbg_beyn* b, int m) {
+  if (m <= b->mcap) return QBG_OK;
+  const size_t n = (size_t)b->n;
+  const int cap = std::max(m, 2 * b->mcap);
+  cxd *a0 = nullptr, *a1 = nullptr;
+  QBG_TRY(dmalloc(&a0, sizeof(cxd) * n * cap * b->ndisk));
+  if (int s = dmalloc(&a1, sizeof(cxd) * n * cap * b->ndisk)) {
+    dfree(a0, b->st);
+    return s;
   }
-  std::lock_guard<std::mutex> lk(b->mu);
+  for (int d = 0; d < b->ndisk && b->mcols > 0; ++d) {
+    QBG_CUDA(cudaMemcpyAsync(a0 + d * n * cap, b->macc0 + d * n * b->mcap, sizeof(cxd) * n * b->mcols,
+                             cudaMemcpyDeviceToDevice, b->st));
+    QBG_CUDA(cudaMemcpyAsync(a1 + d * n * cap, b->macc1 + d * n * b->mcap, sizeof(cxd) * n * b->mcols,
+                             cudaMemcpyDeviceToDevice, b->st));
+  }
+  dfree(b->macc0, b->st);
+  dfree(b->macc1, b->st);
+  b->macc0 = a0;
+  b->macc1 = a1;
+  b->mcap = cap;
+  return QBG_OK;
+}
+
+// moments of V. A0/A1: outputs (host, or device with QBG_PTR_DEVICE), or both
+// NULL; keep >= 0 also stores the moments in the kept blocks (0: replacing
+// them, 1: behind the columns kept so far)
+int moments_impl(qbg_beyn* b, const double* V, int64_t L, double* A0, double* A1, qbg_beyn_stats* stats, int keep) {
   const int n = b->n;
   const bool dev = (b->opts.flags & QBG_PTR_DEVICE) != 0;
   cudaStream_t st = b->st;
@@ -452,15 +486,19 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
   const size_t nl = c.nl, nA = nl * b->ndisk;
   c.per_disk = (b->opts.flags & QBG_V_PER_DISK) != 0 && b->ndisk > 1;
   const size_t nV = c.per_disk ? nA : nl;
+  const bool out = A0 && A1;
   if (dev) {
     c.dV = (cxd*)V;
+  } else {
+    QBG_TRY(c.talloc(&c.dV, sizeof(cxd) * nV));
+    QBG_CUDA(cudaMemcpyAsync(c.dV, V, sizeof(cxd) * nV, cudaMemcpyHostToDevice, st));
+  }
+  if (dev && out) {
     c.dA0 = (cxd*)A0;
     c.dA1 = (cxd*)A1;
   } else {
-    QBG_TRY(c.talloc(&c.dV, sizeof(cxd) * nV));
     QBG_TRY(c.talloc(&c.dA0, sizeof(cxd) * nA));
     QBG_TRY(c.talloc(&c.dA1, sizeof(cxd) * nA));
-    QBG_CUDA(cudaMemcpyAsync(c.dV, V, sizeof(cxd) * nV, cudaMemcpyHostToDevice, st));
   }
   QBG_CUDA(cudaMemsetAsync(c.dA0, 0, sizeof(cxd) * nA, st));
   QBG_CUDA(cudaMemsetAsync(c.dA1, 0, sizeof(cxd) * nA, st));
@@ -511,7 +549,20 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
       QBG_TRY(solve_and_accumulate(c));
     }
   }
-  if (!dev) {
+  if (keep >= 0) {
+    const int off = keep ? b->mcols : 0;
+    if (!keep) b->mcols = 0;
+    QBG_TRY(ensure_moment_blocks(b, off + (int)L));
+    const size_t nn_ = (size_t)n;
+    for (int d = 0; d < b->ndisk; ++d) {
+      QBG_CUDA(cudaMemcpyAsync(b->macc0 + d * nn_ * b->mcap + (size_t)off * nn_, c.dA0 + d * nl, sizeof(cxd) * nl,
+                               cudaMemcpyDeviceToDevice, st));
+      QBG_CUDA(cudaMemcpyAsync(b->macc1 + d * nn_ * b->mcap + (size_t)off * nn_, c.dA1 + d * nl, sizeof(cxd) * nl,
+                               cudaMemcpyDeviceToDevice, st));
+    }
+    b->mcols = off + (int)L;
+  }
+  if (!dev && out) {
     QBG_CUDA(cudaMemcpyAsync(A0, c.dA0, sizeof(cxd) * nA, cudaMemcpyDeviceToHost, st));
     QBG_CUDA(cudaMemcpyAsync(A1, c.dA1, sizeof(cxd) * nA, cudaMemcpyDeviceToHost, st));
   }
@@ -546,6 +597,141 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
     stats->n_solves = (int)c.sev.size() / 2;
   }
   return QBG_OK;
+}
+
+// thin Householder QR of every disk's kept A0 block (N x m) on the device:
+// R (m x m, upper triangular) and C = Q^H A1 (m x m) to the host, column-major per disk
+std::mutex g_qr_mu;
+cusolverDnHandle_t g_qr_h[64] = {};
+
+int qr_reduce(qbg_beyn* b, double* Rh, double* Ch) {
+  const int n = b->n, m = b->mcols;
+  cudaStream_t st = b->st;
+  int dev = 0;
+  QBG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    set_error("qr_reduce: device index %d", dev);
+    return QBG_EINVAL;
+  }
+  std::lock_guard<std::mutex> lk(g_qr_mu);
+  cusolverDnHandle_t& h = g_qr_h[dev];
+  if (!h && cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) {
+    h = nullptr;
+    set_error("cusolverDnCreate failed");
+    return QBG_ECUDA;
+  }
+  if (cusolverDnSetStream(h, st) != CUSOLVER_STATUS_SUCCESS) {
+    set_error("cusolverDnSetStream failed");
+    return QBG_ECUDA;
+  }
+  std::vector<void*> tmp;
+  auto cleanup = [&]() { for (void* p : tmp) dfree(p, st); };
+  cuDoubleComplex *w0 = nullptr, *w1 = nullptr, *tau = nullptr, *work = nullptr;
+  int* info = nullptr;
+  auto get = [&](auto** p, size_t bytes) {
+    int s = dmalloc(p, bytes);
+    if (!s) tmp.push_back(*p);
+    return s;
+  };
+  int s = QBG_OK;
+  if ((s = get(&w0, sizeof(cxd) * (size_t)n * m)) || (s = get(&w1, sizeof(cxd) * (size_t)n * m)) ||
+      (s = get(&tau, sizeof(cxd) * (size_t)m)) || (s = get(&info, sizeof(int) * b->ndisk))) {
+    cleanup();
+    return s;
+  }
+  int l1 = 0, l2 = 0;
+  if (cusolverDnZgeqrf_bufferSize(h, n, m, w0, n, &l1) != CUSOLVER_STATUS_SUCCESS ||
+      cusolverDnZunmqr_bufferSize(h, CUBLAS_SIDE_LEFT, CUBLAS_OP_C, n, m, m, w0, n, tau, w1, n, &l2) !=
+          CUSOLVER_STATUS_SUCCESS) {
+    cleanup();
+    set_error("cuSOLVER workspace query failed");
+    return QBG_ECUDA;
+  }
+  const int lw = std::max(std::max(l1, l2), 1);
+  if ((s = get(&work, sizeof(cxd) * (size_t)lw))) {
+    cleanup();
+    return s;
+  }
+  const size_t nn_ = (size_t)n, mm = (size_t)m * m;
+  for (int d = 0; d < b->ndisk && !s; ++d) {
+    cudaError_t e = cudaMemcpyAsync(w0, b->macc0 + d * nn_ * b->mcap, sizeof(cxd) * nn_ * m,
+                                    cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(w1, b->macc1 + d * nn_ * b->mcap, sizeof(cxd) * nn_ * m, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) {
+      s = cuda_status(e, "qr_reduce copy");
+      break;
+    }
+    if (cusolverDnZgeqrf(h, n, m, w0, n, tau, work, lw, info + d) != CUSOLVER_STATUS_SUCCESS ||
+        cusolverDnZunmqr(h, CUBLAS_SIDE_LEFT, CUBLAS_OP_C, n, m, m, w0, n, tau, w1, n, work, lw, info + d) !=
+            CUSOLVER_STATUS_SUCCESS) {
+      set_error("cusolverDnZgeqrf / Zunmqr failed");
+      s = QBG_ECUDA;
+      break;
+    }
+    e = cudaMemcpy2DAsync(Rh + 2 * d * mm, sizeof(cxd) * m, w0, sizeof(cxd) * nn_, sizeof(cxd) * m, m,
+                          cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(Ch + 2 * d * mm, sizeof(cxd) * m, w1, sizeof(cxd) * nn_, sizeof(cxd) * m, m,
+                            cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) s = cuda_status(e, "qr_reduce D2H");
+  }
+  std::vector<int> hinfo(b->ndisk, 0);
+  if (!s) {
+    cudaError_t e = cudaMemcpyAsync(hinfo.data(), info, sizeof(int) * b->ndisk, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) s = cuda_status(e, "qr_reduce");
+  }
+  cleanup();
+  if (s) return s;
+  for (int d = 0; d < b->ndisk; ++d)
+    if (hinfo[d] < 0) {
+      set_error("cusolverDnZgeqrf: argument %d invalid", -hinfo[d]);
+      return QBG_ECUDA;
+    }
+  // R is the upper triangle; below it geqrf left the Householder vectors
+  for (int d = 0; d < b->ndisk; ++d)
+    for (int j = 0; j < m; ++j)
+      for (int i = j + 1; i < m; ++i) {
+        Rh[2 * (d * mm + (size_t)j * m + i)] = 0.0;
+        Rh[2 * (d * mm + (size_t)j * m + i) + 1] = 0.0;
+      }
+  return QBG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0, double* A1,
+                            qbg_beyn_stats* stats) {
+  if (!b || !V || !A0 || !A1 || L < 1 || L > (1 << 20)) {
+    set_error("qbg_beyn_moments: invalid arguments");
+    return QBG_EINVAL;
+  }
+  std::lock_guard<std::mutex> lk(b->mu);
+  return moments_impl(b, V, L, A0, A1, stats, -1);
+}
+
+qbg_status qbg_beyn_moments_qr(qbg_beyn* b, const double* V, int64_t L, int32_t append, int64_t m, double* R,
+                               double* C, qbg_beyn_stats* stats) {
+  if (!b || !V || !R || !C || L < 1 || L > (1 << 20)) {
+    set_error("qbg_beyn_moments_qr: invalid arguments");
+    return QBG_EINVAL;
+  }
+  std::lock_guard<std::mutex> lk(b->mu);
+  const int64_t want = (append ? b->mcols : 0) + L;
+  if (m != want) {
+    set_error("qbg_beyn_moments_qr: m = %lld, the kept blocks will hold %lld columns", (long long)m,
+              (long long)want);
+    return QBG_EINVAL;
+  }
+  if (m > b->n) {
+    set_error("qbg_beyn_moments_qr: %lld columns exceed the dimension %d", (long long)m, b->n);
+    return QBG_EINVAL;
+  }
+  QBG_TRY(moments_impl(b, V, L, nullptr, nullptr, stats, append ? 1 : 0));
+  return qr_reduce(b, R, C);
 }
 
 qbg_status qbg_beyn_destroy(qbg_beyn* b) {

@@ -8,15 +8,20 @@
 #include "qbg_assemble.cuh"
 
 namespace qbg {
+// caching allocator (qbg_pool.cu)
+int pool_alloc(void** p, size_t bytes);
+// st: the stream whose work last used p (its completion gates reuse);
+// nullptr waits for the whole device before the block is cached
+void pool_free(void* p, cudaStream_t st);
+
 template <class P>
 inline int dmalloc(P** p, size_t bytes) {
-  cudaError_t e = cudaMalloc((void**)p, bytes ? bytes : 1);
-  if (e != cudaSuccess) {
-    *p = nullptr;
-    return cuda_status(e, "cudaMalloc");
-  }
-  return QBG_OK;
+  void* q = nullptr;
+  const int s = pool_alloc(&q, bytes);
+  *p = static_cast<P*>(q);
+  return s;
 }
+inline void dfree(void* p, cudaStream_t st = nullptr) { pool_free(p, st); }
 }  // namespace qbg
 
 struct qbg_geom {
@@ -26,7 +31,7 @@ struct qbg_geom {
   cudaStream_t stream = nullptr;
   std::mutex mu;
   ~qbg_geom() {
-    for (void* p : allocs) cudaFree(p);
+    for (void* p : allocs) qbg::dfree(p, stream);
     if (stream) cudaStreamDestroy(stream);
   }
   template <class P>

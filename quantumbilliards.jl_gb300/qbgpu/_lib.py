@@ -110,6 +110,8 @@ _SIGS = {
                                     C.POINTER(BeynOpts), C.POINTER(C.c_void_p)]),
     "qbg_beyn_moments": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                                      C.POINTER(BeynStats)]),
+    "qbg_beyn_moments_qr": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int64, C.c_void_p,
+                                        C.c_void_p, C.POINTER(BeynStats)]),
     "qbg_beyn_destroy": (C.c_int32, [C.c_void_p]),
     "qbg_sigma_min": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]),
     "qbg_bessel01": (C.c_int32, [C.POINTER(C.c_double), C.c_int64, C.c_int32, C.POINTER(C.c_double)]),
@@ -125,6 +127,8 @@ _SIGS = {
     "qbg_serve_wait": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double, C.POINTER(RequestResult)]),
     "qbg_serve_destroy": (C.c_int32, [C.c_void_p]),
     "qbg_launch_count": (C.c_int32, [C.POINTER(C.c_uint64)]),
+    "qbg_pool_release": (C.c_int32, []),
+    "qbg_pool_stats": (C.c_int32, [C.POINTER(C.c_uint64)] * 4),
     "qbg_candidate_residuals": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.c_void_p,
                                             C.POINTER(ChebParams), C.POINTER(C.c_double)]),
     "qbg_cheb_autotune": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.c_double, C.c_int32,

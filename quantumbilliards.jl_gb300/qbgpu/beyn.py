@@ -72,6 +72,7 @@ class BeynHandle:
         self._h = h
         self.N = ws.dim
         self.last_stats = None
+        self._m = None
 
     def moments(self, V: np.ndarray):
         lib = L.load()
@@ -84,21 +85,51 @@ class BeynHandle:
         A1 = np.empty((self.ndisk, r, N), dtype=np.complex128)
         st = L.BeynStats()
         L.check(lib.qbg_beyn_moments(self._h, L.vptr(V), r, L.vptr(A0), L.vptr(A1), C.byref(st)))
+        self._take_stats(st)
+        self._m = None  # the kept device blocks are not touched by this call
+        A0 = A0.transpose(0, 2, 1)
+        A1 = A1.transpose(0, 2, 1)
+        if self.multi:
+            return A0, A1
+        return np.asfortranarray(A0[0]), np.asfortranarray(A1[0])
+
+    def _take_stats(self, st):
         if self.prec != L.QBG_PREC_FP64 and st.nhist and not st.refine_residual <= self.refine_tol:
             warnings.warn(f"qbgpu: mixed refinement stopped at relative residual {st.refine_residual:.2e} > "
                           f"refine_tol {self.refine_tol:.1e} (history {list(st.refine_history[:st.nhist])}); "
-                          "the moments are less accurate than requested", RuntimeWarning, stacklevel=2)
+                          "the moments are less accurate than requested", RuntimeWarning, stacklevel=3)
         self.last_stats = dict(refine_sweeps=st.refine_sweeps, refine_residual=st.refine_residual,
                                singular=st.singular, ms_assemble=st.ms_assemble, ms_factor=st.ms_factor,
                                ms_solve=st.ms_solve, refine_history=list(st.refine_history[:st.nhist]),
                                ms_residual=st.ms_residual, n_residual=st.n_residual,
                                fp32_history=list(st.fp32_history[:st.nfp32]), ms_solves=st.ms_solves,
                                n_solves=st.n_solves)
-        A0 = A0.transpose(0, 2, 1)
-        A1 = A1.transpose(0, 2, 1)
+
+    def moments_qr(self, V: np.ndarray, append: bool = False):
+        """Moments of V kept on the device and reduced there: returns (R, C)
+        with A0 = Q R (thin QR of all kept columns) and C = Q^H A1, each m x m
+        (per disk for a multi-disk handle). append=True keeps the columns of
+        the previous moments_qr call in front of this call's."""
+        lib = L.load()
+        V = np.asfortranarray(V, dtype=np.complex128)
+        N, r = V.shape
+        if N != self.N:
+            raise ValueError(f"V has {N} rows, the operator has {self.N}")
+        if append and not self._m:
+            raise ValueError("append needs an earlier moments_qr call on this handle")
+        m = (self._m if append else 0) + r
+        Rm = np.empty((self.ndisk, m, m), dtype=np.complex128)
+        Cm = np.empty((self.ndisk, m, m), dtype=np.complex128)
+        st = L.BeynStats()
+        L.check(lib.qbg_beyn_moments_qr(self._h, L.vptr(V), r, int(bool(append)), m, L.vptr(Rm), L.vptr(Cm),
+                                        C.byref(st)))
+        self._take_stats(st)
+        self._m = m
+        Rm = Rm.transpose(0, 2, 1)
+        Cm = Cm.transpose(0, 2, 1)
         if self.multi:
-            return A0, A1
-        return np.asfortranarray(A0[0]), np.asfortranarray(A1[0])
+            return Rm, Cm
+        return np.asfortranarray(Rm[0]), np.asfortranarray(Cm[0])
 
     def close(self):
         if getattr(self, "_h", None) and L.alive():
@@ -113,7 +144,8 @@ class BeynHandle:
 
 
 def _B_from_moments(A0, A1, svd_tol):
-    """Thin SVD of A0, absolute rank, B = U_k^H A1 W_k Sigma_k^-1 (beyn.jl:286-320)."""
+    """Thin SVD of A0, absolute rank, B = U_k^H A1 W_k Sigma_k^-1 (beyn.jl:286-320).
+    Also takes (R, Q^H A1) of a device QR A0 = Q R: same S, W and B, U_R for U."""
     U, S, Wh = np.linalg.svd(A0, full_matrices=False)
     rk = int(np.count_nonzero(S >= svd_tol))
     Uk = U[:, :rk]
@@ -134,47 +166,51 @@ def solve_disks(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed
     k0s = np.atleast_1d(np.asarray(k0s, dtype=np.complex128))
     bh = BeynHandle(ws, k0s, R, nq, mixed, **kw)
     info = dict(stats=[], rk=[], r=[])
+    # moments reduced on the device: per disk R (A0 = Q R) and Q^H A1, m x m
     try:
         V = probe_matrix(N, r, rng)
-        A0s, A1s = bh.moments(V)
+        R1, C1 = bh.moments_qr(V)
         info["stats"].append(bh.last_stats)
-        S = [np.linalg.svd(a, compute_uv=False) for a in A0s]
+        S = [np.linalg.svd(a, compute_uv=False) for a in R1]
         rks = [int(np.count_nonzero(s >= svd_tol)) for s in S]
         grow = [rk == r and 2 * r < N for rk in rks]
         if any(grow):
             Vn = probe_matrix(N, r, rng)
-            A0n, A1n = bh.moments(Vn)
+            R2, C2 = bh.moments_qr(Vn, append=True)
             info["stats"].append(bh.last_stats)
     finally:
         bh.close()
     out = []
     for d in range(len(k0s)):
-        A0, A1 = A0s[d], A1s[d]
-        if grow[d]:
-            A0 = np.hstack([A0, A0n[d]])
-            A1 = np.hstack([A1, A1n[d]])
+        Rd, Cd = (R2[d], C2[d]) if grow[d] else (R1[d], C1[d])
         if rks[d] == 0:
             out.append(np.zeros(0, complex))
             info["rk"].append(0)
             info["r"].append(r)
             continue
-        B, Uk, rk, _ = _B_from_moments(A0, A1, svd_tol)
+        B, _, rk, _ = _B_from_moments(Rd, Cd, svd_tol)
         info["rk"].append(rk)
-        info["r"].append(A0.shape[1])
+        info["r"].append(Rd.shape[1])
         out.append(np.linalg.eigvals(B) if rk else np.zeros(0, complex))
     return (out, info) if return_info else out
 
 
 def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=None, mixed=False, ws=None,
                        max_refine=10, refine_tol=1e-6, return_info=False, regrow="extend", use_chebyshev=True,
-                       cheb=None, fp32_sweeps=0, solve_block=0, node_chunk=0, resid_engine=0):
+                       cheb=None, fp32_sweeps=0, solve_block=0, node_chunk=0, resid_engine=0, basis=True):
     """construct_B_matrix (beyn.jl:257-322). Returns (B, Uk) [, info].
 
     regrow: when the rank saturates (rk == r) the reference draws a fresh
     N x 2r probe block and solves all 2r columns again (beyn.jl:291-309).
     "fresh" does the same; "extend" (default) keeps the r columns already
     solved and draws only r new ones, so the moments of the 2r block cost r
-    new solves. The eigenvalues of B do not depend on the probe block."""
+    new solves. The eigenvalues of B do not depend on the probe block.
+
+    basis=False skips U_k (returned as None): the moments stay on the device,
+    A0 = Q R is factored there and only R and Q^H A1 (m x m) come back, so the
+    SVD runs on R (same singular values and W as A0's, U = Q U_R) and
+    B = U_R,k^H (Q^H A1) W_k Sigma_k^-1. The rank test, the regrowth and B are
+    the reference's; only the order of the dense algebra differs."""
     rng = rng if rng is not None else np.random.default_rng(0)
     ws = ws if ws is not None else Workspace(solver, pts)
     if ws.dim != N:
@@ -187,23 +223,24 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
                     resid_engine=resid_engine)
     host["create"] += (clk() - t) * 1e3
     info = dict(stats=[], host_ms=host)
+    moments = bh.moments if basis else bh.moments_qr
     try:
         V = probe_matrix(N, r, rng)
         t = clk()
-        A0, A1 = bh.moments(V)
+        M0, M1 = moments(V)  # (A0, A1), or (R, Q^H A1)
         host["moments"] += (clk() - t) * 1e3
         info["stats"].append(bh.last_stats)
         # the saturation test needs only the singular values; the factors are
         # computed once, for the block that is finally used
         t = clk()
-        S = np.linalg.svd(A0, compute_uv=False)
+        S = np.linalg.svd(M0, compute_uv=False)
         rk = int(np.count_nonzero(S >= svd_tol))
         if not (rk == r and 2 * r < N) and rk > 0:
-            U, S, Wh = np.linalg.svd(A0, full_matrices=False)
+            U, S, Wh = np.linalg.svd(M0, full_matrices=False)
         host["svd"] += (clk() - t) * 1e3
         rused = r
         if rk == 0:
-            out = (np.zeros((0, 0), complex), np.zeros((N, 0), complex))
+            out = (np.zeros((0, 0), complex), np.zeros((N, 0), complex) if basis else None)
             info.update(rk=0, r=r, S=S)
             return (*out, info) if return_info else out
         if rk == r:
@@ -212,16 +249,19 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
                 t = clk()
                 if regrow == "extend":
                     Vn = probe_matrix(N, r_tmp - r, rng)
-                    A0n, A1n = bh.moments(Vn)
-                    A0 = np.asfortranarray(np.hstack([A0, A0n]))
-                    A1 = np.asfortranarray(np.hstack([A1, A1n]))
+                    if basis:
+                        A0n, A1n = bh.moments(Vn)
+                        M0 = np.asfortranarray(np.hstack([M0, A0n]))
+                        M1 = np.asfortranarray(np.hstack([M1, A1n]))
+                    else:
+                        M0, M1 = bh.moments_qr(Vn, append=True)
                 else:
                     V = probe_matrix(N, r_tmp, rng)
-                    A0, A1 = bh.moments(V)
+                    M0, M1 = moments(V)
                 host["moments"] += (clk() - t) * 1e3
                 info["stats"].append(bh.last_stats)
                 t = clk()
-                U, S, Wh = np.linalg.svd(A0, full_matrices=False)
+                U, S, Wh = np.linalg.svd(M0, full_matrices=False)
                 rk = int(np.count_nonzero(S >= svd_tol))
                 host["svd"] += (clk() - t) * 1e3
                 rused = r_tmp
@@ -232,10 +272,12 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
     t = clk()
     Uk = U[:, :rk]
     Wk = Wh.conj().T[:, :rk]
-    tmp = (A1 @ Wk) / S[:rk][None, :]
+    tmp = (M1 @ Wk) / S[:rk][None, :]
     B = Uk.conj().T @ tmp
     host["B"] += (clk() - t) * 1e3
     info.update(rk=rk, r=rused, S=S)
+    if not basis:
+        Uk = None
     return (B, Uk, info) if return_info else (B, Uk)
 
 
@@ -257,6 +299,7 @@ def solve(solver, pts, k0, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed=False,
     """Eigenvalues only (beyn.jl:388-397): eigvals(B), no eigenvectors."""
     if ws is None:
         ws = Workspace(solver, pts)
+    kw.setdefault("basis", False)  # eigenvalues only: U_k is not needed
     B, Uk, info = construct_B_matrix(solver, pts, ws.dim, k0, R, nq, r, svd_tol, rng, mixed, ws, return_info=True,
                                      **kw)
     t = time.perf_counter()

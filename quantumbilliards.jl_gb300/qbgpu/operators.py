@@ -304,6 +304,19 @@ def launch_count() -> int:
     return int(c.value)
 
 
+def release_cached_memory() -> None:
+    """Return every device block the library's caching allocator holds to the driver."""
+    L.check(L.load().qbg_pool_release())
+
+
+def pool_stats() -> dict:
+    """Cached and live bytes of the library's device allocator, reuse hits and driver allocations."""
+    v = [L.C.c_uint64(0) for _ in range(4)]
+    L.check(L.load().qbg_pool_stats(*[L.C.byref(x) for x in v]))
+    return dict(cached_bytes=int(v[0].value), live_bytes=int(v[1].value), hits=int(v[2].value),
+                misses=int(v[3].value))
+
+
 def set_gemm_engine(engine: int) -> None:
     """Engine of the complex64 GEMMs in the FP32 LU and solves (0 FMA tiles, 1 tcgen05)."""
     L.check(L.load().qbg_set_gemm_engine(int(engine)))

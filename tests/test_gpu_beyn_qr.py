@@ -1,0 +1,74 @@
+"""GPU: Beyn moments reduced on the device (qbg_beyn_moments_qr). With
+A0 = Q R the thin QR of the kept moment columns and C = Q^H A1:
+R is upper triangular, R^H R = A0^H A0 and R^H C = A0^H A1 (to 1e-12 of
+|A0|^2, |A0||A1|), for one call and for columns appended by a second call
+(the r -> 2r regrowth); a wrong column count is rejected before any work;
+eigenvalues from the reduced moments equal those from the full basis (1e-12
+relative) with and without rank saturation, in FP64 and in the mixed form."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _star(qb, n_nodes=400, k=25.0):
+    b = qb.make_star(0.2, 5)
+    sol = qb.CFIE_kress(1.0, b)
+    pts, sol = qb.points_with_n(sol, b, n_nodes, k)
+    return sol, pts, qb.Workspace(sol, pts)
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_qr_reduction_matches_moments(qb, mixed):
+    sol, pts, ws = _star(qb)
+    rng = np.random.default_rng(4)
+    V1 = qb.probe_matrix(ws.dim, 12, rng)
+    V2 = qb.probe_matrix(ws.dim, 12, rng)
+    bh = qb.BeynHandle(ws, 25.0 + 0.05j, 0.4, 16, mixed=mixed)
+    try:
+        A0a, A1a = bh.moments(V1)
+        A0b, A1b = bh.moments(V2)
+        R1, C1 = bh.moments_qr(V1)
+        R2, C2 = bh.moments_qr(V2, append=True)
+    finally:
+        bh.close()
+    for (Rm, Cm, A0, A1) in ((R1, C1, A0a, A1a), (R2, C2, np.hstack([A0a, A0b]), np.hstack([A1a, A1b]))):
+        assert np.array_equal(Rm, np.triu(Rm))
+        s0 = np.linalg.norm(A0) ** 2
+        s01 = np.linalg.norm(A0) * np.linalg.norm(A1)
+        assert np.max(np.abs(Rm.conj().T @ Rm - A0.conj().T @ A0)) < 1e-12 * s0
+        assert np.max(np.abs(Rm.conj().T @ Cm - A0.conj().T @ A1)) < 1e-12 * s01
+
+
+def test_qr_rejects_wrong_column_count(qb):
+    from qbgpu import _lib
+    sol, pts, ws = _star(qb, 200, 15.0)
+    bh = qb.BeynHandle(ws, 15.0, 0.3, 8, mixed=False)
+    try:
+        V = np.asfortranarray(qb.probe_matrix(ws.dim, 4, np.random.default_rng(1)))
+        Rm = np.empty((5, 5), np.complex128)
+        st = _lib.BeynStats()
+        rc = _lib.load().qbg_beyn_moments_qr(bh._h, _lib.vptr(V), 4, 0, 5, _lib.vptr(Rm), _lib.vptr(Rm),
+                                             C.byref(st))
+        assert rc == _lib.QBG_EINVAL
+        assert "m = 5" in _lib.last_error()
+    finally:
+        bh.close()
+
+
+@pytest.mark.parametrize("mixed,r", [(False, 8), (True, 8), (True, 24)])
+def test_solve_reduced_equals_full_basis(qb, mixed, r):
+    sol, pts, ws = _star(qb)
+    kw = dict(nq=24, r=r, svd_tol=1e-12, mixed=mixed, ws=ws)
+    lam_r, info_r = qb.solve(sol, pts, 25.0 + 0j, 0.5, rng=np.random.default_rng(7), return_info=True, **kw)
+    B, Uk, info_f = qb.construct_B_matrix(sol, pts, ws.dim, 25.0 + 0j, 0.5, rng=np.random.default_rng(7),
+                                          return_info=True, basis=True, **{k: v for k, v in kw.items()
+                                                                           if k != "ws"}, ws=ws)
+    lam_f = np.linalg.eigvals(B)
+    assert info_r["rk"] == info_f["rk"] and info_r["r"] == info_f["r"]
+    sel = lambda l: np.sort_complex(l[(np.abs(l - 25.0) < 0.5) & (np.abs(l.imag) < 1e-6)])
+    a, f = sel(lam_r), sel(lam_f)
+    assert len(a) == len(f) > 0
+    assert np.max(np.abs(a - f) / np.abs(f)) < 1e-12
