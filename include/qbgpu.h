@@ -53,7 +53,11 @@ enum { QBG_FORM_DLP = 0, QBG_FORM_CFIE = 1 };
  *                  against the FP32 operator: fastest, accuracy bounded by the
  *                  FP32 rounding of the operator. */
 enum { QBG_PREC_FP64 = 0, QBG_PREC_MIXED = 1, QBG_PREC_FP32 = 2 };
-enum { QBG_PTR_DEVICE = 1, QBG_V_PER_DISK = 2 };
+/* QBG_SPLIT_LO (qbg_assemble, qbg_assemble_cheb with QBG_PREC_MIXED, deriv 0):
+ * outs holds 2 nk pointers, the complex64 high words of A(k_1..k_nk) and then
+ * their low words (value - high, rounded to complex64), so high + low carries
+ * the kernel value to ~2^-48 relative. */
+enum { QBG_PTR_DEVICE = 1, QBG_V_PER_DISK = 2, QBG_SPLIT_LO = 4 };
 
 /* Boundary discretisation (BoundaryPointsCFIE, boundarypoints.jl:487-503),
  * components concatenated; holes already orientation-reversed as

@@ -259,6 +259,18 @@ int make_cheb(qbg_geom* g, const cxd* dks, int nk, const qbg_cheb_params& prm, C
   tmp.push_back(t.J);
   return cheb_build(t, dks, st);
 }
+
+int make_cheb_df(ChebTables& t, const cxd* dks, std::vector<void*>& tmp, cudaStream_t st) {
+  size_t hd = 0, jd = 0, nc = 0;
+  cheb_df_bytes(t, &hd, &jd, &nc);
+  QBG_TRY(dmalloc(&t.HD, hd));
+  tmp.push_back(t.HD);
+  QBG_TRY(dmalloc(&t.JD, jd));
+  tmp.push_back(t.JD);
+  QBG_TRY(dmalloc(&t.nkc, nc));
+  tmp.push_back(t.nkc);
+  return cheb_df_tables(t, dks, st);
+}
 }  // namespace qbg
 
 extern "C" {
@@ -274,7 +286,13 @@ static int assemble_impl(qbg_geom* g, const double* ks, int64_t nk, int32_t deri
   const int64_t dim = g->dim;
   const size_t esz = prec ? sizeof(cxf) : sizeof(cxd);
   const size_t mat_bytes = (size_t)dim * dim * esz;
-  const int nout = 1 + 2 * deriv;
+  // QBG_SPLIT_LO: the mixed form's low words as a second block of nk outputs
+  const bool split = (flags & QBG_SPLIT_LO) != 0;
+  if (split && (prec != QBG_PREC_MIXED || deriv)) {
+    set_error("qbg_assemble: QBG_SPLIT_LO needs prec QBG_PREC_MIXED and deriv = 0");
+    return QBG_EINVAL;
+  }
+  const int nout = split ? 2 : 1 + 2 * deriv;
   const bool dev = (flags & QBG_PTR_DEVICE) != 0;
   // chunk the k list so that device staging stays below 8 GiB for host outputs
   int64_t chunk = nk;
@@ -302,12 +320,15 @@ static int assemble_impl(qbg_geom* g, const double* ks, int64_t nk, int32_t deri
       std::vector<void*> ctmp;
       ChebTables t;
       s = make_cheb(g, dks + k0, (int)c, *cheb, t, ctmp, st);
-      if (!s) s = launch_assemble_cheb(g->d, t, dks + k0, (int)c, deriv, prec, dptrs, nullptr, dim, st);
+      if (!s && prec != QBG_PREC_FP64 && g->d.m == g->d.n && !deriv) s = make_cheb_df(t, dks + k0, ctmp, st);
+      if (!s)
+        s = launch_assemble_cheb(g->d, t, dks + k0, (int)c, deriv, prec, dptrs, split ? dptrs + c : nullptr, dim,
+                                 st);
       cudaError_t e2 = cudaStreamSynchronize(st);
       for (void* p : ctmp) dfree(p);
       if (!s && e2 != cudaSuccess) s = cuda_status(e2, "qbg_assemble_cheb");
     } else {
-      s = launch_assemble(g->d, dks + k0, (int)c, deriv, prec, dptrs, dim, st);
+      s = launch_assemble(g->d, dks + k0, (int)c, deriv, prec, dptrs, dim, st, split ? dptrs + c : nullptr);
     }
     if (s) { cleanup(); return s; }
     if (!dev) {

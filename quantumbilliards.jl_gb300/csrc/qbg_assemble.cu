@@ -20,6 +20,7 @@
 //   CFIE cross-component (smooth kernel)              cfie_kress.jl:480-503
 //   complex k: J0/J1 evaluated separately from H0/H1 and the coefficients
 //   hoisted exactly as chebyshev_euclidian_helmholtz_cfie_kress.jl:596-611.
+#include <algorithm>
 #include <cstring>
 
 #include <vector>
@@ -974,6 +975,296 @@ __global__ void __launch_bounds__(512) k_assemble_cheb_sym(GeomDev g, ChebTables
   }
 }
 
+// ---------------------------------------------------------------------------
+// Double-float evaluation for the complex64 forms (QBG_PREC_MIXED / FP32)
+// ---------------------------------------------------------------------------
+// The FP64 pipe of this part runs at 1/64 of the FP32 rate, and the FP64
+// symmetric kernel above spends nearly all its time there (two degree-M
+// Clenshaw sums and the fold per pair and node). Here every per-node step runs
+// on FP32 pairs (hi + lo, ~2^-48 relative): the Chebyshev polynomials T_m(t)
+// by their recurrence, the four premultiplied series of each table as
+// error-free FMA dot products, and the fold with the pair's real coefficients.
+// Per pair and tile the geometry, the fold coefficients and the panel
+// arguments are computed once in FP64 for all nodes. The result is the mixed
+// form's (hi, lo) pair directly. Pairs below the direct-evaluation cut and the
+// diagonal keep the FP64 route.
+namespace {
+
+struct dfl {
+  float hi, lo;
+};
+
+__device__ __forceinline__ dfl df_of(double x) {
+  dfl r;
+  r.hi = (float)x;
+  r.lo = (float)(x - (double)r.hi);
+  return r;
+}
+
+__device__ __forceinline__ dfl df_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+
+__device__ __forceinline__ dfl df_fast_sum(float a, float b) {  // |a| >= |b|
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return df_fast_sum(p, e);
+}
+
+__device__ __forceinline__ dfl df_sub(dfl a, dfl b) {
+  dfl s = df_two_sum(a.hi, -b.hi);
+  s.lo += a.lo - b.lo;
+  return df_fast_sum(s.hi, s.lo);
+}
+
+// acc += c t, acc kept unnormalised (hi exact partial sums, lo the errors)
+__device__ __forceinline__ void df_acc(dfl& acc, dfl c, dfl t) {
+  const float p = c.hi * t.hi;
+  float e = fmaf(c.hi, t.hi, -p);
+  e = fmaf(c.hi, t.lo, e);
+  e = fmaf(c.lo, t.hi, e);
+  const dfl s = df_two_sum(acc.hi, p);
+  acc.hi = s.hi;
+  acc.lo += s.lo + e;
+}
+
+__device__ __forceinline__ dfl df_norm(dfl a) { return df_two_sum(a.hi, a.lo); }
+
+// sum_m c_m T_m(t) for the two complex series of one table row (float4 pairs
+// per degree: {series 0, series 1}); S0 skips series 0 (DLP needs only J1, H1)
+template <bool S0>
+__device__ __forceinline__ void df_series(const float4* __restrict__ c, int M, dfl t, dfl* v0r, dfl* v0i, dfl* v1r,
+                                          dfl* v1i) {
+  dfl a0r{0.f, 0.f}, a0i{0.f, 0.f}, a1r{0.f, 0.f}, a1i{0.f, 0.f};
+  dfl tp{1.f, 0.f}, tc = t;  // T_{m-1}, T_m
+  const dfl t2{2.f * t.hi, 2.f * t.lo};
+  for (int m = 0; m <= M; ++m) {
+    dfl tm;
+    if (m == 0) {
+      tm = tp;
+    } else if (m == 1) {
+      tm = tc;
+    } else {
+      tm = df_sub(df_mul(t2, tc), tp);
+      tp = tc;
+      tc = tm;
+    }
+    const float4 c1 = __ldg(c + 2 * m + 1);
+    df_acc(a1r, dfl{c1.x, c1.y}, tm);
+    df_acc(a1i, dfl{c1.z, c1.w}, tm);
+    if (S0) {
+      const float4 c0 = __ldg(c + 2 * m);
+      df_acc(a0r, dfl{c0.x, c0.y}, tm);
+      df_acc(a0i, dfl{c0.z, c0.w}, tm);
+    }
+  }
+  *v1r = a1r;
+  *v1i = a1i;
+  if (S0) {
+    *v0r = a0r;
+    *v0i = a0i;
+  }
+}
+
+struct FoldDf {
+  dfl A, B, C, D;
+};
+
+__device__ __forceinline__ FoldDf fold_df(const Fold& f) { return {df_of(f.A), df_of(f.B), df_of(f.C), df_of(f.D)}; }
+
+__device__ __forceinline__ float4 pack_split(cxd v) {
+  const float hr = (float)v.re, hi = (float)v.im;
+  return make_float4(hr, hi, (float)(v.re - (double)hr), (float)(v.im - (double)hi));
+}
+
+}  // namespace
+
+__global__ void k_node_consts(const cxd* __restrict__ ks, int nk, NodeConst* out) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nk) return;
+  const cxd k = ks[q];
+  const double inv2pi = 0.15915494309189533577;
+  NodeConst c;
+  c.kaL1 = (-inv2pi) * k;
+  c.kaL2 = 0.5 * cmul_i(k);
+  c.kg = (-inv2pi) * cmul_i(k);
+  c.kd = -0.5 * k;
+  c.ak = hypot(k.re, k.im);
+  out[q] = c;
+}
+
+// grid (rows / 256, nk, 2 tables); rows = panels x (M + 1)
+__global__ void k_cheb_df_tables(ChebTables t) {
+  const int tab = blockIdx.z, q = blockIdx.y;
+  const long long rows = (long long)(tab ? t.nj : t.nh) * ((tab ? t.Mj : t.Mh) + 1);
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  const NodeConst nc = t.nkc[q];
+  const cxd* src = (tab ? t.J : t.H) + ((size_t)q * rows + r) * 2;
+  const cxd s0 = tab ? nc.kg * src[0] : nc.kd * src[0];
+  const cxd s1 = tab ? nc.kaL1 * src[1] : nc.kaL2 * src[1];
+  float4* dst = (tab ? t.JD : t.HD) + ((size_t)q * rows + r) * 2;
+  const dfl a = df_of(s0.re), b = df_of(s0.im), c = df_of(s1.re), d = df_of(s1.im);
+  dst[0] = make_float4(a.hi, a.lo, b.hi, b.lo);
+  dst[1] = make_float4(c.hi, c.lo, d.hi, d.lo);
+}
+
+// symmetric-pair assembly of the complex64 forms on double-float arithmetic;
+// same tiling as k_assemble_cheb_sym, every node of ks in one pass
+template <int FORM>
+__global__ void __launch_bounds__(512) k_assemble_cheb_sym_df(GeomDev g, ChebTables t, const cxd* __restrict__ ks,
+                                                              int nk, void* const* __restrict__ outs,
+                                                              void* const* __restrict__ los, long long ld) {
+  __shared__ float4 sm[32][33];  // (hi.re, hi.im, lo.re, lo.im) of the mirrored entries
+  const int2 bp = tile_pair(blockIdx.x);
+  const int bi = bp.x, bj = bp.y;
+  const bool dtile = (bi == bj);
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 16
+  const int i = bi * 32 + tx;
+  auto store = [&](int slot, size_t off, float4 v) {
+    reinterpret_cast<cxf*>(outs[slot])[off] = cxf(v.x, v.y);
+    if (los) reinterpret_cast<cxf*>(los[slot])[off] = cxf(v.z, v.w);
+  };
+  // per slot: flags, panels, arguments and fold coefficients (the FP64 route
+  // of the rare direct pairs recomputes its geometry)
+  bool act[2], isdiag[2], zero[2], direct[2], needj[2];
+  FoldDf dij[2], dji[2];
+  int ph[2], pj[2];
+  dfl th[2], tj[2];
+  float rrf[2];
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    const int j = bj * 32 + ty + 16 * s;
+    const bool inb = (i < g.n) && (j < g.n);
+    isdiag[s] = inb && (i == j);
+    act[s] = inb && !isdiag[s] && (!dtile || i < j);
+    zero[s] = false;
+    direct[s] = false;
+    needj[s] = false;
+    rrf[s] = 0.f;
+    ph[s] = pj[s] = 0;
+    double thd = 0.0, tjd = 0.0;
+    Fold fij{0.0, 0.0, 0.0, 0.0}, fji{0.0, 0.0, 0.0, 0.0};
+    if (act[s]) {
+      const PairGeom pa = pair_geom(g, i, j);
+      const PairGeom pb = pair_geom(g, j, i);
+      fij = fold_of<FORM>(pa);
+      fji = fold_of<FORM>(pb);
+      rrf[s] = (float)pa.r;
+      zero[s] = (FORM == 1 && !pa.same && pa.r * pa.r <= 4.93038065763132e-32);
+      panel_of(pa.r, t.rmin, t.rmax, t.dr_h, t.invdr_h, t.nh, ph[s], thd);
+      panel_of(pa.r, 0.0, t.rmax, t.dr_j, t.invdr_j, t.nj, pj[s], tjd);
+      direct[s] = pa.r < t.rmin;
+      needj[s] = fij.A != 0.0 || fij.C != 0.0 || fji.A != 0.0 || fji.C != 0.0;
+    }
+    th[s] = df_of(thd);
+    tj[s] = df_of(tjd);
+    dij[s] = fold_df(fij);
+    dji[s] = fold_df(fji);
+  }
+  for (int q = 0; q < nk; ++q) {
+    // the direct-evaluation cut |k| r < small_cut in FP32 (a threshold, not a value)
+    const float akf = (float)t.nkc[q].ak;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const int j = bj * 32 + ty + 16 * s;
+      float4 vij = make_float4(0.f, 0.f, 0.f, 0.f), vji = vij;
+      if (isdiag[s]) {
+        store(q, (size_t)i + (size_t)j * ld, pack_split(diag_fp64<FORM>(g, i, ks[q])));
+      } else if (act[s]) {
+        if (zero[s]) {
+          // both entries vanish
+        } else if (direct[s] || rrf[s] * akf < (float)t.small_cut) {
+          const PairGeom pa = pair_geom(g, i, j);
+          const PairGeom pb = pair_geom(g, j, i);
+          const Fold fij = fold_of<FORM>(pa), fji = fold_of<FORM>(pb);
+          const NodeConst nc = t.nkc[q];
+          const Bessel01d b = bessel01(pa.r * ks[q]);
+          cxd j0(0.0, 0.0), j1(0.0, 0.0);
+          if (needj[s]) {
+            int pjj = 0;
+            double tjd = 0.0;
+            panel_of(pa.r, 0.0, t.rmax, t.dr_j, t.invdr_j, t.nj, pjj, tjd);
+            clenshaw2(t.J + (((size_t)q * t.nj + pjj) * (t.Mj + 1)) * 2, t.Mj, tjd, j0, j1);
+          }
+          vij = pack_split(folded_entry(fij, nc.kaL1, nc.kaL2, nc.kg, nc.kd, b.h0(), b.h1(), j0, j1));
+          vji = pack_split(folded_entry(fji, nc.kaL1, nc.kaL2, nc.kg, nc.kd, b.h0(), b.h1(), j0, j1));
+        } else {
+          dfl h0r{0.f, 0.f}, h0i{0.f, 0.f}, h1r, h1i, j0r{0.f, 0.f}, j0i{0.f, 0.f}, j1r{0.f, 0.f}, j1i{0.f, 0.f};
+          df_series<FORM == 1>(t.HD + ((size_t)q * t.nh + ph[s]) * (t.Mh + 1) * 2, t.Mh, th[s], &h0r, &h0i, &h1r,
+                               &h1i);
+          if (needj[s])
+            df_series<FORM == 1>(t.JD + ((size_t)q * t.nj + pj[s]) * (t.Mj + 1) * 2, t.Mj, tj[s], &j0r, &j0i,
+                                 &j1r, &j1i);
+          // entry = -(A kaL1 J1 + B kaL2 H1 + C kg J0 + D kd H0), the node factors inside the tables
+          auto fold = [&](const FoldDf& f) {
+            dfl re{0.f, 0.f}, im{0.f, 0.f};
+            df_acc(re, f.B, h1r);
+            df_acc(im, f.B, h1i);
+            if (needj[s]) {
+              df_acc(re, f.A, j1r);
+              df_acc(im, f.A, j1i);
+            }
+            if (FORM == 1) {
+              df_acc(re, f.D, h0r);
+              df_acc(im, f.D, h0i);
+              if (needj[s]) {
+                df_acc(re, f.C, j0r);
+                df_acc(im, f.C, j0i);
+              }
+            }
+            re = df_norm(re);
+            im = df_norm(im);
+            return make_float4(-re.hi, -im.hi, -re.lo, -im.lo);
+          };
+          vij = fold(dij[s]);
+          vji = fold(dji[s]);
+        }
+        store(q, (size_t)i + (size_t)j * ld, vij);
+      }
+    sm[ty + 16 * s][tx] = vji;  // row = j - bj*32, column = i - bi*32
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const int jl = tx, il = ty + 16 * s;  // output (row j, column i)
+      const int j = bj * 32 + jl, ii = bi * 32 + il;
+      const bool ok = (j < g.n) && (ii < g.n) && (dtile ? (jl > il) : true);
+      if (ok) store(q, (size_t)j + (size_t)ii * ld, sm[jl][il]);
+    }
+    __syncthreads();
+  }
+}
+
+void cheb_df_bytes(const ChebTables& t, size_t* hd, size_t* jd, size_t* nkc) {
+  *hd = sizeof(float4) * 2 * (size_t)t.nk * t.nh * (t.Mh + 1);
+  *jd = sizeof(float4) * 2 * (size_t)t.nk * t.nj * (t.Mj + 1);
+  *nkc = sizeof(NodeConst) * (size_t)t.nk;
+}
+
+int cheb_df_tables(ChebTables& t, const cxd* ks, cudaStream_t st) {
+  if (!t.HD || !t.JD || !t.nkc) {
+    set_error("cheb_df_tables: buffers not set");
+    return QBG_EINVAL;
+  }
+  k_node_consts<<<(t.nk + 127) / 128, 128, 0, st>>>(ks, t.nk, t.nkc);
+  QBG_LAUNCH_CHECK("k_node_consts");
+  const long long rows = std::max((long long)t.nh * (t.Mh + 1), (long long)t.nj * (t.Mj + 1));
+  dim3 grd((unsigned)((rows + 255) / 256), t.nk, 2);
+  k_cheb_df_tables<<<grd, 256, 0, st>>>(t);
+  QBG_LAUNCH_CHECK("k_cheb_df_tables");
+  return QBG_OK;
+}
+
 int cheb_r_range(const GeomDev& g, unsigned long long* dscratch2, double* rmin, double* rmax, cudaStream_t st) {
   unsigned long long init[2] = {0ull, 0ull};
   const double big = 1e300;
@@ -1090,6 +1381,12 @@ int launch_assemble_cheb(const GeomDev& g, const ChebTables& t, const cxd* ks, i
         k_assemble_cheb_sym<0, 0><<<sgrd, sblk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
       else
         k_assemble_cheb_sym<1, 0><<<sgrd, sblk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
+    } else if (t.HD && t.JD && t.nkc) {
+      dim3 dgrd((unsigned)(nt * (nt + 1) / 2), 1, 1);
+      if (g.form == 0)
+        k_assemble_cheb_sym_df<0><<<dgrd, sblk, 0, st>>>(g, t, ks, nk, outs_dev, lo_outs_dev, ld);
+      else
+        k_assemble_cheb_sym_df<1><<<dgrd, sblk, 0, st>>>(g, t, ks, nk, outs_dev, lo_outs_dev, ld);
     } else {
       if (g.form == 0)
         k_assemble_cheb_sym<0, 1><<<sgrd, sblk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, lo_outs_dev, ld);

@@ -13,16 +13,32 @@ int launch_kress_column(double* out, int N, cudaStream_t st);
 // Chebyshev panel tables for nk wavenumbers (layout [k][panel][m][2], the pair
 // (H0, H1) on [rmin, rmax] in H and (J0, J1) on [0, rmax] in J).
 #define QBG_CHEB_MAX_DEGREE 16
+// per-wavenumber factors of the folded kernel entry (k_assemble_cheb_sym):
+// the J1, H1, J0, H0 terms carry kaL1 = -k/2pi, kaL2 = ik/2, kg = -ik/2pi, kd = -k/2
+struct NodeConst {
+  cxd kaL1, kaL2, kg, kd;
+  double ak;  // |k|
+};
 struct ChebTables {
   int nk = 0, nh = 0, Mh = 0, nj = 0, Mj = 0;
   double rmin = 0, rmax = 0, dr_h = 0, invdr_h = 0, dr_j = 0, invdr_j = 0;
   double small_cut = 0.2;  // |k r| below which Hankel values are evaluated directly
   cxd* H = nullptr;
   cxd* J = nullptr;
+  // double-float copies of the coefficients, each series premultiplied by its
+  // node factor: per (node, panel, degree) two float4 (re.hi, re.lo, im.hi, im.lo)
+  // = {kd H0, kaL2 H1} and {kg J0, kaL1 J1}; built by cheb_df_tables
+  float4* HD = nullptr;
+  float4* JD = nullptr;
+  NodeConst* nkc = nullptr;
 };
 // min / max pair distance over all off-diagonal pairs (host values; dscratch2 = 2 device words)
 int cheb_r_range(const GeomDev& g, unsigned long long* dscratch2, double* rmin, double* rmax, cudaStream_t st);
 int cheb_build(ChebTables& t, const cxd* ks, cudaStream_t st);
+// double-float tables for the complex64 forms (HD, JD, nkc: device buffers of the
+// sizes cheb_df_bytes reports, owned by the caller); after cheb_build
+void cheb_df_bytes(const ChebTables& t, size_t* hd, size_t* jd, size_t* nkc);
+int cheb_df_tables(ChebTables& t, const cxd* ks, cudaStream_t st);
 // max interpolation errors of H0, H1, J0, J1 per wavenumber at ns sampled radii (err: 4 nk zeroed words)
 int cheb_errors(const ChebTables& t, const cxd* ks, int ns, unsigned long long* err, cudaStream_t st);
 int launch_assemble_cheb(const GeomDev& g, const ChebTables& t, const cxd* ks, int nk, int deriv, int prec,

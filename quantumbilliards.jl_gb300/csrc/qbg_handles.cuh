@@ -54,4 +54,6 @@ qbg_cheb_params cheb_defaults(const qbg_cheb_params* prm);  // zeros -> 15000, 5
 // Chebyshev tables for nk device wavenumbers (device buffers appended to tmp)
 int make_cheb(qbg_geom* g, const cxd* dks, int nk, const qbg_cheb_params& prm, ChebTables& t,
               std::vector<void*>& tmp, cudaStream_t st);
+// double-float tables of t for the complex64 forms (after make_cheb; buffers appended to tmp)
+int make_cheb_df(ChebTables& t, const cxd* dks, std::vector<void*>& tmp, cudaStream_t st);
 }  // namespace qbg

@@ -20,6 +20,7 @@ QBG_FORM_DLP, QBG_FORM_CFIE = 0, 1
 QBG_PREC_FP64, QBG_PREC_MIXED, QBG_PREC_FP32 = 0, 1, 2
 QBG_PTR_DEVICE = 1
 QBG_V_PER_DISK = 2
+QBG_SPLIT_LO = 4
 
 
 def prec_code(p) -> int:

@@ -135,25 +135,29 @@ def _ks_array(ks) -> np.ndarray:
 DEFAULT_CHEB = (15000, 5, 3000, 5)  # the reference's n_panels_h, M_h, n_panels_j, M_j
 
 
-def assemble(ws: Workspace, ks, deriv: bool = False, mixed: bool = False, cheb=None) -> List[np.ndarray]:
+def assemble(ws: Workspace, ks, deriv: bool = False, mixed: bool = False, cheb=None,
+             split_lo: bool = False) -> List[np.ndarray]:
     """Return [A(k)...] (+ [A'(k)...], [A''(k)...]) as Fortran-ordered arrays.
 
     cheb: None for direct evaluation of H0, H1, J0, J1; True or a tuple
-    (n_panels_h, M_h, n_panels_j, M_j) for the Chebyshev-panel route."""
+    (n_panels_h, M_h, n_panels_j, M_j) for the Chebyshev-panel route.
+    split_lo (mixed form only): also return the complex64 low words,
+    [hi(k)..., lo(k)...] with hi + lo the kernel value to ~2^-48."""
     lib = L.load()
     k = _ks_array(ks)
     nk = len(k)
-    nout = 3 if deriv else 1
+    nout = 2 if split_lo else (3 if deriv else 1)
     pc = L.prec_code(mixed)
     dt = np.complex128 if pc == L.QBG_PREC_FP64 else np.complex64
     outs = [np.empty((ws.dim, ws.dim), dtype=dt, order="F") for _ in range(nk * nout)]
     ptrs = (C.c_void_p * len(outs))(*[o.ctypes.data for o in outs])
     kd = k.view(np.float64)
+    flags = L.QBG_SPLIT_LO if split_lo else 0
     if cheb is None or cheb is False:
-        L.check(lib.qbg_assemble(ws.handle, L.dptr(kd), nk, 1 if deriv else 0, pc, 0, ptrs))
+        L.check(lib.qbg_assemble(ws.handle, L.dptr(kd), nk, 1 if deriv else 0, pc, flags, ptrs))
     else:
         prm = L.ChebParams(*(DEFAULT_CHEB if cheb is True else cheb))
-        L.check(lib.qbg_assemble_cheb(ws.handle, L.dptr(kd), nk, 1 if deriv else 0, pc, 0, C.byref(prm), ptrs))
+        L.check(lib.qbg_assemble_cheb(ws.handle, L.dptr(kd), nk, 1 if deriv else 0, pc, flags, C.byref(prm), ptrs))
     return outs
 
 

@@ -1,0 +1,58 @@
+"""GPU: Chebyshev-panel assembly of the mixed form on double-float (FP32 pair)
+arithmetic against the FP64 Chebyshev assembly of the same tables.
+
+hi + lo must carry the FP64 value: |hi + lo - A64| <= 1e-13 max|A64| overall
+and <= 4e-13 |A64| elementwise where |A64| >= 1e-3 max|A64|. The double-float
+sums carry ~2^-48 of the sum of |terms| (FP64: 2^-53), so small entries that
+are cancelling sums (cross-component pairs, near zeros of J0, J1) keep an
+absolute, not a relative, error bound (1.6e-12 relative measured at
+|A64| ~ 1e-6 max on the holed disk); hi alone is A64 rounded to complex64
+(|hi - A64| <= 2^-23 |A64| + 1e-13 max|A64|). CFIE (all four series, the
+cross-component pairs of a holed domain) and DLP (J1, H1 only), complex
+wavenumbers, and a low wavenumber whose near pairs take the direct FP64
+route (|k| r < 0.2)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _check(qb, ws, ks):
+    ref = qb.assemble(ws, ks, cheb=True)
+    out = qb.assemble(ws, ks, mixed=True, cheb=True, split_lo=True)
+    nk = len(ks)
+    for q in range(nk):
+        a = ref[q]
+        hi, lo = out[q], out[nk + q]
+        v = hi.astype(np.complex128) + lo.astype(np.complex128)
+        scale = np.max(np.abs(a))
+        err = np.abs(v - a)
+        assert np.max(err) <= 1e-13 * scale, (q, np.max(err) / scale)
+        big = np.abs(a) >= 1e-3 * scale
+        small = (np.abs(a) >= 1e-6 * scale) & ~big
+        print(f"k={ks[q]}: max err/max|A| {np.max(err) / scale:.2e}, big entries rel {np.max(err[big] / np.abs(a[big])):.2e}"
+              f", small entries rel {np.max(err[small] / np.abs(a[small])) if small.any() else 0.0:.2e}")
+        assert np.max(err[big] / np.abs(a[big])) <= 4e-13, (q, np.max(err[big] / np.abs(a[big])))
+        assert np.all(np.abs(hi.astype(np.complex128) - a) <= 2.0 ** -23 * np.abs(a) + 1e-13 * scale)
+
+
+@pytest.mark.parametrize("ks", [[25.0 + 0.3j, 24.7 - 0.2j], [2.0 + 0.1j]])
+def test_df_assembly_cfie_star(qb, ks):
+    b = qb.make_star(0.2, 5)
+    sol = qb.CFIE_kress(1.0, b)
+    pts, sol = qb.points_with_n(sol, b, 400, 25.0)
+    _check(qb, qb.Workspace(sol, pts), ks)
+
+
+def test_df_assembly_cfie_holed(qb):
+    b = qb.make_circle_with_hole(1.0, (0.3, 0.1, 0.2))
+    sol = qb.CFIE_kress(1.0, b)
+    pts, sol = qb.points_with_n(sol, b, 500, 20.0)
+    _check(qb, qb.Workspace(sol, pts), [20.0 + 0.2j, 19.5 + 0.0j])
+
+
+def test_df_assembly_dlp_stadium(qb):
+    b = qb.make_full_stadium(1.0, 1.0)
+    sol = qb.DLP_kress_global_corners(1.0, b)
+    pts, sol = qb.points_with_n(sol, b, 600, 30.0)
+    _check(qb, qb.Workspace(sol, pts), [30.0 + 0.25j, 29.6 - 0.1j])
