@@ -616,32 +616,66 @@ int lu_factor(LUBatch<T>& f, cudaStream_t st) {
     panel_attr[sizeof(T) == 8] = true;
   }
   QBG_CUDA(cudaMemsetAsync(f.info, 0, sizeof(int) * batch, st));
-  for (int j0 = 0; j0 < n; j0 += nb) {
-    const int w = min(nb, n - j0);
-    if (smem_panel) {
-      const size_t smem = (size_t)(n - j0) * sub * sizeof(cx<T>);
-      k_getrf_panel_smem<T><<<batch, 1024, smem, st>>>(f.A, n, f.stride, j0, nb, sub, f.ipiv, f.info);
-      QBG_LAUNCH_CHECK("k_getrf_panel_smem");
-    } else {
-      k_getf2_panel<T><<<batch, 512, 0, st>>>(f.A, n, f.stride, j0, nb, f.ipiv, f.info);
-      QBG_LAUNCH_CHECK("k_getf2_panel");
+  // two-level right-looking LU: panels of nb columns inside outer blocks of
+  // LU_OUTER panels. A panel's updates reach only the columns of its outer
+  // block; the trailing matrix right of an outer block is updated once, with
+  // K = LU_OUTER * nb, after the outer block's U rows are formed by block
+  // forward substitution (the nb x nb inverses of L from k_trtri). The row
+  // interchanges of every panel still apply to all columns at once (k_laswp),
+  // so the factors are those of the one-level algorithm.
+  constexpr int LU_OUTER = 4;
+  const cx<T> one(1, 0), mone(-1, 0), zero(0, 0);
+  auto linv = [&](int j) { return f.Linv + (long long)(j / nb) * nb * nb; };
+  const long long sLinv = (long long)f.nblk * nb * nb;
+  for (int J0 = 0; J0 < n; J0 += LU_OUTER * nb) {
+    const int E = min(n, J0 + LU_OUTER * nb);  // outer block columns [J0, E)
+    for (int j0 = J0; j0 < E; j0 += nb) {
+      const int w = min(nb, n - j0);
+      if (smem_panel) {
+        const size_t smem = (size_t)(n - j0) * sub * sizeof(cx<T>);
+        k_getrf_panel_smem<T><<<batch, 1024, smem, st>>>(f.A, n, f.stride, j0, nb, sub, f.ipiv, f.info);
+        QBG_LAUNCH_CHECK("k_getrf_panel_smem");
+      } else {
+        k_getf2_panel<T><<<batch, 512, 0, st>>>(f.A, n, f.stride, j0, nb, f.ipiv, f.info);
+        QBG_LAUNCH_CHECK("k_getf2_panel");
+      }
+      dim3 g2((n + 255) / 256, batch);
+      k_laswp<T><<<g2, 256, 0, st>>>(f.A, n, f.stride, j0, nb, f.ipiv);
+      QBG_LAUNCH_CHECK("k_laswp");
+      k_trtri<T, false><<<dim3(1, batch), 256, sm, st>>>(f.A, n, f.stride, nb, j0 / nb, f.Linv, f.nblk);
+      QBG_LAUNCH_CHECK("k_trtri lower");
+      const int rin = E - j0 - w;  // columns of this outer block right of the panel
+      if (rin > 0) {
+        // U12 = inv(L11) A12 and A22 -= L21 U12 on the outer block's columns
+        int s = gemm_batched<T>(w, rin, w, one, linv(j0), nb, sLinv, f.A + j0 + (long long)(j0 + w) * n, n,
+                                f.stride, zero, f.A + j0 + (long long)(j0 + w) * n, n, f.stride, batch, st);
+        if (s) return s;
+        s = gemm_batched<T>(n - j0 - w, rin, w, mone, f.A + (j0 + w) + (long long)j0 * n, n, f.stride,
+                            f.A + j0 + (long long)(j0 + w) * n, n, f.stride, one,
+                            f.A + (j0 + w) + (long long)(j0 + w) * n, n, f.stride, batch, st);
+        if (s) return s;
+      }
     }
-    dim3 g2((n + 255) / 256, batch);
-    k_laswp<T><<<g2, 256, 0, st>>>(f.A, n, f.stride, j0, nb, f.ipiv);
-    QBG_LAUNCH_CHECK("k_laswp");
-    k_trtri<T, false><<<dim3(1, batch), 256, sm, st>>>(f.A, n, f.stride, nb, j0 / nb, f.Linv, f.nblk);
-    QBG_LAUNCH_CHECK("k_trtri lower");
-    const int rest = n - j0 - w;
+    const int rest = n - E;
     if (rest > 0) {
-      // U12 = inv(L11) A12
-      int s = gemm_batched<T>(w, rest, w, cx<T>(1, 0), f.Linv + (long long)(j0 / nb) * nb * nb, nb,
-                              (long long)f.nblk * nb * nb, f.A + j0 + (long long)(j0 + w) * n, n, f.stride,
-                              cx<T>(0, 0), f.A + j0 + (long long)(j0 + w) * n, n, f.stride, batch, st);
-      if (s) return s;
-      // A22 -= L21 U12
-      s = gemm_batched<T>(rest, rest, w, cx<T>(-1, 0), f.A + (j0 + w) + (long long)j0 * n, n, f.stride,
-                          f.A + j0 + (long long)(j0 + w) * n, n, f.stride, cx<T>(1, 0),
-                          f.A + (j0 + w) + (long long)(j0 + w) * n, n, f.stride, batch, st);
+      // U rows of the outer block on the trailing columns: U_b = inv(L_bb) (A_b - sum_{b'<b} L_bb' U_b')
+      for (int j0 = J0; j0 < E; j0 += nb) {
+        const int w = min(nb, E - j0);
+        int s = gemm_batched<T>(w, rest, w, one, linv(j0), nb, sLinv, f.A + j0 + (long long)E * n, n, f.stride,
+                                zero, f.A + j0 + (long long)E * n, n, f.stride, batch, st);
+        if (s) return s;
+        const int below = E - j0 - w;
+        if (below > 0) {
+          s = gemm_batched<T>(below, rest, w, mone, f.A + (j0 + w) + (long long)j0 * n, n, f.stride,
+                              f.A + j0 + (long long)E * n, n, f.stride, one, f.A + (j0 + w) + (long long)E * n, n,
+                              f.stride, batch, st);
+          if (s) return s;
+        }
+      }
+      // trailing update, K = E - J0
+      int s = gemm_batched<T>(rest, rest, E - J0, mone, f.A + E + (long long)J0 * n, n, f.stride,
+                              f.A + J0 + (long long)E * n, n, f.stride, one, f.A + E + (long long)E * n, n, f.stride,
+                              batch, st);
       if (s) return s;
     }
   }
