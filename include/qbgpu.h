@@ -328,7 +328,10 @@ qbg_status qbg_serve_destroy(qbg_server* s);
  * b < batch, column-major host buffers (complex interleaved floats; A_b at
  * A + 2*b*lda*K, B_b at B + 2*b*ldb*N, C_b at C + 2*b*ldc*N). engine selects
  * the GEMM inside the FP32 LU and solves: 0 = CUDA-core FMA tiles,
- * 1 = tcgen05 tensor cores (3xTF32). No reference counterpart: the reference's
+ * 1 = tcgen05 tensor cores (3xTF32; for products of at least 4 x 8 output
+ * tiles the operands are packed once per call into split tile images that
+ * bulk copies stream through a four-stage ring, smaller ones split their
+ * operands in registers), 2 = tcgen05 with operands split in registers always. No reference counterpart: the reference's
  * GEMMs run inside LAPACK's getrf/getrs (beyn.jl:270-280). */
 qbg_status qbg_cgemm_c64(int32_t engine, int32_t M, int32_t N, int32_t K, const float* alpha, const float* A,
                          int64_t lda, const float* B, int64_t ldb, const float* beta, float* C, int64_t ldc,
@@ -342,7 +345,7 @@ qbg_status qbg_cgemm_c64(int32_t engine, int32_t M, int32_t N, int32_t K, const 
 qbg_status qbg_residual_c64(int32_t engine, int32_t n, int32_t L, int32_t batch, const float* Th, const float* Tl,
                             const double* X, const double* V, double* R, double* rmax);
 
-/* Selects the complex64 GEMM engine (0 or 1 as above) for later calls,
+/* Selects the complex64 GEMM engine (0, 1 or 2 as above) for later calls,
  * process-wide; the default is 1. No reference counterpart. */
 qbg_status qbg_set_gemm_engine(int32_t engine);
 

@@ -593,7 +593,7 @@ qbg_status qbg_cgemm_c64(int32_t engine, int32_t M, int32_t N, int32_t K, const 
                          int64_t lda, const float* B, int64_t ldb, const float* beta, float* C, int64_t ldc,
                          int32_t batch) {
   if (!alpha || !beta || !A || !B || !C || M < 1 || N < 1 || K < 1 || batch < 1 || batch > 65535 || lda < M ||
-      ldb < K || ldc < M || (engine != GEMM_ENGINE_SIMT && engine != GEMM_ENGINE_TCGEN05)) {
+      ldb < K || ldc < M || engine < GEMM_ENGINE_SIMT || engine > GEMM_ENGINE_TCGEN05_STAGED) {
     set_error("qbg_cgemm_c64: invalid arguments");
     return QBG_EINVAL;
   }
@@ -610,11 +610,12 @@ qbg_status qbg_cgemm_c64(int32_t engine, int32_t M, int32_t N, int32_t K, const 
   }
   if (!s && e == cudaSuccess) {
     const cxf al(alpha[0], alpha[1]), be(beta[0], beta[1]);
-    if (engine == GEMM_ENGINE_TCGEN05)
-      s = tc_gemm_c64(M, N, K, al, dA, lda, sA, dB, ldb, sB, be, dC, ldc, sC, batch, 0);
+    if (engine != GEMM_ENGINE_SIMT)
+      s = tc_gemm_c64(M, N, K, al, dA, lda, sA, dB, ldb, sB, be, dC, ldc, sC, batch, 0, 1, 0, 0, 0,
+                      engine == GEMM_ENGINE_TCGEN05);
     else
       s = gemm_batched_simt<float>(M, N, K, al, dA, lda, sA, dB, ldb, sB, be, dC, ldc, sC, batch, 0);
-    if (!s && engine == GEMM_ENGINE_TCGEN05) s = tc_check(0);
+    if (!s && engine != GEMM_ENGINE_SIMT) s = tc_check(0);
     if (!s) e = cudaMemcpy(C, dC, sizeof(cxf) * sC * batch, cudaMemcpyDeviceToHost);
   }
   dfree(dA);
@@ -687,8 +688,8 @@ qbg_status qbg_residual_c64(int32_t engine, int32_t n, int32_t L, int32_t batch,
 }
 
 qbg_status qbg_set_gemm_engine(int32_t engine) {
-  if (engine != GEMM_ENGINE_SIMT && engine != GEMM_ENGINE_TCGEN05) {
-    set_error("qbg_set_gemm_engine: engine must be 0 or 1");
+  if (engine < GEMM_ENGINE_SIMT || engine > GEMM_ENGINE_TCGEN05_STAGED) {
+    set_error("qbg_set_gemm_engine: engine must be 0, 1 or 2");
     return QBG_EINVAL;
   }
   set_gemm_engine(engine);

@@ -63,7 +63,10 @@ struct qbg_beyn {
     dfree(macc1, st);
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
-    if (st) cudaStreamDestroy(st);
+    if (st) {
+      tc_release_scratch(st);
+      cudaStreamDestroy(st);
+    }
   }
   template <class P>
   int alloc(P** p, size_t bytes) {

@@ -22,6 +22,8 @@ inline int dmalloc(P** p, size_t bytes) {
   return s;
 }
 inline void dfree(void* p, cudaStream_t st = nullptr) { pool_free(p, st); }
+// returns the tensor-core GEMM's packing scratch of a stream (qbg_tc_gemm.cu)
+void tc_release_scratch(cudaStream_t st);
 }  // namespace qbg
 
 struct qbg_geom {
@@ -32,7 +34,10 @@ struct qbg_geom {
   std::mutex mu;
   ~qbg_geom() {
     for (void* p : allocs) qbg::dfree(p, stream);
-    if (stream) cudaStreamDestroy(stream);
+    if (stream) {
+      qbg::tc_release_scratch(stream);
+      cudaStreamDestroy(stream);
+    }
   }
   template <class P>
   int upload(const P* host, size_t count, const P** dev) {

@@ -86,10 +86,13 @@ int axpy_f2d(const cxf* d, cxd* x, long long count, cudaStream_t st);  // x += d
 // (outer o, inner q) starts at A + o sA + q sA2, and so on.
 int tc_gemm_c64(int M, int N, int K, cxf alpha, const cxf* A, long long lda, long long sA, const cxf* B,
                 long long ldb, long long sB, cxf beta, cxf* C, long long ldc, long long sC, int batch,
-                cudaStream_t st, int batch2 = 1, long long sA2 = 0, long long sB2 = 0, long long sC2 = 0);
+                cudaStream_t st, int batch2 = 1, long long sA2 = 0, long long sB2 = 0, long long sC2 = 0, bool allow_packed = true);
 // Reads the tensor-core GEMM's device error flag (set, and kept set, once an
 // mbarrier wait gave up); synchronizes the stream. Returns QBG_OK or QBG_ECUDA.
 int tc_check(cudaStream_t st);
+// returns the tensor-core GEMM's packing scratch of stream st to the pool
+// (call before destroying a stream that ran library GEMMs)
+void tc_release_scratch(cudaStream_t st);
 
 // Refinement residual on the tensor cores (exact 7-bit digit products, see
 // qbg_tc_resid.cu). The digit planes of the operators T = hi + lo are built
@@ -113,6 +116,7 @@ int tc_error_ptr(int** p);
 // tiles, 1 = tcgen05 tensor cores. Process-wide.
 constexpr int GEMM_ENGINE_SIMT = 0;
 constexpr int GEMM_ENGINE_TCGEN05 = 1;
+constexpr int GEMM_ENGINE_TCGEN05_STAGED = 2;  // tcgen05 with register-staged operands only
 void set_gemm_engine(int e);
 int gemm_engine();
 

@@ -27,7 +27,9 @@
 #include <atomic>
 #include <cstdint>
 #include <mutex>
+#include <vector>
 #include "qbg_common.cuh"
+#include "qbg_handles.cuh"
 #include "qbg_linalg.cuh"
 
 namespace qbg {
@@ -311,10 +313,251 @@ __global__ void __launch_bounds__(128) k_tc_cgemm(int M, int N, int K, cxf alpha
   }
 }
 
+// ---------------------------------------------------------------------------
+// Packed-operand path: A and B are split and laid out once per call in the
+// exact shared-memory images of the stages (k_tc_pack_a / k_tc_pack_b), and
+// the GEMM streams them with one bulk copy per operand and stage through a
+// four-stage ring; thread 0 issues the copies and the MMAs (full / empty
+// mbarriers per stage), all threads prefetch C and run the epilogue.
+//   PA tile (b, mt, kt): [big | small] x 4 MMA steps x 128 rows x 8 real k (32 KB)
+//   PB tile (b, nt, kt): [big | small] x 4 MMA steps x 64 B' rows x 8 real k (16 KB)
+// Every wait is bounded; on a timeout thread 0 records the error, waits
+// (bounded) for the copies and MMAs it issued, and the CTA frees its TMEM and
+// returns without writing C.
+// ---------------------------------------------------------------------------
+constexpr int PK_NST = 4;                                   // stages in the ring
+constexpr int PK_A_TILE = 2 * TC_KSTEPS * TC_A_STEP;        // 8192 floats
+constexpr int PK_B_TILE = 2 * TC_KSTEPS * TC_B_STEP;        // 4096 floats
+constexpr int PK_STAGE = PK_A_TILE + PK_B_TILE;             // 12288 floats (48 KB)
+
+// grid (MT, KT, batch * batch2), 128 threads: thread = row of the tile
+__global__ void __launch_bounds__(128) k_tc_pack_a(const cxf* __restrict__ A, long long lda, long long sA,
+                                                   long long sA2, int batch2, int M, int K, float* __restrict__ PA) {
+  const int tid = threadIdx.x;
+  const int mt = blockIdx.x, kt = blockIdx.y, MT = gridDim.x, KT = gridDim.y;
+  const long long z = blockIdx.z, bo = z / batch2, bi = z % batch2;
+  const cxf* Ab = A + bo * sA + bi * sA2;
+  const int gi = mt * TC_BM + tid, k0 = kt * TC_BK;
+  const bool rowok = gi < M;
+  cxf a[TC_BK];
+#pragma unroll
+  for (int kc = 0; kc < TC_BK; ++kc) {
+    const int gk = k0 + kc;
+    a[kc] = (rowok && gk < K) ? Ab[(long long)gi + (long long)gk * lda] : cxf(0.f, 0.f);
+  }
+  float* tile = PA + ((z * MT + mt) * (long long)KT + kt) * PK_A_TILE;
+#pragma unroll
+  for (int p = 0; p < TC_BK / 2; ++p) {
+    float4 big, small;
+    split4(a[2 * p].re, a[2 * p].im, a[2 * p + 1].re, a[2 * p + 1].im, big, small);
+    const int off = (p >> 1) * TC_A_STEP + kmaj4(tid, p & 1);
+    *reinterpret_cast<float4*>(tile + off) = big;
+    *reinterpret_cast<float4*>(tile + TC_KSTEPS * TC_A_STEP + off) = small;
+  }
+}
+
+// grid (NT, KT, batch * batch2), 128 threads: two (column, k pair) items each
+__global__ void __launch_bounds__(128) k_tc_pack_b(const cxf* __restrict__ B, long long ldb, long long sB,
+                                                   long long sB2, int batch2, int N, int K, float* __restrict__ PB) {
+  const int tid = threadIdx.x;
+  const int nt = blockIdx.x, kt = blockIdx.y, NT = gridDim.x, KT = gridDim.y;
+  const long long z = blockIdx.z, bo = z / batch2, bi = z % batch2;
+  const cxf* Bb = B + bo * sB + bi * sB2;
+  const int n0 = nt * TC_BN, k0 = kt * TC_BK;
+  float* tile = PB + ((z * NT + nt) * (long long)KT + kt) * PK_B_TILE;
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int item = tid + 128 * q;
+    const int j = item & (TC_BN - 1), p = item >> 5;
+    const int gj = n0 + j, gk = k0 + 2 * p;
+    const bool colok = gj < N;
+    const cxf v0 = (colok && gk < K) ? Bb[(long long)gk + (long long)gj * ldb] : cxf(0.f, 0.f);
+    const cxf v1 = (colok && gk + 1 < K) ? Bb[(long long)(gk + 1) + (long long)gj * ldb] : cxf(0.f, 0.f);
+    const int base = (p >> 1) * TC_B_STEP;
+    float4 big, small;
+    split4(v0.re, -v0.im, v1.re, -v1.im, big, small);
+    *reinterpret_cast<float4*>(tile + base + kmaj4(j, p & 1)) = big;
+    *reinterpret_cast<float4*>(tile + TC_KSTEPS * TC_B_STEP + base + kmaj4(j, p & 1)) = small;
+    split4(v0.im, v0.re, v1.im, v1.re, big, small);
+    *reinterpret_cast<float4*>(tile + base + kmaj4(TC_BN + j, p & 1)) = big;
+    *reinterpret_cast<float4*>(tile + TC_KSTEPS * TC_B_STEP + base + kmaj4(TC_BN + j, p & 1)) = small;
+  }
+}
+
+namespace {
+__device__ __forceinline__ void pk_expect(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void pk_bulk(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(mbar)
+      : "memory");
+}
+}  // namespace
+
+// grid (MT, NT, batch * batch2), 128 threads
+__global__ void __launch_bounds__(128, 1) k_tc_cgemm_pk(int M, int N, int KT, cxf alpha, const float* __restrict__ PA,
+                                                        const float* __restrict__ PB, cxf beta, cxf* C, long long ldc,
+                                                        long long sC, int batch2, long long sC2, int* err) {
+  extern __shared__ __align__(1024) unsigned char pk_smem[];
+  float* stages = reinterpret_cast<float*>(pk_smem);  // [PK_NST][A tile | B tile]
+  uint64_t* full = reinterpret_cast<uint64_t*>(stages + PK_NST * PK_STAGE);  // [PK_NST]
+  uint64_t* empty = full + PK_NST;                                          // [PK_NST]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(empty + PK_NST);
+  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int mt = blockIdx.x, nt = blockIdx.y, MT = gridDim.x, NT = gridDim.y;
+  const long long z = blockIdx.z, bo = z / batch2, bi = z % batch2;
+  const int m0 = mt * TC_BM, n0 = nt * TC_BN;
+  cxf* Cb = C + bo * sC + bi * sC2;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < PK_NST; ++s) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(full + s)) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(empty + s)) : "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    *abort_flag = (*reinterpret_cast<volatile int*>(err) != 0) ? 1 : 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  // C of this thread's row, in flight while the k loop runs
+  const int i = m0 + warp * 32 + lane;
+  const bool use_beta = !(beta.re == 0.f && beta.im == 0.f);
+  cxf cold[TC_BN];
+#pragma unroll
+  for (int j = 0; j < TC_BN; ++j) {
+    const int gj = n0 + j;
+    cold[j] = (use_beta && i < M && gj < N) ? Cb[(long long)i + (long long)gj * ldc] : cxf(0.f, 0.f);
+  }
+
+  if (tid == 0 && *abort_flag == 0) {
+    const float* pa = PA + (z * MT + mt) * (long long)KT * PK_A_TILE;
+    const float* pb = PB + (z * NT + nt) * (long long)KT * PK_B_TILE;
+    const uint32_t sbase = smem_u32(stages);
+    auto issue = [&](int t) {
+      const int s = t % PK_NST;
+      const uint32_t fb = smem_u32(full + s);
+      pk_expect(fb, (uint32_t)(PK_STAGE * sizeof(float)));
+      pk_bulk(sbase + (uint32_t)(s * PK_STAGE * sizeof(float)), pa + (long long)t * PK_A_TILE,
+              (uint32_t)(PK_A_TILE * sizeof(float)), fb);
+      pk_bulk(sbase + (uint32_t)((s * PK_STAGE + PK_A_TILE) * sizeof(float)), pb + (long long)t * PK_B_TILE,
+              (uint32_t)(PK_B_TILE * sizeof(float)), fb);
+    };
+    int issued = 0;     // tiles whose copies were issued
+    int consumed = 0;   // tiles whose full barrier was observed
+    int committed = 0;  // tiles whose MMAs were committed
+    int freed = 0;      // tiles whose empty barrier was observed
+    bool good = true;
+    for (; issued < KT && issued < PK_NST; ++issued) issue(issued);
+    for (int kt = 0; kt < KT && good; ++kt) {
+      const int s = kt % PK_NST;
+      if (!mbar_wait_bounded(smem_u32(full + s), (uint32_t)((kt / PK_NST) & 1))) {
+        good = false;
+        break;
+      }
+      ++consumed;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const float* sA = stages + s * PK_STAGE;
+      const float* sB = sA + PK_A_TILE;
+#pragma unroll
+      for (int q = 0; q < TC_KSTEPS; ++q) {
+        const uint64_t dab = smem_desc(smem_u32(sA + q * TC_A_STEP));
+        const uint64_t das = smem_desc(smem_u32(sA + TC_KSTEPS * TC_A_STEP + q * TC_A_STEP));
+        const uint64_t dbb = smem_desc(smem_u32(sB + q * TC_B_STEP));
+        const uint64_t dbs = smem_desc(smem_u32(sB + TC_KSTEPS * TC_B_STEP + q * TC_B_STEP));
+        mma_tf32(tmem, das, dbb, (kt | q) != 0);
+        mma_tf32(tmem, dab, dbs, 1);
+        mma_tf32(tmem, dab, dbb, 1);
+      }
+      mma_commit(smem_u32(empty + s));
+      ++committed;
+      // refill the stage of tile kt - 1 once its MMAs are done
+      if (kt >= 1 && issued < KT) {
+        const int t = kt - 1;
+        if (!mbar_wait_bounded(smem_u32(empty + t % PK_NST), (uint32_t)((t / PK_NST) & 1))) {
+          good = false;
+          break;
+        }
+        ++freed;
+        issue(issued);
+        ++issued;
+      }
+    }
+    // every committed MMA group completes before TMEM is read or freed
+    for (; good && freed < committed; ++freed)
+      if (!mbar_wait_bounded(smem_u32(empty + freed % PK_NST), (uint32_t)((freed / PK_NST) & 1))) good = false;
+    if (!good) {
+      *abort_flag = 1;
+      atomicExch(err, 1);
+      // bounded drain of what this thread started: copies, then MMA groups
+      for (int t = consumed; t < issued; ++t)
+        mbar_wait_bounded(smem_u32(full + t % PK_NST), (uint32_t)((t / PK_NST) & 1));
+      for (int t = freed; t < committed; ++t)
+        mbar_wait_bounded(smem_u32(empty + t % PK_NST), (uint32_t)((t / PK_NST) & 1));
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (*abort_flag == 0 && KT > 0) {
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+    uint32_t re[32], im[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(re[0]), "=r"(re[1]), "=r"(re[2]), "=r"(re[3]), "=r"(re[4]), "=r"(re[5]), "=r"(re[6]), "=r"(re[7]),
+          "=r"(re[8]), "=r"(re[9]), "=r"(re[10]), "=r"(re[11]), "=r"(re[12]), "=r"(re[13]), "=r"(re[14]),
+          "=r"(re[15]), "=r"(re[16]), "=r"(re[17]), "=r"(re[18]), "=r"(re[19]), "=r"(re[20]), "=r"(re[21]),
+          "=r"(re[22]), "=r"(re[23]), "=r"(re[24]), "=r"(re[25]), "=r"(re[26]), "=r"(re[27]), "=r"(re[28]),
+          "=r"(re[29]), "=r"(re[30]), "=r"(re[31])
+        : "r"(taddr));
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(im[0]), "=r"(im[1]), "=r"(im[2]), "=r"(im[3]), "=r"(im[4]), "=r"(im[5]), "=r"(im[6]), "=r"(im[7]),
+          "=r"(im[8]), "=r"(im[9]), "=r"(im[10]), "=r"(im[11]), "=r"(im[12]), "=r"(im[13]), "=r"(im[14]),
+          "=r"(im[15]), "=r"(im[16]), "=r"(im[17]), "=r"(im[18]), "=r"(im[19]), "=r"(im[20]), "=r"(im[21]),
+          "=r"(im[22]), "=r"(im[23]), "=r"(im[24]), "=r"(im[25]), "=r"(im[26]), "=r"(im[27]), "=r"(im[28]),
+          "=r"(im[29]), "=r"(im[30]), "=r"(im[31])
+        : "r"(taddr + (uint32_t)TC_BN));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    if (i < M) {
+#pragma unroll
+      for (int j = 0; j < TC_BN; ++j) {
+        const int gj = n0 + j;
+        if (gj < N) {
+          cxf v = alpha * cxf(__uint_as_float(re[j]), __uint_as_float(im[j]));
+          if (use_beta) v += beta * cold[j];
+          Cb[(long long)i + (long long)gj * ldc] = v;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+  }
+}
+
 // device error flag of the tensor-core GEMM (one per device, found by symbol)
 __device__ int g_tc_err;
 
 static size_t tc_smem_bytes() { return sizeof(float) * (size_t)(2 * TC_STAGE_FLOATS) + 64; }
+static size_t pk_smem_bytes() { return sizeof(float) * (size_t)(PK_NST * PK_STAGE) + 16 * PK_NST + 64; }
 
 namespace {
 constexpr int TC_MAX_DEV = 64;
@@ -322,6 +565,7 @@ std::mutex g_tc_mu;
 int* g_tc_err_addr[TC_MAX_DEV] = {};
 bool g_tc_attr[TC_MAX_DEV] = {};
 std::atomic<int> g_engine{GEMM_ENGINE_TCGEN05};
+std::atomic<bool> g_pk_enabled{true};  // packed-operand path of tc_gemm_c64
 
 int tc_device_setup(int** err_out) {
   int dev = 0;
@@ -333,6 +577,7 @@ int tc_device_setup(int** err_out) {
   std::lock_guard<std::mutex> lk(g_tc_mu);
   if (!g_tc_attr[dev]) {
     QBG_CUDA(cudaFuncSetAttribute(k_tc_cgemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes()));
+    QBG_CUDA(cudaFuncSetAttribute(k_tc_cgemm_pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pk_smem_bytes()));
     void* a = nullptr;
     QBG_CUDA(cudaGetSymbolAddress(&a, g_tc_err));
     g_tc_err_addr[dev] = static_cast<int*>(a);
@@ -341,16 +586,68 @@ int tc_device_setup(int** err_out) {
   *err_out = g_tc_err_addr[dev];
   return QBG_OK;
 }
+
+// Packing scratch, one buffer per (device, stream): the GEMMs of one stream
+// run in order, so a stream reuses its buffer without waiting; a larger
+// request replaces it (the old block goes back to the pool behind the stream's
+// work). The owner of a stream returns its buffer with tc_release_scratch
+// before destroying the stream.
+struct PackScratch {
+  int dev;
+  cudaStream_t st;
+  void* p;
+  size_t bytes;
+};
+std::mutex g_pack_mu;
+std::vector<PackScratch> g_pack;
+
+int pack_scratch(cudaStream_t st, size_t bytes, void** out) {
+  int dev = 0;
+  QBG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_pack_mu);
+  for (auto& e : g_pack)
+    if (e.dev == dev && e.st == st) {
+      if (e.bytes < bytes) {
+        void* q = nullptr;
+        QBG_TRY(dmalloc(&q, bytes));
+        dfree(e.p, st);
+        e.p = q;
+        e.bytes = bytes;
+      }
+      *out = e.p;
+      return QBG_OK;
+    }
+  void* q = nullptr;
+  QBG_TRY(dmalloc(&q, bytes));
+  g_pack.push_back({dev, st, q, bytes});
+  *out = q;
+  return QBG_OK;
+}
 }  // namespace
 
 int tc_error_ptr(int** p) { return tc_device_setup(p); }
 
-void set_gemm_engine(int e) { g_engine.store(e == GEMM_ENGINE_SIMT ? GEMM_ENGINE_SIMT : GEMM_ENGINE_TCGEN05); }
+void tc_release_scratch(cudaStream_t st) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  std::lock_guard<std::mutex> lk(g_pack_mu);
+  for (size_t q = 0; q < g_pack.size(); ++q)
+    if (g_pack[q].dev == dev && g_pack[q].st == st) {
+      dfree(g_pack[q].p, st);
+      g_pack.erase(g_pack.begin() + (long)q);
+      return;
+    }
+}
+
+void set_gemm_engine(int e) {
+  g_engine.store(e == GEMM_ENGINE_SIMT ? GEMM_ENGINE_SIMT : GEMM_ENGINE_TCGEN05);
+  g_pk_enabled.store(e != GEMM_ENGINE_TCGEN05_STAGED);
+}
 int gemm_engine() { return g_engine.load(); }
 
 int tc_gemm_c64(int M, int N, int K, cxf alpha, const cxf* A, long long lda, long long sA, const cxf* B,
                 long long ldb, long long sB, cxf beta, cxf* C, long long ldc, long long sC, int batch,
-                cudaStream_t st, int batch2, long long sA2, long long sB2, long long sC2) {
+                cudaStream_t st, int batch2, long long sA2, long long sB2, long long sC2, bool allow_packed) {
   if (M <= 0 || N <= 0 || batch <= 0 || batch2 <= 0) return QBG_OK;
   if (K <= 0 || (long long)batch * batch2 > 65535) {
     set_error("tc_gemm_c64: K = %d, batch = %d x %d out of range", K, batch, batch2);
@@ -358,7 +655,28 @@ int tc_gemm_c64(int M, int N, int K, cxf alpha, const cxf* A, long long lda, lon
   }
   int* derr = nullptr;
   if (int s = tc_device_setup(&derr)) return s;
-  dim3 grd((M + TC_BM - 1) / TC_BM, (N + TC_BN - 1) / TC_BN, batch * batch2);
+  const int MT = (M + TC_BM - 1) / TC_BM, NT = (N + TC_BN - 1) / TC_BN, KT = (K + TC_BK - 1) / TC_BK;
+  const int nb = batch * batch2;
+  // packed path where packing pays: each packed A tile is read by NT CTAs and
+  // each B tile by MT CTAs (measured on the FP32 LU of 48 operators of
+  // N = 2048: faster from the 512 x 512 trailing updates up; the skinny solve
+  // products, N = 64, and the updates inside an outer block are faster staged)
+  if (allow_packed && g_pk_enabled.load() && KT >= 2 && MT >= 4 && NT >= 8) {
+    const size_t pa = (size_t)nb * MT * KT * PK_A_TILE, pb = (size_t)nb * NT * KT * PK_B_TILE;
+    void* scr = nullptr;
+    QBG_TRY(pack_scratch(st, sizeof(float) * (pa + pb), &scr));
+    float* PA = static_cast<float*>(scr);
+    float* PB = PA + pa;
+    k_tc_pack_a<<<dim3(MT, KT, nb), 128, 0, st>>>(A, lda, sA, sA2, batch2, M, K, PA);
+    QBG_LAUNCH_CHECK("k_tc_pack_a");
+    k_tc_pack_b<<<dim3(NT, KT, nb), 128, 0, st>>>(B, ldb, sB, sB2, batch2, N, K, PB);
+    QBG_LAUNCH_CHECK("k_tc_pack_b");
+    k_tc_cgemm_pk<<<dim3(MT, NT, nb), 128, pk_smem_bytes(), st>>>(M, N, KT, alpha, PA, PB, beta, C, ldc, sC, batch2,
+                                                                   sC2, derr);
+    QBG_LAUNCH_CHECK("k_tc_cgemm_pk");
+    return QBG_OK;
+  }
+  dim3 grd(MT, NT, nb);
   k_tc_cgemm<<<grd, 128, tc_smem_bytes(), st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch2,
                                                  sA2, sB2, sC2, derr);
   QBG_LAUNCH_CHECK("k_tc_cgemm");

@@ -98,10 +98,13 @@ def main(argv=None):
     ap.add_argument("--L", type=int, default=64)
     ap.add_argument("--form", default="mixed", choices=["fp64", "mixed", "fp32"])
     ap.add_argument("--direct", action="store_true", help="direct Hankel evaluation instead of Chebyshev panels")
+    ap.add_argument("--gemm-engine", type=int, default=1, choices=[0, 1, 2],
+                    help="complex64 GEMM engine of the FP32 LU and solves (qbg_set_gemm_engine)")
     a = ap.parse_args(argv)
     import build_qbgpu
     build_qbgpu.build()
     import qbgpu as qb
+    qb.set_gemm_engine(a.gemm_engine)
     if a.case == "disks":
         return disks_case(qb, a)
     if a.case == "large":

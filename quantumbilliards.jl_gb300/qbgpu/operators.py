@@ -322,7 +322,8 @@ def pool_stats() -> dict:
 
 
 def set_gemm_engine(engine: int) -> None:
-    """Engine of the complex64 GEMMs in the FP32 LU and solves (0 FMA tiles, 1 tcgen05)."""
+    """Engine of the complex64 GEMMs in the FP32 LU and solves: 0 FMA tiles, 1 tcgen05 with
+    packed operand tiles (default), 2 tcgen05 with operands split in registers."""
     L.check(L.load().qbg_set_gemm_engine(int(engine)))
 
 

@@ -1,5 +1,7 @@
-"""Complex64 GEMM engines of the FP32 LU: tcgen05 tensor cores (3xTF32) and
-CUDA-core FMA tiles, against a complex128 NumPy product of the same inputs.
+"""Complex64 GEMM engines of the FP32 LU: tcgen05 tensor cores (3xTF32) with
+packed operand tiles streamed by bulk copies (engine 1) or with operands split
+in registers (engine 2), and CUDA-core FMA tiles (engine 0), against a
+complex128 NumPy product of the same inputs.
 
 Tolerance: |C - C_ref| <= 4e-6 * (|alpha| |A| |B| + |beta| |C0|) elementwise,
 i.e. FP32-class accuracy (unit roundoff 6e-8 times a K-term accumulation).
@@ -21,11 +23,13 @@ SHAPES = [
     (64, 64, 64, 3),     # triangular-solve update shape
     (1984, 1984, 64, 2), # LU trailing update at n = 2048, nb = 64
     (2048, 64, 2048, 1), # refinement product T X
+    (1792, 1792, 256, 2),# LU trailing update of an outer block (K = 256)
+    (257, 33, 17, 3),    # ragged everywhere, KT = 2
 ]
 
 
 @pytest.mark.parametrize("M,N,K,batch", SHAPES)
-@pytest.mark.parametrize("engine", [1, 0])
+@pytest.mark.parametrize("engine", [1, 2, 0])
 def test_cgemm_engines(qb, M, N, K, batch, engine):
     rng = np.random.default_rng(M * 7 + N * 3 + K + batch)
     A, B, C0 = _rand(rng, (batch, M, K)), _rand(rng, (batch, K, N)), _rand(rng, (batch, M, N))
@@ -58,7 +62,7 @@ def test_beyn_mixed_same_eigenvalues_both_engines(qb):
     sel = lambda l: np.sort_complex(l[qb.beyn.inside(l, 40.0, 0.5) & (np.abs(l.imag) < 1e-6)])
     res = {}
     try:
-        for eng in (0, 1):
+        for eng in (0, 1, 2):
             qb.set_gemm_engine(eng)
             lam = qb.solve(sol, pts, 40.0 + 0j, 0.5, nq=24, r=24, svd_tol=1e-12, rng=np.random.default_rng(3),
                            mixed=True, ws=ws)
@@ -68,8 +72,8 @@ def test_beyn_mixed_same_eigenvalues_both_engines(qb):
     plain = qb.solve(sol, pts, 40.0 + 0j, 0.5, nq=24, r=24, svd_tol=1e-12, rng=np.random.default_rng(3),
                      mixed=False, ws=ws)
     plain = sel(plain)
-    assert len(res[0]) == len(res[1]) == len(plain) > 0
-    for eng in (0, 1):
+    assert len(res[0]) == len(res[1]) == len(res[2]) == len(plain) > 0
+    for eng in (0, 1, 2):
         assert np.max(np.abs(res[eng] - plain) / np.abs(plain)) < 1e-10, eng
 
 
