@@ -1,7 +1,7 @@
 """Complex64 GEMM engines of the FP32 LU: tcgen05 tensor cores (3xTF32) with
-packed operand tiles streamed by bulk copies (engine 1) or with operands split
-in registers (engine 2), and CUDA-core FMA tiles (engine 0), against a
-complex128 NumPy product of the same inputs.
+packed operand tiles streamed by bulk copies for large products (engine 1) or
+with operands split in registers (engine 2), and CUDA-core FMA tiles (engine
+0), against a complex128 NumPy product of the same inputs.
 
 Tolerance: |C - C_ref| <= 4e-6 * (|alpha| |A| |B| + |beta| |C0|) elementwise,
 i.e. FP32-class accuracy (unit roundoff 6e-8 times a K-term accumulation).
@@ -25,6 +25,9 @@ SHAPES = [
     (2048, 64, 2048, 1), # refinement product T X
     (1792, 1792, 256, 2),# LU trailing update of an outer block (K = 256)
     (257, 33, 17, 3),    # ragged everywhere, KT = 2
+    (1000, 40, 334, 3),  # ragged rows and columns, k tail of one pair
+    (512, 64, 512, 2),   # triangular-solve product shape
+    (640, 1, 96, 1),     # one column
 ]
 
 
