@@ -98,8 +98,8 @@ void tc_release_scratch(cudaStream_t st);
 // qbg_tc_resid.cu). The digit planes of the operators T = hi + lo are built
 // once per factorisation; each residual splits X and forms R = V - T X.
 struct TcResidT {
-  int n = 0, batch = 0, Kp = 0;
-  void* TD = nullptr;   // bf16 digit planes
+  int n = 0, batch = 0, MT = 0, KS = 0;  // 128-row tiles, 16-real-k stages
+  void* TD = nullptr;   // bf16 digit planes, laid out as the kernel's stage images
   int* erow = nullptr;  // row exponents
 };
 size_t tc_resid_T_bytes(int n, int batch);

@@ -23,15 +23,21 @@
 // GEMM kernel: A' rows interleave (Re, Im) along k, B' rows are (Re, -Im) for
 // the real part of an output column and (Im, Re) for its imaginary part.
 //
-// Layouts (bf16, row-major, K padded to Kp, a multiple of 32, with zeros):
-//   T digits  [node][a][i][Kp]          (i < n)
-//   X digits  [node][b][j][Kp]          (j < Lp: real-part rows, Lp + j: imaginary-part rows)
+// Layouts (bf16): the digit planes are written as the shared-memory images of
+// the kernel's stages, so that a stage is two bulk copies. Stage ks covers 16
+// real k (8 complex k); a plane image of R rows holds R x 16 bf16 in the
+// canonical K-major no-swizzle layout (8-row x 16-byte core matrices, the two
+// along k 128 B apart, 8-row groups 256 B apart):
+//   T tile (node, 128-row tile mt, ks): planes a = 1..7 of 128 rows (28 KB)
+//   X tile (node, 32-column tile nt, ks): planes b = 1..7 of 64 B' rows (14 KB)
 // One CTA (128 threads) owns 128 rows x 32 complex columns of R: 7 levels x
-// 64 FP32 TMEM columns. Operands stream through two shared-memory stages of
-// 32 real k (84 KB each) by cp.async; thread 0 issues the 28 x 2 MMAs of a
-// stage and commits them to the stage's mbarrier. Every mbarrier wait is
-// bounded (1e9 SM cycles): on timeout the CTA records an error, waits
-// (bounded) for its own MMAs, frees its TMEM and returns without writing R.
+// 64 FP32 TMEM columns. Thread 0 streams the stages through a four-stage
+// ring (full / empty mbarriers, cp.async.bulk) and issues the 28 MMAs of a
+// stage (K = 16 each); every 32 stages (512 real k) it waits for the MMAs and
+// all threads add the level sums into their double-float accumulators. Every
+// wait is bounded (1e9 SM cycles): on a timeout the CTA records an error,
+// waits (bounded) for the copies and MMAs it started, frees its TMEM and
+// returns without writing R.
 #include <cstdint>
 #include <cuda_bf16.h>
 #include "qbg_common.cuh"
@@ -44,13 +50,14 @@ constexpr int RD = 7;                 // digits per operand
 constexpr int RLEV = 7;               // levels g = 2..8
 constexpr int RBM = 128;              // rows of R per CTA
 constexpr int RBN = 32;               // complex columns of R per CTA (B' rows: 64)
-constexpr int RKS = 32;               // real k per stage (2 MMA k-steps of 16)
-constexpr int RCHUNK = 16;            // stages between exact flushes (512 real k)
-constexpr int RA_STEP = RBM * 16 * 2;           // bytes of one A plane per k-step (4096)
-constexpr int RB_STEP = 2 * RBN * 16 * 2;       // bytes of one B plane per k-step (2048)
-constexpr int RA_STAGE = RD * 2 * RA_STEP;      // 57344
-constexpr int RB_STAGE = RD * 2 * RB_STEP;      // 28672
-constexpr int RSTAGE = RA_STAGE + RB_STAGE;     // 86016
+constexpr int RKS = 16;               // real k per stage (one MMA k-step)
+constexpr int RCHUNK = 32;            // stages between exact flushes (512 real k)
+constexpr int RNST = 4;               // stages in the ring
+constexpr int RA_PLANE = RBM * RKS * 2;         // bytes of one T plane image (4096)
+constexpr int RB_PLANE = 2 * RBN * RKS * 2;     // bytes of one X plane image (2048)
+constexpr int RA_TILE = RD * RA_PLANE;          // 28672
+constexpr int RB_TILE = RD * RB_PLANE;          // 14336
+constexpr int RSTAGE = RA_TILE + RB_TILE;       // 43008
 constexpr uint32_t RTMEM_COLS = 512;
 constexpr long long RSPIN = 1ll << 26;
 // D f32, A/B bf16, K-major, N = 64, M = 128
@@ -94,9 +101,21 @@ __device__ __forceinline__ bool r_wait(uint32_t mbar, uint32_t parity) {
   return false;
 }
 
-// 16-byte global -> shared copy; src_bytes = 0 fills zeros without reading
-__device__ __forceinline__ void r_cp16(uint32_t dst, const void* src, uint32_t src_bytes) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+
+// byte offset of (row, real k kl < 16) inside a plane image (canonical K-major)
+__device__ __forceinline__ uint32_t img_off(int row, int kl) {
+  return (uint32_t)((row >> 3) * 256 + (kl >> 3) * 128 + (row & 7) * 16 + (kl & 7) * 2);
+}
+
+__device__ __forceinline__ void r_expect(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void r_bulk(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(mbar)
+      : "memory");
 }
 
 // exact df32 accumulation of one FP32 value
@@ -201,9 +220,11 @@ __global__ void k_t_rowexp(const cxf* __restrict__ Th, const cxf* __restrict__ T
 }
 
 // T digit planes through a 32 x 32 shared-memory transpose (column-major in,
-// row-major out); grid (n/32, n/32, batch), block (32, 8)
-__global__ void k_t_digits(const cxf* __restrict__ Th, const cxf* __restrict__ Tl, long long sT, int n, int Kp,
-                           const int* __restrict__ erow, __nv_bfloat16* __restrict__ TD) {
+// stage images out); grid (n/32, n/32, batch), block (32, 8). Each warp
+// writes 128 contiguous bytes per plane: 8 rows x 4 complex k of one
+// 16-byte core-matrix column.
+__global__ void k_t_digits(const cxf* __restrict__ Th, const cxf* __restrict__ Tl, long long sT, int n, int MT,
+                           int KS, const int* __restrict__ erow, unsigned char* __restrict__ TD) {
   __shared__ cxf th[32][33], tl[32][33];  // [column][row]
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
@@ -223,11 +244,15 @@ __global__ void k_t_digits(const cxf* __restrict__ Th, const cxf* __restrict__ T
     tl[c][tx] = vl;
   }
   __syncthreads();
+  const int t = ty * 32 + tx;
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
-    const int row = ty + 8 * r, i = i0 + row, k = k0 + tx;
+    const int w = t + 256 * r;
+    const int e4 = w & 3, rr = (w >> 2) & 7, rg = (w >> 5) & 3, cs = w >> 7;  // cs: (stage, core column)
+    const int il = rg * 8 + rr, kloc = (cs >> 1) * 8 + (cs & 1) * 4 + e4;
+    const int i = i0 + il, k = k0 + kloc;
     if (i >= n || k >= n) continue;
-    const cxf vh = th[tx][row], vl = tl[tx][row];
+    const cxf vh = th[kloc][il], vl = tl[kloc][il];
     const int e = erow[b * n + i];
     float dr[RD], di[RD];
     if (e == R_NONFINITE) {
@@ -238,12 +263,13 @@ __global__ void k_t_digits(const cxf* __restrict__ Th, const cxf* __restrict__ T
       digits7(fx_f32(vh.re, Q) + fx_f32(vl.re, Q), dr);
       digits7(fx_f32(vh.im, Q) + fx_f32(vl.im, Q), di);
     }
+    unsigned char* tile = TD + ((b * MT + (i >> 7)) * (long long)KS + (k >> 3)) * RA_TILE + img_off(i & 127, (2 * k) & 15);
 #pragma unroll
     for (int a = 0; a < RD; ++a) {
       __nv_bfloat162 p;
       p.x = __float2bfloat16_rn(dr[a]);
       p.y = __float2bfloat16_rn(di[a]);
-      *reinterpret_cast<__nv_bfloat162*>(TD + (((b * RD + a) * n + i) * (long long)Kp + 2 * (long long)k)) = p;
+      *reinterpret_cast<__nv_bfloat162*>(tile + a * RA_PLANE) = p;
     }
   }
 }
@@ -284,10 +310,11 @@ __global__ void k_x_colexp(const cxd* __restrict__ X, long long sX, int n, int L
   }
 }
 
-// X digit planes in the B' layout: row l = (Re, -Im), row Lp + l = (Im, Re)
-// of column l along k; columns l in [L, Lp) are zero. grid (n/256, Lp, batch)
-__global__ void k_x_digits(const cxd* __restrict__ X, long long sX, int n, int L, int Lp, int Kp,
-                           const int* __restrict__ fcol, __nv_bfloat16* __restrict__ XD) {
+// X digit planes as stage images: column l of tile nt = l / 32 gives B' rows
+// j = l % 32 (Re, -Im) and 32 + j (Im, Re) along k; columns l in [L, Lp) are
+// zero. grid (n/256, Lp, batch)
+__global__ void k_x_digits(const cxd* __restrict__ X, long long sX, int n, int L, int NT, int KS,
+                           const int* __restrict__ fcol, unsigned char* __restrict__ XD) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int l = blockIdx.y;
   const long long b = blockIdx.z;
@@ -302,6 +329,9 @@ __global__ void k_x_digits(const cxd* __restrict__ X, long long sX, int n, int L
     digits7(fx_f64(v.re, 49 - f), dr);
     digits7(fx_f64(v.im, 49 - f), di);
   }
+  const int j = l & (RBN - 1);
+  unsigned char* tile = XD + ((b * NT + (l / RBN)) * (long long)KS + (k >> 3)) * RB_TILE;
+  const uint32_t o_re = img_off(j, (2 * k) & 15), o_im = img_off(RBN + j, (2 * k) & 15);
 #pragma unroll
   for (int a = 0; a < RD; ++a) {
     __nv_bfloat162 pr, pi;
@@ -309,31 +339,31 @@ __global__ void k_x_digits(const cxd* __restrict__ X, long long sX, int n, int L
     pr.y = __float2bfloat16_rn(-di[a]);
     pi.x = __float2bfloat16_rn(di[a]);
     pi.y = __float2bfloat16_rn(dr[a]);
-    const long long base = (b * RD + a) * 2LL * Lp;
-    *reinterpret_cast<__nv_bfloat162*>(XD + ((base + l) * Kp + 2LL * k)) = pr;
-    *reinterpret_cast<__nv_bfloat162*>(XD + ((base + Lp + l) * Kp + 2LL * k)) = pi;
+    *reinterpret_cast<__nv_bfloat162*>(tile + a * RB_PLANE + o_re) = pr;
+    *reinterpret_cast<__nv_bfloat162*>(tile + a * RB_PLANE + o_im) = pi;
   }
 }
 
 // ---------------------------------------------------------------------------
 // R = V - T X from the digit planes; grid (Lp / 32, ceil(n / 128), batch)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128, 1) k_resid_tc(const __nv_bfloat16* __restrict__ TD,
+__global__ void __launch_bounds__(128, 1) k_resid_tc(const unsigned char* __restrict__ TD,
                                                      const int* __restrict__ erow,
-                                                     const __nv_bfloat16* __restrict__ XD,
-                                                     const int* __restrict__ fcol, int n, int L, int Lp, int Kp,
+                                                     const unsigned char* __restrict__ XD,
+                                                     const int* __restrict__ fcol, int n, int L, int MT, int NT, int KS,
                                                      const cxd* __restrict__ V, long long sV, cxd* R, long long sR,
                                                      unsigned long long* rmax, int* err) {
   extern __shared__ __align__(1024) unsigned char r_smem[];
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(r_smem + 2 * RSTAGE);  // [2]
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 2);
+  uint64_t* full = reinterpret_cast<uint64_t*>(r_smem + RNST * RSTAGE);  // [RNST]
+  uint64_t* empty = full + RNST;                                         // [RNST]
+  uint64_t* fbar = empty + RNST;                                         // [1]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(fbar + 1);
   int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
 
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int n0 = blockIdx.x * RBN, m0 = blockIdx.y * RBM;
-  const long long b = blockIdx.z;
-  const __nv_bfloat16* Tb = TD + b * (long long)RD * n * Kp;
-  const __nv_bfloat16* Xb = XD + b * (long long)RD * 2 * Lp * Kp;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int nt = blockIdx.x, mt = blockIdx.y;
+  const long long z = blockIdx.z;
+  const int n0 = nt * RBN, m0 = mt * RBM;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(r_smem_u32(tmem_slot)),
@@ -342,8 +372,11 @@ __global__ void __launch_bounds__(128, 1) k_resid_tc(const __nv_bfloat16* __rest
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(r_smem_u32(mbar)) : "memory");
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(r_smem_u32(mbar + 1)) : "memory");
+    for (int s = 0; s < RNST; ++s) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(r_smem_u32(full + s)) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(r_smem_u32(empty + s)) : "memory");
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(r_smem_u32(fbar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     *abort_flag = (*reinterpret_cast<volatile int*>(err) != 0) ? 1 : 0;
   }
@@ -351,143 +384,122 @@ __global__ void __launch_bounds__(128, 1) k_resid_tc(const __nv_bfloat16* __rest
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const uint32_t mb0 = r_smem_u32(mbar), mb1 = r_smem_u32(mbar + 1);
   const uint32_t sbase = r_smem_u32(r_smem);
-
-  // cp.async of one stage: T digits (7 planes x 128 rows x 4 chunks of 8 k) and
-  // X digits (7 planes x 64 B' rows x 4 chunks) into the canonical K-major layout
-  auto load_stage = [&](int kt, int st) {
-    const uint32_t so = sbase + (uint32_t)st * RSTAGE;
-    const long long k0 = (long long)kt * RKS;
-#pragma unroll 4
-    for (int it = 0; it < (RD * RBM * 4) / 128; ++it) {
-      const int q = tid + 128 * it;
-      const int kc = q & 3, row = (q >> 2) & (RBM - 1), a = q >> 9;
-      const int gi = m0 + row;
-      const bool ok = gi < n;
-      const __nv_bfloat16* src = Tb + ((long long)a * n + (ok ? gi : 0)) * Kp + k0 + 8 * kc;
-      const uint32_t dst = so + (uint32_t)((a * 2 + (kc >> 1)) * RA_STEP + (row >> 3) * 256 + (kc & 1) * 128 +
-                                           (row & 7) * 16);
-      r_cp16(dst, src, ok ? 16u : 0u);
-    }
-#pragma unroll 2
-    for (int it = 0; it < (RD * 2 * RBN * 4) / 128; ++it) {
-      const int q = tid + 128 * it;
-      const int kc = q & 3, row = (q >> 2) & (2 * RBN - 1), a = q >> 8;
-      const int gj = row < RBN ? n0 + row : Lp + n0 + row - RBN;
-      const __nv_bfloat16* src = Xb + ((long long)a * 2 * Lp + gj) * Kp + k0 + 8 * kc;
-      const uint32_t dst = so + RA_STAGE +
-                           (uint32_t)((a * 2 + (kc >> 1)) * RB_STEP + (row >> 3) * 256 + (kc & 1) * 128 + (row & 7) * 16);
-      r_cp16(dst, src, 16u);
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
-  };
 
   float acc_hi[2 * RBN], acc_lo[2 * RBN];
 #pragma unroll
   for (int c = 0; c < 2 * RBN; ++c) { acc_hi[c] = 0.f; acc_lo[c] = 0.f; }
 
-  uint32_t wph0 = 0u, wph1 = 0u;
-  bool pend0 = false, pend1 = false;
-  bool ok = (*abort_flag == 0);
-  const int ktiles = Kp / RKS;
-  uint32_t started = 0u;  // thread 0: levels whose accumulator holds this chunk's sum (bit g - 2)
+  // thread 0: producer and MMA issuer
+  const unsigned char* ta = TD + (z * MT + mt) * (long long)KS * RA_TILE;
+  const unsigned char* xb = XD + (z * NT + nt) * (long long)KS * RB_TILE;
+  int issued = 0, consumed = 0, committed = 0, freed = 0;
+  bool good = (*abort_flag == 0);
+  auto issue = [&](int t) {
+    const int s = t % RNST;
+    const uint32_t fb = r_smem_u32(full + s);
+    r_expect(fb, (uint32_t)RSTAGE);
+    r_bulk(sbase + (uint32_t)(s * RSTAGE), ta + (long long)t * RA_TILE, (uint32_t)RA_TILE, fb);
+    r_bulk(sbase + (uint32_t)(s * RSTAGE + RA_TILE), xb + (long long)t * RB_TILE, (uint32_t)RB_TILE, fb);
+  };
+  if (tid == 0 && good)
+    for (; issued < KS && issued < RNST; ++issued) issue(issued);
 
-  if (ok) load_stage(0, 0);
-  for (int kt = 0; kt < ktiles && ok; ++kt) {
-    const int st = kt & 1;
-    if (kt + 1 < ktiles) {
-      // the other stage was read by the MMAs of tile kt - 1
-      if (st ? pend0 : pend1) {
-        if (r_wait(st ? mb0 : mb1, st ? wph0 : wph1)) {
-          if (st) { wph0 ^= 1u; pend0 = false; } else { wph1 ^= 1u; pend1 = false; }
-        } else {
-          atomicExch(abort_flag, 1);
+  const int nch = (KS + RCHUNK - 1) / RCHUNK;
+  for (int ch = 0; ch < nch; ++ch) {
+    if (tid == 0 && good) {
+      uint32_t started = 0u;  // levels whose accumulator holds this chunk's sum (bit g - 2)
+      const int k1 = min(KS, (ch + 1) * RCHUNK);
+      for (int kt = ch * RCHUNK; kt < k1; ++kt) {
+        const int s = kt % RNST;
+        if (!r_wait(r_smem_u32(full + s), (uint32_t)((kt / RNST) & 1))) {
+          good = false;
+          break;
         }
-      }
-      load_stage(kt + 1, st ^ 1);
-      asm volatile("cp.async.wait_group 1;" ::: "memory");
-    } else {
-      asm volatile("cp.async.wait_group 0;" ::: "memory");
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (*abort_flag) { ok = false; break; }
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t so = sbase + (uint32_t)st * RSTAGE;
-#pragma unroll
-      for (int ks = 0; ks < 2; ++ks) {
+        ++consumed;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t so = sbase + (uint32_t)(s * RSTAGE);
 #pragma unroll
         for (int a = 1; a <= RD; ++a) {
-          const uint64_t da = r_desc(so + (uint32_t)(((a - 1) * 2 + ks) * RA_STEP));
+          const uint64_t da = r_desc(so + (uint32_t)((a - 1) * RA_PLANE));
 #pragma unroll
           for (int bq = 1; bq + a <= RLEV + 1; ++bq) {
             const int g = a + bq;  // 2 .. 8
-            const uint64_t db = r_desc(so + RA_STAGE + (uint32_t)(((bq - 1) * 2 + ks) * RB_STEP));
+            const uint64_t db = r_desc(so + (uint32_t)(RA_TILE + (bq - 1) * RB_PLANE));
             const uint32_t bit = 1u << (g - 2);
             r_mma(tmem + (uint32_t)((g - 2) * 2 * RBN), da, db, (started & bit) ? 1u : 0u);
             started |= bit;
           }
         }
-      }
-      r_commit(st ? mb1 : mb0);
-    }
-    if (st) pend1 = true; else pend0 = true;
-    if ((kt + 1) % RCHUNK == 0 || kt + 1 == ktiles) {
-      // every MMA so far completes before the exact level sums are read back
-      bool good = true;
-      if (pend0) { if (r_wait(mb0, wph0)) { wph0 ^= 1u; pend0 = false; } else good = false; }
-      if (pend1) { if (r_wait(mb1, wph1)) { wph1 ^= 1u; pend1 = false; } else good = false; }
-      if (!good) atomicExch(abort_flag, 1);
-      // the warp-synchronous TMEM loads run only on a CTA-wide decision
-      __syncthreads();
-      const bool flush = (*abort_flag == 0);
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      if (flush) {
-        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-#pragma unroll 1
-        for (int lev = 0; lev < RLEV; ++lev) {
-          const float sc = ldexpf(1.f, -7 * (lev + 2));
-#pragma unroll
-          for (int qt = 0; qt < 4; ++qt) {
-            uint32_t v[16];
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                  "=r"(v[15])
-                : "r"(taddr + (uint32_t)(lev * 2 * RBN + qt * 16)));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-            for (int c = 0; c < 16; ++c) df_add(acc_hi[qt * 16 + c], acc_lo[qt * 16 + c], __uint_as_float(v[c]) * sc);
+        r_commit(r_smem_u32(empty + s));
+        ++committed;
+        // refill the stage of tile kt - 1 once its MMAs are done
+        if (kt >= 1 && issued < KS) {
+          const int t = kt - 1;
+          if (!r_wait(r_smem_u32(empty + t % RNST), (uint32_t)((t / RNST) & 1))) {
+            good = false;
+            break;
           }
+          ++freed;
+          issue(issued);
+          ++issued;
         }
       }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();
-      if (tid == 0) started = 0u;  // the next chunk restarts every level
-      if (*abort_flag) { ok = false; break; }
+      // every MMA of the chunk completes before the exact level sums are read back
+      if (good) {
+        r_commit(r_smem_u32(fbar));
+        if (!r_wait(r_smem_u32(fbar), (uint32_t)(ch & 1))) good = false;
+      }
+      if (!good) *abort_flag = 1;
     }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const bool flush = (*abort_flag == 0);
+    if (flush) {
+      __syncwarp();
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+      for (int lev = 0; lev < RLEV; ++lev) {
+        const float sc = ldexpf(1.f, -7 * (lev + 2));
+#pragma unroll
+        for (int qt = 0; qt < 4; ++qt) {
+          uint32_t v[16];
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+              : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                "=r"(v[15])
+              : "r"(taddr + (uint32_t)(lev * 2 * RBN + qt * 16)));
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int c = 0; c < 16; ++c) df_add(acc_hi[qt * 16 + c], acc_lo[qt * 16 + c], __uint_as_float(v[c]) * sc);
+        }
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (*abort_flag) break;
   }
-  if (!ok) {
-    if (tid == 0) atomicExch(err, 1);
-    if (pend0) r_wait(mb0, wph0);
-    if (pend1) r_wait(mb1, wph1);
-    asm volatile("cp.async.wait_group 0;" ::: "memory");
-  } else {
+  if (tid == 0 && *abort_flag) {
+    atomicExch(err, 1);
+    // bounded drain of what this thread started: copies, then MMA groups
+    for (int t = consumed; t < issued; ++t) r_wait(r_smem_u32(full + t % RNST), (uint32_t)((t / RNST) & 1));
+    for (int t = freed; t < committed; ++t) r_wait(r_smem_u32(empty + t % RNST), (uint32_t)((t / RNST) & 1));
+  }
+  if (*abort_flag == 0) {
     const int i = m0 + tid;
     if (i < n) {
-      const int ei = erow[b * n + i];
-      const cxd* Vb = V + b * sV;
-      cxd* Rb = R + b * sR;
+      const int ei = erow[z * n + i];
+      const cxd* Vb = V + z * sV;
+      cxd* Rb = R + z * sR;
       double lmax = 0.0;
       bool bad = false;
 #pragma unroll
       for (int c = 0; c < RBN; ++c) {
         const int col = n0 + c;
         if (col >= L) continue;  // full unroll keeps the sums in registers
-        const int f = fcol[b * L + col];
+        const int f = fcol[z * L + col];
         const long long e = (long long)i + (long long)col * n;
         const cxd v = Vb[e];
         cxd r;
@@ -519,22 +531,25 @@ __global__ void __launch_bounds__(128, 1) k_resid_tc(const __nv_bfloat16* __rest
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-static int kp_of(int n) { return ((2 * n + RKS - 1) / RKS) * RKS; }
+static int ks_of(int n) { return (2 * n + RKS - 1) / RKS; }
+static int mt_of(int n) { return (n + RBM - 1) / RBM; }
 static int lp_of(int L) { return ((L + RBN - 1) / RBN) * RBN; }
+static size_t r_smem_bytes() { return (size_t)RNST * RSTAGE + 128; }
 
 size_t tc_resid_T_bytes(int n, int batch) {
-  const size_t dig = (size_t)batch * RD * n * kp_of(n) * sizeof(__nv_bfloat16);
+  const size_t dig = (size_t)batch * mt_of(n) * ks_of(n) * RA_TILE;
   return ((dig + 255) & ~(size_t)255) + (size_t)batch * n * sizeof(int);
 }
 
 int tc_resid_bind_T(TcResidT& t, int n, int batch, void* mem, cudaStream_t st) {
   t.n = n;
   t.batch = batch;
-  t.Kp = kp_of(n);
-  const size_t dig = (size_t)batch * RD * n * t.Kp * sizeof(__nv_bfloat16);
+  t.MT = mt_of(n);
+  t.KS = ks_of(n);
+  const size_t dig = (size_t)batch * t.MT * t.KS * RA_TILE;
   t.TD = mem;
   t.erow = reinterpret_cast<int*>(static_cast<unsigned char*>(mem) + ((dig + 255) & ~(size_t)255));
-  // the k padding of every digit row stays zero
+  // rows beyond n and k beyond n stay zero in every image
   QBG_CUDA(cudaMemsetAsync(mem, 0, tc_resid_T_bytes(n, batch), st));
   return QBG_OK;
 }
@@ -547,42 +562,43 @@ int tc_resid_prepare_T(TcResidT& t, const cxf* Th, const cxf* Tl, long long sT, 
   const int n = t.n;
   k_t_rowexp<<<dim3((n + 31) / 32, c), dim3(32, 8), 0, st>>>(Th, Tl, sT, n, t.erow);
   QBG_LAUNCH_CHECK("k_t_rowexp");
-  k_t_digits<<<dim3((n + 31) / 32, (n + 31) / 32, c), dim3(32, 8), 0, st>>>(Th, Tl, sT, n, t.Kp, t.erow, static_cast<__nv_bfloat16*>(t.TD));
+  k_t_digits<<<dim3((n + 31) / 32, (n + 31) / 32, c), dim3(32, 8), 0, st>>>(
+      Th, Tl, sT, n, t.MT, t.KS, t.erow, static_cast<unsigned char*>(t.TD));
   QBG_LAUNCH_CHECK("k_t_digits");
   return QBG_OK;
 }
 
 size_t tc_resid_X_bytes(int n, int L, int batch) {
-  const size_t dig = (size_t)batch * RD * 2 * lp_of(L) * kp_of(n) * sizeof(__nv_bfloat16);
+  const size_t dig = (size_t)batch * (lp_of(L) / RBN) * ks_of(n) * RB_TILE;
   return ((dig + 255) & ~(size_t)255) + (size_t)batch * L * sizeof(int);
 }
 
 int tc_residual(const TcResidT& t, const cxd* X, long long sX, const cxd* V, long long sV, cxd* R, long long sR,
                 int L, int c, double* rmax, void* xmem, cudaStream_t st) {
-  const int n = t.n, Kp = t.Kp, Lp = lp_of(L);
+  const int n = t.n, Lp = lp_of(L), NT = Lp / RBN;
   if (c > t.batch || c < 1 || c > 65535 || L < 1) {
     set_error("tc_residual: bad sizes");
     return QBG_EINVAL;
   }
-  const size_t dig = (size_t)c * RD * 2 * Lp * Kp * sizeof(__nv_bfloat16);
-  __nv_bfloat16* XD = static_cast<__nv_bfloat16*>(xmem);
-  int* fcol = reinterpret_cast<int*>(static_cast<unsigned char*>(xmem) + ((dig + 255) & ~(size_t)255));
+  const size_t dig = (size_t)c * NT * t.KS * RB_TILE;
+  unsigned char* XD = static_cast<unsigned char*>(xmem);
+  int* fcol = reinterpret_cast<int*>(XD + ((dig + 255) & ~(size_t)255));
   int* derr = nullptr;
   QBG_TRY(tc_error_ptr(&derr));
   static bool attr[64] = {};
   int dev = 0;
   QBG_CUDA(cudaGetDevice(&dev));
-  const size_t smem = 2 * (size_t)RSTAGE + 64;
   if (dev >= 0 && dev < 64 && !attr[dev]) {
-    QBG_CUDA(cudaFuncSetAttribute(k_resid_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    QBG_CUDA(cudaFuncSetAttribute(k_resid_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r_smem_bytes()));
     attr[dev] = true;
   }
   k_x_colexp<<<dim3(L, c), 256, 0, st>>>(X, sX, n, L, fcol);
   QBG_LAUNCH_CHECK("k_x_colexp");
-  k_x_digits<<<dim3((n + 255) / 256, Lp, c), 256, 0, st>>>(X, sX, n, L, Lp, Kp, fcol, XD);
+  k_x_digits<<<dim3((n + 255) / 256, Lp, c), 256, 0, st>>>(X, sX, n, L, NT, t.KS, fcol, XD);
   QBG_LAUNCH_CHECK("k_x_digits");
-  k_resid_tc<<<dim3(Lp / RBN, (n + RBM - 1) / RBM, c), 128, smem, st>>>(
-      static_cast<const __nv_bfloat16*>(t.TD), t.erow, XD, fcol, n, L, Lp, Kp, V, sV, R, sR, reinterpret_cast<unsigned long long*>(rmax), derr);
+  k_resid_tc<<<dim3(NT, t.MT, c), 128, r_smem_bytes(), st>>>(
+      static_cast<const unsigned char*>(t.TD), t.erow, XD, fcol, n, L, t.MT, NT, t.KS, V, sV, R, sR,
+      reinterpret_cast<unsigned long long*>(rmax), derr);
   QBG_LAUNCH_CHECK("k_resid_tc");
   return QBG_OK;
 }
