@@ -10,6 +10,7 @@
 // nodes through them in groups (assemble, factor, solve, accumulate), which
 // bounds the memory at large N at the price of re-assembling per call.
 #include <algorithm>
+#include <cstdlib>
 #include <cusolverDn.h>
 #include <limits>
 #include <cmath>
@@ -47,6 +48,11 @@ struct qbg_beyn {
   int res0 = -1, resn = 0;  // nodes [res0, res0 + resn) are factored in the slots
   std::vector<void*> allocs;
   cudaStream_t st = nullptr;
+  // second stream of the LU and the triangular solves (two halves of the
+  // operator batch run concurrently); QBG_LU_SPLIT=0 in the environment keeps
+  // everything on st (the results are the same either way)
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   double ms_assemble = 0, ms_factor = 0;  // device time of the last load(s)
   int singular = 0;
@@ -63,6 +69,13 @@ struct qbg_beyn {
     dfree(macc1, st);
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
+    if (st2) {
+      cudaStreamSynchronize(st2);
+      tc_release_scratch(st2);
+      cudaStreamDestroy(st2);
+    }
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
     if (st) {
       tc_release_scratch(st);
       cudaStreamDestroy(st);
@@ -91,6 +104,12 @@ int setup_lu(qbg_beyn* b, LUBatch<T>& f, int nb, int solve_levels) {
   QBG_TRY(b->alloc(&f.info, sizeof(int) * f.batch));
   QBG_TRY(b->alloc(&f.Linv, sizeof(cx<T>) * (size_t)f.nblk * nb * nb * f.batch));
   QBG_TRY(b->alloc(&f.Uinv, sizeof(cx<T>) * (size_t)f.nblk * nb * nb * f.batch));
+  // the FP64 LU is bound by the FP64 pipe: a second stream only adds contention
+  if (sizeof(T) == sizeof(float)) {
+    f.st2 = b->st2;
+    f.ev_fork = b->ev_fork;
+    f.ev_join = b->ev_join;
+  }
   if (solve_levels > 0) {
     void* mem = nullptr;
     QBG_TRY(b->alloc(&mem, lu_solve_blocks_bytes<T>(f, solve_levels, 128)));
@@ -421,6 +440,13 @@ qbg_status create_impl(qbg_geom* g, const double* k0s, const double* Rs, int ndi
   if (!s) {
     cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
     if (e != cudaSuccess) s = cuda_status(e, "cudaStreamCreate");
+  }
+  const char* split_env = std::getenv("QBG_LU_SPLIT");
+  if (!s && !(split_env && split_env[0] == '0')) {
+    cudaError_t e = cudaStreamCreateWithFlags(&b->st2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
+    if (e != cudaSuccess) s = cuda_status(e, "second LU stream");
   }
   if (!s) s = setup(b, k0s, Rs);
   if (!s && b->cap == b->nn) s = load(b, 0, b->nn);

@@ -595,7 +595,7 @@ static int build_solve_blocks(const LUBatch<T>& f, cudaStream_t st) {
 }
 
 template <class T>
-int lu_factor(LUBatch<T>& f, cudaStream_t st) {
+static int lu_factor_one(LUBatch<T>& f, cudaStream_t st, cudaEvent_t after_first_panel = nullptr) {
   const int n = f.n, nb = f.nb, batch = f.batch;
   const size_t sm = (size_t)nb * nb * sizeof(cx<T>) * 5 / 4;
   static bool attr_set[2] = {false, false};
@@ -644,6 +644,7 @@ int lu_factor(LUBatch<T>& f, cudaStream_t st) {
       QBG_LAUNCH_CHECK("k_laswp");
       k_trtri<T, false><<<dim3(1, batch), 256, sm, st>>>(f.A, n, f.stride, nb, j0 / nb, f.Linv, f.nblk);
       QBG_LAUNCH_CHECK("k_trtri lower");
+      if (j0 == 0 && after_first_panel) QBG_CUDA(cudaEventRecord(after_first_panel, st));
       const int rin = E - j0 - w;  // columns of this outer block right of the panel
       if (rin > 0) {
         // U12 = inv(L11) A12 and A22 -= L21 U12 on the outer block's columns
@@ -691,7 +692,7 @@ int lu_factor(LUBatch<T>& f, cudaStream_t st) {
 }
 
 template <class T>
-int lu_solve_shared(const LUBatch<T>& f, const cx<T>* V, int L, cx<T>* X, long long strideV, cudaStream_t st) {
+static int lu_solve_one(const LUBatch<T>& f, const cx<T>* V, int L, cx<T>* X, long long strideV, cudaStream_t st) {
   const int n = f.n, nb = f.nb, batch = f.batch;
   const long long sX = (long long)n * L;
   dim3 g((unsigned)(((long long)n * L + 255) / 256), batch);
@@ -1048,7 +1049,70 @@ int axpy_f2d(const cxf* d, cxd* x, long long count, cudaStream_t st) {
   return QBG_OK;
 }
 
+// matrices [b0, b0 + cnt) of a batch as a batch of their own (every
+// per-matrix buffer offset by its allocation stride)
+template <class T>
+static LUBatch<T> lu_view(const LUBatch<T>& f, int b0, int cnt) {
+  LUBatch<T> v = f;
+  v.batch = cnt;
+  v.st2 = nullptr;
+  const long long b = b0;
+  v.A = f.A + b * f.stride;
+  v.ipiv = f.ipiv + b * f.n;
+  v.perm = f.perm + b * f.n;
+  v.info = f.info + b;
+  const long long sinv = (long long)f.nblk * f.nb * f.nb;
+  v.Linv = f.Linv + b * sinv;
+  v.Uinv = f.Uinv + b * sinv;
+  if (f.levels > 0) {
+    const long long mid = f.levels == 2 ? (long long)((f.nblk + 1) / 2) * (2 * f.nb) * (2 * f.nb) : 0;
+    const long long fin = (long long)f.nblks * f.nbs * f.nbs;
+    const long long w = (long long)((f.nblk + 1) / 2) * (f.nbs / 2) * (f.nbs / 2);
+    if (f.Linv_mid) v.Linv_mid = f.Linv_mid + b * mid;
+    if (f.Uinv_mid) v.Uinv_mid = f.Uinv_mid + b * mid;
+    v.Linv2 = f.Linv2 + b * fin;
+    v.Uinv2 = f.Uinv2 + b * fin;
+    v.W = f.W + b * w;
+    v.Y = f.Y + b * (long long)f.n * f.ymax_L;
+  }
+  return v;
+}
+
+// With a second stream the two halves of the batch are factored (solved)
+// concurrently: the panel factorisations and the short GEMM chains of one half
+// leave most SMs idle, which the other half's kernels fill. The matrices are
+// independent, so the results are those of one stream.
+template <class T>
+int lu_factor(LUBatch<T>& f, cudaStream_t st) {
+  if (!f.st2 || f.batch < 2) return lu_factor_one<T>(f, st);
+  const int h = f.batch / 2;
+  LUBatch<T> a = lu_view<T>(f, 0, h), b = lu_view<T>(f, h, f.batch - h);
+  // the second half starts one panel behind the first, so that the panels of
+  // one half run under the updates of the other
+  int s = lu_factor_one<T>(a, st, f.ev_fork);
+  QBG_CUDA(cudaStreamWaitEvent(f.st2, f.ev_fork, 0));
+  if (!s) s = lu_factor_one<T>(b, f.st2);
+  QBG_CUDA(cudaEventRecord(f.ev_join, f.st2));
+  QBG_CUDA(cudaStreamWaitEvent(st, f.ev_join, 0));
+  return s;
+}
+
+template <class T>
+int lu_solve_shared(const LUBatch<T>& f, const cx<T>* V, int L, cx<T>* X, long long strideV, cudaStream_t st) {
+  if (!f.st2 || f.batch < 2) return lu_solve_one<T>(f, V, L, X, strideV, st);
+  const int h = f.batch / 2;
+  const LUBatch<T> a = lu_view<T>(f, 0, h), b = lu_view<T>(f, h, f.batch - h);
+  QBG_CUDA(cudaEventRecord(f.ev_fork, st));
+  QBG_CUDA(cudaStreamWaitEvent(f.st2, f.ev_fork, 0));
+  int s = lu_solve_one<T>(a, V, L, X, strideV, st);
+  if (!s) s = lu_solve_one<T>(b, V + (long long)h * strideV, L, X + (long long)h * f.n * L, strideV, f.st2);
+  QBG_CUDA(cudaEventRecord(f.ev_join, f.st2));
+  QBG_CUDA(cudaStreamWaitEvent(st, f.ev_join, 0));
+  return s;
+}
+
 template int lu_factor<double>(LUBatch<double>&, cudaStream_t);
+
 template size_t lu_solve_blocks_bytes<double>(LUBatch<double>&, int, int);
 template size_t lu_solve_blocks_bytes<float>(LUBatch<float>&, int, int);
 template void lu_solve_blocks_bind<double>(LUBatch<double>&, void*);

@@ -28,6 +28,11 @@ struct LUBatch {
   cx<T>* W = nullptr;         // doubling scratch: batch * ceil(nblk / 2) * (nbs / 2)^2
   cx<T>* Y = nullptr;         // solve scratch: batch * n * ymax_L
   int ymax_L = 0;
+  // optional second stream (owned by the caller): lu_factor and lu_solve_shared
+  // then run the two halves of the batch concurrently, forked from and joined
+  // back into the calling stream with these two events
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 // Sets levels/nbs/nblks and returns the device bytes the solve blocks need.
