@@ -320,7 +320,7 @@ static int assemble_impl(qbg_geom* g, const double* ks, int64_t nk, int32_t deri
       std::vector<void*> ctmp;
       ChebTables t;
       s = make_cheb(g, dks + k0, (int)c, *cheb, t, ctmp, st);
-      if (!s && prec != QBG_PREC_FP64 && g->d.m == g->d.n && !deriv) s = make_cheb_df(t, dks + k0, ctmp, st);
+      if (!s && prec != QBG_PREC_FP64 && cheb_df_applies(g->d, deriv)) s = make_cheb_df(t, dks + k0, ctmp, st);
       if (!s)
         s = launch_assemble_cheb(g->d, t, dks + k0, (int)c, deriv, prec, dptrs, split ? dptrs + c : nullptr, dim,
                                  st);

@@ -1245,6 +1245,151 @@ __global__ void __launch_bounds__(512) k_assemble_cheb_sym_df(GeomDev g, ChebTab
   }
 }
 
+// Symmetry-reduced DLP (value, complex64 forms) on double-float arithmetic:
+// one thread per reduced entry (a, b), every node of ks in one pass. Per
+// entry the FP64 geometry, the fold coefficients of the main pair, and for
+// each other orbit member the image coefficient c w_q sc and its panel
+// argument are formed once; per node the premultiplied series (kaL2 H1 on the
+// H table, kaL1 J1 on the J table) are evaluated in FP32 pairs:
+//   F_ab = [1 - w kappa]_(a=b) - (A kaL1 J1 + B kaL2 H1)(r_ij) - sum_images c w_q sc kaL2 H1(r_iq)
+// (dlp_kress.jl:1151-1189 with the images of :1081-1100). Entries with a
+// distance below the panels' r_min take the FP64 route.
+template <int MAXIMG>
+__global__ void __launch_bounds__(256, 1) k_assemble_cheb_reduced_df(GeomDev g, ChebTables t, const cxd* __restrict__ ks,
+                                                                  int nk, void* const* __restrict__ outs,
+                                                                  void* const* __restrict__ los, long long ld) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const int bcol = blockIdx.y * blockDim.y + threadIdx.y;
+  if (a >= g.m || bcol >= g.m) return;
+  const int i = g.fund[a], j = g.fund[bcol];
+  const size_t off = (size_t)a + (size_t)bcol * (size_t)ld;
+  const double xi = g.x[i], yi = g.y[i];
+  const bool diag = (i == j);
+  bool fp64 = false;
+  dfl nA{0.f, 0.f}, nB{0.f, 0.f}, th{0.f, 0.f}, tj{0.f, 0.f}, dc{0.f, 0.f};
+  int ph = 0, pj = 0;
+  if (diag) {
+    dc = df_of(1.0 - g.ws[i] * g.kappa[i]);
+  } else {
+    const PairGeom p = pair_geom(g, i, j);
+    const Fold f = fold_of<0>(p);
+    nA = df_of(-f.A);
+    nB = df_of(-f.B);
+    double thd = 0.0, tjd = 0.0;
+    panel_of(p.r, t.rmin, t.rmax, t.dr_h, t.invdr_h, t.nh, ph, thd);
+    panel_of(p.r, 0.0, t.rmax, t.dr_j, t.invdr_j, t.nj, pj, tjd);
+    th = df_of(thd);
+    tj = df_of(tjd);
+    fp64 |= p.r < t.rmin;
+  }
+  // image slots filled through compile-time indices (registers, not local memory)
+  int nim = 0;
+  int iph[MAXIMG];
+  dfl ith[MAXIMG], ere[MAXIMG], eim[MAXIMG];
+#pragma unroll
+  for (int sl = 0; sl < MAXIMG; ++sl) {
+    iph[sl] = 0;
+    ith[sl] = dfl{0.f, 0.f};
+    ere[sl] = dfl{0.f, 0.f};
+    eim[sl] = dfl{0.f, 0.f};
+  }
+  if (g.norb > MAXIMG + 1) fp64 = true;
+#pragma unroll
+  for (int l = 0; l < MAXIMG + 1; ++l) {
+    if (l >= g.norb) break;
+    const int qn = g.orb[bcol * g.norb + l];
+    if (qn == j) continue;
+    const double dxq = xi - g.x[qn], dyq = yi - g.y[qn];
+    const double r = hypot(dxq, dyq);
+    if (r < 2.220446049250313e-16) continue;
+    if (r < t.rmin) {
+      fp64 = true;
+      continue;
+    }
+    const double c = (g.nx[qn] * dxq + g.ny[qn] * dyq) / r;
+    const double e = c * g.speed[qn] * g.ws[qn];
+    const double scr = g.orb_scale[2 * (bcol * g.norb + l)], sci = g.orb_scale[2 * (bcol * g.norb + l) + 1];
+    int php = 0;
+    double thd = 0.0;
+    panel_of(r, t.rmin, t.rmax, t.dr_h, t.invdr_h, t.nh, php, thd);
+#pragma unroll
+    for (int sl = 0; sl < MAXIMG; ++sl)
+      if (sl == nim) {
+        iph[sl] = php;
+        ith[sl] = df_of(thd);
+        ere[sl] = df_of(-e * scr);  // F -= (e sc) H1': accumulate (-e sc) H1'
+        eim[sl] = df_of(-e * sci);
+      }
+    if (nim < MAXIMG) ++nim;
+    else fp64 = true;
+  }
+  for (int q = 0; q < nk; ++q) {
+    float4 v;
+    if (fp64) {
+      const cxd k = ks[q];
+      cxd F;
+      if (diag) {
+        F = cxd(1.0 - g.ws[i] * g.kappa[i], 0.0);
+      } else {
+        const PairGeom p = pair_geom(g, i, j);
+        int pjj = 0;
+        double tjd = 0.0;
+        panel_of(p.r, 0.0, t.rmax, t.dr_j, t.invdr_j, t.nj, pjj, tjd);
+        cxd h0, h1, j0, j1, F1, F2;
+        cheb_h01(t, q, p.r, k, h0, h1);
+        clenshaw2(t.J + (((size_t)q * t.nj + pjj) * (t.Mj + 1)) * 2, t.Mj, tjd, j0, j1);
+        entry_vals<0, 0>(p, k, h0, h1, j0, j1, &F, &F1, &F2);
+      }
+      for (int l = 0; l < g.norb; ++l) {
+        const int qn = g.orb[bcol * g.norb + l];
+        if (qn == j) continue;
+        const double dxq = xi - g.x[qn], dyq = yi - g.y[qn];
+        const double r = hypot(dxq, dyq);
+        if (r < 2.220446049250313e-16) continue;
+        const double c = (g.nx[qn] * dxq + g.ny[qn] * dyq) / r;
+        const cxd sc(g.orb_scale[2 * (bcol * g.norb + l)], g.orb_scale[2 * (bcol * g.norb + l) + 1]);
+        cxd h0, h1, F1, F2;
+        cheb_h01(t, q, r, k, h0, h1);
+        image_terms<0>(c, g.speed[qn] * g.ws[qn], sc, r, k, h0, h1, F, F1, F2);
+      }
+      v = pack_split(F);
+    } else {
+      dfl re = dc, im{0.f, 0.f};
+      dfl hr, hi_, jr, ji;
+      if (!diag) {
+        df_series<false>(t.HD + ((size_t)q * t.nh + ph) * (t.Mh + 1) * 2, t.Mh, th, nullptr, nullptr, &hr, &hi_);
+        df_series<false>(t.JD + ((size_t)q * t.nj + pj) * (t.Mj + 1) * 2, t.Mj, tj, nullptr, nullptr, &jr, &ji);
+        df_acc(re, nB, hr);
+        df_acc(im, nB, hi_);
+        df_acc(re, nA, jr);
+        df_acc(im, nA, ji);
+      }
+#pragma unroll
+      for (int l = 0; l < MAXIMG; ++l) {
+        if (l >= nim) break;
+        df_series<false>(t.HD + ((size_t)q * t.nh + iph[l]) * (t.Mh + 1) * 2, t.Mh, ith[l], nullptr, nullptr, &hr,
+                         &hi_);
+        // (ere + i eim)(hr + i hi_)
+        df_acc(re, ere[l], hr);
+        df_acc(re, dfl{-eim[l].hi, -eim[l].lo}, hi_);
+        df_acc(im, ere[l], hi_);
+        df_acc(im, eim[l], hr);
+      }
+      re = df_norm(re);
+      im = df_norm(im);
+      v = make_float4(re.hi, im.hi, re.lo, im.lo);
+    }
+    reinterpret_cast<cxf*>(outs[q])[off] = cxf(v.x, v.y);
+    if (los) reinterpret_cast<cxf*>(los[q])[off] = cxf(v.z, v.w);
+  }
+}
+
+bool cheb_df_applies(const GeomDev& g, int deriv) {
+  if (deriv) return false;
+  if (g.m == g.n) return true;
+  return g.form == 0 && g.norb <= 4;
+}
+
 void cheb_df_bytes(const ChebTables& t, size_t* hd, size_t* jd, size_t* nkc) {
   *hd = sizeof(float4) * 2 * (size_t)t.nk * t.nh * (t.Mh + 1);
   *jd = sizeof(float4) * 2 * (size_t)t.nk * t.nj * (t.Mj + 1);
@@ -1367,6 +1512,9 @@ int launch_assemble_cheb(const GeomDev& g, const ChebTables& t, const cxd* ks, i
         k_assemble_cheb_reduced<1, 0><<<grd, blk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
       else
         k_assemble_cheb_reduced<0, 0><<<grd, blk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
+    } else if (t.HD && t.JD && t.nkc && g.norb <= 4) {
+      dim3 dgrd((g.m + 31) / 32, (g.m + 7) / 8, 1);
+      k_assemble_cheb_reduced_df<3><<<dgrd, blk, 0, st>>>(g, t, ks, nk, outs_dev, lo_outs_dev, ld);
     } else {
       k_assemble_cheb_reduced<0, 1><<<grd, blk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, lo_outs_dev, ld);
     }

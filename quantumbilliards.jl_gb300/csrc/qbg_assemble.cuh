@@ -39,6 +39,9 @@ int cheb_build(ChebTables& t, const cxd* ks, cudaStream_t st);
 // sizes cheb_df_bytes reports, owned by the caller); after cheb_build
 void cheb_df_bytes(const ChebTables& t, size_t* hd, size_t* jd, size_t* nkc);
 int cheb_df_tables(ChebTables& t, const cxd* ks, cudaStream_t st);
+// whether the complex64 Chebyshev assembly of g runs on double-float tables
+// (symmetric full operators; the reduced DLP with orbits of at most 4 nodes)
+bool cheb_df_applies(const GeomDev& g, int deriv);
 // max interpolation errors of H0, H1, J0, J1 per wavenumber at ns sampled radii (err: 4 nk zeroed words)
 int cheb_errors(const ChebTables& t, const cxd* ks, int ns, unsigned long long* err, cudaStream_t st);
 int launch_assemble_cheb(const GeomDev& g, const ChebTables& t, const cxd* ks, int nk, int deriv, int prec,

@@ -197,7 +197,7 @@ int load(qbg_beyn* b, int n0, int c) {
     std::vector<void*> ctmp;
     ChebTables t;
     int s = make_cheb(b->g, b->zj + n0, c, cp, t, ctmp, st);
-    if (!s && b->prec != QBG_PREC_FP64 && b->g->d.m == b->g->d.n) s = make_cheb_df(t, b->zj + n0, ctmp, st);
+    if (!s && b->prec != QBG_PREC_FP64 && cheb_df_applies(b->g->d, 0)) s = make_cheb_df(t, b->zj + n0, ctmp, st);
     if (!s) s = launch_assemble_cheb(b->g->d, t, b->zj + n0, c, 0, b->prec, b->dptrs, b->dlo, n, st);
     if (!s) {
       cudaEventRecord(b->ev[1], st);
