@@ -53,6 +53,11 @@ struct qbg_beyn {
   // everything on st (the results are the same either way)
   cudaStream_t st2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // helper streams of the per-disk QR of the moments (created on first use)
+  static constexpr int QR_STREAMS = 8;
+  cudaStream_t qst[QR_STREAMS] = {};
+  cudaEvent_t qev[QR_STREAMS] = {};
+  cudaEvent_t qfork = nullptr;
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   double ms_assemble = 0, ms_factor = 0;  // device time of the last load(s)
   int singular = 0;
@@ -76,6 +81,14 @@ struct qbg_beyn {
     }
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
+    for (int i = 0; i < QR_STREAMS; ++i) {
+      if (qst[i]) {
+        cudaStreamSynchronize(qst[i]);
+        cudaStreamDestroy(qst[i]);
+      }
+      if (qev[i]) cudaEventDestroy(qev[i]);
+    }
+    if (qfork) cudaEventDestroy(qfork);
     if (st) {
       tc_release_scratch(st);
       cudaStreamDestroy(st);
@@ -630,12 +643,15 @@ int moments_impl(qbg_beyn* b, const double* V, int64_t L, double* A0, double* A1
 }
 
 // thin Householder QR of every disk's kept A0 block (N x m) on the device:
-// R (m x m, upper triangular) and C = Q^H A1 (m x m) to the host, column-major per disk
+// R (m x m, upper triangular) and C = Q^H A1 (m x m) to the host, column-major
+// per disk. Several disks run on up to QR_STREAMS helper streams (each with its
+// own cuSOLVER handle and workspace): the factorisations are latency-bound, so
+// disks overlap. R and C are staged on the device and copied back at once.
 std::mutex g_qr_mu;
-cusolverDnHandle_t g_qr_h[64] = {};
+cusolverDnHandle_t g_qr_h[64][qbg_beyn::QR_STREAMS] = {};
 
 int qr_reduce(qbg_beyn* b, double* Rh, double* Ch) {
-  const int n = b->n, m = b->mcols;
+  const int n = b->n, m = b->mcols, nd = b->ndisk;
   cudaStream_t st = b->st;
   int dev = 0;
   QBG_CUDA(cudaGetDevice(&dev));
@@ -643,51 +659,83 @@ int qr_reduce(qbg_beyn* b, double* Rh, double* Ch) {
     set_error("qr_reduce: device index %d", dev);
     return QBG_EINVAL;
   }
+  const int S = nd > 1 ? std::min(nd, (int)qbg_beyn::QR_STREAMS) : 1;
   std::lock_guard<std::mutex> lk(g_qr_mu);
-  cusolverDnHandle_t& h = g_qr_h[dev];
-  if (!h && cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) {
-    h = nullptr;
-    set_error("cusolverDnCreate failed");
-    return QBG_ECUDA;
+  for (int i = 0; i < S; ++i) {
+    cusolverDnHandle_t& h = g_qr_h[dev][i];
+    if (!h && cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) {
+      h = nullptr;
+      set_error("cusolverDnCreate failed");
+      return QBG_ECUDA;
+    }
+    if (S > 1 && !b->qst[i]) {
+      QBG_CUDA(cudaStreamCreateWithFlags(&b->qst[i], cudaStreamNonBlocking));
+      QBG_CUDA(cudaEventCreateWithFlags(&b->qev[i], cudaEventDisableTiming));
+    }
   }
-  if (cusolverDnSetStream(h, st) != CUSOLVER_STATUS_SUCCESS) {
-    set_error("cusolverDnSetStream failed");
-    return QBG_ECUDA;
-  }
+  if (S > 1 && !b->qfork) QBG_CUDA(cudaEventCreateWithFlags(&b->qfork, cudaEventDisableTiming));
+  auto stream_of = [&](int slot) { return S > 1 ? b->qst[slot] : st; };
   std::vector<void*> tmp;
   auto cleanup = [&]() { for (void* p : tmp) dfree(p, st); };
-  cuDoubleComplex *w0 = nullptr, *w1 = nullptr, *tau = nullptr, *work = nullptr;
-  int* info = nullptr;
   auto get = [&](auto** p, size_t bytes) {
     int s = dmalloc(p, bytes);
     if (!s) tmp.push_back(*p);
     return s;
   };
+  const size_t nn_ = (size_t)n, mm = (size_t)m * m;
+  const size_t per_slot = nn_ * m * 2 + (size_t)m;  // w0, w1, tau (complex words)
+  cuDoubleComplex* ws = nullptr;
+  cuDoubleComplex* works = nullptr;
+  cxd* stage = nullptr;
+  int* info = nullptr;
   int s = QBG_OK;
-  if ((s = get(&w0, sizeof(cxd) * (size_t)n * m)) || (s = get(&w1, sizeof(cxd) * (size_t)n * m)) ||
-      (s = get(&tau, sizeof(cxd) * (size_t)m)) || (s = get(&info, sizeof(int) * b->ndisk))) {
+  if ((s = get(&ws, sizeof(cxd) * per_slot * S)) || (s = get(&stage, sizeof(cxd) * 2 * mm * nd)) ||
+      (s = get(&info, sizeof(int) * nd))) {
     cleanup();
     return s;
   }
   int l1 = 0, l2 = 0;
-  if (cusolverDnZgeqrf_bufferSize(h, n, m, w0, n, &l1) != CUSOLVER_STATUS_SUCCESS ||
-      cusolverDnZunmqr_bufferSize(h, CUBLAS_SIDE_LEFT, CUBLAS_OP_C, n, m, m, w0, n, tau, w1, n, &l2) !=
-          CUSOLVER_STATUS_SUCCESS) {
-    cleanup();
-    set_error("cuSOLVER workspace query failed");
-    return QBG_ECUDA;
+  {
+    cusolverDnHandle_t h = g_qr_h[dev][0];
+    cuDoubleComplex* w0 = ws;
+    if (cusolverDnZgeqrf_bufferSize(h, n, m, w0, n, &l1) != CUSOLVER_STATUS_SUCCESS ||
+        cusolverDnZunmqr_bufferSize(h, CUBLAS_SIDE_LEFT, CUBLAS_OP_C, n, m, m, w0, n, w0 + 2 * nn_ * m,
+                                    w0 + nn_ * m, n, &l2) != CUSOLVER_STATUS_SUCCESS) {
+      cleanup();
+      set_error("cuSOLVER workspace query failed");
+      return QBG_ECUDA;
+    }
   }
   const int lw = std::max(std::max(l1, l2), 1);
-  if ((s = get(&work, sizeof(cxd) * (size_t)lw))) {
+  if ((s = get(&works, sizeof(cxd) * (size_t)lw * S))) {
     cleanup();
     return s;
   }
-  const size_t nn_ = (size_t)n, mm = (size_t)m * m;
-  for (int d = 0; d < b->ndisk && !s; ++d) {
+  if (S > 1) {
+    cudaError_t e = cudaEventRecord(b->qfork, st);
+    for (int i = 0; i < S && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(b->qst[i], b->qfork, 0);
+    if (e != cudaSuccess) {
+      cleanup();
+      return cuda_status(e, "qr_reduce fork");
+    }
+  }
+  for (int d = 0; d < nd && !s; ++d) {
+    const int slot = d % S;
+    cudaStream_t qs = stream_of(slot);
+    cusolverDnHandle_t h = g_qr_h[dev][slot];
+    cuDoubleComplex* w0 = ws + per_slot * slot;
+    cuDoubleComplex* w1 = w0 + nn_ * m;
+    cuDoubleComplex* tau = w1 + nn_ * m;
+    cuDoubleComplex* work = works + (size_t)lw * slot;
+    if (cusolverDnSetStream(h, qs) != CUSOLVER_STATUS_SUCCESS) {
+      set_error("cusolverDnSetStream failed");
+      s = QBG_ECUDA;
+      break;
+    }
     cudaError_t e = cudaMemcpyAsync(w0, b->macc0 + d * nn_ * b->mcap, sizeof(cxd) * nn_ * m,
-                                    cudaMemcpyDeviceToDevice, st);
+                                    cudaMemcpyDeviceToDevice, qs);
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(w1, b->macc1 + d * nn_ * b->mcap, sizeof(cxd) * nn_ * m, cudaMemcpyDeviceToDevice, st);
+      e = cudaMemcpyAsync(w1, b->macc1 + d * nn_ * b->mcap, sizeof(cxd) * nn_ * m, cudaMemcpyDeviceToDevice, qs);
     if (e != cudaSuccess) {
       s = cuda_status(e, "qr_reduce copy");
       break;
@@ -699,33 +747,48 @@ int qr_reduce(qbg_beyn* b, double* Rh, double* Ch) {
       s = QBG_ECUDA;
       break;
     }
-    e = cudaMemcpy2DAsync(Rh + 2 * d * mm, sizeof(cxd) * m, w0, sizeof(cxd) * nn_, sizeof(cxd) * m, m,
-                          cudaMemcpyDeviceToHost, st);
+    e = cudaMemcpy2DAsync(stage + 2 * d * mm, sizeof(cxd) * m, w0, sizeof(cxd) * nn_, sizeof(cxd) * m, m,
+                          cudaMemcpyDeviceToDevice, qs);
     if (e == cudaSuccess)
-      e = cudaMemcpy2DAsync(Ch + 2 * d * mm, sizeof(cxd) * m, w1, sizeof(cxd) * nn_, sizeof(cxd) * m, m,
-                            cudaMemcpyDeviceToHost, st);
-    if (e != cudaSuccess) s = cuda_status(e, "qr_reduce D2H");
+      e = cudaMemcpy2DAsync(stage + (2 * d + 1) * mm, sizeof(cxd) * m, w1, sizeof(cxd) * nn_, sizeof(cxd) * m, m,
+                            cudaMemcpyDeviceToDevice, qs);
+    if (e != cudaSuccess) s = cuda_status(e, "qr_reduce staging");
   }
-  std::vector<int> hinfo(b->ndisk, 0);
+  if (S > 1) {
+    // join every helper stream back into the handle's stream (also after an error)
+    for (int i = 0; i < S; ++i) {
+      cudaEventRecord(b->qev[i], b->qst[i]);
+      cudaStreamWaitEvent(st, b->qev[i], 0);
+    }
+  }
+  std::vector<int> hinfo(nd, 0);
+  std::vector<cxd> hstage;
   if (!s) {
-    cudaError_t e = cudaMemcpyAsync(hinfo.data(), info, sizeof(int) * b->ndisk, cudaMemcpyDeviceToHost, st);
+    hstage.resize(2 * mm * nd);
+    cudaError_t e = cudaMemcpyAsync(hstage.data(), stage, sizeof(cxd) * 2 * mm * nd, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hinfo.data(), info, sizeof(int) * nd, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) s = cuda_status(e, "qr_reduce");
+  } else {
+    cudaStreamSynchronize(st);
   }
   cleanup();
   if (s) return s;
-  for (int d = 0; d < b->ndisk; ++d)
+  for (int d = 0; d < nd; ++d)
     if (hinfo[d] < 0) {
       set_error("cusolverDnZgeqrf: argument %d invalid", -hinfo[d]);
       return QBG_ECUDA;
     }
-  // R is the upper triangle; below it geqrf left the Householder vectors
-  for (int d = 0; d < b->ndisk; ++d)
+  for (int d = 0; d < nd; ++d) {
+    std::memcpy(Rh + 2 * d * mm, hstage.data() + 2 * d * mm, sizeof(cxd) * mm);
+    std::memcpy(Ch + 2 * d * mm, hstage.data() + (2 * d + 1) * mm, sizeof(cxd) * mm);
+    // R is the upper triangle; below it geqrf left the Householder vectors
     for (int j = 0; j < m; ++j)
       for (int i = j + 1; i < m; ++i) {
         Rh[2 * (d * mm + (size_t)j * m + i)] = 0.0;
         Rh[2 * (d * mm + (size_t)j * m + i) + 1] = 0.0;
       }
+  }
   return QBG_OK;
 }
 

@@ -49,16 +49,24 @@ def disks_case(qb, a):
         cheb = qb.chebyshev_params_min_cost(sol, pts, zref, ws=ws, tol=1e-12, entries=float(ws.dim) ** 2 * a.ndisk
                                             * a.nq, terms_per_entry=4.0, tables_per_call=a.ndisk * a.nq)[:4]
     t1 = time.perf_counter()
-    lams, info = qb.solve_disks(sol, pts, k0s, 0.5, nq=a.nq, r=a.L, svd_tol=1e-10, rng=np.random.default_rng(3),
-                                mixed=a.form, ws=ws, return_info=True, cheb=cheb)
-    t2 = time.perf_counter()
+    # the first batch allocates every buffer from the driver (cold); later
+    # batches of the same shape reuse the library's cached blocks (warm)
+    times = []
+    for _ in range(max(1, a.repeat)):
+        ts = time.perf_counter()
+        lams, info = qb.solve_disks(sol, pts, k0s, 0.5, nq=a.nq, r=a.L, svd_tol=1e-10, rng=np.random.default_rng(3),
+                                    mixed=a.form, ws=ws, return_info=True, cheb=cheb)
+        times.append(time.perf_counter() - ts)
     n_in = sum(int(np.count_nonzero((np.abs(l - k) < 0.5) & (np.abs(l.imag) < 1e-3))) for l, k in zip(lams, k0s))
     st = info["stats"]
+    warm = min(times[1:]) if len(times) > 1 else times[0]
     print(json.dumps(dict(case="disks", N=pts.n, m=ws.dim, ndisk=a.ndisk, nq=a.nq, operators=a.ndisk * a.nq, L=a.L,
-                          form=a.form, cheb=list(map(int, cheb)), autotune_s=t1 - t0, solve_s=t2 - t1,
-                          eigenvalues=n_in, eigenvalues_per_s=n_in / (t2 - t1), rk=info["rk"],
+                          form=a.form, cheb=list(map(int, cheb)), autotune_s=t1 - t0, solve_s_cold=times[0],
+                          solve_s_warm=warm, eigenvalues=n_in, eigenvalues_per_s_warm=n_in / warm,
+                          eigenvalues_per_s_cold=n_in / times[0], rk=info["rk"],
                           ms_assemble=st[0]["ms_assemble"], ms_factor=st[0]["ms_factor"],
-                          ms_solve=[s["ms_solve"] for s in st], refine=[s["refine_history"] for s in st])))
+                          ms_solve=[s["ms_solve"] for s in st], refine=[s["refine_history"] for s in st],
+                          host_ms=info.get("host_ms"))))
 
 
 def large_case(qb, a):
@@ -91,6 +99,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("case", choices=["beyn", "assemble", "disks", "large"])
     ap.add_argument("--ndisk", type=int, default=32)
+    ap.add_argument("--repeat", type=int, default=1, help="disks: batches run back to back (first cold, rest warm)")
     ap.add_argument("--chunk", type=int, default=8)
     ap.add_argument("--tune", default="min_cost", choices=["min_cost", "reference"])
     ap.add_argument("--nq", type=int, default=8)

@@ -77,3 +77,24 @@ def test_beyn_cheb_eigenvalues(qb):
         a = sel(lam)
         assert len(a) == len(o) > 0
         assert np.max(np.abs(a - o) / np.abs(o)) < 1e-11
+
+
+@pytest.mark.parametrize("form", ["cfie", "dlp"])
+def test_cheb_tables_at_high_k_vs_direct(qb, form):
+    """Device-built tables at high k: with 60000 H panels of degree 7 at
+    k ~ 150 interpolation adds < 1e-15, so the Chebyshev assembly equals the
+    direct-evaluation assembly to the Bessel functions' own accuracy (bound
+    5e-14; measured 1.8e-15 - 5.1e-15). With the reference's default panels
+    the two differ by the panels' interpolation error near r_min, 2.8e-12
+    for this CFIE case."""
+    b = qb.make_star(0.2, 5)
+    sol = qb.CFIE_kress(1.0, b) if form == "cfie" else qb.DLP_kress(1.0, b)
+    pts, sol = qb.points_with_n(sol, b, 1024, 150.0)
+    ws = qb.Workspace(sol, pts)
+    ks = [150.0 + 0.3j, 149.6 - 0.2j, 150.2 + 0.0j]
+    cheb = qb.assemble(ws, ks, cheb=(60000, 7, 12000, 7))
+    direct = qb.assemble(ws, ks)
+    for c, d in zip(cheb, direct):
+        rel = np.max(np.abs(c - d)) / np.max(np.abs(d))
+        print(f"{form} cheb vs direct {rel:.3e}")
+        assert rel < 5e-14
