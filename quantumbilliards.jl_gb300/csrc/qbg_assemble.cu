@@ -1039,6 +1039,49 @@ __device__ __forceinline__ void df_acc(dfl& acc, dfl c, dfl t) {
 
 __device__ __forceinline__ dfl df_norm(dfl a) { return df_two_sum(a.hi, a.lo); }
 
+// Compile-time degree MT: every coefficient of the row is loaded before the
+// recurrence, so a thread waits for one cache latency per series instead of
+// one per degree (the loop over a runtime degree keeps each load in its own
+// iteration).
+template <bool S0, int MT>
+__device__ __forceinline__ void df_series_m(const float4* __restrict__ c, dfl t, dfl* v0r, dfl* v0i, dfl* v1r,
+                                            dfl* v1i) {
+  float4 k1[MT + 1], k0[S0 ? MT + 1 : 1];
+#pragma unroll
+  for (int m = 0; m <= MT; ++m) {
+    k1[m] = __ldg(c + 2 * m + 1);
+    if (S0) k0[m] = __ldg(c + 2 * m);
+  }
+  dfl a0r{0.f, 0.f}, a0i{0.f, 0.f}, a1r{0.f, 0.f}, a1i{0.f, 0.f};
+  dfl tp{1.f, 0.f}, tc = t;
+  const dfl t2{2.f * t.hi, 2.f * t.lo};
+#pragma unroll
+  for (int m = 0; m <= MT; ++m) {
+    dfl tm;
+    if (m == 0) {
+      tm = tp;
+    } else if (m == 1) {
+      tm = tc;
+    } else {
+      tm = df_sub(df_mul(t2, tc), tp);
+      tp = tc;
+      tc = tm;
+    }
+    df_acc(a1r, dfl{k1[m].x, k1[m].y}, tm);
+    df_acc(a1i, dfl{k1[m].z, k1[m].w}, tm);
+    if (S0) {
+      df_acc(a0r, dfl{k0[m].x, k0[m].y}, tm);
+      df_acc(a0i, dfl{k0[m].z, k0[m].w}, tm);
+    }
+  }
+  *v1r = a1r;
+  *v1i = a1i;
+  if (S0) {
+    *v0r = a0r;
+    *v0i = a0i;
+  }
+}
+
 // sum_m c_m T_m(t) for the two complex series of one table row (float4 pairs
 // per degree: {series 0, series 1}); S0 skips series 0 (DLP needs only J1, H1)
 template <bool S0>
@@ -1073,6 +1116,13 @@ __device__ __forceinline__ void df_series(const float4* __restrict__ c, int M, d
     *v0r = a0r;
     *v0i = a0i;
   }
+}
+
+template <bool S0, int DM>
+__device__ __forceinline__ void df_series_d(const float4* __restrict__ c, int M, dfl t, dfl* v0r, dfl* v0i, dfl* v1r,
+                                            dfl* v1i) {
+  if (DM > 0) df_series_m<S0, (DM > 0 ? DM : 1)>(c, t, v0r, v0i, v1r, v1i);
+  else df_series<S0>(c, M, t, v0r, v0i, v1r, v1i);
 }
 
 struct FoldDf {
@@ -1120,7 +1170,7 @@ __global__ void k_cheb_df_tables(ChebTables t) {
 
 // symmetric-pair assembly of the complex64 forms on double-float arithmetic;
 // same tiling as k_assemble_cheb_sym, every node of ks in one pass
-template <int FORM>
+template <int FORM, int DM>
 __global__ void __launch_bounds__(512) k_assemble_cheb_sym_df(GeomDev g, ChebTables t, const cxd* __restrict__ ks,
                                                               int nk, void* const* __restrict__ outs,
                                                               void* const* __restrict__ los, long long ld) {
@@ -1200,11 +1250,11 @@ __global__ void __launch_bounds__(512) k_assemble_cheb_sym_df(GeomDev g, ChebTab
           vji = pack_split(folded_entry(fji, nc.kaL1, nc.kaL2, nc.kg, nc.kd, b.h0(), b.h1(), j0, j1));
         } else {
           dfl h0r{0.f, 0.f}, h0i{0.f, 0.f}, h1r, h1i, j0r{0.f, 0.f}, j0i{0.f, 0.f}, j1r{0.f, 0.f}, j1i{0.f, 0.f};
-          df_series<FORM == 1>(t.HD + ((size_t)q * t.nh + ph[s]) * (t.Mh + 1) * 2, t.Mh, th[s], &h0r, &h0i, &h1r,
-                               &h1i);
+          df_series_d<FORM == 1, DM>(t.HD + ((size_t)q * t.nh + ph[s]) * (t.Mh + 1) * 2, t.Mh, th[s], &h0r, &h0i,
+                                     &h1r, &h1i);
           if (needj[s])
-            df_series<FORM == 1>(t.JD + ((size_t)q * t.nj + pj[s]) * (t.Mj + 1) * 2, t.Mj, tj[s], &j0r, &j0i,
-                                 &j1r, &j1i);
+            df_series_d<FORM == 1, DM>(t.JD + ((size_t)q * t.nj + pj[s]) * (t.Mj + 1) * 2, t.Mj, tj[s], &j0r,
+                                       &j0i, &j1r, &j1i);
           // entry = -(A kaL1 J1 + B kaL2 H1 + C kg J0 + D kd H0), the node factors inside the tables
           auto fold = [&](const FoldDf& f) {
             dfl re{0.f, 0.f}, im{0.f, 0.f};
@@ -1254,7 +1304,7 @@ __global__ void __launch_bounds__(512) k_assemble_cheb_sym_df(GeomDev g, ChebTab
 //   F_ab = [1 - w kappa]_(a=b) - (A kaL1 J1 + B kaL2 H1)(r_ij) - sum_images c w_q sc kaL2 H1(r_iq)
 // (dlp_kress.jl:1151-1189 with the images of :1081-1100). Entries with a
 // distance below the panels' r_min take the FP64 route.
-template <int MAXIMG>
+template <int MAXIMG, int DM>
 __global__ void __launch_bounds__(256, 1) k_assemble_cheb_reduced_df(GeomDev g, ChebTables t, const cxd* __restrict__ ks,
                                                                   int nk, void* const* __restrict__ outs,
                                                                   void* const* __restrict__ los, long long ld) {
@@ -1357,8 +1407,10 @@ __global__ void __launch_bounds__(256, 1) k_assemble_cheb_reduced_df(GeomDev g, 
       dfl re = dc, im{0.f, 0.f};
       dfl hr, hi_, jr, ji;
       if (!diag) {
-        df_series<false>(t.HD + ((size_t)q * t.nh + ph) * (t.Mh + 1) * 2, t.Mh, th, nullptr, nullptr, &hr, &hi_);
-        df_series<false>(t.JD + ((size_t)q * t.nj + pj) * (t.Mj + 1) * 2, t.Mj, tj, nullptr, nullptr, &jr, &ji);
+        df_series_d<false, DM>(t.HD + ((size_t)q * t.nh + ph) * (t.Mh + 1) * 2, t.Mh, th, nullptr, nullptr, &hr,
+                               &hi_);
+        df_series_d<false, DM>(t.JD + ((size_t)q * t.nj + pj) * (t.Mj + 1) * 2, t.Mj, tj, nullptr, nullptr, &jr,
+                               &ji);
         df_acc(re, nB, hr);
         df_acc(im, nB, hi_);
         df_acc(re, nA, jr);
@@ -1367,8 +1419,8 @@ __global__ void __launch_bounds__(256, 1) k_assemble_cheb_reduced_df(GeomDev g, 
 #pragma unroll
       for (int l = 0; l < MAXIMG; ++l) {
         if (l >= nim) break;
-        df_series<false>(t.HD + ((size_t)q * t.nh + iph[l]) * (t.Mh + 1) * 2, t.Mh, ith[l], nullptr, nullptr, &hr,
-                         &hi_);
+        df_series_d<false, DM>(t.HD + ((size_t)q * t.nh + iph[l]) * (t.Mh + 1) * 2, t.Mh, ith[l], nullptr, nullptr,
+                               &hr, &hi_);
         // (ere + i eim)(hr + i hi_)
         df_acc(re, ere[l], hr);
         df_acc(re, dfl{-eim[l].hi, -eim[l].lo}, hi_);
@@ -1514,7 +1566,17 @@ int launch_assemble_cheb(const GeomDev& g, const ChebTables& t, const cxd* ks, i
         k_assemble_cheb_reduced<0, 0><<<grd, blk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
     } else if (t.HD && t.JD && t.nkc && g.norb <= 4) {
       dim3 dgrd((g.m + 31) / 32, (g.m + 7) / 8, 1);
-      k_assemble_cheb_reduced_df<3><<<dgrd, blk, 0, st>>>(g, t, ks, nk, outs_dev, lo_outs_dev, ld);
+      const int dm = (t.Mh == t.Mj) ? t.Mh : 0;
+#define QBG_RED_DF(D) k_assemble_cheb_reduced_df<3, D><<<dgrd, blk, 0, st>>>(g, t, ks, nk, outs_dev, lo_outs_dev, ld)
+      switch (dm) {
+        case 5: QBG_RED_DF(5); break;
+        case 7: QBG_RED_DF(7); break;
+        case 9: QBG_RED_DF(9); break;
+        case 11: QBG_RED_DF(11); break;
+        case 13: QBG_RED_DF(13); break;
+        default: QBG_RED_DF(0); break;
+      }
+#undef QBG_RED_DF
     } else {
       k_assemble_cheb_reduced<0, 1><<<grd, blk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, lo_outs_dev, ld);
     }
@@ -1531,10 +1593,12 @@ int launch_assemble_cheb(const GeomDev& g, const ChebTables& t, const cxd* ks, i
         k_assemble_cheb_sym<1, 0><<<sgrd, sblk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
     } else if (t.HD && t.JD && t.nkc) {
       dim3 dgrd((unsigned)(nt * (nt + 1) / 2), 1, 1);
+      // the degree stays a runtime value here: with 512 threads and the
+      // coefficients of two series in registers the compile-time forms spill
       if (g.form == 0)
-        k_assemble_cheb_sym_df<0><<<dgrd, sblk, 0, st>>>(g, t, ks, nk, outs_dev, lo_outs_dev, ld);
+        k_assemble_cheb_sym_df<0, 0><<<dgrd, sblk, 0, st>>>(g, t, ks, nk, outs_dev, lo_outs_dev, ld);
       else
-        k_assemble_cheb_sym_df<1><<<dgrd, sblk, 0, st>>>(g, t, ks, nk, outs_dev, lo_outs_dev, ld);
+        k_assemble_cheb_sym_df<1, 0><<<dgrd, sblk, 0, st>>>(g, t, ks, nk, outs_dev, lo_outs_dev, ld);
     } else {
       if (g.form == 0)
         k_assemble_cheb_sym<0, 1><<<sgrd, sblk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, lo_outs_dev, ld);

@@ -212,17 +212,22 @@ def chebyshev_params(solver, pts, zj, ws: Workspace = None, npanels_h_init=15000
 
 
 def chebyshev_params_min_cost(solver, pts, zj, ws: Workspace = None, tol=1e-10, entries=None, terms_per_entry=1.0,
-                              degrees=(5, 7, 9, 11, 13, 15), sampling_points=50000, bessel_cost=60.0,
-                              tables_per_call=None):
+                              degrees=(5, 7, 9, 11, 13, 15), sampling_points=50000, bessel_cost=None,
+                              tables_per_call=None, mixed: bool = True):
     """Panels of the lowest estimated assembly cost that still meet tol.
 
     For every degree M in ``degrees`` (kept fixed) the device tuner grows the
     panel counts until every interpolated H0, H1, J0, J1 is within tol. The
     cost of a candidate is the table build (one device Bessel evaluation,
-    about ``bessel_cost`` Clenshaw steps, per Lobatto node per panel per
-    wavenumber) plus the Clenshaw steps of the assembly (``entries`` matrix
+    about ``bessel_cost`` series steps, per Lobatto node per panel per
+    wavenumber) plus the series steps of the assembly (``entries`` matrix
     entries, ``terms_per_entry`` H evaluations each plus one J evaluation).
-    Returns (n_panels_h, M_h, n_panels_j, M_j, errors, cost)."""
+    The default ``bessel_cost`` is measured on GB300: one FP64 device Bessel
+    evaluation costs about 150 steps of the complex64 forms' double-float
+    series (1.55 ns vs 10.5 ps) and about 60 FP64 Clenshaw steps (FP64 form,
+    ``mixed=False``). Returns (n_panels_h, M_h, n_panels_j, M_j, errors, cost)."""
+    if bessel_cost is None:
+        bessel_cost = 150.0 if mixed else 60.0
     ws = ws if ws is not None else Workspace(solver, pts)
     nk = len(np.atleast_1d(zj)) if tables_per_call is None else int(tables_per_call)
     entries = float(ws.dim) ** 2 * nk if entries is None else float(entries)
