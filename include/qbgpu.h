@@ -236,7 +236,10 @@ qbg_status qbg_beyn_destroy(qbg_beyn* b);
 
 /* Smallest singular value of A(k) for nk real wavenumbers (the :svd branch of
  * @svd_or_det_solve, macros.jl:159-161, called by k_sweep,
- * sweepmethods.jl:132-152). */
+ * sweepmethods.jl:132-152): FP64 LU of A(k), then block inverse iteration on
+ * (A^H A)^{-1} with 8 vectors and a Rayleigh-Ritz step, until the estimate
+ * changes by less than 1e-13 relative (at most 40 sweeps); 0 for an exactly
+ * singular A(k). */
 qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig);
 
 /* Panel autotuner (chebyshev_params, chebyshev_optimal_panelization.jl:221-307):
@@ -279,6 +282,7 @@ typedef struct qbg_serve_opts {
   int64_t hbm_budget;   /* device bytes the running requests may hold (0 = 80% of free memory) */
   int32_t workers;      /* requests in flight at once (0 = 4) */
   int32_t max_batch;    /* most Beyn requests merged into one device batch (0 = 8; 1 = no merging) */
+  int32_t max_sweeps;   /* most sigma_min sweeps running at once (0 = 1); later sweeps wait, other kinds pass them */
 } qbg_serve_opts;
 
 enum { QBG_REQ_BEYN = 0, QBG_REQ_EBIM = 1, QBG_REQ_SWEEP = 2 };

@@ -89,7 +89,7 @@ qbg_status qbg_geom_create(const qbg_geom_desc* desc, qbg_geom** out) {
   qbg_geom* g = new (std::nothrow) qbg_geom();
   if (!g) { set_error("host allocation failed"); return QBG_ENOMEM; }
   auto fail = [&](int s) { delete g; return s; };
-  cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+  cudaError_t e = stream_create(&g->stream);
   if (e != cudaSuccess) return fail(cuda_status(e, "cudaStreamCreate"));
   std::vector<double> speed(n), kappa(n), nx(n), ny(n);
   std::vector<int> comp(n), lidx(n), coff(desc->ncomp + 1);
@@ -306,7 +306,7 @@ static int assemble_impl(qbg_geom* g, const double* ks, int64_t nk, int32_t deri
   if (!dev && (s = dmalloc(&stage, mat_bytes * chunk * nout))) { dfree(dks); dfree(dptrs); return s; }
   cudaStream_t st = g->stream;
   std::vector<void*> hp(chunk * nout);
-  auto cleanup = [&]() { dfree(dks); dfree(dptrs); if (stage) dfree(stage); };
+  auto cleanup = [&]() { dfree(dks, st); dfree(dptrs, st); if (stage) dfree(stage, st); };
   cudaError_t e = cudaMemcpyAsync(dks, ks, sizeof(cxd) * nk, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) { cleanup(); return cuda_status(e, "qbg_assemble H2D"); }
   for (int64_t k0 = 0; k0 < nk; k0 += chunk) {
@@ -325,7 +325,7 @@ static int assemble_impl(qbg_geom* g, const double* ks, int64_t nk, int32_t deri
         s = launch_assemble_cheb(g->d, t, dks + k0, (int)c, deriv, prec, dptrs, split ? dptrs + c : nullptr, dim,
                                  st);
       cudaError_t e2 = cudaStreamSynchronize(st);
-      for (void* p : ctmp) dfree(p);
+      for (void* p : ctmp) dfree(p, st);
       if (!s && e2 != cudaSuccess) s = cuda_status(e2, "qbg_assemble_cheb");
     } else {
       s = launch_assemble(g->d, dks + k0, (int)c, deriv, prec, dptrs, dim, st, split ? dptrs + c : nullptr);
@@ -360,51 +360,186 @@ qbg_status qbg_assemble_cheb(qbg_geom* g, const double* ks, int64_t nk, int32_t 
 
 }  // extern "C"
 
+namespace {
+
+// G = W^H W for an n x p column-major W; one CTA per entry (a, b)
+__global__ void k_gram(const cxd* __restrict__ W, int n, int p, cxd* __restrict__ G) {
+  const int a = blockIdx.x % p, b = blockIdx.x / p;
+  const cxd* wa = W + (size_t)a * n;
+  const cxd* wb = W + (size_t)b * n;
+  double re = 0.0, im = 0.0;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    const cxd x = wa[r], y = wb[r];
+    re = fma(x.re, y.re, fma(x.im, y.im, re));
+    im = fma(x.re, y.im, fma(-x.im, y.re, im));
+  }
+  __shared__ double sr[8], si[8];
+  for (int o = 16; o > 0; o >>= 1) {
+    re += __shfl_xor_sync(0xffffffffu, re, o);
+    im += __shfl_xor_sync(0xffffffffu, im, o);
+  }
+  if ((threadIdx.x & 31) == 0) { sr[threadIdx.x >> 5] = re; si[threadIdx.x >> 5] = im; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tr = 0.0, ti = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { tr += sr[w]; ti += si[w]; }
+    G[(size_t)b * p + a] = cxd(tr, ti);
+  }
+}
+
+// largest eigenvalue of a p x p Hermitian matrix (column-major, interleaved
+// complex): cyclic Jacobi on its real symmetric 2p x 2p form [[Re, -Im], [Im, Re]],
+// whose eigenvalues are those of G, each twice
+double herm_lambda_max(const std::vector<cxd>& G, int p) {
+  const int m = 2 * p;
+  std::vector<double> a((size_t)m * m);
+  for (int c = 0; c < p; ++c)
+    for (int r = 0; r < p; ++r) {
+      const cxd v = G[(size_t)c * p + r];
+      a[(size_t)c * m + r] = v.re;
+      a[(size_t)(c + p) * m + r + p] = v.re;
+      a[(size_t)c * m + r + p] = v.im;
+      a[(size_t)(c + p) * m + r] = -v.im;
+    }
+  auto A = [&](int r, int c) -> double& { return a[(size_t)c * m + r]; };
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0.0, dia = 0.0;
+    for (int c = 0; c < m; ++c)
+      for (int r = 0; r < m; ++r) (r == c ? dia : off) += A(r, c) * A(r, c);
+    if (off <= 1e-30 * dia) break;
+    for (int pi = 0; pi < m - 1; ++pi)
+      for (int q = pi + 1; q < m; ++q) {
+        const double apq = A(pi, q);
+        if (apq == 0.0) continue;
+        const double theta = (A(q, q) - A(pi, pi)) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < m; ++k) {  // columns pi, q
+          const double akp = A(k, pi), akq = A(k, q);
+          A(k, pi) = c * akp - sn * akq;
+          A(k, q) = sn * akp + c * akq;
+        }
+        for (int k = 0; k < m; ++k) {  // rows pi, q
+          const double apk = A(pi, k), aqk = A(q, k);
+          A(pi, k) = c * apk - sn * aqk;
+          A(q, k) = sn * apk + c * aqk;
+        }
+      }
+  }
+  double lmax = 0.0;
+  for (int c = 0; c < m; ++c) lmax = std::max(lmax, A(c, c));
+  return lmax;
+}
+
+}  // namespace
+
 extern "C" {
 
 // ---------------------------------------------------------------------------
-// sigma_min via cuSOLVER gesvd (values only)
+// sigma_min: FP64 LU of A(k) (cuSOLVER getrf), then block inverse iteration
+// on (A^H A)^{-1} = A^{-1} A^{-H} with SM_P vectors (getrs with the
+// conjugate transpose and without, thin QR between sweeps) and Rayleigh-Ritz
+// on W^H W, W = A^{-H} X: sigma_min = 1 / sqrt(lambda_max(W^H W)). The
+// estimate converges like (sigma_1 / sigma_{SM_P+1})^4 per sweep; sweeps stop
+// when it changes by less than 1e-13 relative (at most SM_ITERS). An exactly
+// singular U gives sigma_min = 0. Same result as the smallest value of
+// svdvals (macros.jl:159-161) to that tolerance.
 // ---------------------------------------------------------------------------
 qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig) {
   if (!g || !ks || !sig || nk < 1) { set_error("qbg_sigma_min: invalid arguments"); return QBG_EINVAL; }
+  constexpr int SM_P = 8, SM_ITERS = 40;
   std::vector<double> kc(2 * nk);
   for (int64_t q = 0; q < nk; ++q) { kc[2 * q] = ks[q]; kc[2 * q + 1] = 0.0; }
   QBG_TRY(check_ks(kc.data(), nk));
   std::lock_guard<std::mutex> lk(g->mu);
   const int n = (int)g->dim;
-  cudaStream_t st = g->stream;
+  const int p = std::min(SM_P, n);
+  // a sweep runs on a background stream (after the geometry stream's earlier
+  // work): its FP64 factorisations fill every SM for milliseconds, and the
+  // blocks of latency-bound requests on the library's other streams go first
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev_in = nullptr;
+  {
+    cudaError_t e0 = stream_create(&st, true);
+    if (e0 == cudaSuccess) e0 = cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming);
+    if (e0 == cudaSuccess) e0 = cudaEventRecord(ev_in, g->stream);
+    if (e0 == cudaSuccess) e0 = cudaStreamWaitEvent(st, ev_in, 0);
+    if (e0 != cudaSuccess) {
+      if (st) cudaStreamDestroy(st);
+      if (ev_in) cudaEventDestroy(ev_in);
+      return cuda_status(e0, "sigma_min stream");
+    }
+  }
+  // waits inside the sweep block the thread (no spinning): on a host with few
+  // cores a spinning wait takes the core from the threads that serve the
+  // other requests
+  cudaEvent_t ev_wait = nullptr;
+  if (cudaEventCreateWithFlags(&ev_wait, cudaEventBlockingSync | cudaEventDisableTiming) != cudaSuccess) {
+    cudaStreamDestroy(st);
+    cudaEventDestroy(ev_in);
+    return cuda_status(cudaGetLastError(), "sigma_min event");
+  }
+  struct StreamGuard {
+    cudaStream_t s;
+    cudaEvent_t e, w;
+    ~StreamGuard() {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+      cudaEventDestroy(e);
+      cudaEventDestroy(w);
+    }
+  } sguard{st, ev_in, ev_wait};
+  auto wait_st = [&]() -> cudaError_t {
+    cudaError_t e1 = cudaEventRecord(ev_wait, st);
+    return e1 == cudaSuccess ? cudaEventSynchronize(ev_wait) : e1;
+  };
   const int chunk = (int)std::min<int64_t>(nk, 16);
-  cxd *A = nullptr, *dks = nullptr, *work = nullptr;
-  double *S = nullptr, *rwork = nullptr;
-  int* dinfo = nullptr;
+  cxd *A = nullptr, *dks = nullptr, *work = nullptr, *X = nullptr, *W = nullptr, *tau = nullptr, *dG = nullptr;
+  int *ipiv = nullptr, *dinfo = nullptr;
   void** dptrs = nullptr;
   cusolverDnHandle_t h = nullptr;
   std::vector<void*> tmp;
   auto cleanup = [&]() {
-    for (void* p : tmp) dfree(p);
+    for (void* q : tmp) dfree(q, st);
     if (h) cusolverDnDestroy(h);
   };
-  auto talloc = [&](void** p, size_t bytes) {
-    int s = dmalloc(p, bytes);
-    if (!s) tmp.push_back(*p);
+  auto talloc = [&](void** q, size_t bytes) {
+    int s = dmalloc(q, bytes);
+    if (!s) tmp.push_back(*q);
     return s;
   };
   int s = QBG_OK;
   if ((s = talloc((void**)&A, sizeof(cxd) * (size_t)n * n * chunk)) || (s = talloc((void**)&dks, sizeof(cxd) * nk)) ||
-      (s = talloc((void**)&S, sizeof(double) * n)) || (s = talloc((void**)&rwork, sizeof(double) * n)) ||
-      (s = talloc((void**)&dinfo, sizeof(int))) || (s = talloc((void**)&dptrs, sizeof(void*) * chunk))) {
+      (s = talloc((void**)&X, sizeof(cxd) * (size_t)n * p)) || (s = talloc((void**)&W, sizeof(cxd) * (size_t)n * p)) ||
+      (s = talloc((void**)&tau, sizeof(cxd) * p)) || (s = talloc((void**)&ipiv, sizeof(int) * n)) ||
+      (s = talloc((void**)&dinfo, sizeof(int))) || (s = talloc((void**)&dptrs, sizeof(void*) * chunk)) ||
+      (s = talloc((void**)&dG, sizeof(cxd) * (size_t)p * p))) {
     cleanup(); return s;
   }
   if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) { cleanup(); set_error("cusolverDnCreate failed"); return QBG_ECUDA; }
   cusolverDnSetStream(h, st);
-  int lwork = 0;
-  if (cusolverDnZgesvd_bufferSize(h, n, n, &lwork) != CUSOLVER_STATUS_SUCCESS) {
-    cleanup(); set_error("gesvd buffer size failed"); return QBG_ECUDA;
+  int l1 = 0, l2 = 0, l3 = 0;
+  if (cusolverDnZgetrf_bufferSize(h, n, n, (cuDoubleComplex*)A, n, &l1) != CUSOLVER_STATUS_SUCCESS ||
+      cusolverDnZgeqrf_bufferSize(h, n, p, (cuDoubleComplex*)W, n, &l2) != CUSOLVER_STATUS_SUCCESS ||
+      cusolverDnZungqr_bufferSize(h, n, p, p, (cuDoubleComplex*)W, n, (cuDoubleComplex*)tau, &l3) !=
+          CUSOLVER_STATUS_SUCCESS) {
+    cleanup(); set_error("cuSOLVER workspace query failed"); return QBG_ECUDA;
   }
+  const int lwork = std::max(std::max(l1, l2), std::max(l3, 1));
   if ((s = talloc((void**)&work, sizeof(cxd) * (size_t)lwork))) { cleanup(); return s; }
+  // fixed starting block (reproducible): entries of a 64-bit LCG in [-1, 1)
+  std::vector<cxd> hx((size_t)n * p);
+  unsigned long long lcg = 0x9E3779B97F4A7C15ull;
+  auto nxt = [&]() {
+    lcg = lcg * 6364136223846793005ull + 1442695040888963407ull;
+    return (double)(lcg >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+  };
+  for (auto& v : hx) { v.re = nxt(); v.im = nxt(); }
   cudaError_t e = cudaMemcpyAsync(dks, kc.data(), sizeof(cxd) * nk, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) { cleanup(); return cuda_status(e, "ks H2D"); }
   std::vector<void*> hp(chunk);
+  std::vector<cxd> G((size_t)p * p);
+  auto fail_solver = [&](const char* what) { cleanup(); set_error("%s failed", what); return QBG_ECUDA; };
   for (int64_t k0 = 0; k0 < nk; k0 += chunk) {
     const int c = (int)std::min<int64_t>(chunk, nk - k0);
     for (int q = 0; q < c; ++q) hp[q] = A + (size_t)q * n * n;
@@ -412,14 +547,49 @@ qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig)
     if (e != cudaSuccess) { cleanup(); return cuda_status(e, "ptrs"); }
     if ((s = launch_assemble(g->d, dks + k0, c, 0, 0, dptrs, n, st))) { cleanup(); return s; }
     for (int q = 0; q < c; ++q) {
-      cusolverStatus_t cs = cusolverDnZgesvd(h, 'N', 'N', n, n, (cuDoubleComplex*)(A + (size_t)q * n * n), n, S,
-                                             nullptr, n, nullptr, n, (cuDoubleComplex*)work, lwork, rwork, dinfo);
-      if (cs != CUSOLVER_STATUS_SUCCESS) { cleanup(); set_error("cusolverDnZgesvd failed (%d)", (int)cs); return QBG_ECUDA; }
-      e = cudaMemcpyAsync(sig + k0 + q, S + (n - 1), sizeof(double), cudaMemcpyDeviceToHost, st);
-      if (e != cudaSuccess) { cleanup(); return cuda_status(e, "S D2H"); }
+      cuDoubleComplex* Aq = (cuDoubleComplex*)(A + (size_t)q * n * n);
+      if (cusolverDnZgetrf(h, n, n, Aq, n, (cuDoubleComplex*)work, ipiv, dinfo) != CUSOLVER_STATUS_SUCCESS)
+        return fail_solver("cusolverDnZgetrf");
+      int hinfo = 0;
+      e = cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(X, hx.data(), sizeof(cxd) * (size_t)n * p, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = wait_st();
+      if (e != cudaSuccess) { cleanup(); return cuda_status(e, "sigma_min LU"); }
+      if (hinfo > 0) {  // U(hinfo, hinfo) == 0: A(k) is singular
+        sig[k0 + q] = 0.0;
+        continue;
+      }
+      double est = -1.0;
+      for (int it = 0; it < SM_ITERS; ++it) {
+        // W = A^{-H} X
+        e = cudaMemcpyAsync(W, X, sizeof(cxd) * (size_t)n * p, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) { cleanup(); return cuda_status(e, "sigma_min copy"); }
+        if (cusolverDnZgetrs(h, CUBLAS_OP_C, n, p, Aq, n, ipiv, (cuDoubleComplex*)W, n, dinfo) !=
+            CUSOLVER_STATUS_SUCCESS)
+          return fail_solver("cusolverDnZgetrs");
+        // Rayleigh-Ritz: lambda_max(W^H W), X orthonormal; W^H W formed on the device
+        k_gram<<<p * p, 256, 0, st>>>(W, n, p, dG);
+        QBG_LAUNCH_CHECK("k_gram");
+        e = cudaMemcpyAsync(G.data(), dG, sizeof(cxd) * (size_t)p * p, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = wait_st();
+        if (e != cudaSuccess) { cleanup(); return cuda_status(e, "sigma_min D2H"); }
+        const double lam = herm_lambda_max(G, p);
+        const double cur = lam > 0.0 ? 1.0 / std::sqrt(lam) : 0.0;
+        const bool done = it > 0 && std::fabs(cur - est) <= 1e-13 * cur;
+        est = cur;
+        if (done || it + 1 == SM_ITERS) break;
+        // X = orth(A^{-1} W)
+        if (cusolverDnZgetrs(h, CUBLAS_OP_N, n, p, Aq, n, ipiv, (cuDoubleComplex*)W, n, dinfo) !=
+                CUSOLVER_STATUS_SUCCESS ||
+            cusolverDnZgeqrf(h, n, p, (cuDoubleComplex*)W, n, (cuDoubleComplex*)tau, (cuDoubleComplex*)work, lwork,
+                             dinfo) != CUSOLVER_STATUS_SUCCESS ||
+            cusolverDnZungqr(h, n, p, p, (cuDoubleComplex*)W, n, (cuDoubleComplex*)tau, (cuDoubleComplex*)work, lwork,
+                             dinfo) != CUSOLVER_STATUS_SUCCESS)
+          return fail_solver("sigma_min subspace step");
+        std::swap(X, W);
+      }
+      sig[k0 + q] = est;
     }
-    e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) { cleanup(); return cuda_status(e, "sigma_min"); }
   }
   cleanup();
   return QBG_OK;
@@ -444,7 +614,7 @@ qbg_status qbg_cheb_autotune(qbg_geom* g, const double* ks, int64_t nk, double t
   unsigned long long* derr = nullptr;
   QBG_TRY(dmalloc(&dks, sizeof(cxd) * nk));
   int s = dmalloc(&derr, sizeof(unsigned long long) * 4 * nk);
-  if (s) { dfree(dks); return s; }
+  if (s) { dfree(dks, st); return s; }
   std::vector<unsigned long long> herr(4 * nk);
   double worst[4] = {0, 0, 0, 0};
   cudaError_t e = cudaMemcpyAsync(dks, ks, sizeof(cxd) * nk, cudaMemcpyHostToDevice, st);
@@ -458,7 +628,7 @@ qbg_status qbg_cheb_autotune(qbg_geom* g, const double* ks, int64_t nk, double t
     if (!s && e == cudaSuccess)
       e = cudaMemcpyAsync(herr.data(), derr, sizeof(unsigned long long) * 4 * nk, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    for (void* q : ctmp) dfree(q);
+    for (void* q : ctmp) dfree(q, st);
     if (s || e != cudaSuccess) break;
     for (int f = 0; f < 4; ++f) worst[f] = 0.0;
     for (int64_t q = 0; q < nk; ++q)
@@ -478,8 +648,8 @@ qbg_status qbg_cheb_autotune(qbg_geom* g, const double* ks, int64_t nk, double t
     if (!okJ) grow(p.n_panels_j, p.M_j);
     if (p.n_panels_h > (1 << 24) || p.n_panels_j > (1 << 24)) break;
   }
-  dfree(dks);
-  dfree(derr);
+  dfree(dks, st);
+  dfree(derr, st);
   if (s) return s;
   if (e != cudaSuccess) return cuda_status(e, "qbg_cheb_autotune");
   *io = p;
@@ -515,7 +685,7 @@ qbg_status qbg_candidate_residuals(qbg_geom* g, const double* lambdas, int64_t n
   double *nrm = nullptr, *an = nullptr;
   void** dptrs = nullptr;
   std::vector<void*> tmp;
-  auto cleanup = [&]() { for (void* p : tmp) dfree(p); };
+  auto cleanup = [&]() { for (void* p : tmp) dfree(p, st); };
   auto talloc = [&](auto** p, size_t bytes) {
     int s = dmalloc(p, bytes);
     if (!s) tmp.push_back(*p);
@@ -554,7 +724,7 @@ qbg_status qbg_candidate_residuals(qbg_geom* g, const double* lambdas, int64_t n
     if (!s && e == cudaSuccess) e = cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * 4 * c, cudaMemcpyDeviceToHost, st);
     if (!s && e == cudaSuccess) e = cudaMemcpyAsync(ha.data(), an, sizeof(double) * c, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    for (void* p : ctmp) dfree(p);
+    for (void* p : ctmp) dfree(p, st);
     if (s || e != cudaSuccess) break;
     for (int q = 0; q < c; ++q) {
       double* o = out + 5 * (q0 + q);

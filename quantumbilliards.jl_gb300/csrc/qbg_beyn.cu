@@ -451,12 +451,12 @@ qbg_status create_impl(qbg_geom* g, const double* k0s, const double* Rs, int ndi
     if (e != cudaSuccess) s = cuda_status(e, "geometry stream");
   }
   if (!s) {
-    cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+    cudaError_t e = stream_create(&b->st);
     if (e != cudaSuccess) s = cuda_status(e, "cudaStreamCreate");
   }
   const char* split_env = std::getenv("QBG_LU_SPLIT");
   if (!s && !(split_env && split_env[0] == '0')) {
-    cudaError_t e = cudaStreamCreateWithFlags(&b->st2, cudaStreamNonBlocking);
+    cudaError_t e = stream_create(&b->st2);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
     if (e != cudaSuccess) s = cuda_status(e, "second LU stream");
@@ -669,7 +669,7 @@ int qr_reduce(qbg_beyn* b, double* Rh, double* Ch) {
       return QBG_ECUDA;
     }
     if (S > 1 && !b->qst[i]) {
-      QBG_CUDA(cudaStreamCreateWithFlags(&b->qst[i], cudaStreamNonBlocking));
+      QBG_CUDA(stream_create(&b->qst[i]));
       QBG_CUDA(cudaEventCreateWithFlags(&b->qev[i], cudaEventDisableTiming));
     }
   }

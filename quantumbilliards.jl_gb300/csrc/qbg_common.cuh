@@ -78,6 +78,18 @@ namespace qbg {
 void set_error(const char* fmt, ...);
 void note_launch();
 int cuda_status(cudaError_t e, const char* what);
+
+// Streams of the library: request work (assembly, Beyn, QR) one step above
+// the device's least priority, background sweeps at the least, so that the
+// block scheduler dispatches a latency-bound request's blocks ahead of a
+// sweep's FP64 factorisations. Streams at higher priorities stay above both.
+inline cudaError_t stream_create(cudaStream_t* st, bool background = false) {
+  int least = 0, greatest = 0;
+  cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  if (e != cudaSuccess) return e;
+  const int prio = background ? least : (greatest < least ? least - 1 : least);
+  return cudaStreamCreateWithPriority(st, cudaStreamNonBlocking, prio);
+}
 }  // namespace qbg
 
 #define QBG_CUDA(call)                                          \

@@ -137,32 +137,38 @@ int pool_alloc(void** out, size_t bytes) {
 void pool_free(void* p, cudaStream_t st) {
   if (!p) return;
   Pool& P = pool();
-  std::unique_lock<std::mutex> lk(P.mu);
-  auto it = P.live.find(p);
-  if (it == P.live.end()) {  // not from the pool
-    lk.unlock();
-    cudaFree(p);
-    return;
+  size_t rs = 0;
+  int dev = 0;
+  {
+    std::lock_guard<std::mutex> lk(P.mu);
+    auto it = P.live.find(p);
+    if (it == P.live.end()) {  // not from the pool
+      cudaFree(p);
+      return;
+    }
+    rs = it->second.first;
+    dev = it->second.second;
+    P.live.erase(it);
+    P.live_bytes -= rs;
+    resolve_limit(P);
+    if ((long long)rs > P.limit) {
+      if (st) cudaStreamSynchronize(st);
+      cudaFree(p);
+      return;
+    }
   }
-  const size_t rs = it->second.first;
-  const int dev = it->second.second;
-  P.live.erase(it);
-  P.live_bytes -= rs;
-  resolve_limit(P);
-  if ((long long)rs > P.limit) {
-    lk.unlock();
-    if (st) cudaStreamSynchronize(st);
-    cudaFree(p);
-    return;
-  }
+  // the wait that gates reuse happens outside the lock: a device-wide wait
+  // must not hold up the other threads' allocations
   cudaEvent_t ev = nullptr;
   if (st) {
-    if (!P.spare_events.empty()) {
-      ev = P.spare_events.back();
-      P.spare_events.pop_back();
-    } else if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
-      ev = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(P.mu);
+      if (!P.spare_events.empty()) {
+        ev = P.spare_events.back();
+        P.spare_events.pop_back();
+      }
     }
+    if (!ev && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) ev = nullptr;
     if (ev && cudaEventRecord(ev, st) != cudaSuccess) {
       cudaEventDestroy(ev);
       ev = nullptr;
@@ -171,6 +177,7 @@ void pool_free(void* p, cudaStream_t st) {
   } else {
     cudaDeviceSynchronize();
   }
+  std::lock_guard<std::mutex> lk(P.mu);
   P.cached.emplace(rs, FreeBlock{p, dev, ev});
   P.cached_bytes += rs;
   // over the limit: return the largest blocks to the driver

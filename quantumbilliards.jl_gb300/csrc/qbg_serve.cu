@@ -5,6 +5,11 @@
 // a worker takes the first of the next 16 queued requests whose estimated
 // device footprint fits the free budget, but once the head has been passed
 // over 8 times only the head may start (no starvation of large requests).
+// sigma_min sweeps are background work: at most max_sweeps of them run at
+// once, and a queued sweep over that limit is passed over without counting as
+// a pass of the head (it starts when the running sweep ends). Three sweeps in
+// flight would hold three of four workers and every FP64 pipe of the device
+// for seconds, and the Beyn and EBIM requests behind them would queue.
 // A Beyn request picks up every later queued Beyn request on the same
 // geometry with the same nq, precision and probe count (up to max_batch, as
 // long as the merged footprint fits): their contour nodes run as one
@@ -87,20 +92,30 @@ struct qbg_server {
   bool stop = false;
   int64_t next_id = 1;
   int head_skips = 0;
+  int sweeps_running = 0;
+
+  bool held_back(const Req& r) const {
+    const int cap = opts.max_sweeps > 0 ? opts.max_sweeps : 1;
+    return r.d.kind == QBG_REQ_SWEEP && sweeps_running >= cap;
+  }
 
   // with mu held: the requests to run next (empty if nothing fits)
   std::vector<std::shared_ptr<Req>> pick(size_t* bytes) {
     std::vector<std::shared_ptr<Req>> out;
-    const size_t look = head_skips >= 8 ? 1 : std::min<size_t>(queue.size(), 16);
+    size_t head = 0;  // the first request that may start now
+    while (head < queue.size() && held_back(*queue[head])) ++head;
+    if (head == queue.size()) return out;
+    const size_t look = head_skips >= 8 ? head + 1 : std::min<size_t>(queue.size(), head + 16);
     size_t at = queue.size();
-    for (size_t q = 0; q < look; ++q)
-      if (in_use + queue[q]->bytes <= budget) {
+    for (size_t q = head; q < look; ++q)
+      if (!held_back(*queue[q]) && in_use + queue[q]->bytes <= budget) {
         at = q;
         break;
       }
     if (at == queue.size()) return out;
-    head_skips = at == 0 ? 0 : head_skips + 1;
+    head_skips = at == head ? 0 : head_skips + 1;
     std::shared_ptr<Req> first = queue[at];
+    if (first->d.kind == QBG_REQ_SWEEP) ++sweeps_running;
     out.push_back(first);
     std::vector<size_t> taken{at};
     size_t total = first->bytes;
@@ -205,6 +220,7 @@ void worker(qbg_server* srv) {
     finish(group, s, err.c_str());
     for (auto& r : group) r->done = true;
     srv->in_use -= bytes;
+    if (group[0]->d.kind == QBG_REQ_SWEEP) --srv->sweeps_running;
     srv->cv_done.notify_all();
     srv->cv_work.notify_all();
   }

@@ -78,7 +78,8 @@ class BeynStats(C.Structure):
 
 
 class ServeOpts(C.Structure):
-    _fields_ = [("hbm_budget", C.c_int64), ("workers", C.c_int32), ("max_batch", C.c_int32)]
+    _fields_ = [("hbm_budget", C.c_int64), ("workers", C.c_int32), ("max_batch", C.c_int32),
+                ("max_sweeps", C.c_int32)]
 
 
 class RequestDesc(C.Structure):

@@ -40,11 +40,12 @@ class Request:
 
 class Server:
     """qbg_server: ``hbm_budget`` bytes (0 = 80% of free), ``workers`` requests
-    in flight, ``max_batch`` Beyn requests per device batch."""
+    in flight, ``max_batch`` Beyn requests per device batch, ``max_sweeps``
+    sigma_min sweeps running at once (others wait; Beyn and EBIM pass them)."""
 
-    def __init__(self, hbm_budget: int = 0, workers: int = 4, max_batch: int = 8):
+    def __init__(self, hbm_budget: int = 0, workers: int = 4, max_batch: int = 8, max_sweeps: int = 1):
         lib = _lib()
-        o = ServeOpts(int(hbm_budget), int(workers), int(max_batch))
+        o = ServeOpts(int(hbm_budget), int(workers), int(max_batch), int(max_sweeps))
         h = C.c_void_p()
         L.check(lib.qbg_serve_create(C.byref(o), C.byref(h)))
         self._h = h

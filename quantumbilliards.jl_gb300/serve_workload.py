@@ -8,9 +8,9 @@ Seeded synthetic stream: geometry uniform over {unit circle with an
 off-centre hole of radius 0.2 (CFIE), full stadium (DLP, smooth composite),
 half-ellipse-cap mushroom (DLP, corner-graded, kressq = 4), star
 r = 1 + 0.2 cos 5 theta (CFIE)}; N log-uniform in [nmin, nmax] (rounded
-to the node-count rule); k uniform in [kmin, kmax]; 60% Beyn disks (radius
-0.5, 32..64 contour nodes, L probes, mixed form), 30% EBIM (A, A', A'' at
-one k), 10% sigma_min sweeps (nk wavenumbers). Discretisations are built and
+to the node-count rule); k uniform in [kmin, kmax]; by default 60% Beyn disks
+(radius 0.5, 32..64 contour nodes, L probes, mixed form), 30% EBIM (A, A',
+A'' at one k), 10% sigma_min sweeps (nk wavenumbers), set by --mix. Discretisations are built and
 uploaded before the clock starts; the clock covers submission, the device
 work, the copies back and the host part of a Beyn request (SVD, eigvals).
 """
@@ -45,7 +45,7 @@ def make_stream(qb, args):
         n = int(round(math.exp(rng.uniform(math.log(args.nmin), math.log(args.nmax)))))
         k = float(rng.uniform(args.kmin, args.kmax))
         u = rng.uniform()
-        kind = "beyn" if u < 0.6 else ("ebim" if u < 0.9 else "sweep")
+        kind = "beyn" if u < args.mix[0] else ("ebim" if u < args.mix[0] + args.mix[1] else "sweep")
         sol = cls(1.0, bil)
         pts, sol = qb.points_with_n(sol, bil, n, k)
         ws = qb.Workspace(sol, pts)
@@ -72,8 +72,11 @@ def main(argv=None):
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--workers", type=int, default=4)
     ap.add_argument("--max-batch", type=int, default=8)
+    ap.add_argument("--max-sweeps", type=int, default=1)
     ap.add_argument("--seed", type=int, default=4)
+    ap.add_argument("--mix", default="0.6,0.3,0.1", help="fractions of Beyn, EBIM and sweep requests")
     a = ap.parse_args(argv)
+    a.mix = [float(x) for x in a.mix.split(",")]
     import build_qbgpu
     build_qbgpu.build()
     import qbgpu as qb
@@ -81,7 +84,8 @@ def main(argv=None):
     lat = {}
     info = {}
     lock = threading.Lock()
-    with qb.Server(hbm_budget=int(a.budget_gb * 2 ** 30), workers=a.workers, max_batch=a.max_batch) as srv, \
+    with qb.Server(hbm_budget=int(a.budget_gb * 2 ** 30), workers=a.workers, max_batch=a.max_batch,
+                   max_sweeps=a.max_sweeps) as srv, \
             ThreadPoolExecutor(max_workers=64) as pool:
         t0 = time.perf_counter()
 
@@ -94,7 +98,8 @@ def main(argv=None):
                 nl = int(np.count_nonzero((np.abs(lam - reqs[i]["k"]) < 0.5) & (np.abs(lam.imag) < 1e-3)))
             with lock:
                 lat[i] = (done - t_arr) * 1e3
-                info[i] = dict(batched=res["batched"], queue_ms=res["queue_ms"], run_ms=res["run_ms"], eig=nl)
+                info[i] = dict(batched=res["batched"], queue_ms=res["queue_ms"], run_ms=res["run_ms"], eig=nl,
+                               lag_ms=(h.t_submit - t_arr) * 1e3, wait_ms=(done - h.t_submit) * 1e3)
 
         futs = []
         for i, r in enumerate(reqs):
@@ -115,9 +120,16 @@ def main(argv=None):
     L = np.array([lat[i] for i in range(len(reqs))])
     per = {}
     for kind in ("beyn", "ebim", "sweep"):
-        v = np.array([lat[i] for i in range(len(reqs)) if reqs[i]["kind"] == kind])
+        idx = [i for i in range(len(reqs)) if reqs[i]["kind"] == kind]
+        v = np.array([lat[i] for i in idx])
         if len(v):
-            per[kind] = dict(count=int(len(v)), p50_ms=float(np.percentile(v, 50)), p99_ms=float(np.percentile(v, 99)))
+            qv = np.array([info[i]["queue_ms"] for i in idx])
+            rv = np.array([info[i]["run_ms"] for i in idx])
+            lv = np.array([info[i]["lag_ms"] for i in idx])
+            hv = np.array([info[i]["wait_ms"] - info[i]["queue_ms"] - info[i]["run_ms"] for i in idx])
+            per[kind] = dict(count=int(len(v)), p50_ms=float(np.percentile(v, 50)), p99_ms=float(np.percentile(v, 99)),
+                             submit_lag_p50_ms=float(np.percentile(lv, 50)), queue_p50_ms=float(np.percentile(qv, 50)),
+                             run_p50_ms=float(np.percentile(rv, 50)), host_p50_ms=float(np.percentile(hv, 50)))
     eig = sum(info[i]["eig"] for i in info)
     out = dict(requests=len(reqs), rate_per_s=a.rate, wall_s=wall, p50_ms=float(np.percentile(L, 50)),
                p99_ms=float(np.percentile(L, 99)), mean_ms=float(L.mean()), throughput_req_per_s=len(reqs) / wall,
@@ -125,7 +137,8 @@ def main(argv=None):
                beyn_batched_max=max([info[i]["batched"] for i in info] + [1]),
                beyn_in_batches=int(sum(1 for i in info if info[i]["batched"] > 1)),
                config=dict(nmin=a.nmin, nmax=a.nmax, kmin=a.kmin, kmax=a.kmax, L=a.L, nk=a.nk,
-                           budget_gb=a.budget_gb, workers=a.workers, max_batch=a.max_batch, seed=a.seed))
+                           budget_gb=a.budget_gb, workers=a.workers, max_batch=a.max_batch, max_sweeps=a.max_sweeps,
+                           seed=a.seed, mix=a.mix))
     print(json.dumps(out))
 
 

@@ -152,3 +152,16 @@ def test_beyn_eigenvalues_plain_vs_oracle_and_mixed(qb):
     f = sel(lf)
     assert len(f) == len(a)
     assert np.max(np.abs(f - a) / np.abs(a)) < 1e-7
+
+
+def test_sigma_min_star_cfie_vs_oracle(qb):
+    """sigma_min of a CFIE operator without symmetry (a generic spectrum) at
+    several k: inverse iteration agrees with the oracle's full SVD to 1e-10."""
+    b = qb.make_star(0.2, 5)
+    sol = qb.CFIE_kress(1.0, b)
+    pts, sol = qb.points_with_n(sol, b, 300, 15.0)
+    ws = qb.Workspace(sol, pts)
+    ks = np.linspace(14.6, 15.4, 5)
+    sig = qb.sigma_min(ws, ks)
+    ref = np.array([OB.sigma_min(OA.cfie_matrix(pts, k)) for k in ks])
+    assert np.allclose(sig, ref, rtol=1e-10, atol=0.0)
