@@ -242,6 +242,37 @@ qbg_status qbg_beyn_destroy(qbg_beyn* b);
  * singular A(k). */
 qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig);
 
+/* EBIM eigen step at a trial wavenumber k (ebim.jl): the eigenpairs of the
+ * pencil A v = lambda A' v nearest 0, by FP64 LU of A and block shift-invert
+ * iteration on A^{-1} A' (and its adjoint for the left vectors), then the
+ * second-order correction eps1 = -lambda, eps2 = -eps1^2/2 (u^H A'' v)/(u^H A' v)
+ * (0 when |u^H A' v| <= 1e-15) for every lambda with |Re|, |Im| < dk.
+ * Default: solve_krylov! (ebim.jl:464-537): the nev eigenvalues nearest 0, u
+ *   the eigenvector of (A^{-1} A')^H, a result kept when |Re(k_c) - k| < dk.
+ * QBG_EBIM_FULL: solve_full! (ebim.jl:336-375): every eigenvalue inside the
+ *   dk box (nev is the starting block, doubled until the box is covered), u the
+ *   left eigenvector of the pencil.
+ * Writes up to cap results, nearest first: out_k[2i], out_k[2i+1] = corrected
+ * k (complex; the reference returns its real part unless return_imag_part),
+ * out_tens[i] = |eps1 + eps2|; *count = the number of results (may exceed
+ * cap). iters (optional, 3 values): iterations of the right and left blocks
+ * and the final nev. QBG_ESINGULAR when A(k) is exactly singular.
+ * qbg_ebim_eig takes the three N x N complex128 column-major matrices (host,
+ * or device with QBG_PTR_DEVICE; left unchanged); qbg_ebim_solve assembles
+ * A, A', A'' of the geometry at k on the device first (direct FP64 assembly,
+ * as qbg_assemble with deriv = 1). */
+enum { QBG_EBIM_FULL = 8 };
+qbg_status qbg_ebim_eig(int64_t n, const void* A, const void* dA, const void* ddA, double k, double dk, int32_t nev,
+                        int32_t flags, int32_t cap, double* out_k, double* out_tens, int32_t* count,
+                        int32_t* iters);
+qbg_status qbg_ebim_solve(qbg_geom* g, double k, double dk, int32_t nev, int32_t flags, int32_t cap, double* out_k,
+                          double* out_tens, int32_t* count, int32_t* iters);
+/* The host eigen-decomposition behind the EBIM Rayleigh-Ritz step, for
+ * validation: eigenvalues w (p complex) and unit eigenvectors V (p x p
+ * column-major, complex interleaved) of the p x p complex matrix H (Hessenberg
+ * reduction, shifted QR, back substitution; no device work). */
+qbg_status qbg_small_eig(int32_t p, const double* H, double* w, double* V);
+
 /* Panel autotuner (chebyshev_params, chebyshev_optimal_panelization.jl:221-307):
  * starting from *io (zeros = 15000, 5, 3000, 5), grows the panel counts by
  * 1.5x per iteration (every 5th iteration the degrees by grow_M instead; the

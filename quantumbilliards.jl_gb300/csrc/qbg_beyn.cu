@@ -48,10 +48,12 @@ struct qbg_beyn {
   int res0 = -1, resn = 0;  // nodes [res0, res0 + resn) are factored in the slots
   std::vector<void*> allocs;
   cudaStream_t st = nullptr;
-  // second stream of the LU and the triangular solves (two halves of the
-  // operator batch run concurrently); QBG_LU_SPLIT=0 in the environment keeps
-  // everything on st (the results are the same either way)
-  cudaStream_t st2 = nullptr;
+  // extra streams of the LU and the triangular solves: nsplit parts of the
+  // operator batch run concurrently. QBG_LU_SPLIT in the environment sets the
+  // number of parts (default 4, at most 4; 0 or 1 keeps everything on st);
+  // the results are the same either way
+  int nsplit = 1;
+  cudaStream_t stx[LUBatch<float>::MAX_SPLIT - 1] = {};
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // helper streams of the per-disk QR of the moments (created on first use)
   static constexpr int QR_STREAMS = 8;
@@ -74,11 +76,12 @@ struct qbg_beyn {
     dfree(macc1, st);
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
-    if (st2) {
-      cudaStreamSynchronize(st2);
-      tc_release_scratch(st2);
-      cudaStreamDestroy(st2);
-    }
+    for (cudaStream_t x : stx)
+      if (x) {
+        cudaStreamSynchronize(x);
+        tc_release_scratch(x);
+        cudaStreamDestroy(x);
+      }
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
     for (int i = 0; i < QR_STREAMS; ++i) {
@@ -119,7 +122,8 @@ int setup_lu(qbg_beyn* b, LUBatch<T>& f, int nb, int solve_levels) {
   QBG_TRY(b->alloc(&f.Uinv, sizeof(cx<T>) * (size_t)f.nblk * nb * nb * f.batch));
   // the FP64 LU is bound by the FP64 pipe: a second stream only adds contention
   if (sizeof(T) == sizeof(float)) {
-    f.st2 = b->st2;
+    f.nsplit = b->nsplit;
+    for (int i = 0; i + 1 < b->nsplit; ++i) f.stx[i] = b->stx[i];
     f.ev_fork = b->ev_fork;
     f.ev_join = b->ev_join;
   }
@@ -455,11 +459,14 @@ qbg_status create_impl(qbg_geom* g, const double* k0s, const double* Rs, int ndi
     if (e != cudaSuccess) s = cuda_status(e, "cudaStreamCreate");
   }
   const char* split_env = std::getenv("QBG_LU_SPLIT");
-  if (!s && !(split_env && split_env[0] == '0')) {
-    cudaError_t e = stream_create(&b->st2);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
+  int parts = (split_env && *split_env) ? std::atoi(split_env) : LUBatch<float>::MAX_SPLIT;
+  parts = std::max(1, std::min(parts, LUBatch<float>::MAX_SPLIT));
+  if (!s && parts > 1) {
+    cudaError_t e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
-    if (e != cudaSuccess) s = cuda_status(e, "second LU stream");
+    for (int i = 0; i + 1 < parts && e == cudaSuccess; ++i) e = stream_create(&b->stx[i]);
+    if (e != cudaSuccess) s = cuda_status(e, "LU streams");
+    else b->nsplit = parts;
   }
   if (!s) s = setup(b, k0s, Rs);
   if (!s && b->cap == b->nn) s = load(b, 0, b->nn);

@@ -1,0 +1,762 @@
+// EBIM eigen step on the device: the second-order expansion of the boundary
+// operator about a trial k (A(k + eps) = A + eps A' + eps^2/2 A'' + ...).
+//
+// The eigenpairs of the pencil A v = lambda A' v nearest 0 are those of
+// largest |mu| of C = A^{-1} A' (mu = 1 / lambda). They are found by block
+// shift-invert iteration: one FP64 LU of A (cuSOLVER getrf) and from it A^-1
+// and A^-H, then Q <- orth(C Q) with p vectors (C Q = A^-1 (A' Q): two skinny
+// split-k products; Cholesky QR twice for orth), Rayleigh-Ritz on the p x p projection
+// Q^H C Q (formed on the device, eigen-decomposed on the host: a few
+// microseconds at this size) after every step, until the nev largest Ritz
+// values change by less than 1e-13 relative. The left vectors u come from the same
+// iteration on C^H = A'^H A^{-H}, paired with the right ones by
+// mu_l ~ conj(mu_r). Then, per accepted lambda (|Re|, |Im| < dk):
+//   eps1 = -lambda, eps2 = -eps1^2 / 2 (u^H A'' v) / (u^H A' v)
+// (0 when |u^H A' v| <= 1e-15), corrected k = k + eps1 + eps2, tension
+// |eps1 + eps2|.
+//
+// Two conventions, as in the reference:
+// * solve_krylov! (ebim.jl:464-537): the nev eigenvalues of largest |mu|; u is
+//   the eigenvector of C^H itself (the reference pairs it with v as is), and a
+//   corrected k is kept only when |Re(k_c) - k| < dk.
+// * solve_full! (ebim.jl:336-375, QBG_EBIM_FULL): every eigenvalue inside the
+//   dk box; u is the left eigenvector of the pencil, u~ = A^{-H} u
+//   (u~^H A = lambda u~^H A'), as LAPACK's generalized eigensolver returns it.
+//   The block grows (nev doubles) until the nev-th eigenvalue lies outside the
+//   disk |lambda| < sqrt(2) dk that contains the box, so none is missed.
+// Results do not depend on how the eigenpairs are converged: the reference
+// uses Arnoldi (KrylovKit) and QZ (LAPACK); here a block iteration converges
+// the same eigenpairs to FP64 accuracy.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <vector>
+#include <cusolverDn.h>
+#include "qbg_common.cuh"
+#include "qbg_handles.cuh"
+#include "qbg_linalg.cuh"
+#include "qbgpu.h"
+
+using namespace qbg;
+
+namespace {
+
+typedef std::complex<double> zc;
+
+// G[a + b p] = sum_r conj(X[r, a]) Y[r, b], a < p, b < q; one CTA per entry
+__global__ void k_inner(const cxd* __restrict__ X, const cxd* __restrict__ Y, int n, int p, cxd* __restrict__ G) {
+  const int a = blockIdx.x % p, b = blockIdx.x / p;
+  const cxd* x = X + (size_t)a * n;
+  const cxd* y = Y + (size_t)b * n;
+  double re = 0.0, im = 0.0;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    const cxd u = x[r], v = y[r];
+    re = fma(u.re, v.re, fma(u.im, v.im, re));
+    im = fma(u.re, v.im, fma(-u.im, v.re, im));
+  }
+  __shared__ double sr[8], si[8];
+  for (int o = 16; o > 0; o >>= 1) {
+    re += __shfl_xor_sync(0xffffffffu, re, o);
+    im += __shfl_xor_sync(0xffffffffu, im, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    sr[threadIdx.x >> 5] = re;
+    si[threadIdx.x >> 5] = im;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tr = 0.0, ti = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      tr += sr[w];
+      ti += si[w];
+    }
+    G[blockIdx.x] = cxd(tr, ti);
+  }
+}
+
+// AH = A^H for n x n column-major A, through 32 x 32 shared-memory tiles
+__global__ void k_conj_transpose(const cxd* __restrict__ A, cxd* __restrict__ AH, int n) {
+  __shared__ cxd t[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int r = bx + threadIdx.x, c = by + j;
+    if (r < n && c < n) t[j][threadIdx.x] = A[r + (size_t)c * n];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int r = by + threadIdx.x, c = bx + j;  // AH[r, c] = conj(A[c, r]) = conj(t[r - by][c - bx])
+    if (r < n && c < n) {
+      const cxd v = t[threadIdx.x][j];
+      AH[r + (size_t)c * n] = cxd(v.re, -v.im);
+    }
+  }
+}
+
+__global__ void k_identity(cxd* __restrict__ M, int n) {
+  const size_t count = (size_t)n * n;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+    M[i] = cxd(i % (size_t)(n + 1) == 0 ? 1.0 : 0.0, 0.0);
+}
+
+// ---------------------------------------------------------------------------
+// Y = A X for n x n A and n x q X, q <= TALL_MAXQ (FP64 complex, column-major):
+// split over k into ks slices so that a skinny product still fills the device;
+// each CTA computes a 64-row block of one slice's partial product, and a
+// second kernel sums the slices in a fixed order (deterministic).
+// ---------------------------------------------------------------------------
+constexpr int TALL_MAXQ = 128, TALL_KC = 16;  // 16 KB + 32 KB of static shared memory
+
+// CPT: columns per thread (q <= 4 CPT)
+template <int CPT>
+__global__ void __launch_bounds__(256) k_zgemm_tall(const cxd* __restrict__ A, const cxd* __restrict__ X, int n,
+                                                    int q, int kslice, cxd* __restrict__ P) {
+  __shared__ cxd As[TALL_KC][64];
+  __shared__ cxd Xs[TALL_KC][4 * CPT];
+  const int r0 = blockIdx.x * 64, s = blockIdx.y;
+  const int k0 = s * kslice, k1 = min(n, k0 + kslice);
+  const int tr = threadIdx.x & 63, tg = threadIdx.x >> 6;  // row, column group (columns tg, tg + 4, ...)
+  double ar[CPT], ai[CPT];
+#pragma unroll
+  for (int c = 0; c < CPT; ++c) ar[c] = ai[c] = 0.0;
+  for (int kc = k0; kc < k1; kc += TALL_KC) {
+    for (int e = threadIdx.x; e < TALL_KC * 64; e += 256) {
+      const int rr = e & 63, kk = e >> 6;
+      const int r = r0 + rr, k = kc + kk;
+      As[kk][rr] = (r < n && k < k1) ? A[r + (size_t)k * n] : cxd(0, 0);
+    }
+    for (int e = threadIdx.x; e < TALL_KC * q; e += 256) {
+      const int kk = e % TALL_KC, j = e / TALL_KC;
+      const int k = kc + kk;
+      Xs[kk][j] = (k < k1) ? X[k + (size_t)j * n] : cxd(0, 0);
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int kk = 0; kk < TALL_KC; ++kk) {
+      const cxd a = As[kk][tr];
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) {
+        const int j = tg + 4 * c;
+        if (j < q) {
+          const cxd x = Xs[kk][j];
+          ar[c] = fma(a.re, x.re, fma(-a.im, x.im, ar[c]));
+          ai[c] = fma(a.re, x.im, fma(a.im, x.re, ai[c]));
+        }
+      }
+    }
+    __syncthreads();
+  }
+  const int r = r0 + tr;
+  if (r < n) {
+    cxd* ps = P + (size_t)s * n * q;
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) {
+      const int j = tg + 4 * c;
+      if (j < q) ps[r + (size_t)j * n] = cxd(ar[c], ai[c]);
+    }
+  }
+}
+
+__global__ void k_sum_slices(const cxd* __restrict__ P, int ks, size_t count, cxd* __restrict__ Y) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
+    double re = 0.0, im = 0.0;
+    for (int s = 0; s < ks; ++s) {
+      re += P[s * count + i].re;
+      im += P[s * count + i].im;
+    }
+    Y[i] = cxd(re, im);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Eigen-decomposition of a small complex matrix on the host (the Rayleigh-Ritz
+// step): Householder reduction to Hessenberg form, single-shift QR sweeps with
+// Givens rotations and Wilkinson shifts (exceptional shifts after 10 sweeps
+// without deflation) to the Schur form T = Z^H H Z, eigenvectors of T by
+// back substitution, V = Z Y with unit columns. Golub and Van Loan, Matrix
+// Computations, algorithms 7.4.2 (Hessenberg), 7.5 (shifted QR), 7.6.4
+// (eigenvectors of a triangular matrix).
+// ---------------------------------------------------------------------------
+int small_eig(int p, std::vector<zc>& H, std::vector<zc>& w, std::vector<zc>& V) {
+  auto h = [&](int i, int j) -> zc& { return H[(size_t)j * p + i]; };
+  std::vector<zc> Z((size_t)p * p, zc(0.0, 0.0));
+  auto z = [&](int i, int j) -> zc& { return Z[(size_t)j * p + i]; };
+  for (int i = 0; i < p; ++i) z(i, i) = 1.0;
+  double hnorm = 0.0;
+  for (const zc& x : H) hnorm = std::max(hnorm, std::abs(x));
+  // Hessenberg reduction
+  std::vector<zc> v(p);
+  for (int j = 0; j + 2 < p; ++j) {
+    double xn = 0.0;
+    for (int i = j + 1; i < p; ++i) xn += std::norm(h(i, j));
+    xn = std::sqrt(xn);
+    if (xn == 0.0) continue;
+    const zc x0 = h(j + 1, j);
+    const zc ph = std::abs(x0) > 0.0 ? x0 / std::abs(x0) : zc(1.0, 0.0);
+    const zc alpha = -ph * xn;
+    for (int i = j + 1; i < p; ++i) v[i] = h(i, j);
+    v[j + 1] -= alpha;
+    double vn = 0.0;
+    for (int i = j + 1; i < p; ++i) vn += std::norm(v[i]);
+    if (vn == 0.0) continue;
+    const double beta = 2.0 / vn;
+    // H = (I - beta v v^H) H
+    for (int c = 0; c < p; ++c) {
+      zc t(0.0, 0.0);
+      for (int i = j + 1; i < p; ++i) t += std::conj(v[i]) * h(i, c);
+      t *= beta;
+      for (int i = j + 1; i < p; ++i) h(i, c) -= v[i] * t;
+    }
+    // H = H (I - beta v v^H), Z = Z (I - beta v v^H)
+    for (int rr = 0; rr < p; ++rr) {
+      zc t(0.0, 0.0), tz(0.0, 0.0);
+      for (int i = j + 1; i < p; ++i) {
+        t += h(rr, i) * v[i];
+        tz += z(rr, i) * v[i];
+      }
+      t *= beta;
+      tz *= beta;
+      for (int i = j + 1; i < p; ++i) {
+        h(rr, i) -= t * std::conj(v[i]);
+        z(rr, i) -= tz * std::conj(v[i]);
+      }
+    }
+    for (int i = j + 2; i < p; ++i) h(i, j) = 0.0;
+  }
+  // shifted QR on the active window [lo, hi]
+  const double eps = 2.220446049250313e-16;
+  int hi = p - 1, since = 0, total = 0;
+  while (hi > 0) {
+    if (++total > 100 * p) {
+      set_error("small_eig: QR iteration did not converge");
+      return QBG_ECUDA;
+    }
+    int lo = hi;
+    while (lo > 0) {
+      const double sc = std::abs(h(lo - 1, lo - 1)) + std::abs(h(lo, lo));
+      if (std::abs(h(lo, lo - 1)) <= eps * (sc > 0.0 ? sc : hnorm)) {
+        h(lo, lo - 1) = 0.0;
+        break;
+      }
+      --lo;
+    }
+    if (lo == hi) {  // 1 x 1 block converged
+      --hi;
+      since = 0;
+      continue;
+    }
+    zc mu;
+    if (since > 0 && since % 10 == 0) {
+      mu = h(hi, hi) + zc(0.75 * std::abs(h(hi, hi - 1)), 0.0);  // exceptional shift
+    } else {
+      const zc a = h(hi - 1, hi - 1), b = h(hi - 1, hi), c = h(hi, hi - 1), d = h(hi, hi);
+      const zc tr = 0.5 * (a + d), det = a * d - b * c;
+      const zc disc = std::sqrt(tr * tr - det);
+      const zc m1 = tr + disc, m2 = tr - disc;
+      mu = std::abs(m1 - d) < std::abs(m2 - d) ? m1 : m2;
+    }
+    ++since;
+    zc x = h(lo, lo) - mu, y = h(lo + 1, lo);
+    for (int k = lo; k < hi; ++k) {
+      if (k > lo) {
+        x = h(k, k - 1);
+        y = h(k + 1, k - 1);
+      }
+      const double ax = std::abs(x), ay = std::abs(y);
+      if (ay == 0.0) continue;
+      const double r = std::hypot(ax, ay);
+      double c;
+      zc sgn, sn;
+      if (ax == 0.0) {
+        c = 0.0;
+        sn = std::conj(y) / ay;
+      } else {
+        c = ax / r;
+        sgn = x / ax;
+        sn = sgn * std::conj(y) / r;
+      }
+      // rows k, k + 1 (every column from k - 1 on)
+      for (int col = std::max(k - 1, 0); col < p; ++col) {
+        const zc a = h(k, col), b = h(k + 1, col);
+        h(k, col) = c * a + sn * b;
+        h(k + 1, col) = -std::conj(sn) * a + c * b;
+      }
+      // columns k, k + 1 (rows 0 .. min(k + 2, hi)) and Z
+      const int rmax = std::min(k + 2, hi);
+      for (int rr = 0; rr <= rmax; ++rr) {
+        const zc a = h(rr, k), b = h(rr, k + 1);
+        h(rr, k) = c * a + std::conj(sn) * b;
+        h(rr, k + 1) = -sn * a + c * b;
+      }
+      for (int rr = 0; rr < p; ++rr) {
+        const zc a = z(rr, k), b = z(rr, k + 1);
+        z(rr, k) = c * a + std::conj(sn) * b;
+        z(rr, k + 1) = -sn * a + c * b;
+      }
+      if (k > lo) h(k + 1, k - 1) = 0.0;
+    }
+  }
+  // eigenvalues and eigenvectors of the triangular T
+  w.assign(p, zc(0.0, 0.0));
+  for (int i = 0; i < p; ++i) w[i] = h(i, i);
+  V.assign((size_t)p * p, zc(0.0, 0.0));
+  std::vector<zc> x(p);
+  const double smin = std::max(eps * hnorm, 1e-300);
+  for (int k = 0; k < p; ++k) {
+    std::fill(x.begin(), x.end(), zc(0.0, 0.0));
+    x[k] = 1.0;
+    for (int i = k - 1; i >= 0; --i) {
+      zc t = h(i, k);
+      for (int j = i + 1; j < k; ++j) t += h(i, j) * x[j];
+      zc den = h(i, i) - w[k];
+      if (std::abs(den) < smin) den = smin;
+      x[i] = -t / den;
+    }
+    double nrm = 0.0;
+    for (int rr = 0; rr < p; ++rr) {
+      zc t(0.0, 0.0);
+      for (int j = 0; j <= k; ++j) t += z(rr, j) * x[j];
+      V[(size_t)k * p + rr] = t;
+      nrm += std::norm(t);
+    }
+    nrm = std::sqrt(nrm);
+    if (nrm > 0.0)
+      for (int rr = 0; rr < p; ++rr) V[(size_t)k * p + rr] /= nrm;
+  }
+  return QBG_OK;
+}
+
+struct Ebim {
+  int n = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev = nullptr;
+  cusolverDnHandle_t h = nullptr;
+  cxd *LU = nullptr, *dA = nullptr, *ddA = nullptr, *dAH = nullptr, *Ainv = nullptr, *AinvH = nullptr;
+  int *ipiv = nullptr, *dinfo = nullptr;
+  std::vector<void*> tmp;
+  ~Ebim() {
+    if (st) cudaStreamSynchronize(st);
+    for (void* q : tmp) dfree(q, st);
+    if (h) cusolverDnDestroy(h);
+    if (ev) cudaEventDestroy(ev);
+  }
+  template <class P>
+  int alloc(P** q, size_t bytes) {
+    int s = dmalloc(q, bytes);
+    if (!s) tmp.push_back(*q);
+    return s;
+  }
+  int wait() {
+    cudaError_t e = cudaEventRecord(ev, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev);
+    return e == cudaSuccess ? QBG_OK : cuda_status(e, "EBIM wait");
+  }
+};
+
+int solver_fail(const char* what) {
+  set_error("%s failed", what);
+  return QBG_ECUDA;
+}
+
+// Y = A B for n x n A and n x q B (FP64 complex); P: scratch of
+// tall_scratch(n, q) elements
+int tall_slices(int n) {
+  const int rb = (n + 63) / 64;
+  const int want = std::max(1, std::min(16, (2 * 152 + rb - 1) / rb));
+  return std::min(want, std::max(1, n / TALL_KC));
+}
+size_t tall_scratch(int n, int q) { return (size_t)tall_slices(n) * n * q; }
+
+int gemm_nq(const cxd* A, const cxd* B, cxd* Y, int n, int q, cxd* P, cudaStream_t st) {
+  if (q > TALL_MAXQ) return gemm_batched<double>(n, q, n, cxd(1, 0), A, n, 0, B, n, 0, cxd(0, 0), Y, n, 0, 1, st);
+  const int ks = tall_slices(n);
+  const int kslice = ((n + ks - 1) / ks + TALL_KC - 1) / TALL_KC * TALL_KC;
+  const int nsl = (n + kslice - 1) / kslice;
+  const dim3 grd((n + 63) / 64, nsl);
+  if (q <= 32)
+    k_zgemm_tall<8><<<grd, 256, 0, st>>>(A, B, n, q, kslice, P);
+  else if (q <= 64)
+    k_zgemm_tall<16><<<grd, 256, 0, st>>>(A, B, n, q, kslice, P);
+  else
+    k_zgemm_tall<32><<<grd, 256, 0, st>>>(A, B, n, q, kslice, P);
+  QBG_LAUNCH_CHECK("k_zgemm_tall");
+  const size_t count = (size_t)n * q;
+  k_sum_slices<<<(unsigned)std::min<size_t>((count + 255) / 256, 4096), 256, 0, st>>>(P, nsl, count, Y);
+  QBG_LAUNCH_CHECK("k_sum_slices");
+  return QBG_OK;
+}
+
+// orthonormal basis of the columns of W (n x p) in place, Householder QR
+int householder_orth(Ebim& E, cxd* W, int p, cxd* tau, cxd* work, int lwork) {
+  if (cusolverDnZgeqrf(E.h, E.n, p, (cuDoubleComplex*)W, E.n, (cuDoubleComplex*)tau, (cuDoubleComplex*)work, lwork,
+                       E.dinfo) != CUSOLVER_STATUS_SUCCESS ||
+      cusolverDnZungqr(E.h, E.n, p, p, (cuDoubleComplex*)W, E.n, (cuDoubleComplex*)tau, (cuDoubleComplex*)work, lwork,
+                       E.dinfo) != CUSOLVER_STATUS_SUCCESS)
+    return solver_fail("EBIM QR");
+  return QBG_OK;
+}
+
+// Buffers of the orthonormalisation: Gram matrix, its factor, a copy of W.
+struct OrthWork {
+  cxd *G = nullptr, *M = nullptr, *Wt = nullptr, *tau = nullptr, *work = nullptr;
+  int lwork = 0;
+  std::vector<cxd> hg, hm;
+};
+
+// Orthonormal basis of the columns of W (n x p) in place by Cholesky QR, twice
+// (the second pass restores orthogonality to rounding): G = W^H W on the
+// device; on the host, with D = diag(G)^(1/2), the Cholesky factor R of
+// D^-1 G D^-1 and M = D^-1 R^-1; then W <- W M. Falls back to Householder
+// QR when the scaled Gram matrix is not numerically positive definite.
+int orthonormalize(Ebim& E, cxd* W, int p, OrthWork& o) {
+  const int n = E.n;
+  o.hg.resize((size_t)p * p);
+  o.hm.resize((size_t)p * p);
+  std::vector<zc> R((size_t)p * p), Ri((size_t)p * p);
+  std::vector<double> d(p);
+  for (int pass = 0; pass < 2; ++pass) {
+    k_inner<<<p * p, 256, 0, E.st>>>(W, W, n, p, o.G);
+    QBG_LAUNCH_CHECK("k_inner");
+    QBG_CUDA(cudaMemcpyAsync(o.hg.data(), o.G, sizeof(cxd) * o.hg.size(), cudaMemcpyDeviceToHost, E.st));
+    QBG_TRY(E.wait());
+    auto g = [&](int i, int j) { return zc(o.hg[(size_t)j * p + i].re, o.hg[(size_t)j * p + i].im); };
+    bool ok = true;
+    for (int i = 0; i < p && ok; ++i) {
+      const double gi = g(i, i).real();
+      ok = std::isfinite(gi) && gi > 0.0;
+      d[i] = ok ? std::sqrt(gi) : 1.0;
+    }
+    // Cholesky of the scaled Gram matrix, S = R^H R with R upper triangular
+    std::fill(R.begin(), R.end(), zc(0.0, 0.0));
+    for (int j = 0; j < p && ok; ++j) {
+      double djj = g(j, j).real() / (d[j] * d[j]);
+      for (int k = 0; k < j; ++k) djj -= std::norm(R[(size_t)j * p + k]);
+      if (!(djj > 1e-13)) {
+        ok = false;
+        break;
+      }
+      const double rjj = std::sqrt(djj);
+      R[(size_t)j * p + j] = rjj;
+      for (int i = j + 1; i < p; ++i) {
+        zc t = g(j, i) / (d[j] * d[i]);
+        for (int k = 0; k < j; ++k) t -= std::conj(R[(size_t)j * p + k]) * R[(size_t)i * p + k];
+        R[(size_t)i * p + j] = t / rjj;
+      }
+    }
+    if (!ok) return householder_orth(E, W, p, o.tau, o.work, o.lwork);
+    // Ri = R^-1 (upper triangular), M = D^-1 Ri
+    std::fill(Ri.begin(), Ri.end(), zc(0.0, 0.0));
+    for (int j = 0; j < p; ++j) {
+      Ri[(size_t)j * p + j] = 1.0 / R[(size_t)j * p + j];
+      for (int i = j - 1; i >= 0; --i) {
+        zc t(0.0, 0.0);
+        for (int k = i + 1; k <= j; ++k) t += R[(size_t)k * p + i] * Ri[(size_t)j * p + k];
+        Ri[(size_t)j * p + i] = -t / R[(size_t)i * p + i];
+      }
+    }
+    for (int j = 0; j < p; ++j)
+      for (int i = 0; i < p; ++i) {
+        const zc m = Ri[(size_t)j * p + i] / d[i];
+        o.hm[(size_t)j * p + i] = cxd(m.real(), m.imag());
+      }
+    QBG_CUDA(cudaMemcpyAsync(o.M, o.hm.data(), sizeof(cxd) * o.hm.size(), cudaMemcpyHostToDevice, E.st));
+    QBG_CUDA(cudaMemcpyAsync(o.Wt, W, sizeof(cxd) * (size_t)n * p, cudaMemcpyDeviceToDevice, E.st));
+    QBG_TRY(gemm_batched<double>(n, p, p, cxd(1, 0), o.Wt, n, 0, o.M, p, 0, cxd(0, 0), W, n, 0, 1, E.st));
+  }
+  return QBG_OK;
+}
+
+// The nev eigenvalues of largest modulus of C = A^{-1} A' (adjoint: of
+// C^H = A'^H A^{-H}) and their eigenvectors (device, n x nev), largest first.
+int block_eigs(Ebim& E, bool adjoint, int p, int nev, std::vector<zc>& mu, cxd* V, int* iters) {
+  const int n = E.n;
+  constexpr int MAXIT = 400;
+  constexpr double TOL = 1e-13;
+  cxd *Q = nullptr, *Y = nullptr, *T = nullptr, *H = nullptr, *Xs = nullptr, *P = nullptr;
+  const size_t np = (size_t)n * p, pp = (size_t)p * p;
+  OrthWork o;
+  QBG_TRY(E.alloc(&Q, sizeof(cxd) * np));
+  QBG_TRY(E.alloc(&Y, sizeof(cxd) * np));
+  QBG_TRY(E.alloc(&T, sizeof(cxd) * np));
+  QBG_TRY(E.alloc(&H, sizeof(cxd) * pp));
+  QBG_TRY(E.alloc(&Xs, sizeof(cxd) * (size_t)p * nev));
+  QBG_TRY(E.alloc(&P, sizeof(cxd) * std::max<size_t>(tall_scratch(n, p), 1)));
+  QBG_TRY(E.alloc(&o.G, sizeof(cxd) * pp));
+  QBG_TRY(E.alloc(&o.M, sizeof(cxd) * pp));
+  QBG_TRY(E.alloc(&o.Wt, sizeof(cxd) * np));
+  QBG_TRY(E.alloc(&o.tau, sizeof(cxd) * p));
+  int l1 = 0, l2 = 0;
+  if (cusolverDnZgeqrf_bufferSize(E.h, n, p, (cuDoubleComplex*)Q, n, &l1) != CUSOLVER_STATUS_SUCCESS ||
+      cusolverDnZungqr_bufferSize(E.h, n, p, p, (cuDoubleComplex*)Q, n, (cuDoubleComplex*)o.tau, &l2) !=
+          CUSOLVER_STATUS_SUCCESS)
+    return solver_fail("EBIM QR workspace query");
+  o.lwork = std::max(std::max(l1, l2), 1);
+  QBG_TRY(E.alloc(&o.work, sizeof(cxd) * (size_t)o.lwork));
+  // fixed starting block (reproducible): entries of a 64-bit LCG in [-1, 1)
+  std::vector<cxd> hq(np);
+  unsigned long long lcg = adjoint ? 0xD1B54A32D192ED03ull : 0x9E3779B97F4A7C15ull;
+  for (auto& v : hq) {
+    lcg = lcg * 6364136223846793005ull + 1442695040888963407ull;
+    v.re = (double)(lcg >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+    lcg = lcg * 6364136223846793005ull + 1442695040888963407ull;
+    v.im = (double)(lcg >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+  }
+  QBG_CUDA(cudaMemcpyAsync(Q, hq.data(), sizeof(cxd) * np, cudaMemcpyHostToDevice, E.st));
+  QBG_TRY(orthonormalize(E, Q, p, o));
+  std::vector<cxd> hh(pp), hx((size_t)p * nev);
+  std::vector<zc> Hz(pp), w, X;
+  std::vector<zc> prev(nev, zc(0.0, 0.0));
+  std::vector<int> order(p);
+  for (int it = 0; it < MAXIT; ++it) {
+    // Y = C Q = A^-1 (A' Q), or C^H Q = A'^H (A^-H Q)
+    if (!adjoint) {
+      QBG_TRY(gemm_nq(E.dA, Q, T, n, p, P, E.st));
+      QBG_TRY(gemm_nq(E.Ainv, T, Y, n, p, P, E.st));
+    } else {
+      QBG_TRY(gemm_nq(E.AinvH, Q, T, n, p, P, E.st));
+      QBG_TRY(gemm_nq(E.dAH, T, Y, n, p, P, E.st));
+    }
+    // Rayleigh-Ritz on the projection Q^H Y
+    k_inner<<<p * p, 256, 0, E.st>>>(Q, Y, n, p, H);
+    QBG_LAUNCH_CHECK("k_inner");
+    QBG_CUDA(cudaMemcpyAsync(hh.data(), H, sizeof(cxd) * pp, cudaMemcpyDeviceToHost, E.st));
+    QBG_TRY(E.wait());
+    for (size_t i = 0; i < pp; ++i) Hz[i] = zc(hh[i].re, hh[i].im);
+    QBG_TRY(small_eig(p, Hz, w, X));
+    for (int i = 0; i < p; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return std::abs(w[a]) > std::abs(w[b]); });
+    bool conv = it >= 2;
+    for (int j = 0; j < nev; ++j) {
+      const zc m = w[order[j]];
+      if (!(std::abs(m - prev[j]) <= TOL * std::abs(m))) conv = false;
+      prev[j] = m;
+    }
+    if (conv || it + 1 == MAXIT) {
+      // Ritz vectors of the nev largest: V = Q X(:, order[0..nev))
+      for (int j = 0; j < nev; ++j)
+        for (int i = 0; i < p; ++i) {
+          const zc x = X[(size_t)order[j] * p + i];
+          hx[(size_t)j * p + i] = cxd(x.real(), x.imag());
+        }
+      QBG_CUDA(cudaMemcpyAsync(Xs, hx.data(), sizeof(cxd) * hx.size(), cudaMemcpyHostToDevice, E.st));
+      QBG_TRY(gemm_batched<double>(n, nev, p, cxd(1, 0), Q, n, 0, Xs, p, 0, cxd(0, 0), V, n, 0, 1, E.st));
+      QBG_TRY(E.wait());
+      mu = prev;
+      *iters = it + 1;
+      return QBG_OK;
+    }
+    QBG_TRY(orthonormalize(E, Y, p, o));
+    std::swap(Q, Y);
+  }
+  return QBG_OK;  // not reached
+}
+
+// Everything after the three matrices are on the device (LU is overwritten).
+int ebim_run(Ebim& E, double k, double dk, int nev_req, int flags, int cap, double* out_k, double* out_tens,
+             int32_t* count, int32_t* iters_out) {
+  const int n = E.n;
+  const bool full = (flags & QBG_EBIM_FULL) != 0;
+  if (cusolverDnCreate(&E.h) != CUSOLVER_STATUS_SUCCESS) return solver_fail("cusolverDnCreate");
+  cusolverDnSetStream(E.h, E.st);
+  QBG_TRY(E.alloc(&E.ipiv, sizeof(int) * n));
+  QBG_TRY(E.alloc(&E.dinfo, sizeof(int)));
+  QBG_TRY(E.alloc(&E.dAH, sizeof(cxd) * (size_t)n * n));
+  k_conj_transpose<<<dim3((n + 31) / 32, (n + 31) / 32), dim3(32, 8), 0, E.st>>>(E.dA, E.dAH, n);
+  QBG_LAUNCH_CHECK("k_conj_transpose");
+  // LU of A (the reference's lu!(A))
+  int lw = 0;
+  if (cusolverDnZgetrf_bufferSize(E.h, n, n, (cuDoubleComplex*)E.LU, n, &lw) != CUSOLVER_STATUS_SUCCESS)
+    return solver_fail("getrf workspace query");
+  cxd* lwork = nullptr;
+  QBG_TRY(E.alloc(&lwork, sizeof(cxd) * (size_t)std::max(lw, 1)));
+  if (cusolverDnZgetrf(E.h, n, n, (cuDoubleComplex*)E.LU, n, (cuDoubleComplex*)lwork, E.ipiv, E.dinfo) !=
+      CUSOLVER_STATUS_SUCCESS)
+    return solver_fail("cusolverDnZgetrf");
+  int hinfo = 0;
+  QBG_CUDA(cudaMemcpyAsync(&hinfo, E.dinfo, sizeof(int), cudaMemcpyDeviceToHost, E.st));
+  QBG_TRY(E.wait());
+  if (hinfo > 0) {
+    set_error("EBIM: A(k) is exactly singular (U(%d, %d) = 0)", hinfo, hinfo);
+    return QBG_ESINGULAR;
+  }
+  // A^-1 and A^-H from the factors (one solve with n right-hand sides): every
+  // application of the shift-invert operator is then two skinny products
+  QBG_TRY(E.alloc(&E.Ainv, sizeof(cxd) * (size_t)n * n));
+  QBG_TRY(E.alloc(&E.AinvH, sizeof(cxd) * (size_t)n * n));
+  k_identity<<<2048, 256, 0, E.st>>>(E.Ainv, n);
+  QBG_LAUNCH_CHECK("k_identity");
+  if (cusolverDnZgetrs(E.h, CUBLAS_OP_N, n, n, (const cuDoubleComplex*)E.LU, n, E.ipiv, (cuDoubleComplex*)E.Ainv, n,
+                       E.dinfo) != CUSOLVER_STATUS_SUCCESS)
+    return solver_fail("cusolverDnZgetrs");
+  k_conj_transpose<<<dim3((n + 31) / 32, (n + 31) / 32), dim3(32, 8), 0, E.st>>>(E.Ainv, E.AinvH, n);
+  QBG_LAUNCH_CHECK("k_conj_transpose");
+  int nev = std::min(nev_req, n);
+  std::vector<zc> mur, mul;
+  cxd *V = nullptr, *U = nullptr, *W1 = nullptr, *W2 = nullptr;
+  int itr = 0, itl = 0;
+  for (;;) {
+    const int p = std::min(n, 2 * nev + 12);
+    QBG_TRY(E.alloc(&V, sizeof(cxd) * (size_t)n * nev));
+    QBG_TRY(block_eigs(E, false, p, nev, mur, V, &itr));
+    // full: the box |Re|, |Im| < dk lies inside |lambda| < sqrt(2) dk
+    const double lam_last = 1.0 / std::abs(mur[nev - 1]);
+    if (!full || nev >= n || lam_last >= std::sqrt(2.0) * dk) {
+      QBG_TRY(E.alloc(&U, sizeof(cxd) * (size_t)n * nev));
+      QBG_TRY(block_eigs(E, true, p, nev, mul, U, &itl));
+      break;
+    }
+    nev = std::min(n, 2 * nev);
+  }
+  // pair left with right: perm[j] = argmin_i |mu_l[i] - conj(mu_r[j])|
+  std::vector<int> perm(nev);
+  for (int j = 0; j < nev; ++j) {
+    int bi = 0;
+    double bd = INFINITY;
+    for (int i = 0; i < nev; ++i) {
+      const double d = std::abs(mul[i] - std::conj(mur[j]));
+      if (d < bd) {
+        bd = d;
+        bi = i;
+      }
+    }
+    perm[j] = bi;
+  }
+  cxd* P = nullptr;
+  QBG_TRY(E.alloc(&W1, sizeof(cxd) * (size_t)n * nev));
+  QBG_TRY(E.alloc(&W2, sizeof(cxd) * (size_t)n * nev));
+  QBG_TRY(E.alloc(&P, sizeof(cxd) * std::max<size_t>(tall_scratch(n, nev), 1)));
+  if (full) {  // left eigenvectors of the pencil: u~ = A^{-H} u
+    QBG_TRY(gemm_nq(E.AinvH, U, W1, n, nev, P, E.st));
+    QBG_CUDA(cudaMemcpyAsync(U, W1, sizeof(cxd) * (size_t)n * nev, cudaMemcpyDeviceToDevice, E.st));
+  }
+  QBG_TRY(gemm_nq(E.ddA, V, W1, n, nev, P, E.st));
+  QBG_TRY(gemm_nq(E.dA, V, W2, n, nev, P, E.st));
+  std::vector<cxd> hu((size_t)n * nev), h1((size_t)n * nev), h2((size_t)n * nev);
+  QBG_CUDA(cudaMemcpyAsync(hu.data(), U, sizeof(cxd) * hu.size(), cudaMemcpyDeviceToHost, E.st));
+  QBG_CUDA(cudaMemcpyAsync(h1.data(), W1, sizeof(cxd) * h1.size(), cudaMemcpyDeviceToHost, E.st));
+  QBG_CUDA(cudaMemcpyAsync(h2.data(), W2, sizeof(cxd) * h2.size(), cudaMemcpyDeviceToHost, E.st));
+  QBG_TRY(E.wait());
+  int m = 0;
+  for (int j = 0; j < nev; ++j) {
+    const zc lam = 1.0 / mur[j];
+    if (!(std::fabs(lam.real()) < dk && std::fabs(lam.imag()) < dk)) continue;
+    const cxd* u = hu.data() + (size_t)perm[j] * n;
+    const cxd* a1 = h1.data() + (size_t)j * n;
+    const cxd* a2 = h2.data() + (size_t)j * n;
+    zc num(0.0, 0.0), den(0.0, 0.0);
+    for (int r = 0; r < n; ++r) {
+      const zc ur(u[r].re, -u[r].im);
+      num += ur * zc(a1[r].re, a1[r].im);
+      den += ur * zc(a2[r].re, a2[r].im);
+    }
+    const zc c1 = -lam;
+    zc c2(0.0, 0.0);
+    if (std::abs(den) > 1e-15) c2 = -0.5 * c1 * c1 * (num / den);
+    const zc t = c1 + c2;
+    const zc kc = zc(k, 0.0) + t;
+    if (!full && !(std::fabs(kc.real() - k) < dk)) continue;
+    if (m < cap) {
+      out_k[2 * m] = kc.real();
+      out_k[2 * m + 1] = kc.imag();
+      out_tens[m] = std::abs(t);
+    }
+    ++m;
+  }
+  *count = m;
+  if (iters_out) {
+    iters_out[0] = itr;
+    iters_out[1] = itl;
+    iters_out[2] = nev;
+  }
+  return QBG_OK;
+}
+
+int ebim_setup(Ebim& E, int n) {
+  E.n = n;
+  cudaError_t e = stream_create(&E.st);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.ev, cudaEventBlockingSync | cudaEventDisableTiming);
+  return e == cudaSuccess ? QBG_OK : cuda_status(e, "EBIM stream");
+}
+
+bool ebim_args_ok(double k, double dk, int32_t nev, int32_t cap, const double* out_k, const double* out_tens,
+                  const int32_t* count) {
+  return std::isfinite(k) && dk > 0.0 && nev >= 1 && cap >= 0 && count && (cap == 0 || (out_k && out_tens));
+}
+
+}  // namespace
+
+extern "C" {
+
+qbg_status qbg_ebim_eig(int64_t n, const void* A, const void* dA, const void* ddA, double k, double dk, int32_t nev,
+                        int32_t flags, int32_t cap, double* out_k, double* out_tens, int32_t* count,
+                        int32_t* iters) {
+  if (n < 1 || n > (1 << 20) || !A || !dA || !ddA || !ebim_args_ok(k, dk, nev, cap, out_k, out_tens, count)) {
+    set_error("qbg_ebim_eig: invalid arguments");
+    return QBG_EINVAL;
+  }
+  Ebim E;
+  QBG_TRY(ebim_setup(E, (int)n));
+  const size_t bytes = sizeof(cxd) * (size_t)n * n;
+  QBG_TRY(E.alloc(&E.LU, bytes));
+  QBG_TRY(E.alloc(&E.dA, bytes));
+  QBG_TRY(E.alloc(&E.ddA, bytes));
+  const cudaMemcpyKind kind = (flags & QBG_PTR_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  QBG_CUDA(cudaMemcpyAsync(E.LU, A, bytes, kind, E.st));
+  QBG_CUDA(cudaMemcpyAsync(E.dA, dA, bytes, kind, E.st));
+  QBG_CUDA(cudaMemcpyAsync(E.ddA, ddA, bytes, kind, E.st));
+  return ebim_run(E, k, dk, nev, flags, cap, out_k, out_tens, count, iters);
+}
+
+qbg_status qbg_small_eig(int32_t p, const double* H, double* w, double* V) {
+  if (p < 1 || p > 4096 || !H || !w || !V) {
+    set_error("qbg_small_eig: invalid arguments");
+    return QBG_EINVAL;
+  }
+  std::vector<zc> Hz((size_t)p * p), wz, Vz;
+  for (size_t i = 0; i < Hz.size(); ++i) Hz[i] = zc(H[2 * i], H[2 * i + 1]);
+  QBG_TRY(small_eig(p, Hz, wz, Vz));
+  for (int i = 0; i < p; ++i) {
+    w[2 * i] = wz[i].real();
+    w[2 * i + 1] = wz[i].imag();
+  }
+  for (size_t i = 0; i < Vz.size(); ++i) {
+    V[2 * i] = Vz[i].real();
+    V[2 * i + 1] = Vz[i].imag();
+  }
+  return QBG_OK;
+}
+
+qbg_status qbg_ebim_solve(qbg_geom* g, double k, double dk, int32_t nev, int32_t flags, int32_t cap, double* out_k,
+                          double* out_tens, int32_t* count, int32_t* iters) {
+  if (!g || !ebim_args_ok(k, dk, nev, cap, out_k, out_tens, count) || !(k > 0.0)) {
+    set_error("qbg_ebim_solve: invalid arguments");
+    return QBG_EINVAL;
+  }
+  std::lock_guard<std::mutex> lk(g->mu);
+  Ebim E;
+  const int n = (int)g->dim;
+  QBG_TRY(ebim_setup(E, n));
+  // after the geometry stream's earlier work (its uploads)
+  cudaEvent_t ev_in = nullptr;
+  QBG_CUDA(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
+  cudaError_t e = cudaEventRecord(ev_in, g->stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(E.st, ev_in, 0);
+  cudaEventDestroy(ev_in);
+  if (e != cudaSuccess) return cuda_status(e, "EBIM stream order");
+  const size_t bytes = sizeof(cxd) * (size_t)n * n;
+  QBG_TRY(E.alloc(&E.LU, bytes));
+  QBG_TRY(E.alloc(&E.dA, bytes));
+  QBG_TRY(E.alloc(&E.ddA, bytes));
+  cxd* dks = nullptr;
+  void** dptrs = nullptr;
+  QBG_TRY(E.alloc(&dks, sizeof(cxd)));
+  QBG_TRY(E.alloc(&dptrs, sizeof(void*) * 3));
+  const cxd kk(k, 0.0);
+  void* hp[3] = {E.LU, E.dA, E.ddA};
+  QBG_CUDA(cudaMemcpyAsync(dks, &kk, sizeof(cxd), cudaMemcpyHostToDevice, E.st));
+  QBG_CUDA(cudaMemcpyAsync(dptrs, hp, sizeof(hp), cudaMemcpyHostToDevice, E.st));
+  QBG_TRY(launch_assemble(g->d, dks, 1, 1, QBG_PREC_FP64, dptrs, n, E.st));
+  QBG_TRY(E.wait());  // the host staging of k and the pointers is on this frame
+  return ebim_run(E, k, dk, nev, flags, cap, out_k, out_tens, count, iters);
+}
+
+}  // extern "C"

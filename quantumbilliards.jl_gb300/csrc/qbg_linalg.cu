@@ -204,14 +204,29 @@ __global__ void __launch_bounds__(512) k_getf2_panel(cx<T>* A, int n, long long 
 // ---------------------------------------------------------------------------
 // Panel factorisation with shared-memory sub-panels (one CTA per matrix).
 // The panel [j0, jend) is factored in sub-panels of `sub` columns. A
-// sub-panel (rows s0..n-1) is loaded into shared memory, factored column by
-// column there (pivot search, swap, scale, rank-1 update all in smem; the
-// swaps are mirrored in global memory on the other panel columns), written
-// back, and the rest of the panel is updated by one rank-`sub` step
-// (U12 = inv(L11) A12 by forward substitution, A22 -= L21 U12). The L2 traffic
-// of the panel drops from ~n nb^2/2 element updates to ~n nb^2/(2 sub).
+// sub-panel (rows s0..n-1) is loaded into shared memory and factored column
+// by column there: warp 0 finishes the block's pivot search, swaps the pivot
+// row into place and publishes it; every thread then scales its rows, applies
+// the rank-1 update and searches its rows of the next column (two block
+// barriers per column). The sub-panel's interchanges reach the other panel
+// columns afterwards as one composed permutation of at most 2 sub rows, and
+// the rest of the panel is updated by one rank-`sub` step
+// (U12 = inv(L11) A12 by forward substitution, A22 -= L21 U12). The factors
+// and pivots are those of column-by-column partial pivoting (largest
+// |re| + |im|, first index on ties; a zero pivot sets info and skips the
+// scaling, as LAPACK's getf2 does).
 // Dynamic smem: (n - j0) * sub * sizeof(cx<T>) (host picks sub so this fits).
 // ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ void warp_argmax(T& best, int& bi) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const T ov = __shfl_down_sync(0xffffffffu, best, o);
+    const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+    argmax_merge(best, bi, ov, oi);
+  }
+}
+
 template <class T>
 __global__ void __launch_bounds__(1024) k_getrf_panel_smem(cx<T>* A, int n, long long stride, int j0, int nb,
                                                           int sub, int* ipiv, int* info) {
@@ -219,11 +234,14 @@ __global__ void __launch_bounds__(1024) k_getrf_panel_smem(cx<T>* A, int n, long
   cx<T>* S = reinterpret_cast<cx<T>*>(smraw);
   __shared__ T wv[32];
   __shared__ int wi[32];
-  __shared__ int s_p;
-  __shared__ cx<T> Us[8 * 64];  // U rows of the current sub-panel on the remaining panel columns
+  __shared__ cx<T> urow[8];        // pivot row of the current column on the sub-panel's columns
+  __shared__ int spiv[8];          // the sub-panel's pivots (local rows)
+  __shared__ int tpos[16], tsrc[16];  // rows moved by the sub-panel's interchanges: tpos[t] <- row tsrc[t]
+  __shared__ int s_cnt;
+  __shared__ cx<T> Us[8 * 64];     // U rows of the sub-panel on the remaining panel columns
   cx<T>* a = A + (long long)blockIdx.x * stride;
   int* piv = ipiv + (long long)blockIdx.x * n;
-  const int tid = threadIdx.x, nt = blockDim.x;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
   const int jend = min(j0 + nb, n);
   for (int s0 = j0; s0 < jend; s0 += sub) {
     const int w = min(sub, jend - s0);
@@ -233,75 +251,98 @@ __global__ void __launch_bounds__(1024) k_getrf_panel_smem(cx<T>* A, int n, long
       S[c * m + r] = a[(s0 + r) + (long long)(s0 + c) * n];
     }
     __syncthreads();
+    T best = T(-1);
+    int bi = 0x7fffffff;
+    for (int r = tid; r < m; r += nt) {
+      const T v = cabs1(S[r]);
+      if (v > best) { best = v; bi = r; }
+    }
     for (int c = 0; c < w; ++c) {
-      const int cc = s0 + c;
-      T best = T(-1);
-      int bi = 0x7fffffff;
-      for (int r = c + tid; r < m; r += nt) {
-        const T v = cabs1(S[c * m + r]);
-        if (v > best) { best = v; bi = r; }
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        T ov = __shfl_down_sync(0xffffffffu, best, o);
-        int oi = __shfl_down_sync(0xffffffffu, bi, o);
-        argmax_merge(best, bi, ov, oi);
-      }
-      if ((tid & 31) == 0) { wv[tid >> 5] = best; wi[tid >> 5] = bi; }
-      __syncthreads();
-      if (tid < 32) {
-        const int nw = nt >> 5;
-        best = (tid < nw) ? wv[tid] : T(-1);
-        bi = (tid < nw) ? wi[tid] : 0x7fffffff;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          T ov = __shfl_down_sync(0xffffffffu, best, o);
-          int oi = __shfl_down_sync(0xffffffffu, bi, o);
-          argmax_merge(best, bi, ov, oi);
+      warp_argmax(best, bi);
+      if (lane == 0) { wv[wid] = best; wi[wid] = bi; }
+      __syncthreads();  // partial maxima of column c; the update of column c - 1 is complete
+      if (wid == 0) {
+        best = (lane < nw) ? wv[lane] : T(-1);
+        bi = (lane < nw) ? wi[lane] : 0x7fffffff;
+        warp_argmax(best, bi);
+        int p = __shfl_sync(0xffffffffu, bi, 0);
+        const T pb = __shfl_sync(0xffffffffu, best, 0);
+        if (p >= m) p = c;
+        if (lane < w) {
+          const cx<T> vp = S[lane * m + p];
+          S[lane * m + p] = S[lane * m + c];
+          S[lane * m + c] = vp;
+          urow[lane] = vp;
         }
-        if (tid == 0) {
-          if (bi >= m) bi = c;
-          s_p = bi;
-          piv[cc] = s0 + bi;
-          if (!(best > T(0)) && info[blockIdx.x] == 0) info[blockIdx.x] = cc + 1;
+        if (lane == 0) {
+          spiv[c] = p;
+          piv[s0 + c] = s0 + p;
+          if (!(pb > T(0)) && info[blockIdx.x] == 0) info[blockIdx.x] = s0 + c + 1;
         }
       }
-      __syncthreads();
-      const int p = s_p;  // local row
-      if (p != c) {
-        // smem sub-panel columns
-        for (int q = tid; q < w; q += nt) {
-          cx<T> t0 = S[q * m + c];
-          S[q * m + c] = S[q * m + p];
-          S[q * m + p] = t0;
-        }
-        // the other panel columns in global memory: [j0, s0) and [s0 + w, jend)
-        const int nother = (s0 - j0) + (jend - s0 - w);
-        for (int q = tid; q < nother; q += nt) {
-          const int col = (q < s0 - j0) ? (j0 + q) : (s0 + w + (q - (s0 - j0)));
-          cx<T>* pc = a + (long long)col * n;
-          cx<T> t0 = pc[cc];
-          pc[cc] = pc[s0 + p];
-          pc[s0 + p] = t0;
-        }
-      }
-      __syncthreads();
-      const cx<T> pv = S[c * m + c];
+      __syncthreads();  // pivot row in urow and in place
+      const cx<T> pv = urow[c];
       const bool nz = (pv.re != T(0) || pv.im != T(0));
       const cx<T> inv = nz ? cinv(pv) : cx<T>(0, 0);
+      const bool search = c + 1 < w;
+      best = T(-1);
+      bi = 0x7fffffff;
       for (int r = c + 1 + tid; r < m; r += nt) {
         cx<T> l = S[c * m + r];
         if (nz) {
           l = l * inv;
           S[c * m + r] = l;
         }
-        for (int q = c + 1; q < w; ++q) cfms(S[q * m + r], l, S[q * m + c]);
+        for (int q = c + 1; q < w; ++q) cfms(S[q * m + r], l, urow[q]);
+        if (search) {
+          const T v = cabs1(S[(c + 1) * m + r]);
+          if (v > best) { best = v; bi = r; }
+        }
       }
-      __syncthreads();
     }
+    if (tid == 0) {  // compose the sub-panel's interchanges
+      int cnt = 0;
+      for (int c = 0; c < w; ++c) {
+        const int r1 = s0 + c, r2 = s0 + spiv[c];
+        if (r1 == r2) continue;
+        int i1 = -1, i2 = -1;
+        for (int t = 0; t < cnt; ++t) {
+          if (tpos[t] == r1) i1 = t;
+          if (tpos[t] == r2) i2 = t;
+        }
+        if (i1 < 0) { tpos[cnt] = r1; tsrc[cnt] = r1; i1 = cnt++; }
+        if (i2 < 0) { tpos[cnt] = r2; tsrc[cnt] = r2; i2 = cnt++; }
+        const int t0 = tsrc[i1];
+        tsrc[i1] = tsrc[i2];
+        tsrc[i2] = t0;
+      }
+      s_cnt = cnt;
+    }
+    __syncthreads();  // sub-panel factored; permutation composed
     for (int e = tid; e < m * w; e += nt) {
       const int r = e % m, c = e / m;
       a[(s0 + r) + (long long)(s0 + c) * n] = S[c * m + r];
+    }
+    // the interchanges on the other panel columns [j0, s0) and [s0 + w, jend):
+    // whole columns per round, every read of a round before its writes
+    const int cnt = s_cnt;
+    const int nother = (s0 - j0) + (jend - s0 - w);
+    if (cnt > 0) {
+      const int per = nt / cnt;
+      for (int q0 = 0; q0 < nother; q0 += per) {
+        const int q = q0 + tid / cnt, t = tid % cnt;
+        const bool act = tid < per * cnt && q < nother;
+        cx<T> v(0, 0);
+        cx<T>* pc = nullptr;
+        if (act) {
+          const int col = (q < s0 - j0) ? (j0 + q) : (s0 + w + (q - (s0 - j0)));
+          pc = a + (long long)col * n;
+          v = pc[tsrc[t]];
+        }
+        __syncthreads();
+        if (act) pc[tpos[t]] = v;
+        __syncthreads();
+      }
     }
     // rank-w update of the rest of the panel: columns [s0 + w, jend)
     const int nr = jend - s0 - w;
@@ -1055,7 +1096,7 @@ template <class T>
 static LUBatch<T> lu_view(const LUBatch<T>& f, int b0, int cnt) {
   LUBatch<T> v = f;
   v.batch = cnt;
-  v.st2 = nullptr;
+  v.nsplit = 1;
   const long long b = b0;
   v.A = f.A + b * f.stride;
   v.ipiv = f.ipiv + b * f.n;
@@ -1078,36 +1119,53 @@ static LUBatch<T> lu_view(const LUBatch<T>& f, int b0, int cnt) {
   return v;
 }
 
-// With a second stream the two halves of the batch are factored (solved)
-// concurrently: the panel factorisations and the short GEMM chains of one half
-// leave most SMs idle, which the other half's kernels fill. The matrices are
+// With extra streams the parts of the batch are factored (solved)
+// concurrently: the panel factorisations and the short GEMM chains of one part
+// leave most SMs idle, which the other parts' kernels fill. The matrices are
 // independent, so the results are those of one stream.
 template <class T>
+static int split_parts(const LUBatch<T>& f) {
+  return std::max(1, std::min(std::min(f.nsplit, LUBatch<T>::MAX_SPLIT), f.batch));
+}
+
+template <class T>
 int lu_factor(LUBatch<T>& f, cudaStream_t st) {
-  if (!f.st2 || f.batch < 2) return lu_factor_one<T>(f, st);
-  const int h = f.batch / 2;
-  LUBatch<T> a = lu_view<T>(f, 0, h), b = lu_view<T>(f, h, f.batch - h);
-  // the second half starts one panel behind the first, so that the panels of
-  // one half run under the updates of the other
-  int s = lu_factor_one<T>(a, st, f.ev_fork);
-  QBG_CUDA(cudaStreamWaitEvent(f.st2, f.ev_fork, 0));
-  if (!s) s = lu_factor_one<T>(b, f.st2);
-  QBG_CUDA(cudaEventRecord(f.ev_join, f.st2));
-  QBG_CUDA(cudaStreamWaitEvent(st, f.ev_join, 0));
+  const int P = split_parts(f);
+  if (P < 2) return lu_factor_one<T>(f, st);
+  // part i + 1 starts one panel behind part i, so that the panels of one part
+  // run under the updates of the others
+  int s = QBG_OK;
+  for (int i = 0; i < P && !s; ++i) {
+    const int b0 = (int)((long long)i * f.batch / P), b1 = (int)((long long)(i + 1) * f.batch / P);
+    LUBatch<T> v = lu_view<T>(f, b0, b1 - b0);
+    cudaStream_t si = i == 0 ? st : f.stx[i - 1];
+    if (i > 0) QBG_CUDA(cudaStreamWaitEvent(si, f.ev_fork, 0));
+    s = lu_factor_one<T>(v, si, i + 1 < P ? f.ev_fork : nullptr);
+  }
+  for (int i = 1; i < P; ++i) {
+    QBG_CUDA(cudaEventRecord(f.ev_join, f.stx[i - 1]));
+    QBG_CUDA(cudaStreamWaitEvent(st, f.ev_join, 0));
+  }
   return s;
 }
 
 template <class T>
 int lu_solve_shared(const LUBatch<T>& f, const cx<T>* V, int L, cx<T>* X, long long strideV, cudaStream_t st) {
-  if (!f.st2 || f.batch < 2) return lu_solve_one<T>(f, V, L, X, strideV, st);
-  const int h = f.batch / 2;
-  const LUBatch<T> a = lu_view<T>(f, 0, h), b = lu_view<T>(f, h, f.batch - h);
+  const int P = split_parts(f);
+  if (P < 2) return lu_solve_one<T>(f, V, L, X, strideV, st);
   QBG_CUDA(cudaEventRecord(f.ev_fork, st));
-  QBG_CUDA(cudaStreamWaitEvent(f.st2, f.ev_fork, 0));
-  int s = lu_solve_one<T>(a, V, L, X, strideV, st);
-  if (!s) s = lu_solve_one<T>(b, V + (long long)h * strideV, L, X + (long long)h * f.n * L, strideV, f.st2);
-  QBG_CUDA(cudaEventRecord(f.ev_join, f.st2));
-  QBG_CUDA(cudaStreamWaitEvent(st, f.ev_join, 0));
+  int s = QBG_OK;
+  for (int i = 0; i < P && !s; ++i) {
+    const int b0 = (int)((long long)i * f.batch / P), b1 = (int)((long long)(i + 1) * f.batch / P);
+    const LUBatch<T> v = lu_view<T>(f, b0, b1 - b0);
+    cudaStream_t si = i == 0 ? st : f.stx[i - 1];
+    if (i > 0) QBG_CUDA(cudaStreamWaitEvent(si, f.ev_fork, 0));
+    s = lu_solve_one<T>(v, V + (long long)b0 * strideV, L, X + (long long)b0 * f.n * L, strideV, si);
+  }
+  for (int i = 1; i < P; ++i) {
+    QBG_CUDA(cudaEventRecord(f.ev_join, f.stx[i - 1]));
+    QBG_CUDA(cudaStreamWaitEvent(st, f.ev_join, 0));
+  }
   return s;
 }
 

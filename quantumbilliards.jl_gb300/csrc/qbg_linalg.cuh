@@ -28,10 +28,13 @@ struct LUBatch {
   cx<T>* W = nullptr;         // doubling scratch: batch * ceil(nblk / 2) * (nbs / 2)^2
   cx<T>* Y = nullptr;         // solve scratch: batch * n * ymax_L
   int ymax_L = 0;
-  // optional second stream (owned by the caller): lu_factor and lu_solve_shared
-  // then run the two halves of the batch concurrently, forked from and joined
-  // back into the calling stream with these two events
-  cudaStream_t st2 = nullptr;
+  // optional extra streams (owned by the caller): with nsplit > 1, lu_factor
+  // and lu_solve_shared run nsplit contiguous parts of the batch concurrently,
+  // the first on the calling stream and part i on stx[i - 1], forked from and
+  // joined back into the calling stream with these two events
+  static constexpr int MAX_SPLIT = 4;
+  int nsplit = 1;
+  cudaStream_t stx[MAX_SPLIT - 1] = {};
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 

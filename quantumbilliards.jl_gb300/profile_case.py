@@ -97,7 +97,7 @@ def large_case(qb, a):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["beyn", "assemble", "disks", "large"])
+    ap.add_argument("case", choices=["beyn", "assemble", "disks", "large", "ebim"])
     ap.add_argument("--ndisk", type=int, default=32)
     ap.add_argument("--repeat", type=int, default=1, help="disks: batches run back to back (first cold, rest warm)")
     ap.add_argument("--chunk", type=int, default=8)
@@ -107,6 +107,9 @@ def main(argv=None):
     ap.add_argument("--L", type=int, default=64)
     ap.add_argument("--form", default="mixed", choices=["fp64", "mixed", "fp32"])
     ap.add_argument("--direct", action="store_true", help="direct Hankel evaluation instead of Chebyshev panels")
+    ap.add_argument("--dk", type=float, default=0.05, help="ebim: window half-width")
+    ap.add_argument("--nev", type=int, default=5, help="ebim: eigenvalues of the block iteration")
+    ap.add_argument("--full", action="store_true", help="ebim: solve_full! convention (every root in the box)")
     ap.add_argument("--gemm-engine", type=int, default=1, choices=[0, 1, 2],
                     help="complex64 GEMM engine of the FP32 LU and solves (qbg_set_gemm_engine)")
     a = ap.parse_args(argv)
@@ -121,7 +124,13 @@ def main(argv=None):
     b, sol, pts = star_case(qb, a.n)
     ws = qb.Workspace(sol, pts)
     t0 = time.perf_counter()
-    if a.case == "beyn":
+    if a.case == "ebim":
+        for rep in range(3):
+            t1 = time.perf_counter()
+            kc, tens, info = qb.ebim.solve(ws, 200.0, a.dk, nev=a.nev, full=a.full, return_info=True)
+            print("ebim", "full" if a.full else "krylov", "N", ws.dim, "roots", np.round(kc, 6).tolist(),
+                  "tens", np.round(tens, 6).tolist(), info, "ms %.1f" % ((time.perf_counter() - t1) * 1e3), flush=True)
+    elif a.case == "beyn":
         lam, info = qb.solve(sol, pts, 200.0 + 0j, 0.5, nq=a.nq, r=a.L, svd_tol=1e-12, rng=np.random.default_rng(1),
                              mixed=a.form, ws=ws, return_info=True, use_chebyshev=not a.direct)
         print("beyn", a.form, "eigenvalues", len(lam), "stats", info["stats"][0])

@@ -19,6 +19,7 @@ from .operators import (Workspace, build_workspace, assemble, assemble_noalloc, 
                         chebyshev_params_min_cost)
 from .beyn import BeynHandle, construct_B_matrix, solve_vect, solve, solve_disks, probe_matrix, contour
 from .sweep import k_sweep, get_eigenvalues
+from . import ebim
 from .serve import Server
 from .spectrum import (plan_weyl_windows, beyn_disks_from_windows, candidate_residuals,
                        residual_and_norm_select, imag_k_check, compute_spectrum_beyn)

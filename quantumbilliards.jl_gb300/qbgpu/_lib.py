@@ -21,6 +21,7 @@ QBG_PREC_FP64, QBG_PREC_MIXED, QBG_PREC_FP32 = 0, 1, 2
 QBG_PTR_DEVICE = 1
 QBG_V_PER_DISK = 2
 QBG_SPLIT_LO = 4
+QBG_EBIM_FULL = 8
 
 
 def prec_code(p) -> int:
@@ -116,6 +117,13 @@ _SIGS = {
                                         C.c_void_p, C.POINTER(BeynStats)]),
     "qbg_beyn_destroy": (C.c_int32, [C.c_void_p]),
     "qbg_sigma_min": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]),
+    "qbg_ebim_eig": (C.c_int32, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int32,
+                                 C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                 C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "qbg_small_eig": (C.c_int32, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "qbg_ebim_solve": (C.c_int32, [C.c_void_p, C.c_double, C.c_double, C.c_int32, C.c_int32, C.c_int32,
+                                   C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int32),
+                                   C.POINTER(C.c_int32)]),
     "qbg_bessel01": (C.c_int32, [C.POINTER(C.c_double), C.c_int64, C.c_int32, C.POINTER(C.c_double)]),
     "qbg_cgemm_c64": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_float), C.c_void_p,
                                   C.c_int64, C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.c_void_p, C.c_int64,

@@ -213,7 +213,7 @@ def solve_disks(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed
 
 def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=None, mixed=False, ws=None,
                        max_refine=10, refine_tol=1e-6, return_info=False, regrow="extend", use_chebyshev=True,
-                       cheb=None, fp32_sweeps=0, solve_block=0, node_chunk=0, resid_engine=0, basis=True):
+                       cheb=None, fp32_sweeps=0, solve_block=0, node_chunk=0, resid_engine=0, basis=True, nb=0):
     """construct_B_matrix (beyn.jl:257-322). Returns (B, Uk) [, info].
 
     regrow: when the rank saturates (rk == r) the reference draws a fresh
@@ -234,7 +234,7 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
     clk = time.perf_counter
     host = dict(create=0.0, moments=0.0, svd=0.0, B=0.0)  # wall-clock ms of the host-visible phases
     t = clk()
-    bh = BeynHandle(ws, k0, R, nq, mixed, max_refine, refine_tol, use_chebyshev=use_chebyshev, cheb=cheb,
+    bh = BeynHandle(ws, k0, R, nq, mixed, max_refine, refine_tol, nb=nb, use_chebyshev=use_chebyshev, cheb=cheb,
                     fp32_sweeps=fp32_sweeps, solve_block=solve_block, node_chunk=node_chunk,
                     resid_engine=resid_engine)
     host["create"] += (clk() - t) * 1e3

@@ -37,3 +37,24 @@ def test_error_path_without_gpu_work(qb):
     assert "null" in _lib.last_error()
     st = lib.qbg_beyn_moments(None, None, 0, None, None, None)
     assert st == _lib.QBG_EINVAL
+
+
+def test_ebim_argument_checks_without_gpu_work(qb):
+    """qbg_ebim_eig / qbg_ebim_solve reject bad sizes, windows and outputs
+    before any device call."""
+    from qbgpu import _lib
+    lib = _lib.load()
+    cnt = ctypes.c_int32()
+    out = (ctypes.c_double * 16)()
+    tens = (ctypes.c_double * 8)()
+    buf = (ctypes.c_double * 8)()
+    args = (12.0, 0.1, 4, 0, 8, out, tens, ctypes.byref(cnt), None)
+    assert lib.qbg_ebim_eig(0, buf, buf, buf, *args) == _lib.QBG_EINVAL            # n < 1
+    assert lib.qbg_ebim_eig(2, None, buf, buf, *args) == _lib.QBG_EINVAL           # missing A
+    assert lib.qbg_ebim_eig(2, buf, buf, buf, 12.0, 0.0, 4, 0, 8, out, tens, ctypes.byref(cnt), None) \
+        == _lib.QBG_EINVAL                                                          # dk <= 0
+    assert lib.qbg_ebim_eig(2, buf, buf, buf, 12.0, 0.1, 0, 0, 8, out, tens, ctypes.byref(cnt), None) \
+        == _lib.QBG_EINVAL                                                          # nev < 1
+    assert lib.qbg_ebim_eig(2, buf, buf, buf, 12.0, 0.1, 4, 0, 8, None, tens, ctypes.byref(cnt), None) \
+        == _lib.QBG_EINVAL                                                          # cap > 0 without outputs
+    assert lib.qbg_ebim_solve(None, *args) == _lib.QBG_EINVAL                      # no geometry

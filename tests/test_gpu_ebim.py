@@ -1,0 +1,96 @@
+"""GPU: the EBIM eigen step (qbg_ebim_eig, qbg_ebim_solve) against the oracle
+(oracle/ebim.py: ebim.jl solve_full! :336-375, solve_krylov! :464-537).
+
+* same matrices on both sides (the oracle's FP64 assembly of the circle with
+  a hole, CFIE, k = 12.3, dk = 0.15, where the two conventions differ): the
+  corrected k (complex) and tensions agree to 1e-10 absolute, the counts
+  exactly, for solve_krylov (nev = 6) and solve_full;
+* solve_full starting from a block of 2 grows it until the box is covered;
+* qbg_ebim_solve (A, A', A'' assembled on the device) against the oracle run
+  on the device-assembled matrices copied back: 1e-10;
+* the circle (DLP): the corrected k is within 3 d^3 of the J_0 zero for a trial
+  k at distance d;
+* an empty window and cap = 0 (count only).
+"""
+import numpy as np
+import pytest
+from scipy import special as sp
+
+from oracle import assembly as OA, ebim as OE
+
+pytestmark = pytest.mark.gpu
+
+
+def _hole(qb):
+    hb = qb.make_circle_with_hole(1.0, (0.3, 0.1, 0.2))
+    pts = qb.solvers.evaluate_points(qb.CFIE_kress(10.0, hb), hb, 12.0)
+    return hb, pts
+
+
+def _close(a, b, tol):
+    a, b = np.sort_complex(np.asarray(a)), np.sort_complex(np.asarray(b))
+    assert len(a) == len(b), (a, b)
+    assert np.max(np.abs(a - b), initial=0.0) < tol, (a, b)
+
+
+def test_ebim_eig_matches_oracle(qb):
+    _, pts = _hole(qb)
+    k, dk = 12.3, 0.15
+    A, dA, ddA = OA.cfie_matrix_derivs(pts, k)
+    kk, tk = qb.ebim.solve_krylov(None, A, dA, ddA, pts, k, dk, nev=6, return_imag_part=True)
+    ok, otk = OE.solve_krylov(A, dA, ddA, k, dk, nev=6, return_imag_part=True)
+    _close(kk, ok, 1e-10)
+    _close(tk, otk, 1e-10)
+    kf, tf, info = qb.ebim.solve_full(None, A, dA, ddA, pts, k, dk, return_imag_part=True, return_info=True, nev=2)
+    of, otf = OE.solve_full(A, dA, ddA, k, dk, return_imag_part=True)
+    _close(kf, of, 1e-10)
+    _close(tf, otf, 1e-10)
+    assert info["nev"] > 2  # the box holds more eigenvalues than the starting block
+    # the inputs are left unchanged
+    A2, _, _ = OA.cfie_matrix_derivs(pts, k)
+    assert np.array_equal(A, A2)
+
+
+def test_ebim_solve_device_assembly(qb):
+    hb, pts = _hole(qb)
+    sol = qb.CFIE_kress(10.0, hb)
+    ws = qb.Workspace(sol, pts)
+    k, dk = 12.3, 0.15
+    A, dA, ddA = qb.assemble(ws, [k], deriv=True)
+    for full in (False, True):
+        kc, tens = qb.ebim.solve(ws, k, dk, nev=6, full=full, return_imag_part=True)
+        if full:
+            ok, ot = OE.solve_full(A, dA, ddA, k, dk, return_imag_part=True)
+        else:
+            ok, ot = OE.solve_krylov(A, dA, ddA, k, dk, nev=6, return_imag_part=True)
+        _close(kc, ok, 1e-10)
+        _close(tens, ot, 1e-10)
+
+
+def test_ebim_circle_third_order(qb):
+    b = qb.make_circle(1.0)
+    sol = qb.DLP_kress(10.0, b)
+    pts = qb.solvers.evaluate_points(sol, b, 16.0)
+    ws = qb.Workspace(sol, pts)
+    z0 = float(sp.jn_zeros(0, 5)[4])
+    for d in (0.002, 0.01):
+        for full in (False, True):
+            kc, tens = qb.ebim.solve(ws, z0 + d, 0.05, nev=5, full=full)
+            assert len(kc) == 1
+            assert abs(kc[0] - z0) < 3.0 * d ** 3
+            assert abs(tens[0] - d) < 3.0 * d ** 3
+
+
+def test_ebim_empty_window_and_count_only(qb):
+    from qbgpu import _lib
+    import ctypes as C
+    _, pts = _hole(qb)
+    A, dA, ddA = OA.cfie_matrix_derivs(pts, 12.6)
+    kc, tens = qb.ebim.solve_krylov(None, A, dA, ddA, pts, 12.6, 0.02, nev=4)
+    assert len(kc) == 0 and len(tens) == 0
+    A, dA, ddA = [np.asfortranarray(m) for m in OA.cfie_matrix_derivs(pts, 12.3)]
+    cnt = C.c_int32()
+    lib = _lib.load()
+    st = lib.qbg_ebim_eig(A.shape[0], A.ctypes.data, dA.ctypes.data, ddA.ctypes.data, 12.3, 0.15, 6,
+                          _lib.QBG_EBIM_FULL, 0, None, None, C.byref(cnt), None)
+    assert st == _lib.QBG_OK and cnt.value == 4

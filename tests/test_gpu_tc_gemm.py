@@ -99,11 +99,12 @@ def test_mixed_moments_ragged_solve_blocks(qb, n_nodes, L):
         assert np.max(np.abs(a - r)) / np.max(np.abs(r)) < 1e-10
 
 
-def test_lu_two_streams_bitwise_equal(qb):
-    """The LU and the triangular solves of the mixed form run the two halves of
-    the operator batch on two streams; that changes nothing in the results:
-    moments bit-identical to the one-stream run (QBG_LU_SPLIT=0), also for an
-    odd batch (the halves differ in size)."""
+def test_lu_split_streams_bitwise_equal(qb):
+    """The LU and the triangular solves of the mixed form run parts of the
+    operator batch on several streams (QBG_LU_SPLIT parts); that changes
+    nothing in the results: moments bit-identical to the one-stream run
+    (QBG_LU_SPLIT=0) for 2, 3 and 4 parts, also for an odd batch (parts of
+    different sizes)."""
     import os
     b = qb.make_star(0.2, 5)
     sol = qb.CFIE_kress(1.0, b)
@@ -112,7 +113,7 @@ def test_lu_two_streams_bitwise_equal(qb):
     V = qb.probe_matrix(ws.dim, 24, np.random.default_rng(5))
     for nq in (16, 15):
         out = {}
-        for split in ("1", "0"):
+        for split in ("0", "2", "3", "4"):
             os.environ["QBG_LU_SPLIT"] = split
             try:
                 bh = qb.BeynHandle(ws, 30.0 + 0.05j, 0.4, nq, mixed=True)
@@ -120,5 +121,6 @@ def test_lu_two_streams_bitwise_equal(qb):
                 bh.close()
             finally:
                 os.environ.pop("QBG_LU_SPLIT", None)
-        for a, r in zip(out["1"], out["0"]):
-            assert np.array_equal(a, r), nq
+        for split in ("2", "3", "4"):
+            for a, r in zip(out[split], out["0"]):
+                assert np.array_equal(a, r), (nq, split)
