@@ -267,6 +267,17 @@ qbg_status qbg_ebim_eig(int64_t n, const void* A, const void* dA, const void* dd
                         int32_t* iters);
 qbg_status qbg_ebim_solve(qbg_geom* g, double k, double dk, int32_t nev, int32_t flags, int32_t cap, double* out_k,
                           double* out_tens, int32_t* count, int32_t* iters);
+/* Newton refinement of a sweep minimum (newton_refine_svd!,
+ * sweepmethods.jl:307-368) on the geometry's discretisation: Newton steps on
+ * lambda_min(A(k)^H A(k)) with its first and second k-derivatives (second-order
+ * perturbation sum over all eigenpairs of A^H A), k clamped to [a, b], at most
+ * maxiter steps, stop when a step is below tol. Writes the refined k and the
+ * tension sqrt(lambda_min) there (or at the best k met, when smaller); iters
+ * (optional): steps taken. FP64 throughout; A, A', A'' assembled on the device
+ * (direct Hankel evaluation). */
+qbg_status qbg_newton_refine(qbg_geom* g, double k0, double a, double b, int32_t maxiter, double tol,
+                             double* k_out, double* t_out, int32_t* iters);
+
 /* The host eigen-decomposition behind the EBIM Rayleigh-Ritz step, for
  * validation: eigenvalues w (p complex) and unit eigenvectors V (p x p
  * column-major, complex interleaved) of the p x p complex matrix H (Hessenberg

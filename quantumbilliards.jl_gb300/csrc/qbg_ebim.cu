@@ -706,6 +706,165 @@ qbg_status qbg_ebim_eig(int64_t n, const void* A, const void* dA, const void* dd
   return ebim_run(E, k, dk, nev, flags, cap, out_k, out_tens, count, iters);
 }
 
+// ---------------------------------------------------------------------------
+// Newton refinement of a sweep minimum (newton_refine_svd!,
+// sweepmethods.jl:307-368): f(k) = lambda_min(G(k)), G = A^H A, with
+// G' = A'^H A + A^H A' and G'' = A''^H A + 2 A'^H A' + A^H A''. Per step: the
+// three matrices assembled at k on the device, the four products A^H A,
+// A'^H A, A''^H A, A'^H A' (FP64), the full Hermitian eigen-decomposition of G
+// (cuSOLVER heevd); lambda1 = x^H G' x, lambda2 = x^H G'' x + 2 sum_{j != min}
+// |v_j^H G' x|^2 / (lambda - lambda_j) (terms with |lambda - lambda_j| < eps
+// skipped), k <- clamp(k - lambda1 / lambda2, a, b); stops when the step is
+// below tol, lambda1 or lambda2 is not finite, or |lambda2| < sqrt(eps). The
+// best k seen (smallest lambda) is kept; the result is (k, sqrt(lambda_min))
+// at the final k, or at the best k when that is smaller.
+// ---------------------------------------------------------------------------
+__global__ void k_hsum(const cxd* __restrict__ M, const cxd* __restrict__ N2, double c, int n, cxd* __restrict__ out) {
+  // out = M + M^H + c N2 (N2 may be null)
+  const size_t count = (size_t)n * n;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i % n), col = (int)(i / n);
+    const cxd a = M[i], b = M[col + (size_t)r * n];
+    cxd v(a.re + b.re, a.im - b.im);
+    if (N2) {
+      v.re += c * N2[i].re;
+      v.im += c * N2[i].im;
+    }
+    out[i] = v;
+  }
+}
+
+struct Newton {
+  Ebim E;
+  cxd *AH = nullptr, *G = nullptr, *M = nullptr, *Nn = nullptr, *Pp = nullptr, *H = nullptr, *H2 = nullptr,
+      *cwork = nullptr, *xv = nullptr, *gx = nullptr, *hx = nullptr, *cv = nullptr;
+  double* w = nullptr;
+  cxd* dks = nullptr;
+  void** dptrs = nullptr;
+  int lwork = 0;
+};
+
+// G = A^H A at k (and with derivs the pieces of G' and G''); lam: ascending
+// eigenvalues; with vectors G holds the eigenvectors afterwards
+int newton_eval(qbg_geom* g, Newton& W, double k, bool derivs, std::vector<double>& lam) {
+  Ebim& E = W.E;
+  const int n = E.n;
+  const cxd kk(k, 0.0);
+  void* hp[3] = {E.LU, E.dA, E.ddA};
+  QBG_CUDA(cudaMemcpyAsync(W.dks, &kk, sizeof(cxd), cudaMemcpyHostToDevice, E.st));
+  QBG_CUDA(cudaMemcpyAsync(W.dptrs, hp, sizeof(hp), cudaMemcpyHostToDevice, E.st));
+  QBG_TRY(launch_assemble(g->d, W.dks, 1, derivs ? 1 : 0, QBG_PREC_FP64, W.dptrs, n, E.st));
+  QBG_TRY(E.wait());  // k and the pointer table are staged from this frame
+  const dim3 tg((n + 31) / 32, (n + 31) / 32), tb(32, 8);
+  k_conj_transpose<<<tg, tb, 0, E.st>>>(E.LU, W.AH, n);
+  QBG_LAUNCH_CHECK("k_conj_transpose");
+  const cxd one(1, 0), zero(0, 0);
+  QBG_TRY(gemm_batched<double>(n, n, n, one, W.AH, n, 0, E.LU, n, 0, zero, W.G, n, 0, 1, E.st));  // A^H A
+  if (derivs) {
+    k_conj_transpose<<<tg, tb, 0, E.st>>>(E.dA, W.AH, n);
+    QBG_LAUNCH_CHECK("k_conj_transpose");
+    QBG_TRY(gemm_batched<double>(n, n, n, one, W.AH, n, 0, E.LU, n, 0, zero, W.M, n, 0, 1, E.st));   // A'^H A
+    QBG_TRY(gemm_batched<double>(n, n, n, one, W.AH, n, 0, E.dA, n, 0, zero, W.Pp, n, 0, 1, E.st));  // A'^H A'
+    k_conj_transpose<<<tg, tb, 0, E.st>>>(E.ddA, W.AH, n);
+    QBG_LAUNCH_CHECK("k_conj_transpose");
+    QBG_TRY(gemm_batched<double>(n, n, n, one, W.AH, n, 0, E.LU, n, 0, zero, W.Nn, n, 0, 1, E.st));  // A''^H A
+    k_hsum<<<2048, 256, 0, E.st>>>(W.M, nullptr, 0.0, n, W.H);
+    QBG_LAUNCH_CHECK("k_hsum");
+    k_hsum<<<2048, 256, 0, E.st>>>(W.Nn, W.Pp, 2.0, n, W.H2);
+    QBG_LAUNCH_CHECK("k_hsum");
+  }
+  if (cusolverDnZheevd(E.h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, (cuDoubleComplex*)W.G, n, W.w,
+                       (cuDoubleComplex*)W.cwork, W.lwork, E.dinfo) != CUSOLVER_STATUS_SUCCESS)
+    return solver_fail("cusolverDnZheevd");
+  lam.resize(n);
+  QBG_CUDA(cudaMemcpyAsync(lam.data(), W.w, sizeof(double) * n, cudaMemcpyDeviceToHost, E.st));
+  return E.wait();
+}
+
+qbg_status newton_impl(qbg_geom* g, double k0, double a, double b, int maxiter, double tol, double* k_out,
+                       double* t_out, int32_t* iters) {
+  Newton W;
+  Ebim& E = W.E;
+  const int n = (int)g->dim;
+  QBG_TRY(ebim_setup(E, n));
+  cudaEvent_t ev_in = nullptr;
+  QBG_CUDA(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
+  cudaError_t e = cudaEventRecord(ev_in, g->stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(E.st, ev_in, 0);
+  cudaEventDestroy(ev_in);
+  if (e != cudaSuccess) return cuda_status(e, "Newton stream order");
+  if (cusolverDnCreate(&E.h) != CUSOLVER_STATUS_SUCCESS) return solver_fail("cusolverDnCreate");
+  cusolverDnSetStream(E.h, E.st);
+  const size_t bytes = sizeof(cxd) * (size_t)n * n;
+  for (cxd** q : {&E.LU, &E.dA, &E.ddA, &W.AH, &W.G, &W.M, &W.Nn, &W.Pp, &W.H, &W.H2}) QBG_TRY(E.alloc(q, bytes));
+  QBG_TRY(E.alloc(&E.dinfo, sizeof(int)));
+  QBG_TRY(E.alloc(&W.w, sizeof(double) * n));
+  QBG_TRY(E.alloc(&W.dks, sizeof(cxd)));
+  QBG_TRY(E.alloc(&W.dptrs, sizeof(void*) * 3));
+  QBG_TRY(E.alloc(&W.gx, sizeof(cxd) * n));
+  QBG_TRY(E.alloc(&W.hx, sizeof(cxd) * n));
+  QBG_TRY(E.alloc(&W.cv, sizeof(cxd) * n));
+  if (cusolverDnZheevd_bufferSize(E.h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, (cuDoubleComplex*)W.G, n,
+                                  W.w, &W.lwork) != CUSOLVER_STATUS_SUCCESS)
+    return solver_fail("heevd workspace query");
+  QBG_TRY(E.alloc(&W.cwork, sizeof(cxd) * (size_t)std::max(W.lwork, 1)));
+  const double eps = 2.220446049250313e-16;
+  double k = std::min(std::max(k0, a), b), kbest = k, lbest = INFINITY;
+  std::vector<double> lam;
+  std::vector<cxd> hx(n), hg(n), hh(n), hc(n);
+  int it = 0;
+  const cxd one(1, 0), zero(0, 0);
+  for (; it < maxiter; ++it) {
+    QBG_TRY(newton_eval(g, W, k, true, lam));
+    const double l0 = lam[0];  // ascending: the minimum is first
+    if (std::isfinite(l0) && l0 < lbest) {
+      lbest = l0;
+      kbest = k;
+    }
+    const cxd* x = W.G;  // eigenvector of the smallest eigenvalue (column 0)
+    QBG_TRY(gemm_batched<double>(n, 1, n, one, W.H, n, 0, x, n, 0, zero, W.gx, n, 0, 1, E.st));
+    QBG_TRY(gemm_batched<double>(n, 1, n, one, W.H2, n, 0, x, n, 0, zero, W.hx, n, 0, 1, E.st));
+    // c_j = v_j^H (G' x), j = 0..n-1
+    k_inner<<<n, 256, 0, E.st>>>(W.G, W.gx, n, n, W.cv);  // p = n rows of the (n x 1) result: G[a] = v_a^H gx
+    QBG_LAUNCH_CHECK("k_inner");
+    QBG_CUDA(cudaMemcpyAsync(hx.data(), x, sizeof(cxd) * n, cudaMemcpyDeviceToHost, E.st));
+    QBG_CUDA(cudaMemcpyAsync(hg.data(), W.gx, sizeof(cxd) * n, cudaMemcpyDeviceToHost, E.st));
+    QBG_CUDA(cudaMemcpyAsync(hh.data(), W.hx, sizeof(cxd) * n, cudaMemcpyDeviceToHost, E.st));
+    QBG_CUDA(cudaMemcpyAsync(hc.data(), W.cv, sizeof(cxd) * n, cudaMemcpyDeviceToHost, E.st));
+    QBG_TRY(E.wait());
+    double l1 = 0.0, l2 = 0.0;
+    for (int r = 0; r < n; ++r) {
+      l1 += hx[r].re * hg[r].re + hx[r].im * hg[r].im;  // Re(conj(x) gx)
+      l2 += hx[r].re * hh[r].re + hx[r].im * hh[r].im;
+    }
+    for (int j = 1; j < n; ++j) {
+      const double den = l0 - lam[j];
+      if (std::fabs(den) < eps) continue;
+      l2 += 2.0 * (hc[j].re * hc[j].re + hc[j].im * hc[j].im) / den;
+    }
+    if (!std::isfinite(l1) || !std::isfinite(l2) || std::fabs(l2) < std::sqrt(eps)) break;
+    const double knew = std::min(std::max(k - l1 / l2, a), b);
+    if (!std::isfinite(knew)) break;
+    if (std::fabs(knew - k) < tol) {
+      k = knew;
+      ++it;
+      break;
+    }
+    k = knew;
+  }
+  QBG_TRY(newton_eval(g, W, k, false, lam));
+  double lmin = lam[0];
+  if (!(std::isfinite(lmin) && lmin <= lbest)) {
+    k = kbest;
+    QBG_TRY(newton_eval(g, W, k, false, lam));
+    lmin = lam[0];
+  }
+  *k_out = k;
+  *t_out = std::sqrt(std::max(0.0, lmin));
+  if (iters) *iters = it;
+  return QBG_OK;
+}
+
 qbg_status qbg_small_eig(int32_t p, const double* H, double* w, double* V) {
   if (p < 1 || p > 4096 || !H || !w || !V) {
     set_error("qbg_small_eig: invalid arguments");
@@ -723,6 +882,16 @@ qbg_status qbg_small_eig(int32_t p, const double* H, double* w, double* V) {
     V[2 * i + 1] = Vz[i].imag();
   }
   return QBG_OK;
+}
+
+qbg_status qbg_newton_refine(qbg_geom* g, double k0, double a, double b, int32_t maxiter, double tol,
+                             double* k_out, double* t_out, int32_t* iters) {
+  if (!g || !k_out || !t_out || !std::isfinite(k0) || !(a <= b) || maxiter < 0 || !(tol >= 0.0)) {
+    set_error("qbg_newton_refine: invalid arguments");
+    return QBG_EINVAL;
+  }
+  std::lock_guard<std::mutex> lk(g->mu);
+  return newton_impl(g, k0, a, b, maxiter, tol, k_out, t_out, iters);
 }
 
 qbg_status qbg_ebim_solve(qbg_geom* g, double k, double dk, int32_t nev, int32_t flags, int32_t cap, double* out_k,

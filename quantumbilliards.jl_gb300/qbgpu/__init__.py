@@ -18,7 +18,8 @@ from .operators import (Workspace, build_workspace, assemble, assemble_noalloc, 
                         release_cached_memory, pool_stats,
                         chebyshev_params_min_cost)
 from .beyn import BeynHandle, construct_B_matrix, solve_vect, solve, solve_disks, probe_matrix, contour
-from .sweep import k_sweep, get_eigenvalues
+from .sweep import k_sweep, get_eigenvalues, newton_refine_svd, refine_minima
+from . import sweep
 from . import ebim
 from .serve import Server
 from .spectrum import (plan_weyl_windows, beyn_disks_from_windows, candidate_residuals,

@@ -94,3 +94,41 @@ def test_ebim_empty_window_and_count_only(qb):
     st = lib.qbg_ebim_eig(A.shape[0], A.ctypes.data, dA.ctypes.data, ddA.ctypes.data, 12.3, 0.15, 6,
                           _lib.QBG_EBIM_FULL, 0, None, None, C.byref(cnt), None)
     assert st == _lib.QBG_OK and cnt.value == 4
+
+
+def test_newton_refine_matches_oracle(qb):
+    """qbg_newton_refine (newton_refine_svd!) against the oracle on the same
+    circle discretisation. lambda_min(A^H A) reaches its rounding floor
+    (~eps |A|^2) at the eigenvalue, so the minimum fixes k only to about
+    sqrt(eps) / |sigma'| ~ 1e-8 and two correct implementations differ there:
+    refined k to 2e-8 of the oracle's and of the J_m zero, tension to 1e-7
+    absolute (both at the sqrt(eps) |A| floor)."""
+    from oracle import sweep as OS
+    b = qb.make_circle(1.0)
+    sol = qb.DLP_kress(10.0, b)
+    pts = qb.solvers.evaluate_points(sol, b, 16.0)
+    ws = qb.Workspace(sol, pts)
+    for m, i in ((3, 2), (1, 4)):
+        z = float(sp.jn_zeros(m, i + 1)[i])
+        for d in (2e-3, -1e-3):
+            k, t, it = qb.sweep.newton_refine_svd(ws, z + d, z - 0.01, z + 0.01, return_iters=True)
+            ko, to = OS.newton_refine_svd(lambda kk: OA.dlp_fredholm(pts, kk, derivs=True), z + d, z - 0.01, z + 0.01)
+            assert abs(k - ko) < 2e-8, (k, ko)
+            assert abs(t - to) < 1e-7
+            assert abs(k - z) < 2e-8
+            assert 1 <= it <= 8
+
+
+def test_refine_minima_circle_sweep(qb):
+    """refine_minima over a coarse sigma_min sweep of the circle (DLP) finds the
+    J_m zeros in the sweep range to 2e-8, with the reference's three levels."""
+    b = qb.make_circle(1.0)
+    sol = qb.DLP_kress(10.0, b)
+    ks = np.linspace(12.9, 13.1, 41)
+    sig = qb.k_sweep(sol, b, ks)
+    kr, tr, hist = qb.refine_minima(sol, b, ks, sig, threshold=50.0)
+    zeros = sorted(x for m in range(0, 20) for x in sp.jn_zeros(m, 8) if 12.92 < x < 13.08)
+    assert len(kr) >= 1
+    for k in kr:
+        assert min(abs(k - z) for z in zeros) < 2e-8
+    assert all(len(h) == 3 for h in hist)

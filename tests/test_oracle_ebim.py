@@ -47,3 +47,15 @@ def test_oracle_ebim_left_vectors_and_conventions():
     # shared roots differ at the level of the two second-order terms
     d = [np.min(np.abs(kf - x)) for x in kk]
     assert max(d) > 1e-7 and max(d) < 1e-2
+
+
+def test_oracle_newton_refine_circle():
+    """newton_refine_svd! converges to a zero of J_m from a sweep-grid guess;
+    the tension sqrt(lambda_min(A^H A)) bottoms out near sqrt(eps) |A|."""
+    from oracle import sweep as OS
+    b = G.make_circle(1.0)
+    pts = S.evaluate_points(S.DLP_kress(10.0, b), b, 16.0)
+    z = float(sp.jn_zeros(3, 3)[2])  # 13.0152
+    k, t = OS.newton_refine_svd(lambda kk: OA.dlp_fredholm(pts, kk, derivs=True), z + 2e-3, z - 0.01, z + 0.01)
+    assert abs(k - z) < 1e-8
+    assert t < 1e-7
