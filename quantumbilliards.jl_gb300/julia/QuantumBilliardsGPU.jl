@@ -170,4 +170,43 @@ function QB.construct_B_matrix(solver::GPUSolver, pts, N::Int, k0::Complex{Float
     end
 end
 
+# EBIM eigen step on given matrices — solve_krylov! (ebim.jl:464-537) and
+# solve_full! (ebim.jl:336-375); the reference dispatches them on EBIMSolver,
+# so a caller holding A, dA, ddA calls these directly (or adds the two one-line
+# methods for its own solver wrapper). Returns (k_corrected, tensions).
+const QBG_EBIM_FULL = Int32(8)
+function gpu_ebim(A::Matrix{ComplexF64}, dA::Matrix{ComplexF64}, ddA::Matrix{ComplexF64}, k::Real, dk::Real;
+                  nev::Int=5, full::Bool=false, return_imag_part::Bool=false)
+    n = size(A, 1)
+    cap = max(nev, 8)
+    while true
+        out = zeros(Float64, 2cap); tens = zeros(Float64, cap); cnt = Ref{Int32}(0)
+        GC.@preserve A dA ddA out tens qbg_check(ccall((:qbg_ebim_eig, libqbgpu), Int32,
+            (Int64, Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{ComplexF64}, Float64, Float64, Int32, Int32, Int32,
+             Ptr{Float64}, Ptr{Float64}, Ref{Int32}, Ptr{Int32}),
+            n, A, dA, ddA, k, dk, nev, full ? QBG_EBIM_FULL : Int32(0), cap, out, tens, cnt, C_NULL))
+        m = Int(cnt[])
+        if m <= cap
+            kc = [complex(out[2i - 1], out[2i]) for i in 1:m]
+            return (return_imag_part ? kc : real.(kc)), tens[1:m]
+        end
+        cap = m
+    end
+end
+QB.solve_krylov!(solver::GPUSolver, A, dA, ddA, pts, k, dk; nev::Int=5, return_imag_part::Bool=false, kwargs...) =
+    gpu_ebim(A, dA, ddA, k, dk; nev=nev, return_imag_part=return_imag_part)
+QB.solve_full!(solver::GPUSolver, A, dA, ddA, pts, k, dk; return_imag_part::Bool=false, kwargs...) =
+    gpu_ebim(A, dA, ddA, k, dk; full=true, return_imag_part=return_imag_part)
+
+# newton_refine_svd! (sweepmethods.jl:307-368) on the workspace's discretisation:
+# the reference's closure-based version assembles on the host; this one keeps
+# A, A', A'' and A^H A on the device. Returns (k, tension).
+function gpu_newton_refine(ws::GPUWorkspace, k0::Real; a::Real=0.0, b::Real=Inf, maxiter::Int=8, tol::Real=1e-12)
+    kout = Ref{Float64}(0); tout = Ref{Float64}(0)
+    qbg_check(ccall((:qbg_newton_refine, libqbgpu), Int32,
+        (Ptr{Cvoid}, Float64, Float64, Float64, Int32, Float64, Ref{Float64}, Ref{Float64}, Ptr{Int32}),
+        ws.h, k0, a, b, maxiter, tol, kout, tout, C_NULL))
+    return kout[], tout[]
+end
+
 end # module

@@ -125,9 +125,17 @@ def main(argv=None):
     ws = qb.Workspace(sol, pts)
     t0 = time.perf_counter()
     if a.case == "ebim":
-        for rep in range(3):
+        k_ebim, reps = 200.0, 3
+        if a.n >= 8192:  # CFIE on the full stadium at k0 = 1500, the large-N EBIM configuration
+            ws.close()
+            bs = qb.make_full_stadium(1.0, 1.0)
+            sol = qb.CFIE_kress_global_corners(1.0, bs)
+            pts, sol = qb.points_with_n(sol, bs, a.n, 1500.0)
+            ws = qb.Workspace(sol, pts)
+            k_ebim, reps = 1500.0, 1
+        for rep in range(reps):
             t1 = time.perf_counter()
-            kc, tens, info = qb.ebim.solve(ws, 200.0, a.dk, nev=a.nev, full=a.full, return_info=True)
+            kc, tens, info = qb.ebim.solve(ws, k_ebim, a.dk, nev=a.nev, full=a.full, return_info=True)
             print("ebim", "full" if a.full else "krylov", "N", ws.dim, "roots", np.round(kc, 6).tolist(),
                   "tens", np.round(tens, 6).tolist(), info, "ms %.1f" % ((time.perf_counter() - t1) * 1e3), flush=True)
     elif a.case == "beyn":
