@@ -278,6 +278,18 @@ qbg_status qbg_ebim_solve(qbg_geom* g, double k, double dk, int32_t nev, int32_t
 qbg_status qbg_newton_refine(qbg_geom* g, double k0, double a, double b, int32_t maxiter, double tol,
                              double* k_out, double* t_out, int32_t* iters);
 
+/* Boundary densities (DLP Kress, dlp_kress.jl:1451-1500, 1914-1949).
+ * qbg_adjoint_fredholm: the adjoint Fredholm matrix at real k,
+ * A_adj[i, j] = delta_ij - D[j, i] ds_j / ds_i (on a reduced geometry over the
+ * fundamental nodes, ds indexed by their full-boundary nodes); ds: the N
+ * arc-length weights of the full boundary (pts.ds); out: dim x dim complex128
+ * (host, or device with QBG_PTR_DEVICE).
+ * qbg_solve_vect: solve_vect's smallest_nullvec_krylov! (dlp.jl:991-1004) on
+ * that matrix: the eigenvalue mu of largest modulus of A_adj^-1 (FP64 LU, block
+ * iteration), sigma = 1/|mu| and the unit eigenvector u (dim complex). */
+qbg_status qbg_adjoint_fredholm(qbg_geom* g, double k, const double* ds, void* out, int32_t flags);
+qbg_status qbg_solve_vect(qbg_geom* g, double k, const double* ds, double* sigma, double* u);
+
 /* The host eigen-decomposition behind the EBIM Rayleigh-Ritz step, for
  * validation: eigenvalues w (p complex) and unit eigenvectors V (p x p
  * column-major, complex interleaved) of the p x p complex matrix H (Hessenberg

@@ -57,3 +57,21 @@ def newton_refine_svd(assemble, k0, a=0.0, b=np.inf, maxiter=8, tol=1e-12):
     A = assemble(kbest)[0]
     lmin = np.linalg.eigvalsh(A.conj().T @ A).min()
     return kbest, np.sqrt(max(0.0, lmin))
+
+
+def adjoint_fredholm(F, ds, fund=None):
+    """adjoint_fredholm_matrix! (dlp_kress.jl:1451-1500) from the Fredholm
+    matrix F = I - D: A_adj[i, j] = delta_ij - D[j, i] ds_j / ds_i; with a
+    reduction, ds is indexed by the fundamental nodes' full indices."""
+    d = np.asarray(ds if fund is None else np.asarray(ds)[np.asarray(fund)], dtype=np.float64)
+    D = np.eye(F.shape[0]) - F
+    return np.eye(F.shape[0]) - D.T * (d[None, :] / d[:, None])
+
+
+def smallest_nullvec(A):
+    """smallest_nullvec_krylov! (dlp.jl:991-1004), dense: the eigenvalue mu of
+    largest modulus of A^-1 (KrylovKit there), sigma = 1/|mu|, unit vector u."""
+    mu, V = np.linalg.eig(np.linalg.inv(A))
+    i = int(np.argmax(np.abs(mu)))
+    u = V[:, i] / np.linalg.norm(V[:, i])
+    return 1.0 / abs(mu[i]), u

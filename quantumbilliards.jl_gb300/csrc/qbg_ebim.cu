@@ -93,6 +93,36 @@ __global__ void k_conj_transpose(const cxd* __restrict__ A, cxd* __restrict__ AH
   }
 }
 
+__global__ void k_identity(cxd* __restrict__ M, int n) {
+  const size_t count = (size_t)n * n;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+    M[i] = cxd(i % (size_t)(n + 1) == 0 ? 1.0 : 0.0, 0.0);
+}
+
+// Adjoint Fredholm matrix from the Fredholm matrix F = I - D of the DLP:
+// Aadj[a, b] = delta_ab - D[b, a] ds_b / ds_a = F[b, a] ds_b / ds_a (the
+// diagonal ratio is 1). ds: arc-length weights of the full boundary; with a
+// reduction, fund maps reduced index -> full node. 32 x 32 shared-memory tiles.
+__global__ void k_adjoint_fredholm(const cxd* __restrict__ F, const double* __restrict__ ds,
+                                   const int* __restrict__ fund, int m, cxd* __restrict__ out) {
+  __shared__ cxd t[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int r = bx + threadIdx.x, c = by + j;
+    if (r < m && c < m) t[j][threadIdx.x] = F[r + (size_t)c * m];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int a = by + threadIdx.x, b = bx + j;  // out[a, b] = F[b, a] ds_b / ds_a = t[a - by][b - bx] ...
+    if (a < m && b < m) {
+      const double da = ds[fund ? fund[a] : a], db = ds[fund ? fund[b] : b];
+      const cxd v = t[threadIdx.x][j];
+      const double sc = (a == b) ? 1.0 : db / da;
+      out[a + (size_t)b * m] = cxd(v.re * sc, v.im * sc);
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Y = A X for n x n A and n x q X, q <= TALL_MAXQ (FP64 complex, column-major):
 // split over k into ks slices so that a skinny product still fills the device;
@@ -865,6 +895,46 @@ qbg_status newton_impl(qbg_geom* g, double k0, double a, double b, int maxiter, 
   return QBG_OK;
 }
 
+// Assembles the DLP Fredholm matrix at real k into E.LU and overwrites E.C
+// with its adjoint form (both m x m).
+int adjoint_into(qbg_geom* g, Ebim& E, double k, const double* ds_host) {
+  const int m = E.n, n = (int)g->d.n;
+  cxd* dks = nullptr;
+  void** dptrs = nullptr;
+  double* dds = nullptr;
+  QBG_TRY(E.alloc(&dks, sizeof(cxd)));
+  QBG_TRY(E.alloc(&dptrs, sizeof(void*)));
+  QBG_TRY(E.alloc(&dds, sizeof(double) * n));
+  const cxd kk(k, 0.0);
+  void* hp[1] = {E.LU};
+  QBG_CUDA(cudaMemcpyAsync(dks, &kk, sizeof(cxd), cudaMemcpyHostToDevice, E.st));
+  QBG_CUDA(cudaMemcpyAsync(dptrs, hp, sizeof(hp), cudaMemcpyHostToDevice, E.st));
+  QBG_CUDA(cudaMemcpyAsync(dds, ds_host, sizeof(double) * n, cudaMemcpyHostToDevice, E.st));
+  QBG_TRY(launch_assemble(g->d, dks, 1, 0, QBG_PREC_FP64, dptrs, m, E.st));
+  k_adjoint_fredholm<<<dim3((m + 31) / 32, (m + 31) / 32), dim3(32, 8), 0, E.st>>>(
+      E.LU, dds, g->d.m != g->d.n ? g->d.fund : nullptr, m, E.C);
+  QBG_LAUNCH_CHECK("k_adjoint_fredholm");
+  return E.wait();  // k, the pointer table and ds are staged from this frame
+}
+
+int adjoint_setup(qbg_geom* g, Ebim& E) {
+  if (g->d.form != 0 || g->d.quad != 0) {
+    set_error("the adjoint Fredholm matrix is defined for the DLP Kress formulation");
+    return QBG_ENOTSUP;
+  }
+  QBG_TRY(ebim_setup(E, (int)g->dim));
+  cudaEvent_t ev_in = nullptr;
+  QBG_CUDA(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
+  cudaError_t e = cudaEventRecord(ev_in, g->stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(E.st, ev_in, 0);
+  cudaEventDestroy(ev_in);
+  if (e != cudaSuccess) return cuda_status(e, "adjoint stream order");
+  const size_t bytes = sizeof(cxd) * (size_t)E.n * E.n;
+  QBG_TRY(E.alloc(&E.LU, bytes));
+  QBG_TRY(E.alloc(&E.C, bytes));
+  return QBG_OK;
+}
+
 qbg_status qbg_small_eig(int32_t p, const double* H, double* w, double* V) {
   if (p < 1 || p > 4096 || !H || !w || !V) {
     set_error("qbg_small_eig: invalid arguments");
@@ -892,6 +962,78 @@ qbg_status qbg_newton_refine(qbg_geom* g, double k0, double a, double b, int32_t
   }
   std::lock_guard<std::mutex> lk(g->mu);
   return newton_impl(g, k0, a, b, maxiter, tol, k_out, t_out, iters);
+}
+
+qbg_status qbg_adjoint_fredholm(qbg_geom* g, double k, const double* ds, void* out, int32_t flags) {
+  if (!g || !ds || !out || !std::isfinite(k) || !(k > 0.0)) {
+    set_error("qbg_adjoint_fredholm: invalid arguments");
+    return QBG_EINVAL;
+  }
+  std::lock_guard<std::mutex> lk(g->mu);
+  Ebim E;
+  QBG_TRY(adjoint_setup(g, E));
+  QBG_TRY(adjoint_into(g, E, k, ds));
+  const size_t bytes = sizeof(cxd) * (size_t)E.n * E.n;
+  QBG_CUDA(cudaMemcpyAsync(out, E.C, bytes, (flags & QBG_PTR_DEVICE) ? cudaMemcpyDeviceToDevice
+                                                                     : cudaMemcpyDeviceToHost, E.st));
+  return E.wait();
+}
+
+qbg_status qbg_solve_vect(qbg_geom* g, double k, const double* ds, double* sigma, double* u) {
+  if (!g || !ds || !sigma || !u || !std::isfinite(k) || !(k > 0.0)) {
+    set_error("qbg_solve_vect: invalid arguments");
+    return QBG_EINVAL;
+  }
+  std::lock_guard<std::mutex> lk(g->mu);
+  Ebim E;
+  QBG_TRY(adjoint_setup(g, E));
+  QBG_TRY(adjoint_into(g, E, k, ds));
+  const int n = E.n;
+  // LU of the adjoint matrix (in E.LU), then C = A^-1 for the block iteration
+  QBG_CUDA(cudaMemcpyAsync(E.LU, E.C, sizeof(cxd) * (size_t)n * n, cudaMemcpyDeviceToDevice, E.st));
+  if (cusolverDnCreate(&E.h) != CUSOLVER_STATUS_SUCCESS) return solver_fail("cusolverDnCreate");
+  cusolverDnSetStream(E.h, E.st);
+  QBG_TRY(E.alloc(&E.ipiv, sizeof(int) * n));
+  QBG_TRY(E.alloc(&E.dinfo, sizeof(int)));
+  int lw = 0;
+  if (cusolverDnZgetrf_bufferSize(E.h, n, n, (cuDoubleComplex*)E.LU, n, &lw) != CUSOLVER_STATUS_SUCCESS)
+    return solver_fail("getrf workspace query");
+  cxd* lwork = nullptr;
+  QBG_TRY(E.alloc(&lwork, sizeof(cxd) * (size_t)std::max(lw, 1)));
+  if (cusolverDnZgetrf(E.h, n, n, (cuDoubleComplex*)E.LU, n, (cuDoubleComplex*)lwork, E.ipiv, E.dinfo) !=
+      CUSOLVER_STATUS_SUCCESS)
+    return solver_fail("cusolverDnZgetrf");
+  int hinfo = 0;
+  QBG_CUDA(cudaMemcpyAsync(&hinfo, E.dinfo, sizeof(int), cudaMemcpyDeviceToHost, E.st));
+  QBG_TRY(E.wait());
+  if (hinfo > 0) {
+    set_error("solve_vect: the adjoint Fredholm matrix is exactly singular (U(%d, %d) = 0)", hinfo, hinfo);
+    return QBG_ESINGULAR;
+  }
+  k_identity<<<2048, 256, 0, E.st>>>(E.C, n);
+  QBG_LAUNCH_CHECK("k_identity");
+  if (cusolverDnZgetrs(E.h, CUBLAS_OP_N, n, n, (const cuDoubleComplex*)E.LU, n, E.ipiv, (cuDoubleComplex*)E.C, n,
+                       E.dinfo) != CUSOLVER_STATUS_SUCCESS)
+    return solver_fail("cusolverDnZgetrs");
+  // the eigenvalue of largest modulus of A^-1 (smallest_nullvec_krylov!, dlp.jl:991-1004)
+  const int nev = 1, p = std::min(n, 12);
+  std::vector<zc> mu;
+  cxd* V = nullptr;
+  int it = 0;
+  QBG_TRY(E.alloc(&V, sizeof(cxd) * (size_t)n));
+  QBG_TRY(block_eigs(E, false, p, nev, mu, V, &it, INFINITY));
+  std::vector<cxd> hv(n);
+  QBG_CUDA(cudaMemcpyAsync(hv.data(), V, sizeof(cxd) * n, cudaMemcpyDeviceToHost, E.st));
+  QBG_TRY(E.wait());
+  double nrm = 0.0;
+  for (const cxd& x : hv) nrm += x.re * x.re + x.im * x.im;
+  nrm = std::sqrt(nrm);
+  for (int i = 0; i < n; ++i) {
+    u[2 * i] = hv[i].re / nrm;
+    u[2 * i + 1] = hv[i].im / nrm;
+  }
+  *sigma = 1.0 / std::abs(mu[0]);
+  return QBG_OK;
 }
 
 qbg_status qbg_ebim_solve(qbg_geom* g, double k, double dk, int32_t nev, int32_t flags, int32_t cap, double* out_k,

@@ -122,6 +122,8 @@ _SIGS = {
                                  C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "qbg_newton_refine": (C.c_int32, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_double,
                                       C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
+    "qbg_adjoint_fredholm": (C.c_int32, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_int32]),
+    "qbg_solve_vect": (C.c_int32, [C.c_void_p, C.c_double, C.c_void_p, C.POINTER(C.c_double), C.c_void_p]),
     "qbg_small_eig": (C.c_int32, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "qbg_ebim_solve": (C.c_int32, [C.c_void_p, C.c_double, C.c_double, C.c_int32, C.c_int32, C.c_int32,
                                    C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int32),

@@ -68,6 +68,7 @@ class Workspace:
         self.solver = solver
         self.kind = solver.kind
         pts_l = as_list(pts)
+        self.ds = np.ascontiguousarray(np.concatenate([np.asarray(p.ds, dtype=np.float64) for p in pts_l]))
         if self.kind == "dlp" and len(pts_l) != 1:
             raise ValueError("DLP_kress expects one BoundaryPointsCFIE component")
         self._offs, self._arrs = _concat(pts_l)
@@ -338,3 +339,25 @@ def sigma_min(ws: Workspace, ks) -> np.ndarray:
     sig = np.empty(len(k))
     L.check(lib.qbg_sigma_min(ws.handle, L.dptr(k), len(k), L.dptr(sig)))
     return sig
+
+
+def adjoint_fredholm_matrix(ws: Workspace, k: float) -> np.ndarray:
+    """adjoint_fredholm_matrix! (dlp_kress.jl:1451-1500) for a DLP workspace:
+    A_adj[i, j] = delta_ij - D[j, i] ds_j / ds_i at real k (over the fundamental
+    nodes on a reduced workspace)."""
+    lib = L.load()
+    out = np.empty((ws.dim, ws.dim), np.complex128, order="F")
+    L.check(lib.qbg_adjoint_fredholm(ws.handle, float(k), ws.ds.ctypes.data, out.ctypes.data, 0))
+    return out
+
+
+def solve_vect_dlp(ws: Workspace, k: float):
+    """solve_vect for the DLP solvers (dlp_kress.jl:1914-1949): the adjoint
+    Fredholm matrix at k and smallest_nullvec_krylov! (dlp.jl:991-1004) on it.
+    Returns (sigma, u): 1/|mu| for the eigenvalue mu of largest modulus of
+    A_adj^-1 and its unit eigenvector (the boundary density)."""
+    lib = L.load()
+    sig = C.c_double()
+    u = np.empty(ws.dim, np.complex128)
+    L.check(lib.qbg_solve_vect(ws.handle, float(k), ws.ds.ctypes.data, C.byref(sig), u.ctypes.data))
+    return sig.value, u

@@ -132,3 +132,46 @@ def test_refine_minima_circle_sweep(qb):
     for k in kr:
         assert min(abs(k - z) for z in zeros) < 2e-8
     assert all(len(h) == 3 for h in hist)
+
+
+def test_adjoint_fredholm_and_solve_vect(qb):
+    """qbg_adjoint_fredholm / qbg_solve_vect (dlp_kress.jl:1451-1500,
+    1914-1949) against the oracle on the circle: the adjoint matrix to 1e-12 of
+    its max-norm; sigma at the J_0 zero below 1e-10 and 1e-9 relative away from
+    it; the density direction |u^H u_oracle| to 1e-8; the J_0 density constant
+    along the boundary."""
+    from oracle import sweep as OS
+    b = qb.make_circle(1.0)
+    sol = qb.DLP_kress(10.0, b)
+    pts = qb.solvers.evaluate_points(sol, b, 16.0)
+    ws = qb.Workspace(sol, pts)
+    z = float(sp.jn_zeros(0, 5)[4])
+    for k in (z, z + 0.05):
+        F = OA.dlp_fredholm(pts, k)
+        Ao = OS.adjoint_fredholm(F, pts.ds)
+        Ad = qb.adjoint_fredholm_matrix(ws, k)
+        assert np.max(np.abs(Ad - Ao)) < 1e-12 * np.max(np.abs(Ao))
+        sig, u = qb.solve_vect_dlp(ws, k)
+        so, uo = OS.smallest_nullvec(Ao)
+        if k == z:
+            assert sig < 1e-10
+            assert np.max(np.abs(np.abs(u) - np.abs(u).mean())) < 1e-8 * np.abs(u).mean()
+        else:
+            assert abs(sig - so) < 1e-9 * so
+        assert abs(abs(np.vdot(uo, u)) - 1.0) < 1e-8
+
+
+def test_adjoint_fredholm_reduced(qb):
+    """On a reduced workspace (stadium, XYReflection(-1, -1)) the adjoint uses
+    the fundamental nodes' arc lengths: device against the oracle's formula on
+    the device-assembled reduced Fredholm matrix, 1e-13 of its max-norm."""
+    from oracle import sweep as OS
+    bs = qb.make_full_stadium(1.0, 1.0)
+    sol = qb.DLP_kress_global_corners(1.0, bs, symmetry=qb.XYReflection(-1, -1))
+    pts, sol = qb.points_with_n(sol, bs, 512, 30.0)
+    ws = qb.Workspace(sol, pts)
+    F = qb.assemble(ws, [30.0])[0]
+    Ao = OS.adjoint_fredholm(F, ws.ds, ws._red[0])
+    Ad = qb.adjoint_fredholm_matrix(ws, 30.0)
+    assert Ad.shape == (128, 128)
+    assert np.max(np.abs(Ad - Ao)) < 1e-13 * np.max(np.abs(Ao))

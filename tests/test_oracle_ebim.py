@@ -59,3 +59,18 @@ def test_oracle_newton_refine_circle():
     k, t = OS.newton_refine_svd(lambda kk: OA.dlp_fredholm(pts, kk, derivs=True), z + 2e-3, z - 0.01, z + 0.01)
     assert abs(k - z) < 1e-8
     assert t < 1e-7
+
+
+def test_oracle_boundary_density_circle():
+    """On the circle at the simple eigenvalue j_{0,5} (a zero of J_0), the
+    adjoint Fredholm matrix is singular and its null vector, the boundary
+    normal derivative of the J_0 mode, is constant along the boundary."""
+    from oracle import sweep as OS
+    b = G.make_circle(1.0)
+    pts = S.evaluate_points(S.DLP_kress(10.0, b), b, 16.0)
+    z = float(sp.jn_zeros(0, 5)[4])
+    sig, u = OS.smallest_nullvec(OS.adjoint_fredholm(OA.dlp_fredholm(pts, z), pts.ds))
+    assert sig < 1e-10
+    assert np.max(np.abs(np.abs(u) - np.abs(u).mean())) < 1e-8 * np.abs(u).mean()
+    sig2, _ = OS.smallest_nullvec(OS.adjoint_fredholm(OA.dlp_fredholm(pts, z + 0.05), pts.ds))
+    assert sig2 > 1e-4
