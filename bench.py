@@ -276,9 +276,9 @@ def main():
     achieved = res_flops / (res_launch_ms * 1e-3) / 1e12
     issued_tflops = res_issued / (res_launch_ms * 1e-3) / 1e12
     # DRAM traffic per launch: ncu capture of the same kernel at nq = 8, L = 64
-    # (1009.99 MB read + 16.34 MB written), scaled by the contour nodes (48 / 8);
+    # (1009.98 MB read + 16.03 MB written), scaled by the contour nodes (48 / 8);
     # the algorithmic bytes (digit planes of T and X, V, R) are 1.03 GB at nq = 8
-    res_traffic = (1009.99e6 + 16.34e6) * (NQ / 8.0)
+    res_traffic = (1009.98e6 + 16.03e6) * (NQ / 8.0)
     res_alg_bytes = (7 * N * 2 * N * 2 + 7 * 2 * lp * 2 * N * 2 + 2 * 16 * N * L_PROBES) * NQ
     lu_flops = NQ * (8.0 / 3.0) * N ** 3
     ms_factor = float(np.mean([s[0]["ms_factor"] for s in stats]))
