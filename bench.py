@@ -10,6 +10,11 @@ LU, T^-1 V solves (+ regrowth solves), moments, host SVD/eig.
 metric: eigenvalues/s of the mixed form (FP32 assembly/LU + compensated
 refinement) counting eigenvalues inside the disk that agree with the plain
 FP64 GPU path to <= 1e-10 relative; the plain FP64 path is timed beside it.
+
+--workload ebim prints a second line for the EBIM eigen step on the same
+geometry (k = 200, dk = 0.05, nev = 5): steps/s of device assembly + eigen
+step, the same from host matrices (e2e), and the oracle's dense
+solve_krylov on the same matrices as the CPU baseline.
 """
 from __future__ import annotations
 
@@ -183,6 +188,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--workload", default="beyn", choices=["beyn", "ebim"],
+                    help="beyn: the headline Beyn disk (default); ebim: the EBIM eigen step at one k")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -190,7 +197,11 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        return reference_arm(args)
+        return reference_arm_ebim(args) if args.workload == "ebim" else reference_arm(args)
+    if args.workload == "ebim":
+        if rank != 0:
+            return
+        return ebim_workload(args)
     if world > 1:
         # one process per GPU: this rank sees only its own device
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("LOCAL_RANK", str(rank)))
@@ -337,6 +348,89 @@ def main():
                                 "sample": "oracle assembly+LU+solve of 1 of 48 contour nodes, extrapolated x48"}
     if rank == 0:
         print(json.dumps(line))
+
+
+EBIM_K, EBIM_DK, EBIM_NEV = 200.0, 0.05, 5
+EBIM_METRIC = "EBIM eigen steps/s (solve_krylov!, nev = 5, dk = 0.05), CFIE Kress star N = 2048, k = 200"
+EBIM_CONFIG = {"workload": "ebim_cfie_kress_star_N2048_k200_dk0.05_nev5", "N": N_NODES, "k": EBIM_K, "dk": EBIM_DK,
+               "nev": EBIM_NEV, "l2": "A, A', A'' and C = A^-1 A' (67 MB each) stream from HBM"}
+
+
+def ebim_workload(args):
+    """--workload ebim: one step = A, A', A'' assembled at k on the device and
+    the eigen step of solve_krylov! (qbg_ebim_solve); e2e = the same step from
+    host matrices through qbgpu.ebim.solve_krylov (the three N x N matrices
+    copied in every step). cpu_baseline: the oracle's solve_krylov on the same
+    matrices (dense LAPACK eig of A^-1 A' and its adjoint)."""
+    import build_qbgpu as B
+    B.build()
+    import qbgpu as qb
+    from qbgpu import _lib
+    b, sol, pts = star_workspace(qb)
+    ws = qb.Workspace(sol, pts)
+    for _ in range(args.warmup):
+        qb.ebim.solve(ws, EBIM_K, EBIM_DK, nev=EBIM_NEV)
+    _lib.load().qbg_device_sync()
+    clk = ClockSampler()
+    clk.start()
+    launches0 = qb.launch_count()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        kc, tens = qb.ebim.solve(ws, EBIM_K, EBIM_DK, nev=EBIM_NEV)
+    _lib.load().qbg_device_sync()
+    t = (time.perf_counter() - t0) / args.steps
+    launches = qb.launch_count() - launches0
+    clocks = clk.stop()
+    A, dA, ddA = qb.assemble(ws, [EBIM_K], deriv=True)
+    qb.ebim.solve_krylov(None, A, dA, ddA, pts, EBIM_K, EBIM_DK, nev=EBIM_NEV)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        qb.ebim.solve_krylov(None, A, dA, ddA, pts, EBIM_K, EBIM_DK, nev=EBIM_NEV)
+    te = (time.perf_counter() - t0) / args.steps
+    line = {"metric": EBIM_METRIC, "value": 1.0 / t, "unit": "EBIM steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic", "config": EBIM_CONFIG,
+            "roots": [round(float(x), 9) for x in kc], "tensions": [float(x) for x in tens],
+            "e2e": {"value": 1.0 / te, "unit": "EBIM steps/s", "h2d_bytes_per_step": 3 * 16 * ws.dim ** 2,
+                    "d2h_bytes_per_step": 24 * len(kc)},
+            "gpu_launches": launches, "clocks": clocks}
+    if not args.no_cpu_baseline:
+        from oracle import ebim as OE
+        t0 = time.perf_counter()
+        ko, _ = OE.solve_krylov(A, dA, ddA, EBIM_K, EBIM_DK, nev=EBIM_NEV)
+        tc = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": 1.0 / tc, "unit": "EBIM steps/s", "cores": os.cpu_count(), "kind": "port",
+                                "sample": "one solve_krylov step of the oracle (LU, dense eig of A^-1 A' and of its "
+                                          "adjoint) on the same device-assembled matrices"}
+        if len(ko) == len(kc):
+            line["max_abs_diff_vs_oracle"] = float(np.max(np.abs(np.sort(ko) - np.sort(kc)))) if len(ko) else 0.0
+    print(json.dumps(line))
+
+
+def reference_arm_ebim(args):
+    """--impl reference --workload ebim: the oracle's solve_krylov on its own
+    FP64 assembly of the same workload, one eigen step per timed step."""
+    import qbgpu.geometry as G  # host-only modules (no GPU work)
+    from qbgpu import solvers as S
+    from oracle import assembly as OA, ebim as OE
+    b = G.make_star(0.2, 5)
+    pts, sol = S.points_with_n(S.CFIE_kress(1.0, b), b, N_NODES, K0)
+    A, dA, ddA = OA.cfie_matrix_derivs(pts, EBIM_K)
+    for _ in range(min(args.warmup, 1)):
+        OE.solve_krylov(A, dA, ddA, EBIM_K, EBIM_DK, nev=EBIM_NEV)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        OE.solve_krylov(A, dA, ddA, EBIM_K, EBIM_DK, nev=EBIM_NEV)
+        times.append(time.perf_counter() - t0)
+    t = float(np.mean(times))
+    print(json.dumps({"impl": "reference", "metric": EBIM_METRIC, "value": 1.0 / t, "unit": "EBIM steps/s",
+                      "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+                      "higher_is_better": True, "dtype": "c128", "data": "synthetic", "config": EBIM_CONFIG,
+                      "cpu_baseline": {"value": 1.0 / t, "unit": "EBIM steps/s", "cores": os.cpu_count(),
+                                       "kind": "port", "sample": "the full eigen step per timed step"},
+                      "e2e": {"value": 1.0 / t, "unit": "EBIM steps/s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}))
 
 
 def reference_arm(args):

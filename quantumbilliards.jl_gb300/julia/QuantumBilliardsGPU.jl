@@ -209,4 +209,23 @@ function gpu_newton_refine(ws::GPUWorkspace, k0::Real; a::Real=0.0, b::Real=Inf,
     return kout[], tout[]
 end
 
+# adjoint_fredholm_matrix!(A, D, solver, pts, ws, k) (dlp_kress.jl:1451-1500) and
+# solve_vect(solver, basis, pts, ws, k) (dlp_kress.jl:1914-1949) for the DLP
+# forms: the adjoint matrix and the smallest null vector on the device.
+function QB.adjoint_fredholm_matrix!(A::Matrix{ComplexF64}, D::AbstractMatrix{ComplexF64}, solver::GPUSolver,
+                                     pts, ws::GPUWorkspace, k::Real; kwargs...)
+    ds = collect(Float64, pts.ds)
+    GC.@preserve A ds qbg_check(ccall((:qbg_adjoint_fredholm, libqbgpu), Int32,
+        (Ptr{Cvoid}, Float64, Ptr{Float64}, Ptr{ComplexF64}, Int32), ws.h, k, ds, A, Int32(0)))
+    return A
+end
+function QB.solve_vect(solver::GPUSolver, basis::QB.AbsBasis, pts, ws::GPUWorkspace, k::Real; kwargs...)
+    ds = collect(Float64, pts.ds)
+    u = Vector{ComplexF64}(undef, ws.dim)
+    sig = Ref{Float64}(0)
+    GC.@preserve ds u qbg_check(ccall((:qbg_solve_vect, libqbgpu), Int32,
+        (Ptr{Cvoid}, Float64, Ptr{Float64}, Ref{Float64}, Ptr{ComplexF64}), ws.h, k, ds, sig, u))
+    return sig[], u
+end
+
 end # module
