@@ -86,4 +86,105 @@ def solve(ws: Workspace, k, dk, nev=5, full=False, return_imag_part=False, retur
     return (kc, tens, info) if return_info else (kc, tens)
 
 
-__all__ = ["solve_krylov", "solve_full", "solve"]
+def _local_gap(xs, i, w=4):
+    """_local_gap (ebim.jl:1021-1029): median positive gap of xs within +-w."""
+    seg = np.diff(xs[max(0, i - w):min(len(xs), i + w + 1)])
+    seg = seg[seg > 0]
+    return float(np.median(seg)) if len(seg) else np.inf
+
+
+def _score(k, t):
+    """_ebim_scoring_logic (ebim.jl:1001-1003): lower is better."""
+    eps = np.finfo(float).eps
+    return np.log10(abs(complex(k).imag) + eps) + np.log10(abs(float(t)) + eps)
+
+
+def overlap_and_merge_ebim(k_left, ten_left, k_right, ten_right, control_left, kl, kr, tol=1e-5,
+                           spacing_frac=0.02, tolmax=5e-3, local_window=4):
+    """overlap_and_merge_ebim! (ebim.jl:1059-1107): appends the right window's
+    roots, sorts by Re k, clusters neighbours closer than
+    min(tolmax, max(tol, spacing_frac * local gap)) and keeps the best-scoring
+    root of each cluster (control marks clusters of more than one root).
+    Updates the three lists in place."""
+    if len(k_right) == 0:
+        return
+    k_all = list(k_left) + list(k_right)
+    t_all = list(ten_left) + list(ten_right)
+    c_all = list(control_left) + [False] * len(k_right)
+    order = sorted(range(len(k_all)), key=lambda q: np.real(k_all[q]))
+    k_all = [k_all[q] for q in order]
+    t_all = [t_all[q] for q in order]
+    c_all = [c_all[q] for q in order]
+    xs = np.array([np.real(x) for x in k_all])
+    nk, nt, nc = [], [], []
+    i = 0
+    while i < len(k_all):
+        j = i
+        while j < len(k_all) - 1:
+            gap = xs[j + 1] - xs[j]
+            lgap = min(_local_gap(xs, j, local_window), _local_gap(xs, j + 1, local_window))
+            local_tol = min(tolmax, max(tol, spacing_frac * lgap))
+            if gap <= local_tol:
+                j += 1
+            else:
+                break
+        best = min(range(i, j + 1), key=lambda q: (_score(k_all[q], t_all[q]), q))
+        nk.append(k_all[best])
+        nt.append(t_all[best])
+        nc.append(any(c_all[i:j + 1]) or j > i)
+        i = j + 1
+    k_left[:], ten_left[:], control_left[:] = nk, nt, nc
+
+
+def ebim_windows(billiard, k1, k2, dk=lambda k: 0.05 * k ** (-1.0 / 3.0)):
+    """The window centres, half-widths and requested nev of compute_spectrum_ebim
+    (ebim.jl:1159-1173): k advances by dk(k); nev = ceil((area k / 2 pi -
+    length / 4 pi) dk) + 10 (Weyl's law with padding)."""
+    ks, dks = [], []
+    k = float(k1)
+    while k < k2:
+        ks.append(k)
+        d = float(dk(k))
+        dks.append(d)
+        k += d
+    nevs = [int(np.ceil((billiard.area * kk / (2 * np.pi) - billiard.length / (4 * np.pi)) * d)) + 10
+            for kk, d in zip(ks, dks)]
+    return ks, dks, nevs
+
+
+def compute_spectrum_ebim(solver, billiard, k1, k2, dk=lambda k: 0.05 * k ** (-1.0 / 3.0), tol=1e-5,
+                          use_krylov=True, seg_reuse_frac=0.95, return_imag_part=False):
+    """compute_spectrum_ebim (ebim.jl:1158-1268) with direct FP64 assembly:
+    windows from ebim_windows; the discretisation is built at a segment's upper
+    k and reused while k_next <= k_first / seg_reuse_frac; every window runs the
+    device eigen step (solve_krylov!, or solve_full! with use_krylov=False) with
+    its Weyl nev; overlapping roots are merged (overlap_and_merge_ebim!) and
+    those with k1 <= Re k <= k2 kept. Returns (k, tension)."""
+    from .solvers import evaluate_points
+    ks, dks, nevs = ebim_windows(billiard, k1, k2, dk)
+    if not ks:
+        return np.zeros(0), np.zeros(0)
+    results = [None] * len(ks)
+    first = 0
+    while first < len(ks):
+        last = first
+        while last < len(ks) - 1 and ks[last + 1] <= ks[first] / seg_reuse_frac:
+            last += 1
+        ws = Workspace(solver, evaluate_points(solver, billiard, ks[last]))
+        try:
+            for i in range(first, last + 1):
+                results[i] = solve(ws, ks[i], dks[i], nev=nevs[i], full=not use_krylov,
+                                   return_imag_part=return_imag_part)
+        finally:
+            ws.close()
+        first = last + 1
+    k_all, t_all, ctrl = [], [], []
+    for i in range(len(ks)):
+        lam, tens = results[i]
+        if len(lam):
+            overlap_and_merge_ebim(k_all, t_all, list(lam), list(tens), ctrl, ks[i] - dks[i], ks[i] + dks[i], tol=tol)
+    keep = [q for q, x in enumerate(k_all) if k1 <= np.real(x) <= k2]
+    return np.array([k_all[q] for q in keep]), np.array([t_all[q] for q in keep])
+
+
+__all__ = ["solve_krylov", "solve_full", "solve", "overlap_and_merge_ebim", "ebim_windows", "compute_spectrum_ebim"]

@@ -74,3 +74,21 @@ def test_oracle_boundary_density_circle():
     assert np.max(np.abs(np.abs(u) - np.abs(u).mean())) < 1e-8 * np.abs(u).mean()
     sig2, _ = OS.smallest_nullvec(OS.adjoint_fredholm(OA.dlp_fredholm(pts, z + 0.05), pts.ds))
     assert sig2 > 1e-4
+
+
+def test_ebim_merge_and_windows():
+    """Host logic of compute_spectrum_ebim (ebim.jl:1158-1268): the window grid
+    and Weyl nev, and overlap_and_merge_ebim! (ebim.jl:1059-1107) keeping the
+    lower-tension copy of a root found by two windows."""
+    from qbgpu import ebim as QE
+    b = G.make_circle(1.0)
+    ks, dks, nevs = QE.ebim_windows(b, 14.0, 15.0)
+    assert ks[0] == 14.0 and ks[-1] < 15.0 and ks[-1] + dks[-1] >= 15.0
+    assert all(abs(d - 0.05 * k ** (-1 / 3)) < 1e-15 for k, d in zip(ks, dks))
+    assert nevs[0] == int(np.ceil((np.pi * 14.0 / (2 * np.pi) - 2 * np.pi / (4 * np.pi)) * dks[0])) + 10
+    kl, tl, cl = [], [], []
+    QE.overlap_and_merge_ebim(kl, tl, [14.7959518, 14.9309177], [3e-3, 2e-2], cl, 14.78, 14.80)
+    QE.overlap_and_merge_ebim(kl, tl, [14.7959517, 14.8212687], [1e-3, 4e-3], cl, 14.80, 14.82)
+    assert len(kl) == 3
+    assert abs(kl[0] - 14.7959517) < 1e-12 and tl[0] == 1e-3  # the lower tension wins
+    assert cl == [True, False, False]
