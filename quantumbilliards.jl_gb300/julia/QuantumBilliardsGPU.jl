@@ -198,6 +198,16 @@ QB.solve_krylov!(solver::GPUSolver, A, dA, ddA, pts, k, dk; nev::Int=5, return_i
 QB.solve_full!(solver::GPUSolver, A, dA, ddA, pts, k, dk; return_imag_part::Bool=false, kwargs...) =
     gpu_ebim(A, dA, ddA, k, dk; full=true, return_imag_part=return_imag_part)
 
+# solve!(solver, A, dA, ddA, pts, k, dk; use_krylov, nev) (ebim.jl:931-939): one
+# EBIM window, assembly and eigen step on the GPU.
+function QB.solve!(solver::GPUSolver, A::Matrix{ComplexF64}, dA::Matrix{ComplexF64}, ddA::Matrix{ComplexF64},
+                   pts, k::Real, dk::Real; use_krylov::Bool=true, nev::Int=5, return_imag_part::Bool=false,
+                   kwargs...)
+    ws = gpu_workspace(solver, pts)
+    QB.construct_matrices!(solver, A, dA, ddA, pts, ws, k)
+    return gpu_ebim(A, dA, ddA, k, dk; nev=nev, full=!use_krylov, return_imag_part=return_imag_part)
+end
+
 # newton_refine_svd! (sweepmethods.jl:307-368) on the workspace's discretisation:
 # the reference's closure-based version assembles on the host; this one keeps
 # A, A', A'' and A^H A on the device. Returns (k, tension).
