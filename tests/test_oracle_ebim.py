@@ -92,3 +92,76 @@ def test_ebim_merge_and_windows():
     assert len(kl) == 3
     assert abs(kl[0] - 14.7959517) < 1e-12 and tl[0] == 1e-3  # the lower tension wins
     assert cl == [True, False, False]
+
+
+def test_refine_minima_host_logic(monkeypatch):
+    """refine_minima (sweepmethods.jl:471-565) orchestration with the device
+    Newton step faked: window = max(3 dk_grid, 1e-3) shrinking by 3 per level,
+    pts_scaling_factor x (1, 1.5, 2), each level starting from the previous k,
+    and the stop_k_tol early exit."""
+    from qbgpu import sweep as SW
+    calls = []
+
+    class FakeWS:
+        def __init__(self, solver, pts):
+            self.factor = solver.pts_scaling_factor
+
+        def close(self):
+            pass
+
+    def fake_newton(ws, k0, a, b, maxiter, tol):
+        calls.append((ws.factor, k0, a, b))
+        return k0 + 1e-4 / ws.factor, 1e-9  # moves less at finer levels
+
+    monkeypatch.setattr(SW, "Workspace", FakeWS)
+    monkeypatch.setattr(SW, "evaluate_points", lambda s, b, k: None)
+    monkeypatch.setattr(SW, "newton_refine_svd", fake_newton)
+    b = G.make_circle(1.0)
+    sol = S.DLP_kress(10.0, b)
+    ks = np.linspace(13.0, 13.04, 9)              # grid step 0.005
+    tens = np.abs(ks - 13.0152) + 1e-6           # one minimum
+    kr, tr, hist = SW.refine_minima(sol, b, ks, tens, threshold=1.0)
+    assert len(kr) == 1 and len(hist[0]) == 3
+    assert [c[0] for c in calls] == [10.0, 15.0, 20.0]
+    w = [c[3] - c[1] for c in calls]
+    assert abs(w[0] - 0.015) < 1e-12 and abs(w[1] - 0.005) < 1e-12 and abs(w[2] - 0.015 / 9) < 1e-12
+    assert calls[1][1] == hist[0][0]["k"] and calls[2][1] == hist[0][1]["k"]
+    assert kr[0] == hist[0][2]["k"]
+    calls.clear()
+    kr, tr, hist = SW.refine_minima(sol, b, ks, tens, threshold=1.0, stop_k_tol=1e-4)
+    assert len(hist[0]) == 2  # |k2 - k1| = 1e-4 / 15 <= stop_k_tol ends the ladder at level 2
+
+
+def test_compute_spectrum_ebim_host_logic(monkeypatch):
+    """compute_spectrum_ebim orchestration with the device step faked: one
+    discretisation per segment (built at the segment's last k, reused while
+    k_next <= k_first / 0.95), the Weyl nev per window, the merge and the final
+    [k1, k2] filter."""
+    from qbgpu import ebim as QE
+    built, solved = [], []
+
+    class FakeWS:
+        def __init__(self, solver, pts):
+            built.append(pts)
+
+        def close(self):
+            pass
+
+    def fake_solve(ws, k, dk, nev, full, return_imag_part):
+        solved.append((k, dk, nev))
+        return np.array([14.0 + 0.5 * round((k - 14.0) / 0.5)]), np.array([abs(k - 14.0)])
+
+    monkeypatch.setattr(QE, "Workspace", FakeWS)
+    monkeypatch.setattr(QE, "solve", fake_solve)
+    import qbgpu.solvers as QS
+    monkeypatch.setattr(QS, "evaluate_points", lambda s, b, k: k)
+    b = G.make_circle(1.0)
+    ks, dks, nevs = QE.ebim_windows(b, 13.0, 15.0)
+    out, tens = QE.compute_spectrum_ebim(S.DLP_kress(10.0, b), b, 13.0, 15.0)
+    assert [s[2] for s in solved] == nevs and [s[0] for s in solved] == ks
+    # segments: each built at its last window's k; every window inside one
+    firsts = [ks[0]] + [ks[i + 1] for i, k in enumerate(ks[:-1]) if k in built]
+    assert built[-1] == ks[-1] and all(k <= f / 0.95 for f, k in zip(firsts, built))
+    # roots 13.0, 13.5, 14.0, 14.5, 15.0 merged to one copy each, the best (lowest tension) kept
+    assert list(out) == [13.0, 13.5, 14.0, 14.5, 15.0]
+    assert tens[2] == min(abs(k - 14.0) for k in ks)
