@@ -1,6 +1,6 @@
 """Benchmark: Beyn contour step on the star domain (CFIE Kress), one GB300.
 
-Workload (the BASELINE metric's configuration): CFIE_kress on the star
+Workload (the headline metric's configuration): CFIE_kress on the star
 r(theta) = 1 + 0.2 cos(5 theta), N = 2048 nodes, one disk k0 = 200, R = 0.5,
 nq = 48 trapezoid contour nodes, L = 64 seeded complex Gaussian probes (std 1),
 svd_tol = 1e-12, the reference's single r -> 2r regrowth when the rank
