@@ -17,6 +17,7 @@
 //   After the last panel the upper diagonal blocks are inverted so that the
 //   triangular solves are sequences of GEMMs.
 #include <algorithm>
+#include <cstdlib>
 #include <type_traits>
 #include "qbg_linalg.cuh"
 
@@ -664,7 +665,12 @@ static int lu_factor_one(LUBatch<T>& f, cudaStream_t st, cudaEvent_t after_first
   // forward substitution (the nb x nb inverses of L from k_trtri). The row
   // interchanges of every panel still apply to all columns at once (k_laswp),
   // so the factors are those of the one-level algorithm.
-  constexpr int LU_OUTER = 4;
+  // panels per outer block: QBG_LU_OUTER in the environment (1..16, default 4)
+  static const int LU_OUTER = [] {
+    const char* e = std::getenv("QBG_LU_OUTER");
+    const int v = (e && *e) ? std::atoi(e) : 4;
+    return std::max(1, std::min(v, 16));
+  }();
   const cx<T> one(1, 0), mone(-1, 0), zero(0, 0);
   auto linv = [&](int j) { return f.Linv + (long long)(j / nb) * nb * nb; };
   const long long sLinv = (long long)f.nblk * nb * nb;
