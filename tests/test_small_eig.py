@@ -49,3 +49,23 @@ def test_small_eig_matches_numpy(qb):
     Qm, _ = np.linalg.qr(rng.standard_normal((24, 24)) + 1j * rng.standard_normal((24, 24)))
     D = np.diag(np.logspace(4, 0, 24) * np.exp(1j * rng.uniform(0, 6.28, 24)))
     _check(lib, Qm @ D @ np.linalg.inv(Qm))
+
+
+def test_small_eig_edge_cases(qb):
+    """Zero matrix (eigenvalues 0, unit vectors), a Jordan block (the
+    repeated eigenvalue; its eigenvectors are defective, only the values are
+    checked), and a NaN input, which returns an error instead of iterating on."""
+    from qbgpu import _lib
+    lib = _lib.load()
+    w, V = small_eig(lib, np.zeros((5, 5), np.complex128))
+    assert np.all(w == 0) and np.allclose(np.linalg.norm(V, axis=0), 1.0)
+    J = np.diag(np.full(4, 2.0 + 1.0j)) + np.diag(np.ones(3), 1)
+    w, _ = small_eig(lib, J)
+    assert np.max(np.abs(w - (2.0 + 1.0j))) < 1e-3  # a defective eigenvalue moves by eps^(1/4)
+    H = np.ones((4, 4), np.complex128)
+    H[1, 2] = np.nan
+    Hf = np.asfortranarray(H)
+    w = np.zeros(4, np.complex128)
+    V = np.zeros((4, 4), np.complex128, order="F")
+    assert lib.qbg_small_eig(4, Hf.ctypes.data, w.ctypes.data, V.ctypes.data) != 0
+    assert "converge" in _lib.last_error()
