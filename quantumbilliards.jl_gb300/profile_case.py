@@ -95,9 +95,25 @@ def large_case(qb, a):
                           refine=st["refine_history"], ms_residual=st["ms_residual"])))
 
 
+def sweep_case(qb):
+    """The sigma_min sweep of the unit circle (DLP Kress, pts_scaling_factor
+    12.2: N = 512 at k = 42) over 200 k in [40, 42], then refine_minima."""
+    b = qb.make_circle(1.0)
+    sol = qb.DLP_kress(12.2, b)
+    ks = np.linspace(40.0, 42.0, 200)
+    qb.k_sweep(sol, b, ks[:4])  # warm-up
+    t0 = time.perf_counter()
+    sig = qb.k_sweep(sol, b, ks)
+    t1 = time.perf_counter()
+    kr, tr, hist = qb.refine_minima(sol, b, ks, sig)
+    t2 = time.perf_counter()
+    print(json.dumps(dict(case="sweep", N=512, nk=len(ks), sweep_s=t1 - t0, refine_s=t2 - t1, minima=len(kr),
+                          refined=[round(float(k), 10) for k in kr])))
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["beyn", "assemble", "disks", "large", "ebim"])
+    ap.add_argument("case", choices=["beyn", "assemble", "disks", "large", "ebim", "sweep"])
     ap.add_argument("--ndisk", type=int, default=32)
     ap.add_argument("--repeat", type=int, default=1, help="disks: batches run back to back (first cold, rest warm)")
     ap.add_argument("--chunk", type=int, default=8)
@@ -117,6 +133,8 @@ def main(argv=None):
     build_qbgpu.build()
     import qbgpu as qb
     qb.set_gemm_engine(a.gemm_engine)
+    if a.case == "sweep":
+        return sweep_case(qb)
     if a.case == "disks":
         return disks_case(qb, a)
     if a.case == "large":

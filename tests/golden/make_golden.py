@@ -8,8 +8,14 @@ and the device special functions.
 circle_eigs.json: Dirichlet eigenvalues of the unit circle (zeros of J_m)
 in [40, 42] and [14.6, 15.4], the known answers of the sigma_min sweep and the
 Beyn disk on the circle.
+
+c1_sweep.json (``python tests/golden/make_golden.py c1``, about 80 s): the
+oracle's sigma_min sweep of the unit circle, DLP Kress with
+pts_scaling_factor 12.2 (N = 512 at k = 42), 200 k in [40, 42] -- the smallest
+singular value of the FP64 Fredholm matrix at each k.
 """
 import json
+import sys
 from pathlib import Path
 
 import mpmath as mp
@@ -46,7 +52,24 @@ def circle_eigs(lo, hi):
     return sorted(out, key=lambda r: r["k"])
 
 
-if __name__ == "__main__":
+def c1_sweep():
+    root = HERE.parents[1]
+    sys.path.insert(0, str(root))
+    sys.path.insert(0, str(root / "quantumbilliards.jl_gb300"))
+    from oracle import assembly as OA, beyn as OB
+    from qbgpu import geometry as G, solvers as S
+    b = G.make_circle(1.0)
+    sol = S.DLP_kress(12.2, b)
+    ks = np.linspace(40.0, 42.0, 200)
+    pts = S.evaluate_points(sol, b, float(ks.max()))
+    sig = [float(OB.sigma_min(OA.dlp_fredholm(pts, k))) for k in ks]
+    return {"N": int(pts.n), "pts_scaling_factor": 12.2, "ks": ks.tolist(), "sigma": sig}
+
+
+if __name__ == "__main__" and sys.argv[1:] == ["c1"]:
+    (HERE / "c1_sweep.json").write_text(json.dumps(c1_sweep()))
+    print("written")
+elif __name__ == "__main__":
     (HERE / "bessel_mpmath.json").write_text(json.dumps({"dps": 40, "values": bessel_rows()}, indent=1))
     (HERE / "circle_eigs.json").write_text(json.dumps({"ranges": {"40_42": circle_eigs(40.0, 42.0),
                                                                   "14.6_15.4": circle_eigs(14.6, 15.4)}},
