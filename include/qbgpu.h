@@ -154,6 +154,8 @@ qbg_status qbg_assemble_cheb(qbg_geom* g, const double* ks, int64_t nk, int32_t 
  * QBG_PTR_DEVICE). The wavenumbers and the output-pointer table are staged in
  * a fixed device array of QBG_NOALLOC_MAX_K entries (20 KiB, resident on each
  * device until exit); nk > QBG_NOALLOC_MAX_K is rejected with QBG_EINVAL.
+ * Alpert geometries are accepted with prec QBG_PREC_FP64 only (their complex64
+ * forms stage FP64 blocks of N^2 entries): other precisions return QBG_ENOTSUP.
  * Calls share that array and are serialised inside the process; each returns
  * after its kernel finished. The first call on a device resolves the array's
  * address on that device: make it before any stream capture. */

@@ -20,6 +20,9 @@
 //    Calls that overlap on the GPU would race on it: calls made through this
 //    entry point are serialised inside the process and each returns only after
 //    its kernel has finished;
+//  * Alpert geometries are accepted in FP64 only: their complex64 forms stage
+//    FP64 blocks of N^2 entries per wavenumber, which a fixed array cannot
+//    hold, so that combination returns QBG_ENOTSUP;
 //  * the first call on a device resolves the array's device address for that
 //    device (cudaGetSymbolAddress with that device current); make that first
 //    call before any stream capture on the device.
@@ -91,6 +94,12 @@ extern "C" qbg_status qbg_assemble_noalloc(qbg_geom* g, const double* ks, int64_
       qbg::set_error("qbg_assemble_noalloc: output pointer %d is null", o);
       return QBG_EINVAL;
     }
+  if (g->d.quad == 1 && prec != QBG_PREC_FP64) {
+    // the complex64 Alpert forms accumulate their corrections in FP64 staging
+    // blocks of N^2 entries per wavenumber, far larger than a fixed array
+    qbg::set_error("qbg_assemble_noalloc: Alpert geometries are assembled without allocation in FP64 only");
+    return QBG_ENOTSUP;
+  }
   std::lock_guard<std::mutex> lk_all(g_mu);
   std::lock_guard<std::mutex> lk(g->mu);
   void* base = nullptr;
@@ -99,10 +108,14 @@ extern "C" qbg_status qbg_assemble_noalloc(qbg_geom* g, const double* ks, int64_
   cxd* dks = reinterpret_cast<cxd*>(base);
   void** dptrs = reinterpret_cast<void**>(static_cast<unsigned char*>(base) + kKsBytes);
   cudaStream_t st = g->stream;
-  QBG_CUDA(cudaMemcpyAsync(dks, ks, sizeof(cxd) * nk, cudaMemcpyHostToDevice, st));
-  QBG_CUDA(cudaMemcpyAsync(dptrs, outs_dev, sizeof(void*) * nout, cudaMemcpyHostToDevice, st));
-  s = qbg::launch_assemble(g->d, dks, (int)nk, deriv, prec, dptrs, g->dim, st);
+  // From the first queued copy on, every return waits for the stream: the next
+  // call (possibly on another geometry's stream) overwrites the same array.
+  cudaError_t e = cudaMemcpyAsync(dks, ks, sizeof(cxd) * nk, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dptrs, outs_dev, sizeof(void*) * nout, cudaMemcpyHostToDevice, st);
+  s = e == cudaSuccess ? QBG_OK : qbg::cuda_status(e, "qbg_assemble_noalloc staging copy");
+  if (!s) s = qbg::launch_assemble(g->d, dks, (int)nk, deriv, prec, dptrs, g->dim, st);
+  const cudaError_t es = cudaStreamSynchronize(st);
   if (s) return s;
-  QBG_CUDA(cudaStreamSynchronize(st));
+  if (es != cudaSuccess) return qbg::cuda_status(es, "qbg_assemble_noalloc");
   return QBG_OK;
 }

@@ -152,11 +152,29 @@ def ebim_windows(billiard, k1, k2, dk=lambda k: 0.05 * k ** (-1.0 / 3.0)):
     return ks, dks, nevs
 
 
+def segment_plan(ks, seg_reuse_frac=0.95):
+    """Segments of windows that share one discretisation (ebim.jl:1195-1226):
+    a segment runs from first to the last window with
+    ks[last] <= ks[first] / seg_reuse_frac. The first segment uses the points
+    built at ks[0] (pts0, ebim.jl:1176, 1201); every later segment is
+    discretised at its own upper wavenumber ks[last]. Returns a list of
+    (first, last, k_disc), 0-based and inclusive."""
+    out = []
+    first = 0
+    while first < len(ks):
+        last = first
+        while last < len(ks) - 1 and ks[last + 1] <= ks[first] / seg_reuse_frac:
+            last += 1
+        out.append((first, last, ks[0] if first == 0 else ks[last]))
+        first = last + 1
+    return out
+
+
 def compute_spectrum_ebim(solver, billiard, k1, k2, dk=lambda k: 0.05 * k ** (-1.0 / 3.0), tol=1e-5,
                           use_krylov=True, seg_reuse_frac=0.95, return_imag_part=False):
     """compute_spectrum_ebim (ebim.jl:1158-1268) with direct FP64 assembly:
-    windows from ebim_windows; the discretisation is built at a segment's upper
-    k and reused while k_next <= k_first / seg_reuse_frac; every window runs the
+    windows from ebim_windows; the segments are those of segment_plan (the
+    first discretised at ks[0], later ones at their upper k); every window runs the
     device eigen step (solve_krylov!, or solve_full! with use_krylov=False) with
     its Weyl nev; overlapping roots are merged (overlap_and_merge_ebim!) and
     those with k1 <= Re k <= k2 kept. Returns (k, tension)."""
@@ -165,19 +183,14 @@ def compute_spectrum_ebim(solver, billiard, k1, k2, dk=lambda k: 0.05 * k ** (-1
     if not ks:
         return np.zeros(0), np.zeros(0)
     results = [None] * len(ks)
-    first = 0
-    while first < len(ks):
-        last = first
-        while last < len(ks) - 1 and ks[last + 1] <= ks[first] / seg_reuse_frac:
-            last += 1
-        ws = Workspace(solver, evaluate_points(solver, billiard, ks[last]))
+    for first, last, k_disc in segment_plan(ks, seg_reuse_frac):
+        ws = Workspace(solver, evaluate_points(solver, billiard, k_disc))
         try:
             for i in range(first, last + 1):
                 results[i] = solve(ws, ks[i], dks[i], nev=nevs[i], full=not use_krylov,
                                    return_imag_part=return_imag_part)
         finally:
             ws.close()
-        first = last + 1
     k_all, t_all, ctrl = [], [], []
     for i in range(len(ks)):
         lam, tens = results[i]
@@ -187,4 +200,5 @@ def compute_spectrum_ebim(solver, billiard, k1, k2, dk=lambda k: 0.05 * k ** (-1
     return np.array([k_all[q] for q in keep]), np.array([t_all[q] for q in keep])
 
 
-__all__ = ["solve_krylov", "solve_full", "solve", "overlap_and_merge_ebim", "ebim_windows", "compute_spectrum_ebim"]
+__all__ = ["solve_krylov", "solve_full", "solve", "overlap_and_merge_ebim", "ebim_windows", "segment_plan",
+           "compute_spectrum_ebim"]

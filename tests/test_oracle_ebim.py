@@ -134,9 +134,9 @@ def test_refine_minima_host_logic(monkeypatch):
 
 def test_compute_spectrum_ebim_host_logic(monkeypatch):
     """compute_spectrum_ebim orchestration with the device step faked: one
-    discretisation per segment (built at the segment's last k, reused while
-    k_next <= k_first / 0.95), the Weyl nev per window, the merge and the final
-    [k1, k2] filter."""
+    discretisation per segment (the first built at ks[0], later ones at their
+    last k, reused while k_next <= k_first / 0.95), the Weyl nev per window,
+    the merge and the final [k1, k2] filter."""
     from qbgpu import ebim as QE
     built, solved = [], []
 
@@ -159,9 +159,31 @@ def test_compute_spectrum_ebim_host_logic(monkeypatch):
     ks, dks, nevs = QE.ebim_windows(b, 13.0, 15.0)
     out, tens = QE.compute_spectrum_ebim(S.DLP_kress(10.0, b), b, 13.0, 15.0)
     assert [s[2] for s in solved] == nevs and [s[0] for s in solved] == ks
-    # segments: each built at its last window's k; every window inside one
-    firsts = [ks[0]] + [ks[i + 1] for i, k in enumerate(ks[:-1]) if k in built]
-    assert built[-1] == ks[-1] and all(k <= f / 0.95 for f, k in zip(firsts, built))
+    # segments: the first discretised at ks[0] (pts0), later ones at their last window's k
+    plan = QE.segment_plan(ks, 0.95)
+    assert built == [kd for _, _, kd in plan]
+    assert built[0] == ks[0] and built[-1] == ks[-1]
     # roots 13.0, 13.5, 14.0, 14.5, 15.0 merged to one copy each, the best (lowest tension) kept
     assert list(out) == [13.0, 13.5, 14.0, 14.5, 15.0]
     assert tens[2] == min(abs(k - 14.0) for k in ks)
+
+
+def test_ebim_segment_plan_follows_reference_rule():
+    """segment_plan against a literal restatement of ebim.jl:1195-1226 in
+    1-based indices: seg_last grows while ks[seg_last+1] <= ks[seg_first] /
+    seg_reuse_frac; pts = seg_first == 1 ? pts0 (built at ks[1]) :
+    evaluate_points(ks[seg_last])."""
+    from qbgpu import ebim as QE
+    b = G.make_circle(1.0)
+    for k1, k2, frac in ((13.0, 15.0, 0.95), (40.0, 44.0, 0.99), (5.0, 9.0, 0.8)):
+        ks, _, _ = QE.ebim_windows(b, k1, k2)
+        ref = []
+        seg_first = 1
+        while seg_first <= len(ks):
+            seg_last = seg_first
+            while seg_last < len(ks) and ks[seg_last + 1 - 1] <= ks[seg_first - 1] / frac:
+                seg_last += 1
+            ref.append((seg_first - 1, seg_last - 1, ks[0] if seg_first == 1 else ks[seg_last - 1]))
+            seg_first = seg_last + 1
+        assert QE.segment_plan(ks, frac) == ref
+        assert len(ref) >= 2
