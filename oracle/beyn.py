@@ -6,6 +6,9 @@
 * lambda = eig(B)                                      beyn.jl:364-375
 * sigma_min = last singular value of A                  macros.jl:159-161
 * minima from the 2nd difference of log10(sigma)       sweepmethods.jl:193-217
+* beyn_disk: the same step with the contour nodes spread over worker
+  processes (each assembles, factors and solves its nodes; the moments are
+  summed in node order in the parent)
 """
 from __future__ import annotations
 
@@ -102,3 +105,75 @@ def get_eigenvalues(ks, tens, threshold=200.0):
         if g2[i] > g2[i - 1] and g2[i] > g2[i + 1] and g2[i] > threshold:
             out.append(x2[i])
     return np.array(out)
+
+
+# --------------------------------------------------------------------------
+# one disk with the nodes spread over processes
+# --------------------------------------------------------------------------
+def assemble_spec(spec, z):
+    """T(z) for a picklable operator description:
+    ("cfie", [nodes...])                  CFIE Kress, direct AMOS values
+    ("dlp", nodes)                        DLP Kress Fredholm matrix
+    ("dlp_reduced", nodes, orbits)        symmetry-reduced DLP Fredholm matrix
+    ("cfie_cheb", [nodes...], params)     CFIE through Chebyshev panels"""
+    from . import assembly as OA, chebyshev as OC
+    kind = spec[0]
+    if kind == "cfie":
+        return OA.cfie_matrix(spec[1], z)
+    if kind == "dlp":
+        return OA.dlp_fredholm(spec[1], z)
+    if kind == "dlp_reduced":
+        return OA.dlp_fredholm_reduced(spec[1], z, spec[2])
+    if kind == "cfie_cheb":
+        return OC.cfie_matrix(spec[1], z, spec[2])
+    raise ValueError(kind)
+
+
+def _node_solve(args):
+    spec, z, V = args
+    T = assemble_spec(spec, z)
+    f = sla.lu_factor(T, check_finite=False)
+    return sla.lu_solve(f, V, check_finite=False)
+
+
+def beyn_disk(spec, N, k0, R, nq, r, svd_tol, seed, regrow="extend", workers=1):
+    """construct_B_matrix and eig(B) (beyn.jl:257-322, 364-375) for one disk.
+
+    The probes are drawn from NumPy's PCG64 with ``seed``: V1 = probe(N, r);
+    when the rank saturates (rk == r, 2r < N) regrow="extend" appends a
+    second draw V2 = probe(N, r) to the solved block, regrow="fresh" draws a
+    new N x 2r block (the reference's policy). Both blocks are solved at
+    every node in one pass, so a regrowth costs no second factorisation.
+    Returns dict(lam=eigenvalues of B, rk, r, S)."""
+    import multiprocessing as mp
+    rng = np.random.default_rng(seed)
+    V1 = probe_matrix(N, r, rng)
+    V2 = probe_matrix(N, r, rng) if regrow == "extend" else probe_matrix(N, 2 * r, rng)
+    Vall = np.hstack([V1, V2])
+    zj, wj = contour(k0, R, nq)
+    jobs = [(spec, z, Vall) for z in zj]
+    if workers > 1:
+        with mp.get_context("spawn").Pool(workers) as pool:
+            Xs = pool.map(_node_solve, jobs, chunksize=1)
+    else:
+        Xs = [_node_solve(j) for j in jobs]
+    A0 = np.zeros(Vall.shape, complex)
+    A1 = np.zeros(Vall.shape, complex)
+    for X, z, w in zip(Xs, zj, wj):
+        A0 += w * X
+        A1 += (w * z) * X
+    M0, M1 = A0[:, :r], A1[:, :r]
+    S = np.linalg.svd(M0, compute_uv=False)
+    rk = int(np.count_nonzero(S >= svd_tol))
+    rused = r
+    if rk == r and 2 * r < N:
+        M0, M1 = (A0, A1) if regrow == "extend" else (A0[:, r:], A1[:, r:])
+        rused = 2 * r
+    U, S, Wh = np.linalg.svd(M0, full_matrices=False)
+    rk = int(np.count_nonzero(S >= svd_tol))
+    if rk == 0:
+        return dict(lam=np.zeros(0, complex), rk=0, r=rused, S=S)
+    Uk = U[:, :rk]
+    Wk = Wh.conj().T[:, :rk]
+    B = Uk.conj().T @ ((M1 @ Wk) / S[:rk][None, :])
+    return dict(lam=np.linalg.eigvals(B), rk=rk, r=rused, S=S)

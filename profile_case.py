@@ -1,9 +1,9 @@
 """Run one named workload once, for profilers (ncu) and quick checks.
 
-    python quantumbilliards.jl_gb300/profile_case.py beyn --nq 8 --form mixed
-    python quantumbilliards.jl_gb300/profile_case.py assemble --nq 8
-    python quantumbilliards.jl_gb300/profile_case.py disks --n 4096 --ndisk 32 --nq 48 --L 96
-    python quantumbilliards.jl_gb300/profile_case.py large --n 16384 --nq 48 --L 128 --chunk 8
+    python profile_case.py beyn --nq 8 --form mixed
+    python profile_case.py assemble --nq 8
+    python profile_case.py disks --n 4096 --ndisk 32 --nq 48 --L 96
+    python profile_case.py large --n 16384 --nq 48 --L 128 --chunk 8
 
 Cases use the bench workload (CFIE Kress, star r = 1 + 0.2 cos 5 theta,
 N = 2048, k0 = 200, R = 0.5, L = 64) with an adjustable number of contour nodes
@@ -20,6 +20,7 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE))
+sys.path.insert(0, str(HERE / "quantumbilliards.jl_gb300"))
 
 import numpy as np  # noqa: E402
 

@@ -238,12 +238,14 @@ def make_full_stadium(half_width: float = 1.0, radius: float = 1.0) -> Billiard:
 
 
 def make_rectangle(width: float = 1.0, height: float = 1.0) -> Billiard:
-    """Counter-clockwise rectangle [0, w] x [0, h] of four line segments (four
-    corners); Dirichlet eigenvalues k^2 = pi^2 (m^2/w^2 + n^2/h^2)."""
-    w, h = float(width), float(height)
-    pts = [(0.0, 0.0), (w, 0.0), (w, h), (0.0, h)]
-    segs = [LineSegment(pts[j], pts[(j + 1) % 4]) for j in range(4)]
-    return Billiard("rectangle", [segs], w * h, ())
+    """make_full_rectangle (rectangle.jl:72-95): the rectangle centred at the
+    origin as eight counter-clockwise line segments starting at the middle of
+    the right side (four true corners, four straight joins); Dirichlet
+    eigenvalues k^2 = pi^2 (m^2/w^2 + n^2/h^2)."""
+    hw, hh = 0.5 * float(width), 0.5 * float(height)
+    pts = [(hw, 0.0), (hw, hh), (0.0, hh), (-hw, hh), (-hw, 0.0), (-hw, -hh), (0.0, -hh), (hw, -hh)]
+    segs = [LineSegment(pts[j], pts[(j + 1) % 8]) for j in range(8)]
+    return Billiard("rectangle", [segs], float(width) * float(height), ())
 
 
 def make_full_ellipse_mushroom(stem_width=0.6, stem_height=1.0, cap_height=0.8, cap_width=1.2) -> Billiard:

@@ -2,7 +2,7 @@
 requests on mixed geometries and sizes through the request server, with
 p50/p99 latency (arrival -> result on the host) and throughput.
 
-    python quantumbilliards.jl_gb300/serve_workload.py --requests 2000 --rate 20 --nmin 1024 --nmax 8192
+    python serve_workload.py --requests 2000 --rate 20 --nmin 1024 --nmax 8192
 
 Seeded synthetic stream: geometry uniform over {unit circle with an
 off-centre hole of radius 0.2 (CFIE), full stadium (DLP, smooth composite),
@@ -27,6 +27,7 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE))
+sys.path.insert(0, str(HERE / "quantumbilliards.jl_gb300"))
 
 import numpy as np  # noqa: E402
 

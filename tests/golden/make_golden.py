@@ -13,6 +13,21 @@ c1_sweep.json (``python tests/golden/make_golden.py c1``, about 80 s): the
 oracle's sigma_min sweep of the unit circle, DLP Kress with
 pts_scaling_factor 12.2 (N = 512 at k = 42), 200 k in [40, 42] -- the smallest
 singular value of the FP64 Fredholm matrix at each k.
+
+c2_beyn.json (``... c2``, a few minutes on 8 cores): the oracle's Beyn disk
+of the star r = 1 + 0.2 cos 5 theta, CFIE Kress, N = 2048 (b chosen at
+k = 200), k0 = 200, R = 0.5, 48 nodes, 64 probes drawn from PCG64 seed 2 and
+extended by a second draw of 64 when the rank saturates, svd_tol 1e-12; direct
+AMOS kernel values. All eigenvalues of B, the rank and the singular values.
+
+c3_beyn.json (``... c3``): one disk of the desymmetrised stadium, DLP Kress
+global corners on the full stadium (half width 1, radius 1) with the XY
+reflection of parities (-1, -1), N = 4096 (b chosen at k = 332), m = 1024
+reduced unknowns, k0 = 300.5, R = 0.5, 48 nodes, 96 probes from PCG64 seed 3
+(extended by 96 when the rank saturates), svd_tol 1e-10; direct AMOS values.
+
+Everything here is computed by the oracle alone (oracle/geometry.py builds the
+nodes); nothing imports the product.
 """
 import json
 import sys
@@ -52,23 +67,61 @@ def circle_eigs(lo, hi):
     return sorted(out, key=lambda r: r["k"])
 
 
-def c1_sweep():
+def _oracle_path():
     root = HERE.parents[1]
-    sys.path.insert(0, str(root))
-    sys.path.insert(0, str(root / "quantumbilliards.jl_gb300"))
-    from oracle import assembly as OA, beyn as OB
-    from qbgpu import geometry as G, solvers as S
-    b = G.make_circle(1.0)
-    sol = S.DLP_kress(12.2, b)
+    if str(root) not in sys.path:
+        sys.path.insert(0, str(root))
+
+
+def c1_sweep():
+    _oracle_path()
+    from oracle import assembly as OA, beyn as OB, geometry as OG
     ks = np.linspace(40.0, 42.0, 200)
-    pts = S.evaluate_points(sol, b, float(ks.max()))
+    pts = OG.evaluate_points("dlp_kress", OG.circle(1.0), float(ks.max()), 12.2)
     sig = [float(OB.sigma_min(OA.dlp_fredholm(pts, k))) for k in ks]
     return {"N": int(pts.n), "pts_scaling_factor": 12.2, "ks": ks.tolist(), "sigma": sig}
 
 
-if __name__ == "__main__" and sys.argv[1:] == ["c1"]:
-    (HERE / "c1_sweep.json").write_text(json.dumps(c1_sweep()))
-    print("written")
+def _disk_record(res, cfg):
+    lam = res["lam"]
+    return dict(cfg, rk=int(res["rk"]), r_used=int(res["r"]), eigenvalues=[[float(x.real), float(x.imag)] for x in lam],
+                singular_values=[float(x) for x in res["S"]])
+
+
+def c2_beyn(workers=8):
+    _oracle_path()
+    import os
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    from oracle import beyn as OB, geometry as OG
+    pts, b = OG.points_with_n("cfie_kress", OG.star(0.2, 5), 2048, 200.0)
+    cfg = dict(workload="beyn_cfie_kress_star_N2048_k0_200_R0.5_nq48_L64", N=int(pts[0].n), pts_scaling_factor=b,
+               k0=200.0, R=0.5, nq=48, L=64, seed=2, regrow="extend", svd_tol=1e-12, kernel="direct AMOS")
+    res = OB.beyn_disk(("cfie", pts), pts[0].n, 200.0 + 0j, 0.5, 48, 64, 1e-12, 2, "extend", workers)
+    return _disk_record(res, cfg)
+
+
+def c3_beyn(workers=8):
+    _oracle_path()
+    import os
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    from oracle import assembly as OA, beyn as OB, geometry as OG
+    sym = ("xy", -1, -1)
+    p, b = OG.points_with_n("dlp_kress_global_corners", OG.full_stadium(1.0, 1.0), 4096, 332.0, symmetry=sym)
+    orb = OA.periodic_symmetry_index_orbits(p.n, sym)
+    m = len(orb[0])
+    cfg = dict(workload="beyn_dlp_reduced_stadium_N4096_m1024_k0_300.5_R0.5_nq48_L96", N=int(p.n), m=m,
+               pts_scaling_factor=b, k0=300.5, R=0.5, nq=48, L=96, seed=3, regrow="extend", svd_tol=1e-10,
+               symmetry="XYReflection(-1, -1)", kernel="direct AMOS")
+    res = OB.beyn_disk(("dlp_reduced", p, orb), m, 300.5 + 0j, 0.5, 48, 96, 1e-10, 3, "extend", workers)
+    return _disk_record(res, cfg)
+
+
+if __name__ == "__main__" and sys.argv[1:2] in (["c1"], ["c2"], ["c3"]):
+    which = sys.argv[1]
+    fn = {"c1": c1_sweep, "c2": c2_beyn, "c3": c3_beyn}[which]
+    out = {"c1": "c1_sweep.json", "c2": "c2_beyn.json", "c3": "c3_beyn.json"}[which]
+    (HERE / out).write_text(json.dumps(fn()))
+    print("written", out)
 elif __name__ == "__main__":
     (HERE / "bessel_mpmath.json").write_text(json.dumps({"dps": 40, "values": bessel_rows()}, indent=1))
     (HERE / "circle_eigs.json").write_text(json.dumps({"ranges": {"40_42": circle_eigs(40.0, 42.0),
