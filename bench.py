@@ -4,12 +4,24 @@ Workload (the headline metric's configuration): CFIE_kress on the star
 r(theta) = 1 + 0.2 cos(5 theta), N = 2048 nodes, one disk k0 = 200, R = 0.5,
 nq = 48 trapezoid contour nodes, L = 64 seeded complex Gaussian probes (std 1),
 svd_tol = 1e-12, the reference's single r -> 2r regrowth when the rank
-saturates. A step = one full Beyn disk: assembly of the 48 T(z_j), batched
-LU, T^-1 V solves (+ regrowth solves), moments, host SVD/eig.
+saturates. Chebyshev panels are tuned once per run to 1e-13 absolute error
+(the tolerance compute_spectrum_beyn gives chebyshev_params), by the library's
+cost-aware tuner; the tuning time is reported as plan_s. A step = one full Beyn disk: assembly
+of the 48 T(z_j), batched LU, T^-1 V solves (+ regrowth solves), moments,
+host SVD/eig.
 
-metric: eigenvalues/s of the mixed form (FP32 assembly/LU + compensated
-refinement) counting eigenvalues inside the disk that agree with the plain
-FP64 GPU path to <= 1e-10 relative; the plain FP64 path is timed beside it.
+metric: eigenvalues/s of the mixed form (FP32 LU + FP64-accurate refinement)
+counting eigenvalues inside the disk that agree with the oracle's FP64
+eigenvalues (tests/golden/c2_beyn.json: direct AMOS kernel values, LAPACK,
+same probes and regrowth) to <= 1e-10 relative; every eigenvalue's error against the
+oracle is reported, and the plain FP64 path is timed beside it.
+
+cpu_baseline and --impl reference: the reference's CPU algorithm restated on
+the host cores (oracle/cpu.py: Chebyshev tables from AMOS, C assembly threaded
+over columns, LAPACK LU and solves, the fresh 2r regrowth block), one contour
+node per step; the eigenvalues per disk come from one untimed full disk of
+the same code, matched to the oracle fixture of the reference's regrowth
+policy (tests/golden/c2_beyn_fresh.json).
 
 --workload ebim prints a second line for the EBIM eigen step on the same
 geometry (k = 200, dk = 0.05, nev = 5): steps/s of device assembly + eigen
@@ -38,6 +50,9 @@ N_NODES, K0, RADIUS, NQ, L_PROBES, SVD_TOL = 2048, 200.0, 0.5, 48, 64, 1e-12
 TOL_EIG = 1e-10
 IMAG_TOL = 1e-6
 SEED = 2
+CHEB_TOL = 1e-13
+GOLDEN = ROOT / "tests" / "golden" / "c2_beyn.json"
+GOLDEN_FRESH = ROOT / "tests" / "golden" / "c2_beyn_fresh.json"
 
 
 def _peaks():
@@ -98,7 +113,7 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-METRIC = "eigenvalues/s at <=1e-10 rel err (mixed FP32+refinement vs plain FP64), Beyn CFIE Kress star"
+METRIC = "eigenvalues/s at <=1e-10 rel err vs the FP64 oracle (mixed FP32 LU + FP64-accurate refinement), Beyn CFIE Kress star"
 
 
 def workload_config():
@@ -125,12 +140,29 @@ def match(lam, ref):
     return np.array([np.min(np.abs(ref - l)) / abs(l) for l in lam])
 
 
-def run_step(qb, sol, pts, ws, mixed, rng_seed=SEED, with_geometry=False):
+def oracle_eigenvalues(regrow="extend"):
+    """All eigenvalues of B from the oracle's FP64 disk with the same probes and
+    regrowth policy ("extend": the library's; "fresh": the reference's)."""
+    g = json.loads((GOLDEN if regrow == "extend" else GOLDEN_FRESH).read_text())
+    return np.array([complex(*x) for x in g["eigenvalues"]])
+
+
+def accuracy(lam, oracle_all):
+    """Errors of the selected eigenvalues against the oracle's, and the oracle's
+    selected eigenvalues that found no partner within TOL_EIG."""
+    sel = select(lam)
+    e = match(sel, oracle_all)
+    ref = select(oracle_all)
+    missing = int(sum(1 for x in ref if len(sel) == 0 or np.min(np.abs(sel - x)) / abs(x) > TOL_EIG))
+    return sel, e, missing
+
+
+def run_step(qb, sol, pts, ws, mixed, rng_seed=SEED, with_geometry=False, cheb=None):
     t0 = time.perf_counter()
     if with_geometry:
         ws = qb.Workspace(sol, pts)
     lam, info = qb.solve(sol, pts, K0 + 0j, RADIUS, nq=NQ, r=L_PROBES, svd_tol=SVD_TOL,
-                         rng=np.random.default_rng(rng_seed), mixed=mixed, ws=ws, return_info=True)
+                         rng=np.random.default_rng(rng_seed), mixed=mixed, ws=ws, return_info=True, cheb=cheb)
     dt = time.perf_counter() - t0
     if with_geometry:
         ws.close()
@@ -164,20 +196,58 @@ def replica_reduce(world, t_region, eig_count):
     return float(t.item()), float(c.item())
 
 
-def cpu_baseline(qb, sol, pts, nsample=1):
-    """Oracle (NumPy/SciPy FP64 restatement) on a bounded sample: assembly +
-    LU + solves for `nsample` contour nodes, extrapolated to the 48-node disk."""
-    from oracle import assembly as OA
-    import scipy.linalg as sla
-    zj = K0 + RADIUS * np.exp(2j * math.pi * np.arange(NQ) / NQ)
-    V = qb.probe_matrix(pts[0].n, L_PROBES, np.random.default_rng(SEED))
-    t0 = time.perf_counter()
-    for z in zj[:nsample]:
-        T = OA.cfie_matrix(pts, z)
-        f = sla.lu_factor(T, check_finite=False)
-        sla.lu_solve(f, V, check_finite=False)
-    dt = (time.perf_counter() - t0) / nsample * NQ
-    return dt
+def cpu_disk(steps, warmup, threads=None):
+    """The reference's CPU Beyn path restated on the host cores (oracle/cpu.py):
+    the panels tuned once (chebyshev_params rule, tol 1e-13; plan_s), one
+    untimed full disk of the same code for the eigenvalue count (eigenvalues
+    inside the disk within TOL_EIG of the oracle fixture), then `steps` timed
+    steps of one contour node each (table fit, assembly, LU, solves of the r
+    and the fresh 2r probe blocks). The disk time is nq node steps plus the
+    measured moments/SVD/B/eig time of the full disk."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import beyn as OB, cpu as OCPU, geometry as OG
+    threads = threads or os.cpu_count()
+    OCPU.build()
+    pts, _ = OG.points_with_n("cfie_kress", OG.star(0.2, 5), N_NODES, K0)
+    g = OCPU.Geometry(pts)
+    zj, _ = OB.contour(K0 + 0j, RADIUS, NQ)
+    with ThreadPoolExecutor(threads) as pool:
+        t0 = time.perf_counter()
+        prm = OCPU.chebyshev_params(g, zj, tol=CHEB_TOL, pool=pool)
+        plan_s = time.perf_counter() - t0
+    cb = OCPU.BeynCPU(pts, K0, RADIUS, NQ, L_PROBES, SVD_TOL, SEED, prm[:4], threads)
+    try:
+        t0 = time.perf_counter()
+        for j in range(NQ):
+            cb.node(j)
+        t1 = time.perf_counter()
+        lam, rk, r_used = cb.finish()
+        t2 = time.perf_counter()
+        sel, e, missing = accuracy(lam, oracle_eigenvalues("fresh"))
+        n_eig = int(np.count_nonzero(e <= TOL_EIG))
+        for s in range(warmup):
+            cb.node(s % NQ)
+        times = []
+        for s in range(steps):
+            ts = time.perf_counter()
+            cb.node((warmup + s) % NQ)
+            times.append(time.perf_counter() - ts)
+    finally:
+        cb.close()
+    t_node = float(np.mean(times))
+    t_disk = NQ * t_node + (t2 - t1)
+    return dict(value=n_eig / t_disk, n_eig=n_eig, t_node=t_node, t_disk=t_disk, full_disk_s=t2 - t0,
+                finish_s=t2 - t1, plan_s=plan_s, cheb=[int(x) for x in prm[:4]], cores=threads, rk=rk, r=r_used,
+                max_rel_err_vs_oracle=float(e.max()) if len(e) else None, missing=missing, steps=steps,
+                region_s=float(np.sum(times)))
+
+
+def cpu_sample_text(c):
+    return (f"one contour node per timed step ({c['steps']} steps, {c['region_s']:.1f} s): Chebyshev tables "
+            f"{c['cheb']} fitted to AMOS values, C assembly on {c['cores']} threads, LAPACK LU and solves of "
+            f"{L_PROBES} + {2 * L_PROBES} probes; disk = {NQ} node steps + moments/SVD/eig "
+            f"({c['finish_s']:.2f} s); {c['n_eig']} eigenvalues within 1e-10 of the oracle from one untimed full disk "
+            f"({c['full_disk_s']:.1f} s); panel tuning {c['plan_s']:.1f} s not counted")
 
 
 def main():
@@ -188,6 +258,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--cpu-steps", type=int, default=4, help="timed node steps of the cpu_baseline leg")
     ap.add_argument("--workload", default="beyn", choices=["beyn", "ebim"],
                     help="beyn: the headline Beyn disk (default); ebim: the EBIM eigen step at one k")
     args = ap.parse_args()
@@ -214,31 +285,42 @@ def main():
 
     b, sol, pts = star_workspace(qb)
     ws = qb.Workspace(sol, pts)
+    oracle_all = oracle_eigenvalues()
+    oracle_sel = select(oracle_all)
 
-    # FP64 reference eigenvalues for the accuracy filter (plain GPU path, validated against the oracle in tests)
-    lam64, info64, t_plain_first = run_step(qb, sol, pts, ws, mixed=False)
-    ref = select(lam64)
+    # panels tuned once to CHEB_TOL on the device: of the degrees 5..15, the panel layout of the lowest
+    # table-plus-series cost whose H0, H1, J0, J1 all stay within CHEB_TOL (the reference's tuner grows
+    # its default layout to the same tolerance; both reproduce the oracle's eigenvalues to ~2e-13)
+    zref = K0 + RADIUS * np.exp(2j * math.pi * np.arange(NQ) / NQ)
+    t0 = time.perf_counter()
+    cheb = tuple(int(x) for x in qb.chebyshev_params_min_cost(sol, pts, zref, ws=ws, tol=CHEB_TOL)[:4])
+    plan_s = time.perf_counter() - t0
+
+    # plain FP64 form (the drop-in), timed beside the mixed one
+    lam64, info64, _ = run_step(qb, sol, pts, ws, mixed=False, cheb=cheb)
     plain_times = []
-    for _ in range(max(0, args.plain_steps)):
-        _, _, dt = run_step(qb, sol, pts, ws, mixed=False)
+    for _ in range(max(1, args.plain_steps)):
+        lam64, info64, dt = run_step(qb, sol, pts, ws, mixed=False, cheb=cheb)
         plain_times.append(dt)
-    t_plain = float(np.median(plain_times)) if plain_times else t_plain_first
+    t_plain = float(np.median(plain_times))
+    _, e64, miss64 = accuracy(lam64, oracle_all)
+    plain_ok = int(np.count_nonzero(e64 <= TOL_EIG))
 
     for _ in range(args.warmup):
-        run_step(qb, sol, pts, ws, mixed=True)
+        run_step(qb, sol, pts, ws, mixed=True, cheb=cheb)
     _lib.load().qbg_device_sync()
     replica_barrier(world)
     clk = ClockSampler()
     clk.start()
-    times, counts, errs, stats = [], [], [], []
+    times, counts, errs, stats, missing = [], [], [], [], []
     launches0 = qb.launch_count()
     t_region0 = time.perf_counter()
     for s in range(args.steps):
-        lam, info, dt = run_step(qb, sol, pts, ws, mixed=True)
-        sel = select(lam)
-        e = match(sel, ref)
+        lam, info, dt = run_step(qb, sol, pts, ws, mixed=True, cheb=cheb)
+        sel, e, miss = accuracy(lam, oracle_all)
         counts.append(int(np.count_nonzero(e <= TOL_EIG)))
-        errs.append(float(e.max()) if len(e) else float("nan"))
+        errs.append(e)
+        missing.append(miss)
         times.append(dt)
         stats.append(info["stats"])
     _lib.load().qbg_device_sync()
@@ -249,51 +331,43 @@ def main():
     # replicas: every rank ran the same disk on its own GPU; the job's time is the slowest rank's
     t_region_max, eig_total = replica_reduce(world, t_region, float(sum(counts)))
     # end to end through the public API including the geometry upload
-    e2e_times = []
+    e2e_times, e2e_counts = [], []
     for _ in range(max(1, min(args.steps, 3))):
-        _, _, dt = run_step(qb, sol, pts, None, mixed=True, with_geometry=True)
+        lam_e, _, dt = run_step(qb, sol, pts, None, mixed=True, with_geometry=True, cheb=cheb)
         e2e_times.append(dt)
+        e2e_counts.append(int(np.count_nonzero(accuracy(lam_e, oracle_all)[1] <= TOL_EIG)))
     # FP32 form (FP32 kernel values): reported beside, with its own accuracy
-    lam32, info32, t32 = run_step(qb, sol, pts, ws, mixed="fp32")
-    lam32, info32, t32 = run_step(qb, sol, pts, ws, mixed="fp32")
-    e32 = match(select(lam32), ref)
+    run_step(qb, sol, pts, ws, mixed="fp32", cheb=cheb)
+    lam32, info32, t32 = run_step(qb, sol, pts, ws, mixed="fp32", cheb=cheb)
+    _, e32, _ = accuracy(lam32, oracle_all)
     fp32_form = {"ms_per_step": t32 * 1e3, "eigenvalues_inside": int(len(e32)),
                  "eigenvalues_le_1e-10": int(np.count_nonzero(e32 <= TOL_EIG)),
-                 "max_rel_err_vs_fp64": float(e32.max()) if len(e32) else None}
+                 "max_rel_err_vs_oracle": float(e32.max()) if len(e32) else None}
 
     t_step = t_region_max / args.steps
     n_eig = float(np.mean(counts))
     value = eig_total / t_region_max  # whole job: eigenvalues of all replicas / slowest rank's time
-    plain_eigs = len(ref)
-    st0 = stats[-1][0]
     r_final = info["r"]
     N = ws.dim
     h2d = 8 * 8 * N + 16 * N * (L_PROBES + (r_final if r_final != L_PROBES else 0))
     d2h = 2 * 16 * N * (L_PROBES + (r_final if r_final != L_PROBES else 0))
     hbm, bf16, peak_kind = _peaks()
-    # roofline kernel: the tensor-core refinement residual R = V - (hi + lo) X over
-    # all nodes (k_resid_tc). Algorithmic work per launch = one complex GEMM,
-    # 8 N^2 L nq real flops; the kernel issues 28 digit-pair bf16 products of
-    # that real-mapped GEMM (224 N^2 Lp nq flops, Lp = L rounded up to 32).
-    res_ms, res_n = 0.0, 0
-    for srun in stats:
-        for s in srun:
-            res_ms += s["ms_residual"]
-            res_n += s["n_residual"]
-    res_launch_ms = res_ms / max(res_n, 1)
-    res_flops = 8.0 * N * N * L_PROBES * NQ
-    lp = ((L_PROBES + 31) // 32) * 32
-    res_issued = 224.0 * N * N * lp * NQ
-    achieved = res_flops / (res_launch_ms * 1e-3) / 1e12
-    issued_tflops = res_issued / (res_launch_ms * 1e-3) / 1e12
-    # DRAM traffic per launch: ncu capture of the same kernel at nq = 8, L = 64
-    # (1009.98 MB read + 16.03 MB written), scaled by the contour nodes (48 / 8);
-    # the algorithmic bytes (digit planes of T and X, V, R) are 1.03 GB at nq = 8
-    res_traffic = (1009.98e6 + 16.03e6) * (NQ / 8.0)
-    res_alg_bytes = (7 * N * 2 * N * 2 + 7 * 2 * lp * 2 * N * 2 + 2 * 16 * N * L_PROBES) * NQ
-    lu_flops = NQ * (8.0 / 3.0) * N ** 3
+    st_last = stats[-1]
     ms_factor = float(np.mean([s[0]["ms_factor"] for s in stats]))
+    ms_assemble = float(np.mean([s[0]["ms_assemble"] for s in stats]))
+    # dominant work of the step: the FP32 LU of the 48 operators (panels on CUDA cores,
+    # trailing updates on tcgen05 with 3xTF32), timed by CUDA events around the factor phase
+    lu_flops = NQ * (8.0 / 3.0) * N ** 3
     lu_achieved = lu_flops / (ms_factor * 1e-3) / 1e12
+    # tensor-core residual: HBM-bound (digit planes of T and X, V, R per launch)
+    res_ms = sum(s["ms_residual"] for run in stats for s in run)
+    res_n = sum(s["n_residual"] for run in stats for s in run)
+    res_launch_ms = res_ms / max(res_n, 1)
+    lp = ((L_PROBES + 31) // 32) * 32
+    res_alg_bytes = (7 * N * 2 * N * 2 + 7 * 2 * lp * 2 * N * 2 + 2 * 16 * N * L_PROBES) * NQ
+    # assembly: HBM floor of the written operators (complex64 hi + lo = 16 B per entry)
+    asm_bytes = 16.0 * N * N * NQ
+    e_last = errs[-1]
     line = {
         "metric": METRIC,
         "value": value,
@@ -307,34 +381,46 @@ def main():
         "vs_baseline": None,
         "dtype": "c64+c128",
         "data": "synthetic",
-        "config": dict(workload_config(), r_final=r_final,
+        "config": dict(workload_config(), r_final=r_final, cheb_panels=list(cheb), cheb_tol=CHEB_TOL,
                        timing="wall clock of the synchronous API calls between device synchronizations (the step "
                               "ends with the host SVD and eigvals); device phases in phases_ms are CUDA events"),
-        "plain_fp64": {"value": plain_eigs / t_plain, "ms_per_step": t_plain * 1e3, "eigenvalues": plain_eigs},
-        "speedup_vs_plain": ((n_eig / t_step) / (plain_eigs / t_plain)) if plain_eigs else None,
+        "plan_s": plan_s,
         "eigenvalues_per_step": n_eig,
-        "max_rel_err_vs_fp64": float(np.max(errs)),
-        "phases_ms": {"assemble": st0["ms_assemble"], "factor": st0["ms_factor"],
-                      "solve_refine": sum(s["ms_solve"] for s in stats[-1])},
+        "oracle_eigenvalues_in_disk": int(len(oracle_sel)),
+        "oracle_eigenvalues_missed": int(max(missing)),
+        "max_rel_err_vs_oracle": float(max(float(e.max()) for e in errs)),
+        "eig_rel_err_vs_oracle": [float("%.3g" % x) for x in e_last],
+        "plain_fp64": {"value": plain_ok / t_plain, "ms_per_step": t_plain * 1e3, "eigenvalues_le_1e-10": plain_ok,
+                       "eigenvalues_le_1e-12": int(np.count_nonzero(e64 <= 1e-12)),
+                       "max_rel_err_vs_oracle": float(e64.max()) if len(e64) else None,
+                       "oracle_eigenvalues_missed": miss64},
+        "speedup_vs_plain": (n_eig / t_step) / (plain_ok / t_plain) if plain_ok else None,
+        "phases_ms": {"assemble": ms_assemble, "factor": ms_factor,
+                      "solve_refine": sum(s["ms_solve"] for s in st_last)},
         "host_ms": {k: float("%.3g" % v) for k, v in info["host_ms"].items()},
-        "refine_sweeps": [s["refine_sweeps"] for s in stats[-1]],
-        "refine_history": [[float("%.3g" % v) for v in s["refine_history"]] for s in stats[-1]],
+        "refine_sweeps": [s["refine_sweeps"] for s in st_last],
+        "refine_history": [[float("%.3g" % v) for v in s["refine_history"]] for s in st_last],
         "plain_phases_ms": {"assemble": info64["stats"][0]["ms_assemble"], "factor": info64["stats"][0]["ms_factor"],
                             "solve": sum(s["ms_solve"] for s in info64["stats"])},
         "fp32_form": fp32_form,
-        "e2e": {"value": n_eig / float(np.mean(e2e_times)), "unit": "eigenvalues/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
-                     "frac": achieved / bf16, "traffic": res_traffic, "algorithmic_bytes": res_alg_bytes,
-                     "kernel": "k_resid_tc (exact 7-bit digit products on tcgen05, bf16 -> FP32 TMEM)",
-                     "peak_kind": peak_kind, "launch_ms": res_launch_ms,
-                     "launches_per_step": res_n / max(len(stats), 1),
-                     "issued_tflops": issued_tflops, "frac_issued": issued_tflops / bf16,
-                     "note": "achieved counts the complex GEMM's 8 N^2 L flops; the tensor pipe executes 28 "
-                             "digit-pair products of it, whose rate is issued_tflops (frac_issued of the "
-                             "measured bf16 peak)"},
-        "lu_phase": {"achieved_tflops": lu_achieved, "ms": ms_factor, "flops": lu_flops,
-                     "engine": "FP32 panels on CUDA cores; trailing updates and solves on tcgen05 (3xTF32)"},
+        "e2e": {"value": float(np.mean(e2e_counts)) / float(np.mean(e2e_times)), "unit": "eigenvalues/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "tensor", "achieved": lu_achieved, "peak": bf16, "unit": "TFLOP/s",
+                     "frac": lu_achieved / bf16, "traffic": None,
+                     "kernel": "LU factor phase of the 48 operators: k_getrf_panel_smem (FP32 panels, CUDA cores) + "
+                               "k_tc_cgemm / k_tc_cgemm_pk trailing updates (tcgen05, 3xTF32)",
+                     "peak_kind": peak_kind + " bf16 dense (the TF32 tensor rate is half of it and 3xTF32 issues three "
+                                              "MMAs per product)",
+                     "algorithmic_flops": lu_flops, "ms": ms_factor},
+        "phase_rooflines": {
+            "assembly": {"bound": "fp32 alu / hbm", "ms": ms_assemble, "bytes_written": asm_bytes,
+                         "achieved_gbs": asm_bytes / (ms_assemble * 1e-3) / 1e9, "peak_gbs": hbm,
+                         "frac_hbm": asm_bytes / (ms_assemble * 1e-3) / 1e9 / hbm},
+            "k_resid_tc": {"bound": "hbm", "launch_ms": res_launch_ms, "launches_per_step": res_n / max(len(stats), 1),
+                           "algorithmic_bytes": res_alg_bytes,
+                           "achieved_gbs": res_alg_bytes / (res_launch_ms * 1e-3) / 1e9 if res_n else None,
+                           "peak_gbs": hbm,
+                           "frac": res_alg_bytes / (res_launch_ms * 1e-3) / 1e9 / hbm if res_n else None}},
         "clocks": clocks,
         "gpu_launches": gpu_launches,
         "gpu_launches_per_step": gpu_launches / max(args.steps, 1),
@@ -342,10 +428,9 @@ def main():
     if world > 1:
         line["config"]["parallelism"] = f"replicas{world}"
     if not args.no_cpu_baseline and rank == 0 and world == 1:
-        t_cpu = cpu_baseline(qb, sol, pts, 1)
-        line["cpu_baseline"] = {"value": plain_eigs / t_cpu, "unit": "eigenvalues/s", "cores": os.cpu_count(),
-                                "kind": "port",
-                                "sample": "oracle assembly+LU+solve of 1 of 48 contour nodes, extrapolated x48"}
+        c = cpu_disk(args.cpu_steps, 1)
+        line["cpu_baseline"] = {"value": c["value"], "unit": "eigenvalues/s", "cores": c["cores"], "kind": "port",
+                                "sample": cpu_sample_text(c), "max_rel_err_vs_oracle": c["max_rel_err_vs_oracle"]}
     if rank == 0:
         print(json.dumps(line))
 
@@ -410,11 +495,8 @@ def ebim_workload(args):
 def reference_arm_ebim(args):
     """--impl reference --workload ebim: the oracle's solve_krylov on its own
     FP64 assembly of the same workload, one eigen step per timed step."""
-    import qbgpu.geometry as G  # host-only modules (no GPU work)
-    from qbgpu import solvers as S
-    from oracle import assembly as OA, ebim as OE
-    b = G.make_star(0.2, 5)
-    pts, sol = S.points_with_n(S.CFIE_kress(1.0, b), b, N_NODES, K0)
+    from oracle import assembly as OA, ebim as OE, geometry as OG
+    pts, _ = OG.points_with_n("cfie_kress", OG.star(0.2, 5), N_NODES, K0)
     A, dA, ddA = OA.cfie_matrix_derivs(pts, EBIM_K)
     for _ in range(min(args.warmup, 1)):
         OE.solve_krylov(A, dA, ddA, EBIM_K, EBIM_DK, nev=EBIM_NEV)
@@ -434,38 +516,21 @@ def reference_arm_ebim(args):
 
 
 def reference_arm(args):
-    """--impl reference: the oracle's FP64 CPU restatement on the host cores."""
-    import qbgpu.geometry as G  # host-only modules (no GPU work)
-    from qbgpu import solvers as S
-    b = G.make_star(0.2, 5)
-    pts, sol = S.points_with_n(S.CFIE_kress(1.0, b), b, N_NODES, K0)
-    from oracle import assembly as OA
-    import scipy.linalg as sla
-    zj = K0 + RADIUS * np.exp(2j * math.pi * np.arange(NQ) / NQ)
-    rng = np.random.default_rng(SEED)
-    V = (rng.standard_normal((pts[0].n, L_PROBES)) + 1j * rng.standard_normal((pts[0].n, L_PROBES))) * math.sqrt(.5)
-    times = []
-    for s in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        z = zj[s % NQ]
-        T = OA.cfie_matrix(pts, z)
-        f = sla.lu_factor(T, check_finite=False)
-        sla.lu_solve(f, V, check_finite=False)
-        if s >= args.warmup:
-            times.append((time.perf_counter() - t0) * NQ)
-    t = float(np.mean(times))
-    eig_per_disk = 100.0  # Weyl estimate for the disk (area*k/2pi*2R - L/4pi*2R)
-    val = eig_per_disk / t
-    print(json.dumps({"impl": "reference", "metric": METRIC, "value": val,
-                      "unit": "eigenvalues/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-                      "ms_per_step": t * 1e3, "higher_is_better": True, "dtype": "c128", "data": "synthetic",
-                      "config": dict(workload_config(),
-                                     timing="host wall clock of one contour node's FP64 CFIE assembly, LU and "
-                                            "L-column solve, times 48 nodes; eigenvalues per disk = 100, the "
-                                            "Weyl estimate"),
-                      "cpu_baseline": {"value": val, "unit": "eigenvalues/s", "cores": os.cpu_count(), "kind": "port",
-                                       "sample": "one contour node per step, extrapolated x48"},
-                      "e2e": {"value": val, "unit": "eigenvalues/s", "h2d_bytes_per_step": 0,
+    """--impl reference: the reference's CPU Beyn path restated on the host
+    cores (oracle/cpu.py, see cpu_disk), one contour node per timed step."""
+    c = cpu_disk(args.steps, args.warmup)
+    print(json.dumps({"impl": "reference", "metric": METRIC, "value": c["value"], "unit": "eigenvalues/s",
+                      "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": c["t_node"] * 1e3,
+                      "higher_is_better": True, "dtype": "c128", "data": "synthetic",
+                      "config": dict(workload_config(), cheb_panels=c["cheb"], cheb_tol=CHEB_TOL,
+                                     timing="host wall clock of each node step; value = eigenvalues per disk / "
+                                            "(48 node steps + the disk's moments, SVD and eig)"),
+                      "disk_s": c["t_disk"], "full_disk_s": c["full_disk_s"], "plan_s": c["plan_s"],
+                      "eigenvalues_per_disk": c["n_eig"], "max_rel_err_vs_oracle": c["max_rel_err_vs_oracle"],
+                      "rk": c["rk"], "r_final": c["r"],
+                      "cpu_baseline": {"value": c["value"], "unit": "eigenvalues/s", "cores": c["cores"], "kind": "port",
+                                       "sample": cpu_sample_text(c)},
+                      "e2e": {"value": c["value"], "unit": "eigenvalues/s", "h2d_bytes_per_step": 0,
                               "d2h_bytes_per_step": 0}}))
 
 

@@ -20,6 +20,12 @@ k = 200), k0 = 200, R = 0.5, 48 nodes, 64 probes drawn from PCG64 seed 2 and
 extended by a second draw of 64 when the rank saturates, svd_tol 1e-12; direct
 AMOS kernel values. All eigenvalues of B, the rank and the singular values.
 
+c2_beyn_fresh.json (``... c2fresh``): the same disk with the reference's own
+regrowth, a fresh N x 2r block drawn after the first r columns (beyn.jl:291-309);
+it checks the host-core restatement of the reference's path (oracle/cpu.py).
+The rank saturates at 2r on this disk, so eigenvalues near the contour depend
+on the probe block at the 1e-9 level: each fixture matches one probe policy.
+
 c3_beyn.json (``... c3``): one disk of the desymmetrised stadium, DLP Kress
 global corners on the full stadium (half width 1, radius 1) with the XY
 reflection of parities (-1, -1), N = 4096 (b chosen at k = 332), m = 1024
@@ -88,15 +94,15 @@ def _disk_record(res, cfg):
                 singular_values=[float(x) for x in res["S"]])
 
 
-def c2_beyn(workers=8):
+def c2_beyn(workers=8, regrow="extend"):
     _oracle_path()
     import os
     os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
     from oracle import beyn as OB, geometry as OG
     pts, b = OG.points_with_n("cfie_kress", OG.star(0.2, 5), 2048, 200.0)
     cfg = dict(workload="beyn_cfie_kress_star_N2048_k0_200_R0.5_nq48_L64", N=int(pts[0].n), pts_scaling_factor=b,
-               k0=200.0, R=0.5, nq=48, L=64, seed=2, regrow="extend", svd_tol=1e-12, kernel="direct AMOS")
-    res = OB.beyn_disk(("cfie", pts), pts[0].n, 200.0 + 0j, 0.5, 48, 64, 1e-12, 2, "extend", workers)
+               k0=200.0, R=0.5, nq=48, L=64, seed=2, regrow=regrow, svd_tol=1e-12, kernel="direct AMOS")
+    res = OB.beyn_disk(("cfie", pts), pts[0].n, 200.0 + 0j, 0.5, 48, 64, 1e-12, 2, regrow, workers)
     return _disk_record(res, cfg)
 
 
@@ -116,10 +122,10 @@ def c3_beyn(workers=8):
     return _disk_record(res, cfg)
 
 
-if __name__ == "__main__" and sys.argv[1:2] in (["c1"], ["c2"], ["c3"]):
+if __name__ == "__main__" and sys.argv[1:2] in (["c1"], ["c2"], ["c2fresh"], ["c3"]):
     which = sys.argv[1]
-    fn = {"c1": c1_sweep, "c2": c2_beyn, "c3": c3_beyn}[which]
-    out = {"c1": "c1_sweep.json", "c2": "c2_beyn.json", "c3": "c3_beyn.json"}[which]
+    fn = {"c1": c1_sweep, "c2": c2_beyn, "c2fresh": lambda: c2_beyn(regrow="fresh"), "c3": c3_beyn}[which]
+    out = {"c1": "c1_sweep.json", "c2": "c2_beyn.json", "c2fresh": "c2_beyn_fresh.json", "c3": "c3_beyn.json"}[which]
     (HERE / out).write_text(json.dumps(fn()))
     print("written", out)
 elif __name__ == "__main__":

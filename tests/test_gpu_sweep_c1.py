@@ -2,7 +2,9 @@
 (DLP Kress, N = 512 at k = 42, 200 k in [40, 42]) and refine_minima.
 
 * sigma_min(A(k)) against the oracle's FP64 SVD values (tests/golden/c1_sweep.json,
-  made by tests/golden/make_golden.py c1): 1e-9 relative + 1e-12 absolute;
+  made by tests/golden/make_golden.py c1) at all 200 k: 2e-12 relative
+  (measured 8.3e-13; the smallest sigma_min is 5e-4, whose LAPACK value itself
+  carries eps * sigma_max / sigma_min ~ 1e-12 of relative rounding);
 * the minima the sweep detects (get_eigenvalues, threshold 200) are the
   oracle's 17 (of the 19 J_m zeros in the range, one sits at the range edge
   and two are 0.007 apart, inside one 0.01 grid step);
@@ -26,7 +28,7 @@ def test_c1_sweep_and_refine(qb):
     b = qb.make_circle(1.0)
     sol = qb.DLP_kress(g["pts_scaling_factor"], b)
     sig = qb.k_sweep(sol, b, ks)
-    assert np.all(np.abs(sig - so) <= 1e-9 * so + 1e-12)
+    assert np.all(np.abs(sig - so) <= 2e-12 * so)
     mins = qb.get_eigenvalues(ks, sig)
     assert len(mins) == 17
     assert np.allclose(mins, qb.get_eigenvalues(ks, so))
