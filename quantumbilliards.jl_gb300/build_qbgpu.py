@@ -20,7 +20,7 @@ INCLUDE = ROOT.parent / "include"
 BUILD = ROOT / "_build"
 LIB = PKG / "libqbgpu.so"
 
-SOURCES = ["qbg_api.cu", "qbg_assemble.cu", "qbg_linalg.cu", "qbg_noalloc.cu", "qbg_tc_gemm.cu", "qbg_beyn.cu", "qbg_serve.cu", "qbg_tc_resid.cu",
+SOURCES = ["qbg_api.cu", "qbg_assemble.cu", "qbg_linalg.cu", "qbg_dense.cu", "qbg_noalloc.cu", "qbg_tc_gemm.cu", "qbg_beyn.cu", "qbg_serve.cu", "qbg_tc_resid.cu",
            "qbg_pool.cu", "qbg_ebim.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",

@@ -7,11 +7,11 @@
 #include <string>
 #include <vector>
 #include <algorithm>
-#include <cusolverDn.h>
 #include <atomic>
 
 #include "qbg_assemble.cuh"
 #include "qbg_handles.cuh"
+#include "qbg_dense.cuh"
 #include "qbg_linalg.cuh"
 
 namespace qbg {
@@ -360,100 +360,27 @@ qbg_status qbg_assemble_cheb(qbg_geom* g, const double* ks, int64_t nk, int32_t 
 
 }  // extern "C"
 
-namespace {
-
-// G = W^H W for an n x p column-major W; one CTA per entry (a, b)
-__global__ void k_gram(const cxd* __restrict__ W, int n, int p, cxd* __restrict__ G) {
-  const int a = blockIdx.x % p, b = blockIdx.x / p;
-  const cxd* wa = W + (size_t)a * n;
-  const cxd* wb = W + (size_t)b * n;
-  double re = 0.0, im = 0.0;
-  for (int r = threadIdx.x; r < n; r += blockDim.x) {
-    const cxd x = wa[r], y = wb[r];
-    re = fma(x.re, y.re, fma(x.im, y.im, re));
-    im = fma(x.re, y.im, fma(-x.im, y.re, im));
-  }
-  __shared__ double sr[8], si[8];
-  for (int o = 16; o > 0; o >>= 1) {
-    re += __shfl_xor_sync(0xffffffffu, re, o);
-    im += __shfl_xor_sync(0xffffffffu, im, o);
-  }
-  if ((threadIdx.x & 31) == 0) { sr[threadIdx.x >> 5] = re; si[threadIdx.x >> 5] = im; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double tr = 0.0, ti = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { tr += sr[w]; ti += si[w]; }
-    G[(size_t)b * p + a] = cxd(tr, ti);
-  }
-}
-
-// largest eigenvalue of a p x p Hermitian matrix (column-major, interleaved
-// complex): cyclic Jacobi on its real symmetric 2p x 2p form [[Re, -Im], [Im, Re]],
-// whose eigenvalues are those of G, each twice
-double herm_lambda_max(const std::vector<cxd>& G, int p) {
-  const int m = 2 * p;
-  std::vector<double> a((size_t)m * m);
-  for (int c = 0; c < p; ++c)
-    for (int r = 0; r < p; ++r) {
-      const cxd v = G[(size_t)c * p + r];
-      a[(size_t)c * m + r] = v.re;
-      a[(size_t)(c + p) * m + r + p] = v.re;
-      a[(size_t)c * m + r + p] = v.im;
-      a[(size_t)(c + p) * m + r] = -v.im;
-    }
-  auto A = [&](int r, int c) -> double& { return a[(size_t)c * m + r]; };
-  for (int sweep = 0; sweep < 60; ++sweep) {
-    double off = 0.0, dia = 0.0;
-    for (int c = 0; c < m; ++c)
-      for (int r = 0; r < m; ++r) (r == c ? dia : off) += A(r, c) * A(r, c);
-    if (off <= 1e-30 * dia) break;
-    for (int pi = 0; pi < m - 1; ++pi)
-      for (int q = pi + 1; q < m; ++q) {
-        const double apq = A(pi, q);
-        if (apq == 0.0) continue;
-        const double theta = (A(q, q) - A(pi, pi)) / (2.0 * apq);
-        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
-        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
-        for (int k = 0; k < m; ++k) {  // columns pi, q
-          const double akp = A(k, pi), akq = A(k, q);
-          A(k, pi) = c * akp - sn * akq;
-          A(k, q) = sn * akp + c * akq;
-        }
-        for (int k = 0; k < m; ++k) {  // rows pi, q
-          const double apk = A(pi, k), aqk = A(q, k);
-          A(pi, k) = c * apk - sn * aqk;
-          A(q, k) = sn * apk + c * aqk;
-        }
-      }
-  }
-  double lmax = 0.0;
-  for (int c = 0; c < m; ++c) lmax = std::max(lmax, A(c, c));
-  return lmax;
-}
-
-}  // namespace
 
 extern "C" {
 
 // ---------------------------------------------------------------------------
-// sigma_min: FP64 LU of A(k) (cuSOLVER getrf), then block inverse iteration
-// on (A^H A)^{-1} = A^{-1} A^{-H} with SM_P vectors (getrs with the
-// conjugate transpose and without, thin QR between sweeps) and Rayleigh-Ritz
-// on W^H W, W = A^{-H} X: sigma_min = 1 / sqrt(lambda_max(W^H W)). The
-// estimate converges like (sigma_1 / sigma_{SM_P+1})^4 per sweep; sweeps stop
-// when it changes by less than 1e-13 relative (at most SM_ITERS). An exactly
-// singular U gives sigma_min = 0. Same result as the smallest value of
-// svdvals (macros.jl:159-161) to that tolerance.
+// sigma_min (svdvals(A)[end], macros.jl:159-161) for every k: the k are taken
+// in chunks; a chunk's A(k) are assembled in FP64 straight into one LU batch,
+// factored by the library's batched LU and inverted (LU solves with the
+// identity), and the subspace iteration on the inverses runs on the device,
+// one CTA per k (qbg_dense.cu), until 1/sqrt(lambda_max) changes by less
+// than 1e-13 relative (at most SM_ITERS steps). One host synchronisation per
+// chunk reads the pivots' info and the results; an exactly singular U gives
+// sigma_min = 0.
 // ---------------------------------------------------------------------------
 qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig) {
   if (!g || !ks || !sig || nk < 1) { set_error("qbg_sigma_min: invalid arguments"); return QBG_EINVAL; }
-  constexpr int SM_P = 8, SM_ITERS = 40;
+  constexpr int SM_ITERS = 40;
   std::vector<double> kc(2 * nk);
   for (int64_t q = 0; q < nk; ++q) { kc[2 * q] = ks[q]; kc[2 * q + 1] = 0.0; }
   QBG_TRY(check_ks(kc.data(), nk));
   std::lock_guard<std::mutex> lk(g->mu);
   const int n = (int)g->dim;
-  const int p = std::min(SM_P, n);
   // a sweep runs on a background stream (after the geometry stream's earlier
   // work): its FP64 factorisations fill every SM for milliseconds, and the
   // blocks of latency-bound requests on the library's other streams go first
@@ -470,129 +397,55 @@ qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig)
       return cuda_status(e0, "sigma_min stream");
     }
   }
-  // waits inside the sweep block the thread (no spinning): on a host with few
-  // cores a spinning wait takes the core from the threads that serve the
-  // other requests
-  cudaEvent_t ev_wait = nullptr;
-  if (cudaEventCreateWithFlags(&ev_wait, cudaEventBlockingSync | cudaEventDisableTiming) != cudaSuccess) {
-    cudaStreamDestroy(st);
-    cudaEventDestroy(ev_in);
-    return cuda_status(cudaGetLastError(), "sigma_min event");
-  }
   struct StreamGuard {
     cudaStream_t s;
-    cudaEvent_t e, w;
+    cudaEvent_t e;
     ~StreamGuard() {
       cudaStreamSynchronize(s);
       cudaStreamDestroy(s);
       cudaEventDestroy(e);
-      cudaEventDestroy(w);
     }
-  } sguard{st, ev_in, ev_wait};
-  auto wait_st = [&]() -> cudaError_t {
-    cudaError_t e1 = cudaEventRecord(ev_wait, st);
-    return e1 == cudaSuccess ? cudaEventSynchronize(ev_wait) : e1;
-  };
-  const int chunk = (int)std::min<int64_t>(nk, 16);
-  cxd *A = nullptr, *dks = nullptr, *work = nullptr, *X = nullptr, *W = nullptr, *tau = nullptr, *dG = nullptr;
-  int *ipiv = nullptr, *dinfo = nullptr;
-  void** dptrs = nullptr;
-  cusolverDnHandle_t h = nullptr;
-  std::vector<void*> tmp;
-  auto cleanup = [&]() {
-    for (void* q : tmp) dfree(q, st);
-    if (h) cusolverDnDestroy(h);
-  };
-  auto talloc = [&](void** q, size_t bytes) {
-    int s = dmalloc(q, bytes);
-    if (!s) tmp.push_back(*q);
-    return s;
-  };
+  } sguard{st, ev_in};
+  // chunk: the operators and their inverses within about 1 GB
+  const size_t per_k = sizeof(cxd) * (size_t)n * n * 2;
+  const int chunk = (int)std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(nk, 256),
+                                                                (int64_t)((1ull << 30) / per_k)));
   int s = QBG_OK;
-  if ((s = talloc((void**)&A, sizeof(cxd) * (size_t)n * n * chunk)) || (s = talloc((void**)&dks, sizeof(cxd) * nk)) ||
-      (s = talloc((void**)&X, sizeof(cxd) * (size_t)n * p)) || (s = talloc((void**)&W, sizeof(cxd) * (size_t)n * p)) ||
-      (s = talloc((void**)&tau, sizeof(cxd) * p)) || (s = talloc((void**)&ipiv, sizeof(int) * n)) ||
-      (s = talloc((void**)&dinfo, sizeof(int))) || (s = talloc((void**)&dptrs, sizeof(void*) * chunk)) ||
-      (s = talloc((void**)&dG, sizeof(cxd) * (size_t)p * p))) {
-    cleanup(); return s;
-  }
-  if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) { cleanup(); set_error("cusolverDnCreate failed"); return QBG_ECUDA; }
-  cusolverDnSetStream(h, st);
-  int l1 = 0, l2 = 0, l3 = 0;
-  if (cusolverDnZgetrf_bufferSize(h, n, n, (cuDoubleComplex*)A, n, &l1) != CUSOLVER_STATUS_SUCCESS ||
-      cusolverDnZgeqrf_bufferSize(h, n, p, (cuDoubleComplex*)W, n, &l2) != CUSOLVER_STATUS_SUCCESS ||
-      cusolverDnZungqr_bufferSize(h, n, p, p, (cuDoubleComplex*)W, n, (cuDoubleComplex*)tau, &l3) !=
-          CUSOLVER_STATUS_SUCCESS) {
-    cleanup(); set_error("cuSOLVER workspace query failed"); return QBG_ECUDA;
-  }
-  const int lwork = std::max(std::max(l1, l2), std::max(l3, 1));
-  if ((s = talloc((void**)&work, sizeof(cxd) * (size_t)lwork))) { cleanup(); return s; }
-  // fixed starting block (reproducible): entries of a 64-bit LCG in [-1, 1)
-  std::vector<cxd> hx((size_t)n * p);
-  unsigned long long lcg = 0x9E3779B97F4A7C15ull;
-  auto nxt = [&]() {
-    lcg = lcg * 6364136223846793005ull + 1442695040888963407ull;
-    return (double)(lcg >> 11) * (2.0 / 9007199254740992.0) - 1.0;
-  };
-  for (auto& v : hx) { v.re = nxt(); v.im = nxt(); }
-  cudaError_t e = cudaMemcpyAsync(dks, kc.data(), sizeof(cxd) * nk, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) { cleanup(); return cuda_status(e, "ks H2D"); }
-  std::vector<void*> hp(chunk);
-  std::vector<cxd> G((size_t)p * p);
-  auto fail_solver = [&](const char* what) { cleanup(); set_error("%s failed", what); return QBG_ECUDA; };
-  for (int64_t k0 = 0; k0 < nk; k0 += chunk) {
-    const int c = (int)std::min<int64_t>(chunk, nk - k0);
-    for (int q = 0; q < c; ++q) hp[q] = A + (size_t)q * n * n;
-    e = cudaMemcpyAsync(dptrs, hp.data(), sizeof(void*) * c, cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) { cleanup(); return cuda_status(e, "ptrs"); }
-    if ((s = launch_assemble(g->d, dks + k0, c, 0, 0, dptrs, n, st))) { cleanup(); return s; }
-    for (int q = 0; q < c; ++q) {
-      cuDoubleComplex* Aq = (cuDoubleComplex*)(A + (size_t)q * n * n);
-      if (cusolverDnZgetrf(h, n, n, Aq, n, (cuDoubleComplex*)work, ipiv, dinfo) != CUSOLVER_STATUS_SUCCESS)
-        return fail_solver("cusolverDnZgetrf");
-      int hinfo = 0;
-      e = cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(X, hx.data(), sizeof(cxd) * (size_t)n * p, cudaMemcpyHostToDevice, st);
-      if (e == cudaSuccess) e = wait_st();
-      if (e != cudaSuccess) { cleanup(); return cuda_status(e, "sigma_min LU"); }
-      if (hinfo > 0) {  // U(hinfo, hinfo) == 0: A(k) is singular
-        sig[k0 + q] = 0.0;
-        continue;
-      }
-      double est = -1.0;
-      for (int it = 0; it < SM_ITERS; ++it) {
-        // W = A^{-H} X
-        e = cudaMemcpyAsync(W, X, sizeof(cxd) * (size_t)n * p, cudaMemcpyDeviceToDevice, st);
-        if (e != cudaSuccess) { cleanup(); return cuda_status(e, "sigma_min copy"); }
-        if (cusolverDnZgetrs(h, CUBLAS_OP_C, n, p, Aq, n, ipiv, (cuDoubleComplex*)W, n, dinfo) !=
-            CUSOLVER_STATUS_SUCCESS)
-          return fail_solver("cusolverDnZgetrs");
-        // Rayleigh-Ritz: lambda_max(W^H W), X orthonormal; W^H W formed on the device
-        k_gram<<<p * p, 256, 0, st>>>(W, n, p, dG);
-        QBG_LAUNCH_CHECK("k_gram");
-        e = cudaMemcpyAsync(G.data(), dG, sizeof(cxd) * (size_t)p * p, cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = wait_st();
-        if (e != cudaSuccess) { cleanup(); return cuda_status(e, "sigma_min D2H"); }
-        const double lam = herm_lambda_max(G, p);
-        const double cur = lam > 0.0 ? 1.0 / std::sqrt(lam) : 0.0;
-        const bool done = it > 0 && std::fabs(cur - est) <= 1e-13 * cur;
-        est = cur;
-        if (done || it + 1 == SM_ITERS) break;
-        // X = orth(A^{-1} W)
-        if (cusolverDnZgetrs(h, CUBLAS_OP_N, n, p, Aq, n, ipiv, (cuDoubleComplex*)W, n, dinfo) !=
-                CUSOLVER_STATUS_SUCCESS ||
-            cusolverDnZgeqrf(h, n, p, (cuDoubleComplex*)W, n, (cuDoubleComplex*)tau, (cuDoubleComplex*)work, lwork,
-                             dinfo) != CUSOLVER_STATUS_SUCCESS ||
-            cusolverDnZungqr(h, n, p, p, (cuDoubleComplex*)W, n, (cuDoubleComplex*)tau, (cuDoubleComplex*)work, lwork,
-                             dinfo) != CUSOLVER_STATUS_SUCCESS)
-          return fail_solver("sigma_min subspace step");
-        std::swap(X, W);
-      }
-      sig[k0 + q] = est;
+  {
+    Dense64 D;
+    cxd *Cinv = nullptr, *dks = nullptr, *work = nullptr, *X0 = nullptr;
+    double* dsig = nullptr;
+    void** dptrs = nullptr;
+    if ((s = D.create(n, chunk, st)) || (s = D.alloc(&Cinv, sizeof(cxd) * (size_t)n * n * chunk)) ||
+        (s = D.alloc(&dks, sizeof(cxd) * nk)) || (s = D.alloc(&work, sizeof(cxd) * (size_t)3 * n * DENSE_P * chunk)) ||
+        (s = D.alloc(&X0, sizeof(cxd) * (size_t)n * DENSE_P)) || (s = D.alloc(&dsig, sizeof(double) * chunk)) ||
+        (s = D.alloc(&dptrs, sizeof(void*) * chunk)))
+      return s;
+    std::vector<cxd> hx;
+    dense_start_block(n, hx);
+    std::vector<void*> hp(chunk);
+    for (int q = 0; q < chunk; ++q) hp[q] = D.A(q);
+    QBG_CUDA(cudaMemcpyAsync(X0, hx.data(), sizeof(cxd) * hx.size(), cudaMemcpyHostToDevice, st));
+    QBG_CUDA(cudaMemcpyAsync(dks, kc.data(), sizeof(cxd) * nk, cudaMemcpyHostToDevice, st));
+    QBG_CUDA(cudaMemcpyAsync(dptrs, hp.data(), sizeof(void*) * chunk, cudaMemcpyHostToDevice, st));
+    std::vector<int> info;
+    std::vector<double> hs(chunk);
+    for (int64_t k0 = 0; k0 < nk; k0 += chunk) {
+      const int c = (int)std::min<int64_t>(chunk, nk - k0);
+      D.f.batch = c;
+      QBG_TRY(launch_assemble(g->d, dks + k0, c, 0, QBG_PREC_FP64, dptrs, n, st));
+      QBG_TRY(lu_factor<double>(D.f, st));
+      QBG_TRY(D.inverse(Cinv));
+      QBG_TRY(sigma_iterate(Cinv, n, c, X0, work, SM_ITERS, 1e-13, dsig, nullptr, nullptr, st));
+      info.assign(c, 0);
+      QBG_CUDA(cudaMemcpyAsync(info.data(), D.f.info, sizeof(int) * c, cudaMemcpyDeviceToHost, st));
+      QBG_CUDA(cudaMemcpyAsync(hs.data(), dsig, sizeof(double) * c, cudaMemcpyDeviceToHost, st));
+      QBG_CUDA(cudaStreamSynchronize(st));
+      for (int q = 0; q < c; ++q) sig[k0 + q] = info[q] > 0 ? 0.0 : hs[q];
     }
+    D.f.batch = chunk;
   }
-  cleanup();
-  return QBG_OK;
+  return s;
 }
 
 // chebyshev_params (chebyshev_optimal_panelization.jl:221-307): grow the panel

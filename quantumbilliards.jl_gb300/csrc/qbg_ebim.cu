@@ -32,10 +32,10 @@
 #include <cmath>
 #include <complex>
 #include <vector>
-#include <cusolverDn.h>
 #include "qbg_common.cuh"
 #include "qbg_handles.cuh"
 #include "qbg_linalg.cuh"
+#include "qbg_dense.cuh"
 #include "qbgpu.h"
 
 using namespace qbg;
@@ -91,12 +91,6 @@ __global__ void k_conj_transpose(const cxd* __restrict__ A, cxd* __restrict__ AH
       AH[r + (size_t)c * n] = cxd(v.re, -v.im);
     }
   }
-}
-
-__global__ void k_identity(cxd* __restrict__ M, int n) {
-  const size_t count = (size_t)n * n;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
-    M[i] = cxd(i % (size_t)(n + 1) == 0 ? 1.0 : 0.0, 0.0);
 }
 
 // Adjoint Fredholm matrix from the Fredholm matrix F = I - D of the DLP:
@@ -354,16 +348,27 @@ struct Ebim {
   int n = 0;
   cudaStream_t st = nullptr;
   cudaEvent_t ev = nullptr;
-  cusolverDnHandle_t h = nullptr;
   cxd *LU = nullptr, *dA = nullptr, *ddA = nullptr;
   cxd *C = nullptr, *CH = nullptr;  // A^-1 A' and its conjugate transpose
-  int *ipiv = nullptr, *dinfo = nullptr;
+  Dense64 D;                        // the library's FP64 LU of the matrix in LU
   std::vector<void*> tmp;
   ~Ebim() {
     if (st) cudaStreamSynchronize(st);
+    D.release();
     for (void* q : tmp) dfree(q, st);
-    if (h) cusolverDnDestroy(h);
     if (ev) cudaEventDestroy(ev);
+    if (st) cudaStreamDestroy(st);
+  }
+  // LU of the n x n matrix in LU, in place; QBG_ESINGULAR (with what) if U is exactly singular
+  int factor(const char* what) {
+    QBG_TRY(D.bind(LU, n, 1, st));
+    std::vector<int> info;
+    QBG_TRY(D.factor(&info));
+    if (info[0] > 0) {
+      set_error("%s is exactly singular (U(%d, %d) = 0)", what, info[0], info[0]);
+      return QBG_ESINGULAR;
+    }
+    return QBG_OK;
   }
   template <class P>
   int alloc(P** q, size_t bytes) {
@@ -377,11 +382,6 @@ struct Ebim {
     return e == cudaSuccess ? QBG_OK : cuda_status(e, "EBIM wait");
   }
 };
-
-int solver_fail(const char* what) {
-  set_error("%s failed", what);
-  return QBG_ECUDA;
-}
 
 // Y = A B for n x n A and n x q B (FP64 complex); P: scratch of
 // tall_scratch(n, q) elements
@@ -411,28 +411,18 @@ int gemm_nq(const cxd* A, const cxd* B, cxd* Y, int n, int q, cxd* P, cudaStream
   return QBG_OK;
 }
 
-// orthonormal basis of the columns of W (n x p) in place, Householder QR
-int householder_orth(Ebim& E, cxd* W, int p, cxd* tau, cxd* work, int lwork) {
-  if (cusolverDnZgeqrf(E.h, E.n, p, (cuDoubleComplex*)W, E.n, (cuDoubleComplex*)tau, (cuDoubleComplex*)work, lwork,
-                       E.dinfo) != CUSOLVER_STATUS_SUCCESS ||
-      cusolverDnZungqr(E.h, E.n, p, p, (cuDoubleComplex*)W, E.n, (cuDoubleComplex*)tau, (cuDoubleComplex*)work, lwork,
-                       E.dinfo) != CUSOLVER_STATUS_SUCCESS)
-    return solver_fail("EBIM QR");
-  return QBG_OK;
-}
-
 // Buffers of the orthonormalisation: Gram matrix, its factor, a copy of W.
 struct OrthWork {
-  cxd *G = nullptr, *M = nullptr, *Wt = nullptr, *tau = nullptr, *work = nullptr;
-  int lwork = 0;
+  cxd *G = nullptr, *M = nullptr, *Wt = nullptr;
   std::vector<cxd> hg, hm;
 };
 
 // Orthonormal basis of the columns of W (n x p) in place by Cholesky QR, twice
 // (the second pass restores orthogonality to rounding): G = W^H W on the
 // device; on the host, with D = diag(G)^(1/2), the Cholesky factor R of
-// D^-1 G D^-1 and M = D^-1 R^-1; then W <- W M. Falls back to Householder
-// QR when the scaled Gram matrix is not numerically positive definite.
+// D^-1 G D^-1 and M = D^-1 R^-1; then W <- W M. Falls back to Gram-Schmidt
+// on the device (twice per column) when the scaled Gram matrix is not
+// numerically positive definite.
 int orthonormalize(Ebim& E, cxd* W, int p, OrthWork& o) {
   const int n = E.n;
   o.hg.resize((size_t)p * p);
@@ -468,7 +458,7 @@ int orthonormalize(Ebim& E, cxd* W, int p, OrthWork& o) {
         R[(size_t)i * p + j] = t / rjj;
       }
     }
-    if (!ok) return householder_orth(E, W, p, o.tau, o.work, o.lwork);
+    if (!ok) return orth_columns(W, n, p, E.st);
     // Ri = R^-1 (upper triangular), M = D^-1 Ri
     std::fill(Ri.begin(), Ri.end(), zc(0.0, 0.0));
     for (int j = 0; j < p; ++j) {
@@ -513,14 +503,6 @@ int block_eigs(Ebim& E, bool adjoint, int p, int nev, std::vector<zc>& mu, cxd* 
   QBG_TRY(E.alloc(&o.G, sizeof(cxd) * pp));
   QBG_TRY(E.alloc(&o.M, sizeof(cxd) * pp));
   QBG_TRY(E.alloc(&o.Wt, sizeof(cxd) * np));
-  QBG_TRY(E.alloc(&o.tau, sizeof(cxd) * p));
-  int l1 = 0, l2 = 0;
-  if (cusolverDnZgeqrf_bufferSize(E.h, n, p, (cuDoubleComplex*)Q, n, &l1) != CUSOLVER_STATUS_SUCCESS ||
-      cusolverDnZungqr_bufferSize(E.h, n, p, p, (cuDoubleComplex*)Q, n, (cuDoubleComplex*)o.tau, &l2) !=
-          CUSOLVER_STATUS_SUCCESS)
-    return solver_fail("EBIM QR workspace query");
-  o.lwork = std::max(std::max(l1, l2), 1);
-  QBG_TRY(E.alloc(&o.work, sizeof(cxd) * (size_t)o.lwork));
   // fixed starting block (reproducible): entries of a 64-bit LCG in [-1, 1)
   std::vector<cxd> hq(np);
   unsigned long long lcg = adjoint ? 0xD1B54A32D192ED03ull : 0x9E3779B97F4A7C15ull;
@@ -582,34 +564,13 @@ int ebim_run(Ebim& E, double k, double dk, int nev_req, int flags, int cap, doub
              int32_t* count, int32_t* iters_out) {
   const int n = E.n;
   const bool full = (flags & QBG_EBIM_FULL) != 0;
-  if (cusolverDnCreate(&E.h) != CUSOLVER_STATUS_SUCCESS) return solver_fail("cusolverDnCreate");
-  cusolverDnSetStream(E.h, E.st);
-  QBG_TRY(E.alloc(&E.ipiv, sizeof(int) * n));
-  QBG_TRY(E.alloc(&E.dinfo, sizeof(int)));
-  // LU of A (the reference's lu!(A))
-  int lw = 0;
-  if (cusolverDnZgetrf_bufferSize(E.h, n, n, (cuDoubleComplex*)E.LU, n, &lw) != CUSOLVER_STATUS_SUCCESS)
-    return solver_fail("getrf workspace query");
-  cxd* lwork = nullptr;
-  QBG_TRY(E.alloc(&lwork, sizeof(cxd) * (size_t)std::max(lw, 1)));
-  if (cusolverDnZgetrf(E.h, n, n, (cuDoubleComplex*)E.LU, n, (cuDoubleComplex*)lwork, E.ipiv, E.dinfo) !=
-      CUSOLVER_STATUS_SUCCESS)
-    return solver_fail("cusolverDnZgetrf");
-  int hinfo = 0;
-  QBG_CUDA(cudaMemcpyAsync(&hinfo, E.dinfo, sizeof(int), cudaMemcpyDeviceToHost, E.st));
-  QBG_TRY(E.wait());
-  if (hinfo > 0) {
-    set_error("EBIM: A(k) is exactly singular (U(%d, %d) = 0)", hinfo, hinfo);
-    return QBG_ESINGULAR;
-  }
+  // LU of A (the reference's lu!(A)), the library's batched FP64 LU with one matrix
+  QBG_TRY(E.factor("EBIM: A(k)"));
   // C = A^-1 A' and C^H from the factors (one solve with n right-hand sides):
   // every application of the shift-invert operator is then one skinny product
   QBG_TRY(E.alloc(&E.C, sizeof(cxd) * (size_t)n * n));
   QBG_TRY(E.alloc(&E.CH, sizeof(cxd) * (size_t)n * n));
-  QBG_CUDA(cudaMemcpyAsync(E.C, E.dA, sizeof(cxd) * (size_t)n * n, cudaMemcpyDeviceToDevice, E.st));
-  if (cusolverDnZgetrs(E.h, CUBLAS_OP_N, n, n, (const cuDoubleComplex*)E.LU, n, E.ipiv, (cuDoubleComplex*)E.C, n,
-                       E.dinfo) != CUSOLVER_STATUS_SUCCESS)
-    return solver_fail("cusolverDnZgetrs");
+  QBG_TRY(lu_solve_shared<double>(E.D.f, E.dA, n, E.C, 0, E.st));
   k_conj_transpose<<<dim3((n + 31) / 32, (n + 31) / 32), dim3(32, 8), 0, E.st>>>(E.C, E.CH, n);
   QBG_LAUNCH_CHECK("k_conj_transpose");
   int nev = std::min(nev_req, n);
@@ -654,9 +615,9 @@ int ebim_run(Ebim& E, double k, double dk, int nev_req, int flags, int cap, doub
   QBG_TRY(E.alloc(&W2, sizeof(cxd) * (size_t)n * nev));
   QBG_TRY(E.alloc(&P, sizeof(cxd) * std::max<size_t>(tall_scratch(n, nev), 1)));
   if (full) {  // left eigenvectors of the pencil: u~ = A^{-H} u
-    if (cusolverDnZgetrs(E.h, CUBLAS_OP_C, n, nev, (const cuDoubleComplex*)E.LU, n, E.ipiv, (cuDoubleComplex*)U, n,
-                         E.dinfo) != CUSOLVER_STATUS_SUCCESS)
-      return solver_fail("cusolverDnZgetrs");
+    cxd* Us = nullptr;
+    QBG_TRY(E.alloc(&Us, sizeof(cxd) * (size_t)n * nev));
+    QBG_TRY(lu_solve_adjoint<double>(E.D.f, U, 0, nev, U, Us, E.st));
   }
   QBG_TRY(gemm_nq(E.ddA, V, W1, n, nev, P, E.st));
   QBG_TRY(gemm_nq(E.dA, V, W2, n, nev, P, E.st));
@@ -739,76 +700,114 @@ qbg_status qbg_ebim_eig(int64_t n, const void* A, const void* dA, const void* dd
 // ---------------------------------------------------------------------------
 // Newton refinement of a sweep minimum (newton_refine_svd!,
 // sweepmethods.jl:307-368): f(k) = lambda_min(G(k)), G = A^H A, with
-// G' = A'^H A + A^H A' and G'' = A''^H A + 2 A'^H A' + A^H A''. Per step: the
-// three matrices assembled at k on the device, the four products A^H A,
-// A'^H A, A''^H A, A'^H A' (FP64), the full Hermitian eigen-decomposition of G
-// (cuSOLVER heevd); lambda1 = x^H G' x, lambda2 = x^H G'' x + 2 sum_{j != min}
-// |v_j^H G' x|^2 / (lambda - lambda_j) (terms with |lambda - lambda_j| < eps
-// skipped), k <- clamp(k - lambda1 / lambda2, a, b); stops when the step is
-// below tol, lambda1 or lambda2 is not finite, or |lambda2| < sqrt(eps). The
-// best k seen (smallest lambda) is kept; the result is (k, sqrt(lambda_min))
-// at the final k, or at the best k when that is smaller.
+// G' = A'^H A + A^H A' and G'' = A''^H A + 2 A'^H A' + A^H A''. The
+// reference takes lambda = lambda_min, x and every eigenpair (lambda_j, v_j)
+// from a full Hermitian eigen-decomposition of G and forms
+//   lambda1 = x^H G' x,
+//   lambda2 = x^H G'' x + 2 sum_{j != min} |v_j^H G' x|^2 / (lambda - lambda_j).
+// Here, per step, on the device:
+//  * lambda = sigma_min(A)^2 and x = the right singular vector of A, from the
+//    library's FP64 LU of A, its inverse and the subspace iteration on the
+//    inverse (qbg_dense.cu), iterated to rounding;
+//  * with u = A x, u1 = A' x, u2 = A'' x: G' x = A'^H u + A^H u1 and
+//    x^H G'' x = 2 Re(u2^H u) + 2 |u1|^2 (matrix-vector products only);
+//  * the eigen-sum is -b^H y with b = G' x - lambda1 x and y the solution of
+//    (G - lambda I + mu x x^H) y = b (mu = trace(G) / n): b has no x
+//    component, so y = sum_{j != min} v_j (v_j^H b) / (lambda_j - lambda);
+//    G = A^H A is formed once per step and factored by the library's LU.
+// The reference's skip of terms with |lambda - lambda_j| < eps has no
+// counterpart (a numerically degenerate pair makes either form blow up).
+// Steps, clamping, stopping rules and the best-k fallback are the reference's.
 // ---------------------------------------------------------------------------
-__global__ void k_hsum(const cxd* __restrict__ M, const cxd* __restrict__ N2, double c, int n, cxd* __restrict__ out) {
-  // out = M + M^H + c N2 (N2 may be null)
-  const size_t count = (size_t)n * n;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
-    const int r = (int)(i % n), col = (int)(i / n);
-    const cxd a = M[i], b = M[col + (size_t)r * n];
-    cxd v(a.re + b.re, a.im - b.im);
-    if (N2) {
-      v.re += c * N2[i].re;
-      v.im += c * N2[i].im;
-    }
-    out[i] = v;
-  }
-}
-
 struct Newton {
   Ebim E;
-  cxd *AH = nullptr, *G = nullptr, *M = nullptr, *Nn = nullptr, *Pp = nullptr, *H = nullptr, *H2 = nullptr,
-      *cwork = nullptr, *xv = nullptr, *gx = nullptr, *hx = nullptr, *cv = nullptr;
-  double* w = nullptr;
+  Dense64 DM;  // LU of the deflated shift M
+  cxd *Ac = nullptr, *G = nullptr, *M = nullptr, *Cinv = nullptr, *work = nullptr, *X0 = nullptr, *xv = nullptr,
+      *u = nullptr, *u1 = nullptr, *u2 = nullptr, *gx = nullptr, *bv = nullptr, *yv = nullptr;
+  double* dsig = nullptr;
   cxd* dks = nullptr;
   void** dptrs = nullptr;
-  int lwork = 0;
+  ~Newton() {
+    if (E.st) cudaStreamSynchronize(E.st);
+    DM.release();
+  }
 };
 
-// G = A^H A at k (and with derivs the pieces of G' and G''); lam: ascending
-// eigenvalues; with vectors G holds the eigenvectors afterwards
-int newton_eval(qbg_geom* g, Newton& W, double k, bool derivs, std::vector<double>& lam) {
+struct NewtonEval {
+  double lam = 0.0, l1 = 0.0, l2 = 0.0;
+};
+
+int newton_eval(qbg_geom* g, Newton& W, double k, bool derivs, NewtonEval& out) {
   Ebim& E = W.E;
   const int n = E.n;
   const cxd kk(k, 0.0);
-  void* hp[3] = {E.LU, E.dA, E.ddA};
+  void* hp[3] = {W.Ac, E.dA, E.ddA};
   QBG_CUDA(cudaMemcpyAsync(W.dks, &kk, sizeof(cxd), cudaMemcpyHostToDevice, E.st));
   QBG_CUDA(cudaMemcpyAsync(W.dptrs, hp, sizeof(hp), cudaMemcpyHostToDevice, E.st));
   QBG_TRY(launch_assemble(g->d, W.dks, 1, derivs ? 1 : 0, QBG_PREC_FP64, W.dptrs, n, E.st));
-  QBG_TRY(E.wait());  // k and the pointer table are staged from this frame
-  const dim3 tg((n + 31) / 32, (n + 31) / 32), tb(32, 8);
-  k_conj_transpose<<<tg, tb, 0, E.st>>>(E.LU, W.AH, n);
-  QBG_LAUNCH_CHECK("k_conj_transpose");
-  const cxd one(1, 0), zero(0, 0);
-  QBG_TRY(gemm_batched<double>(n, n, n, one, W.AH, n, 0, E.LU, n, 0, zero, W.G, n, 0, 1, E.st));  // A^H A
-  if (derivs) {
-    k_conj_transpose<<<tg, tb, 0, E.st>>>(E.dA, W.AH, n);
-    QBG_LAUNCH_CHECK("k_conj_transpose");
-    QBG_TRY(gemm_batched<double>(n, n, n, one, W.AH, n, 0, E.LU, n, 0, zero, W.M, n, 0, 1, E.st));   // A'^H A
-    QBG_TRY(gemm_batched<double>(n, n, n, one, W.AH, n, 0, E.dA, n, 0, zero, W.Pp, n, 0, 1, E.st));  // A'^H A'
-    k_conj_transpose<<<tg, tb, 0, E.st>>>(E.ddA, W.AH, n);
-    QBG_LAUNCH_CHECK("k_conj_transpose");
-    QBG_TRY(gemm_batched<double>(n, n, n, one, W.AH, n, 0, E.LU, n, 0, zero, W.Nn, n, 0, 1, E.st));  // A''^H A
-    k_hsum<<<2048, 256, 0, E.st>>>(W.M, nullptr, 0.0, n, W.H);
-    QBG_LAUNCH_CHECK("k_hsum");
-    k_hsum<<<2048, 256, 0, E.st>>>(W.Nn, W.Pp, 2.0, n, W.H2);
-    QBG_LAUNCH_CHECK("k_hsum");
+  const size_t nn = (size_t)n * n;
+  QBG_CUDA(cudaMemcpyAsync(E.LU, W.Ac, sizeof(cxd) * nn, cudaMemcpyDeviceToDevice, E.st));
+  std::vector<int> info;
+  QBG_TRY(E.D.factor(&info));  // synchronizes: k and the pointer table are staged from this frame
+  double sig = 0.0;
+  if (info[0] > 0) {
+    out.lam = 0.0;  // A(k) exactly singular: sigma_min = 0
+    if (!derivs) return QBG_OK;
+    set_error("Newton refinement: A(k) is exactly singular at k = %.17g", k);
+    return QBG_ESINGULAR;
   }
-  if (cusolverDnZheevd(E.h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, (cuDoubleComplex*)W.G, n, W.w,
-                       (cuDoubleComplex*)W.cwork, W.lwork, E.dinfo) != CUSOLVER_STATUS_SUCCESS)
-    return solver_fail("cusolverDnZheevd");
-  lam.resize(n);
-  QBG_CUDA(cudaMemcpyAsync(lam.data(), W.w, sizeof(double) * n, cudaMemcpyDeviceToHost, E.st));
-  return E.wait();
+  QBG_TRY(E.D.inverse(W.Cinv));
+  QBG_TRY(sigma_iterate(W.Cinv, n, 1, W.X0, W.work, 60, 1e-15, W.dsig, nullptr, W.xv, E.st));
+  QBG_CUDA(cudaMemcpyAsync(&sig, W.dsig, sizeof(double), cudaMemcpyDeviceToHost, E.st));
+  if (!derivs) {
+    QBG_TRY(E.wait());
+    out.lam = sig * sig;
+    return QBG_OK;
+  }
+  const cxd one(1, 0), zero(0, 0);
+  QBG_TRY(gemm_batched<double>(n, 1, n, one, W.Ac, n, 0, W.xv, n, 0, zero, W.u, n, 0, 1, E.st));     // A x
+  QBG_TRY(gemm_batched<double>(n, 1, n, one, E.dA, n, 0, W.xv, n, 0, zero, W.u1, n, 0, 1, E.st));    // A' x
+  QBG_TRY(gemm_batched<double>(n, 1, n, one, E.ddA, n, 0, W.xv, n, 0, zero, W.u2, n, 0, 1, E.st));   // A'' x
+  QBG_TRY(gemm_batched_ah<double>(n, 1, n, one, E.dA, n, 0, W.u, n, 0, zero, W.gx, n, 0, 1, E.st));  // A'^H A x
+  QBG_TRY(gemm_batched_ah<double>(n, 1, n, one, W.Ac, n, 0, W.u1, n, 0, one, W.gx, n, 0, 1, E.st));  // + A^H A' x
+  QBG_TRY(gemm_batched_ah<double>(n, n, n, one, W.Ac, n, 0, W.Ac, n, 0, zero, W.G, n, 0, 1, E.st));  // G = A^H A
+  std::vector<cxd> hx(n), hu(n), h1(n), h2(n), hg(n), hd(n);
+  QBG_CUDA(cudaMemcpyAsync(hx.data(), W.xv, sizeof(cxd) * n, cudaMemcpyDeviceToHost, E.st));
+  QBG_CUDA(cudaMemcpyAsync(hu.data(), W.u, sizeof(cxd) * n, cudaMemcpyDeviceToHost, E.st));
+  QBG_CUDA(cudaMemcpyAsync(h1.data(), W.u1, sizeof(cxd) * n, cudaMemcpyDeviceToHost, E.st));
+  QBG_CUDA(cudaMemcpyAsync(h2.data(), W.u2, sizeof(cxd) * n, cudaMemcpyDeviceToHost, E.st));
+  QBG_CUDA(cudaMemcpyAsync(hg.data(), W.gx, sizeof(cxd) * n, cudaMemcpyDeviceToHost, E.st));
+  QBG_CUDA(cudaMemcpy2DAsync(hd.data(), sizeof(cxd), W.G, sizeof(cxd) * (n + 1), sizeof(cxd), n,
+                             cudaMemcpyDeviceToHost, E.st));  // diag(G)
+  QBG_TRY(E.wait());
+  const double lam = sig * sig;
+  double l1 = 0.0, g2 = 0.0, tr = 0.0;
+  for (int r = 0; r < n; ++r) {
+    l1 += hx[r].re * hg[r].re + hx[r].im * hg[r].im;                           // Re(x^H G' x)
+    g2 += 2.0 * (h2[r].re * hu[r].re + h2[r].im * hu[r].im) + 2.0 * cabs2(h1[r]);  // x^H G'' x
+    tr += hd[r].re;
+  }
+  std::vector<cxd> hb(n);
+  for (int r = 0; r < n; ++r) hb[r] = cxd(hg[r].re - l1 * hx[r].re, hg[r].im - l1 * hx[r].im);
+  const double mu = tr > 0.0 ? tr / n : 1.0;
+  QBG_TRY(deflate_shift(W.G, W.xv, n, lam, mu, W.M, E.st));
+  std::vector<int> infm;
+  QBG_TRY(W.DM.factor(&infm));
+  if (infm[0] > 0) {
+    set_error("Newton refinement: G - lambda I + mu x x^H is singular (a repeated smallest eigenvalue)");
+    return QBG_ESINGULAR;
+  }
+  QBG_CUDA(cudaMemcpyAsync(W.bv, hb.data(), sizeof(cxd) * n, cudaMemcpyHostToDevice, E.st));
+  QBG_TRY(lu_solve_shared<double>(W.DM.f, W.bv, 1, W.yv, 0, E.st));
+  std::vector<cxd> hy(n);
+  QBG_CUDA(cudaMemcpyAsync(hy.data(), W.yv, sizeof(cxd) * n, cudaMemcpyDeviceToHost, E.st));
+  QBG_TRY(E.wait());
+  double s2 = 0.0;
+  for (int r = 0; r < n; ++r) s2 += hb[r].re * hy[r].re + hb[r].im * hy[r].im;  // Re(b^H y)
+  out.lam = lam;
+  out.l1 = l1;
+  out.l2 = g2 - 2.0 * s2;
+  return QBG_OK;
 }
 
 qbg_status newton_impl(qbg_geom* g, double k0, double a, double b, int maxiter, double tol, double* k_out,
@@ -823,55 +822,32 @@ qbg_status newton_impl(qbg_geom* g, double k0, double a, double b, int maxiter, 
   if (e == cudaSuccess) e = cudaStreamWaitEvent(E.st, ev_in, 0);
   cudaEventDestroy(ev_in);
   if (e != cudaSuccess) return cuda_status(e, "Newton stream order");
-  if (cusolverDnCreate(&E.h) != CUSOLVER_STATUS_SUCCESS) return solver_fail("cusolverDnCreate");
-  cusolverDnSetStream(E.h, E.st);
   const size_t bytes = sizeof(cxd) * (size_t)n * n;
-  for (cxd** q : {&E.LU, &E.dA, &E.ddA, &W.AH, &W.G, &W.M, &W.Nn, &W.Pp, &W.H, &W.H2}) QBG_TRY(E.alloc(q, bytes));
-  QBG_TRY(E.alloc(&E.dinfo, sizeof(int)));
-  QBG_TRY(E.alloc(&W.w, sizeof(double) * n));
+  for (cxd** q : {&E.LU, &E.dA, &E.ddA, &W.Ac, &W.G, &W.M, &W.Cinv}) QBG_TRY(E.alloc(q, bytes));
+  for (cxd** q : {&W.xv, &W.u, &W.u1, &W.u2, &W.gx, &W.bv, &W.yv}) QBG_TRY(E.alloc(q, sizeof(cxd) * n));
+  QBG_TRY(E.alloc(&W.work, sizeof(cxd) * (size_t)3 * n * DENSE_P));
+  QBG_TRY(E.alloc(&W.X0, sizeof(cxd) * (size_t)n * DENSE_P));
+  QBG_TRY(E.alloc(&W.dsig, sizeof(double)));
   QBG_TRY(E.alloc(&W.dks, sizeof(cxd)));
   QBG_TRY(E.alloc(&W.dptrs, sizeof(void*) * 3));
-  QBG_TRY(E.alloc(&W.gx, sizeof(cxd) * n));
-  QBG_TRY(E.alloc(&W.hx, sizeof(cxd) * n));
-  QBG_TRY(E.alloc(&W.cv, sizeof(cxd) * n));
-  if (cusolverDnZheevd_bufferSize(E.h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, (cuDoubleComplex*)W.G, n,
-                                  W.w, &W.lwork) != CUSOLVER_STATUS_SUCCESS)
-    return solver_fail("heevd workspace query");
-  QBG_TRY(E.alloc(&W.cwork, sizeof(cxd) * (size_t)std::max(W.lwork, 1)));
-  const double eps = 2.220446049250313e-16;
+  QBG_TRY(E.D.bind(E.LU, n, 1, E.st));
+  QBG_TRY(W.DM.bind(W.M, n, 1, E.st));
+  {
+    std::vector<cxd> hx0;
+    dense_start_block(n, hx0);
+    QBG_CUDA(cudaMemcpyAsync(W.X0, hx0.data(), sizeof(cxd) * hx0.size(), cudaMemcpyHostToDevice, E.st));
+  }
   double k = std::min(std::max(k0, a), b), kbest = k, lbest = INFINITY;
-  std::vector<double> lam;
-  std::vector<cxd> hx(n), hg(n), hh(n), hc(n);
   int it = 0;
-  const cxd one(1, 0), zero(0, 0);
+  const double eps = 2.220446049250313e-16;
+  NewtonEval ev;
   for (; it < maxiter; ++it) {
-    QBG_TRY(newton_eval(g, W, k, true, lam));
-    const double l0 = lam[0];  // ascending: the minimum is first
-    if (std::isfinite(l0) && l0 < lbest) {
-      lbest = l0;
+    QBG_TRY(newton_eval(g, W, k, true, ev));
+    if (std::isfinite(ev.lam) && ev.lam < lbest) {
+      lbest = ev.lam;
       kbest = k;
     }
-    const cxd* x = W.G;  // eigenvector of the smallest eigenvalue (column 0)
-    QBG_TRY(gemm_batched<double>(n, 1, n, one, W.H, n, 0, x, n, 0, zero, W.gx, n, 0, 1, E.st));
-    QBG_TRY(gemm_batched<double>(n, 1, n, one, W.H2, n, 0, x, n, 0, zero, W.hx, n, 0, 1, E.st));
-    // c_j = v_j^H (G' x), j = 0..n-1
-    k_inner<<<n, 256, 0, E.st>>>(W.G, W.gx, n, n, W.cv);  // p = n rows of the (n x 1) result: G[a] = v_a^H gx
-    QBG_LAUNCH_CHECK("k_inner");
-    QBG_CUDA(cudaMemcpyAsync(hx.data(), x, sizeof(cxd) * n, cudaMemcpyDeviceToHost, E.st));
-    QBG_CUDA(cudaMemcpyAsync(hg.data(), W.gx, sizeof(cxd) * n, cudaMemcpyDeviceToHost, E.st));
-    QBG_CUDA(cudaMemcpyAsync(hh.data(), W.hx, sizeof(cxd) * n, cudaMemcpyDeviceToHost, E.st));
-    QBG_CUDA(cudaMemcpyAsync(hc.data(), W.cv, sizeof(cxd) * n, cudaMemcpyDeviceToHost, E.st));
-    QBG_TRY(E.wait());
-    double l1 = 0.0, l2 = 0.0;
-    for (int r = 0; r < n; ++r) {
-      l1 += hx[r].re * hg[r].re + hx[r].im * hg[r].im;  // Re(conj(x) gx)
-      l2 += hx[r].re * hh[r].re + hx[r].im * hh[r].im;
-    }
-    for (int j = 1; j < n; ++j) {
-      const double den = l0 - lam[j];
-      if (std::fabs(den) < eps) continue;
-      l2 += 2.0 * (hc[j].re * hc[j].re + hc[j].im * hc[j].im) / den;
-    }
+    const double l1 = ev.l1, l2 = ev.l2;
     if (!std::isfinite(l1) || !std::isfinite(l2) || std::fabs(l2) < std::sqrt(eps)) break;
     const double knew = std::min(std::max(k - l1 / l2, a), b);
     if (!std::isfinite(knew)) break;
@@ -882,12 +858,12 @@ qbg_status newton_impl(qbg_geom* g, double k0, double a, double b, int maxiter, 
     }
     k = knew;
   }
-  QBG_TRY(newton_eval(g, W, k, false, lam));
-  double lmin = lam[0];
+  QBG_TRY(newton_eval(g, W, k, false, ev));
+  double lmin = ev.lam;
   if (!(std::isfinite(lmin) && lmin <= lbest)) {
     k = kbest;
-    QBG_TRY(newton_eval(g, W, k, false, lam));
-    lmin = lam[0];
+    QBG_TRY(newton_eval(g, W, k, false, ev));
+    lmin = ev.lam;
   }
   *k_out = k;
   *t_out = std::sqrt(std::max(0.0, lmin));
@@ -991,30 +967,8 @@ qbg_status qbg_solve_vect(qbg_geom* g, double k, const double* ds, double* sigma
   const int n = E.n;
   // LU of the adjoint matrix (in E.LU), then C = A^-1 for the block iteration
   QBG_CUDA(cudaMemcpyAsync(E.LU, E.C, sizeof(cxd) * (size_t)n * n, cudaMemcpyDeviceToDevice, E.st));
-  if (cusolverDnCreate(&E.h) != CUSOLVER_STATUS_SUCCESS) return solver_fail("cusolverDnCreate");
-  cusolverDnSetStream(E.h, E.st);
-  QBG_TRY(E.alloc(&E.ipiv, sizeof(int) * n));
-  QBG_TRY(E.alloc(&E.dinfo, sizeof(int)));
-  int lw = 0;
-  if (cusolverDnZgetrf_bufferSize(E.h, n, n, (cuDoubleComplex*)E.LU, n, &lw) != CUSOLVER_STATUS_SUCCESS)
-    return solver_fail("getrf workspace query");
-  cxd* lwork = nullptr;
-  QBG_TRY(E.alloc(&lwork, sizeof(cxd) * (size_t)std::max(lw, 1)));
-  if (cusolverDnZgetrf(E.h, n, n, (cuDoubleComplex*)E.LU, n, (cuDoubleComplex*)lwork, E.ipiv, E.dinfo) !=
-      CUSOLVER_STATUS_SUCCESS)
-    return solver_fail("cusolverDnZgetrf");
-  int hinfo = 0;
-  QBG_CUDA(cudaMemcpyAsync(&hinfo, E.dinfo, sizeof(int), cudaMemcpyDeviceToHost, E.st));
-  QBG_TRY(E.wait());
-  if (hinfo > 0) {
-    set_error("solve_vect: the adjoint Fredholm matrix is exactly singular (U(%d, %d) = 0)", hinfo, hinfo);
-    return QBG_ESINGULAR;
-  }
-  k_identity<<<2048, 256, 0, E.st>>>(E.C, n);
-  QBG_LAUNCH_CHECK("k_identity");
-  if (cusolverDnZgetrs(E.h, CUBLAS_OP_N, n, n, (const cuDoubleComplex*)E.LU, n, E.ipiv, (cuDoubleComplex*)E.C, n,
-                       E.dinfo) != CUSOLVER_STATUS_SUCCESS)
-    return solver_fail("cusolverDnZgetrs");
+  QBG_TRY(E.factor("solve_vect: the adjoint Fredholm matrix"));
+  QBG_TRY(E.D.inverse(E.C));
   // the eigenvalue of largest modulus of A^-1 (smallest_nullvec_krylov!, dlp.jl:991-1004)
   const int nev = 1, p = std::min(n, 12);
   std::vector<zc> mu;

@@ -29,8 +29,10 @@ namespace qbg {
 // Thread (tx, ty): rows tx + 16 a, columns ty + 16 b, so that the 16 lanes
 // with consecutive tx store 16 consecutive rows of a column.
 // Safe for C == B when one M tile covers all of K (used for inv(L11) A12).
+// CA: the A operand is the conjugate transpose of the K x M block stored at A
+// (leading dimension lda), op(A)[i, k] = conj(A[k + i lda]).
 // ---------------------------------------------------------------------------
-template <class T>
+template <class T, bool CA = false>
 __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, cx<T> alpha, const cx<T>* __restrict__ A,
                                               long long lda, long long sA, const cx<T>* B, long long ldb,
                                               long long sB, cx<T> beta, cx<T>* C, long long ldc, long long sC) {
@@ -53,9 +55,15 @@ __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, cx<T> alpha, 
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int idx = tid + q * 256;
-      const int i = idx & (BM - 1), kk = idx >> 6;
-      const int gi = m0 + i, gk = k0 + kk;
-      As[kk][i] = (gi < M && gk < K) ? Ab[(long long)gi + (long long)gk * lda] : cx<T>(0, 0);
+      if (CA) {  // consecutive threads walk k, the contiguous index of the stored block
+        const int kk = idx & (BK - 1), i = idx >> 4;
+        const int gi = m0 + i, gk = k0 + kk;
+        As[kk][i] = (gi < M && gk < K) ? conj(Ab[(long long)gk + (long long)gi * lda]) : cx<T>(0, 0);
+      } else {
+        const int i = idx & (BM - 1), kk = idx >> 6;
+        const int gi = m0 + i, gk = k0 + kk;
+        As[kk][i] = (gi < M && gk < K) ? Ab[(long long)gi + (long long)gk * lda] : cx<T>(0, 0);
+      }
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -104,6 +112,18 @@ int gemm_batched_simt(int M, int N, int K, cx<T> alpha, const cx<T>* A, long lon
   dim3 grd((M + 63) / 64, (N + 63) / 64, batch);
   k_gemm<T><<<grd, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
   QBG_LAUNCH_CHECK("k_gemm");
+  return QBG_OK;
+}
+
+// C = alpha A^H B + beta C, A^H of the K x M blocks stored at A (CUDA-core tiles)
+template <class T>
+int gemm_batched_ah(int M, int N, int K, cx<T> alpha, const cx<T>* A, long long lda, long long sA,
+                           const cx<T>* B, long long ldb, long long sB, cx<T> beta, cx<T>* C, long long ldc,
+                           long long sC, int batch, cudaStream_t st) {
+  if (M <= 0 || N <= 0 || batch <= 0) return QBG_OK;
+  dim3 grd((M + 63) / 64, (N + 63) / 64, batch);
+  k_gemm<T, true><<<grd, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
+  QBG_LAUNCH_CHECK("k_gemm (A^H)");
   return QBG_OK;
 }
 
@@ -739,12 +759,93 @@ static int lu_factor_one(LUBatch<T>& f, cudaStream_t st, cudaEvent_t after_first
 }
 
 template <class T>
+static int lu_trsolve(const LUBatch<T>& f, int L, cx<T>* X, cudaStream_t st);
+
+template <class T>
 static int lu_solve_one(const LUBatch<T>& f, const cx<T>* V, int L, cx<T>* X, long long strideV, cudaStream_t st) {
-  const int n = f.n, nb = f.nb, batch = f.batch;
-  const long long sX = (long long)n * L;
+  const int n = f.n, batch = f.batch;
   dim3 g((unsigned)(((long long)n * L + 255) / 256), batch);
   k_gather_rows<T><<<g, 256, 0, st>>>(V, strideV, f.perm, n, L, X);
   QBG_LAUNCH_CHECK("k_gather_rows");
+  return lu_trsolve<T>(f, L, X, st);
+}
+
+// X = P (the row permutation of the factorisation, as a matrix)
+template <class T>
+__global__ void k_perm_matrix(const int* perm, int n, cx<T>* X) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (e >= (long long)n * n) return;
+  const int i = (int)(e % n), l = (int)(e / n);
+  X[(long long)b * n * n + e] = cx<T>(perm[(long long)b * n + i] == l ? T(1) : T(0), T(0));
+}
+
+// X[perm[i]] = Y[i]: applies P^T to every column
+template <class T>
+__global__ void k_scatter_rows(const cx<T>* Y, const int* perm, int n, int L, cx<T>* X) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (e >= (long long)n * L) return;
+  const int i = (int)(e % n), l = (int)(e / n);
+  X[(long long)b * n * L + perm[(long long)b * n + i] + (long long)l * n] = Y[(long long)b * n * L + e];
+}
+
+template <class T>
+__global__ void k_copy_rhs(const cx<T>* V, long long strideV, int n, int L, cx<T>* X) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (e >= (long long)n * L) return;
+  X[(long long)b * n * L + e] = V[(long long)b * strideV + e];
+}
+
+// A_b^{-1} for every matrix of the batch (X: batch * n * n)
+template <class T>
+int lu_inverse(const LUBatch<T>& f, cx<T>* X, cudaStream_t st) {
+  const int n = f.n;
+  dim3 g((unsigned)(((long long)n * n + 255) / 256), f.batch);
+  k_perm_matrix<T><<<g, 256, 0, st>>>(f.perm, n, X);
+  QBG_LAUNCH_CHECK("k_perm_matrix");
+  return lu_trsolve<T>(f, n, X, st);
+}
+
+// X_b = A_b^{-H} V_b with P A = L U: A^{-H} = P^T L^{-H} U^{-H}. U^H is lower
+// and L^H unit upper; both use the nb x nb diagonal-block inverses of the
+// factorisation (levels 0). Y: scratch of batch * n * L elements.
+template <class T>
+int lu_solve_adjoint(const LUBatch<T>& f, const cx<T>* V, long long strideV, int L, cx<T>* X, cx<T>* Y,
+                     cudaStream_t st) {
+  const int n = f.n, nb = f.nb, batch = f.batch;
+  const long long sY = (long long)n * L;
+  const long long sInv = (long long)f.nblk * nb * nb;
+  const cx<T> one(1, 0), mone(-1, 0), zero(0, 0);
+  dim3 g((unsigned)(((long long)n * L + 255) / 256), batch);
+  k_copy_rhs<T><<<g, 256, 0, st>>>(V, strideV, n, L, Y);
+  QBG_LAUNCH_CHECK("k_copy_rhs");
+  for (int blk = 0; blk < f.nblk; ++blk) {  // U^H y = v, forward
+    const int r0 = blk * nb, w = min(nb, n - r0), rest = n - r0 - w;
+    QBG_TRY(gemm_batched_ah<T>(w, L, w, one, f.Uinv + (long long)blk * nb * nb, nb, sInv, Y + r0, n, sY, zero,
+                               Y + r0, n, sY, batch, st));
+    if (rest > 0)
+      QBG_TRY(gemm_batched_ah<T>(rest, L, w, mone, f.A + r0 + (long long)(r0 + w) * n, n, f.stride, Y + r0, n, sY,
+                                 one, Y + r0 + w, n, sY, batch, st));
+  }
+  for (int blk = f.nblk - 1; blk >= 0; --blk) {  // L^H x = y, backward
+    const int r0 = blk * nb;
+    const int w = min(nb, n - r0);
+    QBG_TRY(gemm_batched_ah<T>(w, L, w, one, f.Linv + (long long)blk * nb * nb, nb, sInv, Y + r0, n, sY, zero,
+                               Y + r0, n, sY, batch, st));
+    if (r0 > 0)
+      QBG_TRY(gemm_batched_ah<T>(r0, L, w, mone, f.A + r0, n, f.stride, Y + r0, n, sY, one, Y, n, sY, batch, st));
+  }
+  k_scatter_rows<T><<<g, 256, 0, st>>>(Y, f.perm, n, L, X);
+  QBG_LAUNCH_CHECK("k_scatter_rows");
+  return QBG_OK;
+}
+
+template <class T>
+static int lu_trsolve(const LUBatch<T>& f, int L, cx<T>* X, cudaStream_t st) {
+  const int n = f.n, nb = f.nb, batch = f.batch;
+  const long long sX = (long long)n * L;
   if (f.levels > 0) {
     // blocks of nbs rows; forward: Y_b = Linv_b X_b, X_rest -= L_rest,b Y_b;
     // backward: X_b = Uinv_b Y_b, Y_above -= U_above,b X_b (no in-place products)
@@ -1176,6 +1277,10 @@ int lu_solve_shared(const LUBatch<T>& f, const cx<T>* V, int L, cx<T>* X, long l
 }
 
 template int lu_factor<double>(LUBatch<double>&, cudaStream_t);
+template int lu_inverse<double>(const LUBatch<double>&, cxd*, cudaStream_t);
+template int gemm_batched_ah<double>(int, int, int, cxd, const cxd*, long long, long long, const cxd*, long long,
+                                     long long, cxd, cxd*, long long, long long, int, cudaStream_t);
+template int lu_solve_adjoint<double>(const LUBatch<double>&, const cxd*, long long, int, cxd*, cxd*, cudaStream_t);
 
 template size_t lu_solve_blocks_bytes<double>(LUBatch<double>&, int, int);
 template size_t lu_solve_blocks_bytes<float>(LUBatch<float>&, int, int);

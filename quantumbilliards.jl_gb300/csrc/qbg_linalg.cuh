@@ -53,11 +53,28 @@ int lu_factor(LUBatch<T>& f, cudaStream_t st);
 template <class T>
 int lu_solve_shared(const LUBatch<T>& f, const cx<T>* V, int L, cx<T>* X, long long strideV, cudaStream_t st);
 
+// A_b^{-1} of every matrix (X: batch * n * n, column-major). levels == 0.
+template <class T>
+int lu_inverse(const LUBatch<T>& f, cx<T>* X, cudaStream_t st);
+
+// X_b = A_b^{-H} V_b (V_b = V + b strideV, n x L; X, Y: batch * n * L; Y is
+// scratch). levels == 0.
+template <class T>
+int lu_solve_adjoint(const LUBatch<T>& f, const cx<T>* V, long long strideV, int L, cx<T>* X, cx<T>* Y,
+                     cudaStream_t st);
+
 // Batched complex GEMM: C = alpha A B + beta C.
 template <class T>
 int gemm_batched(int M, int N, int K, cx<T> alpha, const cx<T>* A, long long lda, long long sA, const cx<T>* B,
                  long long ldb, long long sB, cx<T> beta, cx<T>* C, long long ldc, long long sC, int batch,
                  cudaStream_t st);
+
+// C = alpha A^H B + beta C with A^H the conjugate transpose of the K x M
+// blocks stored at A (CUDA-core tiles).
+template <class T>
+int gemm_batched_ah(int M, int N, int K, cx<T> alpha, const cx<T>* A, long long lda, long long sA, const cx<T>* B,
+                    long long ldb, long long sB, cx<T> beta, cx<T>* C, long long ldc, long long sC, int batch,
+                    cudaStream_t st);
 
 // The CUDA-core (FMA) tile GEMM, whatever the engine setting.
 template <class T>
