@@ -74,8 +74,11 @@ typedef struct qbg_geom_desc {
   const double* ddy;
   const double* ts;             /* n computational parameters sigma (Kress log term) */
   const double* ws;             /* n quadrature weights */
-  /* optional symmetry reduction for DLP (DLPKressReducedWorkspace, dlp_kress.jl:65-78):
-   * m fundamental nodes, each with norb images (its own index included) */
+  /* optional symmetry reduction (DLP: DLPKressReducedWorkspace, dlp_kress.jl:65-78,
+   * the Kress-split entry at (I_a, I_b) plus regular image kernels; CFIE: the
+   * reduced workspace of cfie_kress.jl:212-316, sum over the orbit of the
+   * Kress-split entries, cfie_kress.jl:512-617): m fundamental nodes, each with
+   * norb images (its own index included) */
   int64_t m;                    /* 0 = no reduction */
   int32_t norb;
   const int64_t* fund;          /* m full indices I_a */

@@ -8,6 +8,7 @@ Follows:
 * CFIE construct_matrices!               cfie_kress.jl:416-510, derivatives :619-757
 * symmetry orbits                        symmetry.jl:214-319
 * reduced DLP (images)                   dlp_kress.jl:1081-1100, 1151-1189, 1293-1345
+* reduced CFIE (orbit sums)              cfie_kress.jl:512-617, 758-892
 * complex-k multi-k CFIE (Chebyshev)     chebyshev_euclidian_helmholtz_cfie_kress.jl:543-666
 * complex-k DLP (Chebyshev)              chebyshev_euclidian_helmholtz_dlp_kress.jl:702-769
 
@@ -337,6 +338,24 @@ def dlp_fredholm_reduced(p, k, orbits, derivs: bool = False, funcs=None, image_h
             F1 -= np.where(mask, sc * 0.5j * c * (kr * h0) * wq, 0.0)
             F2 -= np.where(mask, sc * 0.5j * c * (rs * h0 - k * rs ** 2 * h1) * wq, 0.0)
     return (F, F1, F2) if derivs else F
+
+
+def cfie_reduced(pts, k, orbits, derivs=False, full=None):
+    """Reduced CFIE on the fundamental indices (construct_matrices_reduced!,
+    cfie_kress.jl:512-617; derivatives :758-892): A_red[a, b] = sum over the
+    members q of orbit b of scale_q A[I_a, q], every term the full Kress-split
+    entry (the diagonal formula at q == I_a). ``full`` optionally supplies the
+    full operator (or the (A, A', A'') triple) already assembled."""
+    fund, fullidx, scale = orbits
+    mats = full if full is not None else (cfie_matrix_derivs(pts, k) if derivs else cfie_matrix(pts, k))
+    mats = mats if isinstance(mats, tuple) else (mats,)
+    out = []
+    for M in mats:
+        R = np.zeros((len(fund), len(fund)), dtype=np.complex128)
+        for l in range(fullidx.shape[1]):
+            R += M[np.ix_(fund, fullidx[:, l])] * scale[:, l][None, :]
+        out.append(R)
+    return tuple(out) if derivs else out[0]
 
 
 def assemble(kind, pts, k, derivs=False):

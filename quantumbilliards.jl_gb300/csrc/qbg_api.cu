@@ -129,8 +129,8 @@ qbg_status qbg_geom_create(const qbg_geom_desc* desc, qbg_geom** out) {
   d.kcol = kcol;
   d.m = (int)n;
   if (desc->m > 0) {
-    if (desc->form != QBG_FORM_DLP || desc->norb < 1 || !desc->fund || !desc->orbit || !desc->orbit_scale ||
-        desc->m > n) {
+    if ((desc->form != QBG_FORM_DLP && desc->form != QBG_FORM_CFIE) || desc->norb < 1 || !desc->fund ||
+        !desc->orbit || !desc->orbit_scale || desc->m > n) {
       delete g;
       set_error("qbg_geom_create: invalid symmetry reduction arguments");
       return QBG_EINVAL;

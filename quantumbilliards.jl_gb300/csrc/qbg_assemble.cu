@@ -833,6 +833,112 @@ __global__ void __launch_bounds__(256) k_assemble_cheb_reduced(GeomDev g, ChebTa
 }
 
 // ---------------------------------------------------------------------------
+// Symmetry-reduced CFIE (construct_matrices_reduced!, cfie_kress.jl:512-617;
+// derivatives :758-892; through the panels,
+// chebyshev_euclidian_helmholtz_cfie_kress.jl:698-825 and :1087-1243):
+// A_red[a, b] = sum over the members j of orbit b of scale_j A_full[I_a, j],
+// with A_full the Kress-split CFIE entry (the diagonal formula when j == I_a,
+// the smooth cross-component kernel between components). Unlike the reduced
+// DLP, every member of the orbit carries the full Kress split. CHEB: H0, H1
+// from the panels (direct below r_min or the small-|z| cut-off), J0, J1
+// from the panels; otherwise direct device Bessel values (J = Re H at real k).
+// ---------------------------------------------------------------------------
+template <int CHEB>
+static __device__ __forceinline__ void hj_values(const ChebTables& t, int q, double r, cxd k, bool needj,
+                                                 cxd& h0, cxd& h1, cxd& j0, cxd& j1) {
+  if (CHEB) {
+    cheb_h01(t, q, r, k, h0, h1);
+    if (needj) {
+      int pj;
+      double tj;
+      panel_of(r, 0.0, t.rmax, t.dr_j, t.invdr_j, t.nj, pj, tj);
+      clenshaw2(t.J + (((size_t)q * t.nj + pj) * (t.Mj + 1)) * 2, t.Mj, tj, j0, j1);
+    } else {
+      j0 = cxd(0.0, 0.0);
+      j1 = cxd(0.0, 0.0);
+    }
+  } else {
+    Bessel01d b = bessel01(r * k);
+    if (k.im == 0.0) {
+      b.j0.im = 0.0;
+      b.j1.im = 0.0;
+    }
+    h0 = b.h0();
+    h1 = b.h1();
+    j0 = b.j0;
+    j1 = b.j1;
+  }
+}
+
+template <int DERIV, int OUT, int CHEB>
+__global__ void __launch_bounds__(256) k_assemble_cfie_reduced(GeomDev g, ChebTables t, const cxd* __restrict__ ks,
+                                                               int nk, int kchunk, void* const* __restrict__ outs,
+                                                               void* const* __restrict__ los, long long ld) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const int bcol = blockIdx.y * blockDim.y + threadIdx.y;
+  if (a >= g.m || bcol >= g.m) return;
+  const int q0 = blockIdx.z * kchunk, q1 = min(nk, q0 + kchunk);
+  const int i = g.fund[a];
+  const size_t off = (size_t)a + (size_t)bcol * (size_t)ld;
+  for (int q = q0; q < q1; ++q) {
+    const cxd k = ks[q];
+    cxd F(0.0, 0.0), F1(0.0, 0.0), F2(0.0, 0.0);
+    for (int l = 0; l < g.norb; ++l) {
+      const int j = g.orb[bcol * g.norb + l];
+      const cxd sc(g.orb_scale[2 * (bcol * g.norb + l)], g.orb_scale[2 * (bcol * g.norb + l) + 1]);
+      cxd e, e1(0.0, 0.0), e2(0.0, 0.0);
+      if (j == i) {
+        e = diag_fp64<1>(g, i, k);
+        if (DERIV) diag_derivs<1>(g, i, k, &e1, &e2);
+      } else {
+        const PairGeom p = pair_geom(g, i, j);
+        if (!CHEB && !p.same && p.r * p.r <= 4.93038065763132e-32) continue;  // eps(T)^2 guard, cfie_kress.jl:569
+        cxd h0, h1, j0, j1;
+        hj_values<CHEB>(t, q, p.r, k, p.same, h0, h1, j0, j1);
+        entry_vals<1, DERIV>(p, k, h0, h1, j0, j1, &e, &e1, &e2);
+      }
+      F += sc * e;
+      if (DERIV) {
+        F1 += sc * e1;
+        F2 += sc * e2;
+      }
+    }
+    store_entry<OUT>(outs, los, q, off, F);
+    if (DERIV) {
+      store_entry<OUT>(outs, los, nk + q, off, F1);
+      store_entry<OUT>(outs, los, 2 * nk + q, off, F2);
+    }
+  }
+}
+
+// reduced CFIE launcher: cheb == nullptr evaluates the kernels directly;
+// prec QBG_PREC_FP32 writes complex64 values without low words
+static int launch_cfie_reduced(const GeomDev& g, const ChebTables* cheb, const cxd* ks, int nk, int deriv, int prec,
+                               void* const* outs_dev, void* const* lo_outs_dev, long long ld, cudaStream_t st) {
+  const int kchunk = 8;
+  dim3 blk(32, 8), grd((g.m + 31) / 32, (g.m + 7) / 8, (nk + kchunk - 1) / kchunk);
+  const ChebTables t0 = cheb ? *cheb : ChebTables();
+  void* const* lo = prec == QBG_PREC_MIXED ? lo_outs_dev : nullptr;
+#define QBG_CFR(D, O, C) k_assemble_cfie_reduced<D, O, C><<<grd, blk, 0, st>>>(g, t0, ks, nk, kchunk, outs_dev, lo, ld)
+  if (prec == QBG_PREC_FP64) {
+    if (cheb) {
+      if (deriv) QBG_CFR(1, 0, 1); else QBG_CFR(0, 0, 1);
+    } else {
+      if (deriv) QBG_CFR(1, 0, 0); else QBG_CFR(0, 0, 0);
+    }
+  } else {
+    if (deriv) {
+      set_error("derivative assembly is available in FP64");
+      return QBG_ENOTSUP;
+    }
+    if (cheb) QBG_CFR(0, 1, 1); else QBG_CFR(0, 1, 0);
+  }
+#undef QBG_CFR
+  QBG_LAUNCH_CHECK("k_assemble_cfie_reduced");
+  return QBG_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Symmetric-pair Chebyshev assembly (value only, no derivatives).
 // The kernel values of (i, j) and (j, i) depend on the pair only through r, so
 // one panel evaluation serves both entries. With the pair coefficients folded,
@@ -1554,10 +1660,7 @@ int launch_assemble_cheb(const GeomDev& g, const ChebTables& t, const cxd* ks, i
   }
   const int kchunk = 8;
   if (g.m != g.n) {
-    if (g.form != 0) {
-      set_error("symmetry reduction is built for the DLP formulation");
-      return QBG_ENOTSUP;
-    }
+    if (g.form != 0) return launch_cfie_reduced(g, &t, ks, nk, deriv, prec, outs_dev, lo_outs_dev, ld, st);
     dim3 blk(32, 8), grd((g.m + 31) / 32, (g.m + 7) / 8, (nk + kchunk - 1) / kchunk);
     if (prec == QBG_PREC_FP64) {
       if (deriv)
@@ -1648,10 +1751,7 @@ int launch_assemble(const GeomDev& g, const cxd* ks, int nk, int deriv, int prec
   dim3 grd((dim + 31) / 32, (dim + 7) / 8);
   if (g.quad == 1) return launch_alpert(g, ks, nk, deriv, prec, outs_dev, ld, st, lo_outs_dev);
   if (reduced) {
-    if (g.form != 0) {
-      set_error("symmetry reduction is built for the DLP formulation");
-      return QBG_ENOTSUP;
-    }
+    if (g.form != 0) return launch_cfie_reduced(g, nullptr, ks, nk, deriv, prec, outs_dev, lo_outs_dev, ld, st);
     if (deriv && prec != QBG_PREC_FP64) {
       set_error("derivative assembly is available in FP64");
       return QBG_ENOTSUP;

@@ -95,13 +95,75 @@ def periodic_symmetry_index_orbits(N: int, sym):
     return np.arange(m, dtype=np.int64), full, scale
 
 
+def _match(targets, xy, tol):
+    """Index of the node of xy at each target position (within tol)."""
+    from scipy.spatial import cKDTree
+    d, idx = cKDTree(xy).query(targets)
+    if np.any(d > tol):
+        raise ValueError("the symmetry does not map the boundary nodes onto each other "
+                         f"(largest mismatch {float(d.max()):.3e})")
+    return idx.astype(np.int64)
+
+
+def geometric_orbits(xy, sym, tol=1e-10):
+    """Orbits of the global nodes of a CFIE workspace (build_cfie_kress_workspace,
+    cfie_kress.jl:264-289 with build_symmetry_maps / apply_symmetry_orbit_from_maps,
+    symmetry.jl:746-800): every group element maps each node to the node at
+    its image position; the nodes are visited in global order and each
+    unvisited node opens an orbit [g, images...] with scales [1, characters...].
+    Returns (fund, fund_to_full [m x norb], fund_to_scale [m x norb]), 0-based."""
+    xy = np.asarray(xy, dtype=np.float64)
+    x, y = xy[:, 0], xy[:, 1]
+    if isinstance(sym, Reflection):
+        if sym.axis == "y_axis":
+            maps = [_match(np.stack([-x, y], 1), xy, tol)]
+            sc = [1.0, float(sym.parity[0])]
+        elif sym.axis == "x_axis":
+            maps = [_match(np.stack([x, -y], 1), xy, tol)]
+            sc = [1.0, float(sym.parity[0])]
+        elif sym.axis == "origin":
+            px, py = float(sym.parity[0]), float(sym.parity[1])
+            maps = [_match(np.stack([-x, y], 1), xy, tol), _match(np.stack([x, -y], 1), xy, tol),
+                    _match(np.stack([-x, -y], 1), xy, tol)]
+            sc = [1.0, px, py, px * py]
+        else:
+            raise ValueError(f"unsupported reflection axis {sym.axis}")
+        scales = np.asarray(sc, dtype=np.complex128)
+    elif isinstance(sym, Rotation):
+        n = int(sym.n)
+        maps = []
+        for l in range(1, n):
+            c, s = math.cos(2 * math.pi * l / n), math.sin(2 * math.pi * l / n)
+            maps.append(_match(np.stack([c * x - s * y, s * x + c * y], 1), xy, max(tol, 1e-8)))
+        scales = np.asarray([complex(math.cos(2 * math.pi * sym.m * l / n), math.sin(2 * math.pi * sym.m * l / n))
+                             for l in range(n)], dtype=np.complex128)
+    else:
+        raise TypeError("symmetry must be a Reflection or a Rotation")
+    N = len(xy)
+    visited = np.zeros(N, dtype=bool)
+    fund, full = [], []
+    for g in range(N):
+        if visited[g]:
+            continue
+        orb = [g] + [int(mp[g]) for mp in maps]
+        fund.append(g)
+        full.append(orb)
+        visited[orb] = True
+    full = np.asarray(full, dtype=np.int64)
+    return (np.asarray(fund, dtype=np.int64), full,
+            np.broadcast_to(scales, full.shape).astype(np.complex128))
+
+
 def reduction(solver, pts):
     """Orbit maps for a solver with a symmetry, or None (the reduced workspace
-    is used exactly when the solver has a symmetry, dlp_kress.jl:234)."""
+    is used exactly when the solver has a symmetry, dlp_kress.jl:234,
+    cfie_kress.jl:264-289). DLP: the periodic index orbits of the one
+    component (symmetry.jl:214-261). CFIE: the geometric orbits of all the
+    global nodes (geometric_orbits)."""
     if getattr(solver, "symmetry", None) is None:
         return None
-    if solver.kind != "dlp":
-        raise NotImplementedError("symmetry reduction is built for the DLP formulation "
-                                  "(DLPKressReducedWorkspace, dlp_kress.jl:65-78)")
-    p = pts[0] if isinstance(pts, list) else pts
-    return periodic_symmetry_index_orbits(p.n, solver.symmetry)
+    sym = solver.symmetry
+    plist = pts if isinstance(pts, list) else [pts]
+    if solver.kind == "dlp":
+        return periodic_symmetry_index_orbits(plist[0].n, sym)
+    return geometric_orbits(np.concatenate([np.asarray(p.xy) for p in plist]), sym)
