@@ -389,184 +389,6 @@ __global__ void __launch_bounds__(256) k_assemble_dlp_reduced(GeomDev g, const c
   }
 }
 
-// ---------------------------------------------------------------------------
-// CFIE with Alpert quadrature (cfie_alpert.jl:947-1087 self blocks,
-// 1261-1350 off-component blocks). Kernel terms with weight w
-// (cfie_alpert.jl:233-287):
-//   d0 = w (ik/2) inner H1 / r, d1 = w (i/2) inner k H0, d2 = w (i/2) inner (H0 - k r H1),
-//   s0 = w (i/2) H0 s, s1 = -w (i/2) r H1 s, s2 = w (i/2) r (H1 - k r H0) s / k;
-// an entry loses d0 + ik s0, its k-derivatives d1 + i s0 + ik s1 and
-// d2 + 2i s1 + ik s2. The self block keeps the identity, drops the trapezoid
-// band |i - j| < a and gets the correction nodes' terms spread over the
-// interpolation stencil.
-// ---------------------------------------------------------------------------
-struct AlpTerms {
-  cxd v0, v1, v2;
-};
-
-template <int DERIV>
-static __device__ __forceinline__ AlpTerms alpert_terms(cxd k, double r, double inn, double s, double w) {
-  const Bessel01d b = bessel01(r * k);
-  const cxd h0 = b.h0(), h1 = b.h1();
-  const cxd ik = cmul_i(k);
-  const cxd d0 = (w * inn / r) * cmul_i(0.5 * (k * h1));
-  const cxd s0 = (w * s) * cmul_i(0.5 * h0);
-  AlpTerms t;
-  t.v0 = d0 + ik * s0;
-  if (DERIV) {
-    const cxd kr = r * k;
-    const cxd d1 = (w * inn) * cmul_i(0.5 * (k * h0));
-    const cxd d2 = (w * inn) * cmul_i(0.5 * (h0 - kr * h1));
-    const cxd s1 = (w * s * r) * cmul_i(-0.5 * h1);
-    const cxd s2 = cmul_i(0.5 * (w * s * r) * (h1 - kr * h0)) / k;
-    t.v1 = d1 + cmul_i(s0) + ik * s1;
-    t.v2 = d2 + cmul_i(2.0 * s1) + ik * s2;
-  } else {
-    t.v1 = t.v2 = cxd(0.0, 0.0);
-  }
-  return t;
-}
-
-template <int DERIV>
-__global__ void __launch_bounds__(256) k_assemble_alpert(GeomDev g, const cxd* __restrict__ ks, int nk,
-                                                         cxd* const* __restrict__ outs, long long ld) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.n || j >= g.n) return;
-  const size_t off = (size_t)i + (size_t)j * (size_t)ld;
-  bool zero = false;
-  double r = 0.0, inn = 0.0;
-  if (i != j) {
-    const int ci = g.comp[i], cj = g.comp[j];
-    const double dx = g.x[i] - g.x[j], dy = g.y[i] - g.y[j];
-    const double r2 = dx * dx + dy * dy;
-    if (ci == cj) {
-      const int na = g.coff[ci + 1] - g.coff[ci];
-      int d = abs(g.lidx[i] - g.lidx[j]);
-      d = min(d, na - d);
-      zero = d < g.aa;  // trapezoid band replaced by the correction nodes
-    } else {
-      zero = r2 <= 4.93038065763132e-32;
-    }
-    r = sqrt(r2);
-    inn = g.dy[j] * dx - g.dx[j] * dy;
-  }
-  for (int q = 0; q < nk; ++q) {
-    cxd F(0.0, 0.0), F1(0.0, 0.0), F2(0.0, 0.0);
-    if (i == j) {
-      F = cxd(1.0, 0.0);
-    } else if (!zero) {
-      const AlpTerms t = alpert_terms<DERIV>(ks[q], r, inn, g.speed[j], g.ws[j]);
-      F = -t.v0;
-      F1 = -t.v1;
-      F2 = -t.v2;
-    }
-    outs[q][off] = F;
-    if (DERIV) {
-      outs[nk + q][off] = F1;
-      outs[2 * nk + q][off] = F2;
-    }
-  }
-}
-
-// one thread per (row, wavenumber): the row's correction nodes, scattered into
-// its own row only, so no two threads touch one entry
-template <int DERIV>
-__global__ void __launch_bounds__(128) k_alpert_corrections(GeomDev g, const cxd* __restrict__ ks, int nk,
-                                                            cxd* const* __restrict__ outs, long long ld) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int q = blockIdx.y;
-  if (i >= g.n || q >= nk) return;
-  const int c = g.comp[i], o = g.coff[c], na = g.coff[c + 1] - o, li = g.lidx[i];
-  const double h = g.ws[o];
-  const cxd k = ks[q];
-  const size_t n = (size_t)g.n, plane = (size_t)g.aj * n;
-  for (int p = 0; p < g.aj; ++p) {
-    const double fac = h * g.aw[p];
-    for (int side = 0; side < 2; ++side) {
-      const double r = g.anodes[(size_t)side * plane + (size_t)p * n + i];
-      if (!isfinite(r)) continue;
-      const double inn = g.anodes[(size_t)(2 + side) * plane + (size_t)p * n + i];
-      const double sp = g.anodes[(size_t)(4 + side) * plane + (size_t)p * n + i];
-      const AlpTerms t = alpert_terms<DERIV>(k, r, inn, sp, fac);
-      const int* so = g.aoff + ((size_t)side * g.aj + p) * g.ani;
-      const double* sw = g.awt + ((size_t)side * g.aj + p) * g.ani;
-      for (int m = 0; m < g.ani; ++m) {
-        int col = (li + so[m]) % na;
-        col += col < 0 ? na : 0;
-        const size_t e = (size_t)i + (size_t)(o + col) * (size_t)ld;
-        outs[q][e] -= sw[m] * t.v0;
-        if (DERIV) {
-          outs[nk + q][e] -= sw[m] * t.v1;
-          outs[2 * nk + q][e] -= sw[m] * t.v2;
-        }
-      }
-    }
-  }
-}
-
-// complex128 staging -> complex64 hi (+ lo) through the output pointer table
-__global__ void k_split_slots(const cxd* __restrict__ src, long long count, int q0, int cnt, void* const* his,
-                              void* const* los) {
-  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int q = blockIdx.y;
-  if (e >= count || q >= cnt) return;
-  const cxd v = src[(size_t)q * count + e];
-  const cxf hi(v);
-  reinterpret_cast<cxf*>(his[q0 + q])[e] = hi;
-  if (los) reinterpret_cast<cxf*>(los[q0 + q])[e] = cxf((float)(v.re - (double)hi.re), (float)(v.im - (double)hi.im));
-}
-
-static int launch_alpert(const GeomDev& g, const cxd* ks, int nk, int deriv, int prec, void* const* outs_dev,
-                         long long ld, cudaStream_t st, void* const* lo_outs_dev) {
-  dim3 blk(32, 8), grd((g.n + 31) / 32, (g.n + 7) / 8);
-  if (prec == QBG_PREC_FP64) {
-    if (deriv)
-      k_assemble_alpert<1><<<grd, blk, 0, st>>>(g, ks, nk, (cxd* const*)outs_dev, ld);
-    else
-      k_assemble_alpert<0><<<grd, blk, 0, st>>>(g, ks, nk, (cxd* const*)outs_dev, ld);
-    QBG_LAUNCH_CHECK("k_assemble_alpert");
-    dim3 cg((g.n + 127) / 128, nk);
-    if (deriv)
-      k_alpert_corrections<1><<<cg, 128, 0, st>>>(g, ks, nk, (cxd* const*)outs_dev, ld);
-    else
-      k_alpert_corrections<0><<<cg, 128, 0, st>>>(g, ks, nk, (cxd* const*)outs_dev, ld);
-    QBG_LAUNCH_CHECK("k_alpert_corrections");
-    return QBG_OK;
-  }
-  if (deriv) {
-    set_error("derivative assembly is available in FP64");
-    return QBG_ENOTSUP;
-  }
-  // complex64 forms: the corrections accumulate into FP64 entries, so groups
-  // of wavenumbers are assembled in FP64 staging and then split
-  const int grp = nk < 4 ? nk : 4;
-  const long long count = (long long)g.n * ld;
-  cxd* stage = nullptr;
-  cxd** dp = nullptr;
-  QBG_TRY(dmalloc(&stage, sizeof(cxd) * (size_t)count * grp));
-  if (int sa = dmalloc(&dp, sizeof(cxd*) * grp)) { dfree(stage, st); return sa; }
-  std::vector<cxd*> hp(grp);
-  for (int q = 0; q < grp; ++q) hp[q] = stage + (size_t)q * count;
-  cudaError_t e = cudaMemcpyAsync(dp, hp.data(), sizeof(cxd*) * grp, cudaMemcpyHostToDevice, st);
-  int s = e == cudaSuccess ? QBG_OK : cuda_status(e, "Alpert staging pointers");
-  for (int q0 = 0; !s && q0 < nk; q0 += grp) {
-    const int c = nk - q0 < grp ? nk - q0 : grp;
-    s = launch_alpert(g, ks + q0, c, 0, QBG_PREC_FP64, (void* const*)dp, ld, st, nullptr);
-    if (!s) {
-      dim3 sg((unsigned)((count + 255) / 256), c);
-      k_split_slots<<<sg, 256, 0, st>>>(stage, count, q0, c, outs_dev,
-                                        prec == QBG_PREC_MIXED ? lo_outs_dev : nullptr);
-      QBG_LAUNCH_CHECK("k_split_slots");
-    }
-  }
-  e = cudaStreamSynchronize(st);  // the staging buffers are freed below
-  dfree(stage, st);
-  dfree(dp, st);
-  if (s) return s;
-  if (e != cudaSuccess) return cuda_status(e, "Alpert assembly");
-  return QBG_OK;
-}
 
 // ---------------------------------------------------------------------------
 // Kress first column per component: c_m = -(4 pi/N) sum_{p=1}^{n-1} cos(2 pi p m/N)/p
@@ -781,6 +603,211 @@ static __device__ __forceinline__ void cheb_h01(const ChebTables& t, int q, doub
   double th;
   panel_of(r, t.rmin, t.rmax, t.dr_h, t.invdr_h, t.nh, ph, th);
   clenshaw2(t.H + (((size_t)q * t.nh + ph) * (t.Mh + 1)) * 2, t.Mh, th, h0, h1);
+}
+
+// ---------------------------------------------------------------------------
+// CFIE with Alpert quadrature (cfie_alpert.jl:947-1087 self blocks,
+// 1261-1350 off-component blocks; through the panels,
+// chebyshev_euclidian_helmholtz_cfie_alpert.jl:533-1253). Kernel terms with
+// weight w (cfie_alpert.jl:233-287):
+//   d0 = w (ik/2) inner H1 / r, d1 = w (i/2) inner k H0, d2 = w (i/2) inner (H0 - k r H1),
+//   s0 = w (i/2) H0 s, s1 = -w (i/2) r H1 s, s2 = w (i/2) r (H1 - k r H0) s / k;
+// an entry loses d0 + ik s0, its k-derivatives d1 + i s0 + ik s1 and
+// d2 + 2i s1 + ik s2. The self block keeps the identity, drops the trapezoid
+// band |i - j| < a and gets the correction nodes' terms spread over the
+// interpolation stencil.
+// ---------------------------------------------------------------------------
+struct AlpTerms {
+  cxd v0, v1, v2;
+};
+
+// H0, H1 at k r: the device Bessel routines, or (CHEB) the Chebyshev panels of
+// wavenumber slot q (direct below r_min or the small-|z| cut-off; the Alpert
+// route interpolates H only, chebyshev_euclidian_helmholtz_cfie_alpert.jl:404-470)
+template <int CHEB>
+static __device__ __forceinline__ void alpert_h01(const ChebTables& t, int q, cxd k, double r, cxd& h0, cxd& h1) {
+  if (CHEB) {
+    cheb_h01(t, q, r, k, h0, h1);
+  } else {
+    const Bessel01d b = bessel01(r * k);
+    h0 = b.h0();
+    h1 = b.h1();
+  }
+}
+
+template <int DERIV, int CHEB>
+static __device__ __forceinline__ AlpTerms alpert_terms(const ChebTables& tb, int q, cxd k, double r, double inn,
+                                                        double s, double w) {
+  cxd h0, h1;
+  alpert_h01<CHEB>(tb, q, k, r, h0, h1);
+  const cxd ik = cmul_i(k);
+  const cxd d0 = (w * inn / r) * cmul_i(0.5 * (k * h1));
+  const cxd s0 = (w * s) * cmul_i(0.5 * h0);
+  AlpTerms t;
+  t.v0 = d0 + ik * s0;
+  if (DERIV) {
+    const cxd kr = r * k;
+    const cxd d1 = (w * inn) * cmul_i(0.5 * (k * h0));
+    const cxd d2 = (w * inn) * cmul_i(0.5 * (h0 - kr * h1));
+    const cxd s1 = (w * s * r) * cmul_i(-0.5 * h1);
+    const cxd s2 = cmul_i(0.5 * (w * s * r) * (h1 - kr * h0)) / k;
+    t.v1 = d1 + cmul_i(s0) + ik * s1;
+    t.v2 = d2 + cmul_i(2.0 * s1) + ik * s2;
+  } else {
+    t.v1 = t.v2 = cxd(0.0, 0.0);
+  }
+  return t;
+}
+
+template <int DERIV, int CHEB>
+__global__ void __launch_bounds__(256) k_assemble_alpert(GeomDev g, ChebTables tb, const cxd* __restrict__ ks,
+                                                         int nk, cxd* const* __restrict__ outs, long long ld) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.n || j >= g.n) return;
+  const size_t off = (size_t)i + (size_t)j * (size_t)ld;
+  bool zero = false;
+  double r = 0.0, inn = 0.0;
+  if (i != j) {
+    const int ci = g.comp[i], cj = g.comp[j];
+    const double dx = g.x[i] - g.x[j], dy = g.y[i] - g.y[j];
+    const double r2 = dx * dx + dy * dy;
+    if (ci == cj) {
+      const int na = g.coff[ci + 1] - g.coff[ci];
+      int d = abs(g.lidx[i] - g.lidx[j]);
+      d = min(d, na - d);
+      zero = d < g.aa;  // trapezoid band replaced by the correction nodes
+    } else {
+      zero = r2 <= 4.93038065763132e-32;
+    }
+    r = sqrt(r2);
+    inn = g.dy[j] * dx - g.dx[j] * dy;
+  }
+  for (int q = 0; q < nk; ++q) {
+    cxd F(0.0, 0.0), F1(0.0, 0.0), F2(0.0, 0.0);
+    if (i == j) {
+      F = cxd(1.0, 0.0);
+    } else if (!zero) {
+      const AlpTerms t = alpert_terms<DERIV, CHEB>(tb, q, ks[q], r, inn, g.speed[j], g.ws[j]);
+      F = -t.v0;
+      F1 = -t.v1;
+      F2 = -t.v2;
+    }
+    outs[q][off] = F;
+    if (DERIV) {
+      outs[nk + q][off] = F1;
+      outs[2 * nk + q][off] = F2;
+    }
+  }
+}
+
+// one thread per (row, wavenumber): the row's correction nodes, scattered into
+// its own row only, so no two threads touch one entry
+template <int DERIV, int CHEB>
+__global__ void __launch_bounds__(128) k_alpert_corrections(GeomDev g, ChebTables tb, const cxd* __restrict__ ks,
+                                                            int nk, cxd* const* __restrict__ outs, long long ld) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int q = blockIdx.y;
+  if (i >= g.n || q >= nk) return;
+  const int c = g.comp[i], o = g.coff[c], na = g.coff[c + 1] - o, li = g.lidx[i];
+  const double h = g.ws[o];
+  const cxd k = ks[q];
+  const size_t n = (size_t)g.n, plane = (size_t)g.aj * n;
+  for (int p = 0; p < g.aj; ++p) {
+    const double fac = h * g.aw[p];
+    for (int side = 0; side < 2; ++side) {
+      const double r = g.anodes[(size_t)side * plane + (size_t)p * n + i];
+      if (!isfinite(r)) continue;
+      const double inn = g.anodes[(size_t)(2 + side) * plane + (size_t)p * n + i];
+      const double sp = g.anodes[(size_t)(4 + side) * plane + (size_t)p * n + i];
+      const AlpTerms t = alpert_terms<DERIV, CHEB>(tb, q, k, r, inn, sp, fac);
+      const int* so = g.aoff + ((size_t)side * g.aj + p) * g.ani;
+      const double* sw = g.awt + ((size_t)side * g.aj + p) * g.ani;
+      for (int m = 0; m < g.ani; ++m) {
+        int col = (li + so[m]) % na;
+        col += col < 0 ? na : 0;
+        const size_t e = (size_t)i + (size_t)(o + col) * (size_t)ld;
+        outs[q][e] -= sw[m] * t.v0;
+        if (DERIV) {
+          outs[nk + q][e] -= sw[m] * t.v1;
+          outs[2 * nk + q][e] -= sw[m] * t.v2;
+        }
+      }
+    }
+  }
+}
+
+// complex128 staging -> complex64 hi (+ lo) through the output pointer table
+__global__ void k_split_slots(const cxd* __restrict__ src, long long count, int q0, int cnt, void* const* his,
+                              void* const* los) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int q = blockIdx.y;
+  if (e >= count || q >= cnt) return;
+  const cxd v = src[(size_t)q * count + e];
+  const cxf hi(v);
+  reinterpret_cast<cxf*>(his[q0 + q])[e] = hi;
+  if (los) reinterpret_cast<cxf*>(los[q0 + q])[e] = cxf((float)(v.re - (double)hi.re), (float)(v.im - (double)hi.im));
+}
+
+// cheb == nullptr: direct Hankel values; otherwise the panels of `cheb`
+static int launch_alpert(const GeomDev& g, const ChebTables* cheb, const cxd* ks, int nk, int deriv, int prec,
+                         void* const* outs_dev, long long ld, cudaStream_t st, void* const* lo_outs_dev) {
+  dim3 blk(32, 8), grd((g.n + 31) / 32, (g.n + 7) / 8);
+  const ChebTables tb = cheb ? *cheb : ChebTables();
+  if (prec == QBG_PREC_FP64) {
+    dim3 cg((g.n + 127) / 128, nk);
+    cxd* const* o = (cxd* const*)outs_dev;
+#define QBG_ALP(D, C)                                                        \
+  k_assemble_alpert<D, C><<<grd, blk, 0, st>>>(g, tb, ks, nk, o, ld);        \
+  QBG_LAUNCH_CHECK("k_assemble_alpert");                                     \
+  k_alpert_corrections<D, C><<<cg, 128, 0, st>>>(g, tb, ks, nk, o, ld);      \
+  QBG_LAUNCH_CHECK("k_alpert_corrections")
+    if (cheb) {
+      if (deriv) { QBG_ALP(1, 1); } else { QBG_ALP(0, 1); }
+    } else {
+      if (deriv) { QBG_ALP(1, 0); } else { QBG_ALP(0, 0); }
+    }
+#undef QBG_ALP
+    return QBG_OK;
+  }
+  if (deriv) {
+    set_error("derivative assembly is available in FP64");
+    return QBG_ENOTSUP;
+  }
+  // complex64 forms: the corrections accumulate into FP64 entries, so groups
+  // of wavenumbers are assembled in FP64 staging and then split
+  const int grp = nk < 4 ? nk : 4;
+  const long long count = (long long)g.n * ld;
+  cxd* stage = nullptr;
+  cxd** dp = nullptr;
+  QBG_TRY(dmalloc(&stage, sizeof(cxd) * (size_t)count * grp));
+  if (int sa = dmalloc(&dp, sizeof(cxd*) * grp)) { dfree(stage, st); return sa; }
+  std::vector<cxd*> hp(grp);
+  for (int q = 0; q < grp; ++q) hp[q] = stage + (size_t)q * count;
+  cudaError_t e = cudaMemcpyAsync(dp, hp.data(), sizeof(cxd*) * grp, cudaMemcpyHostToDevice, st);
+  int s = e == cudaSuccess ? QBG_OK : cuda_status(e, "Alpert staging pointers");
+  for (int q0 = 0; !s && q0 < nk; q0 += grp) {
+    const int c = nk - q0 < grp ? nk - q0 : grp;
+    ChebTables sub;
+    if (cheb) {  // the tables of wavenumbers q0 .. q0 + c
+      sub = *cheb;
+      sub.H = cheb->H + (size_t)q0 * cheb->nh * (cheb->Mh + 1) * 2;
+      sub.J = cheb->J + (size_t)q0 * cheb->nj * (cheb->Mj + 1) * 2;
+    }
+    s = launch_alpert(g, cheb ? &sub : nullptr, ks + q0, c, 0, QBG_PREC_FP64, (void* const*)dp, ld, st, nullptr);
+    if (!s) {
+      dim3 sg((unsigned)((count + 255) / 256), c);
+      k_split_slots<<<sg, 256, 0, st>>>(stage, count, q0, c, outs_dev,
+                                        prec == QBG_PREC_MIXED ? lo_outs_dev : nullptr);
+      QBG_LAUNCH_CHECK("k_split_slots");
+    }
+  }
+  e = cudaStreamSynchronize(st);  // the staging buffers are freed below
+  dfree(stage, st);
+  dfree(dp, st);
+  if (s) return s;
+  if (e != cudaSuccess) return cuda_status(e, "Alpert assembly");
+  return QBG_OK;
 }
 
 template <int DERIV, int OUT>
@@ -1646,10 +1673,7 @@ int cheb_build(ChebTables& t, const cxd* ks, cudaStream_t st) {
 
 int launch_assemble_cheb(const GeomDev& g, const ChebTables& t, const cxd* ks, int nk, int deriv, int prec,
                          void* const* outs_dev, void* const* lo_outs_dev, long long ld, cudaStream_t st) {
-  if (g.quad == 1) {
-    set_error("the Alpert quadrature evaluates its kernels directly (no Chebyshev panels)");
-    return QBG_ENOTSUP;
-  }
+  if (g.quad == 1) return launch_alpert(g, &t, ks, nk, deriv, prec, outs_dev, ld, st, lo_outs_dev);
   if (prec == QBG_PREC_FP32) {
     set_error("the FP32 form evaluates its kernel values directly (no Chebyshev panels)");
     return QBG_ENOTSUP;
@@ -1749,7 +1773,7 @@ int launch_assemble(const GeomDev& g, const cxd* ks, int nk, int deriv, int prec
   const int dim = reduced ? g.m : g.n;
   dim3 blk(32, 8);
   dim3 grd((dim + 31) / 32, (dim + 7) / 8);
-  if (g.quad == 1) return launch_alpert(g, ks, nk, deriv, prec, outs_dev, ld, st, lo_outs_dev);
+  if (g.quad == 1) return launch_alpert(g, nullptr, ks, nk, deriv, prec, outs_dev, ld, st, lo_outs_dev);
   if (reduced) {
     if (g.form != 0) return launch_cfie_reduced(g, nullptr, ks, nk, deriv, prec, outs_dev, lo_outs_dev, ld, st);
     if (deriv && prec != QBG_PREC_FP64) {

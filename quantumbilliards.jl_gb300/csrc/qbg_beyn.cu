@@ -206,8 +206,8 @@ int load(qbg_beyn* b, int n0, int c) {
   b->res0 = -1;
   b->resn = 0;
   QBG_CUDA(cudaEventRecord(b->ev[0], st));
-  // the Alpert quadrature and the FP32 form evaluate their kernels directly
-  const bool use_cheb = b->opts.eval_mode == 0 && b->prec != QBG_PREC_FP32 && b->g->d.quad == 0;
+  // the FP32 form evaluates its kernels directly
+  const bool use_cheb = b->opts.eval_mode == 0 && b->prec != QBG_PREC_FP32;
   if (use_cheb) {
     const qbg_cheb_params cp = cheb_defaults(&b->opts.cheb);
     QBG_TRY(cheb_params_check(&cp));

@@ -225,8 +225,6 @@ def compute_spectrum_beyn(solver, billiard, k1, k2, m=50, Rmax=0.5, nq=48, r=Non
     else:
         all_pts = [evaluate_points(solver, billiard, float(z.real)) for z in k0]
         all_ws = [Workspace(solver, p) for p in all_pts]
-    if getattr(solver, "alpert_order", None) is not None:
-        use_chebyshev = False  # the Alpert quadrature evaluates its kernels directly
     if use_chebyshev:
         imax = int(np.argmax(k0.real + R))
         th = 2 * math.pi * np.arange(nq) / nq

@@ -63,3 +63,26 @@ def test_alpert_beyn_unit_disk(qb):
     ref = np.sort(ref)
     assert len(lam) == len(ref) > 0
     assert np.max(np.abs(lam - ref) / ref) < 1e-9
+
+
+def test_alpert_through_chebyshev_panels(qb):
+    """The Alpert route through Chebyshev panels
+    (chebyshev_euclidian_helmholtz_cfie_alpert.jl:533-1253: H0, H1 from the
+    panels on the grid pairs and the correction nodes, direct values below
+    r_min): panels tuned to 1e-13 reproduce the oracle's direct entries to
+    1e-11 (A) and 1e-10 (A', A''); the complex64 form rounds those FP64
+    values."""
+    import math
+    sol, pts, ws, curves, rule = _case(qb, True, 12)
+    ks = [15.1 + 0.2j, 14.8 - 0.1j]
+    zref = 15.0 + 0.5 * np.exp(2j * math.pi * np.arange(8) / 8)
+    cheb = qb.chebyshev_params(sol, pts, zref, ws=ws, tol=1e-13)[:4]
+    got = qb.assemble(ws, ks, cheb=cheb)
+    for z, g in zip(ks, got):
+        assert _rel(g, OAL.cfie_alpert_matrix(curves, pts, z, rule, 12)) < 1e-11
+    gd = qb.assemble(ws, [15.2], cheb=cheb, deriv=True)
+    for g, r in zip(gd, OAL.cfie_alpert_matrix(curves, pts, 15.2, rule, 12, derivs=True)):
+        assert _rel(g, r) < 1e-10
+    hi = qb.assemble(ws, ks, mixed=True, cheb=cheb)
+    for g, h in zip(got, hi):
+        assert np.array_equal(h, g.astype(np.complex64))
