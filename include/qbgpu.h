@@ -237,6 +237,19 @@ qbg_status qbg_beyn_moments(qbg_beyn* b, const double* V, int64_t L, double* A0,
  * m must equal the column count after this call. */
 qbg_status qbg_beyn_moments_qr(qbg_beyn* b, const double* V, int64_t L, int32_t append, int64_t m, double* R,
                                double* C, qbg_beyn_stats* stats);
+/* construct_B_matrix (beyn.jl:257-322) in one call, for a single-disk handle:
+ * the moments of the r probe columns V (N x r, column-major complex128; host,
+ * or device with QBG_PTR_DEVICE), the thin SVD of A0 (reduced on the device
+ * by a QR, the m x m factor decomposed on the host by one-sided Jacobi), the
+ * absolute rank rk = count(S >= svd_tol); when rk == r and 2r < N the block
+ * grows once to 2r with V2 (N x r more columns, appended, the first r kept;
+ * V2 = NULL skips the regrowth), as the reference's loop leaves after one
+ * pass (beyn.jl:307). Outputs: B = U_k^H A1 W_k S_k^-1 (rk x rk, leading
+ * dimension rk, host; room for (2r)^2), U_k (N x rk, leading dimension N;
+ * host, or device with QBG_PTR_DEVICE; may be NULL), S (the singular values
+ * of the final A0, room for 2r; may be NULL), rk and the final column count. */
+qbg_status qbg_beyn_B(qbg_beyn* b, const double* V, int64_t r, const double* V2, double svd_tol, double* B,
+                      double* Uk, double* S, int64_t* rk, int64_t* r_used, qbg_beyn_stats* stats);
 qbg_status qbg_beyn_destroy(qbg_beyn* b);
 
 /* Smallest singular value of A(k) for nk real wavenumbers (the :svd branch of

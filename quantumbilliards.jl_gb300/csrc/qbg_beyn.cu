@@ -10,6 +10,7 @@
 // nodes through them in groups (assemble, factor, solve, accumulate), which
 // bounds the memory at large N at the price of re-assembling per call.
 #include <algorithm>
+#include <complex>
 #include <cstdlib>
 #include <cusolverDn.h>
 #include <limits>
@@ -799,6 +800,71 @@ int qr_reduce(qbg_beyn* b, double* Rh, double* Ch) {
   return QBG_OK;
 }
 
+// One-sided Jacobi SVD (Hestenes; Golub and Van Loan 8.6.4) of the m x m
+// complex matrix R (column-major): columns are rotated pairwise until
+// mutually orthogonal, R W = U diag(sv). On return sv holds the singular
+// values in descending order and W the right singular vectors (m x m,
+// column-major), ordered alike. Small singular values keep high relative
+// accuracy, which the absolute rank test svd_tol relies on.
+void jacobi_svd(int m, std::vector<std::complex<double>> R, std::vector<double>& sv,
+                std::vector<std::complex<double>>& W) {
+  using zc = std::complex<double>;
+  W.assign((size_t)m * m, zc(0.0, 0.0));
+  for (int i = 0; i < m; ++i) W[(size_t)i * m + i] = 1.0;
+  auto col = [&](std::vector<zc>& M, int j) { return M.data() + (size_t)j * m; };
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    bool rotated = false;
+    for (int p = 0; p < m - 1; ++p)
+      for (int q = p + 1; q < m; ++q) {
+        zc* a = col(R, p);
+        zc* b = col(R, q);
+        double al = 0.0, be = 0.0;
+        zc ga(0.0, 0.0);
+        for (int i = 0; i < m; ++i) {
+          al += std::norm(a[i]);
+          be += std::norm(b[i]);
+          ga += std::conj(a[i]) * b[i];
+        }
+        const double g = std::abs(ga);
+        if (!(g > 1e-15 * std::sqrt(al * be)) || g == 0.0) continue;
+        rotated = true;
+        const zc ph = ga / g;  // b e^{-i phi} makes the pair's Gram entry real
+        const double zeta = (be - al) / (2.0 * g);
+        const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1.0 + zeta * zeta));
+        const double c = 1.0 / std::sqrt(1.0 + t * t), sn = c * t;
+        for (int i = 0; i < m; ++i) {
+          const zc x = a[i], y = b[i] * std::conj(ph);
+          a[i] = c * x - sn * y;
+          b[i] = sn * x + c * y;
+        }
+        zc* wa = col(W, p);
+        zc* wb = col(W, q);
+        for (int i = 0; i < m; ++i) {
+          const zc x = wa[i], y = wb[i] * std::conj(ph);
+          wa[i] = c * x - sn * y;
+          wb[i] = sn * x + c * y;
+        }
+      }
+    if (!rotated) break;
+  }
+  std::vector<double> nrm(m);
+  for (int j = 0; j < m; ++j) {
+    double t = 0.0;
+    for (int i = 0; i < m; ++i) t += std::norm(R[(size_t)j * m + i]);
+    nrm[j] = std::sqrt(t);
+  }
+  std::vector<int> ord(m);
+  for (int j = 0; j < m; ++j) ord[j] = j;
+  std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return nrm[x] > nrm[y]; });
+  std::vector<zc> Wo((size_t)m * m);
+  sv.resize(m);
+  for (int j = 0; j < m; ++j) {
+    sv[j] = nrm[ord[j]];
+    std::copy(W.begin() + (size_t)ord[j] * m, W.begin() + (size_t)(ord[j] + 1) * m, Wo.begin() + (size_t)j * m);
+  }
+  W.swap(Wo);
+}
+
 }  // namespace
 
 extern "C" {
@@ -832,6 +898,107 @@ qbg_status qbg_beyn_moments_qr(qbg_beyn* b, const double* V, int64_t L, int32_t 
   }
   QBG_TRY(moments_impl(b, V, L, nullptr, nullptr, stats, append ? 1 : 0));
   return qr_reduce(b, R, C);
+}
+
+// construct_B_matrix (beyn.jl:257-322) in one call on a single-disk handle:
+// moments of V kept on the device, A0 = Q R there, the SVD of R on the host
+// (R = U_R S W^H, so A0 = (Q U_R) S W^H), the absolute rank count(S >= svd_tol),
+// one regrowth r -> 2r with V2 appended when rk == r and 2r < N, then
+// B = U_R,k^H (Q^H A1) W_k S_k^-1 and U_k = A0 W_k S_k^-1 (device product).
+qbg_status qbg_beyn_B(qbg_beyn* b, const double* V, int64_t r, const double* V2, double svd_tol, double* B,
+                      double* Uk, double* S, int64_t* rk_out, int64_t* r_used, qbg_beyn_stats* stats) {
+  if (!b || !V || !B || !rk_out || !r_used || r < 1 || !(svd_tol >= 0.0)) {
+    set_error("qbg_beyn_B: invalid arguments");
+    return QBG_EINVAL;
+  }
+  if (b->ndisk != 1) {
+    set_error("qbg_beyn_B: the handle holds %d disks; B is formed for single-disk handles", b->ndisk);
+    return QBG_EINVAL;
+  }
+  if (r > b->n) {
+    set_error("qbg_beyn_B: r = %lld exceeds the dimension %d", (long long)r, b->n);
+    return QBG_EINVAL;
+  }
+  using zc = std::complex<double>;
+  std::lock_guard<std::mutex> lk(b->mu);
+  const int n = b->n;
+  int m = (int)r;
+  std::vector<double> Rh, Ch;
+  std::vector<double> sv;
+  std::vector<zc> W;
+  auto reduce = [&]() -> int {
+    Rh.assign(2 * (size_t)m * m, 0.0);
+    Ch.assign(2 * (size_t)m * m, 0.0);
+    QBG_TRY(qr_reduce(b, Rh.data(), Ch.data()));
+    std::vector<zc> R((size_t)m * m);
+    for (size_t e = 0; e < R.size(); ++e) R[e] = zc(Rh[2 * e], Rh[2 * e + 1]);
+    jacobi_svd(m, R, sv, W);
+    return QBG_OK;
+  };
+  QBG_TRY(moments_impl(b, V, r, nullptr, nullptr, stats, 0));
+  QBG_TRY(reduce());
+  int rk = 0;
+  for (double x : sv) rk += x >= svd_tol;
+  if (rk == m && 2 * r < n && V2) {  // beyn.jl:291-309: one regrowth, the loop left after it
+    QBG_TRY(moments_impl(b, V2, r, nullptr, nullptr, stats, 1));
+    m = 2 * (int)r;
+    QBG_TRY(reduce());
+    rk = 0;
+    for (double x : sv) rk += x >= svd_tol;
+  }
+  *r_used = m;
+  *rk_out = rk;
+  if (S)
+    for (int j = 0; j < m; ++j) S[j] = sv[j];
+  if (rk == 0) return QBG_OK;
+  // B = U_R,k^H C W_k S_k^-1 with R = U_R S W^H: U_R,k = R W_k S_k^-1
+  std::vector<zc> C((size_t)m * m), Rz((size_t)m * m), Wk((size_t)m * rk), URk((size_t)m * rk), CW((size_t)m * rk);
+  for (size_t e = 0; e < C.size(); ++e) {
+    C[e] = zc(Ch[2 * e], Ch[2 * e + 1]);
+    Rz[e] = zc(Rh[2 * e], Rh[2 * e + 1]);
+  }
+  for (int j = 0; j < rk; ++j)
+    for (int i = 0; i < m; ++i) Wk[(size_t)j * m + i] = W[(size_t)j * m + i] / sv[j];  // W_k S_k^-1
+  for (int j = 0; j < rk; ++j)
+    for (int i = 0; i < m; ++i) {
+      zc u(0.0, 0.0), c(0.0, 0.0);
+      for (int l = 0; l < m; ++l) {
+        u += Rz[(size_t)l * m + i] * Wk[(size_t)j * m + l];
+        c += C[(size_t)l * m + i] * Wk[(size_t)j * m + l];
+      }
+      URk[(size_t)j * m + i] = u;
+      CW[(size_t)j * m + i] = c;
+    }
+  for (int j = 0; j < rk; ++j)
+    for (int i = 0; i < rk; ++i) {
+      zc t(0.0, 0.0);
+      for (int l = 0; l < m; ++l) t += std::conj(URk[(size_t)i * m + l]) * CW[(size_t)j * m + l];
+      B[2 * ((size_t)j * rk + i)] = t.real();
+      B[2 * ((size_t)j * rk + i) + 1] = t.imag();
+    }
+  if (Uk) {  // U_k = A0 W_k S_k^-1 from the kept moments
+    cudaStream_t st = b->st;
+    cxd *dW = nullptr, *dU = nullptr;
+    QBG_TRY(dmalloc(&dW, sizeof(cxd) * (size_t)m * rk));
+    const bool dev = (b->opts.flags & QBG_PTR_DEVICE) != 0;
+    int s2 = dev ? QBG_OK : dmalloc(&dU, sizeof(cxd) * (size_t)n * rk);
+    if (s2) { dfree(dW, st); return s2; }
+    cxd* out = dev ? reinterpret_cast<cxd*>(Uk) : dU;
+    cudaError_t e = cudaMemcpyAsync(dW, Wk.data(), sizeof(cxd) * Wk.size(), cudaMemcpyHostToDevice, st);
+    int s = e == cudaSuccess ? QBG_OK : cuda_status(e, "qbg_beyn_B");
+    if (!s)
+      s = gemm_batched<double>(n, rk, m, cxd(1, 0), b->macc0, n, 0, dW, m, 0, cxd(0, 0), out, n, 0, 1, st);
+    if (!s && !dev) {
+      e = cudaMemcpyAsync(Uk, dU, sizeof(cxd) * (size_t)n * rk, cudaMemcpyDeviceToHost, st);
+      if (e != cudaSuccess) s = cuda_status(e, "qbg_beyn_B U_k");
+    }
+    e = cudaStreamSynchronize(st);
+    dfree(dW, st);
+    if (dU) dfree(dU, st);
+    if (s) return s;
+    if (e != cudaSuccess) return cuda_status(e, "qbg_beyn_B");
+  }
+  return QBG_OK;
 }
 
 qbg_status qbg_beyn_destroy(qbg_beyn* b) {

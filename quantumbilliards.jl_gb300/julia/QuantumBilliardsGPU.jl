@@ -3,9 +3,14 @@
 # Adds GPU methods to QuantumBilliards.jl's own functions for a wrapper solver
 # type, so existing driver code (k_sweep, compute_spectrum_beyn, EBIM) keeps
 # its signatures:
-#   construct_matrices!           (dlp_kress.jl:1627-1679, cfie_kress.jl:893-929)
-#   construct_boundary_matrices!  (chebyshev_euclidian_helmholtz_{dlp,cfie}_kress.jl)
-#   construct_B_matrix            (beyn.jl:257-322)
+#   construct_matrices!                          (dlp_kress.jl:1627-1679, cfie_kress.jl:893-929)
+#   construct_boundary_matrices!                 (chebyshev_euclidian_helmholtz_{dlp,cfie}_kress.jl:1110, 1431)
+#   construct_boundary_matrices_with_derivatives! (..._dlp_kress.jl:1126-1144, ..._cfie_kress.jl:1507-1573)
+#   construct_B_matrix                           (beyn.jl:257-322) through qbg_beyn_B
+#   solve(solver, basis, pts[, ws], k; which=:svd), k_sweep (dlp_kress.jl:1783-1820, sweepmethods.jl:132-152)
+# One device workspace is kept per (solver, discretisation) and reused by every
+# call; methods take the reference's own workspace objects in the place where
+# it passes them and look the device workspace up by the discretisation.
 # Julia is not installed where this project is built and tested; this file is
 # the binding a maintainer adds, written against include/qbgpu.h.
 module QuantumBilliardsGPU
@@ -84,6 +89,29 @@ end
 _form(::Union{QB.DLP_kress,QB.DLP_kress_global_corners}) = QBG_FORM_DLP
 _form(::Union{QB.CFIE_kress,QB.CFIE_kress_corners,QB.CFIE_kress_global_corners}) = QBG_FORM_CFIE
 
+# symmetry orbits in the library's 0-based layout: DLP from the reference's
+# periodic index orbits (symmetry.jl:214-261), CFIE from its reduced workspace
+# (cfie_kress.jl:264-289); nothing without a symmetry
+function _reduction(inner, pts)
+    isnothing(inner.symmetry) && return nothing
+    if _form(inner) == QBG_FORM_DLP
+        p = pts isa AbstractVector ? pts[1] : pts
+        rws = QB.build_dlp_kress_workspace(inner, p)
+        Ifund, f2f, f2s = rws.Ifund, rws.fund_to_full, rws.fund_to_scale
+    else
+        ws = QB.build_cfie_kress_workspace(inner, pts isa AbstractVector ? pts : [pts])
+        Ifund, f2f, f2s = ws.Ifund, ws.fund_to_full, ws.fund_to_scale
+    end
+    m, norb = length(Ifund), length(f2f[1])
+    fund = Int64.(Ifund .- 1)
+    orbit = Int64[f2f[b][l] - 1 for l in 1:norb, b in 1:m]        # orbit b's members contiguous
+    scale = Float64[]
+    for b in 1:m, l in 1:norb
+        push!(scale, real(f2s[b][l]), imag(f2s[b][l]))
+    end
+    return fund, vec(orbit), scale, norb
+end
+
 "Upload a discretisation (BoundaryPointsCFIE or a vector of them)."
 function gpu_workspace(solver::GPUSolver, pts)
     comps = pts isa AbstractVector ? pts : [pts]
@@ -96,12 +124,16 @@ function gpu_workspace(solver::GPUSolver, pts)
     dx = cat(p -> getindex.(p.tangent, 1)); dy = cat(p -> getindex.(p.tangent, 2))
     ddx = cat(p -> getindex.(p.tangent_2, 1)); ddy = cat(p -> getindex.(p.tangent_2, 2))
     ts = cat(p -> p.ts); wsv = cat(p -> p.ws)
-    keep = Any[offs, x, y, dx, dy, ddx, ddy, ts, wsv]
+    red = _reduction(solver.inner, pts)
+    fund, orbit, scale, norb = red === nothing ? (Int64[], Int64[], Float64[], 0) : red
+    keep = Any[offs, x, y, dx, dy, ddx, ddy, ts, wsv, fund, orbit, scale]
     h = Ref{Ptr{Cvoid}}(C_NULL)
     GC.@preserve keep begin
         d = QbgGeomDesc(_form(solver.inner), Int32(length(comps)), pointer(offs), pointer(x), pointer(y),
                         pointer(dx), pointer(dy), pointer(ddx), pointer(ddy), pointer(ts), pointer(wsv),
-                        0, 0, C_NULL, C_NULL, C_NULL,
+                        Int64(length(fund)), Int32(norb),
+                        isempty(fund) ? C_NULL : pointer(fund), isempty(orbit) ? C_NULL : pointer(orbit),
+                        isempty(scale) ? C_NULL : pointer(scale),
                         0, 0, 0, 0, C_NULL, C_NULL, C_NULL, C_NULL)  # Kress; an Alpert solver fills the cache fields
         qbg_check(ccall((:qbg_geom_create, libqbgpu), Int32, (Ref{QbgGeomDesc}, Ref{Ptr{Cvoid}}), d, h))
     end
@@ -110,61 +142,133 @@ function gpu_workspace(solver::GPUSolver, pts)
     return GPUWorkspace(h[], Int(dim[]), keep)
 end
 
-# construct_boundary_matrices!(Tbufs, solver, pts, zj; ...) — complex k, multi-k
-function QB.construct_boundary_matrices!(Tbufs::Vector{Matrix{ComplexF64}}, solver::GPUSolver, pts,
-                                         zj::AbstractVector{ComplexF64}; kwargs...)
-    ws = gpu_workspace(solver, pts)
-    ptrs = [pointer(T) for T in Tbufs]
-    GC.@preserve Tbufs zj qbg_check(ccall((:qbg_assemble, libqbgpu), Int32,
-        (Ptr{Cvoid}, Ptr{ComplexF64}, Int64, Int32, Int32, Int32, Ptr{Ptr{ComplexF64}}),
-        ws.h, collect(zj), length(zj), 0, QBG_PREC_FP64, 0, ptrs))
+# one device workspace per (solver, discretisation), reused by every call
+const _WS_CACHE = IdDict{Any,Any}()
+function cached_workspace(solver::GPUSolver, pts)
+    inner = get!(IdDict{Any,Any}, _WS_CACHE, solver)
+    return get!(() -> gpu_workspace(solver, pts), inner, pts)
+end
+_ws(solver::GPUSolver, pts, ws::GPUWorkspace) = ws
+_ws(solver::GPUSolver, pts, ws) = cached_workspace(solver, pts)   # the reference's own workspace types
+
+# outs: [A(z_1)...A(z_n)] (+ [A'...], [A''...]) in place, direct or through Chebyshev panels
+function _assemble!(ws::GPUWorkspace, zj, outs::Vector{Matrix{ComplexF64}}, deriv::Bool, use_chebyshev::Bool,
+                    n_panels_h::Int, M_h::Int, n_panels_j::Int, M_j::Int)
+    ks = ComplexF64.(collect(zj))
+    ptrs = [pointer(T) for T in outs]
+    GC.@preserve outs ks begin
+        if use_chebyshev
+            prm = QbgChebParams(Int32(n_panels_h), Int32(M_h), Int32(n_panels_j), Int32(M_j))
+            qbg_check(ccall((:qbg_assemble_cheb, libqbgpu), Int32,
+                (Ptr{Cvoid}, Ptr{ComplexF64}, Int64, Int32, Int32, Int32, Ref{QbgChebParams}, Ptr{Ptr{ComplexF64}}),
+                ws.h, ks, length(ks), deriv ? 1 : 0, QBG_PREC_FP64, 0, prm, ptrs))
+        else
+            qbg_check(ccall((:qbg_assemble, libqbgpu), Int32,
+                (Ptr{Cvoid}, Ptr{ComplexF64}, Int64, Int32, Int32, Int32, Ptr{Ptr{ComplexF64}}),
+                ws.h, ks, length(ks), deriv ? 1 : 0, QBG_PREC_FP64, 0, ptrs))
+        end
+    end
     return nothing
 end
 
-# construct_matrices!(solver, A, dA, ddA, pts, ws, k) — real k with derivatives (EBIM, Newton)
-function QB.construct_matrices!(solver::GPUSolver, A::Matrix{ComplexF64}, dA::Matrix{ComplexF64},
-                                ddA::Matrix{ComplexF64}, pts, ws::GPUWorkspace, k::Real; kwargs...)
-    kk = ComplexF64[k]
-    ptrs = [pointer(A), pointer(dA), pointer(ddA)]
-    GC.@preserve A dA ddA kk qbg_check(ccall((:qbg_assemble, libqbgpu), Int32,
-        (Ptr{Cvoid}, Ptr{ComplexF64}, Int64, Int32, Int32, Int32, Ptr{Ptr{ComplexF64}}),
-        ws.h, kk, 1, 1, QBG_PREC_FP64, 0, ptrs))
-    return A, dA, ddA
+# construct_boundary_matrices!(Tbufs, solver, pts, zj; use_chebyshev, panels...) — complex k, multi-k
+function QB.construct_boundary_matrices!(Tbufs::Vector{Matrix{ComplexF64}}, solver::GPUSolver, pts,
+                                         zj::AbstractVector{ComplexF64}; use_chebyshev::Bool=true,
+                                         n_panels_h::Int=15000, M_h::Int=5, n_panels_j::Int=3000, M_j::Int=5,
+                                         kwargs...)
+    _assemble!(cached_workspace(solver, pts), zj, Tbufs, false, use_chebyshev, n_panels_h, M_h, n_panels_j, M_j)
+    return nothing
 end
 
-# construct_B_matrix(solver, pts, N, k0, R; nq, r, svd_tol, rng) — beyn.jl:257-322,
-# with the N^2 / N^3 work on the GPU and the small SVD / B on the host.
+# construct_boundary_matrices_with_derivatives!(Tbufs, dTbufs, ddTbufs, solver, pts, zj; ...)
+function QB.construct_boundary_matrices_with_derivatives!(Tbufs::Vector{Matrix{ComplexF64}},
+                                                          dTbufs::Vector{Matrix{ComplexF64}},
+                                                          ddTbufs::Vector{Matrix{ComplexF64}}, solver::GPUSolver,
+                                                          pts, zj::AbstractVector{ComplexF64};
+                                                          use_chebyshev::Bool=true, n_panels_h::Int=15000,
+                                                          M_h::Int=5, n_panels_j::Int=3000, M_j::Int=5, kwargs...)
+    outs = vcat(Tbufs, dTbufs, ddTbufs)
+    _assemble!(cached_workspace(solver, pts), zj, outs, true, use_chebyshev, n_panels_h, M_h, n_panels_j, M_j)
+    return nothing
+end
+
+# construct_matrices!(solver, A[, dA, ddA], pts, ws, k) — real k (sweep, EBIM, Newton); ws may be the
+# reference's workspace (DLPKressWorkspace, DLPKressReducedWorkspace, CFIEKressWorkspace) or a GPUWorkspace
+function QB.construct_matrices!(solver::GPUSolver, A::Matrix{ComplexF64}, dA::Matrix{ComplexF64},
+                                ddA::Matrix{ComplexF64}, pts, ws, k::Real; kwargs...)
+    _assemble!(_ws(solver, pts, ws), [complex(k)], [A, dA, ddA], true, false, 0, 0, 0, 0)
+    return A, dA, ddA
+end
+function QB.construct_matrices!(solver::GPUSolver, A::Matrix{ComplexF64}, pts, ws, k::Real; kwargs...)
+    _assemble!(_ws(solver, pts, ws), [complex(k)], [A], false, false, 0, 0, 0, 0)
+    return A
+end
+
+# sigma_min over a k list on the device (qbg_sigma_min: batched LU, inverses, subspace iteration)
+function gpu_sigma_min(ws::GPUWorkspace, ks::AbstractVector{<:Real})
+    kk = Float64.(collect(ks))
+    sig = Vector{Float64}(undef, length(kk))
+    GC.@preserve kk sig qbg_check(ccall((:qbg_sigma_min, libqbgpu), Int32,
+        (Ptr{Cvoid}, Ptr{Float64}, Int64, Ptr{Float64}), ws.h, kk, length(kk), sig))
+    return sig
+end
+
+# solve(solver, basis, pts[, ws][, A], k; which=:svd) (dlp_kress.jl:1783-1820): sigma_min(A(k))
+function _solve_svd(solver::GPUSolver, pts, ws, k, which)
+    which === :svd || error("qbgpu: solve on the GPU computes which=:svd (sigma_min), not $(which)")
+    return gpu_sigma_min(_ws(solver, pts, ws), [k])[1]
+end
+QB.solve(solver::GPUSolver, basis::QB.AbsBasis, pts, k::Real; which::Symbol=:svd, kwargs...) =
+    _solve_svd(solver, pts, nothing, k, which)
+QB.solve(solver::GPUSolver, basis::QB.AbsBasis, pts, ws, k::Real; which::Symbol=:svd, kwargs...) =
+    _solve_svd(solver, pts, ws, k, which)
+QB.solve(solver::GPUSolver, basis::QB.AbsBasis, A::AbstractMatrix, pts, ws, k::Real; which::Symbol=:svd, kwargs...) =
+    _solve_svd(solver, pts, ws, k, which)
+
+# k_sweep(solver, basis, billiard, ks; which=:svd) (sweepmethods.jl:132-152): the discretisation at
+# maximum(ks) (sweepmethods.jl:51-60), every sigma_min in one batched device call
+function QB.k_sweep(solver::GPUSolver, basis::QB.AbsBasis, billiard::QB.AbsBilliard, ks; which::Symbol=:svd,
+                    kwargs...)
+    which === :svd || error("qbgpu: k_sweep on the GPU computes which=:svd (sigma_min)")
+    pts = QB.evaluate_points(solver.inner, billiard, maximum(ks))
+    return gpu_sigma_min(cached_workspace(solver, pts), ks)
+end
+
+# construct_B_matrix(solver, pts, N, k0, R; nq, r, svd_tol, rng, use_chebyshev, panels) — beyn.jl:257-322
+# through qbg_beyn_B: the assembly, LU, solves, moments, the thin SVD (device QR of A0, Jacobi SVD of
+# its R), the absolute rank test and B in the library; the regrowth draws a fresh N x 2r block from
+# rng after the first block saturates, and the loop is left after that one pass (beyn.jl:291-309).
 function QB.construct_B_matrix(solver::GPUSolver, pts, N::Int, k0::Complex{Float64}, R::Float64;
-                               nq::Int=64, r::Int=48, svd_tol=1e-14, rng=QB.MersenneTwister(0), kwargs...)
-    ws = gpu_workspace(solver, pts)
+                               nq::Int=64, r::Int=48, svd_tol=1e-14, rng=QB.MersenneTwister(0),
+                               use_chebyshev::Bool=true, n_panels_h::Int=15000, M_h::Int=5, n_panels_j::Int=3000,
+                               M_j::Int=5, kwargs...)
+    ws = cached_workspace(solver, pts)
     @assert ws.dim == N
     h = Ref{Ptr{Cvoid}}(C_NULL)
-    opts = QbgBeynOpts(0, 10, 1e-6, 0, 0, QbgChebParams(0, 0, 0, 0), 0, 0, 0, 0)
+    opts = QbgBeynOpts(0, 10, 1e-6, 0, use_chebyshev ? 0 : 1,
+                       QbgChebParams(Int32(n_panels_h), Int32(M_h), Int32(n_panels_j), Int32(M_j)), 0, 0, 0, 0)
     qbg_check(ccall((:qbg_beyn_create, libqbgpu), Int32,
         (Ptr{Cvoid}, Float64, Float64, Float64, Int32, Int32, Ref{QbgBeynOpts}, Ref{Ptr{Cvoid}}),
         ws.h, real(k0), imag(k0), R, nq, solver.prec, opts, h))
-    moments(V) = begin
-        A0 = similar(V); A1 = similar(V)
-        GC.@preserve V A0 A1 qbg_check(ccall((:qbg_beyn_moments, libqbgpu), Int32,
-            (Ptr{Cvoid}, Ptr{ComplexF64}, Int64, Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{Cvoid}),
-            h[], V, size(V, 2), A0, A1, C_NULL))
-        A0, A1
+    Bcall(V) = begin
+        c = size(V, 2)
+        B = Vector{ComplexF64}(undef, c * c); U = Matrix{ComplexF64}(undef, N, c)
+        rk = Ref{Int64}(0); rused = Ref{Int64}(0)
+        GC.@preserve V B U qbg_check(ccall((:qbg_beyn_B, libqbgpu), Int32,
+            (Ptr{Cvoid}, Ptr{ComplexF64}, Int64, Ptr{ComplexF64}, Float64, Ptr{ComplexF64}, Ptr{ComplexF64},
+             Ptr{Float64}, Ref{Int64}, Ref{Int64}, Ptr{Cvoid}),
+            h[], V, c, C_NULL, svd_tol, B, U, C_NULL, rk, rused, C_NULL))
+        k = Int(rk[])
+        reshape(B[1:k*k], k, k), U[:, 1:k], k
     end
     try
         V = randn(rng, ComplexF64, N, r)
-        A0, A1 = moments(V)
-        U, Σ, W = svd!(A0; full=false)
-        rk = count(>=(svd_tol), Σ)
+        B, Uk, rk = Bcall(V)
         rk == 0 && return Matrix{ComplexF64}(undef, N, 0), Matrix{ComplexF64}(undef, N, 0)
         if rk == r && 2r < N
-            V = randn(rng, ComplexF64, N, 2r)
-            A0, A1 = moments(V)
-            U, Σ, W = svd!(A0; full=false)
-            rk = count(>=(svd_tol), Σ)
+            B, Uk, rk = Bcall(randn(rng, ComplexF64, N, 2r))
         end
-        Uk = U[:, 1:rk]; Wk = W[:, 1:rk]
-        tmp = (A1 * Wk) ./ transpose(Σ[1:rk])
-        return Uk' * tmp, Uk
+        return B, Uk
     finally
         ccall((:qbg_beyn_destroy, libqbgpu), Int32, (Ptr{Cvoid},), h[])
     end
@@ -203,8 +307,7 @@ QB.solve_full!(solver::GPUSolver, A, dA, ddA, pts, k, dk; return_imag_part::Bool
 function QB.solve!(solver::GPUSolver, A::Matrix{ComplexF64}, dA::Matrix{ComplexF64}, ddA::Matrix{ComplexF64},
                    pts, k::Real, dk::Real; use_krylov::Bool=true, nev::Int=5, return_imag_part::Bool=false,
                    kwargs...)
-    ws = gpu_workspace(solver, pts)
-    QB.construct_matrices!(solver, A, dA, ddA, pts, ws, k)
+    QB.construct_matrices!(solver, A, dA, ddA, pts, cached_workspace(solver, pts), k)
     return gpu_ebim(A, dA, ddA, k, dk; nev=nev, full=!use_krylov, return_imag_part=return_imag_part)
 end
 
@@ -223,18 +326,20 @@ end
 # solve_vect(solver, basis, pts, ws, k) (dlp_kress.jl:1914-1949) for the DLP
 # forms: the adjoint matrix and the smallest null vector on the device.
 function QB.adjoint_fredholm_matrix!(A::Matrix{ComplexF64}, D::AbstractMatrix{ComplexF64}, solver::GPUSolver,
-                                     pts, ws::GPUWorkspace, k::Real; kwargs...)
+                                     pts, ws, k::Real; kwargs...)
     ds = collect(Float64, pts.ds)
+    g = _ws(solver, pts, ws)
     GC.@preserve A ds qbg_check(ccall((:qbg_adjoint_fredholm, libqbgpu), Int32,
-        (Ptr{Cvoid}, Float64, Ptr{Float64}, Ptr{ComplexF64}, Int32), ws.h, k, ds, A, Int32(0)))
+        (Ptr{Cvoid}, Float64, Ptr{Float64}, Ptr{ComplexF64}, Int32), g.h, k, ds, A, Int32(0)))
     return A
 end
-function QB.solve_vect(solver::GPUSolver, basis::QB.AbsBasis, pts, ws::GPUWorkspace, k::Real; kwargs...)
+function QB.solve_vect(solver::GPUSolver, basis::QB.AbsBasis, pts, ws, k::Real; kwargs...)
     ds = collect(Float64, pts.ds)
-    u = Vector{ComplexF64}(undef, ws.dim)
+    g = _ws(solver, pts, ws)
+    u = Vector{ComplexF64}(undef, g.dim)
     sig = Ref{Float64}(0)
     GC.@preserve ds u qbg_check(ccall((:qbg_solve_vect, libqbgpu), Int32,
-        (Ptr{Cvoid}, Float64, Ptr{Float64}, Ref{Float64}, Ptr{ComplexF64}), ws.h, k, ds, sig, u))
+        (Ptr{Cvoid}, Float64, Ptr{Float64}, Ref{Float64}, Ptr{ComplexF64}), g.h, k, ds, sig, u))
     return sig[], u
 end
 

@@ -115,6 +115,9 @@ _SIGS = {
                                      C.POINTER(BeynStats)]),
     "qbg_beyn_moments_qr": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int64, C.c_void_p,
                                         C.c_void_p, C.POINTER(BeynStats)]),
+    "qbg_beyn_B": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p,
+                               C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                               C.POINTER(BeynStats)]),
     "qbg_beyn_destroy": (C.c_int32, [C.c_void_p]),
     "qbg_sigma_min": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]),
     "qbg_ebim_eig": (C.c_int32, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int32,

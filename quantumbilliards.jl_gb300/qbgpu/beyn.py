@@ -131,6 +131,37 @@ class BeynHandle:
             return Rm, Cm
         return np.asfortranarray(Rm[0]), np.asfortranarray(Cm[0])
 
+    def B_matrix(self, V: np.ndarray, V2: np.ndarray = None, svd_tol: float = 1e-14, basis: bool = True):
+        """construct_B_matrix in one library call (qbg_beyn_B): moments of V,
+        the absolute rank test, one regrowth with V2 appended when the rank
+        saturates, B = U_k^H A1 W_k S_k^-1 and U_k. Returns (B, U_k or None,
+        info with rk, r and the singular values S)."""
+        lib = L.load()
+        if self.multi:
+            raise ValueError("B_matrix takes a single-disk handle")
+        V = np.asfortranarray(V, dtype=np.complex128)
+        N, r = V.shape
+        if N != self.N:
+            raise ValueError(f"V has {N} rows, the operator has {self.N}")
+        if V2 is not None:
+            V2 = np.asfortranarray(V2, dtype=np.complex128)
+            if V2.shape != V.shape:
+                raise ValueError("V2 must have the shape of V")
+        B = np.empty(4 * r * r, dtype=np.complex128)
+        U = np.empty((N, 2 * r), dtype=np.complex128, order="F") if basis else None
+        S = np.empty(2 * r, dtype=np.float64)
+        rk, rused = C.c_int64(), C.c_int64()
+        st = L.BeynStats()
+        L.check(lib.qbg_beyn_B(self._h, L.vptr(V), r, L.vptr(V2) if V2 is not None else None, float(svd_tol),
+                               L.vptr(B), L.vptr(U) if basis else None, L.dptr(S), C.byref(rk), C.byref(rused),
+                               C.byref(st)))
+        self._take_stats(st)
+        self._m = None
+        k, m = int(rk.value), int(rused.value)
+        Bm = B[:k * k].reshape((k, k), order="F").copy()
+        Uk = np.asfortranarray(U[:, :k]) if basis else None
+        return Bm, Uk, dict(rk=k, r=m, S=S[:m].copy())
+
     def close(self):
         if getattr(self, "_h", None) and L.alive():
             L.load().qbg_beyn_destroy(self._h)

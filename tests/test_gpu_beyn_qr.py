@@ -72,3 +72,34 @@ def test_solve_reduced_equals_full_basis(qb, mixed, r):
     a, f = sel(lam_r), sel(lam_f)
     assert len(a) == len(f) > 0
     assert np.max(np.abs(a - f) / np.abs(f)) < 1e-12
+
+
+def test_beyn_B_entry_matches_host_path(qb):
+    """qbg_beyn_B (construct_B_matrix in one library call: device QR of A0,
+    host one-sided Jacobi SVD of R, the absolute rank test, one regrowth with
+    the appended block) against construct_B_matrix on the same probes, whose
+    SVD runs in LAPACK on the full A0: same rank and final column count,
+    eigenvalues of B to 1e-12 relative, the same singular values to 1e-12 of
+    the largest, and U_k spanning the same space."""
+    import numpy as np
+    b = qb.make_star()
+    sol = qb.CFIE_kress(9.0, b)
+    pts = qb.evaluate_points(sol, b, 30.0)
+    ws = qb.Workspace(sol, pts)
+    N = ws.dim
+    k0, R, nq, r = 30.0 + 0j, 0.3, 24, 8
+    for svd_tol in (1e-12, 1e-3):
+        rng = np.random.default_rng(11)
+        V1 = qb.probe_matrix(N, r, rng)
+        V2 = qb.probe_matrix(N, r, rng)
+        bh = qb.BeynHandle(ws, k0, R, nq)
+        B, Uk, info = bh.B_matrix(V1, V2, svd_tol=svd_tol)
+        bh.close()
+        Bh, Ukh, infoh = qb.construct_B_matrix(sol, pts, N, k0, R, nq=nq, r=r, svd_tol=svd_tol,
+                                               rng=np.random.default_rng(11), ws=ws, return_info=True)
+        assert info["rk"] == infoh["rk"] > 0 and info["r"] == infoh["r"]
+        assert np.max(np.abs(info["S"] - infoh["S"])) <= 1e-12 * infoh["S"][0]
+        lam, lamh = np.linalg.eigvals(B), np.linalg.eigvals(Bh)
+        assert max(np.min(np.abs(lamh - x)) / abs(x) for x in lam) < 1e-12
+        s = np.linalg.svd(Uk.conj().T @ Ukh, compute_uv=False)
+        assert np.all(np.abs(s - 1.0) < 1e-10)
