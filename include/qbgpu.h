@@ -252,6 +252,18 @@ qbg_status qbg_beyn_B(qbg_beyn* b, const double* V, int64_t r, const double* V2,
                       double* Uk, double* S, int64_t* rk, int64_t* r_used, qbg_beyn_stats* stats);
 qbg_status qbg_beyn_destroy(qbg_beyn* b);
 
+/* Failure path of the tensor-core kernels (no counterpart in the reference).
+ * Every mbarrier wait of the tcgen05 GEMM pipeline gives up after a poll
+ * limit (and ~1e9 SM cycles); the kernel then records a sticky error, drains
+ * what it started with the full limit, frees its tensor memory and returns
+ * without writing its output, and the calling entry reports QBG_ECUDA.
+ * qbg_set_tc_wait_limit sets the pipeline waits' poll limit on the current
+ * device (polls < 0 restores the built-in limit; 0 makes every pipeline wait
+ * give up at once), qbg_clear_tc_error resets the sticky flag there. Both
+ * synchronize the device. Meant for tests of that path. */
+qbg_status qbg_set_tc_wait_limit(int64_t polls);
+qbg_status qbg_clear_tc_error(void);
+
 /* Smallest singular value of A(k) for nk real wavenumbers (the :svd branch of
  * @svd_or_det_solve, macros.jl:159-161, called by k_sweep,
  * sweepmethods.jl:132-152): FP64 LU of A(k), then block inverse iteration on

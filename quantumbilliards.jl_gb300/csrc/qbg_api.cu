@@ -649,6 +649,10 @@ qbg_status qbg_cgemm_c64(int32_t engine, int32_t M, int32_t N, int32_t K, const 
   return QBG_OK;
 }
 
+qbg_status qbg_set_tc_wait_limit(int64_t polls) { return tc_set_wait_limit(polls); }
+
+qbg_status qbg_clear_tc_error(void) { return tc_clear_error(); }
+
 qbg_status qbg_launch_count(uint64_t* count) {
   if (!count) { set_error("qbg_launch_count: null pointer"); return QBG_EINVAL; }
   *count = g_launches.load(std::memory_order_relaxed);

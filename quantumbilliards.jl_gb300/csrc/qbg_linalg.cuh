@@ -115,6 +115,11 @@ int tc_gemm_c64(int M, int N, int K, cxf alpha, const cxf* A, long long lda, lon
 // Reads the tensor-core GEMM's device error flag (set, and kept set, once an
 // mbarrier wait gave up); synchronizes the stream. Returns QBG_OK or QBG_ECUDA.
 int tc_check(cudaStream_t st);
+// pipeline-wait poll limit of the tensor-core GEMM (< 0: the built-in limit)
+// and reset of its sticky error flag, on the current device (both synchronize
+// the device first)
+int tc_set_wait_limit(long long polls);
+int tc_clear_error();
 // returns the tensor-core GEMM's packing scratch of stream st to the pool
 // (call before destroying a stream that ran library GEMMs)
 void tc_release_scratch(cudaStream_t st);

@@ -89,10 +89,16 @@ __device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
   return ok != 0;
 }
 
-// bounded wait: gives up after ~0.5 s of SM clock (1e9 cycles) or TC_SPIN_LIMIT polls
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity) {
+// Poll limit of the pipeline waits (not of the drains that follow a give-up):
+// TC_SPIN_LIMIT unless lowered by qbg_set_tc_wait_limit, which lets a test make
+// a wait run out on purpose and check the error path. One copy per device.
+__device__ long long g_tc_wait_polls = TC_SPIN_LIMIT;
+
+// bounded wait: gives up after ~0.5 s of SM clock (1e9 cycles) or `polls` polls
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity,
+                                                  long long polls = TC_SPIN_LIMIT) {
   const long long t0 = clock64();
-  for (long long it = 0; it < TC_SPIN_LIMIT; ++it) {
+  for (long long it = 0; it < polls; ++it) {
     if (mbar_try(mbar, parity)) return true;
     if (clock64() - t0 > 1000000000ll) break;
   }
@@ -231,7 +237,7 @@ __global__ void __launch_bounds__(128) k_tc_cgemm(int M, int N, int K, cxf alpha
     float* sBs = sBb + TC_KSTEPS * TC_B_STEP;
     if (st ? pend1 : pend0) {
       // the MMAs of tile kt-2 read this stage
-      if (mbar_wait_bounded(st ? mb1 : mb0, st ? wph1 : wph0)) {
+      if (mbar_wait_bounded(st ? mb1 : mb0, st ? wph1 : wph0, g_tc_wait_polls)) {
         if (st) { wph1 ^= 1u; pend1 = false; } else { wph0 ^= 1u; pend0 = false; }
       } else {
         atomicExch(abort_flag, 1);
@@ -463,7 +469,7 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm_pk(int M, int N, int KT, cx
     for (; issued < KT && issued < PK_NST; ++issued) issue(issued);
     for (int kt = 0; kt < KT && good; ++kt) {
       const int s = kt % PK_NST;
-      if (!mbar_wait_bounded(smem_u32(full + s), (uint32_t)((kt / PK_NST) & 1))) {
+      if (!mbar_wait_bounded(smem_u32(full + s), (uint32_t)((kt / PK_NST) & 1), g_tc_wait_polls)) {
         good = false;
         break;
       }
@@ -486,7 +492,7 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm_pk(int M, int N, int KT, cx
       // refill the stage of tile kt - 1 once its MMAs are done
       if (kt >= 1 && issued < KT) {
         const int t = kt - 1;
-        if (!mbar_wait_bounded(smem_u32(empty + t % PK_NST), (uint32_t)((t / PK_NST) & 1))) {
+        if (!mbar_wait_bounded(smem_u32(empty + t % PK_NST), (uint32_t)((t / PK_NST) & 1), g_tc_wait_polls)) {
           good = false;
           break;
         }
@@ -497,7 +503,8 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm_pk(int M, int N, int KT, cx
     }
     // every committed MMA group completes before TMEM is read or freed
     for (; good && freed < committed; ++freed)
-      if (!mbar_wait_bounded(smem_u32(empty + freed % PK_NST), (uint32_t)((freed / PK_NST) & 1))) good = false;
+      if (!mbar_wait_bounded(smem_u32(empty + freed % PK_NST), (uint32_t)((freed / PK_NST) & 1), g_tc_wait_polls))
+        good = false;
     if (!good) {
       *abort_flag = 1;
       atomicExch(err, 1);
@@ -680,6 +687,25 @@ int tc_gemm_c64(int M, int N, int K, cxf alpha, const cxf* A, long long lda, lon
   k_tc_cgemm<<<grd, 128, tc_smem_bytes(), st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch2,
                                                  sA2, sB2, sC2, derr);
   QBG_LAUNCH_CHECK("k_tc_cgemm");
+  return QBG_OK;
+}
+
+// runtime pipeline-wait limit (polls; < 0 restores the built-in limit) and
+// reset of the sticky error flag, on the current device
+int tc_set_wait_limit(long long polls) {
+  int* derr = nullptr;
+  if (int s = tc_device_setup(&derr)) return s;
+  const long long v = polls < 0 ? TC_SPIN_LIMIT : polls;
+  QBG_CUDA(cudaDeviceSynchronize());
+  QBG_CUDA(cudaMemcpyToSymbol(g_tc_wait_polls, &v, sizeof(v)));
+  return QBG_OK;
+}
+
+int tc_clear_error() {
+  int* derr = nullptr;
+  if (int s = tc_device_setup(&derr)) return s;
+  QBG_CUDA(cudaDeviceSynchronize());
+  QBG_CUDA(cudaMemset(derr, 0, sizeof(int)));
   return QBG_OK;
 }
 
