@@ -367,11 +367,12 @@ extern "C" {
 // sigma_min (svdvals(A)[end], macros.jl:159-161) for every k: the k are taken
 // in chunks; a chunk's A(k) are assembled in FP64 straight into one LU batch,
 // factored by the library's batched LU and inverted (LU solves with the
-// identity), and the subspace iteration on the inverses runs on the device,
-// one CTA per k (qbg_dense.cu), until 1/sqrt(lambda_max) changes by less
-// than 1e-13 relative (at most SM_ITERS steps). One host synchronisation per
-// chunk reads the pivots' info and the results; an exactly singular U gives
-// sigma_min = 0.
+// identity), and the subspace iteration on the inverses runs on the device
+// until 1/sqrt(lambda_max) changes by less than 1e-13 relative (at most
+// SM_ITERS steps): for many operators of n <= 1024 one CTA per k runs the
+// whole iteration and one host synchronisation per chunk reads the results;
+// otherwise each k's products are split over the whole GPU (sigma_single).
+// An exactly singular U gives sigma_min = 0.
 // ---------------------------------------------------------------------------
 qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig) {
   if (!g || !ks || !sig || nk < 1) { set_error("qbg_sigma_min: invalid arguments"); return QBG_EINVAL; }
@@ -413,13 +414,19 @@ qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig)
   int s = QBG_OK;
   {
     Dense64 D;
-    cxd *Cinv = nullptr, *dks = nullptr, *work = nullptr, *X0 = nullptr;
-    double* dsig = nullptr;
+    cxd *Cinv = nullptr, *dks = nullptr, *work = nullptr, *X0 = nullptr, *CH = nullptr, *P = nullptr;
+    double *dsig = nullptr, *state = nullptr;
     void** dptrs = nullptr;
+    // many small operators: one CTA per k runs the whole iteration (sigma_iterate);
+    // otherwise each k's products are spread over the GPU (sigma_single)
+    const bool per_cta = n <= 1024 && chunk >= 16;
     if ((s = D.create(n, chunk, st)) || (s = D.alloc(&Cinv, sizeof(cxd) * (size_t)n * n * chunk)) ||
         (s = D.alloc(&dks, sizeof(cxd) * nk)) || (s = D.alloc(&work, sizeof(cxd) * (size_t)3 * n * DENSE_P * chunk)) ||
         (s = D.alloc(&X0, sizeof(cxd) * (size_t)n * DENSE_P)) || (s = D.alloc(&dsig, sizeof(double) * chunk)) ||
-        (s = D.alloc(&dptrs, sizeof(void*) * chunk)))
+        (s = D.alloc(&dptrs, sizeof(void*) * chunk)) ||
+        (!per_cta && ((s = D.alloc(&CH, sizeof(cxd) * (size_t)n * n)) ||
+                      (s = D.alloc(&P, sizeof(cxd) * std::max<size_t>(gemm_tall_scratch(n, DENSE_P), 1))) ||
+                      (s = D.alloc(&state, sizeof(double) * (2 + 2 * DENSE_P))))))
       return s;
     std::vector<cxd> hx;
     dense_start_block(n, hx);
@@ -436,11 +443,22 @@ qbg_status qbg_sigma_min(qbg_geom* g, const double* ks, int64_t nk, double* sig)
       QBG_TRY(launch_assemble(g->d, dks + k0, c, 0, QBG_PREC_FP64, dptrs, n, st));
       QBG_TRY(lu_factor<double>(D.f, st));
       QBG_TRY(D.inverse(Cinv));
-      QBG_TRY(sigma_iterate(Cinv, n, c, X0, work, SM_ITERS, 1e-13, dsig, nullptr, nullptr, st));
       info.assign(c, 0);
       QBG_CUDA(cudaMemcpyAsync(info.data(), D.f.info, sizeof(int) * c, cudaMemcpyDeviceToHost, st));
-      QBG_CUDA(cudaMemcpyAsync(hs.data(), dsig, sizeof(double) * c, cudaMemcpyDeviceToHost, st));
-      QBG_CUDA(cudaStreamSynchronize(st));
+      if (per_cta) {
+        QBG_TRY(sigma_iterate(Cinv, n, c, X0, work, SM_ITERS, 1e-13, dsig, nullptr, nullptr, st));
+        QBG_CUDA(cudaMemcpyAsync(hs.data(), dsig, sizeof(double) * c, cudaMemcpyDeviceToHost, st));
+        QBG_CUDA(cudaStreamSynchronize(st));
+      } else {
+        QBG_CUDA(cudaStreamSynchronize(st));
+        for (int q = 0; q < c; ++q) {
+          hs[q] = 0.0;
+          if (info[q] > 0) continue;
+          cxd* W3 = work;
+          QBG_TRY(sigma_single(Cinv + (size_t)q * n * n, CH, n, X0, W3, W3 + (size_t)n * DENSE_P,
+                               W3 + 2 * (size_t)n * DENSE_P, P, state, SM_ITERS, 1e-13, &hs[q], nullptr, st));
+        }
+      }
       for (int q = 0; q < c; ++q) sig[k0 + q] = info[q] > 0 ? 0.0 : hs[q];
     }
     D.f.batch = chunk;

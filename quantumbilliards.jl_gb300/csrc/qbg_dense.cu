@@ -309,6 +309,73 @@ __global__ void __launch_bounds__(256) k_sigma_iter(const cxd* __restrict__ Cb, 
   }
 }
 
+// One-matrix steps of the same iteration for callers that spread the products
+// over the whole GPU (split-k GEMMs between these launches), one CTA each:
+// k_rr_step: G = W^H W, its top eigenpair (lambda, z), est = 1/sqrt(lambda)
+// and the convergence flag against the previous estimate (state: est, done,
+// z[2 SP]); k_orth8: orthonormal columns of Y in place; k_topvec: x = W z / |W z|.
+__global__ void __launch_bounds__(256) k_rr_step(const cxd* __restrict__ W, int n, double tol, double* state) {
+  __shared__ double sh[8 * SP * (SP + 1)];
+  __shared__ double Gs[2 * SP * SP];
+  const int tid = threadIdx.x;
+  double g[SP * (SP + 1)];
+#pragma unroll
+  for (int i = 0; i < SP * (SP + 1); ++i) g[i] = 0.0;
+  for (int r = tid; r < n; r += 256) {
+    cxd w[SP];
+#pragma unroll
+    for (int q = 0; q < SP; ++q) w[q] = W[(size_t)q * n + r];
+    int e = 0;
+#pragma unroll
+    for (int j = 0; j < SP; ++j)
+#pragma unroll
+      for (int i = 0; i <= j; ++i, e += 2) {
+        g[e] += w[i].re * w[j].re + w[i].im * w[j].im;
+        g[e + 1] += w[i].re * w[j].im - w[i].im * w[j].re;
+      }
+  }
+  block_sum<SP * (SP + 1)>(g, sh);
+  if (tid == 0) {
+    int e = 0;
+    for (int j = 0; j < SP; ++j)
+      for (int i = 0; i <= j; ++i, e += 2) {
+        Gs[2 * (j * SP + i)] = g[e];
+        Gs[2 * (j * SP + i) + 1] = g[e + 1];
+        Gs[2 * (i * SP + j)] = g[e];
+        Gs[2 * (i * SP + j) + 1] = -g[e + 1];
+      }
+    double lam = 0.0;
+    herm_top(Gs, &lam, state + 2);
+    const bool ok = lam > 0.0 && isfinite(lam);
+    const double cur = ok ? 1.0 / sqrt(lam) : 0.0;
+    const double prev = state[0];
+    state[1] = (prev >= 0.0 && fabs(cur - prev) <= tol * cur) || !ok ? 1.0 : 0.0;
+    state[0] = cur;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_orth8(cxd* Y, int n, int salt) {
+  __shared__ double sh[8 * 2 * SP];
+  orth_cgs2(Y, n, sh, salt);
+}
+
+__global__ void __launch_bounds__(256) k_topvec(const cxd* __restrict__ W, const double* __restrict__ state, int n,
+                                                cxd* __restrict__ x) {
+  __shared__ double sh[8];
+  const int tid = threadIdx.x;
+  double nv[1] = {0.0};
+  for (int r = tid; r < n; r += 256) {
+    cxd v(0.0, 0.0);
+#pragma unroll
+    for (int q = 0; q < SP; ++q) cfma(v, W[(size_t)q * n + r], cxd(state[2 + 2 * q], state[3 + 2 * q]));
+    x[r] = v;
+    nv[0] += cabs2(v);
+  }
+  block_sum<1>(nv, sh);
+  const double s = nv[0] > 0.0 ? 1.0 / sqrt(nv[0]) : 0.0;
+  for (int r = tid; r < n; r += 256) x[r] = x[r] * s;
+}
+
 // M = G - lam I + mu x x^H (n x n, column-major)
 __global__ void k_deflate_shift(const cxd* __restrict__ G, const cxd* __restrict__ x, int n, double lam, double mu,
                                 cxd* __restrict__ M) {
@@ -440,6 +507,51 @@ void dense_start_block(int n, std::vector<cxd>& hx) {
     v.re = nxt();
     v.im = nxt();
   }
+}
+
+int rr_step(const cxd* W, int n, double tol, double* state, cudaStream_t st) {
+  k_rr_step<<<1, 256, 0, st>>>(W, n, tol, state);
+  QBG_LAUNCH_CHECK("k_rr_step");
+  return QBG_OK;
+}
+
+int orth8(cxd* Y, int n, int salt, cudaStream_t st) {
+  k_orth8<<<1, 256, 0, st>>>(Y, n, salt);
+  QBG_LAUNCH_CHECK("k_orth8");
+  return QBG_OK;
+}
+
+int topvec(const cxd* W, const double* state, int n, cxd* x, cudaStream_t st) {
+  k_topvec<<<1, 256, 0, st>>>(W, state, n, x);
+  QBG_LAUNCH_CHECK("k_topvec");
+  return QBG_OK;
+}
+
+int sigma_single(const cxd* Cinv, cxd* CH, int n, const cxd* X0, cxd* X, cxd* W, cxd* Y, cxd* P, double* state,
+                 int maxit, double tol, double* sig, cxd* x_out, cudaStream_t st) {
+  QBG_TRY(conj_transpose(Cinv, CH, n, st));
+  QBG_CUDA(cudaMemcpyAsync(X, X0, sizeof(cxd) * (size_t)n * DENSE_P, cudaMemcpyDeviceToDevice, st));
+  QBG_TRY(orth8(X, n, 0, st));
+  static const double init[2] = {-1.0, 0.0};
+  QBG_CUDA(cudaMemcpyAsync(state, init, sizeof(init), cudaMemcpyHostToDevice, st));
+  double h[2] = {0.0, 0.0};
+  for (int it = 0; it < maxit; ++it) {
+    QBG_TRY(gemm_tall(Cinv, X, W, n, DENSE_P, P, st));
+    QBG_TRY(rr_step(W, n, tol, state, st));
+    if ((it % 8 == 7) || it + 1 == maxit) {
+      QBG_CUDA(cudaMemcpyAsync(h, state, sizeof(h), cudaMemcpyDeviceToHost, st));
+      QBG_CUDA(cudaStreamSynchronize(st));
+      if (h[1] != 0.0 || it + 1 == maxit) break;
+    }
+    QBG_TRY(gemm_tall(CH, W, Y, n, DENSE_P, P, st));
+    QBG_TRY(orth8(Y, n, 8 * (it + 1), st));
+    cxd* t = X;
+    X = Y;
+    Y = t;
+  }
+  *sig = h[0];
+  if (x_out) QBG_TRY(topvec(W, state, n, x_out, st));
+  return QBG_OK;
 }
 
 int deflate_shift(const cxd* G, const cxd* x, int n, double lam, double mu, cxd* M, cudaStream_t st) {

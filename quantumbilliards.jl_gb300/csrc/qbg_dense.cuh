@@ -46,6 +46,25 @@ void dense_start_block(int n, std::vector<cxd>& hx);
 // orthonormal columns of Q (n x p, column-major) in place on the device:
 // modified Gram-Schmidt applied twice, vanishing columns refilled
 int orth_columns(cxd* Q, int n, int p, cudaStream_t st);
+// One-matrix steps of the iteration for callers that run its products as
+// split-k GEMMs over the whole GPU. state (device, 2 + 2 DENSE_P doubles):
+// [est, done, z]; est starts negative. rr_step: G = W^H W, top eigenpair,
+// est = 1/sqrt(lambda_max), done when est changed by <= tol relative; orth8:
+// orthonormal columns of the n x DENSE_P block Y; topvec: x = W z / |W z|.
+int rr_step(const cxd* W, int n, double tol, double* state, cudaStream_t st);
+int orth8(cxd* Y, int n, int salt, cudaStream_t st);
+int topvec(const cxd* W, const double* state, int n, cxd* x, cudaStream_t st);
+// Y = A B for n x n A and n x q B (FP64), split over k to fill the GPU
+// (qbg_ebim.cu); P: scratch of gemm_tall_scratch(n, q) elements
+size_t gemm_tall_scratch(int n, int q);
+int gemm_tall(const cxd* A, const cxd* B, cxd* Y, int n, int q, cxd* P, cudaStream_t st);
+int conj_transpose(const cxd* A, cxd* AH, int n, cudaStream_t st);
+// sigma_min (and, when x_out is given, the unit right singular vector) of one
+// operator from its inverse Cinv, the products as split-k GEMMs over the whole
+// GPU; CH: n x n scratch; X, W, Y: n x DENSE_P; P: gemm_tall_scratch(n,
+// DENSE_P); state: 2 + 2 DENSE_P doubles; synchronizes st every 8 steps.
+int sigma_single(const cxd* Cinv, cxd* CH, int n, const cxd* X0, cxd* X, cxd* W, cxd* Y, cxd* P, double* state,
+                 int maxit, double tol, double* sig, cxd* x_out, cudaStream_t st);
 // M = G - lam I + mu x x^H
 int deflate_shift(const cxd* G, const cxd* x, int n, double lam, double mu, cxd* M, cudaStream_t st);
 

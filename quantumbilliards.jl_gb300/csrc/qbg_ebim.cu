@@ -675,6 +675,16 @@ bool ebim_args_ok(double k, double dk, int32_t nev, int32_t cap, const double* o
 
 }  // namespace
 
+size_t qbg::gemm_tall_scratch(int n, int q) { return tall_scratch(n, q); }
+int qbg::gemm_tall(const cxd* A, const cxd* B, cxd* Y, int n, int q, cxd* P, cudaStream_t st) {
+  return gemm_nq(A, B, Y, n, q, P, st);
+}
+int qbg::conj_transpose(const cxd* A, cxd* AH, int n, cudaStream_t st) {
+  k_conj_transpose<<<dim3((n + 31) / 32, (n + 31) / 32), dim3(32, 8), 0, st>>>(A, AH, n);
+  QBG_LAUNCH_CHECK("k_conj_transpose");
+  return QBG_OK;
+}
+
 extern "C" {
 
 qbg_status qbg_ebim_eig(int64_t n, const void* A, const void* dA, const void* ddA, double k, double dk, int32_t nev,
@@ -708,7 +718,7 @@ qbg_status qbg_ebim_eig(int64_t n, const void* A, const void* dA, const void* dd
 // Here, per step, on the device:
 //  * lambda = sigma_min(A)^2 and x = the right singular vector of A, from the
 //    library's FP64 LU of A, its inverse and the subspace iteration on the
-//    inverse (qbg_dense.cu), iterated to rounding;
+//    inverse (sigma_single: products over the whole GPU), iterated to rounding;
 //  * with u = A x, u1 = A' x, u2 = A'' x: G' x = A'^H u + A^H u1 and
 //    x^H G'' x = 2 Re(u2^H u) + 2 |u1|^2 (matrix-vector products only);
 //  * the eigen-sum is -b^H y with b = G' x - lambda1 x and y the solution of
@@ -722,9 +732,10 @@ qbg_status qbg_ebim_eig(int64_t n, const void* A, const void* dA, const void* dd
 struct Newton {
   Ebim E;
   Dense64 DM;  // LU of the deflated shift M
-  cxd *Ac = nullptr, *G = nullptr, *M = nullptr, *Cinv = nullptr, *work = nullptr, *X0 = nullptr, *xv = nullptr,
-      *u = nullptr, *u1 = nullptr, *u2 = nullptr, *gx = nullptr, *bv = nullptr, *yv = nullptr;
-  double* dsig = nullptr;
+  cxd *Ac = nullptr, *G = nullptr, *M = nullptr, *Cinv = nullptr, *CH = nullptr, *X0 = nullptr, *Xb = nullptr,
+      *Wb = nullptr, *Yb = nullptr, *Ps = nullptr, *xv = nullptr, *u = nullptr, *u1 = nullptr, *u2 = nullptr,
+      *gx = nullptr, *bv = nullptr, *yv = nullptr;
+  double* state = nullptr;
   cxd* dks = nullptr;
   void** dptrs = nullptr;
   ~Newton() {
@@ -757,10 +768,9 @@ int newton_eval(qbg_geom* g, Newton& W, double k, bool derivs, NewtonEval& out) 
     return QBG_ESINGULAR;
   }
   QBG_TRY(E.D.inverse(W.Cinv));
-  QBG_TRY(sigma_iterate(W.Cinv, n, 1, W.X0, W.work, 60, 1e-15, W.dsig, nullptr, W.xv, E.st));
-  QBG_CUDA(cudaMemcpyAsync(&sig, W.dsig, sizeof(double), cudaMemcpyDeviceToHost, E.st));
+  QBG_TRY(sigma_single(W.Cinv, W.CH, n, W.X0, W.Xb, W.Wb, W.Yb, W.Ps, W.state, 64, 1e-15, &sig,
+                       derivs ? W.xv : nullptr, E.st));
   if (!derivs) {
-    QBG_TRY(E.wait());
     out.lam = sig * sig;
     return QBG_OK;
   }
@@ -823,11 +833,11 @@ qbg_status newton_impl(qbg_geom* g, double k0, double a, double b, int maxiter, 
   cudaEventDestroy(ev_in);
   if (e != cudaSuccess) return cuda_status(e, "Newton stream order");
   const size_t bytes = sizeof(cxd) * (size_t)n * n;
-  for (cxd** q : {&E.LU, &E.dA, &E.ddA, &W.Ac, &W.G, &W.M, &W.Cinv}) QBG_TRY(E.alloc(q, bytes));
+  for (cxd** q : {&E.LU, &E.dA, &E.ddA, &W.Ac, &W.G, &W.M, &W.Cinv, &W.CH}) QBG_TRY(E.alloc(q, bytes));
   for (cxd** q : {&W.xv, &W.u, &W.u1, &W.u2, &W.gx, &W.bv, &W.yv}) QBG_TRY(E.alloc(q, sizeof(cxd) * n));
-  QBG_TRY(E.alloc(&W.work, sizeof(cxd) * (size_t)3 * n * DENSE_P));
-  QBG_TRY(E.alloc(&W.X0, sizeof(cxd) * (size_t)n * DENSE_P));
-  QBG_TRY(E.alloc(&W.dsig, sizeof(double)));
+  for (cxd** q : {&W.X0, &W.Xb, &W.Wb, &W.Yb}) QBG_TRY(E.alloc(q, sizeof(cxd) * (size_t)n * DENSE_P));
+  QBG_TRY(E.alloc(&W.Ps, sizeof(cxd) * std::max<size_t>(tall_scratch(n, DENSE_P), 1)));
+  QBG_TRY(E.alloc(&W.state, sizeof(double) * (2 + 2 * DENSE_P)));
   QBG_TRY(E.alloc(&W.dks, sizeof(cxd)));
   QBG_TRY(E.alloc(&W.dptrs, sizeof(void*) * 3));
   QBG_TRY(E.D.bind(E.LU, n, 1, E.st));
