@@ -17,6 +17,7 @@
 //   After the last panel the upper diagonal blocks are inverted so that the
 //   triangular solves are sequences of GEMMs.
 #include <algorithm>
+#include <cooperative_groups.h>
 #include <cstdlib>
 #include <type_traits>
 #include "qbg_linalg.cuh"
@@ -397,6 +398,119 @@ __global__ void __launch_bounds__(1024) k_getrf_panel_smem(cx<T>* A, int n, long
   }
 }
 
+// ---------------------------------------------------------------------------
+// Panel factorisation on a cluster of PC_CS CTAs per matrix: the m x w panel
+// (m = n - j0 rows, w <= 64 columns) is held in the CTAs' shared memory, rows
+// in blocks of rpc = ceil(m / PC_CS). Per column the pivot is the
+// cluster-wide maximum of |re| + |im| over the rows at or below the diagonal
+// (the lowest row on ties, as izamax), the pivot row and the displaced row are
+// exchanged through distributed shared memory, and every CTA scales and
+// updates its own rows: two cluster barriers per column instead of a
+// single-SM walk through global memory. Same factors, pivots and info as
+// k_getrf_panel_smem.
+// ---------------------------------------------------------------------------
+constexpr int PC_CS = 8, PC_THREADS = 256;
+
+template <class T>
+__global__ void __cluster_dims__(PC_CS, 1, 1) __launch_bounds__(PC_THREADS)
+    k_getrf_panel_cluster(cx<T>* A, int n, long long stride, int j0, int nb, int rpc, int* ipiv, int* info) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ unsigned char smraw[];
+  cx<T>* P = reinterpret_cast<cx<T>*>(smraw);  // column c of the own rows at P + c * rpc
+  __shared__ T cand_v;
+  __shared__ int cand_i;
+  __shared__ cx<T> prow[64], orow[64];
+  __shared__ T wv[PC_THREADS / 32];
+  __shared__ int wi[PC_THREADS / 32];
+  __shared__ int s_p;
+  const int rank = (int)cl.block_rank();
+  const int mat = blockIdx.x / PC_CS;
+  cx<T>* a = A + (long long)mat * stride;
+  int* piv = ipiv + (long long)mat * n;
+  const int m = n - j0, w = min(nb, n - j0);
+  const int r0 = rank * rpc;
+  const int rows = max(0, min(rpc, m - r0));
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int e = tid; e < rows * w; e += PC_THREADS) {
+    const int i = e % rows, c = e / rows;
+    P[c * rpc + i] = a[(long long)(j0 + r0 + i) + (long long)(j0 + c) * n];
+  }
+  __syncthreads();
+  for (int c = 0; c < w; ++c) {
+    T best = T(-1);
+    int bi = 0x7fffffff;
+    for (int i = tid; i < rows; i += PC_THREADS) {
+      const int pr = r0 + i;
+      if (pr >= c) argmax_merge(best, bi, cabs1(P[c * rpc + i]), pr);
+    }
+    warp_argmax(best, bi);
+    if (lane == 0) {
+      wv[wid] = best;
+      wi[wid] = bi;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      for (int q = 1; q < PC_THREADS / 32; ++q) argmax_merge(best, bi, wv[q], wi[q]);
+      cand_v = best;
+      cand_i = bi;
+    }
+    cl.sync();  // every CTA's candidate is visible
+    if (tid == 0) {
+      T bv = T(-1);
+      int bidx = 0x7fffffff;
+      for (int q = 0; q < PC_CS; ++q)
+        argmax_merge(bv, bidx, *cl.map_shared_rank(&cand_v, q), *cl.map_shared_rank(&cand_i, q));
+      if (bidx >= m) bidx = c;
+      s_p = bidx;
+      if (rank == 0) {
+        piv[j0 + c] = j0 + bidx;
+        if (!(bv > T(0)) && info[mat] == 0) info[mat] = j0 + c + 1;
+      }
+    }
+    __syncthreads();
+    const int p = s_p;
+    const int oc = c / rpc, op = p / rpc;
+    {
+      const cx<T>* Pp = cl.map_shared_rank(P, op);
+      const cx<T>* Pc = cl.map_shared_rank(P, oc);
+      for (int q = tid; q < w; q += PC_THREADS) {
+        prow[q] = Pp[q * rpc + (p - op * rpc)];
+        if (rank == op && p != c) orow[q] = Pc[q * rpc + (c - oc * rpc)];
+      }
+    }
+    cl.sync();  // every remote read of this column is done before the exchange writes
+    if (p != c) {
+      if (rank == oc)
+        for (int q = tid; q < w; q += PC_THREADS) P[q * rpc + (c - r0)] = prow[q];
+      if (rank == op)
+        for (int q = tid; q < w; q += PC_THREADS) P[q * rpc + (p - r0)] = orow[q];
+    }
+    __syncthreads();
+    const cx<T> pv = prow[c];
+    const bool nz = (pv.re != T(0) || pv.im != T(0));
+    const cx<T> inv = nz ? cinv(pv) : cx<T>(0, 0);
+    for (int i = tid; i < rows; i += PC_THREADS) {
+      if (r0 + i <= c) continue;
+      cx<T> l = P[c * rpc + i];
+      if (nz) {
+        l = l * inv;
+        P[c * rpc + i] = l;
+      }
+      for (int q = c + 1; q < w; ++q) cfms(P[q * rpc + i], l, prow[q]);
+    }
+    __syncthreads();
+  }
+  cl.sync();  // no CTA leaves while another might still read its shared memory
+  for (int e = tid; e < rows * w; e += PC_THREADS) {
+    const int i = e % rows, c = e / rows;
+    a[(long long)(j0 + r0 + i) + (long long)(j0 + c) * n] = P[c * rpc + i];
+  }
+}
+
+// largest rows per CTA of the cluster panel (64 complex64 columns within 224 KiB)
+constexpr int PC_MAX_RPC = (224 * 1024) / (64 * 8);
+
 // row interchanges of one panel on the columns outside the panel
 template <class T>
 __global__ void k_laswp(cx<T>* A, int n, long long stride, int j0, int nb, const int* ipiv) {
@@ -677,6 +791,19 @@ static int lu_factor_one(LUBatch<T>& f, cudaStream_t st, cudaEvent_t after_first
                                   (int)kPanelSmem));
     panel_attr[sizeof(T) == 8] = true;
   }
+  // complex64 panels of up to 64 columns and n <= PC_CS * PC_MAX_RPC rows go to a
+  // cluster of CTAs (QBG_LU_CLUSTER=0 in the environment keeps one CTA per panel)
+  static const bool cluster_on = [] {
+    const char* e = std::getenv("QBG_LU_CLUSTER");
+    return !(e && *e == '0');
+  }();
+  const bool use_cluster = cluster_on && sizeof(T) == sizeof(float) && nb <= 64 && n <= PC_CS * PC_MAX_RPC;
+  static bool cluster_attr[2] = {false, false};
+  if (use_cluster && !cluster_attr[sizeof(T) == 8]) {
+    QBG_CUDA(cudaFuncSetAttribute(k_getrf_panel_cluster<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  PC_MAX_RPC * 64 * (int)sizeof(cx<T>)));
+    cluster_attr[sizeof(T) == 8] = true;
+  }
   QBG_CUDA(cudaMemsetAsync(f.info, 0, sizeof(int) * batch, st));
   // two-level right-looking LU: panels of nb columns inside outer blocks of
   // LU_OUTER panels. A panel's updates reach only the columns of its outer
@@ -698,7 +825,13 @@ static int lu_factor_one(LUBatch<T>& f, cudaStream_t st, cudaEvent_t after_first
     const int E = min(n, J0 + LU_OUTER * nb);  // outer block columns [J0, E)
     for (int j0 = J0; j0 < E; j0 += nb) {
       const int w = min(nb, n - j0);
-      if (smem_panel) {
+      if (use_cluster) {
+        const int rpc = (n - j0 + PC_CS - 1) / PC_CS;
+        const size_t smem = (size_t)rpc * 64 * sizeof(cx<T>);
+        k_getrf_panel_cluster<T><<<batch * PC_CS, PC_THREADS, smem, st>>>(f.A, n, f.stride, j0, nb, rpc, f.ipiv,
+                                                                          f.info);
+        QBG_LAUNCH_CHECK("k_getrf_panel_cluster");
+      } else if (smem_panel) {
         const size_t smem = (size_t)(n - j0) * sub * sizeof(cx<T>);
         k_getrf_panel_smem<T><<<batch, 1024, smem, st>>>(f.A, n, f.stride, j0, nb, sub, f.ipiv, f.info);
         QBG_LAUNCH_CHECK("k_getrf_panel_smem");
