@@ -262,6 +262,12 @@ qbg_status qbg_beyn_destroy(qbg_beyn* b);
  * give up at once), qbg_clear_tc_error resets the sticky flag there. Both
  * synchronize the device. Meant for tests of that path. */
 qbg_status qbg_set_tc_wait_limit(int64_t polls);
+/* Validation entry (no counterpart in the reference): the library's batched
+ * FP64 LU and explicit inverses of `batch` n x n complex128 matrices (host,
+ * column-major, contiguous), X = A^{-1}; with sig != NULL also sigma_min of
+ * every matrix by the device subspace iteration on its inverse, and with
+ * work_out != NULL its final blocks (3 n x 8 complex128 per matrix). */
+qbg_status qbg_dense_inverse(int32_t n, int32_t batch, const double* A, double* X, double* sig, double* work_out);
 qbg_status qbg_clear_tc_error(void);
 
 /* Smallest singular value of A(k) for nk real wavenumbers (the :svd branch of

@@ -667,6 +667,45 @@ qbg_status qbg_cgemm_c64(int32_t engine, int32_t M, int32_t N, int32_t K, const 
   return QBG_OK;
 }
 
+qbg_status qbg_dense_inverse(int32_t n, int32_t batch, const double* A, double* X, double* sig, double* work_out) {
+  if (n < 1 || batch < 1 || batch > 65535 || !A || !X) {
+    set_error("qbg_dense_inverse: invalid arguments");
+    return QBG_EINVAL;
+  }
+  cudaStream_t st = nullptr;
+  QBG_CUDA(stream_create(&st));
+  int s = QBG_OK;
+  {
+    Dense64 D;
+    cxd *Cinv = nullptr, *work = nullptr, *X0 = nullptr;
+    double* dsig = nullptr;
+    const size_t nn = (size_t)n * n;
+    if (!(s = D.create(n, batch, st)) && !(s = D.alloc(&Cinv, sizeof(cxd) * nn * batch)) &&
+        !(s = D.alloc(&work, sizeof(cxd) * (size_t)3 * n * DENSE_P * batch)) &&
+        !(s = D.alloc(&X0, sizeof(cxd) * (size_t)n * DENSE_P)) && !(s = D.alloc(&dsig, sizeof(double) * batch))) {
+      std::vector<cxd> hx;
+      dense_start_block(n, hx);
+      cudaError_t e = cudaMemcpyAsync(D.f.A, A, sizeof(cxd) * nn * batch, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(X0, hx.data(), sizeof(cxd) * hx.size(), cudaMemcpyHostToDevice, st);
+      s = e == cudaSuccess ? QBG_OK : cuda_status(e, "qbg_dense_inverse");
+      if (!s) s = lu_factor<double>(D.f, st);
+      if (!s) s = D.inverse(Cinv);
+      if (!s && sig) s = sigma_iterate(Cinv, n, batch, X0, work, 40, 1e-13, dsig, nullptr, nullptr, st);
+      if (!s) {
+        e = cudaMemcpyAsync(X, Cinv, sizeof(cxd) * nn * batch, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess && sig)
+          e = cudaMemcpyAsync(sig, dsig, sizeof(double) * batch, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess && work_out)
+          e = cudaMemcpyAsync(work_out, work, sizeof(cxd) * (size_t)3 * n * DENSE_P * batch, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) s = cuda_status(e, "qbg_dense_inverse");
+      }
+    }
+  }
+  cudaStreamDestroy(st);
+  return s;
+}
+
 qbg_status qbg_set_tc_wait_limit(int64_t polls) { return tc_set_wait_limit(polls); }
 
 qbg_status qbg_clear_tc_error(void) { return tc_clear_error(); }

@@ -109,62 +109,87 @@ __device__ void orth_cgs2(cxd* Q, int n, double* sh, int salt) {
 }
 
 // largest eigenvalue and its eigenvector of the Hermitian SP x SP matrix G
-// (column-major, complex) by cyclic Jacobi on its real 2SP x 2SP embedding
-// [[Re G, -Im G], [Im G, Re G]]; one thread.
-__device__ void herm_top(const double* G, double* lam, double* z) {
+// (column-major, complex, exactly Hermitian) by cyclic Jacobi on its real
+// 2SP x 2SP embedding [[Re G, -Im G], [Im G, Re G]], run by one whole warp on
+// the shared scratch wk (2 (2SP)^2 doubles): for each rotation every lane
+// derives the same (c, s) from the pivot entries, then lane k < 2SP rotates
+// column k's pair (p, q) and row k's pair of the matrix, lanes 2SP.. the
+// eigenvector columns. Lane 0 writes lam and z (SP complex). A one-thread
+// version on thread-local 16 x 16 arrays lost the symmetry of the matrix
+// after its first sweep when built with device optimisation for sm_103a
+// (correct at -G and on the host), hence the shared-memory form.
+__device__ void herm_top(const double* G, double* lam, double* z, double* wk) {
   constexpr int M2 = 2 * SP;
-  double a[M2][M2], v[M2][M2];
-  for (int c = 0; c < SP; ++c)
-    for (int r = 0; r < SP; ++r) {
-      const double gr = G[2 * (c * SP + r)], gi = G[2 * (c * SP + r) + 1];
-      a[r][c] = gr;
-      a[r + SP][c + SP] = gr;
-      a[r + SP][c] = gi;
-      a[r][c + SP] = -gi;
-    }
-  for (int r = 0; r < M2; ++r)
-    for (int c = 0; c < M2; ++c) v[r][c] = r == c ? 1.0 : 0.0;
+  const int lane = threadIdx.x & 31;
+  double* a = wk;
+  double* v = wk + M2 * M2;
+  for (int e = lane; e < M2 * M2; e += 32) {
+    const int r = e / M2, c = e % M2, gr = r % SP, gc = c % SP;
+    const double re = G[2 * (gc * SP + gr)], im = G[2 * (gc * SP + gr) + 1];
+    a[e] = (r < SP) == (c < SP) ? re : (r >= SP ? im : -im);
+    v[e] = r == c ? 1.0 : 0.0;
+  }
+  __syncwarp();
   for (int sweep = 0; sweep < 40; ++sweep) {
     double off = 0.0, dia = 0.0;
-    for (int r = 0; r < M2; ++r)
-      for (int c = 0; c < M2; ++c) (r == c ? dia : off) += a[r][c] * a[r][c];
+    for (int e = lane; e < M2 * M2; e += 32) {
+      const double t = a[e] * a[e];
+      if (e / M2 == e % M2)
+        dia += t;
+      else
+        off += t;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      dia += __shfl_xor_sync(0xffffffffu, dia, o);
+    }
+    // lane 0's sums decide for the whole warp (the butterfly may round per lane)
+    off = __shfl_sync(0xffffffffu, off, 0);
+    dia = __shfl_sync(0xffffffffu, dia, 0);
     if (!(off > 1e-32 * dia)) break;
     for (int p = 0; p < M2 - 1; ++p)
       for (int q = p + 1; q < M2; ++q) {
-        const double apq = a[p][q];
+        const double apq = a[p * M2 + q];
         if (fabs(apq) < 1e-300) continue;
-        const double th = (a[q][q] - a[p][p]) / (2.0 * apq);
+        const double th = (a[q * M2 + q] - a[p * M2 + p]) / (2.0 * apq);
         const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
         const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-        for (int k = 0; k < M2; ++k) {
-          const double akp = a[k][p], akq = a[k][q];
-          a[k][p] = c * akp - s * akq;
-          a[k][q] = s * akp + c * akq;
+        __syncwarp();
+        if (lane < M2) {
+          const double akp = a[lane * M2 + p], akq = a[lane * M2 + q];
+          a[lane * M2 + p] = c * akp - s * akq;
+          a[lane * M2 + q] = s * akp + c * akq;
+        } else {
+          const int k = lane - M2;
+          const double vkp = v[k * M2 + p], vkq = v[k * M2 + q];
+          v[k * M2 + p] = c * vkp - s * vkq;
+          v[k * M2 + q] = s * vkp + c * vkq;
         }
-        for (int k = 0; k < M2; ++k) {
-          const double apk = a[p][k], aqk = a[q][k];
-          a[p][k] = c * apk - s * aqk;
-          a[q][k] = s * apk + c * aqk;
+        __syncwarp();
+        if (lane < M2) {
+          const double apk = a[p * M2 + lane], aqk = a[q * M2 + lane];
+          a[p * M2 + lane] = c * apk - s * aqk;
+          a[q * M2 + lane] = s * apk + c * aqk;
         }
-        for (int k = 0; k < M2; ++k) {
-          const double vkp = v[k][p], vkq = v[k][q];
-          v[k][p] = c * vkp - s * vkq;
-          v[k][q] = s * vkp + c * vkq;
-        }
+        __syncwarp();
       }
   }
-  int best = 0;
-  for (int i = 1; i < M2; ++i)
-    if (a[i][i] > a[best][best]) best = i;
-  *lam = a[best][best];
-  double nrm = 0.0;
-  for (int i = 0; i < SP; ++i) {
-    z[2 * i] = v[i][best];
-    z[2 * i + 1] = v[i + SP][best];
-    nrm += z[2 * i] * z[2 * i] + z[2 * i + 1] * z[2 * i + 1];
+  if (lane == 0) {
+    int best = 0;
+    for (int i = 1; i < M2; ++i)
+      if (a[i * M2 + i] > a[best * M2 + best]) best = i;
+    *lam = a[best * M2 + best];
+    double nrm = 0.0;
+    for (int i = 0; i < SP; ++i) {
+      z[2 * i] = v[i * M2 + best];
+      z[2 * i + 1] = v[(i + SP) * M2 + best];
+      nrm += z[2 * i] * z[2 * i] + z[2 * i + 1] * z[2 * i + 1];
+    }
+    nrm = nrm > 0.0 ? 1.0 / sqrt(nrm) : 0.0;
+    for (int i = 0; i < 2 * SP; ++i) z[i] *= nrm;
   }
-  nrm = nrm > 0.0 ? 1.0 / sqrt(nrm) : 0.0;
-  for (int i = 0; i < 2 * SP; ++i) z[i] *= nrm;
+  __syncwarp();
 }
 
 // One CTA per matrix: the subspace iteration on C_b = A_b^{-1} (n x n,
@@ -184,6 +209,7 @@ __global__ void __launch_bounds__(256) k_sigma_iter(const cxd* __restrict__ Cb, 
   __shared__ double Gs[2 * SP * SP];
   __shared__ double zs[2 * SP];
   __shared__ double lam_s;
+  __shared__ double hw[2 * 4 * SP * SP];
   for (size_t e = tid; e < (size_t)n * SP; e += 256) X[e] = X0[e];
   __syncthreads();
   orth_cgs2(X, n, sh, 0);
@@ -237,18 +263,22 @@ __global__ void __launch_bounds__(256) k_sigma_iter(const cxd* __restrict__ Cb, 
           }
       }
       block_sum<SP * (SP + 1)>(g, sh);
-      if (tid == 0) {
-        int e = 0;
-        for (int j = 0; j < SP; ++j)
-          for (int i = 0; i <= j; ++i, e += 2) {
-            Gs[2 * (j * SP + i)] = g[e];
-            Gs[2 * (j * SP + i) + 1] = g[e + 1];
-            Gs[2 * (i * SP + j)] = g[e];
-            Gs[2 * (i * SP + j) + 1] = -g[e + 1];
-          }
-        double lam = 0.0;
-        herm_top(Gs, &lam, zs);
-        lam_s = lam;
+      if (wid == 0) {
+        if (lane == 0) {
+          int e = 0;
+          for (int j = 0; j < SP; ++j)
+            for (int i = 0; i <= j; ++i, e += 2) {
+              // exactly Hermitian: the diagonal of W^H W is real, the summed
+              // products only leave a rounding residue there
+              const double im = (i == j) ? 0.0 : g[e + 1];
+              Gs[2 * (j * SP + i)] = g[e];
+              Gs[2 * (j * SP + i) + 1] = im;
+              Gs[2 * (i * SP + j)] = g[e];
+              Gs[2 * (i * SP + j) + 1] = -im;
+            }
+        }
+        __syncwarp();
+        herm_top(Gs, &lam_s, zs, hw);
       }
       __syncthreads();
     }
@@ -317,6 +347,8 @@ __global__ void __launch_bounds__(256) k_sigma_iter(const cxd* __restrict__ Cb, 
 __global__ void __launch_bounds__(256) k_rr_step(const cxd* __restrict__ W, int n, double tol, double* state) {
   __shared__ double sh[8 * SP * (SP + 1)];
   __shared__ double Gs[2 * SP * SP];
+  __shared__ double hw[2 * 4 * SP * SP];
+  __shared__ double lam_s;
   const int tid = threadIdx.x;
   double g[SP * (SP + 1)];
 #pragma unroll
@@ -335,17 +367,22 @@ __global__ void __launch_bounds__(256) k_rr_step(const cxd* __restrict__ W, int 
       }
   }
   block_sum<SP * (SP + 1)>(g, sh);
+  if (tid >= 32) return;
   if (tid == 0) {
     int e = 0;
     for (int j = 0; j < SP; ++j)
       for (int i = 0; i <= j; ++i, e += 2) {
+        const double im = (i == j) ? 0.0 : g[e + 1];  // real diagonal (see k_sigma_iter)
         Gs[2 * (j * SP + i)] = g[e];
-        Gs[2 * (j * SP + i) + 1] = g[e + 1];
+        Gs[2 * (j * SP + i) + 1] = im;
         Gs[2 * (i * SP + j)] = g[e];
-        Gs[2 * (i * SP + j) + 1] = -g[e + 1];
+        Gs[2 * (i * SP + j) + 1] = -im;
       }
-    double lam = 0.0;
-    herm_top(Gs, &lam, state + 2);
+  }
+  __syncwarp();
+  herm_top(Gs, &lam_s, state + 2, hw);
+  if (tid == 0) {
+    const double lam = lam_s;
     const bool ok = lam > 0.0 && isfinite(lam);
     const double cur = ok ? 1.0 / sqrt(lam) : 0.0;
     const double prev = state[0];

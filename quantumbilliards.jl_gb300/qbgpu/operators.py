@@ -83,7 +83,7 @@ class Workspace:
         if reduction is not None:
             fund, orbit, scale = reduction
             self._red = (np.ascontiguousarray(fund, dtype=np.int64), np.ascontiguousarray(orbit, dtype=np.int64),
-                         np.ascontiguousarray(np.asarray(scale, dtype=np.complex128).view(np.float64)))
+                         np.ascontiguousarray(scale, dtype=np.complex128).view(np.float64))
             d.m = len(fund)
             d.norb = orbit.shape[1]
             d.fund = L.dptr(self._red[0], C.c_int64)

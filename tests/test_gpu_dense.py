@@ -1,0 +1,71 @@
+"""GPU: the library's FP64 dense path through qbg_dense_inverse -- batched LU
+(own panel and GEMM kernels), explicit inverses, and sigma_min by the device
+subspace iteration on the inverse (the :svd branch, macros.jl:159-161).
+
+* matrices with a prescribed spectrum A = U diag(s) V^H (U, V Haar-random
+  unitary, n = 100 and 257, so no tile divides n), including a doubly
+  degenerate smallest singular value: |A X - I| <= 1e-12 * cond(A) and
+  sigma_min to 1e-15 * sigma_max absolute (the backward-stable bound);
+* the C1 circle matrices (DLP Kress, N = 512 at k = 42) at the first eight k
+  of the golden sweep, whose smallest singular values come in exact pairs
+  (the rotational symmetry): sigma_min against the oracle's LAPACK values
+  (tests/golden/c1_sweep.json) to 2e-12 relative.
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).parent / "golden"
+
+
+def _haar(n, rng):
+    z = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    q, r = np.linalg.qr(z)
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+def _run(lib, L, As):
+    batch, n = len(As), As[0].shape[0]
+    Ac = np.ascontiguousarray(np.stack(As).transpose(0, 2, 1))  # column-major per matrix
+    X = np.empty_like(Ac)
+    sig = np.zeros(batch)
+    L.check(lib.qbg_dense_inverse(n, batch, L.vptr(Ac), L.vptr(X), L.dptr(sig), None))
+    return [x.T for x in X], sig
+
+
+@pytest.mark.parametrize("n", [100, 257])
+def test_prescribed_spectrum(qb, n):
+    from qbgpu import _lib as L
+    lib = L.load()
+    rng = np.random.default_rng(20 + n)
+    As, smin, conds = [], [], []
+    for case in range(3):
+        s = np.sort(rng.uniform(0.5, 3.0, n))[::-1]
+        s[-1] = 10.0 ** -(2 + case)
+        if case != 1:
+            s[-2] = s[-1]  # a degenerate smallest pair
+        As.append((_haar(n, rng) * s) @ _haar(n, rng).conj().T)
+        smin.append(s[-1])
+        conds.append(s[0] / s[-1])
+    Xs, sig = _run(lib, L, As)
+    for A, X, c in zip(As, Xs, conds):
+        assert np.abs(A @ X - np.eye(n)).max() <= 1e-12 * c
+    # a backward-stable sigma_min is exact to a few eps * sigma_max in absolute terms
+    assert np.all(np.abs(sig - np.array(smin)) <= 1e-15 * 3.0), (sig - np.array(smin))
+
+
+def test_c1_degenerate_pairs(qb):
+    from qbgpu import _lib as L
+    lib = L.load()
+    g = json.loads((GOLD / "c1_sweep.json").read_text())
+    ks, so = np.array(g["ks"][:8]), np.array(g["sigma"][:8])
+    b = qb.make_circle(1.0)
+    sol = qb.DLP_kress(g["pts_scaling_factor"], b)
+    pts = qb.evaluate_points(sol, b, 42.0)
+    ws = qb.Workspace(sol, pts)
+    As = qb.assemble(ws, ks)
+    _, sig = _run(lib, L, As)
+    assert np.all(np.abs(sig - so) <= 2e-12 * so), np.abs(sig - so) / so
