@@ -263,11 +263,25 @@ qbg_status qbg_beyn_destroy(qbg_beyn* b);
  * synchronize the device. Meant for tests of that path. */
 qbg_status qbg_set_tc_wait_limit(int64_t polls);
 /* Validation entry (no counterpart in the reference): the library's batched
- * FP64 LU and explicit inverses of `batch` n x n complex128 matrices (host,
- * column-major, contiguous), X = A^{-1}; with sig != NULL also sigma_min of
+ * LU and explicit inverses of `batch` n x n complex128 matrices (host,
+ * column-major, contiguous), X = A^{-1}. prec QBG_PREC_FP64: FP64 LU (the
+ * path of sigma_min, EBIM and Newton); with sig != NULL also sigma_min of
  * every matrix by the device subspace iteration on its inverse, and with
- * work_out != NULL its final blocks (3 n x 8 complex128 per matrix). */
-qbg_status qbg_dense_inverse(int32_t n, int32_t batch, const double* A, double* X, double* sig, double* work_out);
+ * work_out != NULL its final blocks (3 n x 8 complex128 per matrix).
+ * prec QBG_PREC_FP32: the matrices rounded to complex64 and factored by the
+ * complex64 LU of the Beyn mixed form (panels and tensor-core updates as the
+ * current plan and GEMM engine select), X widened back; sig and work_out must
+ * be NULL. */
+qbg_status qbg_dense_inverse(int32_t n, int32_t batch, int32_t prec, const double* A, double* X, double* sig,
+                             double* work_out);
+/* Plan of the batched LU, process-wide (no counterpart in the reference):
+ * panels per outer block of the two-level factorisation (1..16, default 4;
+ * <= 0 keeps the current value) and the complex64 panel form (-1 automatic:
+ * a cluster of 8 CTAs per panel for batches of at most 4 matrices; 0 one CTA
+ * per panel; 1 a cluster). QBG_LU_OUTER and QBG_LU_CLUSTER in the environment
+ * give the initial values. */
+qbg_status qbg_set_lu_plan(int32_t outer, int32_t cluster);
+qbg_status qbg_get_lu_plan(int32_t* outer, int32_t* cluster);
 qbg_status qbg_clear_tc_error(void);
 
 /* Smallest singular value of A(k) for nk real wavenumbers (the :svd branch of

@@ -667,19 +667,62 @@ qbg_status qbg_cgemm_c64(int32_t engine, int32_t M, int32_t N, int32_t K, const 
   return QBG_OK;
 }
 
-qbg_status qbg_dense_inverse(int32_t n, int32_t batch, const double* A, double* X, double* sig, double* work_out) {
-  if (n < 1 || batch < 1 || batch > 65535 || !A || !X) {
+qbg_status qbg_dense_inverse(int32_t n, int32_t batch, int32_t prec, const double* A, double* X, double* sig,
+                             double* work_out) {
+  if (n < 1 || batch < 1 || batch > 65535 || !A || !X || (prec != QBG_PREC_FP64 && prec != QBG_PREC_FP32) ||
+      (prec == QBG_PREC_FP32 && (sig || work_out))) {
     set_error("qbg_dense_inverse: invalid arguments");
     return QBG_EINVAL;
   }
   cudaStream_t st = nullptr;
   QBG_CUDA(stream_create(&st));
   int s = QBG_OK;
+  const size_t nn = (size_t)n * n;
+  if (prec == QBG_PREC_FP32) {
+    LUBatch<float> f;
+    f.n = n;
+    f.batch = batch;
+    f.stride = (long long)nn;
+    f.nb = std::min(64, n);
+    f.nblk = (n + f.nb - 1) / f.nb;
+    std::vector<void*> mem;
+    auto alloc = [&](auto** p, size_t bytes) {
+      int r = dmalloc(p, bytes);
+      if (!r) mem.push_back(*p);
+      return r;
+    };
+    cxd* Ad = nullptr;
+    cxf* Xf = nullptr;
+    if (!(s = alloc(&Ad, sizeof(cxd) * nn * batch)) && !(s = alloc(&f.A, sizeof(cxf) * nn * batch)) &&
+        !(s = alloc(&Xf, sizeof(cxf) * nn * batch)) && !(s = alloc(&f.ipiv, sizeof(int) * (size_t)n * batch)) &&
+        !(s = alloc(&f.perm, sizeof(int) * (size_t)n * batch)) && !(s = alloc(&f.info, sizeof(int) * batch)) &&
+        !(s = alloc(&f.Linv, sizeof(cxf) * (size_t)f.nblk * f.nb * f.nb * batch)) &&
+        !(s = alloc(&f.Uinv, sizeof(cxf) * (size_t)f.nblk * f.nb * f.nb * batch))) {
+      cudaError_t e = cudaMemcpyAsync(Ad, A, sizeof(cxd) * nn * batch, cudaMemcpyHostToDevice, st);
+      s = e == cudaSuccess ? QBG_OK : cuda_status(e, "qbg_dense_inverse");
+      if (!s) s = convert_d2f(Ad, f.A, (long long)(nn * batch), st);
+      if (!s) s = lu_factor<float>(f, st);
+      if (!s) s = lu_inverse<float>(f, Xf, st);
+      if (!s) s = tc_check(st);
+      if (!s) {
+        e = cudaMemsetAsync(Ad, 0, sizeof(cxd) * nn * batch, st);
+        s = e == cudaSuccess ? axpy_f2d(Xf, Ad, (long long)(nn * batch), st) : cuda_status(e, "qbg_dense_inverse");
+      }
+      if (!s) {
+        e = cudaMemcpyAsync(X, Ad, sizeof(cxd) * nn * batch, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) s = cuda_status(e, "qbg_dense_inverse");
+      }
+    }
+    cudaStreamSynchronize(st);
+    for (void* p : mem) dfree(p);
+    cudaStreamDestroy(st);
+    return s;
+  }
   {
     Dense64 D;
     cxd *Cinv = nullptr, *work = nullptr, *X0 = nullptr;
     double* dsig = nullptr;
-    const size_t nn = (size_t)n * n;
     if (!(s = D.create(n, batch, st)) && !(s = D.alloc(&Cinv, sizeof(cxd) * nn * batch)) &&
         !(s = D.alloc(&work, sizeof(cxd) * (size_t)3 * n * DENSE_P * batch)) &&
         !(s = D.alloc(&X0, sizeof(cxd) * (size_t)n * DENSE_P)) && !(s = D.alloc(&dsig, sizeof(double) * batch))) {
@@ -704,6 +747,23 @@ qbg_status qbg_dense_inverse(int32_t n, int32_t batch, const double* A, double* 
   }
   cudaStreamDestroy(st);
   return s;
+}
+
+qbg_status qbg_set_lu_plan(int32_t outer, int32_t cluster) {
+  if (outer > 16 || cluster > 1 || cluster < -1) {
+    set_error("qbg_set_lu_plan: outer must be <= 16 and cluster -1, 0 or 1");
+    return QBG_EINVAL;
+  }
+  set_lu_plan(outer, cluster);
+  return QBG_OK;
+}
+
+qbg_status qbg_get_lu_plan(int32_t* outer, int32_t* cluster) {
+  int o = 0, c = 0;
+  get_lu_plan(&o, &c);
+  if (outer) *outer = o;
+  if (cluster) *cluster = c;
+  return QBG_OK;
 }
 
 qbg_status qbg_set_tc_wait_limit(int64_t polls) { return tc_set_wait_limit(polls); }

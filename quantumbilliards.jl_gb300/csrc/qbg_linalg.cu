@@ -16,6 +16,7 @@
 //     5. gemm            A22 -= L21 U12       (trailing update)
 //   After the last panel the upper diagonal blocks are inverted so that the
 //   triangular solves are sequences of GEMMs.
+#include <atomic>
 #include <algorithm>
 #include <cooperative_groups.h>
 #include <cstdlib>
@@ -249,6 +250,36 @@ __device__ __forceinline__ void warp_argmax(T& best, int& bi) {
   }
 }
 
+// dst[c * ldd + i] = src[i + c * lds] for i < rows, c < cols (a column block
+// from global to shared memory), eight columns at a time (four for
+// complex128): a thread issues the loads of its row in those columns before it
+// stores them, so that the loads
+// overlap instead of each waiting for the previous shared-memory store, and
+// no index is divided.
+template <class T>
+__device__ __forceinline__ void load_block(cx<T>* dst, int ldd, const cx<T>* src, long long lds, int rows, int cols,
+                                           int tid, int nt) {
+  constexpr int G = sizeof(T) == 4 ? 8 : 4;  // columns per group (registers)
+  for (int c0 = 0; c0 < cols; c0 += G)
+    for (int i = tid; i < rows; i += nt) {
+      cx<T> v[G];
+#pragma unroll
+      for (int u = 0; u < G; ++u)
+        if (c0 + u < cols) v[u] = src[i + (long long)(c0 + u) * lds];
+#pragma unroll
+      for (int u = 0; u < G; ++u)
+        if (c0 + u < cols) dst[(c0 + u) * ldd + i] = v[u];
+    }
+}
+
+// the reverse copy, shared to global memory
+template <class T>
+__device__ __forceinline__ void store_block(cx<T>* dst, long long ldd, const cx<T>* src, int lds, int rows, int cols,
+                                            int tid, int nt) {
+  for (int c = 0; c < cols; ++c)
+    for (int i = tid; i < rows; i += nt) dst[i + (long long)c * ldd] = src[c * lds + i];
+}
+
 template <class T>
 __global__ void __launch_bounds__(1024) k_getrf_panel_smem(cx<T>* A, int n, long long stride, int j0, int nb,
                                                           int sub, int* ipiv, int* info) {
@@ -268,10 +299,7 @@ __global__ void __launch_bounds__(1024) k_getrf_panel_smem(cx<T>* A, int n, long
   for (int s0 = j0; s0 < jend; s0 += sub) {
     const int w = min(sub, jend - s0);
     const int m = n - s0;  // rows held in smem
-    for (int e = tid; e < m * w; e += nt) {
-      const int r = e % m, c = e / m;
-      S[c * m + r] = a[(s0 + r) + (long long)(s0 + c) * n];
-    }
+    load_block<T>(S, m, a + s0 + (long long)s0 * n, n, m, w, tid, nt);
     __syncthreads();
     T best = T(-1);
     int bi = 0x7fffffff;
@@ -341,10 +369,7 @@ __global__ void __launch_bounds__(1024) k_getrf_panel_smem(cx<T>* A, int n, long
       s_cnt = cnt;
     }
     __syncthreads();  // sub-panel factored; permutation composed
-    for (int e = tid; e < m * w; e += nt) {
-      const int r = e % m, c = e / m;
-      a[(s0 + r) + (long long)(s0 + c) * n] = S[c * m + r];
-    }
+    store_block<T>(a + s0 + (long long)s0 * n, n, S, m, m, w, tid, nt);
     // the interchanges on the other panel columns [j0, s0) and [s0 + w, jend):
     // whole columns per round, every read of a round before its writes
     const int cnt = s_cnt;
@@ -382,15 +407,29 @@ __global__ void __launch_bounds__(1024) k_getrf_panel_smem(cx<T>* A, int n, long
         }
       }
       __syncthreads();
-      // A22 -= L21 U12, one thread per row
+      // A22 -= L21 U12, one thread per row; the row's entries of CH columns are
+      // loaded together before they are updated, so the global-memory latency
+      // is paid once per CH columns instead of once per column (within the 64
+      // registers a thread has at 1024 threads)
+      constexpr int CH = sizeof(T) == 4 ? 8 : 4;
       for (int r = w + tid; r < m; r += nt) {
         cx<T> lr[8];
-        for (int l = 0; l < w; ++l) lr[l] = S[l * m + r];
-        cx<T>* pr = a + (s0 + r);
-        for (int q = 0; q < nr; ++q) {
-          cx<T> v = pr[(long long)(s0 + w + q) * n];
-          for (int l = 0; l < w; ++l) cfms(v, lr[l], Us[l * 64 + q]);
-          pr[(long long)(s0 + w + q) * n] = v;
+#pragma unroll
+        for (int l = 0; l < 8; ++l) lr[l] = l < w ? S[l * m + r] : cx<T>(0, 0);
+        cx<T>* pr = a + (s0 + r) + (long long)(s0 + w) * n;
+        for (int q0 = 0; q0 < nr; q0 += CH) {
+          cx<T> v[CH];
+#pragma unroll
+          for (int u = 0; u < CH; ++u)
+            if (q0 + u < nr) v[u] = pr[(long long)(q0 + u) * n];
+#pragma unroll
+          for (int u = 0; u < CH; ++u)
+            if (q0 + u < nr) {
+#pragma unroll
+              for (int l = 0; l < 8; ++l)
+                if (l < w) cfms(v[u], lr[l], Us[l * 64 + q0 + u]);
+              pr[(long long)(q0 + u) * n] = v[u];
+            }
         }
       }
     }
@@ -401,15 +440,26 @@ __global__ void __launch_bounds__(1024) k_getrf_panel_smem(cx<T>* A, int n, long
 // ---------------------------------------------------------------------------
 // Panel factorisation on a cluster of PC_CS CTAs per matrix: the m x w panel
 // (m = n - j0 rows, w <= 64 columns) is held in the CTAs' shared memory, rows
-// in blocks of rpc = ceil(m / PC_CS). Per column the pivot is the
-// cluster-wide maximum of |re| + |im| over the rows at or below the diagonal
-// (the lowest row on ties, as izamax), the pivot row and the displaced row are
-// exchanged through distributed shared memory, and every CTA scales and
-// updates its own rows: two cluster barriers per column instead of a
-// single-SM walk through global memory. Same factors, pivots and info as
-// k_getrf_panel_smem.
+// in blocks of rpc = ceil(m / PC_CS) per CTA. One cluster barrier per column:
+// before it, every CTA pushes into every CTA's shared memory its candidate
+// (the largest |re| + |im| of the column over its rows at or below the
+// diagonal, lowest row on ties, as izamax) together with that whole candidate
+// row, and the owner of the diagonal row pushes the diagonal row; after it,
+// every CTA picks the pivot from the eight candidates locally, so the pivot
+// row and the displaced row are already on chip, the two owners write the
+// interchange into their rows and every CTA scales and updates its own rows.
+// The push buffers alternate between two copies by column parity: a CTA
+// pushing column c + 1 writes the other copy than the one a slower CTA may
+// still read for column c, and cannot reach column c + 2 before that CTA has
+// passed the barrier of column c + 1. Same factors, pivots and info as
+// k_getrf_panel_smem. (Measured on 2048 x 64 panels: 228 us with 256 threads
+// per CTA; 1024 threads sharing each row's columns took 274 us, the per-thread
+// pivot bookkeeping then outweighing the split update.)
 // ---------------------------------------------------------------------------
 constexpr int PC_CS = 8, PC_THREADS = 256;
+// largest rows per CTA: 64 complex64 columns within 216 KiB of dynamic shared
+// memory (the push buffers take another ~10 KiB of static shared memory)
+constexpr int PC_MAX_RPC = 432;
 
 template <class T>
 __global__ void __cluster_dims__(PC_CS, 1, 1) __launch_bounds__(PC_THREADS)
@@ -418,12 +468,13 @@ __global__ void __cluster_dims__(PC_CS, 1, 1) __launch_bounds__(PC_THREADS)
   cg::cluster_group cl = cg::this_cluster();
   extern __shared__ unsigned char smraw[];
   cx<T>* P = reinterpret_cast<cx<T>*>(smraw);  // column c of the own rows at P + c * rpc
-  __shared__ T cand_v;
-  __shared__ int cand_i;
-  __shared__ cx<T> prow[64], orow[64];
+  __shared__ cx<T> crow[2][PC_CS][64];  // candidate rows pushed by every CTA
+  __shared__ cx<T> drow[2][64];         // the diagonal row, pushed by its owner
+  __shared__ T cv[2][PC_CS];
+  __shared__ int ci[2][PC_CS];
   __shared__ T wv[PC_THREADS / 32];
   __shared__ int wi[PC_THREADS / 32];
-  __shared__ int s_p;
+  __shared__ int s_bi;
   const int rank = (int)cl.block_rank();
   const int mat = blockIdx.x / PC_CS;
   cx<T>* a = A + (long long)mat * stride;
@@ -432,12 +483,11 @@ __global__ void __cluster_dims__(PC_CS, 1, 1) __launch_bounds__(PC_THREADS)
   const int r0 = rank * rpc;
   const int rows = max(0, min(rpc, m - r0));
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  for (int e = tid; e < rows * w; e += PC_THREADS) {
-    const int i = e % rows, c = e / rows;
-    P[c * rpc + i] = a[(long long)(j0 + r0 + i) + (long long)(j0 + c) * n];
-  }
+  load_block<T>(P, rpc, a + (j0 + r0) + (long long)j0 * n, n, rows, w, tid, PC_THREADS);
   __syncthreads();
+  cl.sync();  // every CTA of the cluster runs before the first remote store
   for (int c = 0; c < w; ++c) {
+    const int buf = c & 1;
     T best = T(-1);
     int bi = 0x7fffffff;
     for (int i = tid; i < rows; i += PC_THREADS) {
@@ -450,41 +500,55 @@ __global__ void __cluster_dims__(PC_CS, 1, 1) __launch_bounds__(PC_THREADS)
       wi[wid] = bi;
     }
     __syncthreads();
-    if (tid == 0) {
-      for (int q = 1; q < PC_THREADS / 32; ++q) argmax_merge(best, bi, wv[q], wi[q]);
-      cand_v = best;
-      cand_i = bi;
-    }
-    cl.sync();  // every CTA's candidate is visible
-    if (tid == 0) {
-      T bv = T(-1);
-      int bidx = 0x7fffffff;
-      for (int q = 0; q < PC_CS; ++q)
-        argmax_merge(bv, bidx, *cl.map_shared_rank(&cand_v, q), *cl.map_shared_rank(&cand_i, q));
-      if (bidx >= m) bidx = c;
-      s_p = bidx;
-      if (rank == 0) {
-        piv[j0 + c] = j0 + bidx;
-        if (!(bv > T(0)) && info[mat] == 0) info[mat] = j0 + c + 1;
+    if (wid == 0) {
+      best = lane < PC_THREADS / 32 ? wv[lane] : T(-1);
+      bi = lane < PC_THREADS / 32 ? wi[lane] : 0x7fffffff;
+      warp_argmax(best, bi);  // the result is in lane 0
+      best = __shfl_sync(0xffffffffu, best, 0);
+      bi = __shfl_sync(0xffffffffu, bi, 0);
+      if (lane == 0) s_bi = bi;
+      if (lane < PC_CS) {  // the candidate to CTA `lane`
+        *cl.map_shared_rank(&cv[buf][rank], lane) = best;
+        *cl.map_shared_rank(&ci[buf][rank], lane) = bi;
       }
     }
     __syncthreads();
-    const int p = s_p;
-    const int oc = c / rpc, op = p / rpc;
     {
-      const cx<T>* Pp = cl.map_shared_rank(P, op);
-      const cx<T>* Pc = cl.map_shared_rank(P, oc);
-      for (int q = tid; q < w; q += PC_THREADS) {
-        prow[q] = Pp[q * rpc + (p - op * rpc)];
-        if (rank == op && p != c) orow[q] = Pc[q * rpc + (c - oc * rpc)];
+      const int mine = s_bi;  // the candidate row (global panel row), or none
+      const int oc = c / rpc;
+      for (int e = tid; e < PC_CS * w; e += PC_THREADS) {
+        const int q = e / w, col = e % w;  // destination CTA, column
+        if (mine < m) *cl.map_shared_rank(&crow[buf][rank][col], q) = P[col * rpc + (mine - r0)];
+        if (rank == oc) *cl.map_shared_rank(&drow[buf][col], q) = P[col * rpc + (c - r0)];
       }
     }
-    cl.sync();  // every remote read of this column is done before the exchange writes
+    cl.sync();  // candidates, candidate rows and the diagonal row of column c everywhere
+    T bv = T(-1);
+    int p = 0x7fffffff, ps = 0;
+#pragma unroll
+    for (int q = 0; q < PC_CS; ++q) {
+      const T v = cv[buf][q];
+      const int ix = ci[buf][q];
+      if (v > bv || (v == bv && ix < p)) {
+        bv = v;
+        p = ix;
+        ps = q;
+      }
+    }
+    if (p >= m) {  // no row at or below the diagonal compared (NaN column): no interchange
+      p = c;
+      ps = -1;
+    }
+    if (rank == 0 && tid == 0) {
+      piv[j0 + c] = j0 + p;
+      if (!(bv > T(0)) && info[mat] == 0) info[mat] = j0 + c + 1;
+    }
+    const cx<T>* prow = ps >= 0 ? crow[buf][ps] : drow[buf];  // the new row c
     if (p != c) {
-      if (rank == oc)
+      if (c >= r0 && c < r0 + rows)
         for (int q = tid; q < w; q += PC_THREADS) P[q * rpc + (c - r0)] = prow[q];
-      if (rank == op)
-        for (int q = tid; q < w; q += PC_THREADS) P[q * rpc + (p - r0)] = orow[q];
+      if (p >= r0 && p < r0 + rows)
+        for (int q = tid; q < w; q += PC_THREADS) P[q * rpc + (p - r0)] = drow[buf][q];
     }
     __syncthreads();
     const cx<T> pv = prow[c];
@@ -497,19 +561,28 @@ __global__ void __cluster_dims__(PC_CS, 1, 1) __launch_bounds__(PC_THREADS)
         l = l * inv;
         P[c * rpc + i] = l;
       }
-      for (int q = c + 1; q < w; ++q) cfms(P[q * rpc + i], l, prow[q]);
+      // 8 columns at a time through registers: the shared-memory loads of a
+      // group are independent of the group's stores
+      for (int q0 = c + 1; q0 < w; q0 += 8) {
+        cx<T> u[8], v[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+          if (q0 + t < w) {
+            u[t] = prow[q0 + t];
+            v[t] = P[(q0 + t) * rpc + i];
+          }
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+          if (q0 + t < w) {
+            cfms(v[t], l, u[t]);
+            P[(q0 + t) * rpc + i] = v[t];
+          }
+      }
     }
     __syncthreads();
   }
-  cl.sync();  // no CTA leaves while another might still read its shared memory
-  for (int e = tid; e < rows * w; e += PC_THREADS) {
-    const int i = e % rows, c = e / rows;
-    a[(long long)(j0 + r0 + i) + (long long)(j0 + c) * n] = P[c * rpc + i];
-  }
+  store_block<T>(a + (j0 + r0) + (long long)j0 * n, n, P, rpc, rows, w, tid, PC_THREADS);
 }
-
-// largest rows per CTA of the cluster panel (64 complex64 columns within 224 KiB)
-constexpr int PC_MAX_RPC = (224 * 1024) / (64 * 8);
 
 // row interchanges of one panel on the columns outside the panel
 template <class T>
@@ -770,6 +843,28 @@ static int build_solve_blocks(const LUBatch<T>& f, cudaStream_t st) {
   return s;
 }
 
+// process-wide plan of lu_factor: panels per outer block (1..16) and the
+// panel form (-1 automatic, 0 one CTA per panel, 1 a cluster of CTAs); the
+// environment variables QBG_LU_OUTER and QBG_LU_CLUSTER give the initial values
+static std::atomic<int> g_lu_outer{[] {
+  const char* e = std::getenv("QBG_LU_OUTER");
+  const int v = (e && *e) ? std::atoi(e) : 4;
+  return std::max(1, std::min(v, 16));
+}()};
+static std::atomic<int> g_lu_cluster{[] {
+  const char* e = std::getenv("QBG_LU_CLUSTER");
+  return (e && *e) ? (*e == '0' ? 0 : 1) : -1;
+}()};
+
+void set_lu_plan(int outer, int cluster) {
+  if (outer > 0) g_lu_outer.store(std::max(1, std::min(outer, 16)));
+  g_lu_cluster.store(cluster < 0 ? -1 : (cluster ? 1 : 0));
+}
+void get_lu_plan(int* outer, int* cluster) {
+  if (outer) *outer = g_lu_outer.load();
+  if (cluster) *cluster = g_lu_cluster.load();
+}
+
 template <class T>
 static int lu_factor_one(LUBatch<T>& f, cudaStream_t st, cudaEvent_t after_first_panel = nullptr) {
   const int n = f.n, nb = f.nb, batch = f.batch;
@@ -791,12 +886,15 @@ static int lu_factor_one(LUBatch<T>& f, cudaStream_t st, cudaEvent_t after_first
                                   (int)kPanelSmem));
     panel_attr[sizeof(T) == 8] = true;
   }
-  // complex64 panels of up to 64 columns and n <= PC_CS * PC_MAX_RPC rows go to a
-  // cluster of CTAs (QBG_LU_CLUSTER=0 in the environment keeps one CTA per panel)
-  static const bool cluster_on = [] {
-    const char* e = std::getenv("QBG_LU_CLUSTER");
-    return !(e && *e == '0');
-  }();
+  // complex64 panels of up to 64 columns and n <= PC_CS * PC_MAX_RPC rows of a
+  // small batch (at most 4 matrices, where one CTA per panel leaves most SMs
+  // idle) go to a cluster of CTAs. For larger batches the one-CTA panels of
+  // several matrices already run side by side with other matrices' updates,
+  // and the cluster form measured slower (48 operators of 2048 in four
+  // stream parts: factor phase 38.5 ms with clusters against 34.0 ms without).
+  // set_lu_plan (or QBG_LU_CLUSTER=0 / =1 in the environment) forces either form.
+  const int cluster_set = g_lu_cluster.load();
+  const bool cluster_on = cluster_set < 0 ? batch <= 4 : cluster_set == 1;
   const bool use_cluster = cluster_on && sizeof(T) == sizeof(float) && nb <= 64 && n <= PC_CS * PC_MAX_RPC;
   static bool cluster_attr[2] = {false, false};
   if (use_cluster && !cluster_attr[sizeof(T) == 8]) {
@@ -812,12 +910,8 @@ static int lu_factor_one(LUBatch<T>& f, cudaStream_t st, cudaEvent_t after_first
   // forward substitution (the nb x nb inverses of L from k_trtri). The row
   // interchanges of every panel still apply to all columns at once (k_laswp),
   // so the factors are those of the one-level algorithm.
-  // panels per outer block: QBG_LU_OUTER in the environment (1..16, default 4)
-  static const int LU_OUTER = [] {
-    const char* e = std::getenv("QBG_LU_OUTER");
-    const int v = (e && *e) ? std::atoi(e) : 4;
-    return std::max(1, std::min(v, 16));
-  }();
+  // panels per outer block: set_lu_plan (or QBG_LU_OUTER in the environment), 1..16, default 4
+  const int LU_OUTER = g_lu_outer.load();
   const cx<T> one(1, 0), mone(-1, 0), zero(0, 0);
   auto linv = [&](int j) { return f.Linv + (long long)(j / nb) * nb * nb; };
   const long long sLinv = (long long)f.nblk * nb * nb;
@@ -1420,6 +1514,7 @@ template size_t lu_solve_blocks_bytes<float>(LUBatch<float>&, int, int);
 template void lu_solve_blocks_bind<double>(LUBatch<double>&, void*);
 template void lu_solve_blocks_bind<float>(LUBatch<float>&, void*);
 template int lu_factor<float>(LUBatch<float>&, cudaStream_t);
+template int lu_inverse<float>(const LUBatch<float>&, cxf*, cudaStream_t);
 template int lu_solve_shared<double>(const LUBatch<double>&, const cxd*, int, cxd*, long long, cudaStream_t);
 template int lu_solve_shared<float>(const LUBatch<float>&, const cxf*, int, cxf*, long long, cudaStream_t);
 template int gemm_batched<double>(int, int, int, cxd, const cxd*, long long, long long, const cxd*, long long,

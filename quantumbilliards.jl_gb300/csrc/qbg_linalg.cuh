@@ -149,5 +149,10 @@ constexpr int GEMM_ENGINE_TCGEN05 = 1;
 constexpr int GEMM_ENGINE_TCGEN05_STAGED = 2;  // tcgen05 with register-staged operands only
 void set_gemm_engine(int e);
 int gemm_engine();
+// Plan of lu_factor, process-wide: panels per outer block (1..16; <= 0 keeps
+// the current value) and the panel form (< 0 automatic: a cluster of CTAs per
+// complex64 panel for batches of at most 4 matrices; 0 one CTA; 1 a cluster).
+void set_lu_plan(int outer, int cluster);
+void get_lu_plan(int* outer, int* cluster);
 
 }  // namespace qbg

@@ -9,7 +9,12 @@ subspace iteration on the inverse (the :svd branch, macros.jl:159-161).
 * the C1 circle matrices (DLP Kress, N = 512 at k = 42) at the first eight k
   of the golden sweep, whose smallest singular values come in exact pairs
   (the rotational symmetry): sigma_min against the oracle's LAPACK values
-  (tests/golden/c1_sweep.json) to 2e-12 relative.
+  (tests/golden/c1_sweep.json) to 2e-12 relative;
+* the complex64 LU of the Beyn mixed form (panels, interchanges, tcgen05
+  trailing updates) through both panel forms (one CTA per panel and the
+  8-CTA cluster) and two outer-block depths, n = 700 and 2050, batch 3:
+  |A X - I| <= 2e-5 for matrices of condition ~3 (numpy's complex64 inverse
+  reaches ~1e-6), and the two panel forms agree to 1e-5.
 """
 import json
 from pathlib import Path
@@ -32,8 +37,16 @@ def _run(lib, L, As):
     Ac = np.ascontiguousarray(np.stack(As).transpose(0, 2, 1))  # column-major per matrix
     X = np.empty_like(Ac)
     sig = np.zeros(batch)
-    L.check(lib.qbg_dense_inverse(n, batch, L.vptr(Ac), L.vptr(X), L.dptr(sig), None))
+    L.check(lib.qbg_dense_inverse(n, batch, 0, L.vptr(Ac), L.vptr(X), L.dptr(sig), None))
     return [x.T for x in X], sig
+
+
+def _inv32(lib, L, As):
+    batch, n = len(As), As[0].shape[0]
+    Ac = np.ascontiguousarray(np.stack(As).transpose(0, 2, 1))
+    X = np.empty_like(Ac)
+    L.check(lib.qbg_dense_inverse(n, batch, 2, L.vptr(Ac), L.vptr(X), None, None))
+    return [x.T for x in X]
 
 
 @pytest.mark.parametrize("n", [100, 257])
@@ -69,3 +82,28 @@ def test_c1_degenerate_pairs(qb):
     As = qb.assemble(ws, ks)
     _, sig = _run(lib, L, As)
     assert np.all(np.abs(sig - so) <= 2e-12 * so), np.abs(sig - so) / so
+
+
+@pytest.mark.parametrize("n", [700, 2050])
+def test_complex64_lu_panel_forms(qb, n):
+    from qbgpu import _lib as L
+    import ctypes as C
+    lib = L.load()
+    rng = np.random.default_rng(n)
+    As = [(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(2 * n) + 3.0 * np.eye(n)
+          for _ in range(3)]
+    o0, c0 = C.c_int32(), C.c_int32()
+    L.check(lib.qbg_get_lu_plan(C.byref(o0), C.byref(c0)))
+    out = {}
+    try:
+        for outer, cluster in ((4, 0), (4, 1), (2, 1)):
+            L.check(lib.qbg_set_lu_plan(outer, cluster))
+            Xs = _inv32(lib, L, As)
+            for A, X in zip(As, Xs):
+                assert np.abs(A @ X - np.eye(n)).max() < 2e-5, (outer, cluster)
+            out[(outer, cluster)] = Xs
+    finally:
+        L.check(lib.qbg_set_lu_plan(o0.value, c0.value))
+    for key in ((4, 1), (2, 1)):
+        for X0, X1 in zip(out[(4, 0)], out[key]):
+            assert np.abs(X1 - X0).max() < 1e-5 * np.abs(X0).max()
