@@ -23,10 +23,19 @@ node per step; the eigenvalues per disk come from one untimed full disk of
 the same code, matched to the oracle fixture of the reference's regrowth
 policy (tests/golden/c2_beyn_fresh.json).
 
---workload ebim prints a second line for the EBIM eigen step on the same
-geometry (k = 200, dk = 0.05, nev = 5): steps/s of device assembly + eigen
-step, the same from host matrices (e2e), and the oracle's dense
-solve_krylov on the same matrices as the CPU baseline.
+other_configs (default run, after the timed region; --no-extras leaves it
+out): bounded samples of the other configurations -- C1 (the sigma_min sweep
+of the unit circle and refine_minima), C3 (32 batched disks of the
+desymmetrised stadium) and the first 60 requests of the C4 served stream with
+N capped at 2048, with p50/p99 latency.
+
+--workload ebim prints a line for the EBIM eigen step on the same geometry
+(k = 200, dk = 0.05, nev = 5): steps/s of device assembly + eigen step, the
+same from host matrices (e2e), and the oracle's dense solve_krylov on the
+same matrices as the CPU baseline. --workload c1 / c3 / serve print one line
+for that configuration (serve: the full C4 stream, 2000 requests at 20 req/s,
+N in [1024, 8192], unless --requests / --rate / --nmin / --nmax / --nk say
+otherwise).
 """
 from __future__ import annotations
 
@@ -259,8 +268,19 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--cpu-steps", type=int, default=4, help="timed node steps of the cpu_baseline leg")
-    ap.add_argument("--workload", default="beyn", choices=["beyn", "ebim"],
-                    help="beyn: the headline Beyn disk (default); ebim: the EBIM eigen step at one k")
+    ap.add_argument("--workload", default="beyn", choices=["beyn", "ebim", "c1", "c3", "serve"],
+                    help="beyn: the headline Beyn disk (default); ebim: the EBIM eigen step at one k; c1: the "
+                         "sigma_min sweep of the unit circle and refine_minima; c3: 32 batched disks of the "
+                         "desymmetrised stadium; serve: the served mixed request stream")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="beyn: leave out the bounded samples of the other configurations (other_configs)")
+    ap.add_argument("--requests", type=int, default=2000, help="serve: requests of the stream")
+    ap.add_argument("--rate", type=float, default=20.0, help="serve: Poisson arrival rate (requests/s)")
+    ap.add_argument("--nmin", type=int, default=1024, help="serve: smallest N")
+    ap.add_argument("--nmax", type=int, default=8192, help="serve: largest N")
+    ap.add_argument("--nk", type=int, default=64, help="serve: wavenumbers of a sweep request")
+    ap.add_argument("--max-sweeps", type=int, default=1, help="serve: sweeps running at once")
+    ap.add_argument("--mix", default="0.6,0.3,0.1", help="serve: fractions of Beyn, EBIM and sweep requests")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -273,6 +293,10 @@ def main():
         if rank != 0:
             return
         return ebim_workload(args)
+    if args.workload in ("c1", "c3", "serve"):
+        if rank != 0:
+            return
+        return other_workload(args)
     if world > 1:
         # one process per GPU: this rank sees only its own device
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("LOCAL_RANK", str(rank)))
@@ -427,12 +451,224 @@ def main():
     }
     if world > 1:
         line["config"]["parallelism"] = f"replicas{world}"
+    if not args.no_extras and rank == 0 and world == 1:
+        ws.close()
+        line["other_configs"] = {
+            "c1": c1_sweep(qb),
+            "c3": c3_disks(qb, repeat=2),
+            "c4_sample": serve_stream(qb, requests=60, rate=20.0, nmin=1024, nmax=2048, nk=16, max_sweeps=1),
+            "note": "bounded samples run after the timed region: C1 and C3 at their full configurations, C4 as the "
+                    "first 60 requests of its seeded stream with N capped at 2048 and 16-k sweeps (FP64 sweeps at "
+                    "N = 8192 take minutes per request on this part); bench.py --workload serve runs the full "
+                    "stream"}
     if not args.no_cpu_baseline and rank == 0 and world == 1:
         c = cpu_disk(args.cpu_steps, 1)
         line["cpu_baseline"] = {"value": c["value"], "unit": "eigenvalues/s", "cores": c["cores"], "kind": "port",
                                 "sample": cpu_sample_text(c), "max_rel_err_vs_oracle": c["max_rel_err_vs_oracle"]}
     if rank == 0:
         print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# the other configurations: C1 (sweep), C3 (batched disks), C4 (served stream)
+# ---------------------------------------------------------------------------
+GOLDEN_C1 = ROOT / "tests" / "golden" / "c1_sweep.json"
+CIRCLE_EIGS = ROOT / "tests" / "golden" / "circle_eigs.json"
+
+
+def c1_sweep(qb):
+    """C1: the unit circle, DLP Kress with N = 512 at k = 42 (pts_scaling_factor
+    of the golden fixture), sigma_min(A(k)) at 200 k in [40, 42], then
+    refine_minima (three discretisation levels, Newton on lambda_min(A^H A)).
+    Errors: sigma_min against the oracle's LAPACK values (c1_sweep.json), the
+    refined roots against the J_m zeros (circle_eigs.json)."""
+    g = json.loads(GOLDEN_C1.read_text())
+    ks, so = np.array(g["ks"]), np.array(g["sigma"])
+    b = qb.make_circle(1.0)
+    sol = qb.DLP_kress(g["pts_scaling_factor"], b)
+    qb.k_sweep(sol, b, ks[:4])  # warm-up (workspace and kernels)
+    t0 = time.perf_counter()
+    sig = qb.k_sweep(sol, b, ks)
+    t1 = time.perf_counter()
+    kr, tr, _ = qb.refine_minima(sol, b, ks, sig)
+    t2 = time.perf_counter()
+    zeros = np.array([r["k"] for r in json.loads(CIRCLE_EIGS.read_text())["ranges"]["40_42"]])
+    root_err = [float(np.min(np.abs(zeros - k))) for k in kr]
+    return {"workload": "c1_dlp_kress_circle_N512_200k_40_42", "sweep_s": t1 - t0, "refine_s": t2 - t1,
+            "k_per_s": len(ks) / (t1 - t0), "minima": len(kr),
+            "sigma_max_rel_err_vs_oracle": float(np.max(np.abs(sig - so) / so)),
+            "root_max_abs_err_vs_jm_zeros": max(root_err) if root_err else None}
+
+
+def c3_disks(qb, repeat=2, n=4096, ndisk=32, nq=48, L=96):
+    """C3: DLP Kress on the full stadium (radius 1, straight length 2)
+    desymmetrised by XYReflection(-1, -1): N = 4096 full nodes (m = 1024), 32
+    disks of radius 0.5 centred at 300.5 ... 331.5, 48 nodes each, L = 96
+    seeded probes, Chebyshev panels at tol 1e-12 (the library's cost-aware
+    tuner), mixed form; all 1536 operators assembled in one launch and
+    factored as one batch. The first batch allocates (cold), the later ones
+    reuse the library's cached blocks (warm). Eigenvalues: inside each disk
+    with |Im| < 1e-3."""
+    b = qb.make_full_stadium(1.0, 1.0)
+    sol = qb.DLP_kress_global_corners(1.0, b, symmetry=qb.XYReflection(-1, -1))
+    k0s = 300.5 + np.arange(ndisk)
+    pts, sol = qb.points_with_n(sol, b, n, float(k0s[-1] + 0.5))
+    ws = qb.Workspace(sol, pts)
+    t0 = time.perf_counter()
+    zref = k0s[-1] + 0.5 * np.exp(2j * math.pi * np.arange(nq) / nq)
+    cheb = qb.chebyshev_params_min_cost(sol, pts, zref, ws=ws, tol=1e-12, entries=float(ws.dim) ** 2 * ndisk * nq,
+                                        terms_per_entry=4.0, tables_per_call=ndisk * nq)[:4]
+    plan_s = time.perf_counter() - t0
+    times, info, lams = [], None, None
+    for _ in range(max(1, repeat)):
+        ts = time.perf_counter()
+        lams, info = qb.solve_disks(sol, pts, k0s, 0.5, nq=nq, r=L, svd_tol=1e-10, rng=np.random.default_rng(3),
+                                    mixed=True, ws=ws, return_info=True, cheb=cheb)
+        times.append(time.perf_counter() - ts)
+    m = int(ws.dim)
+    ws.close()
+    n_in = sum(int(np.count_nonzero((np.abs(l - k) < 0.5) & (np.abs(l.imag) < 1e-3))) for l, k in zip(lams, k0s))
+    st = info["stats"]
+    warm = min(times[1:]) if len(times) > 1 else times[0]
+    return {"workload": "c3_dlp_kress_quarter_stadium_N4096_32disks_nq48_L96", "m": m, "operators": ndisk * nq,
+            "plan_s": plan_s, "batch_s_cold": times[0], "batch_s_warm": warm, "eigenvalues": n_in,
+            "eigenvalues_per_s_warm": n_in / warm, "ms_assemble": st[0]["ms_assemble"],
+            "ms_factor": st[0]["ms_factor"], "ms_solve": [s["ms_solve"] for s in st],
+            "host_ms": {k: float("%.3g" % v) for k, v in info.get("host_ms", {}).items()}}
+
+
+def make_stream(qb, requests, rate, nmin, nmax, kmin, kmax, L, nk, seed, mix):
+    """The seeded request stream of C4: Poisson arrivals; geometry uniform over
+    {unit circle with an off-centre hole of radius 0.2 (CFIE Kress), full
+    stadium (DLP, smooth composite), half-ellipse-cap mushroom (DLP,
+    corner-graded, kressq = 4), star r = 1 + 0.2 cos 5 theta (CFIE Kress)}; N
+    log-uniform in [nmin, nmax] (rounded by the node-count rule); k uniform in
+    [kmin, kmax]; request kinds by `mix` (Beyn disk of radius 0.5 with 32..64
+    contour nodes and L probes; EBIM at one k; sigma_min sweep of nk
+    wavenumbers). Discretisations are built and uploaded before the clock."""
+    rng = np.random.default_rng(seed)
+    geoms = [("hole", qb.make_circle_with_hole(1.0, (0.3, 0.1, 0.2)), qb.CFIE_kress),
+             ("stadium", qb.make_full_stadium(1.0, 1.0), qb.DLP_kress_global_corners),
+             ("mushroom", qb.make_full_ellipse_mushroom(), qb.DLP_kress_global_corners),
+             ("star", qb.make_star(0.2, 5), qb.CFIE_kress)]
+    reqs = []
+    t = 0.0
+    for _ in range(requests):
+        t += rng.exponential(1.0 / rate)
+        gname, bil, cls = geoms[int(rng.integers(0, len(geoms)))]
+        n = int(round(math.exp(rng.uniform(math.log(nmin), math.log(nmax)))))
+        k = float(rng.uniform(kmin, kmax))
+        u = rng.uniform()
+        kind = "beyn" if u < mix[0] else ("ebim" if u < mix[0] + mix[1] else "sweep")
+        sol = cls(1.0, bil)
+        pts, sol = qb.points_with_n(sol, bil, n, k)
+        ws = qb.Workspace(sol, pts)
+        r = dict(t=t, kind=kind, geom=gname, n=ws.dim, k=k, ws=ws)
+        if kind == "beyn":
+            r["nq"] = int(rng.integers(32, 65))
+            r["V"] = qb.probe_matrix(ws.dim, L, rng)
+        elif kind == "sweep":
+            r["ks"] = k + 0.01 * np.arange(nk)
+        reqs.append(r)
+    return reqs
+
+
+def serve_stream(qb, requests=2000, rate=20.0, nmin=1024, nmax=8192, kmin=50.0, kmax=800.0, L=32, nk=64,
+                 budget_gb=150.0, workers=4, max_batch=8, max_sweeps=1, seed=4, mix=(0.6, 0.3, 0.1)):
+    """C4 through the request server (qbgpu.Server: device-resident state,
+    HBM-budget admission, Beyn requests on the same geometry merged into one
+    batch, priority streams): requests are submitted at their arrival times
+    and latency = arrival -> result on the host (submission, queue, device
+    work, copies back and the host part of a Beyn request). Reports p50/p99
+    overall and per kind, with the queue / run / host split."""
+    import threading
+    from concurrent.futures import ThreadPoolExecutor
+    reqs = make_stream(qb, requests, rate, nmin, nmax, kmin, kmax, L, nk, seed, mix)
+    lat, info = {}, {}
+    lock = threading.Lock()
+    with qb.Server(hbm_budget=int(budget_gb * 2 ** 30), workers=workers, max_batch=max_batch,
+                   max_sweeps=max_sweeps) as srv, ThreadPoolExecutor(max_workers=64) as pool:
+        t0 = time.perf_counter()
+
+        def finish(i, h, t_arr):
+            res = srv.wait(h)
+            done = time.perf_counter()
+            nl = 0
+            if reqs[i]["kind"] == "beyn":
+                lam = res["lam"]
+                nl = int(np.count_nonzero((np.abs(lam - reqs[i]["k"]) < 0.5) & (np.abs(lam.imag) < 1e-3)))
+            with lock:
+                lat[i] = (done - t_arr) * 1e3
+                info[i] = dict(batched=res["batched"], queue_ms=res["queue_ms"], run_ms=res["run_ms"], eig=nl,
+                               lag_ms=(h.t_submit - t_arr) * 1e3, wait_ms=(done - h.t_submit) * 1e3)
+
+        futs = []
+        for i, r in enumerate(reqs):
+            now = time.perf_counter() - t0
+            if r["t"] > now:
+                time.sleep(r["t"] - now)
+            t_arr = t0 + r["t"]
+            if r["kind"] == "beyn":
+                h = srv.submit_beyn(r["ws"], r["k"], 0.5, r["nq"], r["V"], mixed=True)
+            elif r["kind"] == "ebim":
+                h = srv.submit_ebim(r["ws"], r["k"])
+            else:
+                h = srv.submit_sweep(r["ws"], r["ks"])
+            futs.append(pool.submit(finish, i, h, t_arr))
+        for f in futs:
+            f.result()
+        wall = time.perf_counter() - t0
+    for r in reqs:
+        r["ws"].close()
+    Lm = np.array([lat[i] for i in range(len(reqs))])
+    per = {}
+    for kind in ("beyn", "ebim", "sweep"):
+        idx = [i for i in range(len(reqs)) if reqs[i]["kind"] == kind]
+        if not idx:
+            continue
+        v = np.array([lat[i] for i in idx])
+        qv = np.array([info[i]["queue_ms"] for i in idx])
+        rv = np.array([info[i]["run_ms"] for i in idx])
+        hv = np.array([info[i]["wait_ms"] - info[i]["queue_ms"] - info[i]["run_ms"] for i in idx])
+        per[kind] = dict(count=len(idx), p50_ms=float(np.percentile(v, 50)), p99_ms=float(np.percentile(v, 99)),
+                         queue_p50_ms=float(np.percentile(qv, 50)), run_p50_ms=float(np.percentile(rv, 50)),
+                         host_p50_ms=float(np.percentile(hv, 50)),
+                         n_range=[int(min(reqs[i]["n"] for i in idx)), int(max(reqs[i]["n"] for i in idx))])
+    eig = sum(info[i]["eig"] for i in info)
+    return {"workload": "c4_served_stream", "requests": len(reqs), "rate_per_s": rate, "wall_s": wall,
+            "p50_ms": float(np.percentile(Lm, 50)), "p99_ms": float(np.percentile(Lm, 99)),
+            "throughput_req_per_s": len(reqs) / wall, "eigenvalues": eig, "eigenvalues_per_s": eig / wall,
+            "per_kind": per, "beyn_batched_max": max([info[i]["batched"] for i in info] + [1]),
+            "config": dict(nmin=nmin, nmax=nmax, kmin=kmin, kmax=kmax, L=L, nk=nk, budget_gb=budget_gb,
+                           workers=workers, max_batch=max_batch, max_sweeps=max_sweeps, seed=seed, mix=list(mix))}
+
+
+def other_workload(args):
+    """--workload c1 | c3 | serve: one configuration in its own JSON line."""
+    import build_qbgpu as B
+    B.build()
+    import qbgpu as qb
+    clk = ClockSampler()
+    clk.start()
+    launches0 = qb.launch_count()
+    if args.workload == "c1":
+        r = c1_sweep(qb)
+        metric, value, unit = "sigma_min evaluations/s, C1 sweep (DLP Kress circle, N = 512, 200 k)", r["k_per_s"], "k/s"
+        ms = r["sweep_s"] * 1e3
+    elif args.workload == "c3":
+        r = c3_disks(qb, repeat=max(2, args.steps))
+        metric, value, unit = "eigenvalues/s, C3 batched disks (warm batch)", r["eigenvalues_per_s_warm"], "eigenvalues/s"
+        ms = r["batch_s_warm"] * 1e3
+    else:
+        r = serve_stream(qb, requests=args.requests, rate=args.rate, nmin=args.nmin, nmax=args.nmax, nk=args.nk,
+                         max_sweeps=args.max_sweeps, mix=tuple(float(x) for x in args.mix.split(",")))
+        metric, value, unit = "served requests/s (p50/p99 latency beside), C4 stream", r["throughput_req_per_s"], "req/s"
+        ms = r["wall_s"] * 1e3
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64+c128",
+            "data": "synthetic", "config": {"workload": r["workload"]}, "result": r,
+            "gpu_launches": qb.launch_count() - launches0, "clocks": clk.stop()}
+    print(json.dumps(line))
 
 
 EBIM_K, EBIM_DK, EBIM_NEV = 200.0, 0.05, 5
