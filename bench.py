@@ -6,7 +6,10 @@ nq = 48 trapezoid contour nodes, L = 64 seeded complex Gaussian probes (std 1),
 svd_tol = 1e-12, the reference's single r -> 2r regrowth when the rank
 saturates. Chebyshev panels are tuned once per run to 1e-13 absolute error
 (the tolerance compute_spectrum_beyn gives chebyshev_params), by the library's
-cost-aware tuner; the tuning time is reported as plan_s. A step = one full Beyn disk: assembly
+cost-aware tuner; the tuning time is reported as plan_s. The LU plan of the
+mixed step (panel width, outer-block depth, stream parts) is then chosen by
+timing whole steps of this workload (qbgpu.autotune.tune_beyn; lu_plan lists
+the plans tried). A step = one full Beyn disk: assembly
 of the 48 T(z_j), batched LU, T^-1 V solves (+ regrowth solves), moments,
 host SVD/eig.
 
@@ -166,12 +169,12 @@ def accuracy(lam, oracle_all):
     return sel, e, missing
 
 
-def run_step(qb, sol, pts, ws, mixed, rng_seed=SEED, with_geometry=False, cheb=None):
+def run_step(qb, sol, pts, ws, mixed, rng_seed=SEED, with_geometry=False, cheb=None, nb=0):
     t0 = time.perf_counter()
     if with_geometry:
         ws = qb.Workspace(sol, pts)
     lam, info = qb.solve(sol, pts, K0 + 0j, RADIUS, nq=NQ, r=L_PROBES, svd_tol=SVD_TOL,
-                         rng=np.random.default_rng(rng_seed), mixed=mixed, ws=ws, return_info=True, cheb=cheb)
+                         rng=np.random.default_rng(rng_seed), mixed=mixed, ws=ws, return_info=True, cheb=cheb, nb=nb)
     dt = time.perf_counter() - t0
     if with_geometry:
         ws.close()
@@ -319,6 +322,10 @@ def main():
     t0 = time.perf_counter()
     cheb = tuple(int(x) for x in qb.chebyshev_params_min_cost(sol, pts, zref, ws=ws, tol=CHEB_TOL)[:4])
     plan_s = time.perf_counter() - t0
+    # LU plan of the mixed step (panel width, outer-block depth, stream parts) chosen by timing this workload
+    tuned = qb.autotune.tune_beyn(sol, pts, ws, K0 + 0j, RADIUS, NQ, L_PROBES, mixed=True, cheb=cheb,
+                                  svd_tol=SVD_TOL, seed=SEED)
+    nb = tuned["nb"]
 
     # plain FP64 form (the drop-in), timed beside the mixed one
     lam64, info64, _ = run_step(qb, sol, pts, ws, mixed=False, cheb=cheb)
@@ -331,7 +338,7 @@ def main():
     plain_ok = int(np.count_nonzero(e64 <= TOL_EIG))
 
     for _ in range(args.warmup):
-        run_step(qb, sol, pts, ws, mixed=True, cheb=cheb)
+        run_step(qb, sol, pts, ws, mixed=True, cheb=cheb, nb=nb)
     _lib.load().qbg_device_sync()
     replica_barrier(world)
     clk = ClockSampler()
@@ -340,7 +347,7 @@ def main():
     launches0 = qb.launch_count()
     t_region0 = time.perf_counter()
     for s in range(args.steps):
-        lam, info, dt = run_step(qb, sol, pts, ws, mixed=True, cheb=cheb)
+        lam, info, dt = run_step(qb, sol, pts, ws, mixed=True, cheb=cheb, nb=nb)
         sel, e, miss = accuracy(lam, oracle_all)
         counts.append(int(np.count_nonzero(e <= TOL_EIG)))
         errs.append(e)
@@ -357,7 +364,7 @@ def main():
     # end to end through the public API including the geometry upload
     e2e_times, e2e_counts = [], []
     for _ in range(max(1, min(args.steps, 3))):
-        lam_e, _, dt = run_step(qb, sol, pts, None, mixed=True, with_geometry=True, cheb=cheb)
+        lam_e, _, dt = run_step(qb, sol, pts, None, mixed=True, with_geometry=True, cheb=cheb, nb=nb)
         e2e_times.append(dt)
         e2e_counts.append(int(np.count_nonzero(accuracy(lam_e, oracle_all)[1] <= TOL_EIG)))
     # FP32 form (FP32 kernel values): reported beside, with its own accuracy
@@ -409,6 +416,8 @@ def main():
                        timing="wall clock of the synchronous API calls between device synchronizations (the step "
                               "ends with the host SVD and eigvals); device phases in phases_ms are CUDA events"),
         "plan_s": plan_s,
+        "lu_plan": {"nb": nb, "outer": tuned["outer"], "parts": tuned["parts"], "tune_s": tuned["tune_s"],
+                    "tried": [[t["nb"], t["outer"], t["parts"], round(t["ms"], 1)] for t in tuned["table"]]},
         "eigenvalues_per_step": n_eig,
         "oracle_eigenvalues_in_disk": int(len(oracle_sel)),
         "oracle_eigenvalues_missed": int(max(missing)),
@@ -531,7 +540,9 @@ def c3_disks(qb, repeat=2, n=4096, ndisk=32, nq=48, L=96):
     st = info["stats"]
     warm = min(times[1:]) if len(times) > 1 else times[0]
     return {"workload": "c3_dlp_kress_quarter_stadium_N4096_32disks_nq48_L96", "m": m, "operators": ndisk * nq,
-            "plan_s": plan_s, "batch_s_cold": times[0], "batch_s_warm": warm, "eigenvalues": n_in,
+            "plan_s": plan_s,
+        "lu_plan": {"nb": nb, "outer": tuned["outer"], "parts": tuned["parts"], "tune_s": tuned["tune_s"],
+                    "tried": [[t["nb"], t["outer"], t["parts"], round(t["ms"], 1)] for t in tuned["table"]]}, "batch_s_cold": times[0], "batch_s_warm": warm, "eigenvalues": n_in,
             "eigenvalues_per_s_warm": n_in / warm, "ms_assemble": st[0]["ms_assemble"],
             "ms_factor": st[0]["ms_factor"], "ms_solve": [s["ms_solve"] for s in st],
             "host_ms": {k: float("%.3g" % v) for k, v in info.get("host_ms", {}).items()}}

@@ -276,12 +276,15 @@ qbg_status qbg_dense_inverse(int32_t n, int32_t batch, int32_t prec, const doubl
                              double* work_out);
 /* Plan of the batched LU, process-wide (no counterpart in the reference):
  * panels per outer block of the two-level factorisation (1..16, default 4;
- * <= 0 keeps the current value) and the complex64 panel form (-1 automatic:
+ * <= 0 keeps the current value), the complex64 panel form (-1 automatic:
  * a cluster of 8 CTAs per panel for batches of at most 4 matrices; 0 one CTA
- * per panel; 1 a cluster). QBG_LU_OUTER and QBG_LU_CLUSTER in the environment
- * give the initial values. */
-qbg_status qbg_set_lu_plan(int32_t outer, int32_t cluster);
-qbg_status qbg_get_lu_plan(int32_t* outer, int32_t* cluster);
+ * per panel; 1 a cluster) and the number of stream parts a Beyn handle
+ * created afterwards factors and solves its operator batch in (1..8,
+ * default 4; <= 0 keeps the current value). QBG_LU_OUTER, QBG_LU_CLUSTER and
+ * QBG_LU_SPLIT in the environment give the initial values; qbgpu.autotune
+ * chooses them by timing. */
+qbg_status qbg_set_lu_plan(int32_t outer, int32_t cluster, int32_t parts);
+qbg_status qbg_get_lu_plan(int32_t* outer, int32_t* cluster, int32_t* parts);
 qbg_status qbg_clear_tc_error(void);
 
 /* Smallest singular value of A(k) for nk real wavenumbers (the :svd branch of

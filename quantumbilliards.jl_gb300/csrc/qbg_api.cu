@@ -749,20 +749,21 @@ qbg_status qbg_dense_inverse(int32_t n, int32_t batch, int32_t prec, const doubl
   return s;
 }
 
-qbg_status qbg_set_lu_plan(int32_t outer, int32_t cluster) {
-  if (outer > 16 || cluster > 1 || cluster < -1) {
-    set_error("qbg_set_lu_plan: outer must be <= 16 and cluster -1, 0 or 1");
+qbg_status qbg_set_lu_plan(int32_t outer, int32_t cluster, int32_t parts) {
+  if (outer > 16 || cluster > 1 || cluster < -1 || parts > LUBatch<float>::MAX_SPLIT) {
+    set_error("qbg_set_lu_plan: outer must be <= 16, cluster -1, 0 or 1 and parts <= %d", LUBatch<float>::MAX_SPLIT);
     return QBG_EINVAL;
   }
-  set_lu_plan(outer, cluster);
+  set_lu_plan(outer, cluster, parts);
   return QBG_OK;
 }
 
-qbg_status qbg_get_lu_plan(int32_t* outer, int32_t* cluster) {
-  int o = 0, c = 0;
-  get_lu_plan(&o, &c);
+qbg_status qbg_get_lu_plan(int32_t* outer, int32_t* cluster, int32_t* parts) {
+  int o = 0, c = 0, q = 0;
+  get_lu_plan(&o, &c, &q);
   if (outer) *outer = o;
   if (cluster) *cluster = c;
+  if (parts) *parts = q;
   return QBG_OK;
 }
 

@@ -459,8 +459,8 @@ qbg_status create_impl(qbg_geom* g, const double* k0s, const double* Rs, int ndi
     cudaError_t e = stream_create(&b->st);
     if (e != cudaSuccess) s = cuda_status(e, "cudaStreamCreate");
   }
-  const char* split_env = std::getenv("QBG_LU_SPLIT");
-  int parts = (split_env && *split_env) ? std::atoi(split_env) : LUBatch<float>::MAX_SPLIT;
+  int parts = 1;
+  get_lu_plan(nullptr, nullptr, &parts);  // stream parts of the operator batch (qbg_set_lu_plan)
   parts = std::max(1, std::min(parts, LUBatch<float>::MAX_SPLIT));
   if (!s && parts > 1) {
     cudaError_t e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);

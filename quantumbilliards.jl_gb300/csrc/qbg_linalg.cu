@@ -843,9 +843,11 @@ static int build_solve_blocks(const LUBatch<T>& f, cudaStream_t st) {
   return s;
 }
 
-// process-wide plan of lu_factor: panels per outer block (1..16) and the
-// panel form (-1 automatic, 0 one CTA per panel, 1 a cluster of CTAs); the
-// environment variables QBG_LU_OUTER and QBG_LU_CLUSTER give the initial values
+// process-wide plan of lu_factor: panels per outer block (1..16), the panel
+// form (-1 automatic, 0 one CTA per panel, 1 a cluster of CTAs) and the
+// number of stream parts a Beyn operator batch is factored and solved in;
+// the environment variables QBG_LU_OUTER, QBG_LU_CLUSTER and QBG_LU_SPLIT give
+// the initial values
 static std::atomic<int> g_lu_outer{[] {
   const char* e = std::getenv("QBG_LU_OUTER");
   const int v = (e && *e) ? std::atoi(e) : 4;
@@ -856,13 +858,21 @@ static std::atomic<int> g_lu_cluster{[] {
   return (e && *e) ? (*e == '0' ? 0 : 1) : -1;
 }()};
 
-void set_lu_plan(int outer, int cluster) {
+static std::atomic<int> g_lu_parts{[] {
+  const char* e = std::getenv("QBG_LU_SPLIT");
+  const int v = (e && *e) ? std::atoi(e) : 4;
+  return std::max(1, std::min(v, LUBatch<float>::MAX_SPLIT));
+}()};
+
+void set_lu_plan(int outer, int cluster, int parts) {
   if (outer > 0) g_lu_outer.store(std::max(1, std::min(outer, 16)));
   g_lu_cluster.store(cluster < 0 ? -1 : (cluster ? 1 : 0));
+  if (parts > 0) g_lu_parts.store(std::min(parts, LUBatch<float>::MAX_SPLIT));
 }
-void get_lu_plan(int* outer, int* cluster) {
+void get_lu_plan(int* outer, int* cluster, int* parts) {
   if (outer) *outer = g_lu_outer.load();
   if (cluster) *cluster = g_lu_cluster.load();
+  if (parts) *parts = g_lu_parts.load();
 }
 
 template <class T>

@@ -32,7 +32,7 @@ struct LUBatch {
   // and lu_solve_shared run nsplit contiguous parts of the batch concurrently,
   // the first on the calling stream and part i on stx[i - 1], forked from and
   // joined back into the calling stream with these two events
-  static constexpr int MAX_SPLIT = 4;
+  static constexpr int MAX_SPLIT = 8;
   int nsplit = 1;
   cudaStream_t stx[MAX_SPLIT - 1] = {};
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -150,9 +150,10 @@ constexpr int GEMM_ENGINE_TCGEN05_STAGED = 2;  // tcgen05 with register-staged o
 void set_gemm_engine(int e);
 int gemm_engine();
 // Plan of lu_factor, process-wide: panels per outer block (1..16; <= 0 keeps
-// the current value) and the panel form (< 0 automatic: a cluster of CTAs per
-// complex64 panel for batches of at most 4 matrices; 0 one CTA; 1 a cluster).
-void set_lu_plan(int outer, int cluster);
-void get_lu_plan(int* outer, int* cluster);
+// the current value), the panel form (< 0 automatic: a cluster of CTAs per
+// complex64 panel for batches of at most 4 matrices; 0 one CTA; 1 a cluster)
+// and the stream parts of a Beyn operator batch (1..MAX_SPLIT; <= 0 keeps).
+void set_lu_plan(int outer, int cluster, int parts);
+void get_lu_plan(int* outer, int* cluster, int* parts);
 
 }  // namespace qbg

@@ -25,6 +25,7 @@
 // bounded: on timeout the kernel records an error, waits (bounded) for its own
 // MMAs, frees its TMEM and returns without writing C.
 #include <atomic>
+#include <cstdlib>
 #include <cstdint>
 #include <mutex>
 #include <vector>
@@ -560,11 +561,252 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm_pk(int M, int N, int KT, cx
   }
 }
 
+// ---------------------------------------------------------------------------
+// Wide packed GEMM for large products (the LU's trailing updates): one CTA
+// computes a 128 x 128 complex tile as one real M = 128, N = 256 MMA per k
+// step (B' rows 0..127 = (Re, -Im) of the tile's columns, 128..255 =
+// (Im, Re)), so an A tile read from L2 feeds four times the MMA work of the
+// 128 x 32 tile. Accumulator: 256 TMEM columns (Re C in 0..127, Im C in
+// 128..255). Operands are packed (split into big and small TF32 parts) in
+// tiles of 8 complex k (two MMA k steps), one bulk copy per operand and
+// stage, through a four-stage ring:
+//   PAW tile (b, mt, kt): [big | small] x 2 MMA steps x 128 rows x 8 real k (16 KB)
+//   PBW tile (b, nt, kt): [big | small] x 2 MMA steps x 256 B' rows x 8 real k (32 KB)
+// The epilogue reads the accumulator in 32-column chunks and updates C
+// (beta C read there, not prefetched). Waits bounded as in k_tc_cgemm_pk.
+// ---------------------------------------------------------------------------
+constexpr int PW_BN = 128;                                  // complex columns per CTA (real N = 256)
+constexpr int PW_BK = 8;                                    // complex k per stage (two MMA k steps)
+constexpr int PW_KSTEPS = 2;
+constexpr int PW_NST = 4;
+constexpr int PW_A_TILE = 2 * PW_KSTEPS * TC_A_STEP;        // 4096 floats
+constexpr int PW_B_STEP = 2 * PW_BN * 8;                    // floats per B' block per MMA step (8 KB)
+constexpr int PW_B_TILE = 2 * PW_KSTEPS * PW_B_STEP;        // 8192 floats
+constexpr int PW_STAGE = PW_A_TILE + PW_B_TILE;             // 12288 floats (48 KB)
+constexpr uint32_t PW_TMEM_COLS = 256;
+// instruction descriptor: D f32, A/B tf32, both K-major, N = 256, M = 128
+constexpr uint32_t PW_IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((256u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32_w(uint32_t dtmem, uint64_t da, uint64_t db, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(da), "l"(db), "r"(PW_IDESC), "r"(acc));
+}
+
+// grid (MT, KTW, batch * batch2), 128 threads: thread = row of the tile
+__global__ void __launch_bounds__(128) k_tc_pack_aw(const cxf* __restrict__ A, long long lda, long long sA,
+                                                    long long sA2, int batch2, int M, int K, float* __restrict__ PA) {
+  const int tid = threadIdx.x;
+  const int mt = blockIdx.x, kt = blockIdx.y, MT = gridDim.x, KT = gridDim.y;
+  const long long z = blockIdx.z, bo = z / batch2, bi = z % batch2;
+  const cxf* Ab = A + bo * sA + bi * sA2;
+  const int gi = mt * TC_BM + tid, k0 = kt * PW_BK;
+  const bool rowok = gi < M;
+  cxf a[PW_BK];
+#pragma unroll
+  for (int kc = 0; kc < PW_BK; ++kc) {
+    const int gk = k0 + kc;
+    a[kc] = (rowok && gk < K) ? Ab[(long long)gi + (long long)gk * lda] : cxf(0.f, 0.f);
+  }
+  float* tile = PA + ((z * MT + mt) * (long long)KT + kt) * PW_A_TILE;
+#pragma unroll
+  for (int p = 0; p < PW_BK / 2; ++p) {
+    float4 big, small;
+    split4(a[2 * p].re, a[2 * p].im, a[2 * p + 1].re, a[2 * p + 1].im, big, small);
+    const int off = (p >> 1) * TC_A_STEP + kmaj4(tid, p & 1);
+    *reinterpret_cast<float4*>(tile + off) = big;
+    *reinterpret_cast<float4*>(tile + PW_KSTEPS * TC_A_STEP + off) = small;
+  }
+}
+
+// grid (NTW, KTW, batch * batch2), 128 threads: four (column, k pair) items each
+__global__ void __launch_bounds__(128) k_tc_pack_bw(const cxf* __restrict__ B, long long ldb, long long sB,
+                                                    long long sB2, int batch2, int N, int K, float* __restrict__ PB) {
+  const int tid = threadIdx.x;
+  const int nt = blockIdx.x, kt = blockIdx.y, NT = gridDim.x, KT = gridDim.y;
+  const long long z = blockIdx.z, bo = z / batch2, bi = z % batch2;
+  const cxf* Bb = B + bo * sB + bi * sB2;
+  const int n0 = nt * PW_BN, k0 = kt * PW_BK;
+  float* tile = PB + ((z * NT + nt) * (long long)KT + kt) * PW_B_TILE;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int item = tid + 128 * q;
+    const int j = item & (PW_BN - 1), p = item >> 7;  // j fastest: consecutive columns per warp
+    const int gj = n0 + j, gk = k0 + 2 * p;
+    const bool colok = gj < N;
+    const cxf v0 = (colok && gk < K) ? Bb[(long long)gk + (long long)gj * ldb] : cxf(0.f, 0.f);
+    const cxf v1 = (colok && gk + 1 < K) ? Bb[(long long)(gk + 1) + (long long)gj * ldb] : cxf(0.f, 0.f);
+    const int base = (p >> 1) * PW_B_STEP;
+    float4 big, small;
+    split4(v0.re, -v0.im, v1.re, -v1.im, big, small);
+    *reinterpret_cast<float4*>(tile + base + kmaj4(j, p & 1)) = big;
+    *reinterpret_cast<float4*>(tile + PW_KSTEPS * PW_B_STEP + base + kmaj4(j, p & 1)) = small;
+    split4(v0.im, v0.re, v1.im, v1.re, big, small);
+    *reinterpret_cast<float4*>(tile + base + kmaj4(PW_BN + j, p & 1)) = big;
+    *reinterpret_cast<float4*>(tile + PW_KSTEPS * PW_B_STEP + base + kmaj4(PW_BN + j, p & 1)) = small;
+  }
+}
+
+// grid (MT, NTW, batch * batch2), 128 threads
+__global__ void __launch_bounds__(128, 1) k_tc_cgemm_pkw(int M, int N, int KT, cxf alpha, const float* __restrict__ PA,
+                                                         const float* __restrict__ PB, cxf beta, cxf* C, long long ldc,
+                                                         long long sC, int batch2, long long sC2, int* err) {
+  extern __shared__ __align__(1024) unsigned char pw_smem[];
+  float* stages = reinterpret_cast<float*>(pw_smem);  // [PW_NST][A tile | B tile]
+  uint64_t* full = reinterpret_cast<uint64_t*>(stages + PW_NST * PW_STAGE);  // [PW_NST]
+  uint64_t* empty = full + PW_NST;                                          // [PW_NST]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(empty + PW_NST);
+  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int mt = blockIdx.x, nt = blockIdx.y, MT = gridDim.x, NT = gridDim.y;
+  const long long z = blockIdx.z, bo = z / batch2, bi = z % batch2;
+  const int m0 = mt * TC_BM, n0 = nt * PW_BN;
+  cxf* Cb = C + bo * sC + bi * sC2;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(PW_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < PW_NST; ++s) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(full + s)) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(empty + s)) : "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    *abort_flag = (*reinterpret_cast<volatile int*>(err) != 0) ? 1 : 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (tid == 0 && *abort_flag == 0) {
+    const float* pa = PA + (z * MT + mt) * (long long)KT * PW_A_TILE;
+    const float* pb = PB + (z * NT + nt) * (long long)KT * PW_B_TILE;
+    const uint32_t sbase = smem_u32(stages);
+    auto issue = [&](int t) {
+      const int s = t % PW_NST;
+      const uint32_t fb = smem_u32(full + s);
+      pk_expect(fb, (uint32_t)(PW_STAGE * sizeof(float)));
+      pk_bulk(sbase + (uint32_t)(s * PW_STAGE * sizeof(float)), pa + (long long)t * PW_A_TILE,
+              (uint32_t)(PW_A_TILE * sizeof(float)), fb);
+      pk_bulk(sbase + (uint32_t)((s * PW_STAGE + PW_A_TILE) * sizeof(float)), pb + (long long)t * PW_B_TILE,
+              (uint32_t)(PW_B_TILE * sizeof(float)), fb);
+    };
+    int issued = 0, consumed = 0, committed = 0, freed = 0;
+    bool good = true;
+    for (; issued < KT && issued < PW_NST; ++issued) issue(issued);
+    for (int kt = 0; kt < KT && good; ++kt) {
+      const int s = kt % PW_NST;
+      if (!mbar_wait_bounded(smem_u32(full + s), (uint32_t)((kt / PW_NST) & 1), g_tc_wait_polls)) {
+        good = false;
+        break;
+      }
+      ++consumed;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const float* sA = stages + s * PW_STAGE;
+      const float* sB = sA + PW_A_TILE;
+#pragma unroll
+      for (int q = 0; q < PW_KSTEPS; ++q) {
+        const uint64_t dab = smem_desc(smem_u32(sA + q * TC_A_STEP));
+        const uint64_t das = smem_desc(smem_u32(sA + PW_KSTEPS * TC_A_STEP + q * TC_A_STEP));
+        const uint64_t dbb = smem_desc(smem_u32(sB + q * PW_B_STEP));
+        const uint64_t dbs = smem_desc(smem_u32(sB + PW_KSTEPS * PW_B_STEP + q * PW_B_STEP));
+        mma_tf32_w(tmem, das, dbb, (kt | q) != 0);
+        mma_tf32_w(tmem, dab, dbs, 1);
+        mma_tf32_w(tmem, dab, dbb, 1);
+      }
+      mma_commit(smem_u32(empty + s));
+      ++committed;
+      if (kt >= 1 && issued < KT) {  // refill the stage of tile kt - 1 once its MMAs are done
+        const int t = kt - 1;
+        if (!mbar_wait_bounded(smem_u32(empty + t % PW_NST), (uint32_t)((t / PW_NST) & 1), g_tc_wait_polls)) {
+          good = false;
+          break;
+        }
+        ++freed;
+        issue(issued);
+        ++issued;
+      }
+    }
+    for (; good && freed < committed; ++freed)
+      if (!mbar_wait_bounded(smem_u32(empty + freed % PW_NST), (uint32_t)((freed / PW_NST) & 1), g_tc_wait_polls))
+        good = false;
+    if (!good) {
+      *abort_flag = 1;
+      atomicExch(err, 1);
+      for (int t = consumed; t < issued; ++t)
+        mbar_wait_bounded(smem_u32(full + t % PW_NST), (uint32_t)((t / PW_NST) & 1));
+      for (int t = freed; t < committed; ++t)
+        mbar_wait_bounded(smem_u32(empty + t % PW_NST), (uint32_t)((t / PW_NST) & 1));
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (*abort_flag == 0 && KT > 0) {
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+    const int i = m0 + warp * 32 + lane;
+    const bool use_beta = !(beta.re == 0.f && beta.im == 0.f);
+#pragma unroll 1
+    for (int ch = 0; ch < PW_BN / 32; ++ch) {
+      uint32_t re[32], im[32];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+          : "=r"(re[0]), "=r"(re[1]), "=r"(re[2]), "=r"(re[3]), "=r"(re[4]), "=r"(re[5]), "=r"(re[6]), "=r"(re[7]),
+            "=r"(re[8]), "=r"(re[9]), "=r"(re[10]), "=r"(re[11]), "=r"(re[12]), "=r"(re[13]), "=r"(re[14]),
+            "=r"(re[15]), "=r"(re[16]), "=r"(re[17]), "=r"(re[18]), "=r"(re[19]), "=r"(re[20]), "=r"(re[21]),
+            "=r"(re[22]), "=r"(re[23]), "=r"(re[24]), "=r"(re[25]), "=r"(re[26]), "=r"(re[27]), "=r"(re[28]),
+            "=r"(re[29]), "=r"(re[30]), "=r"(re[31])
+          : "r"(taddr + (uint32_t)(ch * 32)));
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+          : "=r"(im[0]), "=r"(im[1]), "=r"(im[2]), "=r"(im[3]), "=r"(im[4]), "=r"(im[5]), "=r"(im[6]), "=r"(im[7]),
+            "=r"(im[8]), "=r"(im[9]), "=r"(im[10]), "=r"(im[11]), "=r"(im[12]), "=r"(im[13]), "=r"(im[14]),
+            "=r"(im[15]), "=r"(im[16]), "=r"(im[17]), "=r"(im[18]), "=r"(im[19]), "=r"(im[20]), "=r"(im[21]),
+            "=r"(im[22]), "=r"(im[23]), "=r"(im[24]), "=r"(im[25]), "=r"(im[26]), "=r"(im[27]), "=r"(im[28]),
+            "=r"(im[29]), "=r"(im[30]), "=r"(im[31])
+          : "r"(taddr + (uint32_t)(PW_BN + ch * 32)));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (i < M) {
+        cxf cold[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int gj = n0 + ch * 32 + j;
+          cold[j] = (use_beta && gj < N) ? Cb[(long long)i + (long long)gj * ldc] : cxf(0.f, 0.f);
+        }
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int gj = n0 + ch * 32 + j;
+          if (gj < N) {
+            cxf v = alpha * cxf(__uint_as_float(re[j]), __uint_as_float(im[j]));
+            if (use_beta) v += beta * cold[j];
+            Cb[(long long)i + (long long)gj * ldc] = v;
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(PW_TMEM_COLS) : "memory");
+  }
+}
+
 // device error flag of the tensor-core GEMM (one per device, found by symbol)
 __device__ int g_tc_err;
 
 static size_t tc_smem_bytes() { return sizeof(float) * (size_t)(2 * TC_STAGE_FLOATS) + 64; }
 static size_t pk_smem_bytes() { return sizeof(float) * (size_t)(PK_NST * PK_STAGE) + 16 * PK_NST + 64; }
+static size_t pw_smem_bytes() { return sizeof(float) * (size_t)(PW_NST * PW_STAGE) + 16 * PW_NST + 64; }
 
 namespace {
 constexpr int TC_MAX_DEV = 64;
@@ -573,6 +815,11 @@ int* g_tc_err_addr[TC_MAX_DEV] = {};
 bool g_tc_attr[TC_MAX_DEV] = {};
 std::atomic<int> g_engine{GEMM_ENGINE_TCGEN05};
 std::atomic<bool> g_pk_enabled{true};  // packed-operand path of tc_gemm_c64
+// wide-tile packed path (QBG_GEMM_WIDE=0 in the environment keeps the 128 x 32 tiles)
+std::atomic<bool> g_pkw_enabled{[] {
+  const char* e = std::getenv("QBG_GEMM_WIDE");
+  return !(e && *e == '0');
+}()};
 
 int tc_device_setup(int** err_out) {
   int dev = 0;
@@ -585,6 +832,7 @@ int tc_device_setup(int** err_out) {
   if (!g_tc_attr[dev]) {
     QBG_CUDA(cudaFuncSetAttribute(k_tc_cgemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes()));
     QBG_CUDA(cudaFuncSetAttribute(k_tc_cgemm_pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pk_smem_bytes()));
+    QBG_CUDA(cudaFuncSetAttribute(k_tc_cgemm_pkw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pw_smem_bytes()));
     void* a = nullptr;
     QBG_CUDA(cudaGetSymbolAddress(&a, g_tc_err));
     g_tc_err_addr[dev] = static_cast<int*>(a);
@@ -668,6 +916,25 @@ int tc_gemm_c64(int M, int N, int K, cxf alpha, const cxf* A, long long lda, lon
   // each B tile by MT CTAs (measured on the FP32 LU of 48 operators of
   // N = 2048: faster from the 512 x 512 trailing updates up; the skinny solve
   // products, N = 64, and the updates inside an outer block are faster staged)
+  // wide tiles (128 x 128 complex) for the large products: N of at least two
+  // wide tiles and enough tiles to fill the device
+  const int NTW = (N + PW_BN - 1) / PW_BN, KTW = (K + PW_BK - 1) / PW_BK;
+  if (allow_packed && g_pk_enabled.load() && g_pkw_enabled.load() && KTW >= 4 && NTW >= 2 &&
+      (long long)MT * NTW * nb >= 152) {
+    const size_t pa = (size_t)nb * MT * KTW * PW_A_TILE, pb = (size_t)nb * NTW * KTW * PW_B_TILE;
+    void* scr = nullptr;
+    QBG_TRY(pack_scratch(st, sizeof(float) * (pa + pb), &scr));
+    float* PA = static_cast<float*>(scr);
+    float* PB = PA + pa;
+    k_tc_pack_aw<<<dim3(MT, KTW, nb), 128, 0, st>>>(A, lda, sA, sA2, batch2, M, K, PA);
+    QBG_LAUNCH_CHECK("k_tc_pack_aw");
+    k_tc_pack_bw<<<dim3(NTW, KTW, nb), 128, 0, st>>>(B, ldb, sB, sB2, batch2, N, K, PB);
+    QBG_LAUNCH_CHECK("k_tc_pack_bw");
+    k_tc_cgemm_pkw<<<dim3(MT, NTW, nb), 128, pw_smem_bytes(), st>>>(M, N, KTW, alpha, PA, PB, beta, C, ldc, sC,
+                                                                     batch2, sC2, derr);
+    QBG_LAUNCH_CHECK("k_tc_cgemm_pkw");
+    return QBG_OK;
+  }
   if (allow_packed && g_pk_enabled.load() && KT >= 2 && MT >= 4 && NT >= 8) {
     const size_t pa = (size_t)nb * MT * KT * PK_A_TILE, pb = (size_t)nb * NT * KT * PK_B_TILE;
     void* scr = nullptr;

@@ -21,6 +21,7 @@ from .beyn import BeynHandle, construct_B_matrix, solve_vect, solve, solve_disks
 from .sweep import k_sweep, get_eigenvalues, newton_refine_svd, refine_minima
 from . import sweep
 from . import ebim
+from . import autotune
 from .serve import Server
 from .spectrum import (plan_weyl_windows, beyn_disks_from_windows, candidate_residuals,
                        residual_and_norm_select, imag_k_check, compute_spectrum_beyn)

@@ -122,8 +122,8 @@ _SIGS = {
     "qbg_set_tc_wait_limit": (C.c_int32, [C.c_int64]),
     "qbg_dense_inverse": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                       C.POINTER(C.c_double), C.c_void_p]),
-    "qbg_set_lu_plan": (C.c_int32, [C.c_int32, C.c_int32]),
-    "qbg_get_lu_plan": (C.c_int32, [C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "qbg_set_lu_plan": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32]),
+    "qbg_get_lu_plan": (C.c_int32, [C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "qbg_clear_tc_error": (C.c_int32, []),
     "qbg_sigma_min": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]),
     "qbg_ebim_eig": (C.c_int32, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int32,

@@ -92,18 +92,18 @@ def test_complex64_lu_panel_forms(qb, n):
     rng = np.random.default_rng(n)
     As = [(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(2 * n) + 3.0 * np.eye(n)
           for _ in range(3)]
-    o0, c0 = C.c_int32(), C.c_int32()
-    L.check(lib.qbg_get_lu_plan(C.byref(o0), C.byref(c0)))
+    o0, c0, p0 = C.c_int32(), C.c_int32(), C.c_int32()
+    L.check(lib.qbg_get_lu_plan(C.byref(o0), C.byref(c0), C.byref(p0)))
     out = {}
     try:
         for outer, cluster in ((4, 0), (4, 1), (2, 1)):
-            L.check(lib.qbg_set_lu_plan(outer, cluster))
+            L.check(lib.qbg_set_lu_plan(outer, cluster, 0))
             Xs = _inv32(lib, L, As)
             for A, X in zip(As, Xs):
                 assert np.abs(A @ X - np.eye(n)).max() < 2e-5, (outer, cluster)
             out[(outer, cluster)] = Xs
     finally:
-        L.check(lib.qbg_set_lu_plan(o0.value, c0.value))
+        L.check(lib.qbg_set_lu_plan(o0.value, c0.value, p0.value))
     for key in ((4, 1), (2, 1)):
         for X0, X1 in zip(out[(4, 0)], out[key]):
             assert np.abs(X1 - X0).max() < 1e-5 * np.abs(X0).max()

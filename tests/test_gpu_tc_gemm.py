@@ -1,5 +1,7 @@
 """Complex64 GEMM engines of the FP32 LU: tcgen05 tensor cores (3xTF32) with
-packed operand tiles streamed by bulk copies for large products (engine 1) or
+packed operand tiles streamed by bulk copies for large products (engine 1:
+128 x 128 complex tiles, real N = 256 per MMA, when N spans two such tiles and
+the grid fills the device, else 128 x 32) or
 with operands split in registers (engine 2), and CUDA-core FMA tiles (engine
 0), against a complex128 NumPy product of the same inputs.
 
@@ -28,6 +30,8 @@ SHAPES = [
     (1000, 40, 334, 3),  # ragged rows and columns, k tail of one pair
     (512, 64, 512, 2),   # triangular-solve product shape
     (640, 1, 96, 1),     # one column
+    (1000, 1100, 77, 3), # wide 128 x 128 tiles: ragged M, N and K
+    (129, 257, 33, 60),  # wide tiles, one row and one column past a tile, many matrices
 ]
 
 
