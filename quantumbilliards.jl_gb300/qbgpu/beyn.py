@@ -186,7 +186,7 @@ def _B_from_moments(A0, A1, svd_tol):
 
 
 def solve_disks(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed=False, ws=None,
-                return_info=False, **kw):
+                return_info=False, regrow_ahead=True, **kw):
     """Eigenvalues of several disks from one device batch: construct_B_matrix
     for every disk (beyn.jl:257-322, one r -> 2r regrowth per disk, extending
     the probe block) with the contour nodes of all disks resident together.
@@ -204,16 +204,22 @@ def solve_disks(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed
     # moments reduced on the device: per disk R (A0 = Q R) and Q^H A1, m x m
     try:
         V = probe_matrix(N, r, rng)
+        ahead = regrow_ahead and 2 * r < N
+        if ahead:  # the regrowth block solved with the first one (see construct_B_matrix)
+            V = np.hstack([V, probe_matrix(N, r, rng)])
         t = clk()
-        R1, C1 = bh.moments_qr(V)
+        Rf, Cf = bh.moments_qr(V)
         host["moments"] += (clk() - t) * 1e3
         info["stats"].append(bh.last_stats)
+        R1, C1 = ([a[:r, :r] for a in Rf], [c[:r, :r] for c in Cf]) if ahead else (Rf, Cf)
         t = clk()
         S = [np.linalg.svd(a, compute_uv=False) for a in R1]
         host["svd"] += (clk() - t) * 1e3
         rks = [int(np.count_nonzero(s >= svd_tol)) for s in S]
         grow = [rk == r and 2 * r < N for rk in rks]
-        if any(grow):
+        if ahead:
+            R2, C2 = Rf, Cf
+        elif any(grow):
             Vn = probe_matrix(N, r, rng)
             t = clk()
             R2, C2 = bh.moments_qr(Vn, append=True)
@@ -244,7 +250,8 @@ def solve_disks(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed
 
 def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=None, mixed=False, ws=None,
                        max_refine=10, refine_tol=1e-6, return_info=False, regrow="extend", use_chebyshev=True,
-                       cheb=None, fp32_sweeps=0, solve_block=0, node_chunk=0, resid_engine=0, basis=True, nb=0):
+                       cheb=None, fp32_sweeps=0, solve_block=0, node_chunk=0, resid_engine=0, basis=True, nb=0,
+                       regrow_ahead=True):
     """construct_B_matrix (beyn.jl:257-322). Returns (B, Uk) [, info].
 
     regrow: when the rank saturates (rk == r) the reference draws a fresh
@@ -252,6 +259,15 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
     "fresh" does the same; "extend" (default) keeps the r columns already
     solved and draws only r new ones, so the moments of the 2r block cost r
     new solves. The eigenvalues of B do not depend on the probe block.
+
+    regrow_ahead (with "extend"): the r regrowth columns are drawn up front
+    and solved together with the first r, so the nodes' solves and the mixed
+    form's refinement run once on 2r columns instead of twice on r (the
+    operators' residual digit planes are streamed half as often). The rank
+    test still looks at the first r columns only (the leading r x r block of
+    R in A0 = Q R is the R of those columns), and without saturation B comes
+    from them alone, as in the reference; the extra columns are then work
+    spent for nothing, so pass False when r is expected to exceed the count.
 
     basis=False skips U_k (returned as None): the moments stay on the device,
     A0 = Q R is factored there and only R and Q^H A1 (m x m) come back, so the
@@ -273,10 +289,19 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
     moments = bh.moments if basis else bh.moments_qr
     try:
         V = probe_matrix(N, r, rng)
+        ahead = regrow == "extend" and regrow_ahead and 2 * r < N
+        if ahead:
+            V = np.hstack([V, probe_matrix(N, r, rng)])
         t = clk()
         M0, M1 = moments(V)  # (A0, A1), or (R, Q^H A1)
         host["moments"] += (clk() - t) * 1e3
         info["stats"].append(bh.last_stats)
+        if ahead:
+            M0f, M1f = M0, M1
+            if basis:
+                M0, M1 = np.asfortranarray(M0f[:, :r]), np.asfortranarray(M1f[:, :r])
+            else:
+                M0, M1 = np.asfortranarray(M0f[:r, :r]), np.asfortranarray(M1f[:r, :r])
         # the saturation test needs only the singular values; the factors are
         # computed once, for the block that is finally used
         t = clk()
@@ -292,7 +317,14 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
             return (*out, info) if return_info else out
         if rk == r:
             r_tmp = 2 * r
-            if r_tmp < N:
+            if r_tmp < N and ahead:
+                M0, M1 = M0f, M1f
+                t = clk()
+                U, S, Wh = np.linalg.svd(M0, full_matrices=False)
+                rk = int(np.count_nonzero(S >= svd_tol))
+                host["svd"] += (clk() - t) * 1e3
+                rused = r_tmp
+            elif r_tmp < N:
                 t = clk()
                 if regrow == "extend":
                     Vn = probe_matrix(N, r_tmp - r, rng)
