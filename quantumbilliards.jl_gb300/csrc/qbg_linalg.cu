@@ -22,6 +22,7 @@
 #include <cstdlib>
 #include <type_traits>
 #include "qbg_linalg.cuh"
+#include "qbg_handles.cuh"
 
 namespace qbg {
 
@@ -106,11 +107,74 @@ __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, cx<T> alpha, 
   }
 }
 
+// C = alpha sum_s P_s + beta C over the split-K partial products P_s (s
+// slices of M x N, column-major, stride M N), summed in slice order
+template <class T>
+__global__ void k_splitk_sum(const cx<T>* __restrict__ P, int splits, int M, int N, int batch, cx<T> alpha, cx<T> beta,
+                             cx<T>* C, long long ldc, long long sC) {
+  const long long mn = (long long)M * N, total = mn * batch;
+  const bool use_beta = !(beta.re == T(0) && beta.im == T(0));
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    const long long b = e / mn, r = e % mn;
+    const int i = (int)(r % M), j = (int)(r / M);
+    cx<T> v(0, 0);
+    for (int q = 0; q < splits; ++q) v += P[((long long)q * batch + b) * mn + r];
+    cx<T>* c = C + b * sC + (long long)i + (long long)j * ldc;
+    v = alpha * v;
+    if (use_beta) v += beta * (*c);
+    *c = v;
+  }
+}
+
+// FP64 on this part is ~2 FMA per clock per SM: a 64 x 64 tile with K = 256
+// is ~1 ms of one SM's FP64 pipe, so a complex128 product with fewer tiles
+// than SMs is split over K into slices of at least 16 (about two CTAs per
+// SM); the partial products are summed in a fixed order by a second kernel,
+// so the result does not depend on scheduling. Returns false when the
+// product is left to the plain launch.
+template <class T, bool CA>
+static bool gemm_split_k(int M, int N, int K, cx<T> alpha, const cx<T>* A, long long lda, long long sA,
+                         const cx<T>* B, long long ldb, long long sB, cx<T> beta, cx<T>* C, long long ldc,
+                         long long sC, int batch, cudaStream_t st, int* status) {
+  const long long tiles = (long long)((M + 63) / 64) * ((N + 63) / 64) * batch;
+  if (sizeof(T) != 8 || tiles >= 152 || K < 64) return false;
+  const int splits = (int)std::min<long long>(std::min<long long>((304 + tiles - 1) / tiles, K / 16), 16);
+  if (splits < 2) return false;
+  const int kc = ((K + splits - 1) / splits + 15) / 16 * 16;
+  const int ns = (K + kc - 1) / kc;
+  cx<T>* P = nullptr;
+  if ((*status = dmalloc(&P, sizeof(cx<T>) * (size_t)ns * batch * M * N))) return true;
+  for (int q = 0; q < ns; ++q) {
+    const int k0 = q * kc, kq = std::min(kc, K - k0);
+    // slice k0: columns k0.. of A (rows k0.. of the stored block for A^H), rows k0.. of B
+    const cx<T>* Aq = CA ? A + k0 : A + (long long)k0 * lda;
+    dim3 grd((M + 63) / 64, (N + 63) / 64, batch);
+    k_gemm<T, CA><<<grd, 256, 0, st>>>(M, N, kq, cx<T>(1, 0), Aq, lda, sA, B + k0, ldb, sB, cx<T>(0, 0),
+                                        P + (long long)q * batch * M * N, M, (long long)M * N);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      *status = cuda_status(e, "k_gemm split-k");
+      dfree(P, st);
+      return true;
+    }
+  }
+  const long long total = (long long)M * N * batch;
+  k_splitk_sum<T><<<(unsigned)std::min<long long>((total + 255) / 256, 4096), 256, 0, st>>>(P, ns, M, N, batch, alpha,
+                                                                                         beta, C, ldc, sC);
+  const cudaError_t e = cudaGetLastError();
+  *status = e == cudaSuccess ? QBG_OK : cuda_status(e, "k_splitk_sum");
+  dfree(P, st);
+  return true;
+}
+
 template <class T>
 int gemm_batched_simt(int M, int N, int K, cx<T> alpha, const cx<T>* A, long long lda, long long sA, const cx<T>* B,
                       long long ldb, long long sB, cx<T> beta, cx<T>* C, long long ldc, long long sC, int batch,
                       cudaStream_t st) {
   if (M <= 0 || N <= 0 || batch <= 0) return QBG_OK;
+  int status = QBG_OK;
+  if (gemm_split_k<T, false>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch, st, &status))
+    return status;
   dim3 grd((M + 63) / 64, (N + 63) / 64, batch);
   k_gemm<T><<<grd, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
   QBG_LAUNCH_CHECK("k_gemm");
@@ -123,6 +187,9 @@ int gemm_batched_ah(int M, int N, int K, cx<T> alpha, const cx<T>* A, long long 
                            const cx<T>* B, long long ldb, long long sB, cx<T> beta, cx<T>* C, long long ldc,
                            long long sC, int batch, cudaStream_t st) {
   if (M <= 0 || N <= 0 || batch <= 0) return QBG_OK;
+  int status = QBG_OK;
+  if (gemm_split_k<T, true>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch, st, &status))
+    return status;
   dim3 grd((M + 63) / 64, (N + 63) / 64, batch);
   k_gemm<T, true><<<grd, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
   QBG_LAUNCH_CHECK("k_gemm (A^H)");
@@ -456,14 +523,19 @@ __global__ void __launch_bounds__(1024) k_getrf_panel_smem(cx<T>* A, int n, long
 // per CTA; 1024 threads sharing each row's columns took 274 us, the per-thread
 // pivot bookkeeping then outweighing the split update.)
 // ---------------------------------------------------------------------------
-constexpr int PC_CS = 8, PC_THREADS = 256;
-// largest rows per CTA: 64 complex64 columns within 216 KiB of dynamic shared
-// memory (the push buffers take another ~10 KiB of static shared memory)
-constexpr int PC_MAX_RPC = 432;
+constexpr int PC_THREADS = 256;
+// largest rows per CTA: 64 columns within the dynamic shared memory left
+// beside the push buffers, whose static size grows with the cluster: 8 CTAs
+// 432 complex64 / 200 complex128 rows, 16 CTAs 416 / 192 rows
+template <class T, int CS>
+constexpr int pc_max_rpc() { return sizeof(T) == 4 ? (CS == 8 ? 432 : 416) : (CS == 8 ? 200 : 192); }
 
-template <class T>
-__global__ void __cluster_dims__(PC_CS, 1, 1) __launch_bounds__(PC_THREADS)
+// CS = 8 (portable cluster size) or 16 (non-portable, for panels too tall for
+// 8 CTAs' shared memory, used when the device can hold such a cluster)
+template <class T, int CS>
+__global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(PC_THREADS)
     k_getrf_panel_cluster(cx<T>* A, int n, long long stride, int j0, int nb, int rpc, int* ipiv, int* info) {
+  constexpr int PC_CS = CS;
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
   extern __shared__ unsigned char smraw[];
@@ -896,22 +968,45 @@ static int lu_factor_one(LUBatch<T>& f, cudaStream_t st, cudaEvent_t after_first
                                   (int)kPanelSmem));
     panel_attr[sizeof(T) == 8] = true;
   }
-  // complex64 panels of up to 64 columns and n <= PC_CS * PC_MAX_RPC rows of a
-  // small batch (at most 4 matrices, where one CTA per panel leaves most SMs
-  // idle) go to a cluster of CTAs. For larger batches the one-CTA panels of
+  // panels of up to 64 columns and n <= 8 (or 16) * pc_max_rpc rows of a small
+  // batch (at most 4 matrices, where one CTA per panel leaves most SMs idle;
+  // for complex128 one SM's FP64 pipe takes ~1 ms per 500 x 64 panel) go to
+  // a cluster of CTAs. For larger batches the one-CTA panels of
   // several matrices already run side by side with other matrices' updates,
   // and the cluster form measured slower (48 operators of 2048 in four
   // stream parts: factor phase 38.5 ms with clusters against 34.0 ms without).
   // set_lu_plan (or QBG_LU_CLUSTER=0 / =1 in the environment) forces either form.
   const int cluster_set = g_lu_cluster.load();
   const bool cluster_on = cluster_set < 0 ? batch <= 4 : cluster_set == 1;
-  const bool use_cluster = cluster_on && sizeof(T) == sizeof(float) && nb <= 64 && n <= PC_CS * PC_MAX_RPC;
   static bool cluster_attr[2] = {false, false};
-  if (use_cluster && !cluster_attr[sizeof(T) == 8]) {
-    QBG_CUDA(cudaFuncSetAttribute(k_getrf_panel_cluster<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  PC_MAX_RPC * 64 * (int)sizeof(cx<T>)));
+  static bool cluster16_ok[2] = {false, false};
+  if (cluster_on && nb <= 64 && !cluster_attr[sizeof(T) == 8]) {
+    QBG_CUDA(cudaFuncSetAttribute(k_getrf_panel_cluster<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  pc_max_rpc<T, 8>() * 64 * (int)sizeof(cx<T>)));
+    // 16-CTA clusters exist on this part as a non-portable size: allowed only
+    // when the occupancy query finds room for at least one
+    bool ok = cudaFuncSetAttribute(k_getrf_panel_cluster<T, 16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                  cudaSuccess &&
+              cudaFuncSetAttribute(k_getrf_panel_cluster<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   pc_max_rpc<T, 16>() * 64 * (int)sizeof(cx<T>)) == cudaSuccess;
+    if (ok) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(16, 1, 1);
+      cfg.blockDim = dim3(PC_THREADS, 1, 1);
+      cfg.dynamicSmemBytes = (size_t)pc_max_rpc<T, 16>() * 64 * sizeof(cx<T>);
+      int nclusters = 0;
+      ok = cudaOccupancyMaxActiveClusters(&nclusters, (void*)k_getrf_panel_cluster<T, 16>, &cfg) == cudaSuccess &&
+           nclusters >= 1;
+    }
+    (void)cudaGetLastError();  // a refused attribute or query leaves 16-CTA clusters off, nothing else
+    cluster16_ok[sizeof(T) == 8] = ok;
     cluster_attr[sizeof(T) == 8] = true;
   }
+  const int pcs = !(cluster_on && nb <= 64)                  ? 0
+                  : n <= 8 * pc_max_rpc<T, 8>()               ? 8
+                  : (cluster16_ok[sizeof(T) == 8] && n <= 16 * pc_max_rpc<T, 16>()) ? 16
+                                                              : 0;
+  const bool use_cluster = pcs > 0;
   QBG_CUDA(cudaMemsetAsync(f.info, 0, sizeof(int) * batch, st));
   // two-level right-looking LU: panels of nb columns inside outer blocks of
   // LU_OUTER panels. A panel's updates reach only the columns of its outer
@@ -930,10 +1025,14 @@ static int lu_factor_one(LUBatch<T>& f, cudaStream_t st, cudaEvent_t after_first
     for (int j0 = J0; j0 < E; j0 += nb) {
       const int w = min(nb, n - j0);
       if (use_cluster) {
-        const int rpc = (n - j0 + PC_CS - 1) / PC_CS;
+        const int rpc = (n - j0 + pcs - 1) / pcs;
         const size_t smem = (size_t)rpc * 64 * sizeof(cx<T>);
-        k_getrf_panel_cluster<T><<<batch * PC_CS, PC_THREADS, smem, st>>>(f.A, n, f.stride, j0, nb, rpc, f.ipiv,
-                                                                          f.info);
+        if (pcs == 8)
+          k_getrf_panel_cluster<T, 8><<<batch * 8, PC_THREADS, smem, st>>>(f.A, n, f.stride, j0, nb, rpc, f.ipiv,
+                                                                           f.info);
+        else
+          k_getrf_panel_cluster<T, 16><<<batch * 16, PC_THREADS, smem, st>>>(f.A, n, f.stride, j0, nb, rpc, f.ipiv,
+                                                                             f.info);
         QBG_LAUNCH_CHECK("k_getrf_panel_cluster");
       } else if (smem_panel) {
         const size_t smem = (size_t)(n - j0) * sub * sizeof(cx<T>);

@@ -79,9 +79,10 @@ def test_beyn_B_entry_matches_host_path(qb):
     host one-sided Jacobi SVD of R, the absolute rank test, one regrowth with
     the appended block) against construct_B_matrix on the same probes, whose
     SVD runs in LAPACK on the full A0: same rank and final column count,
-    eigenvalues of B inside the contour to 1e-11 relative (measured 4.7e-12
-    at svd_tol 1e-12, where the kept singular values reach 1e-12; all of them
-    to 1e-9), the same singular values to 1e-12 of
+    eigenvalues of B inside the contour to 5e-11 relative (measured 4.7e-12
+    and 1.1e-11 with different summation orders of the FP64 products, at
+    svd_tol 1e-12, where the kept singular values reach 1e-12; all of them to
+    1e-9), the same singular values to 1e-12 of
     the largest, and U_k spanning the same space (principal-angle cosines
     within 1e-8 of one, the median within 1e-13)."""
     import numpy as np
@@ -108,7 +109,7 @@ def test_beyn_B_entry_matches_host_path(qb):
         assert inside.any()
         # the eigenvalues inside the contour are the well-conditioned ones; the
         # spurious ones outside it carry the conditioning of the truncated A0
-        assert rel[inside].max() < 1e-11, (svd_tol, rel[inside].max())
+        assert rel[inside].max() < 5e-11, (svd_tol, rel[inside].max())
         assert rel.max() < 1e-9, (svd_tol, rel.max())
         # cosines of the principal angles; the directions whose singular values
         # sit near svd_tol are fixed only to eps * S[0] / S[rk-1] (1.5e-10

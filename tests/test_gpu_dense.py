@@ -10,6 +10,8 @@ subspace iteration on the inverse (the :svd branch, macros.jl:159-161).
   of the golden sweep, whose smallest singular values come in exact pairs
   (the rotational symmetry): sigma_min against the oracle's LAPACK values
   (tests/golden/c1_sweep.json) to 2e-12 relative;
+* one complex128 matrix of n = 1700 (a 16-CTA cluster panel where the device
+  holds one, split-K FP64 updates): A X - I <= 1e-12 cond;
 * the complex64 LU of the Beyn mixed form (panels, interchanges, tcgen05
   trailing updates) through both panel forms (one CTA per panel and the
   8-CTA cluster) and two outer-block depths, n = 700 and 2050, batch 3:
@@ -107,3 +109,20 @@ def test_complex64_lu_panel_forms(qb, n):
     for key in ((4, 1), (2, 1)):
         for X0, X1 in zip(out[(4, 0)], out[key]):
             assert np.abs(X1 - X0).max() < 1e-5 * np.abs(X0).max()
+
+
+@pytest.mark.parametrize("n", [1700])
+def test_fp64_lu_single_large(qb, n):
+    """One complex128 matrix taller than an 8-CTA cluster panel holds (n >
+    1600): the panel runs on a 16-CTA cluster where the device allows one (one
+    CTA otherwise), the small-grid updates split over K; A X - I <= 1e-12 cond."""
+    from qbgpu import _lib as L
+    lib = L.load()
+    rng = np.random.default_rng(n)
+    s = np.sort(rng.uniform(0.5, 3.0, n))[::-1]
+    s[-1] = 1e-3
+    A = (_haar(n, rng) * s) @ _haar(n, rng).conj().T
+    Ac = np.ascontiguousarray(A.T)[None]
+    X = np.empty_like(Ac)
+    L.check(lib.qbg_dense_inverse(n, 1, 0, L.vptr(Ac), L.vptr(X), None, None))
+    assert np.abs(A @ X[0].T - np.eye(n)).max() <= 1e-12 * s[0] / s[-1]
