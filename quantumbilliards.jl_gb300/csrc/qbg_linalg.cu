@@ -35,37 +35,33 @@ namespace qbg {
 // CA: the A operand is the conjugate transpose of the K x M block stored at A
 // (leading dimension lda), op(A)[i, k] = conj(A[k + i lda]).
 // ---------------------------------------------------------------------------
-template <class T, bool CA = false>
-__global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, cx<T> alpha, const cx<T>* __restrict__ A,
-                                              long long lda, long long sA, const cx<T>* B, long long ldb,
-                                              long long sB, cx<T> beta, cx<T>* C, long long ldc, long long sC) {
+// One 64 x 64 tile of op(A) B over k in [kb, ke) accumulated in acc (the
+// thread's 4 x 4 outputs); Ab, Bb point at the batch entry.
+template <class T, bool CA>
+__device__ __forceinline__ void gemm_tile(int M, int N, int K, int kb, int ke, const cx<T>* __restrict__ Ab,
+                                          long long lda, const cx<T>* Bb, long long ldb, int m0, int n0,
+                                          cx<T> (&acc)[4][4]) {
   constexpr int BM = 64, BN = 64, BK = 16;
   __shared__ cx<T> As[BK][BM];
   __shared__ cx<T> Bs[BK][BN + 1];
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
-  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
-  const long long bz = blockIdx.z;
-  const cx<T>* Ab = A + bz * sA;
-  const cx<T>* Bb = B + bz * sB;
-  cx<T>* Cb = C + bz * sC;
-  cx<T> acc[4][4];
 #pragma unroll
   for (int a = 0; a < 4; ++a)
 #pragma unroll
     for (int b = 0; b < 4; ++b) acc[a][b] = cx<T>(0, 0);
-  for (int k0 = 0; k0 < K; k0 += BK) {
+  for (int k0 = kb; k0 < ke; k0 += BK) {
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int idx = tid + q * 256;
       if (CA) {  // consecutive threads walk k, the contiguous index of the stored block
         const int kk = idx & (BK - 1), i = idx >> 4;
         const int gi = m0 + i, gk = k0 + kk;
-        As[kk][i] = (gi < M && gk < K) ? conj(Ab[(long long)gk + (long long)gi * lda]) : cx<T>(0, 0);
+        As[kk][i] = (gi < M && gk < ke) ? conj(Ab[(long long)gk + (long long)gi * lda]) : cx<T>(0, 0);
       } else {
         const int i = idx & (BM - 1), kk = idx >> 6;
         const int gi = m0 + i, gk = k0 + kk;
-        As[kk][i] = (gi < M && gk < K) ? Ab[(long long)gi + (long long)gk * lda] : cx<T>(0, 0);
+        As[kk][i] = (gi < M && gk < ke) ? Ab[(long long)gi + (long long)gk * lda] : cx<T>(0, 0);
       }
     }
 #pragma unroll
@@ -73,7 +69,7 @@ __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, cx<T> alpha, 
       const int idx = tid + q * 256;
       const int kk = idx & (BK - 1), jj = idx >> 4;
       const int gk = k0 + kk, gj = n0 + jj;
-      Bs[kk][jj] = (gk < K && gj < N) ? Bb[(long long)gk + (long long)gj * ldb] : cx<T>(0, 0);
+      Bs[kk][jj] = (gk < ke && gj < N) ? Bb[(long long)gk + (long long)gj * ldb] : cx<T>(0, 0);
     }
     __syncthreads();
 #pragma unroll
@@ -90,6 +86,20 @@ __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, cx<T> alpha, 
     }
     __syncthreads();
   }
+  (void)K;
+}
+
+template <class T, bool CA = false>
+__global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, cx<T> alpha, const cx<T>* __restrict__ A,
+                                              long long lda, long long sA, const cx<T>* B, long long ldb,
+                                              long long sB, cx<T> beta, cx<T>* C, long long ldc, long long sC) {
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int m0 = blockIdx.x * 64, n0 = blockIdx.y * 64;
+  const long long bz = blockIdx.z;
+  cx<T>* Cb = C + bz * sC;
+  cx<T> acc[4][4];
+  gemm_tile<T, CA>(M, N, K, 0, K, A + bz * sA, lda, B + bz * sB, ldb, m0, n0, acc);
   const bool use_beta = !(beta.re == T(0) && beta.im == T(0));
 #pragma unroll
   for (int b = 0; b < 4; ++b) {
@@ -103,6 +113,32 @@ __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, cx<T> alpha, 
       cx<T> v = alpha * acc[a][b];
       if (use_beta) v += beta * (*c);
       *c = v;
+    }
+  }
+}
+
+// Split-K partial products in one launch: z = b * ns + q computes
+// P[q, b] = op(A_b) B_b over k in [q kc, min(K, (q + 1) kc)).
+template <class T, bool CA>
+__global__ void __launch_bounds__(256) k_gemm_sk(int M, int N, int K, int kc, int ns, const cx<T>* __restrict__ A,
+                                                 long long lda, long long sA, const cx<T>* B, long long ldb,
+                                                 long long sB, cx<T>* P, int batch) {
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int m0 = blockIdx.x * 64, n0 = blockIdx.y * 64;
+  const long long b = blockIdx.z / ns, q = blockIdx.z % ns;
+  const int kb = (int)q * kc, ke = min(K, kb + kc);
+  cx<T> acc[4][4];
+  gemm_tile<T, CA>(M, N, K, kb, ke, A + b * sA, lda, B + b * sB, ldb, m0, n0, acc);
+  cx<T>* Pq = P + (q * batch + b) * (long long)M * N;
+#pragma unroll
+  for (int bb = 0; bb < 4; ++bb) {
+    const int gj = n0 + ty + 16 * bb;
+    if (gj >= N) continue;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int gi = m0 + tx + 16 * a;
+      if (gi < M) Pq[(long long)gi + (long long)gj * M] = acc[a][bb];
     }
   }
 }
@@ -137,23 +173,19 @@ static bool gemm_split_k(int M, int N, int K, cx<T> alpha, const cx<T>* A, long 
                          const cx<T>* B, long long ldb, long long sB, cx<T> beta, cx<T>* C, long long ldc,
                          long long sC, int batch, cudaStream_t st, int* status) {
   const long long tiles = (long long)((M + 63) / 64) * ((N + 63) / 64) * batch;
-  if (sizeof(T) != 8 || tiles >= 152 || K < 64) return false;
+  if (sizeof(T) != 8 || tiles >= 152 || K < 64 || (long long)batch * 16 > 65535) return false;
   const int splits = (int)std::min<long long>(std::min<long long>((304 + tiles - 1) / tiles, K / 16), 16);
   if (splits < 2) return false;
   const int kc = ((K + splits - 1) / splits + 15) / 16 * 16;
   const int ns = (K + kc - 1) / kc;
   cx<T>* P = nullptr;
   if ((*status = dmalloc(&P, sizeof(cx<T>) * (size_t)ns * batch * M * N))) return true;
-  for (int q = 0; q < ns; ++q) {
-    const int k0 = q * kc, kq = std::min(kc, K - k0);
-    // slice k0: columns k0.. of A (rows k0.. of the stored block for A^H), rows k0.. of B
-    const cx<T>* Aq = CA ? A + k0 : A + (long long)k0 * lda;
-    dim3 grd((M + 63) / 64, (N + 63) / 64, batch);
-    k_gemm<T, CA><<<grd, 256, 0, st>>>(M, N, kq, cx<T>(1, 0), Aq, lda, sA, B + k0, ldb, sB, cx<T>(0, 0),
-                                        P + (long long)q * batch * M * N, M, (long long)M * N);
+  {
+    dim3 grd((M + 63) / 64, (N + 63) / 64, batch * ns);
+    k_gemm_sk<T, CA><<<grd, 256, 0, st>>>(M, N, K, kc, ns, A, lda, sA, B, ldb, sB, P, batch);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
-      *status = cuda_status(e, "k_gemm split-k");
+      *status = cuda_status(e, "k_gemm_sk");
       dfree(P, st);
       return true;
     }
