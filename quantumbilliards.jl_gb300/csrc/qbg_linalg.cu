@@ -657,31 +657,34 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(PC_THREADS)
     __syncthreads();
     const cx<T> pv = prow[c];
     const bool nz = (pv.re != T(0) || pv.im != T(0));
-    const cx<T> inv = nz ? cinv(pv) : cx<T>(0, 0);
-    for (int i = tid; i < rows; i += PC_THREADS) {
-      if (r0 + i <= c) continue;
-      cx<T> l = P[c * rpc + i];
-      if (nz) {
-        l = l * inv;
-        P[c * rpc + i] = l;
-      }
-      // 8 columns at a time through registers: the shared-memory loads of a
-      // group are independent of the group's stores
-      for (int q0 = c + 1; q0 < w; q0 += 8) {
-        cx<T> u[8], v[8];
+    if (nz) {  // multipliers of column c
+      const cx<T> inv = cinv(pv);
+      for (int i = tid; i < rows; i += PC_THREADS)
+        if (r0 + i > c) P[c * rpc + i] = P[c * rpc + i] * inv;
+      __syncthreads();
+    }
+    // rank-1 update of the trailing columns as (row, 8-column chunk) items
+    // over all threads, so that short row blocks (small n, or 16 CTAs) still
+    // keep every thread busy; a chunk goes through registers, its
+    // shared-memory loads independent of its stores
+    const int i0 = max(0, c + 1 - r0);  // first own row below the diagonal
+    const int nrow = rows - i0, nch = (w - c - 1 + 7) >> 3;
+    for (int it = tid; it < nrow * nch; it += PC_THREADS) {
+      const int i = i0 + it % nrow, q0 = c + 1 + 8 * (it / nrow);
+      const cx<T> l = P[c * rpc + i];
+      cx<T> u[8], v[8];
 #pragma unroll
-        for (int t = 0; t < 8; ++t)
-          if (q0 + t < w) {
-            u[t] = prow[q0 + t];
-            v[t] = P[(q0 + t) * rpc + i];
-          }
+      for (int t = 0; t < 8; ++t)
+        if (q0 + t < w) {
+          u[t] = prow[q0 + t];
+          v[t] = P[(q0 + t) * rpc + i];
+        }
 #pragma unroll
-        for (int t = 0; t < 8; ++t)
-          if (q0 + t < w) {
-            cfms(v[t], l, u[t]);
-            P[(q0 + t) * rpc + i] = v[t];
-          }
-      }
+      for (int t = 0; t < 8; ++t)
+        if (q0 + t < w) {
+          cfms(v[t], l, u[t]);
+          P[(q0 + t) * rpc + i] = v[t];
+        }
     }
     __syncthreads();
   }
