@@ -540,9 +540,7 @@ def c3_disks(qb, repeat=2, n=4096, ndisk=32, nq=48, L=96):
     st = info["stats"]
     warm = min(times[1:]) if len(times) > 1 else times[0]
     return {"workload": "c3_dlp_kress_quarter_stadium_N4096_32disks_nq48_L96", "m": m, "operators": ndisk * nq,
-            "plan_s": plan_s,
-        "lu_plan": {"nb": nb, "outer": tuned["outer"], "parts": tuned["parts"], "tune_s": tuned["tune_s"],
-                    "tried": [[t["nb"], t["outer"], t["parts"], round(t["ms"], 1)] for t in tuned["table"]]}, "batch_s_cold": times[0], "batch_s_warm": warm, "eigenvalues": n_in,
+            "plan_s": plan_s, "batch_s_cold": times[0], "batch_s_warm": warm, "eigenvalues": n_in,
             "eigenvalues_per_s_warm": n_in / warm, "ms_assemble": st[0]["ms_assemble"],
             "ms_factor": st[0]["ms_factor"], "ms_solve": [s["ms_solve"] for s in st],
             "host_ms": {k: float("%.3g" % v) for k, v in info.get("host_ms", {}).items()}}
