@@ -12,6 +12,8 @@ the reference's ``;break`` does at :307), B = U_k^H A1 W_k Sigma_k^-1 and
 from __future__ import annotations
 
 import ctypes as C
+import glob
+import os
 import math
 import time
 import warnings
@@ -174,6 +176,65 @@ class BeynHandle:
             pass
 
 
+_LAPACKE = None
+
+
+def _lapacke_zgeev():
+    """(zgeev through LAPACKE of NumPy's bundled OpenBLAS, its thread setter
+    and getter), found by their exported names, or None."""
+    global _LAPACKE
+    if _LAPACKE is None:
+        _LAPACKE = False
+        try:
+            d = os.path.join(os.path.dirname(np.__file__), os.pardir, "numpy.libs")
+            for path in sorted(glob.glob(os.path.join(d, "libscipy_openblas*.so*"))):
+                lib = C.CDLL(path)
+                if all(hasattr(lib, x) for x in ("scipy_LAPACKE_zgeev64_", "scipy_openblas_set_num_threads64_",
+                                                 "scipy_openblas_get_num_threads64_")):
+                    f = lib.scipy_LAPACKE_zgeev64_
+                    f.restype = C.c_int64
+                    f.argtypes = [C.c_int, C.c_char, C.c_char, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p,
+                                  C.c_void_p, C.c_int64, C.c_void_p, C.c_int64]
+                    _LAPACKE = (f, lib.scipy_openblas_set_num_threads64_, lib.scipy_openblas_get_num_threads64_)
+                    break
+        except OSError:
+            _LAPACKE = False
+    return _LAPACKE or None
+
+
+def _eigvals_many(Bs):
+    """eigvals of every matrix of Bs (None: no eigenvalues), beyn.jl:371. With
+    several matrices the calls run on host threads through LAPACKE's zgeev
+    (ctypes releases the interpreter lock; NumPy's eigvals holds it), the BLAS
+    held to one thread per call; otherwise, or when LAPACKE is not found,
+    NumPy's eigvals one after another. Same LAPACK routine either way."""
+    empty = np.zeros(0, complex)
+    z = _lapacke_zgeev() if sum(B is not None for B in Bs) > 1 else None
+    if z is None:
+        return [np.linalg.eigvals(B) if B is not None else empty for B in Bs]
+    zgeev, set_threads, get_threads = z
+
+    def one(B):
+        if B is None:
+            return empty
+        A = np.array(B, dtype=np.complex128, order="F", copy=True)
+        n = A.shape[0]
+        w = np.empty(n, np.complex128)
+        info = zgeev(102, b"N", b"N", n, A.ctypes.data, n, w.ctypes.data, None, 1, None, 1)
+        if info != 0:
+            raise np.linalg.LinAlgError(f"zgeev info {info}")
+        return w
+
+    from concurrent.futures import ThreadPoolExecutor
+    n0 = int(get_threads())
+    set_threads(C.c_int(1))
+    try:
+        with ThreadPoolExecutor(max_workers=min(len(Bs), os.cpu_count() or 1)) as pool:
+            return list(pool.map(one, Bs))
+    finally:
+        set_threads(C.c_int(max(1, n0)))
+
+
 def _B_from_moments(A0, A1, svd_tol):
     """Thin SVD of A0, absolute rank, B = U_k^H A1 W_k Sigma_k^-1 (beyn.jl:286-320).
     Also takes (R, Q^H A1) of a device QR A0 = Q R: same S, W and B, U_R for U."""
@@ -231,17 +292,15 @@ def solve_disks(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed
         host["create"] += (clk() - t) * 1e3
     t = clk()
 
-    def one_disk(d):  # SVD of R, B and eig(B) of disk d
+    def one_disk(d):  # SVD of R and B of disk d
         Rd, Cd = (R2[d], C2[d]) if grow[d] else (R1[d], C1[d])
         if rks[d] == 0:
-            return np.zeros(0, complex), 0, r
+            return None, 0, r
         B, _, rk, _ = _B_from_moments(Rd, Cd, svd_tol)
-        return (np.linalg.eigvals(B) if rk else np.zeros(0, complex)), rk, Rd.shape[1]
+        return (B if rk else None), rk, Rd.shape[1]
 
-    # serial: LAPACK's own threads already use the host cores (a thread pool
-    # over disks measured slower on the 16-core host, 928 vs 649 ms for 32 disks)
     res = [one_disk(d) for d in range(len(k0s))]
-    out = [x[0] for x in res]
+    out = _eigvals_many([x[0] for x in res])
     info["rk"] = [x[1] for x in res]
     info["r"] = [x[2] for x in res]
     host["B_eigvals"] += (clk() - t) * 1e3

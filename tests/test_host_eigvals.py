@@ -1,0 +1,29 @@
+"""Host eigenvalues of many B matrices (qbgpu.beyn._eigvals_many, the last
+step of solve_disks; beyn.jl:371): LAPACK's zgeev on host threads through
+LAPACKE when NumPy's bundled OpenBLAS exports it, NumPy's eigvals otherwise.
+Against NumPy on the same matrices: every eigenvalue within 1e-12 of the
+largest modulus, disks without a B (rank 0) give none, and the BLAS thread
+count is restored."""
+import sys
+from pathlib import Path
+
+import numpy as np
+
+sys.path.insert(0, str(Path(__file__).resolve().parents[1] / "quantumbilliards.jl_gb300"))
+
+
+def test_eigvals_many_matches_numpy():
+    from qbgpu import beyn
+    rng = np.random.default_rng(3)
+    Bs = [rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) for n in (1, 7, 64, 150)] + [None]
+    z = beyn._lapacke_zgeev()
+    before = int(z[2]()) if z else None
+    got = beyn._eigvals_many(Bs)
+    assert len(got) == len(Bs) and len(got[-1]) == 0
+    for B, w in zip(Bs[:-1], got[:-1]):
+        ref = np.linalg.eigvals(B)
+        assert len(w) == len(ref)
+        d = max(np.min(np.abs(ref - x)) for x in w)
+        assert d <= 1e-12 * np.max(np.abs(ref)), d
+    if z:
+        assert int(z[2]()) == before
