@@ -179,9 +179,9 @@ class BeynHandle:
 _LAPACKE = None
 
 
-def _lapacke_zgeev():
-    """(zgeev through LAPACKE of NumPy's bundled OpenBLAS, its thread setter
-    and getter), found by their exported names, or None."""
+def _lapacke():
+    """dict(zgeev, zgesdd, set_threads, get_threads) of LAPACKE in NumPy's
+    bundled OpenBLAS, found by their exported names, or None."""
     global _LAPACKE
     if _LAPACKE is None:
         _LAPACKE = False
@@ -189,56 +189,83 @@ def _lapacke_zgeev():
             d = os.path.join(os.path.dirname(np.__file__), os.pardir, "numpy.libs")
             for path in sorted(glob.glob(os.path.join(d, "libscipy_openblas*.so*"))):
                 lib = C.CDLL(path)
-                if all(hasattr(lib, x) for x in ("scipy_LAPACKE_zgeev64_", "scipy_openblas_set_num_threads64_",
-                                                 "scipy_openblas_get_num_threads64_")):
-                    f = lib.scipy_LAPACKE_zgeev64_
-                    f.restype = C.c_int64
-                    f.argtypes = [C.c_int, C.c_char, C.c_char, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p,
-                                  C.c_void_p, C.c_int64, C.c_void_p, C.c_int64]
-                    _LAPACKE = (f, lib.scipy_openblas_set_num_threads64_, lib.scipy_openblas_get_num_threads64_)
+                names = ("scipy_LAPACKE_zgeev64_", "scipy_LAPACKE_zgesdd64_", "scipy_openblas_set_num_threads64_",
+                         "scipy_openblas_get_num_threads64_")
+                if all(hasattr(lib, x) for x in names):
+                    ev, sd = lib.scipy_LAPACKE_zgeev64_, lib.scipy_LAPACKE_zgesdd64_
+                    ev.restype = sd.restype = C.c_int64
+                    ev.argtypes = [C.c_int, C.c_char, C.c_char, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p,
+                                   C.c_void_p, C.c_int64, C.c_void_p, C.c_int64]
+                    sd.argtypes = [C.c_int, C.c_char, C.c_int64, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p,
+                                   C.c_void_p, C.c_int64, C.c_void_p, C.c_int64]
+                    _LAPACKE = dict(zgeev=ev, zgesdd=sd, set_threads=lib.scipy_openblas_set_num_threads64_,
+                                    get_threads=lib.scipy_openblas_get_num_threads64_)
                     break
         except OSError:
             _LAPACKE = False
     return _LAPACKE or None
 
 
-def _eigvals_many(Bs):
-    """eigvals of every matrix of Bs (None: no eigenvalues), beyn.jl:371. With
-    several matrices the calls run on host threads through LAPACKE's zgeev
-    (ctypes releases the interpreter lock; NumPy's eigvals holds it), the BLAS
-    held to one thread per call; otherwise, or when LAPACKE is not found,
-    NumPy's eigvals one after another. Same LAPACK routine either way."""
-    empty = np.zeros(0, complex)
-    z = _lapacke_zgeev() if sum(B is not None for B in Bs) > 1 else None
-    if z is None:
-        return [np.linalg.eigvals(B) if B is not None else empty for B in Bs]
-    zgeev, set_threads, get_threads = z
+def _svd_lapacke(z, A):
+    """Thin SVD U, S, W^H of A through LAPACKE's zgesdd (jobz 'S'), as numpy.linalg.svd."""
+    A = np.array(A, dtype=np.complex128, order="F", copy=True)
+    m, n = A.shape
+    k = min(m, n)
+    S = np.empty(k, np.float64)
+    U = np.empty((m, k), np.complex128, order="F")
+    Vh = np.empty((k, n), np.complex128, order="F")
+    info = z["zgesdd"](102, b"S", m, n, A.ctypes.data, m, S.ctypes.data, U.ctypes.data, m, Vh.ctypes.data, k)
+    if info != 0:
+        raise np.linalg.LinAlgError(f"zgesdd info {info}")
+    return U, S, Vh
 
-    def one(B):
+
+def _eigvals_lapacke(z, B):
+    A = np.array(B, dtype=np.complex128, order="F", copy=True)
+    n = A.shape[0]
+    w = np.empty(n, np.complex128)
+    info = z["zgeev"](102, b"N", b"N", n, A.ctypes.data, n, w.ctypes.data, None, 1, None, 1)
+    if info != 0:
+        raise np.linalg.LinAlgError(f"zgeev info {info}")
+    return w
+
+
+def _per_disk_host(jobs, fn):
+    """fn(job, lapacke) for every job: on host threads with the BLAS at one
+    thread per call when LAPACKE is found (ctypes releases the interpreter
+    lock, NumPy's svd and eigvals hold it), else one after another with
+    lapacke = None (NumPy). Same LAPACK routines either way."""
+    z = _lapacke() if len(jobs) > 1 else None
+    if z is None:
+        return [fn(j, None) for j in jobs]
+    from concurrent.futures import ThreadPoolExecutor
+    n0 = int(z["get_threads"]())
+    z["set_threads"](C.c_int(1))
+    try:
+        with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 1)) as pool:
+            return list(pool.map(lambda j: fn(j, z), jobs))
+    finally:
+        z["set_threads"](C.c_int(max(1, n0)))
+
+
+def _eigvals_many(Bs):
+    """eigvals of every matrix of Bs (None: no eigenvalues), beyn.jl:371,
+    on host threads (see _per_disk_host)."""
+    empty = np.zeros(0, complex)
+
+    def one(B, z):
         if B is None:
             return empty
-        A = np.array(B, dtype=np.complex128, order="F", copy=True)
-        n = A.shape[0]
-        w = np.empty(n, np.complex128)
-        info = zgeev(102, b"N", b"N", n, A.ctypes.data, n, w.ctypes.data, None, 1, None, 1)
-        if info != 0:
-            raise np.linalg.LinAlgError(f"zgeev info {info}")
-        return w
+        return _eigvals_lapacke(z, B) if z else np.linalg.eigvals(B)
 
-    from concurrent.futures import ThreadPoolExecutor
-    n0 = int(get_threads())
-    set_threads(C.c_int(1))
-    try:
-        with ThreadPoolExecutor(max_workers=min(len(Bs), os.cpu_count() or 1)) as pool:
-            return list(pool.map(one, Bs))
-    finally:
-        set_threads(C.c_int(max(1, n0)))
+    return _per_disk_host(list(Bs), one)
 
 
-def _B_from_moments(A0, A1, svd_tol):
+def _B_from_moments(A0, A1, svd_tol, svd=None):
     """Thin SVD of A0, absolute rank, B = U_k^H A1 W_k Sigma_k^-1 (beyn.jl:286-320).
-    Also takes (R, Q^H A1) of a device QR A0 = Q R: same S, W and B, U_R for U."""
-    U, S, Wh = np.linalg.svd(A0, full_matrices=False)
+    Also takes (R, Q^H A1) of a device QR A0 = Q R: same S, W and B, U_R for U.
+    svd: a thin-SVD function in place of numpy.linalg.svd."""
+    U, S, Wh = svd(A0) if svd else np.linalg.svd(A0, full_matrices=False)
     rk = int(np.count_nonzero(S >= svd_tol))
     Uk = U[:, :rk]
     Wk = Wh.conj().T[:, :rk]
@@ -274,7 +301,7 @@ def solve_disks(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed
         info["stats"].append(bh.last_stats)
         R1, C1 = ([a[:r, :r] for a in Rf], [c[:r, :r] for c in Cf]) if ahead else (Rf, Cf)
         t = clk()
-        S = [np.linalg.svd(a, compute_uv=False) for a in R1]
+        S = _per_disk_host(list(R1), lambda a, z: _svd_lapacke(z, a)[1] if z else np.linalg.svd(a, compute_uv=False))
         host["svd"] += (clk() - t) * 1e3
         rks = [int(np.count_nonzero(s >= svd_tol)) for s in S]
         grow = [rk == r and 2 * r < N for rk in rks]
@@ -292,15 +319,17 @@ def solve_disks(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed
         host["create"] += (clk() - t) * 1e3
     t = clk()
 
-    def one_disk(d):  # SVD of R and B of disk d
+    def one_disk(d, z):  # SVD of R, B and eig(B) of disk d
         Rd, Cd = (R2[d], C2[d]) if grow[d] else (R1[d], C1[d])
         if rks[d] == 0:
-            return None, 0, r
-        B, _, rk, _ = _B_from_moments(Rd, Cd, svd_tol)
-        return (B if rk else None), rk, Rd.shape[1]
+            return np.zeros(0, complex), 0, r
+        B, _, rk, _ = _B_from_moments(Rd, Cd, svd_tol, svd=(lambda A: _svd_lapacke(z, A)) if z else None)
+        if not rk:
+            return np.zeros(0, complex), 0, Rd.shape[1]
+        return (_eigvals_lapacke(z, B) if z else np.linalg.eigvals(B)), rk, Rd.shape[1]
 
-    res = [one_disk(d) for d in range(len(k0s))]
-    out = _eigvals_many([x[0] for x in res])
+    res = _per_disk_host(list(range(len(k0s))), one_disk)
+    out = [x[0] for x in res]
     info["rk"] = [x[1] for x in res]
     info["r"] = [x[2] for x in res]
     host["B_eigvals"] += (clk() - t) * 1e3

@@ -2,8 +2,8 @@
 step of solve_disks; beyn.jl:371): LAPACK's zgeev on host threads through
 LAPACKE when NumPy's bundled OpenBLAS exports it, NumPy's eigvals otherwise.
 Against NumPy on the same matrices: every eigenvalue within 1e-12 of the
-largest modulus, disks without a B (rank 0) give none, and the BLAS thread
-count is restored."""
+largest modulus, disks without a B (rank 0) give none, the BLAS thread
+count is restored, and LAPACKE's zgesdd reproduces NumPy's thin SVD."""
 import sys
 from pathlib import Path
 
@@ -16,8 +16,8 @@ def test_eigvals_many_matches_numpy():
     from qbgpu import beyn
     rng = np.random.default_rng(3)
     Bs = [rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) for n in (1, 7, 64, 150)] + [None]
-    z = beyn._lapacke_zgeev()
-    before = int(z[2]()) if z else None
+    z = beyn._lapacke()
+    before = int(z["get_threads"]()) if z else None
     got = beyn._eigvals_many(Bs)
     assert len(got) == len(Bs) and len(got[-1]) == 0
     for B, w in zip(Bs[:-1], got[:-1]):
@@ -26,4 +26,8 @@ def test_eigvals_many_matches_numpy():
         d = max(np.min(np.abs(ref - x)) for x in w)
         assert d <= 1e-12 * np.max(np.abs(ref)), d
     if z:
-        assert int(z[2]()) == before
+        assert int(z["get_threads"]()) == before
+        A = Bs[3]
+        U, S, Vh = beyn._svd_lapacke(z, A)
+        assert np.max(np.abs(S - np.linalg.svd(A, compute_uv=False))) <= 1e-12 * S[0]
+        assert np.max(np.abs((U * S) @ Vh - A)) <= 1e-12 * S[0]
