@@ -4,6 +4,7 @@
     python profile_case.py assemble --nq 8
     python profile_case.py disks --n 4096 --ndisk 32 --nq 48 --L 96
     python profile_case.py large --n 16384 --nq 48 --L 128 --chunk 8
+    python profile_case.py newton
 
 Cases use the bench workload (CFIE Kress, star r = 1 + 0.2 cos 5 theta,
 N = 2048, k0 = 200, R = 0.5, L = 64) with an adjustable number of contour nodes
@@ -112,9 +113,23 @@ def sweep_case(qb):
                           refined=[round(float(k), 10) for k in kr])))
 
 
+def newton_case(qb):
+    """One newton_refine_svd call (two Newton steps) on the unit circle, DLP
+    Kress with pts_scaling_factor 12.2 discretised at k = 40.06 (N = 490),
+    window [40.0574, 40.0594], twice (the second call warm)."""
+    from qbgpu import sweep
+    b = qb.make_circle(1.0)
+    sol = qb.DLP_kress(12.2, b)
+    ws = qb.Workspace(sol, qb.evaluate_points(sol, b, 40.06))
+    for _ in range(2):
+        t0 = time.perf_counter()
+        k, t, it = sweep.newton_refine_svd(ws, 40.0584, 40.0574, 40.0594, 8, 1e-12, return_iters=True)
+        print(json.dumps(dict(case="newton", N=ws.dim, k=k, tension=t, iters=it, ms=(time.perf_counter() - t0) * 1e3)))
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["beyn", "assemble", "disks", "large", "ebim", "sweep"])
+    ap.add_argument("case", choices=["beyn", "assemble", "disks", "large", "ebim", "sweep", "newton"])
     ap.add_argument("--ndisk", type=int, default=32)
     ap.add_argument("--repeat", type=int, default=1, help="disks: batches run back to back (first cold, rest warm)")
     ap.add_argument("--chunk", type=int, default=8)
@@ -136,6 +151,8 @@ def main(argv=None):
     qb.set_gemm_engine(a.gemm_engine)
     if a.case == "sweep":
         return sweep_case(qb)
+    if a.case == "newton":
+        return newton_case(qb)
     if a.case == "disks":
         return disks_case(qb, a)
     if a.case == "large":
