@@ -21,10 +21,10 @@ oracle is reported, and the plain FP64 path is timed beside it.
 
 cpu_baseline and --impl reference: the reference's CPU algorithm restated on
 the host cores (oracle/cpu.py: Chebyshev tables from AMOS, C assembly threaded
-over columns, LAPACK LU and solves, the fresh 2r regrowth block), one contour
-node per step; the eigenvalues per disk come from one untimed full disk of
-the same code, matched to the oracle fixture of the reference's regrowth
-policy (tests/golden/c2_beyn_fresh.json).
+over columns, LAPACK LU and solves, the fresh 2r regrowth block), one whole
+disk per timed step (at most three, after at most one untimed: a disk is ~18 s
+on 16 cores); the eigenvalues are matched to the oracle fixture of the
+reference's regrowth policy (tests/golden/c2_beyn_fresh.json).
 
 other_configs (default run, after the timed region; --no-extras leaves it
 out): bounded samples of the other configurations -- C1 (the sigma_min sweep
@@ -210,12 +210,12 @@ def replica_reduce(world, t_region, eig_count):
 
 def cpu_disk(steps, warmup, threads=None):
     """The reference's CPU Beyn path restated on the host cores (oracle/cpu.py):
-    the panels tuned once (chebyshev_params rule, tol 1e-13; plan_s), one
-    untimed full disk of the same code for the eigenvalue count (eigenvalues
-    inside the disk within TOL_EIG of the oracle fixture), then `steps` timed
-    steps of one contour node each (table fit, assembly, LU, solves of the r
-    and the fresh 2r probe blocks). The disk time is nq node steps plus the
-    measured moments/SVD/B/eig time of the full disk."""
+    the panels tuned once (chebyshev_params rule, tol 1e-13; plan_s, not
+    timed), `warmup` untimed whole disks, then `steps` timed whole disks, each
+    the 48 contour nodes (table fit, assembly, LAPACK LU, solves of the r and
+    the fresh 2r probe blocks) and the disk's moments, SVD, B and eig(B). The
+    eigenvalue count is that of the last disk: eigenvalues inside the disk
+    within TOL_EIG of the oracle fixture of the reference's regrowth policy."""
     from concurrent.futures import ThreadPoolExecutor
     from oracle import beyn as OB, cpu as OCPU, geometry as OG
     threads = threads or os.cpu_count()
@@ -227,39 +227,38 @@ def cpu_disk(steps, warmup, threads=None):
         t0 = time.perf_counter()
         prm = OCPU.chebyshev_params(g, zj, tol=CHEB_TOL, pool=pool)
         plan_s = time.perf_counter() - t0
-    cb = OCPU.BeynCPU(pts, K0, RADIUS, NQ, L_PROBES, SVD_TOL, SEED, prm[:4], threads)
-    try:
-        t0 = time.perf_counter()
-        for j in range(NQ):
-            cb.node(j)
-        t1 = time.perf_counter()
-        lam, rk, r_used = cb.finish()
-        t2 = time.perf_counter()
-        sel, e, missing = accuracy(lam, oracle_eigenvalues("fresh"))
-        n_eig = int(np.count_nonzero(e <= TOL_EIG))
-        for s in range(warmup):
-            cb.node(s % NQ)
-        times = []
-        for s in range(steps):
-            ts = time.perf_counter()
-            cb.node((warmup + s) % NQ)
-            times.append(time.perf_counter() - ts)
-    finally:
-        cb.close()
-    t_node = float(np.mean(times))
-    t_disk = NQ * t_node + (t2 - t1)
-    return dict(value=n_eig / t_disk, n_eig=n_eig, t_node=t_node, t_disk=t_disk, full_disk_s=t2 - t0,
-                finish_s=t2 - t1, plan_s=plan_s, cheb=[int(x) for x in prm[:4]], cores=threads, rk=rk, r=r_used,
-                max_rel_err_vs_oracle=float(e.max()) if len(e) else None, missing=missing, steps=steps,
-                region_s=float(np.sum(times)))
+    times, node_s, finish_s = [], [], []
+    lam, rk, r_used = None, 0, 0
+    for s in range(warmup + steps):
+        cb = OCPU.BeynCPU(pts, K0, RADIUS, NQ, L_PROBES, SVD_TOL, SEED, prm[:4], threads)
+        try:
+            t0 = time.perf_counter()
+            for j in range(NQ):
+                cb.node(j)
+            t1 = time.perf_counter()
+            lam, rk, r_used = cb.finish()
+            t2 = time.perf_counter()
+        finally:
+            cb.close()
+        if s >= warmup:
+            times.append(t2 - t0)
+            node_s.append((t1 - t0) / NQ)
+            finish_s.append(t2 - t1)
+    sel, e, missing = accuracy(lam, oracle_eigenvalues("fresh"))
+    n_eig = int(np.count_nonzero(e <= TOL_EIG))
+    t_disk = float(np.mean(times))
+    return dict(value=n_eig / t_disk, n_eig=n_eig, t_disk=t_disk, t_node=float(np.mean(node_s)),
+                finish_s=float(np.mean(finish_s)), plan_s=plan_s, cheb=[int(x) for x in prm[:4]], cores=threads, rk=rk,
+                r=r_used, max_rel_err_vs_oracle=float(e.max()) if len(e) else None, missing=missing, steps=steps,
+                warmup=warmup, region_s=float(np.sum(times)))
 
 
 def cpu_sample_text(c):
-    return (f"one contour node per timed step ({c['steps']} steps, {c['region_s']:.1f} s): Chebyshev tables "
-            f"{c['cheb']} fitted to AMOS values, C assembly on {c['cores']} threads, LAPACK LU and solves of "
-            f"{L_PROBES} + {2 * L_PROBES} probes; disk = {NQ} node steps + moments/SVD/eig "
-            f"({c['finish_s']:.2f} s); {c['n_eig']} eigenvalues within 1e-10 of the oracle from one untimed full disk "
-            f"({c['full_disk_s']:.1f} s); panel tuning {c['plan_s']:.1f} s not counted")
+    return (f"{c['steps']} whole disk(s) timed after {c['warmup']} untimed ({c['region_s']:.1f} s): per disk "
+            f"{NQ} contour nodes (Chebyshev tables {c['cheb']} fitted to AMOS values, C assembly on {c['cores']} "
+            f"threads, LAPACK LU and solves of {L_PROBES} + {2 * L_PROBES} probes; {c['t_node']:.2f} s per node) and "
+            f"the moments/SVD/B/eig ({c['finish_s']:.2f} s); {c['n_eig']} eigenvalues within 1e-10 of the oracle; "
+            f"panel tuning {c['plan_s']:.1f} s not counted")
 
 
 def main():
@@ -270,7 +269,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=1)
-    ap.add_argument("--cpu-steps", type=int, default=4, help="timed node steps of the cpu_baseline leg")
+    ap.add_argument("--cpu-steps", type=int, default=1, help="timed whole disks of the cpu_baseline leg")
     ap.add_argument("--workload", default="beyn", choices=["beyn", "ebim", "c1", "c3", "serve"],
                     help="beyn: the headline Beyn disk (default); ebim: the EBIM eigen step at one k; c1: the "
                          "sigma_min sweep of the unit circle and refine_minima; c3: 32 batched disks of the "
@@ -471,7 +470,7 @@ def main():
                     "N = 8192 take minutes per request on this part); bench.py --workload serve runs the full "
                     "stream"}
     if not args.no_cpu_baseline and rank == 0 and world == 1:
-        c = cpu_disk(args.cpu_steps, 1)
+        c = cpu_disk(max(1, args.cpu_steps), 0)
         line["cpu_baseline"] = {"value": c["value"], "unit": "eigenvalues/s", "cores": c["cores"], "kind": "port",
                                 "sample": cpu_sample_text(c), "max_rel_err_vs_oracle": c["max_rel_err_vs_oracle"]}
     if rank == 0:
@@ -762,15 +761,20 @@ def reference_arm_ebim(args):
 
 def reference_arm(args):
     """--impl reference: the reference's CPU Beyn path restated on the host
-    cores (oracle/cpu.py, see cpu_disk), one contour node per timed step."""
-    c = cpu_disk(args.steps, args.warmup)
+    cores (oracle/cpu.py, see cpu_disk), one whole disk per timed step. A disk
+    takes ~18 s on the 16 host cores, so at most 3 timed disks after at most
+    one untimed one are run, whatever --steps / --warmup ask (steps and
+    warmup in the line are the numbers run)."""
+    steps, warmup = max(1, min(args.steps, 3)), min(args.warmup, 1)
+    c = cpu_disk(steps, warmup)
     print(json.dumps({"impl": "reference", "metric": METRIC, "value": c["value"], "unit": "eigenvalues/s",
-                      "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": c["t_node"] * 1e3,
+                      "n_gpus": 1, "steps": steps, "warmup": warmup, "steps_requested": args.steps,
+                      "warmup_requested": args.warmup, "ms_per_step": c["t_disk"] * 1e3,
                       "higher_is_better": True, "dtype": "c128", "data": "synthetic",
                       "config": dict(workload_config(), cheb_panels=c["cheb"], cheb_tol=CHEB_TOL,
-                                     timing="host wall clock of each node step; value = eigenvalues per disk / "
-                                            "(48 node steps + the disk's moments, SVD and eig)"),
-                      "disk_s": c["t_disk"], "full_disk_s": c["full_disk_s"], "plan_s": c["plan_s"],
+                                     timing="host wall clock of each whole disk (48 node steps, moments, SVD, B, "
+                                            "eig); value = eigenvalues per disk / mean disk time"),
+                      "disk_s": c["t_disk"], "plan_s": c["plan_s"],
                       "eigenvalues_per_disk": c["n_eig"], "max_rel_err_vs_oracle": c["max_rel_err_vs_oracle"],
                       "rk": c["rk"], "r_final": c["r"],
                       "cpu_baseline": {"value": c["value"], "unit": "eigenvalues/s", "cores": c["cores"], "kind": "port",
