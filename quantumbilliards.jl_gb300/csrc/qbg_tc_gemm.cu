@@ -24,7 +24,9 @@
 // registers before the k loop. Every mbarrier wait is
 // bounded: on timeout the kernel records an error, waits (bounded) for its own
 // MMAs, frees its TMEM and returns without writing C.
+#include <algorithm>
 #include <atomic>
+#include <type_traits>
 #include <cstdlib>
 #include <cstdint>
 #include <mutex>
@@ -568,22 +570,27 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm_pk(int M, int N, int KT, cx
 // (Im, Re)), so an A tile read from L2 feeds four times the MMA work of the
 // 128 x 32 tile. Accumulator: 256 TMEM columns (Re C in 0..127, Im C in
 // 128..255). Operands are packed (split into big and small TF32 parts) in
-// tiles of 8 complex k (two MMA k steps), one bulk copy per operand and
+// tiles of 4 KS complex k (KS MMA k steps), one bulk copy per operand and
 // stage, through a four-stage ring:
-//   PAW tile (b, mt, kt): [big | small] x 2 MMA steps x 128 rows x 8 real k (16 KB)
-//   PBW tile (b, nt, kt): [big | small] x 2 MMA steps x 256 B' rows x 8 real k (32 KB)
+//   PAW tile (b, mt, kt): [big | small] x KS MMA steps x 128 rows x 8 real k (8 KS KB)
+//   PBW tile (b, nt, kt): [big | small] x KS MMA steps x 256 B' rows x 8 real k (16 KS KB)
 // The epilogue reads the accumulator in 32-column chunks and updates C
 // (beta C read there, not prefetched). Waits bounded as in k_tc_cgemm_pk.
 // ---------------------------------------------------------------------------
 constexpr int PW_BN = 128;                                  // complex columns per CTA (real N = 256)
-constexpr int PW_BK = 8;                                    // complex k per stage (two MMA k steps)
-constexpr int PW_KSTEPS = 2;
-constexpr int PW_NST = 4;
-constexpr int PW_A_TILE = 2 * PW_KSTEPS * TC_A_STEP;        // 4096 floats
+constexpr int PW_NST = 4;                                   // stages in the ring
 constexpr int PW_B_STEP = 2 * PW_BN * 8;                    // floats per B' block per MMA step (8 KB)
-constexpr int PW_B_TILE = 2 * PW_KSTEPS * PW_B_STEP;        // 8192 floats
-constexpr int PW_STAGE = PW_A_TILE + PW_B_TILE;             // 12288 floats (48 KB)
 constexpr uint32_t PW_TMEM_COLS = 256;
+// KS MMA k steps (4 KS complex k) per stage: KS = 2, 48 KB stages, one CTA per
+// SM; KS = 1, 24 KB stages, two CTAs per SM (96 KB of stages and 256 TMEM
+// columns each), so one CTA's epilogue and pipeline fill overlap the other's MMAs
+template <int KS> struct PW {
+  static constexpr int BK = 4 * KS;                           // complex k per stage
+  static constexpr int A_TILE = 2 * KS * TC_A_STEP;           // floats
+  static constexpr int B_TILE = 2 * KS * PW_B_STEP;
+  static constexpr int STAGE = A_TILE + B_TILE;
+  static constexpr int CTAS = KS == 1 ? 2 : 1;                // resident CTAs per SM
+};
 // instruction descriptor: D f32, A/B tf32, both K-major, N = 256, M = 128
 constexpr uint32_t PW_IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((256u >> 3) << 17) | ((128u >> 4) << 24);
 
@@ -595,8 +602,10 @@ __device__ __forceinline__ void mma_tf32_w(uint32_t dtmem, uint64_t da, uint64_t
 }
 
 // grid (MT, KTW, batch * batch2), 128 threads: thread = row of the tile
+template <int KS>
 __global__ void __launch_bounds__(128) k_tc_pack_aw(const cxf* __restrict__ A, long long lda, long long sA,
                                                     long long sA2, int batch2, int M, int K, float* __restrict__ PA) {
+  constexpr int PW_BK = PW<KS>::BK, PW_KSTEPS = KS, PW_A_TILE = PW<KS>::A_TILE;
   const int tid = threadIdx.x;
   const int mt = blockIdx.x, kt = blockIdx.y, MT = gridDim.x, KT = gridDim.y;
   const long long z = blockIdx.z, bo = z / batch2, bi = z % batch2;
@@ -620,9 +629,11 @@ __global__ void __launch_bounds__(128) k_tc_pack_aw(const cxf* __restrict__ A, l
   }
 }
 
-// grid (NTW, KTW, batch * batch2), 128 threads: four (column, k pair) items each
+// grid (NTW, KTW, batch * batch2), 128 threads: 2 KS (column, k pair) items each
+template <int KS>
 __global__ void __launch_bounds__(128) k_tc_pack_bw(const cxf* __restrict__ B, long long ldb, long long sB,
                                                     long long sB2, int batch2, int N, int K, float* __restrict__ PB) {
+  constexpr int PW_BK = PW<KS>::BK, PW_KSTEPS = KS, PW_B_TILE = PW<KS>::B_TILE;
   const int tid = threadIdx.x;
   const int nt = blockIdx.x, kt = blockIdx.y, NT = gridDim.x, KT = gridDim.y;
   const long long z = blockIdx.z, bo = z / batch2, bi = z % batch2;
@@ -630,7 +641,7 @@ __global__ void __launch_bounds__(128) k_tc_pack_bw(const cxf* __restrict__ B, l
   const int n0 = nt * PW_BN, k0 = kt * PW_BK;
   float* tile = PB + ((z * NT + nt) * (long long)KT + kt) * PW_B_TILE;
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
+  for (int q = 0; q < 2 * KS; ++q) {
     const int item = tid + 128 * q;
     const int j = item & (PW_BN - 1), p = item >> 7;  // j fastest: consecutive columns per warp
     const int gj = n0 + j, gk = k0 + 2 * p;
@@ -649,9 +660,13 @@ __global__ void __launch_bounds__(128) k_tc_pack_bw(const cxf* __restrict__ B, l
 }
 
 // grid (MT, NTW, batch * batch2), 128 threads
-__global__ void __launch_bounds__(128, 1) k_tc_cgemm_pkw(int M, int N, int KT, cxf alpha, const float* __restrict__ PA,
-                                                         const float* __restrict__ PB, cxf beta, cxf* C, long long ldc,
-                                                         long long sC, int batch2, long long sC2, int* err) {
+template <int KS>
+__global__ void __launch_bounds__(128, PW<KS>::CTAS) k_tc_cgemm_pkw(int M, int N, int KT, cxf alpha,
+                                                                   const float* __restrict__ PA,
+                                                                   const float* __restrict__ PB, cxf beta, cxf* C,
+                                                                   long long ldc, long long sC, int batch2,
+                                                                   long long sC2, int* err) {
+  constexpr int PW_KSTEPS = KS, PW_A_TILE = PW<KS>::A_TILE, PW_B_TILE = PW<KS>::B_TILE, PW_STAGE = PW<KS>::STAGE;
   extern __shared__ __align__(1024) unsigned char pw_smem[];
   float* stages = reinterpret_cast<float*>(pw_smem);  // [PW_NST][A tile | B tile]
   uint64_t* full = reinterpret_cast<uint64_t*>(stages + PW_NST * PW_STAGE);  // [PW_NST]
@@ -806,7 +821,8 @@ __device__ int g_tc_err;
 
 static size_t tc_smem_bytes() { return sizeof(float) * (size_t)(2 * TC_STAGE_FLOATS) + 64; }
 static size_t pk_smem_bytes() { return sizeof(float) * (size_t)(PK_NST * PK_STAGE) + 16 * PK_NST + 64; }
-static size_t pw_smem_bytes() { return sizeof(float) * (size_t)(PW_NST * PW_STAGE) + 16 * PW_NST + 64; }
+template <int KS>
+static size_t pw_smem_bytes() { return sizeof(float) * (size_t)(PW_NST * PW<KS>::STAGE) + 16 * PW_NST + 64; }
 
 namespace {
 constexpr int TC_MAX_DEV = 64;
@@ -815,10 +831,12 @@ int* g_tc_err_addr[TC_MAX_DEV] = {};
 bool g_tc_attr[TC_MAX_DEV] = {};
 std::atomic<int> g_engine{GEMM_ENGINE_TCGEN05};
 std::atomic<bool> g_pk_enabled{true};  // packed-operand path of tc_gemm_c64
-// wide-tile packed path (QBG_GEMM_WIDE=0 in the environment keeps the 128 x 32 tiles)
-std::atomic<bool> g_pkw_enabled{[] {
+// wide-tile packed path: QBG_GEMM_WIDE in the environment, 0 keeps the
+// 128 x 32 tiles, 1 one wide CTA per SM (48 KB stages), 2 (default) two per
+// SM (24 KB stages; C2 factor phase 28.1 -> 26.7 ms against 1)
+std::atomic<int> g_pkw_mode{[] {
   const char* e = std::getenv("QBG_GEMM_WIDE");
-  return !(e && *e == '0');
+  return (e && *e) ? std::max(0, std::min(std::atoi(e), 2)) : 2;
 }()};
 
 int tc_device_setup(int** err_out) {
@@ -832,7 +850,10 @@ int tc_device_setup(int** err_out) {
   if (!g_tc_attr[dev]) {
     QBG_CUDA(cudaFuncSetAttribute(k_tc_cgemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes()));
     QBG_CUDA(cudaFuncSetAttribute(k_tc_cgemm_pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pk_smem_bytes()));
-    QBG_CUDA(cudaFuncSetAttribute(k_tc_cgemm_pkw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pw_smem_bytes()));
+    QBG_CUDA(cudaFuncSetAttribute(k_tc_cgemm_pkw<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)pw_smem_bytes<2>()));
+    QBG_CUDA(cudaFuncSetAttribute(k_tc_cgemm_pkw<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)pw_smem_bytes<1>()));
     void* a = nullptr;
     QBG_CUDA(cudaGetSymbolAddress(&a, g_tc_err));
     g_tc_err_addr[dev] = static_cast<int*>(a);
@@ -918,22 +939,27 @@ int tc_gemm_c64(int M, int N, int K, cxf alpha, const cxf* A, long long lda, lon
   // products, N = 64, and the updates inside an outer block are faster staged)
   // wide tiles (128 x 128 complex) for the large products: N of at least two
   // wide tiles and enough tiles to fill the device
-  const int NTW = (N + PW_BN - 1) / PW_BN, KTW = (K + PW_BK - 1) / PW_BK;
-  if (allow_packed && g_pk_enabled.load() && g_pkw_enabled.load() && KTW >= 4 && NTW >= 2 &&
-      (long long)MT * NTW * nb >= 152) {
-    const size_t pa = (size_t)nb * MT * KTW * PW_A_TILE, pb = (size_t)nb * NTW * KTW * PW_B_TILE;
-    void* scr = nullptr;
-    QBG_TRY(pack_scratch(st, sizeof(float) * (pa + pb), &scr));
-    float* PA = static_cast<float*>(scr);
-    float* PB = PA + pa;
-    k_tc_pack_aw<<<dim3(MT, KTW, nb), 128, 0, st>>>(A, lda, sA, sA2, batch2, M, K, PA);
-    QBG_LAUNCH_CHECK("k_tc_pack_aw");
-    k_tc_pack_bw<<<dim3(NTW, KTW, nb), 128, 0, st>>>(B, ldb, sB, sB2, batch2, N, K, PB);
-    QBG_LAUNCH_CHECK("k_tc_pack_bw");
-    k_tc_cgemm_pkw<<<dim3(MT, NTW, nb), 128, pw_smem_bytes(), st>>>(M, N, KTW, alpha, PA, PB, beta, C, ldc, sC,
-                                                                     batch2, sC2, derr);
-    QBG_LAUNCH_CHECK("k_tc_cgemm_pkw");
-    return QBG_OK;
+  const int wide = g_pkw_mode.load();  // 0 off, 1 one CTA per SM (KS = 2), 2 two CTAs per SM (KS = 1)
+  const int NTW = (N + PW_BN - 1) / PW_BN, KTW8 = (K + 7) / 8;
+  if (allow_packed && g_pk_enabled.load() && wide > 0 && KTW8 >= 4 && NTW >= 2 && (long long)MT * NTW * nb >= 152) {
+    auto run = [&](auto ks) -> int {
+      constexpr int KS = decltype(ks)::value;
+      const int KTW = (K + PW<KS>::BK - 1) / PW<KS>::BK;
+      const size_t pa = (size_t)nb * MT * KTW * PW<KS>::A_TILE, pb = (size_t)nb * NTW * KTW * PW<KS>::B_TILE;
+      void* scr = nullptr;
+      QBG_TRY(pack_scratch(st, sizeof(float) * (pa + pb), &scr));
+      float* PA = static_cast<float*>(scr);
+      float* PB = PA + pa;
+      k_tc_pack_aw<KS><<<dim3(MT, KTW, nb), 128, 0, st>>>(A, lda, sA, sA2, batch2, M, K, PA);
+      QBG_LAUNCH_CHECK("k_tc_pack_aw");
+      k_tc_pack_bw<KS><<<dim3(NTW, KTW, nb), 128, 0, st>>>(B, ldb, sB, sB2, batch2, N, K, PB);
+      QBG_LAUNCH_CHECK("k_tc_pack_bw");
+      k_tc_cgemm_pkw<KS><<<dim3(MT, NTW, nb), 128, pw_smem_bytes<KS>(), st>>>(M, N, KTW, alpha, PA, PB, beta, C,
+                                                                               ldc, sC, batch2, sC2, derr);
+      QBG_LAUNCH_CHECK("k_tc_cgemm_pkw");
+      return QBG_OK;
+    };
+    return wide == 2 ? run(std::integral_constant<int, 1>{}) : run(std::integral_constant<int, 2>{});
   }
   if (allow_packed && g_pk_enabled.load() && KT >= 2 && MT >= 4 && NT >= 8) {
     const size_t pa = (size_t)nb * MT * KT * PK_A_TILE, pb = (size_t)nb * NT * KT * PK_B_TILE;
