@@ -938,10 +938,14 @@ int tc_gemm_c64(int M, int N, int K, cxf alpha, const cxf* A, long long lda, lon
   // N = 2048: faster from the 512 x 512 trailing updates up; the skinny solve
   // products, N = 64, and the updates inside an outer block are faster staged)
   // wide tiles (128 x 128 complex) for the large products: N of at least two
-  // wide tiles and enough tiles to fill the device
+  // wide tiles and enough tiles to fill the device, or one mostly full wide
+  // tile (the triangular-solve products of a 128-column block) and half as
+  // many tiles (the other stream parts' products fill the rest; C2 solve
+  // phase 33.7 -> 29.0 ms)
   const int wide = g_pkw_mode.load();  // 0 off, 1 one CTA per SM (KS = 2), 2 two CTAs per SM (KS = 1)
   const int NTW = (N + PW_BN - 1) / PW_BN, KTW8 = (K + 7) / 8;
-  if (allow_packed && g_pk_enabled.load() && wide > 0 && KTW8 >= 4 && NTW >= 2 && (long long)MT * NTW * nb >= 152) {
+  if (allow_packed && g_pk_enabled.load() && wide > 0 && KTW8 >= 4 && (NTW >= 2 || N >= 96) &&
+      (long long)MT * NTW * nb >= (NTW >= 2 ? 152 : 64)) {
     auto run = [&](auto ks) -> int {
       constexpr int KS = decltype(ks)::value;
       const int KTW = (K + PW<KS>::BK - 1) / PW<KS>::BK;

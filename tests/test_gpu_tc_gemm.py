@@ -1,7 +1,7 @@
 """Complex64 GEMM engines of the FP32 LU: tcgen05 tensor cores (3xTF32) with
 packed operand tiles streamed by bulk copies for large products (engine 1:
 128 x 128 complex tiles, real N = 256 per MMA, when N spans two such tiles and
-the grid fills the device, else 128 x 32) or
+the grid fills the device or N fills most of one tile, else 128 x 32) or
 with operands split in registers (engine 2), and CUDA-core FMA tiles (engine
 0), against a complex128 NumPy product of the same inputs.
 
@@ -32,6 +32,8 @@ SHAPES = [
     (640, 1, 96, 1),     # one column
     (1000, 1100, 77, 3), # wide 128 x 128 tiles: ragged M, N and K
     (129, 257, 33, 60),  # wide tiles, one row and one column past a tile, many matrices
+    (1792, 128, 256, 6), # one wide tile in N: a triangular-solve product of a 128-column block
+    (1000, 100, 64, 8),  # one mostly full wide tile, ragged M and N
 ]
 
 
