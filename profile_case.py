@@ -139,6 +139,9 @@ def main(argv=None):
     ap.add_argument("--L", type=int, default=64)
     ap.add_argument("--form", default="mixed", choices=["fp64", "mixed", "fp32"])
     ap.add_argument("--direct", action="store_true", help="direct Hankel evaluation instead of Chebyshev panels")
+    ap.add_argument("--cheb-tol", type=float, default=0.0,
+                    help="beyn / assemble: panels by chebyshev_params_min_cost at this tolerance (the bench's "
+                         "1e-13) instead of the reference's defaults")
     ap.add_argument("--dk", type=float, default=0.05, help="ebim: window half-width")
     ap.add_argument("--nev", type=int, default=5, help="ebim: eigenvalues of the block iteration")
     ap.add_argument("--full", action="store_true", help="ebim: solve_full! convention (every root in the box)")
@@ -159,6 +162,11 @@ def main(argv=None):
         return large_case(qb, a)
     b, sol, pts = star_case(qb, a.n)
     ws = qb.Workspace(sol, pts)
+    cheb = None
+    if a.cheb_tol > 0 and a.case in ("beyn", "assemble"):
+        zref = 200.0 + 0.5 * np.exp(2j * math.pi * np.arange(a.nq) / a.nq)
+        cheb = tuple(int(x) for x in qb.chebyshev_params_min_cost(sol, pts, zref, ws=ws, tol=a.cheb_tol)[:4])
+        print("panels", cheb)
     t0 = time.perf_counter()
     if a.case == "ebim":
         k_ebim, reps = 200.0, 3
@@ -176,11 +184,12 @@ def main(argv=None):
                   "tens", np.round(tens, 6).tolist(), info, "ms %.1f" % ((time.perf_counter() - t1) * 1e3), flush=True)
     elif a.case == "beyn":
         lam, info = qb.solve(sol, pts, 200.0 + 0j, 0.5, nq=a.nq, r=a.L, svd_tol=1e-12, rng=np.random.default_rng(1),
-                             mixed=a.form, ws=ws, return_info=True, use_chebyshev=not a.direct)
+                             mixed=a.form, ws=ws, return_info=True, use_chebyshev=not a.direct, cheb=cheb)
         print("beyn", a.form, "eigenvalues", len(lam), "stats", info["stats"][0])
     else:
         zj = 200.0 + 0.5 * np.exp(2j * math.pi * np.arange(a.nq) / a.nq)
-        out = qb.assemble(ws, zj, mixed=a.form, cheb=None if a.direct else True)
+        out = qb.assemble(ws, zj, mixed=a.form, cheb=None if a.direct else (cheb if cheb else True),
+                          split_lo=a.form == "mixed")
         print("assembled", len(out), out[0].shape)
     print("wall ms", (time.perf_counter() - t0) * 1e3)
 
