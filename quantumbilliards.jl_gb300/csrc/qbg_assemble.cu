@@ -1428,6 +1428,379 @@ __global__ void __launch_bounds__(512) k_assemble_cheb_sym_df(GeomDev g, ChebTab
   }
 }
 
+// ---------------------------------------------------------------------------
+// J/E tables and the sorted-tile double-float assembly of full operators.
+//
+// With z = k r, l = (2/pi) ln r and the ascending series of A&S 9.1.11 and
+// 9.1.13, Y0 = (2/pi)(ln(z/2) + gamma) J0 + ..., Y1 = -2/(pi z) +
+// (2/pi)(ln(z/2) + gamma) J1 + ..., the functions
+//   G0 = Y0 - l J0 = (2/pi) [(ln(k/2) + gamma) J0 - s0],
+//   G1 = Y1 - l J1 + 2/(pi z) = (2/pi)(ln(k/2) + gamma) J1 - s1 / pi
+// (s0 = sum H_m t0_m, s1 = sum (H_m + H_{m+1}) t1_m over the series terms)
+// are entire in r: the logarithm and the pole of the Hankel functions are
+// exact per-pair factors, ln r and 1/r, while the panels only resolve the
+// oscillation e^{+-ikr}. One table on the J grid of [0, rmax] therefore
+// replaces the H table on [rmin, rmax], whose panels also had to resolve
+// 1/r near rmin (7695 against 863 J panels at N = 2048, k = 200, 1e-13),
+// and one Chebyshev recurrence per pair serves all four series.
+// ---------------------------------------------------------------------------
+// J0, J1, G0, G1 at r for the node k; lkg = ln(k/2) + gamma
+static __device__ void je_values(cxd k, cxd lkg, double r, cxd& j0, cxd& j1, cxd& g0, cxd& g1) {
+  const double inv_pi = 0.31830988618379067154, two_over_pi = 0.63661977236758134308;
+  if (r == 0.0) {
+    j0 = cxd(1.0, 0.0);
+    j1 = cxd(0.0, 0.0);
+    g0 = two_over_pi * lkg;
+    g1 = cxd(0.0, 0.0);
+    return;
+  }
+  const cxd z = r * k;
+  if (cabs_d(z) < 4.0) {
+    // terms t0_m = (-z^2/4)^m / (m!)^2, t1_m = (z/2)(-z^2/4)^m / (m!(m+1)!); at
+    // |z| < 4 the largest term is below 5, so the sums lose no digits
+    const cxd h = 0.5 * z, q = -(h * h);
+    cxd t0(1.0, 0.0), t1 = h, a0(0.0, 0.0), a1(0.0, 0.0), s0(0.0, 0.0), s1(0.0, 0.0);
+    double hm = 0.0;  // harmonic number H_m
+    for (int m = 0; m < 48; ++m) {
+      if (m > 0) {
+        t0 = t0 * q * (1.0 / ((double)m * m));
+        t1 = t1 * q * (1.0 / ((double)m * (m + 1)));
+        hm += 1.0 / m;
+      }
+      a0 += t0;
+      a1 += t1;
+      s0 += hm * t0;
+      s1 += (2.0 * hm + 1.0 / (m + 1)) * t1;
+      if (cabs_d(t0) < 1e-18 && cabs_d(t1) < 1e-18) break;
+    }
+    j0 = a0;
+    j1 = a1;
+    g0 = two_over_pi * (lkg * a0 - s0);
+    g1 = two_over_pi * (lkg * a1) - inv_pi * s1;
+  } else {
+    const Bessel01d b = bessel01(z);
+    const double l = two_over_pi * log(r);
+    j0 = b.j0;
+    j1 = b.j1;
+    g0 = b.y0 - l * b.j0;
+    g1 = b.y1 - l * b.j1 + two_over_pi * cinv(z);
+  }
+}
+
+// one thread per (panel, node): the values at the M + 1 Chebyshev-Lobatto
+// points of the panel, their DCT-I (as k_cheb_build) and the double-float split
+template <int NS>
+__global__ void k_cheb_build_je(ChebTables t, const cxd* __restrict__ ks) {
+  constexpr int MMAX = QBG_CHEB_MAX_DEGREE;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int q = blockIdx.y;
+  if (p >= t.nje) return;
+  const int M = t.Mje;
+  const double a = (double)p * t.dr_je;
+  const double b = (p + 1 == t.nje) ? t.rmax : (double)(p + 1) * t.dr_je;
+  const cxd k = ks[q];
+  const bool realk = (k.im == 0.0);
+  const cxd kaL2 = 0.5 * cmul_i(k), kd = -0.5 * k;
+  const cxd lkg = clog_d(0.5 * k) + cxd(0.57721566490153286061, 0.0);
+  cxd f[MMAX + 1][NS];
+  for (int jn = 0; jn <= M; ++jn) {
+    const double tn = cospi((double)jn / (double)M);
+    const double r = 0.5 * ((b + a) + (b - a) * tn);
+    cxd j0, j1, g0, g1;
+    je_values(k, lkg, r, j0, j1, g0, g1);
+    if (realk) { j0.im = 0.0; j1.im = 0.0; g0.im = 0.0; g1.im = 0.0; }
+    f[jn][0] = kaL2 * j1;
+    f[jn][1] = kaL2 * (j1 + cmul_i(g1));
+    if (NS == 4) {
+      f[jn][2] = kd * j0;
+      f[jn][3] = kd * (j0 + cmul_i(g0));
+    }
+  }
+  float4* out = t.JE + ((size_t)q * t.nje + p) * (size_t)(M + 1) * NS;
+  for (int m = 0; m <= M; ++m) {
+    const double sg = (m & 1) ? -1.0 : 1.0;
+    double sc = 2.0 / (double)M;
+    if (m == 0) sc *= 0.5;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      cxd acc = 0.5 * f[0][s] + (0.5 * sg) * f[M][s];
+      for (int jn = 1; jn < M; ++jn) acc += cospi((double)(jn * m) / (double)M) * f[jn][s];
+      acc = sc * acc;
+      const dfl re = df_of(acc.re), im = df_of(acc.im);
+      out[m * NS + s] = make_float4(re.hi, re.lo, im.hi, im.lo);
+    }
+  }
+}
+
+namespace {
+// pair coefficients of one entry on the J/E series (negated as stored):
+//   entry.re = b U.re + a P.im + d W.re + c R.im + kk
+//   entry.im = b U.im - a P.re + d W.im - c R.re
+// with b = -B, a = A/pi + B l, d = -D, c = C/pi + D l, kk = -B/(pi r)
+struct JeCoef {
+  dfl b, a, d, c, kk;
+};
+
+template <int FORM>
+__device__ __forceinline__ JeCoef je_coef(const Fold& f, double l, double invr) {
+  const double inv_pi = 0.31830988618379067154;
+  JeCoef e;
+  e.b = df_of(-f.B);
+  e.a = df_of(f.A * inv_pi + f.B * l);
+  e.kk = df_of(-f.B * inv_pi * invr);
+  if (FORM == 1) {
+    e.d = df_of(-f.D);
+    e.c = df_of(f.C * inv_pi + f.D * l);
+  } else {
+    e.d = dfl{0.f, 0.f};
+    e.c = dfl{0.f, 0.f};
+  }
+  return e;
+}
+
+// shared-memory layout of the two entries' coefficients of a slot: NC float4
+// rows of 1024 slots, {b, a} (ij), {b, a} (ji), {kk_ij, kk_ji}, then for the
+// CFIE {d, c} (ij), {d, c} (ji)
+template <int FORM>
+__host__ __device__ constexpr int je_coef_words() {
+  return FORM == 1 ? 5 : 3;
+}
+
+template <int FORM>
+__device__ __forceinline__ void je_coef_store(float4* sm, int slot, const JeCoef& x, const JeCoef& y) {
+  sm[0 * 1024 + slot] = make_float4(x.b.hi, x.b.lo, x.a.hi, x.a.lo);
+  sm[1 * 1024 + slot] = make_float4(y.b.hi, y.b.lo, y.a.hi, y.a.lo);
+  sm[2 * 1024 + slot] = make_float4(x.kk.hi, x.kk.lo, y.kk.hi, y.kk.lo);
+  if (FORM == 1) {
+    sm[3 * 1024 + slot] = make_float4(x.d.hi, x.d.lo, x.c.hi, x.c.lo);
+    sm[4 * 1024 + slot] = make_float4(y.d.hi, y.d.lo, y.c.hi, y.c.lo);
+  }
+}
+
+template <int FORM>
+__device__ __forceinline__ void je_coef_load(const float4* sm, int slot, JeCoef& x, JeCoef& y) {
+  float4 u = sm[0 * 1024 + slot];
+  x.b = dfl{u.x, u.y};
+  x.a = dfl{u.z, u.w};
+  u = sm[1 * 1024 + slot];
+  y.b = dfl{u.x, u.y};
+  y.a = dfl{u.z, u.w};
+  u = sm[2 * 1024 + slot];
+  x.kk = dfl{u.x, u.y};
+  y.kk = dfl{u.z, u.w};
+  if (FORM == 1) {
+    u = sm[3 * 1024 + slot];
+    x.d = dfl{u.x, u.y};
+    x.c = dfl{u.z, u.w};
+    u = sm[4 * 1024 + slot];
+    y.d = dfl{u.x, u.y};
+    y.c = dfl{u.z, u.w};
+  } else {
+    x.d = x.c = y.d = y.c = dfl{0.f, 0.f};
+  }
+}
+
+template <int FORM>
+__device__ __forceinline__ float4 je_fold(const JeCoef& e, const dfl* v) {
+  // v: P.re, P.im, U.re, U.im, R.re, R.im, W.re, W.im
+  dfl re = e.kk, im{0.f, 0.f};
+  const dfl na{-e.a.hi, -e.a.lo};
+  df_acc(re, e.b, v[2]);
+  df_acc(re, e.a, v[1]);
+  df_acc(im, e.b, v[3]);
+  df_acc(im, na, v[0]);
+  if (FORM == 1) {
+    const dfl nc{-e.c.hi, -e.c.lo};
+    df_acc(re, e.d, v[6]);
+    df_acc(re, e.c, v[5]);
+    df_acc(im, e.d, v[7]);
+    df_acc(im, nc, v[4]);
+  }
+  re = df_norm(re);
+  im = df_norm(im);
+  return make_float4(re.hi, im.hi, re.lo, im.lo);
+}
+
+// the FP64 routes of the J/E kernel, out of line so that their registers do
+// not weigh on the series loop: the diagonal, and coincident nodes of different
+// components (r below every table radius; the CFIE's vanish before this)
+template <int FORM>
+__device__ __noinline__ float4 je_diag(const GeomDev& g, int i, cxd k) {
+  return pack_split(diag_fp64<FORM>(g, i, k));
+}
+
+template <int FORM>
+__device__ __noinline__ void je_direct_pair(const GeomDev& g, int i, int j, cxd k, float4* vij, float4* vji) {
+  const PairGeom pa = pair_geom(g, i, j);
+  const PairGeom pb = pair_geom(g, j, i);
+  const double inv2pi = 0.15915494309189533577;
+  const cxd kaL1 = (-inv2pi) * k, kaL2 = 0.5 * cmul_i(k), kg = (-inv2pi) * cmul_i(k), kd = -0.5 * k;
+  const Bessel01d bz = bessel01(pa.r * k);
+  *vij = pack_split(folded_entry(fold_of<FORM>(pa), kaL1, kaL2, kg, kd, bz.h0(), bz.h1(), bz.j0, bz.j1));
+  *vji = pack_split(folded_entry(fold_of<FORM>(pb), kaL1, kaL2, kg, kd, bz.h0(), bz.h1(), bz.j0, bz.j1));
+}
+
+// sum_m c_m T_m(t) of the NS complex series of one table row
+template <int NS>
+__device__ __forceinline__ void je_series(const float4* __restrict__ c, int M, dfl t, dfl* v) {
+#pragma unroll
+  for (int s = 0; s < 2 * NS; ++s) v[s] = dfl{0.f, 0.f};
+  dfl tp{1.f, 0.f}, tc = t;
+  const dfl t2{2.f * t.hi, 2.f * t.lo};
+#pragma unroll 2
+  for (int m = 0; m <= M; ++m) {
+    dfl tm;
+    if (m == 0) {
+      tm = tp;
+    } else if (m == 1) {
+      tm = tc;
+    } else {
+      tm = df_sub(df_mul(t2, tc), tp);
+      tp = tc;
+      tc = tm;
+    }
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      const float4 cc = __ldg(c + m * NS + s);
+      df_acc(v[2 * s], dfl{cc.x, cc.y}, tm);
+      df_acc(v[2 * s + 1], dfl{cc.z, cc.w}, tm);
+    }
+  }
+}
+}  // namespace
+
+// Full symmetric operator on the J/E tables, every node of ks in one pass.
+// CTA = one 32 x 32 tile pair (bi <= bj) as k_assemble_cheb_sym_df, but the
+// tile's pairs are sorted by table panel before the node loop (bitonic sort of
+// 1024 keys in shared memory), so the 32 pairs of a warp read a few table rows
+// instead of 32 (the row loads were the bound of the per-pair order: 23
+// sectors per request, half the issue slots lost to long-scoreboard stalls).
+// Both mirrored entries of a pair are staged in shared memory per node and
+// written as coalesced columns.
+template <int FORM>
+__global__ void __launch_bounds__(512) k_assemble_je_df(GeomDev g, ChebTables t, const cxd* __restrict__ ks, int nk,
+                                                        void* const* __restrict__ outs, void* const* __restrict__ los,
+                                                        long long ld) {
+  constexpr int NS = FORM == 1 ? 4 : 2;
+  constexpr int NC = je_coef_words<FORM>();
+  __shared__ float4 tA[32][33];  // entries (i, j): [j - 32 bj][i - 32 bi]; the whole tile when bi == bj
+  __shared__ float4 tB[32][33];  // entries (j, i): [i - 32 bi][j - 32 bj]
+  __shared__ unsigned keys[1024];
+  extern __shared__ float4 coef[];  // [NC][1024]: the pair coefficients of every sorted slot
+  const int2 bp = tile_pair(blockIdx.x);
+  const int bi = bp.x, bj = bp.y;
+  const bool dtile = (bi == bj);
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  const unsigned NOPANEL = (1u << 22) - 1;
+  // keys: panel << 10 | pair index e = il + 32 jl; inactive pairs last
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int e = tid + 512 * h;
+    const int i = bi * 32 + (e & 31), j = bj * 32 + (e >> 5);
+    unsigned pk = NOPANEL;
+    if (i < g.n && j < g.n && i != j && (!dtile || i < j)) {
+      const double r = hypot(g.x[i] - g.x[j], g.y[i] - g.y[j]);
+      int qp = (int)floor(r * t.invdr_je);
+      qp = qp < 0 ? 0 : (qp >= t.nje ? t.nje - 1 : qp);
+      pk = (unsigned)qp;
+    }
+    keys[e] = (pk << 10) | (unsigned)e;
+  }
+  __syncthreads();
+  for (int kk = 2; kk <= 1024; kk <<= 1) {
+    for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+      const int lo = 2 * tid - (tid & (jj - 1)), hi = lo + jj;
+      const bool up = (lo & kk) == 0;
+      const unsigned x = keys[lo], y = keys[hi];
+      if ((x > y) == up) {
+        keys[lo] = y;
+        keys[hi] = x;
+      }
+      __syncthreads();
+    }
+  }
+  // per slot (sorted positions tid and tid + 512): indices, panel, argument;
+  // the coefficients go to shared memory (registers would spill)
+  int pe[2], ppan[2];
+  bool act[2], zero[2], direct[2];
+  dfl tt[2];
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    const unsigned key = keys[tid + 512 * s];
+    const int e = (int)(key & 1023u);
+    pe[s] = e;
+    act[s] = (key >> 10) != NOPANEL;
+    zero[s] = false;
+    direct[s] = false;
+    ppan[s] = 0;
+    double td = 0.0;
+    Fold fij{0.0, 0.0, 0.0, 0.0}, fji{0.0, 0.0, 0.0, 0.0};
+    double l = 0.0, invr = 0.0;
+    if (act[s]) {
+      const int i = bi * 32 + (e & 31), j = bj * 32 + (e >> 5);
+      const PairGeom pa = pair_geom(g, i, j);
+      const PairGeom pb = pair_geom(g, j, i);
+      fij = fold_of<FORM>(pa);
+      fji = fold_of<FORM>(pb);
+      zero[s] = (FORM == 1 && !pa.same && pa.r * pa.r <= 4.93038065763132e-32);
+      direct[s] = !zero[s] && pa.r < t.rmin;
+      panel_of(pa.r, 0.0, t.rmax, t.dr_je, t.invdr_je, t.nje, ppan[s], td);
+      l = 0.63661977236758134308 * log(pa.r);
+      invr = pa.invr;
+    }
+    tt[s] = df_of(td);
+    je_coef_store<FORM>(coef, tid + 512 * s, je_coef<FORM>(fij, l, invr), je_coef<FORM>(fji, l, invr));
+  }
+  const int Mt = t.Mje;
+  for (int q = 0; q < nk; ++q) {
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      if (!act[s]) continue;
+      const int il = pe[s] & 31, jl = pe[s] >> 5;
+      float4 vij = make_float4(0.f, 0.f, 0.f, 0.f), vji = vij;
+      if (zero[s]) {
+        // both entries vanish
+      } else if (direct[s]) {
+        je_direct_pair<FORM>(g, bi * 32 + il, bj * 32 + jl, ks[q], &vij, &vji);
+      } else {
+        dfl v[8];
+        je_series<NS>(t.JE + ((size_t)q * t.nje + ppan[s]) * (size_t)(Mt + 1) * NS, Mt, tt[s], v);
+        JeCoef cij, cji;
+        je_coef_load<FORM>(coef, tid + 512 * s, cij, cji);
+        vij = je_fold<FORM>(cij, v);
+        vji = je_fold<FORM>(cji, v);
+      }
+      tA[jl][il] = vij;
+      if (dtile) tA[il][jl] = vji;
+      else tB[il][jl] = vji;
+    }
+    if (dtile && tid < 32 && bi * 32 + tid < g.n) tA[tid][tid] = je_diag<FORM>(g, bi * 32 + tid, ks[q]);
+    __syncthreads();
+    const int row = threadIdx.x;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int c = threadIdx.y + 16 * h;
+      const int i = bi * 32 + row, j = bj * 32 + c;  // tile A: row i, column j
+      if (i < g.n && j < g.n) {
+        const float4 v = tA[c][row];
+        const size_t off = (size_t)i + (size_t)j * ld;
+        reinterpret_cast<cxf*>(outs[q])[off] = cxf(v.x, v.y);
+        if (los) reinterpret_cast<cxf*>(los[q])[off] = cxf(v.z, v.w);
+      }
+      if (!dtile) {
+        const int jr = bj * 32 + row, ic = bi * 32 + c;  // tile B: row j, column i
+        if (jr < g.n && ic < g.n) {
+          const float4 v = tB[c][row];
+          const size_t off = (size_t)jr + (size_t)ic * ld;
+          reinterpret_cast<cxf*>(outs[q])[off] = cxf(v.x, v.y);
+          if (los) reinterpret_cast<cxf*>(los[q])[off] = cxf(v.z, v.w);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // Symmetry-reduced DLP (value, complex64 forms) on double-float arithmetic:
 // one thread per reduced entry (a, b), every node of ks in one pass. Per
 // entry the FP64 geometry, the fold coefficients of the main pair, and for
@@ -1567,6 +1940,27 @@ __global__ void __launch_bounds__(256, 1) k_assemble_cheb_reduced_df(GeomDev g, 
     reinterpret_cast<cxf*>(outs[q])[off] = cxf(v.x, v.y);
     if (los) reinterpret_cast<cxf*>(los[q])[off] = cxf(v.z, v.w);
   }
+}
+
+bool cheb_je_applies(const GeomDev& g, int deriv, int prec) {
+  return prec == QBG_PREC_MIXED && !deriv && g.m == g.n && g.quad != 1;
+}
+
+size_t cheb_je_bytes(const ChebTables& t) {
+  return sizeof(float4) * (size_t)t.nse * t.nk * t.nje * (size_t)(t.Mje + 1);
+}
+
+int cheb_je_build(ChebTables& t, const cxd* ks, cudaStream_t st) {
+  if (!t.JE || t.nje < 1 || t.nje >= (1 << 21) || t.Mje < 1 || t.Mje > QBG_CHEB_MAX_DEGREE ||
+      (t.nse != 2 && t.nse != 4)) {
+    set_error("cheb_je_build: invalid table parameters");
+    return QBG_EINVAL;
+  }
+  dim3 grd((t.nje + 63) / 64, t.nk);
+  if (t.nse == 4) k_cheb_build_je<4><<<grd, 64, 0, st>>>(t, ks);
+  else k_cheb_build_je<2><<<grd, 64, 0, st>>>(t, ks);
+  QBG_LAUNCH_CHECK("k_cheb_build_je");
+  return QBG_OK;
 }
 
 bool cheb_df_applies(const GeomDev& g, int deriv) {
@@ -1718,6 +2112,16 @@ int launch_assemble_cheb(const GeomDev& g, const ChebTables& t, const cxd* ks, i
         k_assemble_cheb_sym<0, 0><<<sgrd, sblk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
       else
         k_assemble_cheb_sym<1, 0><<<sgrd, sblk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
+    } else if (t.JE && prec == QBG_PREC_MIXED) {
+      dim3 dgrd((unsigned)(nt * (nt + 1) / 2), 1, 1);
+      const size_t dyn = sizeof(float4) * 1024 * (g.form == 0 ? je_coef_words<0>() : je_coef_words<1>());
+      if (g.form == 0) {
+        QBG_CUDA(cudaFuncSetAttribute(k_assemble_je_df<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+        k_assemble_je_df<0><<<dgrd, sblk, dyn, st>>>(g, t, ks, nk, outs_dev, lo_outs_dev, ld);
+      } else {
+        QBG_CUDA(cudaFuncSetAttribute(k_assemble_je_df<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+        k_assemble_je_df<1><<<dgrd, sblk, dyn, st>>>(g, t, ks, nk, outs_dev, lo_outs_dev, ld);
+      }
     } else if (t.HD && t.JD && t.nkc) {
       dim3 dgrd((unsigned)(nt * (nt + 1) / 2), 1, 1);
       // the degree stays a runtime value here: with 512 threads and the

@@ -31,6 +31,16 @@ struct ChebTables {
   float4* HD = nullptr;
   float4* JD = nullptr;
   NodeConst* nkc = nullptr;
+  // J/E form for the double-float assembly of full operators (k_cheb_build_je):
+  // on nje uniform panels of [0, rmax], degree Mje, per (node, panel, degree)
+  // nse float4 (re.hi, re.lo, im.hi, im.lo) = {P, U, R, W} (DLP: {P, U}) with
+  //   P = kaL2 J1,  U = kaL2 (J1 + i G1),  R = kd J0,  W = kd (J0 + i G0),
+  //   G0 = Y0 - l J0,  G1 = Y1 - l J1 + 2/(pi k r),  l = (2/pi) ln r,
+  // all entire in r, so that kaL2 H1 = U + i l P + 1/(pi r), kd H0 = W + i l R,
+  // kaL1 J1 = (i/pi) P and kg J0 = (i/pi) R
+  float4* JE = nullptr;
+  int nje = 0, Mje = 0, nse = 0;
+  double dr_je = 0, invdr_je = 0;
 };
 // min / max pair distance over all off-diagonal pairs (host values; dscratch2 = 2 device words)
 int cheb_r_range(const GeomDev& g, unsigned long long* dscratch2, double* rmin, double* rmax, cudaStream_t st);
@@ -39,6 +49,11 @@ int cheb_build(ChebTables& t, const cxd* ks, cudaStream_t st);
 // sizes cheb_df_bytes reports, owned by the caller); after cheb_build
 void cheb_df_bytes(const ChebTables& t, size_t* hd, size_t* jd, size_t* nkc);
 int cheb_df_tables(ChebTables& t, const cxd* ks, cudaStream_t st);
+// the J/E tables of the mixed form's full symmetric assembly: whether they
+// apply, their bytes (t.nk, nje, Mje, nse set), and their build (t.JE set)
+bool cheb_je_applies(const GeomDev& g, int deriv, int prec);
+size_t cheb_je_bytes(const ChebTables& t);
+int cheb_je_build(ChebTables& t, const cxd* ks, cudaStream_t st);
 // whether the complex64 Chebyshev assembly of g runs on double-float tables
 // (symmetric full operators; the reduced DLP with orbits of at most 4 nodes)
 bool cheb_df_applies(const GeomDev& g, int deriv);

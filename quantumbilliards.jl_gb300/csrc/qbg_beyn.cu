@@ -214,8 +214,13 @@ int load(qbg_beyn* b, int n0, int c) {
     QBG_TRY(cheb_params_check(&cp));
     std::vector<void*> ctmp;
     ChebTables t;
-    int s = make_cheb(b->g, b->zj + n0, c, cp, t, ctmp, st);
-    if (!s && b->prec != QBG_PREC_FP64 && cheb_df_applies(b->g->d, 0)) s = make_cheb_df(t, b->zj + n0, ctmp, st);
+    int s = QBG_OK;
+    if (cheb_je_applies(b->g->d, 0, b->prec)) {
+      s = make_cheb_je(b->g, b->zj + n0, c, cp, t, ctmp, st);
+    } else {
+      s = make_cheb(b->g, b->zj + n0, c, cp, t, ctmp, st);
+      if (!s && b->prec != QBG_PREC_FP64 && cheb_df_applies(b->g->d, 0)) s = make_cheb_df(t, b->zj + n0, ctmp, st);
+    }
     if (!s) s = launch_assemble_cheb(b->g->d, t, b->zj + n0, c, 0, b->prec, b->dptrs, b->dlo, n, st);
     if (!s) {
       cudaEventRecord(b->ev[1], st);

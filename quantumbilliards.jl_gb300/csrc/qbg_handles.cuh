@@ -61,4 +61,7 @@ int make_cheb(qbg_geom* g, const cxd* dks, int nk, const qbg_cheb_params& prm, C
               std::vector<void*>& tmp, cudaStream_t st);
 // double-float tables of t for the complex64 forms (after make_cheb; buffers appended to tmp)
 int make_cheb_df(ChebTables& t, const cxd* dks, std::vector<void*>& tmp, cudaStream_t st);
+// the J/E tables alone (instead of make_cheb + make_cheb_df) where cheb_je_applies
+int make_cheb_je(qbg_geom* g, const cxd* dks, int nk, const qbg_cheb_params& prm, ChebTables& t,
+                 std::vector<void*>& tmp, cudaStream_t st);
 }  // namespace qbg

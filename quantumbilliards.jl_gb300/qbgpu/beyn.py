@@ -206,18 +206,53 @@ def _lapacke():
     return _LAPACKE or None
 
 
-def _svd_lapacke(z, A):
-    """Thin SVD U, S, W^H of A through LAPACKE's zgesdd (jobz 'S'), as numpy.linalg.svd."""
+def _svd_lapacke(z, A, vals_only=False):
+    """Thin SVD U, S, W^H of A through LAPACKE's zgesdd (jobz 'S'), as
+    numpy.linalg.svd; vals_only: S alone (jobz 'N')."""
     A = np.array(A, dtype=np.complex128, order="F", copy=True)
     m, n = A.shape
     k = min(m, n)
     S = np.empty(k, np.float64)
+    if vals_only:
+        d = np.empty(1, np.complex128)
+        info = z["zgesdd"](102, b"N", m, n, A.ctypes.data, m, S.ctypes.data, d.ctypes.data, 1, d.ctypes.data, 1)
+        if info != 0:
+            raise np.linalg.LinAlgError(f"zgesdd info {info}")
+        return S
     U = np.empty((m, k), np.complex128, order="F")
     Vh = np.empty((k, n), np.complex128, order="F")
     info = z["zgesdd"](102, b"S", m, n, A.ctypes.data, m, S.ctypes.data, U.ctypes.data, m, Vh.ctypes.data, k)
     if info != 0:
         raise np.linalg.LinAlgError(f"zgesdd info {info}")
     return U, S, Vh
+
+
+def _one_thread(fn):
+    """fn(lapacke) with the BLAS at one thread, or fn(None) without LAPACKE.
+    The moments' SVDs and eig(B) are dense problems of at most a few hundred
+    rows, which the threaded BLAS runs slower than one thread does (zgeev of a
+    128 x 128 matrix: 13 ms at one thread against 16 ms at eight)."""
+    z = _lapacke()
+    if z is None:
+        return fn(None)
+    n0 = int(z["get_threads"]())
+    z["set_threads"](C.c_int(1))
+    try:
+        return fn(z)
+    finally:
+        z["set_threads"](C.c_int(max(1, n0)))
+
+
+def _svdvals(A):
+    return _one_thread(lambda z: _svd_lapacke(z, A, vals_only=True) if z else np.linalg.svd(A, compute_uv=False))
+
+
+def _svd(A):
+    return _one_thread(lambda z: _svd_lapacke(z, A) if z else np.linalg.svd(A, full_matrices=False))
+
+
+def _eigvals(B):
+    return _one_thread(lambda z: _eigvals_lapacke(z, B) if z else np.linalg.eigvals(B))
 
 
 def _eigvals_lapacke(z, B):
@@ -265,7 +300,7 @@ def _B_from_moments(A0, A1, svd_tol, svd=None):
     """Thin SVD of A0, absolute rank, B = U_k^H A1 W_k Sigma_k^-1 (beyn.jl:286-320).
     Also takes (R, Q^H A1) of a device QR A0 = Q R: same S, W and B, U_R for U.
     svd: a thin-SVD function in place of numpy.linalg.svd."""
-    U, S, Wh = svd(A0) if svd else np.linalg.svd(A0, full_matrices=False)
+    U, S, Wh = svd(A0) if svd else _svd(A0)
     rk = int(np.count_nonzero(S >= svd_tol))
     Uk = U[:, :rk]
     Wk = Wh.conj().T[:, :rk]
@@ -301,7 +336,7 @@ def solve_disks(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed
         info["stats"].append(bh.last_stats)
         R1, C1 = ([a[:r, :r] for a in Rf], [c[:r, :r] for c in Cf]) if ahead else (Rf, Cf)
         t = clk()
-        S = _per_disk_host(list(R1), lambda a, z: _svd_lapacke(z, a)[1] if z else np.linalg.svd(a, compute_uv=False))
+        S = _per_disk_host(list(R1), lambda a, z: _svd_lapacke(z, a, vals_only=True) if z else np.linalg.svd(a, compute_uv=False))
         host["svd"] += (clk() - t) * 1e3
         rks = [int(np.count_nonzero(s >= svd_tol)) for s in S]
         grow = [rk == r and 2 * r < N for rk in rks]
@@ -393,10 +428,10 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
         # the saturation test needs only the singular values; the factors are
         # computed once, for the block that is finally used
         t = clk()
-        S = np.linalg.svd(M0, compute_uv=False)
+        S = _svdvals(M0)
         rk = int(np.count_nonzero(S >= svd_tol))
         if not (rk == r and 2 * r < N) and rk > 0:
-            U, S, Wh = np.linalg.svd(M0, full_matrices=False)
+            U, S, Wh = _svd(M0)
         host["svd"] += (clk() - t) * 1e3
         rused = r
         if rk == 0:
@@ -408,7 +443,7 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
             if r_tmp < N and ahead:
                 M0, M1 = M0f, M1f
                 t = clk()
-                U, S, Wh = np.linalg.svd(M0, full_matrices=False)
+                U, S, Wh = _svd(M0)
                 rk = int(np.count_nonzero(S >= svd_tol))
                 host["svd"] += (clk() - t) * 1e3
                 rused = r_tmp
@@ -428,7 +463,7 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
                 host["moments"] += (clk() - t) * 1e3
                 info["stats"].append(bh.last_stats)
                 t = clk()
-                U, S, Wh = np.linalg.svd(M0, full_matrices=False)
+                U, S, Wh = _svd(M0)
                 rk = int(np.count_nonzero(S >= svd_tol))
                 host["svd"] += (clk() - t) * 1e3
                 rused = r_tmp
@@ -470,7 +505,7 @@ def solve(solver, pts, k0, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed=False,
     B, Uk, info = construct_B_matrix(solver, pts, ws.dim, k0, R, nq, r, svd_tol, rng, mixed, ws, return_info=True,
                                      **kw)
     t = time.perf_counter()
-    lam = np.zeros(0, complex) if B.size == 0 else np.linalg.eigvals(B)
+    lam = np.zeros(0, complex) if B.size == 0 else _eigvals(B)
     info["host_ms"]["eigvals"] = (time.perf_counter() - t) * 1e3
     return (lam, info) if return_info else lam
 

@@ -1,5 +1,10 @@
 """GPU: Chebyshev-panel assembly of the mixed form on double-float (FP32 pair)
-arithmetic against the FP64 Chebyshev assembly of the same tables.
+arithmetic. Full operators (no symmetry) run on the J/E tables
+(k_cheb_build_je / k_assemble_je_df: J0, J1 and the entire parts of Y0, Y1 on
+1.5x the J panels, the logarithm and the pole of the Hankel functions applied
+per pair) and are checked against the FP64 direct assembly (no tables); the
+symmetry-reduced DLP runs on the H and J tables of the FP64 route and is
+checked against the FP64 Chebyshev assembly of the same tables.
 
 hi + lo must carry the FP64 value: |hi + lo - A64| <= 1e-13 max|A64| overall
 and <= 1e-12 |A64| elementwise where |A64| >= 1e-3 max|A64| (measured at most
@@ -19,8 +24,11 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _check(qb, ws, ks):
-    ref = qb.assemble(ws, ks, cheb=True)
+def _check(qb, ws, ks, ref_direct=False):
+    # the J/E tables and the FP64 route's H and J tables interpolate
+    # differently, so full operators are held against the FP64 direct
+    # evaluation (no tables); the reduced ones share the FP64 route's tables
+    ref = qb.assemble(ws, ks) if ref_direct else qb.assemble(ws, ks, cheb=True)
     out = qb.assemble(ws, ks, mixed=True, cheb=True, split_lo=True)
     nk = len(ks)
     for q in range(nk):
@@ -43,21 +51,45 @@ def test_df_assembly_cfie_star(qb, ks):
     b = qb.make_star(0.2, 5)
     sol = qb.CFIE_kress(1.0, b)
     pts, sol = qb.points_with_n(sol, b, 400, 25.0)
-    _check(qb, qb.Workspace(sol, pts), ks)
+    _check(qb, qb.Workspace(sol, pts), ks, ref_direct=True)
 
 
 def test_df_assembly_cfie_holed(qb):
     b = qb.make_circle_with_hole(1.0, (0.3, 0.1, 0.2))
     sol = qb.CFIE_kress(1.0, b)
     pts, sol = qb.points_with_n(sol, b, 500, 20.0)
-    _check(qb, qb.Workspace(sol, pts), [20.0 + 0.2j, 19.5 + 0.0j])
+    _check(qb, qb.Workspace(sol, pts), [20.0 + 0.2j, 19.5 + 0.0j], ref_direct=True)
 
 
 def test_df_assembly_dlp_stadium(qb):
     b = qb.make_full_stadium(1.0, 1.0)
     sol = qb.DLP_kress_global_corners(1.0, b)
     pts, sol = qb.points_with_n(sol, b, 600, 30.0)
-    _check(qb, qb.Workspace(sol, pts), [30.0 + 0.25j, 29.6 - 0.1j])
+    _check(qb, qb.Workspace(sol, pts), [30.0 + 0.25j, 29.6 - 0.1j], ref_direct=True)
+
+
+def test_df_assembly_je_high_k(qb):
+    """The bench's regime: CFIE star at k ~ 200 (|k| r from 0.6 to 500, the
+    series branch of the table builder below |k r| = 4 and the asymptotic one
+    above), panels tuned to 1e-13 (chebyshev_params_min_cost), against the
+    FP64 direct assembly (no tables): |hi + lo - A| <= 2e-13 max|A|."""
+    import math
+    b = qb.make_star(0.2, 5)
+    sol = qb.CFIE_kress(1.0, b)
+    pts, sol = qb.points_with_n(sol, b, 1024, 200.0)
+    ws = qb.Workspace(sol, pts)
+    ks = [200.0 + 0.4j, 199.6 - 0.3j]
+    zref = 200.0 + 0.5 * np.exp(2j * math.pi * np.arange(8) / 8)
+    cheb = tuple(int(x) for x in qb.chebyshev_params_min_cost(sol, pts, zref, ws=ws, tol=1e-13)[:4])
+    ref = qb.assemble(ws, ks)
+    out = qb.assemble(ws, ks, mixed=True, cheb=cheb, split_lo=True)
+    for q in range(len(ks)):
+        a = ref[q]
+        v = out[q].astype(np.complex128) + out[len(ks) + q].astype(np.complex128)
+        scale = np.max(np.abs(a))
+        err = np.max(np.abs(v - a)) / scale
+        print(f"k={ks[q]} panels {cheb}: max err/max|A| {err:.2e}")
+        assert err <= 2e-13, (q, err)
 
 
 def _reduced(qb, b, sym, n, k, corners=True):

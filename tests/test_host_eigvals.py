@@ -31,3 +31,23 @@ def test_eigvals_many_matches_numpy():
         U, S, Vh = beyn._svd_lapacke(z, A)
         assert np.max(np.abs(S - np.linalg.svd(A, compute_uv=False))) <= 1e-12 * S[0]
         assert np.max(np.abs((U * S) @ Vh - A)) <= 1e-12 * S[0]
+
+
+def test_one_thread_helpers_match_numpy():
+    """The single-disk path's SVD values, thin SVD and eigvals (BLAS at one
+    thread around each call) against NumPy; the thread count is restored."""
+    from qbgpu import beyn
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((96, 64)) + 1j * rng.standard_normal((96, 64))
+    B = rng.standard_normal((100, 100)) + 1j * rng.standard_normal((100, 100))
+    z = beyn._lapacke()
+    before = int(z["get_threads"]()) if z else None
+    S0 = np.linalg.svd(A, compute_uv=False)
+    assert np.max(np.abs(beyn._svdvals(A) - S0)) <= 1e-12 * S0[0]
+    U, S, Vh = beyn._svd(A)
+    assert np.max(np.abs(S - S0)) <= 1e-12 * S0[0]
+    assert np.max(np.abs((U * S) @ Vh - A)) <= 1e-12 * S0[0]
+    w, ref = beyn._eigvals(B), np.linalg.eigvals(B)
+    assert max(np.min(np.abs(ref - x)) for x in w) <= 1e-12 * np.max(np.abs(ref))
+    if z:
+        assert int(z["get_threads"]()) == before
