@@ -142,6 +142,9 @@ def main(argv=None):
     ap.add_argument("--cheb-tol", type=float, default=0.0,
                     help="beyn / assemble: panels by chebyshev_params_min_cost at this tolerance (the bench's "
                          "1e-13) instead of the reference's defaults")
+    ap.add_argument("--cheb-panels", default="",
+                    help="beyn / assemble: explicit panels n_h,M_h,n_j,M_j (no tuning launches; the bench's "
+                         "C2 tuning gives 7695,9,863,9)")
     ap.add_argument("--dk", type=float, default=0.05, help="ebim: window half-width")
     ap.add_argument("--nev", type=int, default=5, help="ebim: eigenvalues of the block iteration")
     ap.add_argument("--full", action="store_true", help="ebim: solve_full! convention (every root in the box)")
@@ -163,7 +166,9 @@ def main(argv=None):
     b, sol, pts = star_case(qb, a.n)
     ws = qb.Workspace(sol, pts)
     cheb = None
-    if a.cheb_tol > 0 and a.case in ("beyn", "assemble"):
+    if a.cheb_panels and a.case in ("beyn", "assemble"):
+        cheb = tuple(int(x) for x in a.cheb_panels.split(","))
+    elif a.cheb_tol > 0 and a.case in ("beyn", "assemble"):
         zref = 200.0 + 0.5 * np.exp(2j * math.pi * np.arange(a.nq) / a.nq)
         cheb = tuple(int(x) for x in qb.chebyshev_params_min_cost(sol, pts, zref, ws=ws, tol=a.cheb_tol)[:4])
         print("panels", cheb)

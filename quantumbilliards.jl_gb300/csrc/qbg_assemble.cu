@@ -1258,11 +1258,6 @@ __device__ __forceinline__ void df_series_d(const float4* __restrict__ c, int M,
   else df_series<S0>(c, M, t, v0r, v0i, v1r, v1i);
 }
 
-struct FoldDf {
-  dfl A, B, C, D;
-};
-
-__device__ __forceinline__ FoldDf fold_df(const Fold& f) { return {df_of(f.A), df_of(f.B), df_of(f.C), df_of(f.D)}; }
 
 __device__ __forceinline__ float4 pack_split(cxd v) {
   const float hr = (float)v.re, hi = (float)v.im;
@@ -1299,133 +1294,6 @@ __global__ void k_cheb_df_tables(ChebTables t) {
   const dfl a = df_of(s0.re), b = df_of(s0.im), c = df_of(s1.re), d = df_of(s1.im);
   dst[0] = make_float4(a.hi, a.lo, b.hi, b.lo);
   dst[1] = make_float4(c.hi, c.lo, d.hi, d.lo);
-}
-
-// symmetric-pair assembly of the complex64 forms on double-float arithmetic;
-// same tiling as k_assemble_cheb_sym, every node of ks in one pass
-template <int FORM, int DM>
-__global__ void __launch_bounds__(512) k_assemble_cheb_sym_df(GeomDev g, ChebTables t, const cxd* __restrict__ ks,
-                                                              int nk, void* const* __restrict__ outs,
-                                                              void* const* __restrict__ los, long long ld) {
-  __shared__ float4 sm[32][33];  // (hi.re, hi.im, lo.re, lo.im) of the mirrored entries
-  const int2 bp = tile_pair(blockIdx.x);
-  const int bi = bp.x, bj = bp.y;
-  const bool dtile = (bi == bj);
-  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 16
-  const int i = bi * 32 + tx;
-  auto store = [&](int slot, size_t off, float4 v) {
-    reinterpret_cast<cxf*>(outs[slot])[off] = cxf(v.x, v.y);
-    if (los) reinterpret_cast<cxf*>(los[slot])[off] = cxf(v.z, v.w);
-  };
-  // per slot: flags, panels, arguments and fold coefficients (the FP64 route
-  // of the rare direct pairs recomputes its geometry)
-  bool act[2], isdiag[2], zero[2], direct[2], needj[2];
-  FoldDf dij[2], dji[2];
-  int ph[2], pj[2];
-  dfl th[2], tj[2];
-  float rrf[2];
-#pragma unroll
-  for (int s = 0; s < 2; ++s) {
-    const int j = bj * 32 + ty + 16 * s;
-    const bool inb = (i < g.n) && (j < g.n);
-    isdiag[s] = inb && (i == j);
-    act[s] = inb && !isdiag[s] && (!dtile || i < j);
-    zero[s] = false;
-    direct[s] = false;
-    needj[s] = false;
-    rrf[s] = 0.f;
-    ph[s] = pj[s] = 0;
-    double thd = 0.0, tjd = 0.0;
-    Fold fij{0.0, 0.0, 0.0, 0.0}, fji{0.0, 0.0, 0.0, 0.0};
-    if (act[s]) {
-      const PairGeom pa = pair_geom(g, i, j);
-      const PairGeom pb = pair_geom(g, j, i);
-      fij = fold_of<FORM>(pa);
-      fji = fold_of<FORM>(pb);
-      rrf[s] = (float)pa.r;
-      zero[s] = (FORM == 1 && !pa.same && pa.r * pa.r <= 4.93038065763132e-32);
-      panel_of(pa.r, t.rmin, t.rmax, t.dr_h, t.invdr_h, t.nh, ph[s], thd);
-      panel_of(pa.r, 0.0, t.rmax, t.dr_j, t.invdr_j, t.nj, pj[s], tjd);
-      direct[s] = pa.r < t.rmin;
-      needj[s] = fij.A != 0.0 || fij.C != 0.0 || fji.A != 0.0 || fji.C != 0.0;
-    }
-    th[s] = df_of(thd);
-    tj[s] = df_of(tjd);
-    dij[s] = fold_df(fij);
-    dji[s] = fold_df(fji);
-  }
-  for (int q = 0; q < nk; ++q) {
-    // the direct-evaluation cut |k| r < small_cut in FP32 (a threshold, not a value)
-    const float akf = (float)t.nkc[q].ak;
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-      const int j = bj * 32 + ty + 16 * s;
-      float4 vij = make_float4(0.f, 0.f, 0.f, 0.f), vji = vij;
-      if (isdiag[s]) {
-        store(q, (size_t)i + (size_t)j * ld, pack_split(diag_fp64<FORM>(g, i, ks[q])));
-      } else if (act[s]) {
-        if (zero[s]) {
-          // both entries vanish
-        } else if (direct[s] || rrf[s] * akf < (float)t.small_cut) {
-          const PairGeom pa = pair_geom(g, i, j);
-          const PairGeom pb = pair_geom(g, j, i);
-          const Fold fij = fold_of<FORM>(pa), fji = fold_of<FORM>(pb);
-          const NodeConst nc = t.nkc[q];
-          const Bessel01d b = bessel01(pa.r * ks[q]);
-          cxd j0(0.0, 0.0), j1(0.0, 0.0);
-          if (needj[s]) {
-            int pjj = 0;
-            double tjd = 0.0;
-            panel_of(pa.r, 0.0, t.rmax, t.dr_j, t.invdr_j, t.nj, pjj, tjd);
-            clenshaw2(t.J + (((size_t)q * t.nj + pjj) * (t.Mj + 1)) * 2, t.Mj, tjd, j0, j1);
-          }
-          vij = pack_split(folded_entry(fij, nc.kaL1, nc.kaL2, nc.kg, nc.kd, b.h0(), b.h1(), j0, j1));
-          vji = pack_split(folded_entry(fji, nc.kaL1, nc.kaL2, nc.kg, nc.kd, b.h0(), b.h1(), j0, j1));
-        } else {
-          dfl h0r{0.f, 0.f}, h0i{0.f, 0.f}, h1r, h1i, j0r{0.f, 0.f}, j0i{0.f, 0.f}, j1r{0.f, 0.f}, j1i{0.f, 0.f};
-          df_series_d<FORM == 1, DM>(t.HD + ((size_t)q * t.nh + ph[s]) * (t.Mh + 1) * 2, t.Mh, th[s], &h0r, &h0i,
-                                     &h1r, &h1i);
-          if (needj[s])
-            df_series_d<FORM == 1, DM>(t.JD + ((size_t)q * t.nj + pj[s]) * (t.Mj + 1) * 2, t.Mj, tj[s], &j0r,
-                                       &j0i, &j1r, &j1i);
-          // entry = -(A kaL1 J1 + B kaL2 H1 + C kg J0 + D kd H0), the node factors inside the tables
-          auto fold = [&](const FoldDf& f) {
-            dfl re{0.f, 0.f}, im{0.f, 0.f};
-            df_acc(re, f.B, h1r);
-            df_acc(im, f.B, h1i);
-            if (needj[s]) {
-              df_acc(re, f.A, j1r);
-              df_acc(im, f.A, j1i);
-            }
-            if (FORM == 1) {
-              df_acc(re, f.D, h0r);
-              df_acc(im, f.D, h0i);
-              if (needj[s]) {
-                df_acc(re, f.C, j0r);
-                df_acc(im, f.C, j0i);
-              }
-            }
-            re = df_norm(re);
-            im = df_norm(im);
-            return make_float4(-re.hi, -im.hi, -re.lo, -im.lo);
-          };
-          vij = fold(dij[s]);
-          vji = fold(dji[s]);
-        }
-        store(q, (size_t)i + (size_t)j * ld, vij);
-      }
-    sm[ty + 16 * s][tx] = vji;  // row = j - bj*32, column = i - bi*32
-    }
-    __syncthreads();
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-      const int jl = tx, il = ty + 16 * s;  // output (row j, column i)
-      const int j = bj * 32 + jl, ii = bi * 32 + il;
-      const bool ok = (j < g.n) && (ii < g.n) && (dtile ? (jl > il) : true);
-      if (ok) store(q, (size_t)j + (size_t)ii * ld, sm[jl][il]);
-    }
-    __syncthreads();
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1487,48 +1355,86 @@ static __device__ void je_values(cxd k, cxd lkg, double r, cxd& j0, cxd& j1, cxd
   }
 }
 
-// one thread per (panel, node): the values at the M + 1 Chebyshev-Lobatto
-// points of the panel, their DCT-I (as k_cheb_build) and the double-float split
+// CTA = (JE_BUILD_THREADS / (M + 1)) panels of one node, one thread per
+// Chebyshev-Lobatto point (the FP64 Bessel evaluation is the cost: one
+// thread per panel left the FP64 pipe idle on latency); then one thread per
+// (panel, degree) forms the DCT-I coefficients (as k_cheb_build) from the
+// values in shared memory and stores their double-float split; last, one
+// thread per panel folds the panel's FP32-tail degree into JEm by atomicMax
+// (the largest over the nodes, so the assembly reads it once per pair).
+constexpr int JE_BUILD_THREADS = 128;
+
 template <int NS>
-__global__ void k_cheb_build_je(ChebTables t, const cxd* __restrict__ ks) {
+__global__ void __launch_bounds__(JE_BUILD_THREADS) k_cheb_build_je(ChebTables t, const cxd* __restrict__ ks) {
   constexpr int MMAX = QBG_CHEB_MAX_DEGREE;
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ cxd fv[JE_BUILD_THREADS][NS];
+  __shared__ double mag[JE_BUILD_THREADS][NS];
+  __shared__ double dct[(MMAX + 1) * (MMAX + 1)];
+  const int M = t.Mje, P = M + 1, ppb = JE_BUILD_THREADS / P;
   const int q = blockIdx.y;
-  if (p >= t.nje) return;
-  const int M = t.Mje;
-  const double a = (double)p * t.dr_je;
-  const double b = (p + 1 == t.nje) ? t.rmax : (double)(p + 1) * t.dr_je;
+  const int tid = threadIdx.x;
+  for (int x = tid; x < P * P; x += JE_BUILD_THREADS) {
+    const int jn = x / P, m = x % P;
+    dct[x] = cospi((double)(jn * m) / (double)M);  // cos(pi jn m / M)
+  }
+  const int lp = tid / P, n = tid % P;
+  const int p = blockIdx.x * ppb + lp;
+  const bool live = lp < ppb && p < t.nje;
   const cxd k = ks[q];
-  const bool realk = (k.im == 0.0);
-  const cxd kaL2 = 0.5 * cmul_i(k), kd = -0.5 * k;
-  const cxd lkg = clog_d(0.5 * k) + cxd(0.57721566490153286061, 0.0);
-  cxd f[MMAX + 1][NS];
-  for (int jn = 0; jn <= M; ++jn) {
-    const double tn = cospi((double)jn / (double)M);
+  if (live) {
+    const double a = (double)p * t.dr_je;
+    const double b = (p + 1 == t.nje) ? t.rmax : (double)(p + 1) * t.dr_je;
+    const bool realk = (k.im == 0.0);
+    const cxd kaL2 = 0.5 * cmul_i(k), kd = -0.5 * k;
+    const cxd lkg = clog_d(0.5 * k) + cxd(0.57721566490153286061, 0.0);
+    const double tn = cospi((double)n / (double)M);
     const double r = 0.5 * ((b + a) + (b - a) * tn);
     cxd j0, j1, g0, g1;
     je_values(k, lkg, r, j0, j1, g0, g1);
     if (realk) { j0.im = 0.0; j1.im = 0.0; g0.im = 0.0; g1.im = 0.0; }
-    f[jn][0] = kaL2 * j1;
-    f[jn][1] = kaL2 * (j1 + cmul_i(g1));
+    fv[tid][0] = kaL2 * j1;
+    fv[tid][1] = kaL2 * (j1 + cmul_i(g1));
     if (NS == 4) {
-      f[jn][2] = kd * j0;
-      f[jn][3] = kd * (j0 + cmul_i(g0));
+      fv[tid][2] = kd * j0;
+      fv[tid][3] = kd * (j0 + cmul_i(g0));
     }
   }
-  float4* out = t.JE + ((size_t)q * t.nje + p) * (size_t)(M + 1) * NS;
-  for (int m = 0; m <= M; ++m) {
+  __syncthreads();
+  if (live) {
+    const int m = n, base = lp * P;  // this thread: degree m of panel p
     const double sg = (m & 1) ? -1.0 : 1.0;
     double sc = 2.0 / (double)M;
     if (m == 0) sc *= 0.5;
+    float4* out = t.JE + ((size_t)q * t.nje + p) * (size_t)P * NS;
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
-      cxd acc = 0.5 * f[0][s] + (0.5 * sg) * f[M][s];
-      for (int jn = 1; jn < M; ++jn) acc += cospi((double)(jn * m) / (double)M) * f[jn][s];
+      cxd acc = 0.5 * fv[base][s] + (0.5 * sg) * fv[base + M][s];
+      for (int jn = 1; jn < M; ++jn) acc += dct[jn * P + m] * fv[base + jn][s];
       acc = sc * acc;
       const dfl re = df_of(acc.re), im = df_of(acc.im);
       out[m * NS + s] = make_float4(re.hi, re.lo, im.hi, im.lo);
+      mag[tid][s] = fabs(acc.re) + fabs(acc.im);
     }
+  }
+  __syncthreads();
+  if (live && n == 0) {
+    // FP32 tail: terms from degree m0 on, in every series, sum to at most
+    // 2^-26 of the series' coefficient magnitudes; FP32 products of those
+    // terms (|T_m| <= 1, error <= 2^-23 each) then stay below 2^-49 of that
+    // sum, the order of the double-float rounding of the head (m0 >= 2: the
+    // recurrence of the head supplies T_{m0-1} and T_{m0-2})
+    const int base = lp * P;
+    int m0 = 2;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      double tot = 0.0;
+      for (int m = 0; m <= M; ++m) tot += mag[base + m][s];
+      double tail = 0.0;
+      int ms = M + 1;
+      while (ms > 2 && tail + mag[base + ms - 1][s] <= 0x1p-26 * tot) tail += mag[base + --ms][s];
+      m0 = ms > m0 ? ms : m0;
+    }
+    atomicMax(t.JEm + p, m0);
   }
 }
 
@@ -1640,15 +1546,17 @@ __device__ __noinline__ void je_direct_pair(const GeomDev& g, int i, int j, cxd 
   *vji = pack_split(folded_entry(fold_of<FORM>(pb), kaL1, kaL2, kg, kd, bz.h0(), bz.h1(), bz.j0, bz.j1));
 }
 
-// sum_m c_m T_m(t) of the NS complex series of one table row
+// sum_m c_m T_m(t) of the NS complex series of one table row: degrees below
+// m0 in double-float, the tail (m0 <= m <= M) as FP32 products added to the
+// low words (the accumulators are unnormalised: hi exact partial sums)
 template <int NS>
-__device__ __forceinline__ void je_series(const float4* __restrict__ c, int M, dfl t, dfl* v) {
+__device__ __forceinline__ void je_series(const float4* __restrict__ c, int M, int m0, dfl t, dfl* v) {
 #pragma unroll
   for (int s = 0; s < 2 * NS; ++s) v[s] = dfl{0.f, 0.f};
   dfl tp{1.f, 0.f}, tc = t;
   const dfl t2{2.f * t.hi, 2.f * t.lo};
 #pragma unroll 2
-  for (int m = 0; m <= M; ++m) {
+  for (int m = 0; m < m0; ++m) {
     dfl tm;
     if (m == 0) {
       tm = tp;
@@ -1666,27 +1574,47 @@ __device__ __forceinline__ void je_series(const float4* __restrict__ c, int M, d
       df_acc(v[2 * s + 1], dfl{cc.z, cc.w}, tm);
     }
   }
+  // m0 >= 2: tc = T_{m0-1}, tp = T_{m0-2}
+  float fp = tp.hi, fc = tc.hi;
+  const float f2 = t2.hi;
+#pragma unroll 2
+  for (int m = m0; m <= M; ++m) {
+    const float fm = fmaf(f2, fc, -fp);
+    fp = fc;
+    fc = fm;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      const float4 cc = __ldg(c + m * NS + s);
+      v[2 * s].lo = fmaf(cc.x, fm, v[2 * s].lo);
+      v[2 * s + 1].lo = fmaf(cc.z, fm, v[2 * s + 1].lo);
+    }
+  }
 }
 }  // namespace
 
 // Full symmetric operator on the J/E tables, every node of ks in one pass.
-// CTA = one 32 x 32 tile pair (bi <= bj) as k_assemble_cheb_sym_df, but the
+// CTA = one 32 x 32 tile pair (bi <= bj) as k_assemble_cheb_sym, but the
 // tile's pairs are sorted by table panel before the node loop (bitonic sort of
 // 1024 keys in shared memory), so the 32 pairs of a warp read a few table rows
 // instead of 32 (the row loads were the bound of the per-pair order: 23
 // sectors per request, half the issue slots lost to long-scoreboard stalls).
 // Both mirrored entries of a pair are staged in shared memory per node and
 // written as coalesced columns.
-template <int FORM>
-__global__ void __launch_bounds__(512) k_assemble_je_df(GeomDev g, ChebTables t, const cxd* __restrict__ ks, int nk,
-                                                        void* const* __restrict__ outs, void* const* __restrict__ los,
-                                                        long long ld) {
+template <int FORM, int OCC>
+__global__ void __launch_bounds__(512, OCC) k_assemble_je_df(GeomDev g, ChebTables t, const cxd* __restrict__ ks,
+                                                             int nk, void* const* __restrict__ outs,
+                                                             void* const* __restrict__ los, long long ld) {
   constexpr int NS = FORM == 1 ? 4 : 2;
-  constexpr int NC = je_coef_words<FORM>();
-  __shared__ float4 tA[32][33];  // entries (i, j): [j - 32 bj][i - 32 bi]; the whole tile when bi == bj
-  __shared__ float4 tB[32][33];  // entries (j, i): [i - 32 bi][j - 32 bj]
-  __shared__ unsigned keys[1024];
-  extern __shared__ float4 coef[];  // [NC][1024]: the pair coefficients of every sorted slot
+  // dynamic shared memory: tA [32][32] float4 = entries (i, j) at [j - 32 bj][i - 32 bi] (the whole
+  // tile when bi == bj); tB [32][32] = entries (j, i) at [i - 32 bi][j - 32 bj], its first 4 KB
+  // holding the sort keys before the node loop; coef [NC][1024], the pair coefficients of every
+  // sorted slot (registers would spill). Column reads of tA / tB are contiguous per warp, so the
+  // tiles need no padding.
+  extern __shared__ float4 smem_je[];
+  float4(*tA)[32] = reinterpret_cast<float4(*)[32]>(smem_je);
+  float4(*tB)[32] = reinterpret_cast<float4(*)[32]>(smem_je + 1024);
+  unsigned* keys = reinterpret_cast<unsigned*>(smem_je + 1024);
+  float4* coef = smem_je + 2048;
   const int2 bp = tile_pair(blockIdx.x);
   const int bi = bp.x, bj = bp.y;
   const bool dtile = (bi == bj);
@@ -1719,52 +1647,54 @@ __global__ void __launch_bounds__(512) k_assemble_je_df(GeomDev g, ChebTables t,
       __syncthreads();
     }
   }
-  // per slot (sorted positions tid and tid + 512): indices, panel, argument;
-  // the coefficients go to shared memory (registers would spill)
-  int pe[2], ppan[2];
-  bool act[2], zero[2], direct[2];
+  // per slot (sorted positions tid and tid + 512): meta = e | m0 << 10 | flags, panel, argument
+  constexpr unsigned ACT = 1u << 16, ZERO = 1u << 17, DIRECT = 1u << 18;
+  unsigned meta[2];
+  int ppan[2];
   dfl tt[2];
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
     const unsigned key = keys[tid + 512 * s];
     const int e = (int)(key & 1023u);
-    pe[s] = e;
-    act[s] = (key >> 10) != NOPANEL;
-    zero[s] = false;
-    direct[s] = false;
+    unsigned mt = (unsigned)e;
     ppan[s] = 0;
     double td = 0.0;
     Fold fij{0.0, 0.0, 0.0, 0.0}, fji{0.0, 0.0, 0.0, 0.0};
     double l = 0.0, invr = 0.0;
-    if (act[s]) {
+    if ((key >> 10) != NOPANEL) {
       const int i = bi * 32 + (e & 31), j = bj * 32 + (e >> 5);
       const PairGeom pa = pair_geom(g, i, j);
       const PairGeom pb = pair_geom(g, j, i);
       fij = fold_of<FORM>(pa);
       fji = fold_of<FORM>(pb);
-      zero[s] = (FORM == 1 && !pa.same && pa.r * pa.r <= 4.93038065763132e-32);
-      direct[s] = !zero[s] && pa.r < t.rmin;
+      const bool zero = (FORM == 1 && !pa.same && pa.r * pa.r <= 4.93038065763132e-32);
+      mt |= ACT | (zero ? ZERO : 0u) | ((!zero && pa.r < t.rmin) ? DIRECT : 0u);
       panel_of(pa.r, 0.0, t.rmax, t.dr_je, t.invdr_je, t.nje, ppan[s], td);
+      mt |= (unsigned)t.JEm[ppan[s]] << 10;
       l = 0.63661977236758134308 * log(pa.r);
       invr = pa.invr;
     }
+    meta[s] = mt;
     tt[s] = df_of(td);
     je_coef_store<FORM>(coef, tid + 512 * s, je_coef<FORM>(fij, l, invr), je_coef<FORM>(fji, l, invr));
   }
+  __syncthreads();  // every key is read before the node loop writes tB
   const int Mt = t.Mje;
   for (int q = 0; q < nk; ++q) {
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
-      if (!act[s]) continue;
-      const int il = pe[s] & 31, jl = pe[s] >> 5;
+      const unsigned mt = meta[s];
+      if (!(mt & ACT)) continue;
+      const int il = mt & 31, jl = (mt >> 5) & 31;
       float4 vij = make_float4(0.f, 0.f, 0.f, 0.f), vji = vij;
-      if (zero[s]) {
+      if (mt & ZERO) {
         // both entries vanish
-      } else if (direct[s]) {
+      } else if (mt & DIRECT) {
         je_direct_pair<FORM>(g, bi * 32 + il, bj * 32 + jl, ks[q], &vij, &vji);
       } else {
         dfl v[8];
-        je_series<NS>(t.JE + ((size_t)q * t.nje + ppan[s]) * (size_t)(Mt + 1) * NS, Mt, tt[s], v);
+        je_series<NS>(t.JE + ((size_t)q * t.nje + ppan[s]) * (size_t)(Mt + 1) * NS, Mt, (int)((mt >> 10) & 31u),
+                      tt[s], v);
         JeCoef cij, cji;
         je_coef_load<FORM>(coef, tid + 512 * s, cij, cji);
         vij = je_fold<FORM>(cij, v);
@@ -1947,7 +1877,7 @@ bool cheb_je_applies(const GeomDev& g, int deriv, int prec) {
 }
 
 size_t cheb_je_bytes(const ChebTables& t) {
-  return sizeof(float4) * (size_t)t.nse * t.nk * t.nje * (size_t)(t.Mje + 1);
+  return sizeof(float4) * (size_t)t.nse * t.nk * t.nje * (size_t)(t.Mje + 1) + sizeof(int) * (size_t)t.nje;
 }
 
 int cheb_je_build(ChebTables& t, const cxd* ks, cudaStream_t st) {
@@ -1956,17 +1886,19 @@ int cheb_je_build(ChebTables& t, const cxd* ks, cudaStream_t st) {
     set_error("cheb_je_build: invalid table parameters");
     return QBG_EINVAL;
   }
-  dim3 grd((t.nje + 63) / 64, t.nk);
-  if (t.nse == 4) k_cheb_build_je<4><<<grd, 64, 0, st>>>(t, ks);
-  else k_cheb_build_je<2><<<grd, 64, 0, st>>>(t, ks);
+  t.JEm = reinterpret_cast<int*>(t.JE + (size_t)t.nse * t.nk * t.nje * (size_t)(t.Mje + 1));
+  QBG_CUDA(cudaMemsetAsync(t.JEm, 0, sizeof(int) * (size_t)t.nje, st));
+  const int ppb = JE_BUILD_THREADS / (t.Mje + 1);
+  dim3 grd((t.nje + ppb - 1) / ppb, t.nk);
+  if (t.nse == 4) k_cheb_build_je<4><<<grd, JE_BUILD_THREADS, 0, st>>>(t, ks);
+  else k_cheb_build_je<2><<<grd, JE_BUILD_THREADS, 0, st>>>(t, ks);
   QBG_LAUNCH_CHECK("k_cheb_build_je");
   return QBG_OK;
 }
 
 bool cheb_df_applies(const GeomDev& g, int deriv) {
-  if (deriv) return false;
-  if (g.m == g.n) return true;
-  return g.form == 0 && g.norb <= 4;
+  // full operators take the J/E tables (cheb_je_applies)
+  return !deriv && g.m != g.n && g.form == 0 && g.norb <= 4;
 }
 
 void cheb_df_bytes(const ChebTables& t, size_t* hd, size_t* jd, size_t* nkc) {
@@ -2065,6 +1997,33 @@ int cheb_build(ChebTables& t, const cxd* ks, cudaStream_t st) {
   return QBG_OK;
 }
 
+// blocks per SM of k_assemble_je_df: 2 (64 registers, 2 x 112 KB of shared
+// memory for the CFIE; default) or 1 (128 registers, QBG_JE_OCC=1). On C2 the
+// assembly phase took 8.2 ms at 2 and 9.2 ms at 1.
+static int je_occupancy() {
+  static const int occ = [] {
+    const char* e = getenv("QBG_JE_OCC");
+    return (e && atoi(e) == 1) ? 1 : 2;
+  }();
+  return occ;
+}
+
+template <int FORM>
+static int launch_je_df(const GeomDev& g, const ChebTables& t, const cxd* ks, int nk, void* const* outs,
+                        void* const* los, long long ld, dim3 grd, dim3 blk, cudaStream_t st) {
+  const size_t dyn = sizeof(float4) * (2048 + 1024 * (size_t)je_coef_words<FORM>());
+  if (je_occupancy() == 2) {
+    QBG_CUDA(cudaFuncSetAttribute(k_assemble_je_df<FORM, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    QBG_CUDA(cudaFuncSetAttribute(k_assemble_je_df<FORM, 2>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  (int)cudaSharedmemCarveoutMaxShared));
+    k_assemble_je_df<FORM, 2><<<grd, blk, dyn, st>>>(g, t, ks, nk, outs, los, ld);
+  } else {
+    QBG_CUDA(cudaFuncSetAttribute(k_assemble_je_df<FORM, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    k_assemble_je_df<FORM, 1><<<grd, blk, dyn, st>>>(g, t, ks, nk, outs, los, ld);
+  }
+  return QBG_OK;
+}
+
 int launch_assemble_cheb(const GeomDev& g, const ChebTables& t, const cxd* ks, int nk, int deriv, int prec,
                          void* const* outs_dev, void* const* lo_outs_dev, long long ld, cudaStream_t st) {
   if (g.quad == 1) return launch_alpert(g, &t, ks, nk, deriv, prec, outs_dev, ld, st, lo_outs_dev);
@@ -2114,22 +2073,8 @@ int launch_assemble_cheb(const GeomDev& g, const ChebTables& t, const cxd* ks, i
         k_assemble_cheb_sym<1, 0><<<sgrd, sblk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, nullptr, ld);
     } else if (t.JE && prec == QBG_PREC_MIXED) {
       dim3 dgrd((unsigned)(nt * (nt + 1) / 2), 1, 1);
-      const size_t dyn = sizeof(float4) * 1024 * (g.form == 0 ? je_coef_words<0>() : je_coef_words<1>());
-      if (g.form == 0) {
-        QBG_CUDA(cudaFuncSetAttribute(k_assemble_je_df<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-        k_assemble_je_df<0><<<dgrd, sblk, dyn, st>>>(g, t, ks, nk, outs_dev, lo_outs_dev, ld);
-      } else {
-        QBG_CUDA(cudaFuncSetAttribute(k_assemble_je_df<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-        k_assemble_je_df<1><<<dgrd, sblk, dyn, st>>>(g, t, ks, nk, outs_dev, lo_outs_dev, ld);
-      }
-    } else if (t.HD && t.JD && t.nkc) {
-      dim3 dgrd((unsigned)(nt * (nt + 1) / 2), 1, 1);
-      // the degree stays a runtime value here: with 512 threads and the
-      // coefficients of two series in registers the compile-time forms spill
-      if (g.form == 0)
-        k_assemble_cheb_sym_df<0, 0><<<dgrd, sblk, 0, st>>>(g, t, ks, nk, outs_dev, lo_outs_dev, ld);
-      else
-        k_assemble_cheb_sym_df<1, 0><<<dgrd, sblk, 0, st>>>(g, t, ks, nk, outs_dev, lo_outs_dev, ld);
+      if (g.form == 0) QBG_TRY(launch_je_df<0>(g, t, ks, nk, outs_dev, lo_outs_dev, ld, dgrd, sblk, st));
+      else QBG_TRY(launch_je_df<1>(g, t, ks, nk, outs_dev, lo_outs_dev, ld, dgrd, sblk, st));
     } else {
       if (g.form == 0)
         k_assemble_cheb_sym<0, 1><<<sgrd, sblk, 0, st>>>(g, t, ks, nk, kchunk, outs_dev, lo_outs_dev, ld);

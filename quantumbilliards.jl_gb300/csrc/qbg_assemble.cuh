@@ -39,6 +39,11 @@ struct ChebTables {
   // all entire in r, so that kaL2 H1 = U + i l P + 1/(pi r), kd H0 = W + i l R,
   // kaL1 J1 = (i/pi) P and kg J0 = (i/pi) R
   float4* JE = nullptr;
+  // per panel: the first degree whose terms, and all higher ones, sum to at
+  // most 2^-26 of the row's coefficient magnitudes in every series and at
+  // every node; the assembly adds those terms in FP32 (stored after the
+  // coefficients in JE)
+  int* JEm = nullptr;
   int nje = 0, Mje = 0, nse = 0;
   double dr_je = 0, invdr_je = 0;
 };
