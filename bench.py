@@ -264,10 +264,13 @@ def cpu_sample_text(c):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serial", action="store_true",
+                    help="time the disks one solve() call after another instead of through solve_pipelined "
+                         "(host SVD / eig of a disk overlapped with the device work of the next)")
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--cpu-steps", type=int, default=1, help="timed whole disks of the cpu_baseline leg")
     ap.add_argument("--workload", default="beyn", choices=["beyn", "ebim", "c1", "c3", "serve"],
@@ -345,16 +348,33 @@ def main():
     times, counts, errs, stats, missing = [], [], [], [], []
     launches0 = qb.launch_count()
     t_region0 = time.perf_counter()
-    for s in range(args.steps):
-        lam, info, dt = run_step(qb, sol, pts, ws, mixed=True, cheb=cheb, nb=nb)
-        sel, e, miss = accuracy(lam, oracle_all)
-        counts.append(int(np.count_nonzero(e <= TOL_EIG)))
-        errs.append(e)
-        missing.append(miss)
-        times.append(dt)
-        stats.append(info["stats"])
+    if args.serial:
+        for s in range(args.steps):
+            lam, info, dt = run_step(qb, sol, pts, ws, mixed=True, cheb=cheb, nb=nb)
+            sel, e, miss = accuracy(lam, oracle_all)
+            counts.append(int(np.count_nonzero(e <= TOL_EIG)))
+            errs.append(e)
+            missing.append(miss)
+            times.append(dt)
+            stats.append(info["stats"])
+    else:
+        # the same disk every step, each with the probes of run_step (a fresh generator seeded SEED)
+        lams, pinfo = qb.solve_pipelined(sol, pts, [K0 + 0j] * args.steps, RADIUS, nq=NQ, r=L_PROBES,
+                                         svd_tol=SVD_TOL, rngs=[np.random.default_rng(SEED)
+                                                                for _ in range(args.steps)],
+                                         mixed=True, ws=ws, return_info=True, cheb=cheb, nb=nb)
+        for lam, st in zip(lams, pinfo["stats"]):
+            sel, e, miss = accuracy(lam, oracle_all)
+            counts.append(int(np.count_nonzero(e <= TOL_EIG)))
+            errs.append(e)
+            missing.append(miss)
+            stats.append([st])
+        info = {"r": pinfo["r"][-1], "host_ms": {"finish_per_disk": float(np.mean(pinfo["host_ms"])),
+                                                 "device_calls_per_disk": float(np.mean(pinfo["device_call_ms"]))}}
     _lib.load().qbg_device_sync()
     t_region = time.perf_counter() - t_region0
+    if not args.serial:
+        times = [t_region / args.steps] * args.steps
     gpu_launches = qb.launch_count() - launches0
     replica_barrier(world)
     clocks = clk.stop()
@@ -362,10 +382,27 @@ def main():
     t_region_max, eig_total = replica_reduce(world, t_region, float(sum(counts)))
     # end to end through the public API including the geometry upload
     e2e_times, e2e_counts = [], []
-    for _ in range(max(1, min(args.steps, 3))):
-        lam_e, _, dt = run_step(qb, sol, pts, None, mixed=True, with_geometry=True, cheb=cheb, nb=nb)
-        e2e_times.append(dt)
-        e2e_counts.append(int(np.count_nonzero(accuracy(lam_e, oracle_all)[1] <= TOL_EIG)))
+    if args.serial:
+        for _ in range(max(1, min(args.steps, 3))):
+            lam_e, _, dt = run_step(qb, sol, pts, None, mixed=True, with_geometry=True, cheb=cheb, nb=nb)
+            e2e_times.append(dt)
+            e2e_counts.append(int(np.count_nonzero(accuracy(lam_e, oracle_all)[1] <= TOL_EIG)))
+    else:
+        t_e = time.perf_counter()
+        ws_e = qb.Workspace(sol, pts)
+        lams_e = qb.solve_pipelined(sol, pts, [K0 + 0j] * args.steps, RADIUS, nq=NQ, r=L_PROBES, svd_tol=SVD_TOL,
+                                    rngs=[np.random.default_rng(SEED) for _ in range(args.steps)], mixed=True,
+                                    ws=ws_e, cheb=cheb, nb=nb)
+        ws_e.close()
+        dt = (time.perf_counter() - t_e) / args.steps
+        for lam_e in lams_e:
+            e2e_times.append(dt)
+            e2e_counts.append(int(np.count_nonzero(accuracy(lam_e, oracle_all)[1] <= TOL_EIG)))
+    # the same disks one synchronous solve() after another, for comparison
+    serial_times = []
+    if not args.serial:
+        for _ in range(max(1, min(args.steps, 3))):
+            serial_times.append(run_step(qb, sol, pts, ws, mixed=True, cheb=cheb, nb=nb)[2])
     # FP32 form (FP32 kernel values): reported beside, with its own accuracy
     run_step(qb, sol, pts, ws, mixed="fp32", cheb=cheb)
     lam32, info32, t32 = run_step(qb, sol, pts, ws, mixed="fp32", cheb=cheb)
@@ -412,8 +449,12 @@ def main():
         "dtype": "c64+c128",
         "data": "synthetic",
         "config": dict(workload_config(), r_final=r_final, cheb_panels=list(cheb), cheb_tol=CHEB_TOL,
-                       timing="wall clock of the synchronous API calls between device synchronizations (the step "
-                              "ends with the host SVD and eigvals); device phases in phases_ms are CUDA events"),
+                       timing=("wall clock of the synchronous API calls between device synchronizations (the step "
+                               "ends with the host SVD and eigvals)" if args.serial else
+                               "wall clock of one solve_pipelined call over `steps` disks (each disk's host SVD "
+                               "and eigvals overlap the device work of the next; the last disk's are inside the "
+                               "region)") + "; device phases in phases_ms are CUDA events"),
+        "serial_ms_per_step": (float(np.median(serial_times)) * 1e3 if serial_times else None),
         "plan_s": plan_s,
         "lu_plan": {"nb": nb, "outer": tuned["outer"], "parts": tuned["parts"], "tune_s": tuned["tune_s"],
                     "tried": [[t["nb"], t["outer"], t["parts"], round(t["ms"], 1)] for t in tuned["table"]]},

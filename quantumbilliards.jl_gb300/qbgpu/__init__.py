@@ -17,7 +17,7 @@ from .operators import (Workspace, build_workspace, assemble, assemble_noalloc, 
                         set_gemm_engine, launch_count, chebyshev_params, residual_c64,
                         release_cached_memory, pool_stats, adjoint_fredholm_matrix, solve_vect_dlp,
                         chebyshev_params_min_cost)
-from .beyn import BeynHandle, construct_B_matrix, solve_vect, solve, solve_disks, probe_matrix, contour
+from .beyn import BeynHandle, construct_B_matrix, solve_vect, solve, solve_disks, solve_pipelined, probe_matrix, contour
 from .sweep import k_sweep, get_eigenvalues, newton_refine_svd, refine_minima
 from . import sweep
 from . import ebim

@@ -510,5 +510,81 @@ def solve(solver, pts, k0, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed=False,
     return (lam, info) if return_info else lam
 
 
+def _finish_ahead(M0f, M1f, r, N, svd_tol):
+    """The host part of construct_B_matrix after moments_qr of the 2r-column
+    block drawn up front (regrow_ahead, basis=False): the rank test on the
+    leading r x r block of R, the thin SVD of the block finally used, B and
+    eig(B) (beyn.jl:283-322, 371). Returns (eigenvalues, rk, r used, host ms)."""
+    clk = time.perf_counter
+    t = clk()
+    ahead = M0f.shape[0] == 2 * r
+    M0, M1 = (np.asfortranarray(M0f[:r, :r]), np.asfortranarray(M1f[:r, :r])) if ahead else (M0f, M1f)
+    S = _svdvals(M0)
+    rk = int(np.count_nonzero(S >= svd_tol))
+    rused = r
+    U = Wh = None
+    if rk == r and ahead:
+        M0, M1 = M0f, M1f
+        U, S, Wh = _svd(M0)
+        rk = int(np.count_nonzero(S >= svd_tol))
+        rused = 2 * r
+    elif rk > 0:
+        U, S, Wh = _svd(M0)
+    if rk == 0:
+        return np.zeros(0, complex), 0, rused, (clk() - t) * 1e3
+    B = U[:, :rk].conj().T @ ((M1 @ Wh.conj().T[:, :rk]) / S[:rk][None, :])
+    lam = _eigvals(B)
+    return lam, rk, rused, (clk() - t) * 1e3
+
+
+def solve_pipelined(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rngs=None, mixed=False, ws=None,
+                    return_info=False, nb=0, use_chebyshev=True, cheb=None, max_refine=10, refine_tol=1e-6):
+    """Eigenvalues of a sequence of disks (as `solve` on each, beyn.jl:388-397),
+    one disk at a time on the device, with each disk's host part (the SVDs of
+    R, B and eig(B)) on a worker thread while the device assembles, factors
+    and solves the next disk: LAPACKE and the library release the interpreter
+    lock, so the two overlap. The regrowth block is drawn up front (as
+    `solve`'s default); a disk whose 2r probes would not fit (2r >= N) is
+    finished the same way without regrowth, as construct_B_matrix does.
+
+    rngs: one numpy Generator per disk (default: default_rng(d) for disk d);
+    disk d draws its probes as `solve(..., rng=rngs[d])` would, so the
+    eigenvalues are those of `solve` disk by disk. Returns the list of
+    eigenvalue arrays [, info with per-disk rk, r and host times]."""
+    from concurrent.futures import ThreadPoolExecutor
+    ws = ws if ws is not None else Workspace(solver, pts)
+    N = ws.dim
+    k0s = list(np.atleast_1d(np.asarray(k0s, dtype=np.complex128)))
+    Rs = np.broadcast_to(np.asarray(R, dtype=np.float64), (len(k0s),))
+    rngs = rngs if rngs is not None else [np.random.default_rng(d) for d in range(len(k0s))]
+    if len(rngs) != len(k0s):
+        raise ValueError("one generator per disk")
+    ahead = 2 * r < N
+    clk = time.perf_counter
+    futs, stats, dev_ms = [], [], []
+    with ThreadPoolExecutor(max_workers=1) as pool:
+        for k0, Rd, g in zip(k0s, Rs, rngs):
+            t = clk()
+            bh = BeynHandle(ws, complex(k0), float(Rd), nq, mixed, max_refine, refine_tol, nb=nb,
+                            use_chebyshev=use_chebyshev, cheb=cheb)
+            try:
+                V = probe_matrix(N, r, g)
+                if ahead:
+                    V = np.hstack([V, probe_matrix(N, r, g)])
+                M0f, M1f = bh.moments_qr(V)
+                stats.append(bh.last_stats)
+            finally:
+                bh.close()
+            dev_ms.append((clk() - t) * 1e3)
+            futs.append(pool.submit(_finish_ahead, M0f, M1f, r, N, svd_tol))
+        res = [f.result() for f in futs]
+    out = [x[0] for x in res]
+    if not return_info:
+        return out
+    info = dict(stats=stats, rk=[x[1] for x in res], r=[x[2] for x in res], host_ms=[x[3] for x in res],
+                device_call_ms=dev_ms)
+    return out, info
+
+
 def inside(lam, k0, R):
     return np.abs(lam - k0) <= R
