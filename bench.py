@@ -370,7 +370,8 @@ def main():
             missing.append(miss)
             stats.append([st])
         info = {"r": pinfo["r"][-1], "host_ms": {"finish_per_disk": float(np.mean(pinfo["host_ms"])),
-                                                 "device_calls_per_disk": float(np.mean(pinfo["device_call_ms"]))}}
+                                                 "device_calls_per_disk": float(np.mean(pinfo["device_call_ms"])),
+                                                 **pinfo["call_split_ms"]}}
     _lib.load().qbg_device_sync()
     t_region = time.perf_counter() - t_region0
     if not args.serial:

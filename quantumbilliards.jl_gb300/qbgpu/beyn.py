@@ -320,16 +320,26 @@ def solve_disks(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed
     k0s = np.atleast_1d(np.asarray(k0s, dtype=np.complex128))
     clk = time.perf_counter
     host = dict(create=0.0, moments=0.0, svd=0.0, B_eigvals=0.0)  # wall-clock ms of the host-visible phases
+    ahead = regrow_ahead and 2 * r < N
+
+    def draw():  # the probe block (and the regrowth block, see construct_B_matrix), drawn during the factorisation
+        V = probe_matrix(N, r, rng)
+        return np.asfortranarray(np.hstack([V, probe_matrix(N, r, rng)])) if ahead else V
+
+    from concurrent.futures import ThreadPoolExecutor
     t = clk()
-    bh = BeynHandle(ws, k0s, R, nq, mixed, **kw)
-    host["create"] += (clk() - t) * 1e3
+    with ThreadPoolExecutor(max_workers=1) as ex:
+        fut = ex.submit(draw)
+        bh = BeynHandle(ws, k0s, R, nq, mixed, **kw)
+        host["create"] += (clk() - t) * 1e3
+        try:
+            V = fut.result()
+        except BaseException:
+            bh.close()
+            raise
     info = dict(stats=[], rk=[], r=[], host_ms=host)
     # moments reduced on the device: per disk R (A0 = Q R) and Q^H A1, m x m
     try:
-        V = probe_matrix(N, r, rng)
-        ahead = regrow_ahead and 2 * r < N
-        if ahead:  # the regrowth block solved with the first one (see construct_B_matrix)
-            V = np.hstack([V, probe_matrix(N, r, rng)])
         t = clk()
         Rf, Cf = bh.moments_qr(V)
         host["moments"] += (clk() - t) * 1e3
@@ -403,18 +413,28 @@ def construct_B_matrix(solver, pts, N, k0, R, nq=64, r=48, svd_tol=1e-14, rng=No
         raise ValueError(f"N={N} does not match the operator dimension {ws.dim}")
     clk = time.perf_counter
     host = dict(create=0.0, moments=0.0, svd=0.0, B=0.0)  # wall-clock ms of the host-visible phases
+    ahead = regrow == "extend" and regrow_ahead and 2 * r < N
+
+    def draw():  # the probe block, drawn while the library assembles and factors
+        V = probe_matrix(N, r, rng)
+        return np.asfortranarray(np.hstack([V, probe_matrix(N, r, rng)])) if ahead else V
+
+    from concurrent.futures import ThreadPoolExecutor
     t = clk()
-    bh = BeynHandle(ws, k0, R, nq, mixed, max_refine, refine_tol, nb=nb, use_chebyshev=use_chebyshev, cheb=cheb,
-                    fp32_sweeps=fp32_sweeps, solve_block=solve_block, node_chunk=node_chunk,
-                    resid_engine=resid_engine)
-    host["create"] += (clk() - t) * 1e3
+    with ThreadPoolExecutor(max_workers=1) as ex:
+        fut = ex.submit(draw)
+        bh = BeynHandle(ws, k0, R, nq, mixed, max_refine, refine_tol, nb=nb, use_chebyshev=use_chebyshev, cheb=cheb,
+                        fp32_sweeps=fp32_sweeps, solve_block=solve_block, node_chunk=node_chunk,
+                        resid_engine=resid_engine)
+        host["create"] += (clk() - t) * 1e3
+        try:
+            V = fut.result()
+        except BaseException:
+            bh.close()
+            raise
     info = dict(stats=[], host_ms=host)
     moments = bh.moments if basis else bh.moments_qr
     try:
-        V = probe_matrix(N, r, rng)
-        ahead = regrow == "extend" and regrow_ahead and 2 * r < N
-        if ahead:
-            V = np.hstack([V, probe_matrix(N, r, rng)])
         t = clk()
         M0, M1 = moments(V)  # (A0, A1), or (R, Q^H A1)
         host["moments"] += (clk() - t) * 1e3
@@ -561,28 +581,42 @@ def solve_pipelined(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rngs=None, 
         raise ValueError("one generator per disk")
     ahead = 2 * r < N
     clk = time.perf_counter
-    futs, stats, dev_ms = [], [], []
-    with ThreadPoolExecutor(max_workers=1) as pool:
-        for k0, Rd, g in zip(k0s, Rs, rngs):
+
+    def probes(g):  # numpy fills the normals without the interpreter lock
+        V = probe_matrix(N, r, g)
+        return np.asfortranarray(np.hstack([V, probe_matrix(N, r, g)])) if ahead else V
+
+    futs, stats, dev_ms, split = [], [], [], []
+    # two workers: the next disk's probes and the previous disk's host part
+    with ThreadPoolExecutor(max_workers=2) as pool:
+        nxt = pool.submit(probes, rngs[0]) if k0s else None
+        for d, (k0, Rd) in enumerate(zip(k0s, Rs)):
             t = clk()
+            V = nxt.result()
+            if d + 1 < len(k0s):
+                nxt = pool.submit(probes, rngs[d + 1])
+            t1 = clk()
             bh = BeynHandle(ws, complex(k0), float(Rd), nq, mixed, max_refine, refine_tol, nb=nb,
                             use_chebyshev=use_chebyshev, cheb=cheb)
+            t2 = clk()
             try:
-                V = probe_matrix(N, r, g)
-                if ahead:
-                    V = np.hstack([V, probe_matrix(N, r, g)])
                 M0f, M1f = bh.moments_qr(V)
                 stats.append(bh.last_stats)
             finally:
+                t3 = clk()
                 bh.close()
-            dev_ms.append((clk() - t) * 1e3)
+            t4 = clk()
+            dev_ms.append((t4 - t) * 1e3)
+            split.append(((t1 - t) * 1e3, (t2 - t1) * 1e3, (t3 - t2) * 1e3, (t4 - t3) * 1e3))
             futs.append(pool.submit(_finish_ahead, M0f, M1f, r, N, svd_tol))
         res = [f.result() for f in futs]
     out = [x[0] for x in res]
     if not return_info:
         return out
     info = dict(stats=stats, rk=[x[1] for x in res], r=[x[2] for x in res], host_ms=[x[3] for x in res],
-                device_call_ms=dev_ms)
+                device_call_ms=dev_ms,
+                call_split_ms=dict(zip(("probe_wait", "create", "moments_qr", "close"),
+                                       [float(np.mean(c)) for c in zip(*split)])) if split else {})
     return out, info
 
 
