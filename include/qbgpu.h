@@ -451,7 +451,9 @@ qbg_status qbg_cgemm_c64(int32_t engine, int32_t M, int32_t N, int32_t K, const 
 /* Refinement residual, for validation: R_b = V_b - (Th_b + Tl_b) X_b for b < batch
  * (host buffers, column-major; Th, Tl: n x n complex64 per b, Tl may be NULL;
  * X, V, R: n x L complex128 per b), rmax = max |re R| + |im R|. engine 0 =
- * tensor cores (exact digit products), 1 = compensated FP32 on CUDA cores.
+ * tensor cores (exact digit products of seven 7-bit digits), 1 = compensated
+ * FP32 on CUDA cores, 2 = tensor cores from the leading six digits (the
+ * refinement's first residual, ~2^-40 of the row and column scales).
  * No reference counterpart (the reference has no refinement). */
 qbg_status qbg_residual_c64(int32_t engine, int32_t n, int32_t L, int32_t batch, const float* Th, const float* Tl,
                             const double* X, const double* V, double* R, double* rmax);

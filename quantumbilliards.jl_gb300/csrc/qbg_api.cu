@@ -812,8 +812,7 @@ qbg_status qbg_launch_count(uint64_t* count) {
 
 qbg_status qbg_residual_c64(int32_t engine, int32_t n, int32_t L, int32_t batch, const float* Th, const float* Tl,
                             const double* X, const double* V, double* R, double* rmax) {
-  if (!Th || !X || !V || !R || !rmax || n < 1 || L < 1 || batch < 1 || batch > 65535 ||
-      (engine != 0 && engine != 1)) {
+  if (!Th || !X || !V || !R || !rmax || n < 1 || L < 1 || batch < 1 || batch > 65535 || engine < 0 || engine > 2) {
     set_error("qbg_residual_c64: invalid arguments");
     return QBG_EINVAL;
   }
@@ -853,7 +852,9 @@ qbg_status qbg_residual_c64(int32_t engine, int32_t n, int32_t L, int32_t batch,
     }
     if (!s) s = tc_resid_bind_T(t, n, batch, tmem, 0);
     if (!s) s = tc_resid_prepare_T(t, dTh, dTl, (long long)nn, batch, 0);
-    if (!s) s = tc_residual(t, dX, (long long)nl, dV, (long long)nl, dR, (long long)nl, L, batch, dmax, xmem, 0);
+    if (!s)
+      s = tc_residual(t, dX, (long long)nl, dV, (long long)nl, dR, (long long)nl, L, batch, dmax, xmem, 0,
+                      engine == 2 ? 6 : 7);
     if (!s) s = tc_check(0);
   }
   if (!s) {

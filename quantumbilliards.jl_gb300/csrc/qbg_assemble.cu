@@ -63,6 +63,36 @@ static __device__ __forceinline__ PairGeom pair_geom(const GeomDev& g, int i, in
   return p;
 }
 
+// pair_geom of (i, j) and of (j, i) together: the distance, its reciprocal
+// and the Kress log term are symmetric and computed once (FP64 is 1/64 of the
+// FP32 rate on this part)
+static __device__ __forceinline__ void pair_geom_sym(const GeomDev& g, int i, int j, PairGeom& a, PairGeom& b) {
+  const double dxij = g.x[i] - g.x[j], dyij = g.y[i] - g.y[j];
+  a.r = b.r = hypot(dxij, dyij);
+  a.invr = b.invr = 1.0 / a.r;
+  a.inn = g.dy[j] * dxij - g.dx[j] * dyij;
+  b.inn = g.dx[i] * dyij - g.dy[i] * dxij;
+  a.wj = g.ws[j];
+  a.sj = g.speed[j];
+  b.wj = g.ws[i];
+  b.sj = g.speed[i];
+  const int ci = g.comp[i], cj = g.comp[j];
+  a.same = b.same = (ci == cj);
+  if (a.same) {
+    const int o = g.coff[ci], na = g.coff[ci + 1] - o;
+    int d = g.lidx[i] - g.lidx[j];
+    d += (d < 0) ? na : 0;
+    a.Rk = g.kcol[o + d];
+    int e = g.lidx[j] - g.lidx[i];
+    e += (e < 0) ? na : 0;
+    b.Rk = g.kcol[o + e];
+    a.lt = b.lt = pair_logterm(g.ts[i], g.ts[j]);
+  } else {
+    a.Rk = b.Rk = 0.0;
+    a.lt = b.lt = 0.0;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // FP64 entry for one wavenumber
 // ---------------------------------------------------------------------------
@@ -1627,8 +1657,9 @@ __global__ void __launch_bounds__(512, OCC) k_assemble_je_df(GeomDev g, ChebTabl
     const int i = bi * 32 + (e & 31), j = bj * 32 + (e >> 5);
     unsigned pk = NOPANEL;
     if (i < g.n && j < g.n && i != j && (!dtile || i < j)) {
-      const double r = hypot(g.x[i] - g.x[j], g.y[i] - g.y[j]);
-      int qp = (int)floor(r * t.invdr_je);
+      // FP32 distance: the key only groups pairs by panel (the slot's panel is FP64)
+      const float dx = (float)(g.x[i] - g.x[j]), dy = (float)(g.y[i] - g.y[j]);
+      int qp = (int)(sqrtf(fmaf(dx, dx, dy * dy)) * (float)t.invdr_je);
       qp = qp < 0 ? 0 : (qp >= t.nje ? t.nje - 1 : qp);
       pk = (unsigned)qp;
     }
@@ -1663,8 +1694,8 @@ __global__ void __launch_bounds__(512, OCC) k_assemble_je_df(GeomDev g, ChebTabl
     double l = 0.0, invr = 0.0;
     if ((key >> 10) != NOPANEL) {
       const int i = bi * 32 + (e & 31), j = bj * 32 + (e >> 5);
-      const PairGeom pa = pair_geom(g, i, j);
-      const PairGeom pb = pair_geom(g, j, i);
+      PairGeom pa, pb;
+      pair_geom_sym(g, i, j, pa, pb);
       fij = fold_of<FORM>(pa);
       fji = fold_of<FORM>(pb);
       const bool zero = (FORM == 1 && !pa.same && pa.r * pa.r <= 4.93038065763132e-32);

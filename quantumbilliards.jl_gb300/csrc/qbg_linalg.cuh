@@ -136,8 +136,10 @@ size_t tc_resid_T_bytes(int n, int batch);
 int tc_resid_bind_T(TcResidT& t, int n, int batch, void* mem, cudaStream_t st);  // zeroes mem
 int tc_resid_prepare_T(TcResidT& t, const cxf* Th, const cxf* Tl, long long sT, int c, cudaStream_t st);
 size_t tc_resid_X_bytes(int n, int L, int batch);  // scratch per residual call (zeroed once by the caller)
+// ndig: 7 (the full digit product, ~2^-47 of the row and column scales) or 6
+// (the leading six digits of T and X, ~2^-40: for a sweep that is not the last)
 int tc_residual(const TcResidT& t, const cxd* X, long long sX, const cxd* V, long long sV, cxd* R, long long sR,
-                int L, int c, double* rmax, void* xmem, cudaStream_t st);
+                int L, int c, double* rmax, void* xmem, cudaStream_t st, int ndig = 7);
 // device address of the tensor-core error flag (shared by the GEMM and the residual)
 int tc_error_ptr(int** p);
 

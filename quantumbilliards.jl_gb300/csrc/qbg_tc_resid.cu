@@ -16,7 +16,9 @@
 // own TMEM accumulator. A level collects at most 7 pairs, so over 512 real
 // terms its partial sum stays below 7 * 2^21 < 2^24 and is exact; every 512
 // terms the levels are read back and added, scaled by 2^{-7g}, into
-// double-float (hi + lo FP32) sums, which carry ~48 bits. The pairs left out
+// double-float (hi + lo FP32) sums, which carry ~48 bits. (A residual for a
+// refinement sweep that is not the last may use the leading six digits of
+// both operands: 21 pairs in 6 levels, ~2^-40 of the scales.) The pairs left out
 // (a + b >= 9) and the truncation of both digit expansions are below 2^-47 of
 // max|T_i.| max|X_.l| per term, the accuracy of the compensated FP32 kernel
 // this replaces. The complex product uses the real mapping of the complex
@@ -46,8 +48,7 @@
 namespace qbg {
 namespace {
 
-constexpr int RD = 7;                 // digits per operand
-constexpr int RLEV = 7;               // levels g = 2..8
+constexpr int RD = 7;                 // digits per operand (levels g = 2..8 of the full product)
 constexpr int RBM = 128;              // rows of R per CTA
 constexpr int RBN = 32;               // complex columns of R per CTA (B' rows: 64)
 constexpr int RKS = 16;               // real k per stage (one MMA k-step)
@@ -347,6 +348,10 @@ __global__ void k_x_digits(const cxd* __restrict__ X, long long sX, int n, int L
 // ---------------------------------------------------------------------------
 // R = V - T X from the digit planes; grid (Lp / 32, ceil(n / 128), batch)
 // ---------------------------------------------------------------------------
+// ND <= RD: the leading ND digits of T and X, pairs a + b <= ND + 1 (ND levels);
+// ND = RD is the full product, a smaller ND a residual to ~2^-(7 ND) of the
+// scales (for refinement sweeps whose correction is not the last)
+template <int ND>
 __global__ void __launch_bounds__(128, 1) k_resid_tc(const unsigned char* __restrict__ TD,
                                                      const int* __restrict__ erow,
                                                      const unsigned char* __restrict__ XD,
@@ -395,12 +400,13 @@ __global__ void __launch_bounds__(128, 1) k_resid_tc(const unsigned char* __rest
   const unsigned char* xb = XD + (z * NT + nt) * (long long)KS * RB_TILE;
   int issued = 0, consumed = 0, committed = 0, freed = 0;
   bool good = (*abort_flag == 0);
+  // the leading ND planes of each tile image (planes are stored most significant first)
   auto issue = [&](int t) {
     const int s = t % RNST;
     const uint32_t fb = r_smem_u32(full + s);
-    r_expect(fb, (uint32_t)RSTAGE);
-    r_bulk(sbase + (uint32_t)(s * RSTAGE), ta + (long long)t * RA_TILE, (uint32_t)RA_TILE, fb);
-    r_bulk(sbase + (uint32_t)(s * RSTAGE + RA_TILE), xb + (long long)t * RB_TILE, (uint32_t)RB_TILE, fb);
+    r_expect(fb, (uint32_t)(ND * (RA_PLANE + RB_PLANE)));
+    r_bulk(sbase + (uint32_t)(s * RSTAGE), ta + (long long)t * RA_TILE, (uint32_t)(ND * RA_PLANE), fb);
+    r_bulk(sbase + (uint32_t)(s * RSTAGE + RA_TILE), xb + (long long)t * RB_TILE, (uint32_t)(ND * RB_PLANE), fb);
   };
   if (tid == 0 && good)
     for (; issued < KS && issued < RNST; ++issued) issue(issued);
@@ -420,10 +426,10 @@ __global__ void __launch_bounds__(128, 1) k_resid_tc(const unsigned char* __rest
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t so = sbase + (uint32_t)(s * RSTAGE);
 #pragma unroll
-        for (int a = 1; a <= RD; ++a) {
+        for (int a = 1; a <= ND; ++a) {
           const uint64_t da = r_desc(so + (uint32_t)((a - 1) * RA_PLANE));
 #pragma unroll
-          for (int bq = 1; bq + a <= RLEV + 1; ++bq) {
+          for (int bq = 1; bq + a <= ND + 1; ++bq) {
             const int g = a + bq;  // 2 .. 8
             const uint64_t db = r_desc(so + (uint32_t)(RA_TILE + (bq - 1) * RB_PLANE));
             const uint32_t bit = 1u << (g - 2);
@@ -460,7 +466,7 @@ __global__ void __launch_bounds__(128, 1) k_resid_tc(const unsigned char* __rest
       __syncwarp();
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll 1
-      for (int lev = 0; lev < RLEV; ++lev) {
+      for (int lev = 0; lev < ND; ++lev) {
         const float sc = ldexpf(1.f, -7 * (lev + 2));
 #pragma unroll
         for (int qt = 0; qt < 4; ++qt) {
@@ -574,9 +580,9 @@ size_t tc_resid_X_bytes(int n, int L, int batch) {
 }
 
 int tc_residual(const TcResidT& t, const cxd* X, long long sX, const cxd* V, long long sV, cxd* R, long long sR,
-                int L, int c, double* rmax, void* xmem, cudaStream_t st) {
+                int L, int c, double* rmax, void* xmem, cudaStream_t st, int ndig) {
   const int n = t.n, Lp = lp_of(L), NT = Lp / RBN;
-  if (c > t.batch || c < 1 || c > 65535 || L < 1) {
+  if (c > t.batch || c < 1 || c > 65535 || L < 1 || (ndig != RD && ndig != 6)) {
     set_error("tc_residual: bad sizes");
     return QBG_EINVAL;
   }
@@ -589,16 +595,22 @@ int tc_residual(const TcResidT& t, const cxd* X, long long sX, const cxd* V, lon
   int dev = 0;
   QBG_CUDA(cudaGetDevice(&dev));
   if (dev >= 0 && dev < 64 && !attr[dev]) {
-    QBG_CUDA(cudaFuncSetAttribute(k_resid_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r_smem_bytes()));
+    QBG_CUDA(cudaFuncSetAttribute(k_resid_tc<RD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r_smem_bytes()));
+    QBG_CUDA(cudaFuncSetAttribute(k_resid_tc<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r_smem_bytes()));
     attr[dev] = true;
   }
   k_x_colexp<<<dim3(L, c), 256, 0, st>>>(X, sX, n, L, fcol);
   QBG_LAUNCH_CHECK("k_x_colexp");
   k_x_digits<<<dim3((n + 255) / 256, Lp, c), 256, 0, st>>>(X, sX, n, L, NT, t.KS, fcol, XD);
   QBG_LAUNCH_CHECK("k_x_digits");
-  k_resid_tc<<<dim3(NT, t.MT, c), 128, r_smem_bytes(), st>>>(
-      static_cast<const unsigned char*>(t.TD), t.erow, XD, fcol, n, L, t.MT, NT, t.KS, V, sV, R, sR,
-      reinterpret_cast<unsigned long long*>(rmax), derr);
+  if (ndig == 6)
+    k_resid_tc<6><<<dim3(NT, t.MT, c), 128, r_smem_bytes(), st>>>(
+        static_cast<const unsigned char*>(t.TD), t.erow, XD, fcol, n, L, t.MT, NT, t.KS, V, sV, R, sR,
+        reinterpret_cast<unsigned long long*>(rmax), derr);
+  else
+    k_resid_tc<RD><<<dim3(NT, t.MT, c), 128, r_smem_bytes(), st>>>(
+        static_cast<const unsigned char*>(t.TD), t.erow, XD, fcol, n, L, t.MT, NT, t.KS, V, sV, R, sR,
+        reinterpret_cast<unsigned long long*>(rmax), derr);
   QBG_LAUNCH_CHECK("k_resid_tc");
   return QBG_OK;
 }

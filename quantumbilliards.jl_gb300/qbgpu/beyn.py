@@ -200,6 +200,13 @@ def _lapacke():
                                    C.c_void_p, C.c_int64, C.c_void_p, C.c_int64]
                     _LAPACKE = dict(zgeev=ev, zgesdd=sd, set_threads=lib.scipy_openblas_set_num_threads64_,
                                     get_threads=lib.scipy_openblas_get_num_threads64_)
+                    if hasattr(lib, "scipy_LAPACKE_zgeqrf64_") and hasattr(lib, "scipy_LAPACKE_zunmqr64_"):
+                        qf, qm = lib.scipy_LAPACKE_zgeqrf64_, lib.scipy_LAPACKE_zunmqr64_
+                        qf.restype = qm.restype = C.c_int64
+                        qf.argtypes = [C.c_int, C.c_int64, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p]
+                        qm.argtypes = [C.c_int, C.c_char, C.c_char, C.c_int64, C.c_int64, C.c_int64, C.c_void_p,
+                                       C.c_int64, C.c_void_p, C.c_void_p, C.c_int64]
+                        _LAPACKE.update(zgeqrf=qf, zunmqr=qm)
                     break
         except OSError:
             _LAPACKE = False
@@ -530,6 +537,41 @@ def solve(solver, pts, k0, R, nq=32, r=48, svd_tol=1e-14, rng=None, mixed=False,
     return (lam, info) if return_info else lam
 
 
+def _qr_reduce_host(A0, A1, threads=4):
+    """(R, Q^H A1), m x m each, of the thin Householder QR A0 = Q R: LAPACK's
+    zgeqrf and zunmqr (the routines behind the device path's cuSOLVER calls)
+    with the BLAS at `threads`, or NumPy's qr without LAPACKE."""
+    z = _lapacke()
+    m = A0.shape[1]
+    if not z or "zgeqrf" not in z:
+        Q, R = np.linalg.qr(A0)
+        return R, Q.conj().T @ A1
+    a = np.array(A0, dtype=np.complex128, order="F", copy=True)
+    c = np.array(A1, dtype=np.complex128, order="F", copy=True)
+    n = a.shape[0]
+    k = min(n, m)  # reflectors
+    tau = np.empty(k, np.complex128)
+    n0 = int(z["get_threads"]())
+    z["set_threads"](C.c_int(max(1, threads)))
+    try:
+        info = z["zgeqrf"](102, n, m, a.ctypes.data, n, tau.ctypes.data)
+        if info == 0:
+            info = z["zunmqr"](102, b"L", b"C", n, m, k, a.ctypes.data, n, tau.ctypes.data, c.ctypes.data, n)
+    finally:
+        z["set_threads"](C.c_int(max(1, n0)))
+    if info != 0:
+        raise np.linalg.LinAlgError(f"zgeqrf / zunmqr info {info}")
+    return np.asfortranarray(np.triu(a[:k, :m])), np.asfortranarray(c[:k, :m])
+
+
+def _finish_host_qr(A0, A1, r, N, svd_tol):
+    """_finish_ahead after the QR reduction of the moments on the host."""
+    t = time.perf_counter()
+    R, Cm = _qr_reduce_host(A0, A1)
+    lam, rk, rused, _ = _finish_ahead(R, Cm, r, N, svd_tol)
+    return lam, rk, rused, (time.perf_counter() - t) * 1e3
+
+
 def _finish_ahead(M0f, M1f, r, N, svd_tol):
     """The host part of construct_B_matrix after moments_qr of the 2r-column
     block drawn up front (regrow_ahead, basis=False): the rank test on the
@@ -558,7 +600,8 @@ def _finish_ahead(M0f, M1f, r, N, svd_tol):
 
 
 def solve_pipelined(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rngs=None, mixed=False, ws=None,
-                    return_info=False, nb=0, use_chebyshev=True, cheb=None, max_refine=10, refine_tol=1e-6):
+                    return_info=False, nb=0, use_chebyshev=True, cheb=None, max_refine=10, refine_tol=1e-6,
+                    host_qr=True):
     """Eigenvalues of a sequence of disks (as `solve` on each, beyn.jl:388-397),
     one disk at a time on the device, with each disk's host part (the SVDs of
     R, B and eig(B)) on a worker thread while the device assembles, factors
@@ -566,6 +609,10 @@ def solve_pipelined(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rngs=None, 
     lock, so the two overlap. The regrowth block is drawn up front (as
     `solve`'s default); a disk whose 2r probes would not fit (2r >= N) is
     finished the same way without regrowth, as construct_B_matrix does.
+
+    host_qr: the moments come back whole and their QR reduction (A0 = Q R,
+    Q^H A1) runs on the worker too (LAPACK zgeqrf / zunmqr), off the device's
+    path; False reduces them on the device (moments_qr) as `solve` does.
 
     rngs: one numpy Generator per disk (default: default_rng(d) for disk d);
     disk d draws its probes as `solve(..., rng=rngs[d])` would, so the
@@ -600,7 +647,7 @@ def solve_pipelined(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rngs=None, 
                             use_chebyshev=use_chebyshev, cheb=cheb)
             t2 = clk()
             try:
-                M0f, M1f = bh.moments_qr(V)
+                M0f, M1f = bh.moments(V) if host_qr else bh.moments_qr(V)
                 stats.append(bh.last_stats)
             finally:
                 t3 = clk()
@@ -608,14 +655,14 @@ def solve_pipelined(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rngs=None, 
             t4 = clk()
             dev_ms.append((t4 - t) * 1e3)
             split.append(((t1 - t) * 1e3, (t2 - t1) * 1e3, (t3 - t2) * 1e3, (t4 - t3) * 1e3))
-            futs.append(pool.submit(_finish_ahead, M0f, M1f, r, N, svd_tol))
+            futs.append(pool.submit(_finish_host_qr if host_qr else _finish_ahead, M0f, M1f, r, N, svd_tol))
         res = [f.result() for f in futs]
     out = [x[0] for x in res]
     if not return_info:
         return out
     info = dict(stats=stats, rk=[x[1] for x in res], r=[x[2] for x in res], host_ms=[x[3] for x in res],
                 device_call_ms=dev_ms,
-                call_split_ms=dict(zip(("probe_wait", "create", "moments_qr", "close"),
+                call_split_ms=dict(zip(("probe_wait", "create", "moments", "close"),
                                        [float(np.mean(c)) for c in zip(*split)])) if split else {})
     return out, info
 

@@ -287,7 +287,8 @@ def cgemm(A, B, C=None, alpha=1.0, beta=0.0, engine: int = 1) -> np.ndarray:
 def residual_c64(Th, Tl, X, V, engine: int = 0):
     """Device refinement residual R = V - (Th + Tl) X (validation helper).
     Th, Tl: (batch, n, n) complex64 (Tl may be None); X, V: (batch, n, L)
-    complex128. engine 0 = tensor cores, 1 = compensated FP32. Returns (R, rmax)."""
+    complex128. engine 0 = tensor cores, 1 = compensated FP32, 2 = tensor cores
+    from the leading six digits (the refinement's first residual). Returns (R, rmax)."""
     Th = np.asarray(Th, np.complex64)
     single = Th.ndim == 2
     Th = Th[None] if single else Th

@@ -51,3 +51,25 @@ def test_one_thread_helpers_match_numpy():
     assert max(np.min(np.abs(ref - x)) for x in w) <= 1e-12 * np.max(np.abs(ref))
     if z:
         assert int(z["get_threads"]()) == before
+
+
+def test_host_qr_reduction():
+    """The pipelined driver's host QR of the moments (LAPACK zgeqrf / zunmqr):
+    R upper triangular with R^H R = A0^H A0 and R^H C = A0^H A1 (1e-12 of
+    |A0|^2, |A0||A1|), for tall and for wide moment blocks; the BLAS thread
+    count is restored."""
+    from qbgpu import beyn
+    rng = np.random.default_rng(8)
+    z = beyn._lapacke()
+    before = int(z["get_threads"]()) if z else None
+    for n, m in ((300, 64), (40, 64)):
+        A0 = rng.standard_normal((n, m)) + 1j * rng.standard_normal((n, m))
+        A1 = rng.standard_normal((n, m)) + 1j * rng.standard_normal((n, m))
+        R, Cm = beyn._qr_reduce_host(A0, A1)
+        assert R.shape == (min(n, m), m) and Cm.shape == (min(n, m), m)
+        assert np.array_equal(R, np.triu(R))
+        s0, s01 = np.linalg.norm(A0) ** 2, np.linalg.norm(A0) * np.linalg.norm(A1)
+        assert np.max(np.abs(R.conj().T @ R - A0.conj().T @ A0)) < 1e-12 * s0
+        assert np.max(np.abs(R.conj().T @ Cm - A0.conj().T @ A1)) < 1e-12 * s01
+    if z:
+        assert int(z["get_threads"]()) == before
