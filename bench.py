@@ -457,8 +457,10 @@ def main():
                                "region)") + "; device phases in phases_ms are CUDA events"),
         "serial_ms_per_step": (float(np.median(serial_times)) * 1e3 if serial_times else None),
         "plan_s": plan_s,
-        "lu_plan": {"nb": nb, "outer": tuned["outer"], "parts": tuned["parts"], "tune_s": tuned["tune_s"],
-                    "tried": [[t["nb"], t["outer"], t["parts"], round(t["ms"], 1)] for t in tuned["table"]]},
+        "lu_plan": {"nb": nb, "outer": tuned["outer"], "parts": tuned["parts"], "cluster": tuned["cluster"],
+                    "tune_s": tuned["tune_s"],
+                    "tried": [[t["nb"], t["outer"], t["parts"], t["cluster"], round(t["ms"], 1)]
+                              for t in tuned["table"]]},
         "eigenvalues_per_step": n_eig,
         "oracle_eigenvalues_in_disk": int(len(oracle_sel)),
         "oracle_eigenvalues_missed": int(max(missing)),
@@ -503,6 +505,7 @@ def main():
         line["config"]["parallelism"] = f"replicas{world}"
     if not args.no_extras and rank == 0 and world == 1:
         ws.close()
+        qb.autotune.set_lu_plan(cluster=-1)  # the panel form tuned for C2's batch back to automatic
         line["other_configs"] = {
             "c1": c1_sweep(qb),
             "c3": c3_disks(qb, repeat=2),

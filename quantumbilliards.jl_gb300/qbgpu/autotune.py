@@ -11,13 +11,15 @@ updates' summation order):
 * ``parts``: contiguous parts of the operator batch factored and solved on
   their own streams, so one part's panels overlap another part's tensor-core
   updates, process-wide (read when a handle is created);
-* ``cluster``: the panel form, automatic by batch size.
+* ``cluster``: the panel form: -1 automatic (the 8-CTA cluster panel for
+  batches of at most 4 operators per part, one CTA per panel otherwise),
+  0 always one CTA, 1 the cluster wherever the panel fits it.
 
 ``tune_beyn`` times whole Beyn steps (assembly, factorisation, solves,
 moments and the host rank test and eigenvalues) of the caller's own workload
 and keeps the fastest plan, by coordinate descent: parts, then outer, then
-nb, each from the best so far. The plan is left set in the library and
-returned (pass ``nb`` on to ``solve`` / ``solve_disks``).
+nb, then the panel form, each from the best so far. The plan is left set in
+the library and returned (pass ``nb`` on to ``solve`` / ``solve_disks``).
 """
 from __future__ import annotations
 
@@ -47,17 +49,17 @@ def set_lu_plan(outer=None, cluster=None, parts=None):
 
 
 def tune_beyn(solver, pts, ws, k0, R, nq, r, mixed=True, cheb=None, svd_tol=1e-12, seed=0, reps=2,
-              parts=(2, 4, 8), outers=(2, 4, 8), nbs=(64, 32)):
+              parts=(2, 4, 8), outers=(2, 4, 8), nbs=(64, 32), clusters=(1,)):
     """Times Beyn steps of this workload under candidate plans and keeps the
-    fastest. Returns dict(nb, outer, parts, ms, table, tune_s): ``table``
-    lists every plan tried with its median step time in ms."""
+    fastest. Returns dict(nb, outer, parts, cluster, ms, table, tune_s):
+    ``table`` lists every plan tried with its median step time in ms."""
     from .beyn import solve
 
     t_start = time.perf_counter()
     table = []
 
-    def run(nb, outer, npart):
-        set_lu_plan(outer=outer, cluster=-1, parts=npart)
+    def run(nb, outer, npart, cluster=-1):
+        set_lu_plan(outer=outer, cluster=cluster, parts=npart)
         kw = dict(nq=nq, r=r, svd_tol=svd_tol, mixed=mixed, ws=ws, cheb=cheb, nb=nb)
         solve(solver, pts, k0, R, rng=np.random.default_rng(seed), **kw)  # warm: buffers of this plan
         ts = []
@@ -66,11 +68,11 @@ def tune_beyn(solver, pts, ws, k0, R, nq, r, mixed=True, cheb=None, svd_tol=1e-1
             solve(solver, pts, k0, R, rng=np.random.default_rng(seed), **kw)
             ts.append(time.perf_counter() - t0)
         ms = 1e3 * float(np.median(ts))
-        table.append({"nb": nb, "outer": outer, "parts": npart, "ms": ms})
+        table.append({"nb": nb, "outer": outer, "parts": npart, "cluster": cluster, "ms": ms})
         return ms
 
     cur = lu_plan()
-    best = {"nb": nbs[0], "outer": cur["outer"], "parts": cur["parts"]}
+    best = {"nb": nbs[0], "outer": cur["outer"], "parts": cur["parts"], "cluster": -1}
     best["ms"] = run(best["nb"], best["outer"], best["parts"])
     for p in parts:
         if p != best["parts"]:
@@ -89,7 +91,12 @@ def tune_beyn(solver, pts, ws, k0, R, nq, r, mixed=True, cheb=None, svd_tol=1e-1
             ms = run(nb, o, best["parts"])
             if ms < best["ms"]:
                 best.update(nb=nb, outer=o, ms=ms)
-    set_lu_plan(outer=best["outer"], cluster=-1, parts=best["parts"])
+    for c in clusters:
+        if c != best["cluster"]:
+            ms = run(best["nb"], best["outer"], best["parts"], c)
+            if ms < best["ms"]:
+                best.update(cluster=c, ms=ms)
+    set_lu_plan(outer=best["outer"], cluster=best["cluster"], parts=best["parts"])
     best["table"] = table
     best["tune_s"] = time.perf_counter() - t_start
     return best

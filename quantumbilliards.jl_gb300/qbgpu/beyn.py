@@ -601,13 +601,23 @@ def _finish_ahead(M0f, M1f, r, N, svd_tol):
 
 def solve_pipelined(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rngs=None, mixed=False, ws=None,
                     return_info=False, nb=0, use_chebyshev=True, cheb=None, max_refine=10, refine_tol=1e-6,
-                    host_qr=True):
-    """Eigenvalues of a sequence of disks (as `solve` on each, beyn.jl:388-397),
-    one disk at a time on the device, with each disk's host part (the SVDs of
-    R, B and eig(B)) on a worker thread while the device assembles, factors
-    and solves the next disk: LAPACKE and the library release the interpreter
-    lock, so the two overlap. The regrowth block is drawn up front (as
-    `solve`'s default); a disk whose 2r probes would not fit (2r >= N) is
+                    host_qr=True, overlap=True):
+    """Eigenvalues of a sequence of disks (as `solve` on each, beyn.jl:388-397)
+    through a pipeline:
+
+    * overlap=True: two disks in flight on the device. A creator thread builds
+      the next disk's handle (assembly and factorisation of its nodes, on the
+      handle's own streams) while the calling thread runs the current disk's
+      solves and moments, so the factorisation's panel chains and the solves'
+      GEMMs and residuals of two disks share the GPU; two handles' operators
+      are resident at once. overlap=False: one disk at a time on the device.
+    * each disk's host part (the QR reduction of the moments with host_qr, the
+      SVDs of R, B and eig(B)) on a worker thread, and the next disk's probe
+      block drawn on another.
+
+    The library, LAPACKE and NumPy's normal fills release the interpreter
+    lock, so all of these run at once. The regrowth block is drawn up front
+    (as `solve`'s default); a disk whose 2r probes would not fit (2r >= N) is
     finished the same way without regrowth, as construct_B_matrix does.
 
     host_qr: the moments come back whole and their QR reduction (A0 = Q R,
@@ -633,36 +643,63 @@ def solve_pipelined(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rngs=None, 
         V = probe_matrix(N, r, g)
         return np.asfortranarray(np.hstack([V, probe_matrix(N, r, g)])) if ahead else V
 
+    def create(d):
+        t = clk()
+        bh = BeynHandle(ws, complex(k0s[d]), float(Rs[d]), nq, mixed, max_refine, refine_tol, nb=nb,
+                        use_chebyshev=use_chebyshev, cheb=cheb)
+        return bh, (clk() - t) * 1e3
+
     futs, stats, dev_ms, split = [], [], [], []
-    # two workers: the next disk's probes and the previous disk's host part
-    with ThreadPoolExecutor(max_workers=2) as pool:
-        nxt = pool.submit(probes, rngs[0]) if k0s else None
-        for d, (k0, Rd) in enumerate(zip(k0s, Rs)):
-            t = clk()
-            V = nxt.result()
-            if d + 1 < len(k0s):
-                nxt = pool.submit(probes, rngs[d + 1])
-            t1 = clk()
-            bh = BeynHandle(ws, complex(k0), float(Rd), nq, mixed, max_refine, refine_tol, nb=nb,
-                            use_chebyshev=use_chebyshev, cheb=cheb)
-            t2 = clk()
-            try:
-                M0f, M1f = bh.moments(V) if host_qr else bh.moments_qr(V)
-                stats.append(bh.last_stats)
-            finally:
-                t3 = clk()
-                bh.close()
-            t4 = clk()
-            dev_ms.append((t4 - t) * 1e3)
-            split.append(((t1 - t) * 1e3, (t2 - t1) * 1e3, (t3 - t2) * 1e3, (t4 - t3) * 1e3))
-            futs.append(pool.submit(_finish_host_qr if host_qr else _finish_ahead, M0f, M1f, r, N, svd_tol))
-        res = [f.result() for f in futs]
+    nd = len(k0s)
+    handles = []  # every handle made, closed on the way out whatever happens
+    # host workers: the next disk's probes and the previous disk's host part;
+    # the creator: the next disk's handle (overlap)
+    with ThreadPoolExecutor(max_workers=2) as pool, ThreadPoolExecutor(max_workers=1) as maker:
+        try:
+            nxt = pool.submit(probes, rngs[0]) if nd else None
+            hnext = maker.submit(create, 0) if (nd and overlap) else None
+            for d in range(nd):
+                t = clk()
+                V = nxt.result()
+                if d + 1 < nd:
+                    nxt = pool.submit(probes, rngs[d + 1])
+                t1 = clk()
+                if overlap:
+                    bh, c_ms = hnext.result()
+                    handles.append(bh)
+                    if d + 1 < nd:
+                        hnext = maker.submit(create, d + 1)
+                else:
+                    bh, c_ms = create(d)
+                    handles.append(bh)
+                t2 = clk()
+                try:
+                    M0f, M1f = bh.moments(V) if host_qr else bh.moments_qr(V)
+                    stats.append(bh.last_stats)
+                finally:
+                    t3 = clk()
+                    bh.close()
+                t4 = clk()
+                dev_ms.append((t4 - t) * 1e3)
+                split.append(((t1 - t) * 1e3, (t2 - t1) * 1e3, c_ms, (t3 - t2) * 1e3, (t4 - t3) * 1e3))
+                futs.append(pool.submit(_finish_host_qr if host_qr else _finish_ahead, M0f, M1f, r, N, svd_tol))
+            res = [f.result() for f in futs]
+        finally:
+            if overlap and hnext is not None and nd:
+                try:
+                    extra, _ = hnext.result()
+                    if extra not in handles:
+                        extra.close()
+                except Exception:
+                    pass
+            for h in handles:
+                h.close()
     out = [x[0] for x in res]
     if not return_info:
         return out
     info = dict(stats=stats, rk=[x[1] for x in res], r=[x[2] for x in res], host_ms=[x[3] for x in res],
                 device_call_ms=dev_ms,
-                call_split_ms=dict(zip(("probe_wait", "create", "moments", "close"),
+                call_split_ms=dict(zip(("probe_wait", "handle_wait", "create", "moments", "close"),
                                        [float(np.mean(c)) for c in zip(*split)])) if split else {})
     return out, info
 

@@ -1,6 +1,8 @@
-"""GPU: solve_pipelined (a sequence of disks, each disk's host QR of the
-moments, SVDs and eig(B) on a worker thread while the device runs the next
-disk) against `solve` with the same probe generator, disk by disk: three disks
+"""GPU: solve_pipelined (a sequence of disks; the next disk's handle built on
+a second thread while the current disk solves, each disk's host QR of the
+moments, SVDs and eig(B) on a worker thread) against `solve` with the same
+probe generator, disk by disk, and against itself with one disk in flight
+(overlap=False, identical to 1e-12): three disks
 of the CFIE star (one whose rank saturates and regrows, one that does not),
 mixed and FP64 forms, and r >= N/2 (no regrowth block).
 
@@ -48,7 +50,10 @@ def test_pipelined_matches_solve(qb, mixed):
     rngs = lambda: [np.random.default_rng(10 + d) for d in range(3)]
     lams_d, info_d = qb.solve_pipelined(sol, pts, k0s, 0.4, rngs=rngs(), return_info=True, host_qr=False, **kw)
     lams_h = qb.solve_pipelined(sol, pts, k0s, 0.4, rngs=rngs(), **kw)
+    lams_1 = qb.solve_pipelined(sol, pts, k0s, 0.4, rngs=rngs(), host_qr=False, overlap=False, **kw)
     assert len(lams_d) == 3 and len(info_d["rk"]) == 3
+    for a, b in zip(lams_1, lams_d):  # one disk or two in flight: the same computation
+        _same(a, b)
     inside = 0
     for d, k0 in enumerate(k0s):
         ref, rinfo = qb.solve(sol, pts, k0, 0.4, rng=np.random.default_rng(10 + d), return_info=True, **kw)
