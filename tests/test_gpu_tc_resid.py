@@ -41,7 +41,7 @@ def _exact(Th, Tl, X, V):
 
 
 @pytest.mark.parametrize("n,L,b,row_scale,zero_col", [(200, 40, 2, False, False), (257, 64, 1, True, True),
-                                                       (512, 96, 1, False, False)])
+                                                       (512, 96, 1, False, False), (150, 20, 2, False, False)])
 def test_residual_engines_vs_exact(qb, n, L, b, row_scale, zero_col):
     rng = np.random.default_rng(n + L)
     Th, Tl, X, V = _case(rng, b, n, L, row_scale, zero_col)
