@@ -400,10 +400,14 @@ def main():
             e2e_times.append(dt)
             e2e_counts.append(int(np.count_nonzero(accuracy(lam_e, oracle_all)[1] <= TOL_EIG)))
     # the same disks one synchronous solve() after another, for comparison
-    serial_times = []
+    # device phases of a disk with the GPU to itself (the pipelined disks share it): the roofline's
+    # factor time and phases_ms come from these serial steps
+    serial_times, serial_stats = [], []
     if not args.serial:
         for _ in range(max(1, min(args.steps, 3))):
-            serial_times.append(run_step(qb, sol, pts, ws, mixed=True, cheb=cheb, nb=nb)[2])
+            _, sinfo, sdt = run_step(qb, sol, pts, ws, mixed=True, cheb=cheb, nb=nb)
+            serial_times.append(sdt)
+            serial_stats.append(sinfo["stats"])
     # FP32 form (FP32 kernel values): reported beside, with its own accuracy
     run_step(qb, sol, pts, ws, mixed="fp32", cheb=cheb)
     lam32, info32, t32 = run_step(qb, sol, pts, ws, mixed="fp32", cheb=cheb)
@@ -420,16 +424,17 @@ def main():
     h2d = 8 * 8 * N + 16 * N * (L_PROBES + (r_final if r_final != L_PROBES else 0))
     d2h = 2 * 16 * N * (L_PROBES + (r_final if r_final != L_PROBES else 0))
     hbm, bf16, peak_kind = _peaks()
-    st_last = stats[-1]
-    ms_factor = float(np.mean([s[0]["ms_factor"] for s in stats]))
-    ms_assemble = float(np.mean([s[0]["ms_assemble"] for s in stats]))
+    pstats = serial_stats if serial_stats else stats  # phases of a disk alone on the device
+    st_last = pstats[-1]
+    ms_factor = float(np.mean([s[0]["ms_factor"] for s in pstats]))
+    ms_assemble = float(np.mean([s[0]["ms_assemble"] for s in pstats]))
     # dominant work of the step: the FP32 LU of the 48 operators (panels on CUDA cores,
     # trailing updates on tcgen05 with 3xTF32), timed by CUDA events around the factor phase
     lu_flops = NQ * (8.0 / 3.0) * N ** 3
     lu_achieved = lu_flops / (ms_factor * 1e-3) / 1e12
     # tensor-core residual: HBM-bound (digit planes of T and X, V, R per launch)
-    res_ms = sum(s["ms_residual"] for run in stats for s in run)
-    res_n = sum(s["n_residual"] for run in stats for s in run)
+    res_ms = sum(s["ms_residual"] for run in pstats for s in run)
+    res_n = sum(s["n_residual"] for run in pstats for s in run)
     res_launch_ms = res_ms / max(res_n, 1)
     lp = ((L_PROBES + 31) // 32) * 32
     res_alg_bytes = (7 * N * 2 * N * 2 + 7 * 2 * lp * 2 * N * 2 + 2 * 16 * N * L_PROBES) * NQ
@@ -471,6 +476,10 @@ def main():
                        "max_rel_err_vs_oracle": float(e64.max()) if len(e64) else None,
                        "oracle_eigenvalues_missed": miss64},
         "speedup_vs_plain": (n_eig / t_step) / (plain_ok / t_plain) if plain_ok else None,
+        "phases_ms_pipelined": ({"assemble": float(np.mean([s[0]["ms_assemble"] for s in stats])),
+                                 "factor": float(np.mean([s[0]["ms_factor"] for s in stats])),
+                                 "solve_refine": float(np.mean([sum(x["ms_solve"] for x in s) for s in stats]))}
+                                if serial_stats else None),
         "phases_ms": {"assemble": ms_assemble, "factor": ms_factor,
                       "solve_refine": sum(s["ms_solve"] for s in st_last)},
         "host_ms": {k: float("%.3g" % v) for k, v in info["host_ms"].items()},
@@ -492,7 +501,7 @@ def main():
             "assembly": {"bound": "fp32 alu / hbm", "ms": ms_assemble, "bytes_written": asm_bytes,
                          "achieved_gbs": asm_bytes / (ms_assemble * 1e-3) / 1e9, "peak_gbs": hbm,
                          "frac_hbm": asm_bytes / (ms_assemble * 1e-3) / 1e9 / hbm},
-            "k_resid_tc": {"bound": "hbm", "launch_ms": res_launch_ms, "launches_per_step": res_n / max(len(stats), 1),
+            "k_resid_tc": {"bound": "hbm", "launch_ms": res_launch_ms, "launches_per_step": res_n / max(len(pstats), 1),
                            "algorithmic_bytes": res_alg_bytes,
                            "achieved_gbs": res_alg_bytes / (res_launch_ms * 1e-3) / 1e9 if res_n else None,
                            "peak_gbs": hbm,
