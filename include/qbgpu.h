@@ -448,6 +448,17 @@ qbg_status qbg_cgemm_c64(int32_t engine, int32_t M, int32_t N, int32_t K, const 
                          int64_t lda, const float* B, int64_t ldb, const float* beta, float* C, int64_t ldc,
                          int32_t batch);
 
+/* Complex128 product on the tensor cores, for validation: C_b -= A_b B_b for
+ * b < batch (host buffers, column-major complex128: A lda x K, B ldb x N, C
+ * ldc x N per b; the M x K, K x N and M x N leading blocks are used). Both
+ * operands are cut into eight 7-bit digits against the row maxima of A and the
+ * column maxima of B; the digit products are exact on the tensor cores and
+ * summed in double-float (~2^-56 of max|A_i.| max|B_.j| per term). The FP64 LU
+ * runs its blocked updates through the same routine. No reference
+ * counterpart: the reference's products run inside LAPACK (beyn.jl:270-280). */
+qbg_status qbg_zgemm_sub_tc(int32_t M, int32_t N, int32_t K, const double* A, int64_t lda, const double* B,
+                            int64_t ldb, double* C, int64_t ldc, int32_t batch);
+
 /* Refinement residual, for validation: R_b = V_b - (Th_b + Tl_b) X_b for b < batch
  * (host buffers, column-major; Th, Tl: n x n complex64 per b, Tl may be NULL;
  * X, V, R: n x L complex128 per b), rmax = max |re R| + |im R|. engine 0 =

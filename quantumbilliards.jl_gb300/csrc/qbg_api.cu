@@ -810,6 +810,34 @@ qbg_status qbg_launch_count(uint64_t* count) {
   return QBG_OK;
 }
 
+qbg_status qbg_zgemm_sub_tc(int32_t M, int32_t N, int32_t K, const double* A, int64_t lda, const double* B,
+                            int64_t ldb, double* C, int64_t ldc, int32_t batch) {
+  if (!A || !B || !C || M < 1 || N < 1 || K < 1 || batch < 1 || batch > 65535 || lda < M || ldb < K || ldc < M) {
+    set_error("qbg_zgemm_sub_tc: invalid arguments");
+    return QBG_EINVAL;
+  }
+  const size_t na = (size_t)lda * K, nbm = (size_t)ldb * N, nc = (size_t)ldc * N;
+  cxd *dA = nullptr, *dB = nullptr, *dC = nullptr;
+  int s = QBG_OK;
+  if ((s = dmalloc(&dA, sizeof(cxd) * na * batch))) return s;
+  if ((s = dmalloc(&dB, sizeof(cxd) * nbm * batch))) { dfree(dA); return s; }
+  if ((s = dmalloc(&dC, sizeof(cxd) * nc * batch))) { dfree(dA); dfree(dB); return s; }
+  cudaError_t e = cudaMemcpy(dA, A, sizeof(cxd) * na * batch, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dB, B, sizeof(cxd) * nbm * batch, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dC, C, sizeof(cxd) * nc * batch, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) s = cuda_status(e, "qbg_zgemm_sub_tc staging");
+  if (!s) s = tc_gemm_sub_f64(M, N, K, dA, lda, (long long)na, dB, ldb, (long long)nbm, dC, ldc, (long long)nc, batch, 0);
+  if (!s) s = tc_check(0);
+  if (!s) {
+    e = cudaMemcpy(C, dC, sizeof(cxd) * nc * batch, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) s = cuda_status(e, "qbg_zgemm_sub_tc D2H");
+  }
+  dfree(dA);
+  dfree(dB);
+  dfree(dC);
+  return s;
+}
+
 qbg_status qbg_residual_c64(int32_t engine, int32_t n, int32_t L, int32_t batch, const float* Th, const float* Tl,
                             const double* X, const double* V, double* R, double* rmax) {
   if (!Th || !X || !V || !R || !rmax || n < 1 || L < 1 || batch < 1 || batch > 65535 || engine < 0 || engine > 2) {

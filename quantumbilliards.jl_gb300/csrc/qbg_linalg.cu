@@ -982,6 +982,25 @@ void get_lu_plan(int* outer, int* cluster, int* parts) {
   if (parts) *parts = g_lu_parts.load();
 }
 
+// complex128 blocked updates C -= A B on the tensor cores (eight-digit
+// products, tc_gemm_sub_f64) where the product fills the device; QBG_F64_TC=0
+// keeps every FP64 product on the FP64 CUDA-core kernels
+static std::atomic<int> g_f64_tc{[] {
+  const char* e = std::getenv("QBG_F64_TC");
+  return (e && *e) ? (std::atoi(e) != 0 ? 1 : 0) : 1;
+}()};
+
+template <class T>
+static int gemm_sub(int M, int N, int K, const cx<T>* A, long long lda, long long sA, const cx<T>* B, long long ldb,
+                    long long sB, cx<T>* C, long long ldc, long long sC, int batch, cudaStream_t st) {
+  if constexpr (sizeof(T) == 8) {
+    if (g_f64_tc.load() && M >= 256 && N >= 64 && K >= 16 && batch <= 65535)
+      return tc_gemm_sub_f64(M, N, K, reinterpret_cast<const cxd*>(A), lda, sA, reinterpret_cast<const cxd*>(B), ldb,
+                             sB, reinterpret_cast<cxd*>(C), ldc, sC, batch, st);
+  }
+  return gemm_batched<T>(M, N, K, cx<T>(-1, 0), A, lda, sA, B, ldb, sB, cx<T>(1, 0), C, ldc, sC, batch, st);
+}
+
 template <class T>
 static int lu_factor_one(LUBatch<T>& f, cudaStream_t st, cudaEvent_t after_first_panel = nullptr) {
   const int n = f.n, nb = f.nb, batch = f.batch;
@@ -1089,9 +1108,9 @@ static int lu_factor_one(LUBatch<T>& f, cudaStream_t st, cudaEvent_t after_first
         int s = gemm_batched<T>(w, rin, w, one, linv(j0), nb, sLinv, f.A + j0 + (long long)(j0 + w) * n, n,
                                 f.stride, zero, f.A + j0 + (long long)(j0 + w) * n, n, f.stride, batch, st);
         if (s) return s;
-        s = gemm_batched<T>(n - j0 - w, rin, w, mone, f.A + (j0 + w) + (long long)j0 * n, n, f.stride,
-                            f.A + j0 + (long long)(j0 + w) * n, n, f.stride, one,
-                            f.A + (j0 + w) + (long long)(j0 + w) * n, n, f.stride, batch, st);
+        s = gemm_sub<T>(n - j0 - w, rin, w, f.A + (j0 + w) + (long long)j0 * n, n, f.stride,
+                        f.A + j0 + (long long)(j0 + w) * n, n, f.stride, f.A + (j0 + w) + (long long)(j0 + w) * n, n,
+                        f.stride, batch, st);
         if (s) return s;
       }
     }
@@ -1105,16 +1124,15 @@ static int lu_factor_one(LUBatch<T>& f, cudaStream_t st, cudaEvent_t after_first
         if (s) return s;
         const int below = E - j0 - w;
         if (below > 0) {
-          s = gemm_batched<T>(below, rest, w, mone, f.A + (j0 + w) + (long long)j0 * n, n, f.stride,
-                              f.A + j0 + (long long)E * n, n, f.stride, one, f.A + (j0 + w) + (long long)E * n, n,
-                              f.stride, batch, st);
+          s = gemm_sub<T>(below, rest, w, f.A + (j0 + w) + (long long)j0 * n, n, f.stride,
+                          f.A + j0 + (long long)E * n, n, f.stride, f.A + (j0 + w) + (long long)E * n, n, f.stride,
+                          batch, st);
           if (s) return s;
         }
       }
       // trailing update, K = E - J0
-      int s = gemm_batched<T>(rest, rest, E - J0, mone, f.A + E + (long long)J0 * n, n, f.stride,
-                              f.A + J0 + (long long)E * n, n, f.stride, one, f.A + E + (long long)E * n, n, f.stride,
-                              batch, st);
+      int s = gemm_sub<T>(rest, rest, E - J0, f.A + E + (long long)J0 * n, n, f.stride, f.A + J0 + (long long)E * n,
+                          n, f.stride, f.A + E + (long long)E * n, n, f.stride, batch, st);
       if (s) return s;
     }
   }
@@ -1233,8 +1251,8 @@ static int lu_trsolve(const LUBatch<T>& f, int L, cx<T>* X, cudaStream_t st) {
         int s = gemm_batched<T>(w, Lc, w, one, f.Linv2 + (long long)blk * bs * bs, bs, sI2, Xc + r0, n, sX, zero,
                                 Yc + r0, n, sY, batch, st);
         if (!s && rest > 0)
-          s = gemm_batched<T>(rest, Lc, w, mone, f.A + (r0 + w) + (long long)r0 * n, n, f.stride, Yc + r0, n, sY,
-                              one, Xc + r0 + w, n, sX, batch, st);
+          s = gemm_sub<T>(rest, Lc, w, f.A + (r0 + w) + (long long)r0 * n, n, f.stride, Yc + r0, n, sY,
+                          Xc + r0 + w, n, sX, batch, st);
         if (s) return s;
       }
       for (int blk = f.nblks - 1; blk >= 0; --blk) {
@@ -1242,8 +1260,7 @@ static int lu_trsolve(const LUBatch<T>& f, int L, cx<T>* X, cudaStream_t st) {
         int s = gemm_batched<T>(w, Lc, w, one, f.Uinv2 + (long long)blk * bs * bs, bs, sI2, Yc + r0, n, sY, zero,
                                 Xc + r0, n, sX, batch, st);
         if (!s && r0 > 0)
-          s = gemm_batched<T>(r0, Lc, w, mone, f.A + (long long)r0 * n, n, f.stride, Xc + r0, n, sX, one, Yc, n,
-                              sY, batch, st);
+          s = gemm_sub<T>(r0, Lc, w, f.A + (long long)r0 * n, n, f.stride, Xc + r0, n, sX, Yc, n, sY, batch, st);
         if (s) return s;
       }
     }
@@ -1257,8 +1274,8 @@ static int lu_trsolve(const LUBatch<T>& f, int L, cx<T>* X, cudaStream_t st) {
     if (s) return s;
     const int rest = n - r0 - w;
     if (rest > 0) {
-      s = gemm_batched<T>(rest, L, w, cx<T>(-1, 0), f.A + (r0 + w) + (long long)r0 * n, n, f.stride, X + r0, n,
-                          sX, cx<T>(1, 0), X + r0 + w, n, sX, batch, st);
+      s = gemm_sub<T>(rest, L, w, f.A + (r0 + w) + (long long)r0 * n, n, f.stride, X + r0, n, sX, X + r0 + w, n, sX,
+                      batch, st);
       if (s) return s;
     }
   }
@@ -1268,8 +1285,7 @@ static int lu_trsolve(const LUBatch<T>& f, int L, cx<T>* X, cudaStream_t st) {
                             cx<T>(0, 0), X + r0, n, sX, batch, st);
     if (s) return s;
     if (r0 > 0) {
-      s = gemm_batched<T>(r0, L, w, cx<T>(-1, 0), f.A + (long long)r0 * n, n, f.stride, X + r0, n, sX,
-                          cx<T>(1, 0), X, n, sX, batch, st);
+      s = gemm_sub<T>(r0, L, w, f.A + (long long)r0 * n, n, f.stride, X + r0, n, sX, X, n, sX, batch, st);
       if (s) return s;
     }
   }

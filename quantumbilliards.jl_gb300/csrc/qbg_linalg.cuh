@@ -140,6 +140,10 @@ size_t tc_resid_X_bytes(int n, int L, int batch);  // scratch per residual call 
 // (the leading six digits of T and X, ~2^-40: for a sweep that is not the last)
 int tc_residual(const TcResidT& t, const cxd* X, long long sX, const cxd* V, long long sV, cxd* R, long long sR,
                 int L, int c, double* rmax, void* xmem, cudaStream_t st, int ndig = 7);
+// C_b -= A_b B_b in complex128 from eight-digit products on the tensor cores
+// (qbg_tc_resid.cu); scratch from the pool, stream-ordered
+int tc_gemm_sub_f64(int M, int N, int K, const cxd* A, long long lda, long long sA, const cxd* B, long long ldb,
+                    long long sB, cxd* C, long long ldc, long long sC, int batch, cudaStream_t st);
 // device address of the tensor-core error flag (shared by the GEMM and the residual)
 int tc_error_ptr(int** p);
 

@@ -43,6 +43,7 @@
 #include <cstdint>
 #include <cuda_bf16.h>
 #include "qbg_common.cuh"
+#include "qbg_handles.cuh"
 #include "qbg_linalg.cuh"
 
 namespace qbg {
@@ -59,6 +60,14 @@ constexpr int RB_PLANE = 2 * RBN * RKS * 2;     // bytes of one X plane image (2
 constexpr int RA_TILE = RD * RA_PLANE;          // 28672
 constexpr int RB_TILE = RD * RB_PLANE;          // 14336
 constexpr int RSTAGE = RA_TILE + RB_TILE;       // 43008
+// stage layout for P digit planes per operand (P = RD for the refinement
+// residual, 8 for the FP64 products of tc_gemm_sub_f64)
+template <int P>
+struct RLay {
+  static constexpr int A_TILE = P * RA_PLANE;
+  static constexpr int B_TILE = P * RB_PLANE;
+  static constexpr int STAGE = A_TILE + B_TILE;
+};
 constexpr uint32_t RTMEM_COLS = 512;
 constexpr long long RSPIN = 1ll << 26;
 // D f32, A/B bf16, K-major, N = 64, M = 128
@@ -163,16 +172,19 @@ __device__ __forceinline__ long long fx_f64(double v, int Q) {
   return (u >> 63) ? -m : m;
 }
 
-// balanced base-128 digits of V (|V| <= 2^48 + 1): d[0] most significant, |d| <= 64
-__device__ __forceinline__ void digits7(long long V, float* d) {
+// P balanced base-128 digits of V (|V| <= 2^(7P - 1) + 1): d[0] most significant, |d| <= 64
+template <int P>
+__device__ __forceinline__ void digitsP(long long V, float* d) {
 #pragma unroll
-  for (int a = RD - 1; a > 0; --a) {
+  for (int a = P - 1; a > 0; --a) {
     const int q = (int)(((uint32_t)V + 64u) & 127u) - 64;
     d[a] = (float)q;
     V = (V - q) >> 7;
   }
   d[0] = (float)V;
 }
+
+__device__ __forceinline__ void digits7(long long V, float* d) { digitsP<RD>(V, d); }
 
 // row exponent e_i with max_k |T_ik| < 2^(e_i - 1) (re and im parts; T = hi + lo).
 // From FP32 maxima: |hi + lo| <= max|hi| + max|lo|, and that sum rounded to
@@ -276,10 +288,11 @@ __global__ void k_t_digits(const cxf* __restrict__ Th, const cxf* __restrict__ T
 }
 
 // column exponent f_l with max_k |X_kl| < 2^(f_l - 1); grid (L, batch)
-__global__ void k_x_colexp(const cxd* __restrict__ X, long long sX, int n, int L, int* __restrict__ fcol) {
+__global__ void k_x_colexp(const cxd* __restrict__ X, long long sX, long long ldx, int n, int L,
+                           int* __restrict__ fcol) {
   const int l = blockIdx.x;
   const long long b = blockIdx.y;
-  const cxd* x = X + b * sX + (long long)l * n;
+  const cxd* x = X + b * sX + (long long)l * ldx;
   double m = 0.0;
   int bad = 0;
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
@@ -311,30 +324,32 @@ __global__ void k_x_colexp(const cxd* __restrict__ X, long long sX, int n, int L
   }
 }
 
-// X digit planes as stage images: column l of tile nt = l / 32 gives B' rows
-// j = l % 32 (Re, -Im) and 32 + j (Im, Re) along k; columns l in [L, Lp) are
-// zero. grid (n/256, Lp, batch)
-__global__ void k_x_digits(const cxd* __restrict__ X, long long sX, int n, int L, int NT, int KS,
+// X digit planes (P per value, fixed point 2^(7P)) as stage images: column l
+// of tile nt = l / 32 gives B' rows j = l % 32 (Re, -Im) and 32 + j (Im, Re)
+// along k; columns l in [L, Lp) are zero. X: n rows (the k extent) per
+// column, leading dimension ldx. grid (n/256, Lp, batch)
+template <int P>
+__global__ void k_x_digits(const cxd* __restrict__ X, long long sX, long long ldx, int n, int L, int NT, int KS,
                            const int* __restrict__ fcol, unsigned char* __restrict__ XD) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int l = blockIdx.y;
   const long long b = blockIdx.z;
   if (k >= n) return;
-  float dr[RD], di[RD];
+  float dr[P], di[P];
   const int f = l < L ? fcol[b * L + l] : R_NONFINITE;
   if (f == R_NONFINITE) {  // padding column, or a column holding Inf / NaN
 #pragma unroll
-    for (int a = 0; a < RD; ++a) { dr[a] = 0.f; di[a] = 0.f; }
+    for (int a = 0; a < P; ++a) { dr[a] = 0.f; di[a] = 0.f; }
   } else {
-    const cxd v = X[b * sX + (long long)l * n + k];
-    digits7(fx_f64(v.re, 49 - f), dr);
-    digits7(fx_f64(v.im, 49 - f), di);
+    const cxd v = X[b * sX + (long long)l * ldx + k];
+    digitsP<P>(fx_f64(v.re, 7 * P - f), dr);
+    digitsP<P>(fx_f64(v.im, 7 * P - f), di);
   }
   const int j = l & (RBN - 1);
-  unsigned char* tile = XD + ((b * NT + (l / RBN)) * (long long)KS + (k >> 3)) * RB_TILE;
+  unsigned char* tile = XD + ((b * NT + (l / RBN)) * (long long)KS + (k >> 3)) * RLay<P>::B_TILE;
   const uint32_t o_re = img_off(j, (2 * k) & 15), o_im = img_off(RBN + j, (2 * k) & 15);
 #pragma unroll
-  for (int a = 0; a < RD; ++a) {
+  for (int a = 0; a < P; ++a) {
     __nv_bfloat162 pr, pi;
     pr.x = __float2bfloat16_rn(dr[a]);
     pr.y = __float2bfloat16_rn(-di[a]);
@@ -345,19 +360,108 @@ __global__ void k_x_digits(const cxd* __restrict__ X, long long sX, int n, int L
   }
 }
 
+// A operand of tc_gemm_sub_f64 (complex128, M x K, leading dimension lda):
+// row exponents e_i with max_k |A_ik| < 2^(e_i - 1); block (32, 8), grid
+// (ceil(M / 32), batch)
+__global__ void k_a_rowexp_f64(const cxd* __restrict__ A, long long sA, long long lda, int M, int K,
+                               int* __restrict__ erow) {
+  __shared__ double red[8][33];
+  __shared__ int redb[8][33];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i = blockIdx.x * 32 + tx;
+  const long long b = blockIdx.y;
+  const cxd* a = A + b * sA;
+  double m = 0.0;
+  int bad = 0;
+  if (i < M)
+    for (int k = ty; k < K; k += 8) {
+      const cxd v = a[(long long)i + (long long)k * lda];
+      const double x = fmax(fabs(v.re), fabs(v.im));
+      bad |= !(x <= 1.79769313486231570815e308);
+      m = fmax(m, x);
+    }
+  red[ty][tx] = m;
+  redb[ty][tx] = bad;
+  __syncthreads();
+  if (ty == 0 && i < M) {
+#pragma unroll
+    for (int r = 1; r < 8; ++r) {
+      m = fmax(m, red[r][tx]);
+      bad |= redb[r][tx];
+    }
+    int E = 0;
+    frexp(m, &E);
+    erow[b * M + i] = bad ? R_NONFINITE : (m > 0.0 ? E + 1 : 0);
+  }
+}
+
+// A digit planes (P per value) as stage images, as k_t_digits for a
+// complex128 M x K block; grid (ceil(M / 32), ceil(K / 32), batch), block
+// (32, 8): a 32 x 32 shared-memory transpose, then each warp writes 8 rows x
+// 4 complex k of one 16-byte core-matrix column per plane
+template <int P>
+__global__ void k_a_digits_f64(const cxd* __restrict__ A, long long sA, long long lda, int M, int K, int MT, int KS,
+                               const int* __restrict__ erow, unsigned char* __restrict__ TD) {
+  __shared__ cxd tv[32][33];  // [column][row]
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  const long long b = blockIdx.z;
+  const cxd* a = A + b * sA;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int c = ty + 8 * r, i = i0 + tx, k = k0 + c;
+    tv[c][tx] = (i < M && k < K) ? a[(long long)i + (long long)k * lda] : cxd(0.0, 0.0);
+  }
+  __syncthreads();
+  const int t = ty * 32 + tx;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int w = t + 256 * r;
+    const int e4 = w & 3, rr = (w >> 2) & 7, rg = (w >> 5) & 3, cs = w >> 7;  // cs: (stage, core column)
+    const int il = rg * 8 + rr, kloc = (cs >> 1) * 8 + (cs & 1) * 4 + e4;
+    const int i = i0 + il, k = k0 + kloc;
+    if (i >= M || k >= K) continue;
+    const cxd v = tv[kloc][il];
+    const int e = erow[b * M + i];
+    float dr[P], di[P];
+    if (e == R_NONFINITE) {
+#pragma unroll
+      for (int q = 0; q < P; ++q) { dr[q] = 0.f; di[q] = 0.f; }
+    } else {
+      digitsP<P>(fx_f64(v.re, 7 * P - e), dr);
+      digitsP<P>(fx_f64(v.im, 7 * P - e), di);
+    }
+    unsigned char* tile =
+        TD + ((b * MT + (i >> 7)) * (long long)KS + (k >> 3)) * RLay<P>::A_TILE + img_off(i & 127, (2 * k) & 15);
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+      __nv_bfloat162 pq;
+      pq.x = __float2bfloat16_rn(dr[q]);
+      pq.y = __float2bfloat16_rn(di[q]);
+      *reinterpret_cast<__nv_bfloat162*>(tile + q * RA_PLANE) = pq;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // R = V - T X from the digit planes; grid (Lp / 32, ceil(n / 128), batch)
 // ---------------------------------------------------------------------------
 // ND <= RD: the leading ND digits of T and X, pairs a + b <= ND + 1 (ND levels);
 // ND = RD is the full product, a smaller ND a residual to ~2^-(7 ND) of the
 // scales (for refinement sweeps whose correction is not the last)
-template <int ND>
+// P: digit planes per operand image (ND <= P); n: rows of T, V and R; ldv:
+// leading dimension of V and R (column l of row i at i + l ldv)
+template <int ND, int P>
 __global__ void __launch_bounds__(128, 1) k_resid_tc(const unsigned char* __restrict__ TD,
                                                      const int* __restrict__ erow,
                                                      const unsigned char* __restrict__ XD,
                                                      const int* __restrict__ fcol, int n, int L, int MT, int NT, int KS,
                                                      const cxd* __restrict__ V, long long sV, cxd* R, long long sR,
-                                                     unsigned long long* rmax, int* err) {
+                                                     long long ldv, unsigned long long* rmax, int* err) {
+  constexpr int RA_TILE = RLay<P>::A_TILE, RB_TILE = RLay<P>::B_TILE, RSTAGE = RLay<P>::STAGE;
+  // stages between exact flushes: a level of ND digits collects up to ND
+  // pairs, so 16 stages (256 real k) keep eight-digit level sums below 2^23
+  constexpr int RCHUNK = ND >= 8 ? 16 : 32;
   extern __shared__ __align__(1024) unsigned char r_smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(r_smem + RNST * RSTAGE);  // [RNST]
   uint64_t* empty = full + RNST;                                         // [RNST]
@@ -506,7 +610,7 @@ __global__ void __launch_bounds__(128, 1) k_resid_tc(const unsigned char* __rest
         const int col = n0 + c;
         if (col >= L) continue;  // full unroll keeps the sums in registers
         const int f = fcol[z * L + col];
-        const long long e = (long long)i + (long long)col * n;
+        const long long e = (long long)i + (long long)col * ldv;
         const cxd v = Vb[e];
         cxd r;
         if (ei == R_NONFINITE || f == R_NONFINITE) {
@@ -540,7 +644,8 @@ __global__ void __launch_bounds__(128, 1) k_resid_tc(const unsigned char* __rest
 static int ks_of(int n) { return (2 * n + RKS - 1) / RKS; }
 static int mt_of(int n) { return (n + RBM - 1) / RBM; }
 static int lp_of(int L) { return ((L + RBN - 1) / RBN) * RBN; }
-static size_t r_smem_bytes() { return (size_t)RNST * RSTAGE + 128; }
+template <int P = RD>
+static size_t r_smem_bytes() { return (size_t)RNST * RLay<P>::STAGE + 128; }
 
 size_t tc_resid_T_bytes(int n, int batch) {
   const size_t dig = (size_t)batch * mt_of(n) * ks_of(n) * RA_TILE;
@@ -595,24 +700,102 @@ int tc_residual(const TcResidT& t, const cxd* X, long long sX, const cxd* V, lon
   int dev = 0;
   QBG_CUDA(cudaGetDevice(&dev));
   if (dev >= 0 && dev < 64 && !attr[dev]) {
-    QBG_CUDA(cudaFuncSetAttribute(k_resid_tc<RD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r_smem_bytes()));
-    QBG_CUDA(cudaFuncSetAttribute(k_resid_tc<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r_smem_bytes()));
+    QBG_CUDA(cudaFuncSetAttribute(k_resid_tc<RD, RD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)r_smem_bytes()));
+    QBG_CUDA(cudaFuncSetAttribute(k_resid_tc<6, RD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)r_smem_bytes()));
     attr[dev] = true;
   }
-  k_x_colexp<<<dim3(L, c), 256, 0, st>>>(X, sX, n, L, fcol);
+  k_x_colexp<<<dim3(L, c), 256, 0, st>>>(X, sX, n, n, L, fcol);
   QBG_LAUNCH_CHECK("k_x_colexp");
-  k_x_digits<<<dim3((n + 255) / 256, Lp, c), 256, 0, st>>>(X, sX, n, L, NT, t.KS, fcol, XD);
+  k_x_digits<RD><<<dim3((n + 255) / 256, Lp, c), 256, 0, st>>>(X, sX, n, n, L, NT, t.KS, fcol, XD);
   QBG_LAUNCH_CHECK("k_x_digits");
   if (ndig == 6)
-    k_resid_tc<6><<<dim3(NT, t.MT, c), 128, r_smem_bytes(), st>>>(
-        static_cast<const unsigned char*>(t.TD), t.erow, XD, fcol, n, L, t.MT, NT, t.KS, V, sV, R, sR,
+    k_resid_tc<6, RD><<<dim3(NT, t.MT, c), 128, r_smem_bytes(), st>>>(
+        static_cast<const unsigned char*>(t.TD), t.erow, XD, fcol, n, L, t.MT, NT, t.KS, V, sV, R, sR, n,
         reinterpret_cast<unsigned long long*>(rmax), derr);
   else
-    k_resid_tc<RD><<<dim3(NT, t.MT, c), 128, r_smem_bytes(), st>>>(
-        static_cast<const unsigned char*>(t.TD), t.erow, XD, fcol, n, L, t.MT, NT, t.KS, V, sV, R, sR,
+    k_resid_tc<RD, RD><<<dim3(NT, t.MT, c), 128, r_smem_bytes(), st>>>(
+        static_cast<const unsigned char*>(t.TD), t.erow, XD, fcol, n, L, t.MT, NT, t.KS, V, sV, R, sR, n,
         reinterpret_cast<unsigned long long*>(rmax), derr);
   QBG_LAUNCH_CHECK("k_resid_tc");
   return QBG_OK;
+}
+
+// C_b -= A_b B_b (complex128; A: M x K, B: K x N, C: M x N, column-major with
+// leading dimensions lda, ldb, ldc and batch strides sA, sB, sC). Both
+// operands are cut into eight balanced 7-bit digits against the row maxima of
+// A and the column maxima of B (56-bit fixed point), the 36 digit pairs with
+// a + b <= 9 are multiplied exactly on the tensor cores into 8 TMEM level
+// sums (exact FP32 integers over 256 real k), the levels are added in
+// double-float and subtracted from C in FP64: per product term the error is
+// ~2^-56 of max_k |A_ik| max_k |B_kj|, the order of an FP64 GEMM's rounding.
+int tc_gemm_sub_f64(int M, int N, int K, const cxd* A, long long lda, long long sA, const cxd* B, long long ldb,
+                    long long sB, cxd* C, long long ldc, long long sC, int batch, cudaStream_t st) {
+  constexpr int P = 8;
+  if (M < 1 || N < 1 || K < 1 || batch < 1 || batch > 65535 || lda < M || ldb < K || ldc < M) {
+    set_error("tc_gemm_sub_f64: bad sizes");
+    return QBG_EINVAL;
+  }
+  const int MT = (M + RBM - 1) / RBM, KS = (2 * K + RKS - 1) / RKS, Lp = lp_of(N), NT = Lp / RBN;
+  const size_t td = (size_t)batch * MT * KS * RLay<P>::A_TILE;
+  const size_t xd = (size_t)batch * NT * KS * RLay<P>::B_TILE;
+  const size_t td_r = (td + 255) & ~(size_t)255, xd_r = (xd + 255) & ~(size_t)255;
+  const size_t er = (((size_t)batch * M * sizeof(int)) + 255) & ~(size_t)255;
+  const size_t bytes = td_r + xd_r + er + (size_t)batch * N * sizeof(int);
+  int* derr = nullptr;
+  QBG_TRY(tc_error_ptr(&derr));
+  static bool attr[64] = {};
+  int dev = 0;
+  QBG_CUDA(cudaGetDevice(&dev));
+  if (dev >= 0 && dev < 64 && !attr[dev]) {
+    QBG_CUDA(cudaFuncSetAttribute(k_resid_tc<P, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)r_smem_bytes<P>()));
+    attr[dev] = true;
+  }
+  unsigned char* mem = nullptr;
+  QBG_TRY(dmalloc(&mem, bytes));
+  unsigned char* TDm = mem;
+  unsigned char* XDm = mem + td_r;
+  int* erow = reinterpret_cast<int*>(mem + td_r + xd_r);
+  int* fcol = reinterpret_cast<int*>(mem + td_r + xd_r + er);
+  int s = QBG_OK;
+  // images of rows past M, k past K or columns past N stay zero
+  if (M % RBM || K % 8) {
+    cudaError_t e = cudaMemsetAsync(TDm, 0, td, st);
+    if (e != cudaSuccess) s = cuda_status(e, "tc_gemm_sub_f64 memset");
+  }
+  if (!s && (K % 8 || N % RBN)) {
+    cudaError_t e = cudaMemsetAsync(XDm, 0, xd, st);
+    if (e != cudaSuccess) s = cuda_status(e, "tc_gemm_sub_f64 memset");
+  }
+  auto launched = [&](const char* what) {
+    note_launch();
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) s = cuda_status(e, what);
+    return s == QBG_OK;
+  };
+  if (!s) {
+    k_a_rowexp_f64<<<dim3((M + 31) / 32, batch), dim3(32, 8), 0, st>>>(A, sA, lda, M, K, erow);
+    if (launched("k_a_rowexp_f64")) {
+      k_a_digits_f64<P><<<dim3((M + 31) / 32, (K + 31) / 32, batch), dim3(32, 8), 0, st>>>(A, sA, lda, M, K, MT, KS,
+                                                                                         erow, TDm);
+      launched("k_a_digits_f64");
+    }
+  }
+  if (!s) {
+    k_x_colexp<<<dim3(N, batch), 256, 0, st>>>(B, sB, ldb, K, N, fcol);
+    if (launched("k_x_colexp"))
+      k_x_digits<P><<<dim3((K + 255) / 256, Lp, batch), 256, 0, st>>>(B, sB, ldb, K, N, NT, KS, fcol, XDm);
+    launched("k_x_digits");
+  }
+  if (!s) {
+    k_resid_tc<P, P><<<dim3(NT, MT, batch), 128, r_smem_bytes<P>(), st>>>(TDm, erow, XDm, fcol, M, N, MT, NT, KS,
+                                                                           C, sC, C, sC, ldc, nullptr, derr);
+    launched("k_resid_tc");
+  }
+  dfree(mem, st);
+  return s;
 }
 
 }  // namespace qbg

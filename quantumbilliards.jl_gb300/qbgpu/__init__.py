@@ -14,7 +14,7 @@ from . import operators
 from .operators import (Workspace, build_workspace, assemble, assemble_noalloc, construct_matrices,
                         construct_boundary_matrices,
                         construct_boundary_matrices_with_derivatives, bessel01, sigma_min, cgemm,
-                        set_gemm_engine, launch_count, chebyshev_params, residual_c64,
+                        set_gemm_engine, launch_count, chebyshev_params, residual_c64, zgemm_sub_tc,
                         release_cached_memory, pool_stats, adjoint_fredholm_matrix, solve_vect_dlp,
                         chebyshev_params_min_cost)
 from .beyn import BeynHandle, construct_B_matrix, solve_vect, solve, solve_disks, solve_pipelined, probe_matrix, contour

@@ -142,6 +142,8 @@ _SIGS = {
                                   C.c_int64, C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.c_void_p, C.c_int64,
                                   C.c_int32]),
     "qbg_set_gemm_engine": (C.c_int32, [C.c_int32]),
+    "qbg_zgemm_sub_tc": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p,
+                                     C.c_int64, C.c_void_p, C.c_int64, C.c_int32]),
     "qbg_residual_c64": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
     "qbg_serve_create": (C.c_int32, [C.POINTER(ServeOpts), C.POINTER(C.c_void_p)]),

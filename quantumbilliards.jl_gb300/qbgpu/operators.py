@@ -284,6 +284,24 @@ def cgemm(A, B, C=None, alpha=1.0, beta=0.0, engine: int = 1) -> np.ndarray:
     return out[0] if single else out
 
 
+def zgemm_sub_tc(A, B, C):
+    """C - A B in complex128 through the library's eight-digit tensor-core
+    product (qbg_zgemm_sub_tc, validation helper). A: (batch, M, K) or (M, K),
+    B: (batch, K, N), C: (batch, M, N). Returns the new C."""
+    A3, B3, C3 = (np.asarray(x, dtype=np.complex128) for x in (A, B, C))
+    single = A3.ndim == 2
+    if single:
+        A3, B3, C3 = A3[None], B3[None], C3[None]
+    bsz, M, K = A3.shape
+    N = B3.shape[2]
+    a = np.ascontiguousarray(A3.transpose(0, 2, 1))  # column-major per matrix
+    b = np.ascontiguousarray(B3.transpose(0, 2, 1))
+    c = np.ascontiguousarray(C3.transpose(0, 2, 1))
+    L.check(L.load().qbg_zgemm_sub_tc(M, N, K, L.vptr(a), M, L.vptr(b), K, L.vptr(c), M, bsz))
+    out = c.transpose(0, 2, 1)
+    return out[0] if single else out
+
+
 def residual_c64(Th, Tl, X, V, engine: int = 0):
     """Device refinement residual R = V - (Th + Tl) X (validation helper).
     Th, Tl: (batch, n, n) complex64 (Tl may be None); X, V: (batch, n, L)
