@@ -622,7 +622,8 @@ def solve_pipelined(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rngs=None, 
 
     host_qr: the moments come back whole and their QR reduction (A0 = Q R,
     Q^H A1) runs on the worker too (LAPACK zgeqrf / zunmqr), off the device's
-    path; False reduces them on the device (moments_qr) as `solve` does.
+    path (the last disk's, which nothing follows, stay on the device); False
+    reduces them on the device (moments_qr) as `solve` does.
 
     rngs: one numpy Generator per disk (default: default_rng(d) for disk d);
     disk d draws its probes as `solve(..., rng=rngs[d])` would, so the
@@ -673,8 +674,11 @@ def solve_pipelined(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rngs=None, 
                     bh, c_ms = create(d)
                     handles.append(bh)
                 t2 = clk()
+                # the last disk has no successor to overlap its host QR with:
+                # its moments are reduced on the device
+                hq = host_qr and d + 1 < nd
                 try:
-                    M0f, M1f = bh.moments(V) if host_qr else bh.moments_qr(V)
+                    M0f, M1f = bh.moments(V) if hq else bh.moments_qr(V)
                     stats.append(bh.last_stats)
                 finally:
                     t3 = clk()
@@ -682,7 +686,7 @@ def solve_pipelined(solver, pts, k0s, R, nq=32, r=48, svd_tol=1e-14, rngs=None, 
                 t4 = clk()
                 dev_ms.append((t4 - t) * 1e3)
                 split.append(((t1 - t) * 1e3, (t2 - t1) * 1e3, c_ms, (t3 - t2) * 1e3, (t4 - t3) * 1e3))
-                futs.append(pool.submit(_finish_host_qr if host_qr else _finish_ahead, M0f, M1f, r, N, svd_tol))
+                futs.append(pool.submit(_finish_host_qr if hq else _finish_ahead, M0f, M1f, r, N, svd_tol))
             res = [f.result() for f in futs]
         finally:
             if overlap and hnext is not None and nd:
