@@ -15,6 +15,7 @@ import ctypes as C
 import glob
 import os
 import math
+import threading
 import time
 import warnings
 from dataclasses import dataclass, field
@@ -234,6 +235,22 @@ def _svd_lapacke(z, A, vals_only=False):
     return U, S, Vh
 
 
+# OpenBLAS's thread count is one process-wide setting: the calls that change
+# it for their own duration hold this lock, so that two host workers cannot
+# interleave their set and restore
+_BLAS_THREADS_LOCK = threading.RLock()
+
+
+def _with_threads(z, threads, fn):
+    with _BLAS_THREADS_LOCK:
+        n0 = int(z["get_threads"]())
+        z["set_threads"](C.c_int(max(1, threads)))
+        try:
+            return fn()
+        finally:
+            z["set_threads"](C.c_int(max(1, n0)))
+
+
 def _one_thread(fn):
     """fn(lapacke) with the BLAS at one thread, or fn(None) without LAPACKE.
     The moments' SVDs and eig(B) are dense problems of at most a few hundred
@@ -242,12 +259,7 @@ def _one_thread(fn):
     z = _lapacke()
     if z is None:
         return fn(None)
-    n0 = int(z["get_threads"]())
-    z["set_threads"](C.c_int(1))
-    try:
-        return fn(z)
-    finally:
-        z["set_threads"](C.c_int(max(1, n0)))
+    return _with_threads(z, 1, lambda: fn(z))
 
 
 def _svdvals(A):
@@ -276,18 +288,19 @@ def _per_disk_host(jobs, fn):
     """fn(job, lapacke) for every job: on host threads with the BLAS at one
     thread per call when LAPACKE is found (ctypes releases the interpreter
     lock, NumPy's svd and eigvals hold it), else one after another with
-    lapacke = None (NumPy). Same LAPACK routines either way."""
+    lapacke = None (NumPy). Same LAPACK routines either way. fn runs on pool
+    threads while this thread holds the BLAS-thread lock, so it calls the
+    LAPACKE wrappers directly (not _svd / _eigvals, which take the lock)."""
     z = _lapacke() if len(jobs) > 1 else None
     if z is None:
         return [fn(j, None) for j in jobs]
     from concurrent.futures import ThreadPoolExecutor
-    n0 = int(z["get_threads"]())
-    z["set_threads"](C.c_int(1))
-    try:
+
+    def run():
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 1)) as pool:
             return list(pool.map(lambda j: fn(j, z), jobs))
-    finally:
-        z["set_threads"](C.c_int(max(1, n0)))
+
+    return _with_threads(z, 1, run)
 
 
 def _eigvals_many(Bs):
@@ -551,14 +564,13 @@ def _qr_reduce_host(A0, A1, threads=4):
     n = a.shape[0]
     k = min(n, m)  # reflectors
     tau = np.empty(k, np.complex128)
-    n0 = int(z["get_threads"]())
-    z["set_threads"](C.c_int(max(1, threads)))
-    try:
+    def run():
         info = z["zgeqrf"](102, n, m, a.ctypes.data, n, tau.ctypes.data)
         if info == 0:
             info = z["zunmqr"](102, b"L", b"C", n, m, k, a.ctypes.data, n, tau.ctypes.data, c.ctypes.data, n)
-    finally:
-        z["set_threads"](C.c_int(max(1, n0)))
+        return info
+
+    info = _with_threads(z, threads, run)
     if info != 0:
         raise np.linalg.LinAlgError(f"zgeqrf / zunmqr info {info}")
     return np.asfortranarray(np.triu(a[:k, :m])), np.asfortranarray(c[:k, :m])
