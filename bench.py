@@ -457,9 +457,10 @@ def main():
         "config": dict(workload_config(), r_final=r_final, cheb_panels=list(cheb), cheb_tol=CHEB_TOL,
                        timing=("wall clock of the synchronous API calls between device synchronizations (the step "
                                "ends with the host SVD and eigvals)" if args.serial else
-                               "wall clock of one solve_pipelined call over `steps` disks (each disk's host SVD "
-                               "and eigvals overlap the device work of the next; the last disk's are inside the "
-                               "region)") + "; device phases in phases_ms are CUDA events"),
+                               "wall clock of one solve_pipelined call over `steps` disks (two disks in flight on "
+                               "the device; each disk's host QR, SVDs and eigvals beside the next disk's device "
+                               "work; the last disk's are inside the region)") +
+                              "; device phases in phases_ms are CUDA events of a disk alone on the device"),
         "serial_ms_per_step": (float(np.median(serial_times)) * 1e3 if serial_times else None),
         "plan_s": plan_s,
         "lu_plan": {"nb": nb, "outer": tuned["outer"], "parts": tuned["parts"], "cluster": tuned["cluster"],
@@ -492,8 +493,9 @@ def main():
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "tensor", "achieved": lu_achieved, "peak": bf16, "unit": "TFLOP/s",
                      "frac": lu_achieved / bf16, "traffic": None,
-                     "kernel": "LU factor phase of the 48 operators: k_getrf_panel_smem (FP32 panels, CUDA cores) + "
-                               "k_tc_cgemm / k_tc_cgemm_pk trailing updates (tcgen05, 3xTF32)",
+                     "kernel": "LU factor phase of the 48 operators, one disk alone on the device: "
+                               "k_getrf_panel_smem (FP32 panels, CUDA cores) + k_tc_cgemm_pkw trailing updates and "
+                               "k_tc_cgemm in-block products (tcgen05, 3xTF32)",
                      "peak_kind": peak_kind + " bf16 dense (the TF32 tensor rate is half of it and 3xTF32 issues three "
                                               "MMAs per product)",
                      "algorithmic_flops": lu_flops, "ms": ms_factor},
