@@ -325,8 +325,9 @@ def main():
     cheb = tuple(int(x) for x in qb.chebyshev_params_min_cost(sol, pts, zref, ws=ws, tol=CHEB_TOL)[:4])
     plan_s = time.perf_counter() - t0
     # LU plan of the mixed step (panel width, outer-block depth, stream parts) chosen by timing this workload
+    # on the path the region times: the pipelined driver (4 disks per trial), or serial solve() calls
     tuned = qb.autotune.tune_beyn(sol, pts, ws, K0 + 0j, RADIUS, NQ, L_PROBES, mixed=True, cheb=cheb,
-                                  svd_tol=SVD_TOL, seed=SEED)
+                                  svd_tol=SVD_TOL, seed=SEED, pipelined=0 if args.serial else 4)
     nb = tuned["nb"]
 
     # plain FP64 form (the drop-in), timed beside the mixed one

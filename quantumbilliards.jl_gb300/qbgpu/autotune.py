@@ -49,24 +49,33 @@ def set_lu_plan(outer=None, cluster=None, parts=None):
 
 
 def tune_beyn(solver, pts, ws, k0, R, nq, r, mixed=True, cheb=None, svd_tol=1e-12, seed=0, reps=2,
-              parts=(2, 4, 8), outers=(2, 4, 8), nbs=(64, 32), clusters=(1,)):
+              parts=(2, 4, 8), outers=(2, 4, 8), nbs=(64, 32), clusters=(1,), pipelined=0):
     """Times Beyn steps of this workload under candidate plans and keeps the
-    fastest. Returns dict(nb, outer, parts, cluster, ms, table, tune_s):
-    ``table`` lists every plan tried with its median step time in ms."""
-    from .beyn import solve
+    fastest. pipelined > 0 times each plan on `solve_pipelined` over that many
+    disks (the per-disk time with two disks in flight) instead of one `solve`
+    call. Returns dict(nb, outer, parts, cluster, ms, table, tune_s): ``table``
+    lists every plan tried with its median time per disk in ms."""
+    from .beyn import solve, solve_pipelined
 
     t_start = time.perf_counter()
     table = []
 
+    def one(kw):
+        if pipelined > 0:
+            rngs = [np.random.default_rng(seed) for _ in range(pipelined)]
+            solve_pipelined(solver, pts, [k0] * pipelined, R, rngs=rngs, **kw)
+        else:
+            solve(solver, pts, k0, R, rng=np.random.default_rng(seed), **kw)
+
     def run(nb, outer, npart, cluster=-1):
         set_lu_plan(outer=outer, cluster=cluster, parts=npart)
         kw = dict(nq=nq, r=r, svd_tol=svd_tol, mixed=mixed, ws=ws, cheb=cheb, nb=nb)
-        solve(solver, pts, k0, R, rng=np.random.default_rng(seed), **kw)  # warm: buffers of this plan
+        one(kw)  # warm: buffers of this plan
         ts = []
         for _ in range(max(1, reps)):
             t0 = time.perf_counter()
-            solve(solver, pts, k0, R, rng=np.random.default_rng(seed), **kw)
-            ts.append(time.perf_counter() - t0)
+            one(kw)
+            ts.append((time.perf_counter() - t0) / max(1, pipelined))
         ms = 1e3 * float(np.median(ts))
         table.append({"nb": nb, "outer": outer, "parts": npart, "cluster": cluster, "ms": ms})
         return ms
